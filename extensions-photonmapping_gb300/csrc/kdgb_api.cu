@@ -1,0 +1,498 @@
+// C ABI of the kd-tree builder and tracers (include/kdgb.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kdgb_internal.cuh"
+
+namespace kdgb {
+
+int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
+                 int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s);
+int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, int64_t n, const float *light,
+                  int32_t *occ, cudaStream_t s);
+int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, int32_t T, int tie, const float *o,
+                 const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv, cudaStream_t s);
+
+namespace {
+thread_local std::string g_last_error;
+std::once_flag g_pool_once;
+
+// Stream-ordered allocations come from the device's default pool; keeping
+// freed blocks cached makes per-level scratch allocations cheap.
+void setup_pool()
+{
+    std::call_once(g_pool_once, [] {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return;
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) return;
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    });
+}
+}  // namespace
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int fail(int status, const std::string &msg)
+{
+    g_last_error = msg;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();  // clear a non-sticky error
+    return e == cudaErrorMemoryAllocation ? KDGB_ERR_OUT_OF_MEMORY : KDGB_ERR_CUDA;
+}
+
+template <class T>
+int ensure(DevArray<T> &a, int64_t n, cudaStream_t s, int64_t keep, bool zero)
+{
+    if (n <= a.cap && a.p) return KDGB_OK;
+    const int64_t cap = n > 0 ? n : 1;
+    T *p = nullptr;
+    KDGB_CUDA(cudaMallocAsync(&p, sizeof(T) * (size_t)cap, s));
+    if (zero) {
+        cudaError_t e = cudaMemsetAsync(p, 0, sizeof(T) * (size_t)cap, s);
+        if (e != cudaSuccess) { cudaFreeAsync(p, s); return cuda_fail(e, "cudaMemsetAsync"); }
+    }
+    if (a.p && keep > 0) {
+        cudaError_t e = cudaMemcpyAsync(p, a.p, sizeof(T) * (size_t)keep, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) { cudaFreeAsync(p, s); return cuda_fail(e, "cudaMemcpyAsync"); }
+    }
+    if (a.p) cudaFreeAsync(a.p, s);
+    a.p = p;
+    a.cap = cap;
+    return KDGB_OK;
+}
+
+template <class T>
+void release(DevArray<T> &a, cudaStream_t s)
+{
+    if (a.p) cudaFreeAsync(a.p, s);
+    a.p = nullptr;
+    a.cap = 0;
+}
+
+template int ensure<int8_t>(DevArray<int8_t> &, int64_t, cudaStream_t, int64_t, bool);
+template int ensure<float>(DevArray<float> &, int64_t, cudaStream_t, int64_t, bool);
+template int ensure<float4>(DevArray<float4> &, int64_t, cudaStream_t, int64_t, bool);
+template int ensure<int32_t>(DevArray<int32_t> &, int64_t, cudaStream_t, int64_t, bool);
+template int ensure<int2>(DevArray<int2> &, int64_t, cudaStream_t, int64_t, bool);
+template int ensure<int4>(DevArray<int4> &, int64_t, cudaStream_t, int64_t, bool);
+
+static void release_all(Tree &t, cudaStream_t s)
+{
+    release(t.p0, s); release(t.p1, s); release(t.p2, s);
+    release(t.info, s); release(t.split, s); release(t.bmin, s); release(t.bmax, s);
+    release(t.pidx, s); release(t.bitmap, s); release(t.parent, s); release(t.children, s);
+    release(t.area, s); release(t.prim_indices, s); release(t.leaf_ids, s);
+    release(t.tnode, s); release(t.ttri, s);
+}
+
+static int check_device()
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(KDGB_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    setup_pool();
+    return KDGB_OK;
+}
+
+static int validate_build_params(const kdgb_build_params &p)
+{
+    if (p.mode != KDGB_BUILD_REFERENCE && p.mode != KDGB_BUILD_TUNED)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown build mode");
+    if (p.lower != KDGB_LOWER_BITMAP && p.lower != KDGB_LOWER_SAH)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown lower algorithm");
+    if (p.leaf_size < 1 || p.leaf_size > 32) return fail(KDGB_ERR_INVALID_ARGUMENT, "leaf_size must be in 1..32");
+    if (p.max_levels < 1 || p.max_levels > 4096) return fail(KDGB_ERR_INVALID_ARGUMENT, "max_levels out of range");
+    if (!std::isfinite(p.empty_space_threshold) || !std::isfinite(p.traversal_cost) ||
+        !std::isfinite(p.intersection_cost))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "non-finite cost parameter");
+    if (p.mode == KDGB_BUILD_TUNED && (p.upper_levels < 0 || p.sah_bins < 2 || p.sah_bins > 256))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "tuned build: upper_levels >= 0, sah_bins in 2..256");
+    return KDGB_OK;
+}
+
+static int validate_trace_params(const kdgb_trace_params &p, int64_t n)
+{
+    if (p.tracer < KDGB_TRACER_RESTART || p.tracer > KDGB_TRACER_BRUTE)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown tracer");
+    if (p.tie != KDGB_TIE_LOWEST_ID && p.tie != KDGB_TIE_REF_LAST) return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown tie rule");
+    if (p.stack_depth < 1 || p.stack_depth > 8) return fail(KDGB_ERR_INVALID_ARGUMENT, "stack_depth must be in 1..8");
+    if (p.block_size < 0 || p.block_size > 1024 || (p.block_size % 32) != 0)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "block_size must be 0 or a multiple of 32 up to 1024");
+    if (p.max_iterations < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "max_iterations must be >= 0");
+    if (p.tile_width < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "tile_width must be >= 0");
+    if (p.tile_width > 0 && (p.tile_width % 4 != 0 || n % ((int64_t)p.tile_width * 8) != 0))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "tile_width needs width % 4 == 0 and height % 8 == 0");
+    return KDGB_OK;
+}
+
+static int do_build(Tree &t, const float *tri_v_dev, int32_t n_tris, const kdgb_build_params &p, cudaStream_t s)
+{
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    KDGB_CUDA(cudaEventCreate(&e0));
+    KDGB_CUDA(cudaEventCreate(&e1));
+    cudaEventRecord(e0, s);
+    int rc = p.mode == KDGB_BUILD_TUNED ? build_tuned(t, tri_v_dev, n_tris, p, s)
+                                        : build_reference(t, tri_v_dev, n_tris, p, s);
+    if (rc == KDGB_OK) rc = pack_for_traversal(t, s);
+    cudaEventRecord(e1, s);
+    if (rc == KDGB_OK) {
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) rc = cuda_fail(e, "build");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        t.stats.build_ms = ms;
+        t.stats.n_nodes = t.n_nodes;
+        t.stats.n_refs = t.n_refs;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+}  // namespace kdgb
+
+using namespace kdgb;
+
+extern "C" {
+
+int kdgb_abi_version(void) { return KDGB_ABI_VERSION; }
+
+const char *kdgb_status_string(int status)
+{
+    switch (status) {
+    case KDGB_OK: return "ok";
+    case KDGB_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case KDGB_ERR_CUDA: return "CUDA error";
+    case KDGB_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case KDGB_ERR_CAPACITY: return "capacity exceeded";
+    case KDGB_ERR_DEGENERATE: return "degenerate input";
+    case KDGB_ERR_NONFINITE: return "non-finite input";
+    case KDGB_ERR_TIMEOUT: return "device wait timed out";
+    case KDGB_ERR_UNSUPPORTED: return "unsupported";
+    case KDGB_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+const char *kdgb_last_error(void) { return g_last_error.c_str(); }
+
+void kdgb_build_params_default(kdgb_build_params *p)
+{
+    if (!p) return;
+    p->mode = KDGB_BUILD_REFERENCE;
+    p->lower = KDGB_LOWER_BITMAP;
+    p->split_empty_space = 1;
+    p->propagate_aabbs = 1;
+    p->empty_space_threshold = 0.35f;
+    p->traversal_cost = 24.0f;
+    p->intersection_cost = 1.0f;
+    p->min_leaf = 0;
+    p->esc_zmax_as_x = 1;
+    p->max_levels = 64;
+    p->leaf_size = 32;
+    p->upper_levels = 8;
+    p->sah_bins = 32;
+}
+
+void kdgb_trace_params_default(kdgb_trace_params *p)
+{
+    if (!p) return;
+    p->tracer = KDGB_TRACER_RESTART;
+    p->leaf_skipping = 1;
+    p->tie = KDGB_TIE_LOWEST_ID;
+    p->stack_depth = 4;
+    p->max_iterations = 0;
+    p->block_size = 0;
+    p->tile_width = 0;
+}
+
+int kdgb_build(const float *tri_v_dev, int32_t n_tris, const kdgb_build_params *params, kdgb_tree **out,
+               kdgb_stream_t stream)
+{
+    if (!out) return fail(KDGB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (n_tris < 0 || (n_tris > 0 && !tri_v_dev)) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad triangle buffer");
+    KDGB_CHECK(check_device());
+    kdgb_build_params p;
+    if (params) p = *params; else kdgb_build_params_default(&p);
+    KDGB_CHECK(validate_build_params(p));
+    kdgb_tree *h = new (std::nothrow) kdgb_tree();
+    if (!h) return fail(KDGB_ERR_OUT_OF_MEMORY, "host allocation");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int rc = do_build(h->t, tri_v_dev, n_tris, p, s);
+    if (rc != KDGB_OK) {
+        release_all(h->t, s);
+        cudaStreamSynchronize(s);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return KDGB_OK;
+}
+
+int kdgb_rebuild(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris, const kdgb_build_params *params,
+                 kdgb_stream_t stream)
+{
+    if (!tree) return fail(KDGB_ERR_INVALID_ARGUMENT, "tree is NULL");
+    if (n_tris < 0 || (n_tris > 0 && !tri_v_dev)) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad triangle buffer");
+    KDGB_CHECK(check_device());
+    kdgb_build_params p;
+    if (params) p = *params; else kdgb_build_params_default(&p);
+    KDGB_CHECK(validate_build_params(p));
+    return do_build(tree->t, tri_v_dev, n_tris, p, (cudaStream_t)stream);
+}
+
+int kdgb_tree_upload(const kdgb_tree_view *a, const float *tri_v_host, int32_t n_tris, kdgb_tree **out,
+                     kdgb_stream_t stream)
+{
+    if (!out || !a) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    const int32_t n = a->n_nodes, r = a->n_refs, nl = a->n_upper_leaves;
+    if (n < 1 || r < 0 || nl < 0 || n_tris < 0 || (n_tris > 0 && !tri_v_host) || !a->info || !a->split ||
+        !a->aabb_min || !a->aabb_max || !a->prim_index || !a->bitmap || !a->children ||
+        (r > 0 && !a->prim_indices))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "incomplete tree arrays");
+    // Validate everything the tracers dereference so a malformed tree is an
+    // error here rather than an out-of-bounds access on the device.
+    for (int32_t i = 0; i < n; ++i) {
+        const int axis = a->info[i];
+        if (axis < 0 || axis > 3) return fail(KDGB_ERR_INVALID_ARGUMENT, "info out of range");
+        if (axis == KDGB_LEAF) {
+            const uint32_t bmp = (uint32_t)a->bitmap[i];
+            if (bmp) {
+                const int hi = 31 - __builtin_clz(bmp);
+                if (a->prim_index[i] < 0 || (int64_t)a->prim_index[i] + hi >= r)
+                    return fail(KDGB_ERR_INVALID_ARGUMENT, "leaf references out of range");
+            }
+        } else {
+            const int32_t c0 = a->children[2 * i], c1 = a->children[2 * i + 1];
+            if (c0 < 0 || c0 >= n || c1 < 0 || c1 >= n) return fail(KDGB_ERR_INVALID_ARGUMENT, "child out of range");
+        }
+    }
+    for (int32_t i = 0; i < r; ++i)
+        if (a->prim_indices[i] < 0 || a->prim_indices[i] >= n_tris)
+            return fail(KDGB_ERR_INVALID_ARGUMENT, "primitive index out of range");
+    KDGB_CHECK(check_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    kdgb_tree *h = new (std::nothrow) kdgb_tree();
+    if (!h) return fail(KDGB_ERR_OUT_OF_MEMORY, "host allocation");
+    Tree &t = h->t;
+    int rc = KDGB_OK;
+    float *dtri = nullptr;
+    std::vector<float> zeros;
+    do {
+        if ((rc = ensure(t.info, n, s)) || (rc = ensure(t.split, n, s)) || (rc = ensure(t.bmin, n, s)) ||
+            (rc = ensure(t.bmax, n, s)) || (rc = ensure(t.pidx, n, s)) || (rc = ensure(t.bitmap, n, s)) ||
+            (rc = ensure(t.children, n, s)) || (rc = ensure(t.area, n, s, 0, true)) ||
+            (rc = ensure(t.parent, n, s, 0, true)) || (rc = ensure(t.prim_indices, r, s)) ||
+            (rc = ensure(t.leaf_ids, nl, s)))
+            break;
+        cudaError_t e = cudaSuccess;
+        auto up = [&](void *dst, const void *src, size_t bytes) {
+            if (e == cudaSuccess && bytes && src) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+        };
+        up(t.info.p, a->info, (size_t)n);
+        up(t.split.p, a->split, 4 * (size_t)n);
+        up(t.bmin.p, a->aabb_min, 16 * (size_t)n);
+        up(t.bmax.p, a->aabb_max, 16 * (size_t)n);
+        up(t.pidx.p, a->prim_index, 4 * (size_t)n);
+        up(t.bitmap.p, a->bitmap, 4 * (size_t)n);
+        up(t.children.p, a->children, 8 * (size_t)n);
+        up(t.area.p, a->area, 4 * (size_t)n);
+        up(t.parent.p, a->parent, 4 * (size_t)n);
+        up(t.prim_indices.p, a->prim_indices, 4 * (size_t)r);
+        up(t.leaf_ids.p, a->leaf_ids, 4 * (size_t)nl);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "tree upload"); break; }
+        if (n_tris > 0) {
+            if ((e = cudaMallocAsync(&dtri, sizeof(float) * 9 * (size_t)n_tris, s)) != cudaSuccess ||
+                (e = cudaMemcpyAsync(dtri, tri_v_host, sizeof(float) * 9 * (size_t)n_tris, cudaMemcpyHostToDevice, s)) !=
+                    cudaSuccess) {
+                rc = cuda_fail(e, "triangle upload");
+                break;
+            }
+        }
+        if ((rc = load_geometry(t, dtri, n_tris, s))) break;
+        t.n_nodes = n;
+        t.n_refs = r;
+        t.n_upper_leaves = nl;
+        if ((rc = pack_for_traversal(t, s))) break;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) { rc = cuda_fail(e, "tree upload"); break; }
+    } while (0);
+    if (dtri) cudaFreeAsync(dtri, s);
+    if (rc != KDGB_OK) {
+        release_all(t, s);
+        cudaStreamSynchronize(s);
+        delete h;
+        return rc;
+    }
+    t.stats.n_nodes = n;
+    t.stats.n_refs = r;
+    *out = h;
+    return KDGB_OK;
+}
+
+int kdgb_tree_destroy(kdgb_tree *tree)
+{
+    if (!tree) return KDGB_OK;
+    release_all(tree->t, 0);
+    cudaError_t e = cudaStreamSynchronize(0);
+    delete tree;
+    if (e != cudaSuccess) return cuda_fail(e, "kdgb_tree_destroy");
+    return KDGB_OK;
+}
+
+int kdgb_tree_view_get(const kdgb_tree *tree, kdgb_tree_view *v)
+{
+    if (!tree || !v) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    const Tree &t = tree->t;
+    v->n_nodes = t.n_nodes;
+    v->n_refs = t.n_refs;
+    v->n_upper_leaves = t.n_upper_leaves;
+    v->n_tris = t.n_tris;
+    v->info = t.info.p;
+    v->split = t.split.p;
+    v->aabb_min = reinterpret_cast<float *>(t.bmin.p);
+    v->aabb_max = reinterpret_cast<float *>(t.bmax.p);
+    v->prim_index = t.pidx.p;
+    v->bitmap = t.bitmap.p;
+    v->children = reinterpret_cast<int32_t *>(t.children.p);
+    v->area = t.area.p;
+    v->parent = t.parent.p;
+    v->prim_indices = t.prim_indices.p;
+    v->leaf_ids = t.leaf_ids.p;
+    v->p0 = reinterpret_cast<float *>(t.p0.p);
+    v->p1 = reinterpret_cast<float *>(t.p1.p);
+    v->p2 = reinterpret_cast<float *>(t.p2.p);
+    return KDGB_OK;
+}
+
+int kdgb_tree_download(const kdgb_tree *tree, kdgb_tree_view *d)
+{
+    if (!tree || !d) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    const Tree &t = tree->t;
+    const size_t n = (size_t)t.n_nodes, r = (size_t)t.n_refs, nl = (size_t)t.n_upper_leaves;
+    cudaError_t e = cudaSuccess;
+    auto dn = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && dst && bytes) e = cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
+    };
+    KDGB_CUDA(cudaDeviceSynchronize());
+    dn(d->info, t.info.p, n);
+    dn(d->split, t.split.p, 4 * n);
+    dn(d->aabb_min, t.bmin.p, 16 * n);
+    dn(d->aabb_max, t.bmax.p, 16 * n);
+    dn(d->prim_index, t.pidx.p, 4 * n);
+    dn(d->bitmap, t.bitmap.p, 4 * n);
+    dn(d->children, t.children.p, 8 * n);
+    dn(d->area, t.area.p, 4 * n);
+    dn(d->parent, t.parent.p, 4 * n);
+    dn(d->prim_indices, t.prim_indices.p, 4 * r);
+    dn(d->leaf_ids, t.leaf_ids.p, 4 * nl);
+    dn(d->p0, t.p0.p, 16 * (size_t)t.n_tris);
+    dn(d->p1, t.p1.p, 16 * (size_t)t.n_tris);
+    dn(d->p2, t.p2.p, 16 * (size_t)t.n_tris);
+    if (e != cudaSuccess) return cuda_fail(e, "kdgb_tree_download");
+    return KDGB_OK;
+}
+
+int kdgb_tree_stats(const kdgb_tree *tree, kdgb_build_stats *stats)
+{
+    if (!tree || !stats) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    *stats = tree->t.stats;
+    return KDGB_OK;
+}
+
+int kdgb_trace(const kdgb_tree *tree, const kdgb_trace_params *params, const float *ray_o_dev,
+               const float *ray_d_dev, int32_t n, int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
+               kdgb_stream_t stream)
+{
+    if (!tree) return fail(KDGB_ERR_INVALID_ARGUMENT, "tree is NULL");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "negative ray count");
+    KDGB_CHECK(validate_trace_params(p, n));
+    if (n == 0) return KDGB_OK;
+    if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    const Tree &t = tree->t;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (p.tracer == KDGB_TRACER_BRUTE)
+        return brute_launch(t.p0.p, t.p1.p, t.p2.p, t.n_tris, p.tie, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev,
+                            v_dev, s);
+    return trace_launch(t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, nullptr, nullptr, s);
+}
+
+int kdgb_trace_shadow(const kdgb_tree *tree, const kdgb_trace_params *params, const float *points_dev, int32_t n,
+                      const float light[3], int32_t *occluded_dev, kdgb_stream_t stream)
+{
+    if (!tree || !light) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "negative point count");
+    p.tile_width = 0;
+    KDGB_CHECK(validate_trace_params(p, n));
+    if (n == 0) return KDGB_OK;
+    if (!points_dev || !occluded_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL buffer");
+    return shadow_launch(tree->t, p, points_dev, n, light, occluded_dev, (cudaStream_t)stream);
+}
+
+int kdgb_trace_primary_shadow(const kdgb_tree *tree, const kdgb_trace_params *params, const float *ray_o_dev,
+                              const float *ray_d_dev, int32_t n, const float light[3], int32_t *hit_dev,
+                              float *t_dev, float *u_dev, float *v_dev, int32_t *occluded_dev, kdgb_stream_t stream)
+{
+    if (!tree || !light) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "negative ray count");
+    KDGB_CHECK(validate_trace_params(p, n));
+    if (p.tracer == KDGB_TRACER_BRUTE) return fail(KDGB_ERR_UNSUPPORTED, "fused shadow rays need a kd tracer");
+    if (n == 0) return KDGB_OK;
+    if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev || !occluded_dev)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    return trace_launch(tree->t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, occluded_dev, light,
+                        (cudaStream_t)stream);
+}
+
+int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie, const float *ray_o_dev,
+                     const float *ray_d_dev, int32_t n, int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
+                     kdgb_stream_t stream)
+{
+    if (n_tris < 0 || n < 0 || (n_tris > 0 && !tri_v_dev)) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (tie != KDGB_TIE_LOWEST_ID && tie != KDGB_TIE_REF_LAST) return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown tie rule");
+    if (n == 0) return KDGB_OK;
+    if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    KDGB_CHECK(check_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    Tree t;
+    int rc = load_geometry(t, tri_v_dev, n_tris, s);
+    if (rc == KDGB_OK)
+        rc = brute_launch(t.p0.p, t.p1.p, t.p2.p, n_tris, tie, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, s);
+    release_all(t, s);
+    return rc;
+}
+
+}  // extern "C"
+
+namespace kdgb {
+int build_tuned(Tree &, const float *, int32_t, const kdgb_build_params &, cudaStream_t)
+{
+    return fail(KDGB_ERR_UNSUPPORTED, "tuned build not available in this library build");
+}
+}  // namespace kdgb

@@ -1,0 +1,167 @@
+// Internal declarations shared by the kdgb CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "kdgb.h"
+
+namespace kdgb {
+
+// ---------------------------------------------------------------------------
+// Status handling: no exception crosses the C ABI.
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int status, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define KDGB_CUDA(call)                                        \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return ::kdgb::cuda_fail(e_, #call); \
+    } while (0)
+
+#define KDGB_CHECK(call)                 \
+    do {                                 \
+        int s_ = (call);                 \
+        if (s_ != KDGB_OK) return s_;    \
+    } while (0)
+
+#define KDGB_LAUNCH_CHECK() KDGB_CUDA(cudaGetLastError())
+
+// ---------------------------------------------------------------------------
+// Device arrays owned by a tree handle.  `cap` counts elements.
+// ---------------------------------------------------------------------------
+template <class T>
+struct DevArray {
+    T *p = nullptr;
+    int64_t cap = 0;
+};
+
+// Grows `a` to hold at least n elements (stream-ordered allocation).  When
+// `keep` elements are live they are copied into the new block.  Newly
+// allocated storage is zero-filled when `zero` is set.
+template <class T>
+int ensure(DevArray<T> &a, int64_t n, cudaStream_t s, int64_t keep = 0, bool zero = false);
+
+template <class T>
+void release(DevArray<T> &a, cudaStream_t s);
+
+struct Tree {
+    int32_t n_tris = 0;
+    int32_t n_nodes = 0;
+    int32_t n_refs = 0;
+    int32_t n_upper_leaves = 0;
+    int32_t n_leaf_tris = 0;     // rows of the leaf-ordered triangle records
+    kdgb_build_stats stats{};
+
+    // Geometry (GeometryList SoA) and the packed triangle array used by builds.
+    DevArray<float4> p0, p1, p2;
+
+    // TriangleNode SoA (KDNode.h:65-73, TriangleNode.h:20-21).
+    DevArray<int8_t> info;
+    DevArray<float> split;
+    DevArray<float4> bmin, bmax;
+    DevArray<int32_t> pidx, bitmap, parent;
+    DevArray<int2> children;
+    DevArray<float> area;
+    DevArray<int32_t> prim_indices, leaf_ids;
+
+    // Traversal layout: one 16-byte record per node and leaf-ordered
+    // triangle records (v0, e1, e2, id) of 48 bytes.
+    DevArray<int4> tnode;
+    DevArray<float4> ttri;
+};
+
+// Builders (kdgb_build.cu).  tri_v_dev: T*9 floats.
+int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p,
+                    cudaStream_t s);
+int build_tuned(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p,
+                cudaStream_t s);
+int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s);
+
+// Traversal layout from the SoA arrays (kdgb_trace.cu).
+int pack_for_traversal(Tree &t, cudaStream_t s);
+
+// Device-wide exclusive scan of n records of K int32 lanes (lanes scanned
+// independently).  out has n+1 records; record n holds the totals.
+template <int K>
+int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Device helpers.
+// ---------------------------------------------------------------------------
+#ifdef __CUDACC__
+
+__device__ __forceinline__ float3 sub3(float3 a, float3 b)
+{
+    return make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+// dot and cross of the CUDA-SDK vector helpers, left to right, no FMA.
+__device__ __forceinline__ float dot3(float3 a, float3 b)
+{
+    float s = __fmul_rn(a.x, b.x);
+    s = __fadd_rn(s, __fmul_rn(a.y, b.y));
+    s = __fadd_rn(s, __fmul_rn(a.z, b.z));
+    return s;
+}
+__device__ __forceinline__ float3 cross3(float3 a, float3 b)
+{
+    return make_float3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)),
+                       __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+                       __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float3 inv3(float3 d)
+{
+    return make_float3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+}
+
+// min / max with IEEE totalOrder between -0 and +0 (finite inputs).
+__device__ __forceinline__ float kmin(float a, float b)
+{
+    return a < b ? a : (b < a ? b : (signbit(a) ? a : b));
+}
+__device__ __forceinline__ float kmax(float a, float b)
+{
+    return a > b ? a : (b > a ? b : (signbit(a) ? b : a));
+}
+
+// Order-preserving float <-> uint32 keys (totalOrder on non-NaN values).
+__device__ __forceinline__ unsigned fkey(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float funkey(unsigned k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__device__ __forceinline__ float axis_of(float3 a, int axis)
+{
+    return axis == KDGB_X ? a.x : (axis == KDGB_Y ? a.y : a.z);
+}
+__device__ __forceinline__ float axis_of4(float4 a, int axis)
+{
+    return axis == KDGB_X ? a.x : (axis == KDGB_Y ? a.y : a.z);
+}
+
+// IRayTracer.h:60-65 AdjustRayDirection.
+__device__ __forceinline__ float3 adjust_dir(float3 d)
+{
+    const float ooeps = 0x1p-80f;
+    d.x = fabsf(d.x) > ooeps ? d.x : copysignf(ooeps, d.x);
+    d.y = fabsf(d.y) > ooeps ? d.y : copysignf(ooeps, d.y);
+    d.z = fabsf(d.z) > ooeps ? d.z : copysignf(ooeps, d.z);
+    return d;
+}
+
+#endif  // __CUDACC__
+
+}  // namespace kdgb
+
+struct kdgb_tree {
+    kdgb::Tree t;
+};

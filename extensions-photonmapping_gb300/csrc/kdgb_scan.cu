@@ -1,0 +1,202 @@
+// Device-wide exclusive prefix sums of multi-lane int32 records.
+//
+// The reference scans with CUDPP (TriangleMapUpperCreator.cu:58-76, one plan
+// of 262,144 elements, return codes ignored).  This replacement is a
+// reduce-then-scan over records of K independent lanes: one pass of block
+// totals, one single-block scan of the totals, one pass that rescans each
+// block with its offset.  It needs no inter-block waiting, so it cannot
+// hang, and has no size cap below 2^31 records.
+#include "kdgb_internal.cuh"
+
+namespace kdgb {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 4;
+constexpr int kTile = kThreads * kItems;
+
+// Exclusive block scan of one value per lane per thread.  Returns the block
+// total of every lane in `total`.
+template <int K>
+__device__ __forceinline__ void block_scan(int32_t (&v)[K], int32_t (&total)[K])
+{
+    __shared__ int32_t warp_sum[K][kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int32_t incl[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        int32_t x = v[k];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        incl[k] = x;
+        if (lane == 31) warp_sum[k][warp] = x;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            int32_t x = lane < kThreads / 32 ? warp_sum[k][lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane < kThreads / 32) warp_sum[k][lane] = x;  // inclusive over warps
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int32_t before = warp > 0 ? warp_sum[k][warp - 1] : 0;
+        total[k] = warp_sum[k][kThreads / 32 - 1];
+        v[k] = before + incl[k] - v[k];
+    }
+    __syncthreads();
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) scan_reduce_kernel(const int32_t *__restrict__ in, int64_t n,
+                                                               int32_t *__restrict__ partial)
+{
+    const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
+    int32_t s[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] = 0;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const int64_t r = base + i;
+        if (r < n) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) s[k] += in[r * K + k];
+        }
+    }
+    int32_t tot[K];
+    block_scan<K>(s, tot);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) partial[(int64_t)blockIdx.x * K + k] = tot[k];
+    }
+}
+
+// Single block: exclusive scan of nb partial records in place; writes the
+// grand totals to `totals`.
+template <int K>
+__global__ void __launch_bounds__(kThreads) scan_partials_kernel(int32_t *__restrict__ partial, int64_t nb,
+                                                                 int32_t *__restrict__ totals)
+{
+    int32_t carry[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) carry[k] = 0;
+    for (int64_t start = 0; start < nb; start += kTile) {
+        const int64_t b = start + (int64_t)threadIdx.x * kItems;
+        int32_t vals[kItems][K];
+        int32_t s[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) s[k] = 0;
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                vals[i][k] = (b + i < nb) ? partial[(b + i) * K + k] : 0;
+                s[k] += vals[i][k];
+            }
+        }
+        int32_t tot[K];
+        block_scan<K>(s, tot);
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (b + i < nb) partial[(b + i) * K + k] = carry[k] + s[k];
+                s[k] += vals[i][k];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) carry[k] += tot[k];
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) totals[k] = carry[k];
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) scan_down_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                                                             int64_t n, const int32_t *__restrict__ partial)
+{
+    const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
+    int32_t vals[kItems][K];
+    int32_t s[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] = 0;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const int64_t r = base + i;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            vals[i][k] = r < n ? in[r * K + k] : 0;
+            s[k] += vals[i][k];
+        }
+    }
+    int32_t tot[K];
+    block_scan<K>(s, tot);
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] += partial ? partial[(int64_t)blockIdx.x * K + k] : 0;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const int64_t r = base + i;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (r < n) out[r * K + k] = s[k];
+            s[k] += vals[i][k];
+        }
+    }
+    // The last tile writes the totals record out[n] when there is a single tile.
+    if (partial == nullptr && threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[n * K + k] = tot[k];
+    }
+}
+
+}  // namespace
+
+template <int K>
+int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s)
+{
+    if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "scan: negative length");
+    if (n == 0) {
+        KDGB_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t) * K, s));
+        return KDGB_OK;
+    }
+    const int64_t nb = (n + kTile - 1) / kTile;
+    if (nb == 1) {
+        scan_down_kernel<K><<<1, kThreads, 0, s>>>(in, out, n, nullptr);
+        KDGB_LAUNCH_CHECK();
+        return KDGB_OK;
+    }
+    int32_t *partial = nullptr;
+    KDGB_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * K * (size_t)nb, s));
+    scan_reduce_kernel<K><<<(unsigned)nb, kThreads, 0, s>>>(in, n, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        scan_partials_kernel<K><<<1, kThreads, 0, s>>>(partial, nb, out + n * K);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        scan_down_kernel<K><<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, partial);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(partial, s);
+    if (e != cudaSuccess) return cuda_fail(e, "scan kernels");
+    return KDGB_OK;
+}
+
+template int scan_exclusive<1>(const int32_t *, int32_t *, int64_t, cudaStream_t);
+template int scan_exclusive<2>(const int32_t *, int32_t *, int64_t, cudaStream_t);
+template int scan_exclusive<6>(const int32_t *, int32_t *, int64_t, cudaStream_t);
+
+}  // namespace kdgb

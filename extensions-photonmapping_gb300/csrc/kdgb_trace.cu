@@ -1,0 +1,480 @@
+// Traversal: kd-restart, short-stack, brute force and shadow rays.
+//
+// Each tracer restates its reference kernel with the shading left out and
+// the first hit returned:
+//   kd-restart  Raytracer.cu:57-106 (TraceNode) + :165-262 (KDRestart)
+//   short-stack ShortStack.h:27-98 (ring buffer) + ShortStack.cu:58-194
+//   brute force BruteTracer.cu:54-96 (cap of 4096 triangles lifted)
+//   shadow      Raytracer.cu:108-163 (ShadowRay)
+// with Moeller-Trumbore (IRayTracer.h:111-145) and the leaf-skipping slab test
+// (IRayTracer.h:147-168).  Divisions are IEEE (__frcp_rn), products and sums
+// separately rounded, so hit ids match the CPU restatement bit for bit.
+//
+// Memory layout read by the tracers (built by pack_for_traversal):
+//   tnode[i]  int4  interior: {split bits, left, right, axis}
+//                   leaf:     {first record, record count, 0, 0}
+//   ttri[3r..3r+2]  float4 x3 per leaf record, in leaf order:
+//                   {v0.xyz, e1.x} {e1.yz, e2.xy} {e2.z, id bits, 0, 0}
+//   bmin/bmax       float4 node boxes (leaf skipping)
+// One 16-byte load per traversal step and three 16-byte loads per triangle
+// test, with no index indirection; e1 = v1 - v0 and e2 = v2 - v0 are the
+// same fp32 values the reference computes per test.
+#include <cuda_runtime.h>
+
+#include "kdgb_internal.cuh"
+
+namespace kdgb {
+
+namespace {
+
+constexpr int kPackBlock = 256;
+constexpr int kMaxStack = 8;
+// Hard cap on restarts/pops per ray when the caller passes 0, so that a
+// pathological ray cannot keep a thread alive forever.
+constexpr int kDefaultMaxIterations = 1 << 22;
+
+inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+__global__ void k_leaf_counts(int32_t n, const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
+                              int32_t *__restrict__ cnt)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) cnt[i] = info[i] == KDGB_LEAF ? __popc((unsigned)bitmap[i]) : 0;
+}
+
+__global__ void k_pack_nodes(int32_t n, const int8_t *__restrict__ info, const float *__restrict__ split,
+                             const int2 *__restrict__ ch, const int32_t *__restrict__ off, int4 *__restrict__ tnode)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int a = info[i] & 3;
+    if (a == KDGB_LEAF) {
+        tnode[i] = make_int4(off[i], off[i + 1] - off[i], 0, 0);
+    } else {
+        const int2 c = ch[i];
+        tnode[i] = make_int4(__float_as_int(split[i]), c.x, c.y, a);
+    }
+}
+
+// One warp per leaf: lane j handles bitmap bit j (LSB-first order).
+__global__ void k_pack_tris(int32_t n, const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
+                            const int32_t *__restrict__ pidx, const int32_t *__restrict__ prim_indices,
+                            const float4 *__restrict__ p0, const float4 *__restrict__ p1,
+                            const float4 *__restrict__ p2, const int32_t *__restrict__ off,
+                            float4 *__restrict__ ttri)
+{
+    const int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (node >= n) return;
+    if ((info[node] & 3) != KDGB_LEAF) return;
+    const unsigned bmp = (unsigned)bitmap[node];
+    if (!((bmp >> lane) & 1u)) return;
+    const int32_t rec = off[node] + __popc(bmp & ((1u << lane) - 1u));
+    const int32_t prim = prim_indices[pidx[node] + lane];
+    const float4 a = p0[prim], b = p1[prim], c = p2[prim];
+    const float3 v0 = make_float3(a.x, a.y, a.z);
+    const float3 e1 = sub3(make_float3(b.x, b.y, b.z), v0);
+    const float3 e2 = sub3(make_float3(c.x, c.y, c.z), v0);
+    ttri[3 * (int64_t)rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
+    ttri[3 * (int64_t)rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
+    ttri[3 * (int64_t)rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
+}
+
+struct Ctx {
+    const int4 *__restrict__ node;
+    const float4 *__restrict__ bmin;
+    const float4 *__restrict__ bmax;
+    const float4 *__restrict__ tri;
+};
+
+// Moeller-Trumbore on one packed record (IRayTracer.h:111-145).
+__device__ __forceinline__ void mt_test(float3 v0, float3 e1, float3 e2, int id, float3 o, float3 d, int tie,
+                                        int &hit, float &tb, float &ub, float &vb)
+{
+    const float3 p = cross3(d, e2);
+    const float3 t = sub3(o, v0);
+    const float3 q = cross3(t, e1);
+    const float inv_det = __frcp_rn(dot3(p, e1));
+    const float ht = __fmul_rn(inv_det, dot3(q, e2));
+    if (0.0f <= ht && ht <= tb) {
+        const float hu = __fmul_rn(inv_det, dot3(p, t));
+        const float hv = __fmul_rn(inv_det, dot3(q, d));
+        if (hu >= 0.0f && hv >= 0.0f && __fadd_rn(hu, hv) <= 1.0f) {
+            if (tie == KDGB_TIE_REF_LAST || hit == -1 || ht < tb || id < hit) {
+                hit = id; tb = ht; ub = hu; vb = hv;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void mt_record(const float4 *__restrict__ tri, int32_t rec, float3 o, float3 d, int tie,
+                                          int &hit, float &tb, float &ub, float &vb)
+{
+    const float4 a = __ldg(tri + 3 * (int64_t)rec);
+    const float4 b = __ldg(tri + 3 * (int64_t)rec + 1);
+    const float4 c = __ldg(tri + 3 * (int64_t)rec + 2);
+    mt_test(make_float3(a.x, a.y, a.z), make_float3(a.w, b.x, b.y), make_float3(b.z, b.w, c.x), __float_as_int(c.y),
+            o, d, tie, hit, tb, ub, vb);
+}
+
+// RayBoxIntersection<true> (IRayTracer.h:147-168).
+__device__ __forceinline__ bool ray_box(float3 o, float3 inv, float4 bmin, float4 bmax)
+{
+    const float lx = __fmul_rn(__fsub_rn(bmin.x, o.x), inv.x), ly = __fmul_rn(__fsub_rn(bmin.y, o.y), inv.y),
+                lz = __fmul_rn(__fsub_rn(bmin.z, o.z), inv.z);
+    const float hx = __fmul_rn(__fsub_rn(bmax.x, o.x), inv.x), hy = __fmul_rn(__fsub_rn(bmax.y, o.y), inv.y),
+                hz = __fmul_rn(__fsub_rn(bmax.z, o.z), inv.z);
+    float n = kmin(lx, hx);
+    n = kmax(n, kmin(ly, hy));
+    n = kmax(n, kmin(lz, hz));
+    float f = kmax(hx, lx);
+    f = kmin(f, kmax(ly, hy));
+    f = kmin(f, kmax(lz, hz));
+    return n <= f;
+}
+
+__device__ __forceinline__ int leaf_test(const Ctx &c, int4 leaf, float3 o, float3 d, int tie, float &tb, float &ub,
+                                         float &vb)
+{
+    int hit = -1;
+    for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) mt_record(c.tri, r, o, d, tie, hit, tb, ub, vb);
+    return hit;
+}
+
+// kd-restart, first hit (Raytracer.cu:57-106, 165-262).
+template <bool SKIP>
+__device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int maxit, float &t, float &u, float &v)
+{
+    const float3 d = adjust_dir(din);
+    const float3 inv = inv3(d);
+    float tmin = 0.0f;
+    int iters = 0;
+    do {
+        float tnext = KDGB_FINF;
+        int node = 0;
+        int4 nd = __ldg(c.node);
+        while (nd.w != KDGB_LEAF) {
+            const float ori = axis_of(o, nd.w), dir = axis_of(inv, nd.w);
+            const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
+            if (tmin < ts) {
+                node = 0 < dir ? nd.y : nd.z;
+                tnext = kmin(ts, tnext);
+            } else {
+                node = 0 < dir ? nd.z : nd.y;
+            }
+            nd = __ldg(c.node + node);
+        }
+        tmin = __fmul_rn(tnext, 1.00001f);
+        if (!SKIP || ray_box(o, inv, __ldg(c.bmin + node), __ldg(c.bmax + node))) {
+            float tb = tmin, ub = 0.0f, vb = 0.0f;
+            const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
+            if (h != -1) { t = tb; u = ub; v = vb; return h; }
+        }
+        if (++iters >= maxit) break;
+    } while (tmin < KDGB_FINF);
+    return -1;
+}
+
+// Short-stack, first hit (ShortStack.cu:58-194).  The stack of this thread
+// lives in shared memory at st[i * stride]; entries are (node, tMax bits).
+// The direction is inverted in place before each descent and inverted back
+// after it (ShortStack.cu:134,148), exactly as the reference does.
+template <bool SKIP>
+__device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int depth, int maxit, int2 *st,
+                                int stride, float &t, float &u, float &v)
+{
+    int nxt = 0, cnt = 0;
+    float3 d = adjust_dir(din);
+    float th = 0.0f;
+    int iters = 0;
+    do {
+        int node;
+        float tnext;
+        if (cnt == 0) {
+            node = 0;
+            tnext = KDGB_FINF;
+        } else {
+            nxt = (nxt == 0 ? depth : nxt) - 1;
+            --cnt;
+            const int2 e = st[nxt * stride];
+            node = e.x;
+            tnext = __int_as_float(e.y);
+        }
+        int4 nd = __ldg(c.node + node);
+        d = inv3(d);
+        while (nd.w != KDGB_LEAF) {
+            const float ori = axis_of(o, nd.w), dir = axis_of(d, nd.w);
+            const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
+            const int lower = 0 < dir ? nd.y : nd.z;
+            const int upper = 0 < dir ? nd.z : nd.y;
+            if (th < ts) {
+                node = lower;
+                if (ts < tnext) {
+                    st[nxt * stride] = make_int2(upper, __float_as_int(tnext));
+                    nxt = nxt == depth - 1 ? 0 : nxt + 1;
+                    cnt = cnt == depth ? depth : cnt + 1;
+                }
+                tnext = kmin(ts, tnext);
+            } else {
+                node = upper;
+            }
+            nd = __ldg(c.node + node);
+        }
+        d = inv3(d);
+        th = __fmul_rn(tnext, 1.00001f);
+        if (!SKIP || ray_box(o, inv3(d), __ldg(c.bmin + node), __ldg(c.bmax + node))) {
+            float tb = th, ub = 0.0f, vb = 0.0f;
+            const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
+            if (h != -1) { t = tb; u = ub; v = vb; return h; }
+        }
+        if (++iters >= maxit) break;
+    } while (th < KDGB_FINF);
+    return -1;
+}
+
+// ShadowRay (Raytracer.cu:108-163): from the light toward the point, the
+// direction neither normalised nor clamped; leaves whose exit reaches 0.999
+// are not tested; any hit occludes.
+__device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit)
+{
+    const float3 d = sub3(pt, lp);
+    const float3 inv = inv3(d);
+    float tmin = 0.0f;
+    int iters = 0;
+    do {
+        float tnext = KDGB_FINF;
+        int node = 0;
+        int4 nd = __ldg(c.node);
+        while (nd.w != KDGB_LEAF) {
+            const float ori = axis_of(lp, nd.w), dir = axis_of(inv, nd.w);
+            const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
+            if (tmin < ts) {
+                node = 0 < dir ? nd.y : nd.z;
+                tnext = kmin(ts, tnext);
+            } else {
+                node = 0 < dir ? nd.z : nd.y;
+            }
+            nd = __ldg(c.node + node);
+        }
+        tmin = __fmul_rn(tnext, 1.00001f);
+        if (tmin >= 0.999f) return 0;
+        float tb = tmin, ub = 0.0f, vb = 0.0f;
+        if (leaf_test(c, nd, lp, d, KDGB_TIE_REF_LAST, tb, ub, vb) != -1) return 1;
+        if (++iters >= maxit) break;
+    } while (tmin < 0.999f);
+    return 0;
+}
+
+// PacketIndex (IRayTracer.h:67-76): 4x8 pixel packets per warp.
+__device__ __forceinline__ int64_t ray_index(int64_t id, int tile_width)
+{
+    if (tile_width <= 0) return id;
+    const int64_t cell = id / 32;
+    const int64_t cols = tile_width / 4;
+    const int64_t bx = cell % cols, by = cell / cols;
+    const int64_t x = id % 4, y = (id % 32) / 4;
+    return bx * 4 + x + (by * 8 + y) * tile_width;
+}
+
+__device__ __forceinline__ float3 ld3(const float *__restrict__ p, int64_t i)
+{
+    return make_float3(__ldg(p + 3 * i), __ldg(p + 3 * i + 1), __ldg(p + 3 * i + 2));
+}
+
+struct TraceArgs {
+    Ctx c;
+    const float *o, *d;
+    int64_t n;
+    int32_t *hit;
+    float *t, *u, *v;
+    int32_t *occ;
+    float3 light;
+    int tie, depth, maxit, tile_width;
+};
+
+template <int TRACER, bool SKIP, bool SHADOW>
+__global__ void k_trace(TraceArgs a)
+{
+    extern __shared__ int2 stack_smem[];
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.n) return;
+    const int64_t i = ray_index(id, a.tile_width);
+    const float3 o = ld3(a.o, i), d = ld3(a.d, i);
+    float t = 0.0f, u = 0.0f, v = 0.0f;
+    int h;
+    if (TRACER == KDGB_TRACER_SHORTSTACK)
+        h = trace_shortstack<SKIP>(a.c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u, v);
+    else
+        h = trace_restart<SKIP>(a.c, o, d, a.tie, a.maxit, t, u, v);
+    if (h < 0) { t = INFINITY; u = 0.0f; v = 0.0f; }
+    a.hit[i] = h;
+    a.t[i] = t;
+    a.u[i] = u;
+    a.v[i] = v;
+    if (SHADOW) {
+        int occ = 0;
+        if (h >= 0) {
+            const float3 p = make_float3(__fadd_rn(o.x, __fmul_rn(t, d.x)), __fadd_rn(o.y, __fmul_rn(t, d.y)),
+                                         __fadd_rn(o.z, __fmul_rn(t, d.z)));
+            occ = trace_shadow(a.c, a.light, p, a.maxit);
+        }
+        a.occ[i] = occ;
+    }
+}
+
+__global__ void k_shadow(TraceArgs a)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    a.occ[i] = trace_shadow(a.c, a.light, ld3(a.o, i), a.maxit);
+}
+
+// Brute force (BruteTracer.cu:54-96): every ray tests every triangle in id
+// order; triangles are staged through shared memory one tile at a time.
+constexpr int kBruteBlock = 128;
+
+__global__ void __launch_bounds__(kBruteBlock) k_brute(const float4 *__restrict__ p0, const float4 *__restrict__ p1,
+                                                      const float4 *__restrict__ p2, int32_t T, int tie,
+                                                      const float *__restrict__ ro, const float *__restrict__ rd,
+                                                      int64_t n, int32_t *hit, float *ot, float *ou, float *ov)
+{
+    __shared__ float4 sa[kBruteBlock], sb[kBruteBlock], sc[kBruteBlock];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    float3 o = make_float3(0.f, 0.f, 0.f), d = o;
+    if (live) { o = ld3(ro, i); d = ld3(rd, i); }
+    int h = -1;
+    float tb = KDGB_FINF, ub = 0.0f, vb = 0.0f;
+    for (int32_t base = 0; base < T; base += kBruteBlock) {
+        const int32_t j = base + threadIdx.x;
+        if (j < T) {
+            const float4 a = p0[j], b = p1[j], c = p2[j];
+            const float3 v0 = make_float3(a.x, a.y, a.z);
+            const float3 e1 = sub3(make_float3(b.x, b.y, b.z), v0);
+            const float3 e2 = sub3(make_float3(c.x, c.y, c.z), v0);
+            sa[threadIdx.x] = make_float4(v0.x, v0.y, v0.z, e1.x);
+            sb[threadIdx.x] = make_float4(e1.y, e1.z, e2.x, e2.y);
+            sc[threadIdx.x] = make_float4(e2.z, __int_as_float(j), 0.0f, 0.0f);
+        }
+        __syncthreads();
+        const int m = min(kBruteBlock, T - base);
+        if (live) {
+            for (int k = 0; k < m; ++k) {
+                const float4 a = sa[k], b = sb[k], c = sc[k];
+                mt_test(make_float3(a.x, a.y, a.z), make_float3(a.w, b.x, b.y), make_float3(b.z, b.w, c.x),
+                        __float_as_int(c.y), o, d, tie, h, tb, ub, vb);
+            }
+        }
+        __syncthreads();
+    }
+    if (!live) return;
+    if (tb < KDGB_FINF) {
+        hit[i] = h; ot[i] = tb; ou[i] = ub; ov[i] = vb;
+    } else {
+        hit[i] = -1; ot[i] = INFINITY; ou[i] = 0.0f; ov[i] = 0.0f;
+    }
+}
+
+}  // namespace
+
+int pack_for_traversal(Tree &t, cudaStream_t s)
+{
+    const int32_t n = t.n_nodes;
+    int32_t *cnt = nullptr, *off = nullptr;
+    KDGB_CUDA(cudaMallocAsync(&cnt, sizeof(int32_t) * (size_t)(n > 0 ? n : 1), s));
+    cudaError_t e = cudaMallocAsync(&off, sizeof(int32_t) * ((size_t)n + 1), s);
+    if (e != cudaSuccess) { cudaFreeAsync(cnt, s); return cuda_fail(e, "cudaMallocAsync"); }
+    int rc = KDGB_OK;
+    int32_t total = 0;
+    do {
+        if (n > 0) {
+            k_leaf_counts<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.bitmap.p, cnt);
+            if ((e = cudaGetLastError()) != cudaSuccess) { rc = cuda_fail(e, "k_leaf_counts"); break; }
+        }
+        if ((rc = scan_exclusive<1>(cnt, off, n, s)) != KDGB_OK) break;
+        if ((e = cudaMemcpyAsync(&total, off + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+            rc = cuda_fail(e, "pack: total");
+            break;
+        }
+        if ((rc = ensure(t.tnode, n, s)) != KDGB_OK) break;
+        if ((rc = ensure(t.ttri, 3 * (int64_t)total, s)) != KDGB_OK) break;
+        t.n_leaf_tris = total;
+        if (n > 0) {
+            k_pack_nodes<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.split.p, t.children.p, off,
+                                                                         t.tnode.p);
+            k_pack_tris<<<blocks_for((int64_t)n * 32, kPackBlock), kPackBlock, 0, s>>>(
+                n, t.info.p, t.bitmap.p, t.pidx.p, t.prim_indices.p, t.p0.p, t.p1.p, t.p2.p, off, t.ttri.p);
+            if ((e = cudaGetLastError()) != cudaSuccess) { rc = cuda_fail(e, "pack kernels"); break; }
+        }
+    } while (0);
+    cudaFreeAsync(cnt, s);
+    cudaFreeAsync(off, s);
+    return rc;
+}
+
+int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
+                 int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s)
+{
+    TraceArgs a;
+    a.c.node = t.tnode.p;
+    a.c.bmin = t.bmin.p;
+    a.c.bmax = t.bmax.p;
+    a.c.tri = t.ttri.p;
+    a.o = o; a.d = d; a.n = n;
+    a.hit = hit; a.t = tt; a.u = uu; a.v = vv; a.occ = occ;
+    a.light = light ? make_float3(light[0], light[1], light[2]) : make_float3(0.f, 0.f, 0.f);
+    a.tie = p.tie;
+    a.depth = p.stack_depth;
+    a.maxit = p.max_iterations > 0 ? p.max_iterations : kDefaultMaxIterations;
+    a.tile_width = p.tile_width;
+    const int bs = p.block_size > 0 ? p.block_size : 128;
+    const unsigned grid = blocks_for(n, bs);
+    const bool skip = p.leaf_skipping != 0;
+    const bool shadow = occ != nullptr;
+    size_t smem = 0;
+    if (p.tracer == KDGB_TRACER_SHORTSTACK) {
+        smem = sizeof(int2) * (size_t)p.stack_depth * bs;
+        if (skip && shadow) k_trace<KDGB_TRACER_SHORTSTACK, true, true><<<grid, bs, smem, s>>>(a);
+        else if (skip) k_trace<KDGB_TRACER_SHORTSTACK, true, false><<<grid, bs, smem, s>>>(a);
+        else if (shadow) k_trace<KDGB_TRACER_SHORTSTACK, false, true><<<grid, bs, smem, s>>>(a);
+        else k_trace<KDGB_TRACER_SHORTSTACK, false, false><<<grid, bs, smem, s>>>(a);
+    } else {
+        if (skip && shadow) k_trace<KDGB_TRACER_RESTART, true, true><<<grid, bs, 0, s>>>(a);
+        else if (skip) k_trace<KDGB_TRACER_RESTART, true, false><<<grid, bs, 0, s>>>(a);
+        else if (shadow) k_trace<KDGB_TRACER_RESTART, false, true><<<grid, bs, 0, s>>>(a);
+        else k_trace<KDGB_TRACER_RESTART, false, false><<<grid, bs, 0, s>>>(a);
+    }
+    KDGB_LAUNCH_CHECK();
+    return KDGB_OK;
+}
+
+int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, int64_t n, const float *light,
+                  int32_t *occ, cudaStream_t s)
+{
+    TraceArgs a;
+    a.c.node = t.tnode.p;
+    a.c.bmin = t.bmin.p;
+    a.c.bmax = t.bmax.p;
+    a.c.tri = t.ttri.p;
+    a.o = pts; a.d = nullptr; a.n = n;
+    a.hit = nullptr; a.t = a.u = a.v = nullptr; a.occ = occ;
+    a.light = make_float3(light[0], light[1], light[2]);
+    a.tie = p.tie; a.depth = p.stack_depth;
+    a.maxit = p.max_iterations > 0 ? p.max_iterations : kDefaultMaxIterations;
+    a.tile_width = 0;
+    const int bs = p.block_size > 0 ? p.block_size : 128;
+    k_shadow<<<blocks_for(n, bs), bs, 0, s>>>(a);
+    KDGB_LAUNCH_CHECK();
+    return KDGB_OK;
+}
+
+int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, int32_t T, int tie, const float *o,
+                 const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv, cudaStream_t s)
+{
+    k_brute<<<blocks_for(n, kBruteBlock), kBruteBlock, 0, s>>>(p0, p1, p2, T, tie, o, d, n, hit, tt, uu, vv);
+    KDGB_LAUNCH_CHECK();
+    return KDGB_OK;
+}
+
+}  // namespace kdgb

@@ -1,0 +1,374 @@
+"""kdgb -- GB300 kd-tree builder and ray tracer (host-side Python mirror).
+
+The compute runs in libkdgb.so (hand-written sm_103a CUDA behind the C ABI in
+include/kdgb.h).  This module is a thin host layer over that ABI with the
+reference's plugin names:
+
+* ``TriangleMap``  -- Utils/CUDA/TriangleMap.h:31-83 (Create, setters, GetNodes)
+* ``RayTracer``, ``ShortStack``, ``BruteTracer`` -- the IRayTracer family
+  (Utils/CUDA/IRayTracer.h:28-58); ``Trace`` returns first-hit buffers
+  instead of drawing into an OpenGL canvas.
+* ``KDTree`` -- the handle itself (build / rebuild / upload / view / trace).
+
+PyTorch supplies device memory and the current stream; nothing here falls
+back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import scenes
+from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ERR_NO_DEVICE, FINF, LEAF, LOWER_BITMAP, LOWER_SAH,
+                   TIE_LOWEST_ID, TIE_REF_LAST, TRACER_BRUTE, TRACER_RESTART, TRACER_SHORTSTACK, X, Y, Z,
+                   BuildParams, BuildStats, KdgbError, TraceParams, TreeView, build_params, check, lib,
+                   library_path, trace_params)
+
+__all__ = ["KDTree", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
+           "trace_params", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
+           "BUILD_REFERENCE", "BUILD_TUNED", "TRACER_RESTART", "TRACER_SHORTSTACK", "TRACER_BRUTE",
+           "TIE_LOWEST_ID", "TIE_REF_LAST", "FINF", "lib", "library_path"]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream(stream=None) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _dev(a, dtype, shape_last=None):
+    """A contiguous CUDA tensor of `dtype` from a tensor or numpy array."""
+    torch = _torch()
+    if isinstance(a, np.ndarray):
+        a = torch.from_numpy(np.ascontiguousarray(a))
+    if not a.is_cuda:
+        a = a.cuda()
+    a = a.to(dtype).contiguous()
+    if shape_last is not None:
+        a = a.reshape(-1, shape_last)
+    return a
+
+
+def _ptr(t) -> C.c_void_p:
+    return C.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else C.c_void_p(0)
+
+
+@dataclass
+class HostTree:
+    """Tree arrays copied to host memory (KDNode / TriangleNode SoA)."""
+    info: np.ndarray
+    split: np.ndarray
+    aabb_min: np.ndarray
+    aabb_max: np.ndarray
+    prim_index: np.ndarray
+    bitmap: np.ndarray
+    children: np.ndarray
+    area: np.ndarray
+    parent: np.ndarray
+    prim_indices: np.ndarray
+    leaf_ids: np.ndarray
+
+
+class KDTree:
+    """Owner of one kdgb_tree handle."""
+
+    def __init__(self, handle: C.c_void_p, n_tris: int):
+        self._h = handle
+        self.n_tris = n_tris
+
+    # -- construction -----------------------------------------------------
+    @classmethod
+    def build(cls, tris, params: BuildParams | None = None, stream=None, **kw) -> "KDTree":
+        tri = _dev(tris, _torch().float32, 9)
+        p = params if params is not None else build_params(**kw)
+        h = C.c_void_p()
+        check(lib().kdgb_build(_ptr(tri), tri.shape[0], C.byref(p), C.byref(h), C.c_void_p(_stream(stream))),
+              "kdgb_build")
+        return cls(h, tri.shape[0])
+
+    def rebuild(self, tris, params: BuildParams | None = None, stream=None, **kw) -> None:
+        tri = _dev(tris, _torch().float32, 9)
+        p = params if params is not None else build_params(**kw)
+        check(lib().kdgb_rebuild(self._h, _ptr(tri), tri.shape[0], C.byref(p), C.c_void_p(_stream(stream))),
+              "kdgb_rebuild")
+        self.n_tris = tri.shape[0]
+
+    @classmethod
+    def upload(cls, arrays, tris: np.ndarray, stream=None) -> "KDTree":
+        """Creates a handle from host tree arrays (any object with the
+        HostTree fields, e.g. a CPU-built tree) and host triangles."""
+        tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+        keep = {}
+
+        def host(name, dtype):
+            a = np.ascontiguousarray(getattr(arrays, name), dtype=dtype)
+            keep[name] = a
+            return a.ctypes.data_as(C.c_void_p)
+
+        v = TreeView()
+        v.n_nodes = int(np.asarray(arrays.info).shape[0])
+        v.n_refs = int(np.asarray(arrays.prim_indices).shape[0])
+        v.n_upper_leaves = int(np.asarray(arrays.leaf_ids).shape[0])
+        v.n_tris = tris.shape[0]
+        v.info = host("info", np.int8)
+        v.split = host("split", np.float32)
+        v.aabb_min = host("aabb_min", np.float32)
+        v.aabb_max = host("aabb_max", np.float32)
+        v.prim_index = host("prim_index", np.int32)
+        v.bitmap = host("bitmap", np.int32)
+        v.children = host("children", np.int32)
+        v.area = host("area", np.float32)
+        v.parent = host("parent", np.int32)
+        v.prim_indices = host("prim_indices", np.int32)
+        v.leaf_ids = host("leaf_ids", np.int32)
+        h = C.c_void_p()
+        check(lib().kdgb_tree_upload(C.byref(v), tris.ctypes.data_as(C.c_void_p), tris.shape[0], C.byref(h),
+                                     C.c_void_p(_stream(stream))), "kdgb_tree_upload")
+        return cls(h, tris.shape[0])
+
+    def close(self) -> None:
+        if self._h:
+            check(lib().kdgb_tree_destroy(self._h), "kdgb_tree_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().kdgb_tree_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- inspection -------------------------------------------------------
+    def view(self) -> TreeView:
+        v = TreeView()
+        check(lib().kdgb_tree_view_get(self._h, C.byref(v)), "kdgb_tree_view_get")
+        return v
+
+    def stats(self) -> BuildStats:
+        s = BuildStats()
+        check(lib().kdgb_tree_stats(self._h, C.byref(s)), "kdgb_tree_stats")
+        return s
+
+    def to_host(self) -> HostTree:
+        """Copies the SoA tree arrays to host memory (kdgb_tree_download)."""
+        v = self.view()
+        n, r, nl = v.n_nodes, v.n_refs, v.n_upper_leaves
+        h = HostTree(info=np.empty(n, np.int8), split=np.empty(n, np.float32),
+                     aabb_min=np.empty((n, 4), np.float32), aabb_max=np.empty((n, 4), np.float32),
+                     prim_index=np.empty(n, np.int32), bitmap=np.empty(n, np.int32),
+                     children=np.empty((n, 2), np.int32), area=np.empty(n, np.float32),
+                     parent=np.empty(n, np.int32), prim_indices=np.empty(r, np.int32),
+                     leaf_ids=np.empty(nl, np.int32))
+        dst = TreeView()
+        for name in ("info", "split", "aabb_min", "aabb_max", "prim_index", "bitmap", "children", "area",
+                     "parent", "prim_indices", "leaf_ids"):
+            setattr(dst, name, getattr(h, name).ctypes.data_as(C.c_void_p))
+        dst.n_nodes, dst.n_refs, dst.n_upper_leaves = n, r, nl
+        check(lib().kdgb_tree_download(self._h, C.byref(dst)), "kdgb_tree_download")
+        return h
+
+    # -- tracing ----------------------------------------------------------
+    def trace(self, o, d, params: TraceParams | None = None, stream=None, out=None, **kw):
+        """First hit of each ray: (hit int32, t, u, v float32) CUDA tensors."""
+        torch = _torch()
+        o = _dev(o, torch.float32, 3)
+        d = _dev(d, torch.float32, 3)
+        n = o.shape[0]
+        p = params if params is not None else trace_params(**kw)
+        if out is None:
+            out = (torch.empty(n, dtype=torch.int32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device))
+        hit, t, u, v = out
+        check(lib().kdgb_trace(self._h, C.byref(p), _ptr(o), _ptr(d), n, _ptr(hit), _ptr(t), _ptr(u), _ptr(v),
+                               C.c_void_p(_stream(stream))), "kdgb_trace")
+        return hit, t, u, v
+
+    def trace_shadow(self, points, light, params: TraceParams | None = None, stream=None, **kw):
+        torch = _torch()
+        pts = _dev(points, torch.float32, 3)
+        p = params if params is not None else trace_params(**kw)
+        lp = (C.c_float * 3)(*[float(x) for x in light])
+        occ = torch.empty(pts.shape[0], dtype=torch.int32, device=pts.device)
+        check(lib().kdgb_trace_shadow(self._h, C.byref(p), _ptr(pts), pts.shape[0], lp, _ptr(occ),
+                                      C.c_void_p(_stream(stream))), "kdgb_trace_shadow")
+        return occ
+
+    def trace_primary_shadow(self, o, d, light, params: TraceParams | None = None, stream=None, out=None, **kw):
+        torch = _torch()
+        o = _dev(o, torch.float32, 3)
+        d = _dev(d, torch.float32, 3)
+        n = o.shape[0]
+        p = params if params is not None else trace_params(**kw)
+        lp = (C.c_float * 3)(*[float(x) for x in light])
+        if out is None:
+            out = (torch.empty(n, dtype=torch.int32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device),
+                   torch.empty(n, dtype=torch.int32, device=o.device))
+        hit, t, u, v, occ = out
+        check(lib().kdgb_trace_primary_shadow(self._h, C.byref(p), _ptr(o), _ptr(d), n, lp, _ptr(hit), _ptr(t),
+                                              _ptr(u), _ptr(v), _ptr(occ), C.c_void_p(_stream(stream))),
+              "kdgb_trace_primary_shadow")
+        return hit, t, u, v, occ
+
+
+def trace_brute(tris, o, d, tie: int = TIE_LOWEST_ID, stream=None):
+    """BruteTracer over device triangles, without a tree."""
+    torch = _torch()
+    tri = _dev(tris, torch.float32, 9)
+    o = _dev(o, torch.float32, 3)
+    d = _dev(d, torch.float32, 3)
+    n = o.shape[0]
+    hit = torch.empty(n, dtype=torch.int32, device=o.device)
+    t = torch.empty(n, dtype=torch.float32, device=o.device)
+    u = torch.empty_like(t)
+    v = torch.empty_like(t)
+    check(lib().kdgb_trace_brute(_ptr(tri), tri.shape[0], tie, _ptr(o), _ptr(d), n, _ptr(hit), _ptr(t), _ptr(u),
+                                 _ptr(v), C.c_void_p(_stream(stream))), "kdgb_trace_brute")
+    return hit, t, u, v
+
+
+class TriangleMap:
+    """Utils/CUDA/TriangleMap.h:31-83 over the C ABI.  The scene is a (T, 9)
+    triangle array (the GeometryList the reference collects from the scene
+    graph); Create() builds, the getters return the handle's arrays."""
+
+    BITMAP, BALANCED, SAH = 0, 1, 2
+    BOX, DIVIDE, SPLIT = 0, 1, 2
+
+    def __init__(self, tris=None):
+        self.geometry = tris
+        self.params = build_params()
+        self.tree: KDTree | None = None
+        self.construction_time = 0.0
+
+    def SetGeometry(self, tris) -> None:
+        self.geometry = tris
+
+    def Create(self) -> None:
+        if self.tree is None:
+            self.tree = KDTree.build(self.geometry, self.params)
+        else:
+            self.tree.rebuild(self.geometry, self.params)
+        self.construction_time = self.tree.stats().build_ms
+
+    def SetLowerAlgorithm(self, algo: int) -> None:
+        if algo == self.BALANCED:
+            raise KdgbError(8, "SetLowerAlgorithm(BALANCED)")
+        self.params.lower = LOWER_SAH if algo == self.SAH else LOWER_BITMAP
+
+    def GetLowerAlgorithm(self) -> int:
+        return self.SAH if self.params.lower == LOWER_SAH else self.BITMAP
+
+    def SplitEmptySpace(self, s: bool) -> None:
+        self.params.split_empty_space = int(bool(s))
+
+    def IsSplittingEmptySpace(self) -> bool:
+        return bool(self.params.split_empty_space)
+
+    def SetSplitMethod(self, m: int) -> None:
+        if m != self.BOX:
+            raise KdgbError(8, "SetSplitMethod: only BOX is provided")
+
+    def GetSplitMethod(self) -> int:
+        return self.BOX
+
+    def SetPropagateBoundingBox(self, p: bool) -> None:
+        self.params.propagate_aabbs = int(bool(p))
+
+    def GetPropagateBoundingBox(self) -> bool:
+        return bool(self.params.propagate_aabbs)
+
+    def SetTraversalCost(self, t: float) -> None:
+        self.params.traversal_cost = float(t)
+
+    def GetTraversalCost(self) -> float:
+        return float(self.params.traversal_cost)
+
+    @staticmethod
+    def SetEmptySpaceThreshold(t: float) -> None:
+        TriangleMap._threshold = float(t)
+
+    def GetConstructionTime(self) -> float:
+        return self.construction_time
+
+    def GetNodes(self) -> TreeView:
+        return self.tree.view()
+
+    def GetPrimitiveIndices(self):
+        return self.tree.view().prim_indices
+
+
+class IRayTracer:
+    """IRayTracer (IRayTracer.h:28-58).  Trace(o, d) returns (hit, t, u, v)."""
+
+    MOELLER, WOOP = 0, 1
+    _tracer = TRACER_RESTART
+
+    def __init__(self, triangle_map: TriangleMap):
+        self.map = triangle_map
+        self.params = trace_params(tracer=self._tracer)
+        self.render_time = 0.0
+
+    def SetLeafSkipping(self, s: bool) -> None:
+        self.params.leaf_skipping = int(bool(s))
+
+    def GetLeafSkipping(self) -> bool:
+        return bool(self.params.leaf_skipping)
+
+    def SetIntersectionAlgorithm(self, a: int) -> None:
+        if a != self.MOELLER:
+            raise KdgbError(8, "SetIntersectionAlgorithm: only MOELLER is provided")
+
+    def GetRenderTime(self) -> float:
+        return self.render_time
+
+    def Trace(self, o, d, tile_width: int = 0):
+        torch = _torch()
+        p = TraceParams.from_buffer_copy(self.params)
+        p.tile_width = tile_width
+        if not self.map.GetPropagateBoundingBox():
+            p.leaf_skipping = 0  # Raytracer.cu:313
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = self.map.tree.trace(o, d, p)
+        e1.record()
+        e1.synchronize()
+        self.render_time = e0.elapsed_time(e1)
+        return out
+
+    def HostTrace(self, o, d):
+        """Single-ray trace for debugging (the reference's HostTrace): runs
+        the same device kernel on one ray and returns host values."""
+        hit, t, u, v = self.map.tree.trace(np.asarray(o, np.float32).reshape(1, 3),
+                                           np.asarray(d, np.float32).reshape(1, 3), self.params)
+        return int(hit.cpu()[0]), float(t.cpu()[0]), float(u.cpu()[0]), float(v.cpu()[0])
+
+
+class RayTracer(IRayTracer):
+    _tracer = TRACER_RESTART
+
+
+class ShortStack(IRayTracer):
+    _tracer = TRACER_SHORTSTACK
+
+
+class BruteTracer(IRayTracer):
+    _tracer = TRACER_BRUTE

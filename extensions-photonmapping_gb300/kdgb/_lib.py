@@ -1,0 +1,137 @@
+"""ctypes binding of libkdgb.so (the C ABI declared in include/kdgb.h).
+
+Loading fails loudly when the library has not been built: there is no CPU
+fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+LEAF, X, Y, Z = 0, 1, 2, 3
+LOWER_BITMAP, LOWER_SAH = 0, 1
+BUILD_REFERENCE, BUILD_TUNED = 0, 1
+TRACER_RESTART, TRACER_SHORTSTACK, TRACER_BRUTE = 0, 1, 2
+TIE_LOWEST_ID, TIE_REF_LAST = 0, 1
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_CUDA = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_CAPACITY = 4
+ERR_DEGENERATE = 5
+ERR_NONFINITE = 6
+ERR_TIMEOUT = 7
+ERR_UNSUPPORTED = 8
+ERR_NO_DEVICE = 9
+
+FINF = 2139095040.0
+
+
+class BuildParams(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("lower", C.c_int32), ("split_empty_space", C.c_int32),
+                ("propagate_aabbs", C.c_int32), ("empty_space_threshold", C.c_float),
+                ("traversal_cost", C.c_float), ("intersection_cost", C.c_float), ("min_leaf", C.c_int32),
+                ("esc_zmax_as_x", C.c_int32), ("max_levels", C.c_int32), ("leaf_size", C.c_int32),
+                ("upper_levels", C.c_int32), ("sah_bins", C.c_int32)]
+
+
+class TraceParams(C.Structure):
+    _fields_ = [("tracer", C.c_int32), ("leaf_skipping", C.c_int32), ("tie", C.c_int32),
+                ("stack_depth", C.c_int32), ("max_iterations", C.c_int32), ("block_size", C.c_int32),
+                ("tile_width", C.c_int32)]
+
+
+class TreeView(C.Structure):
+    _fields_ = [("n_nodes", C.c_int32), ("n_refs", C.c_int32), ("n_upper_leaves", C.c_int32),
+                ("n_tris", C.c_int32), ("info", C.c_void_p), ("split", C.c_void_p), ("aabb_min", C.c_void_p),
+                ("aabb_max", C.c_void_p), ("prim_index", C.c_void_p), ("bitmap", C.c_void_p),
+                ("children", C.c_void_p), ("area", C.c_void_p), ("parent", C.c_void_p),
+                ("prim_indices", C.c_void_p), ("leaf_ids", C.c_void_p), ("p0", C.c_void_p), ("p1", C.c_void_p),
+                ("p2", C.c_void_p)]
+
+
+class BuildStats(C.Structure):
+    _fields_ = [("upper_levels", C.c_int32), ("lower_levels", C.c_int32), ("n_nodes", C.c_int32),
+                ("n_refs", C.c_int32), ("n_leaves", C.c_int32), ("max_depth", C.c_int32),
+                ("build_ms", C.c_float)]
+
+
+# Every symbol include/kdgb.h declares, with its ctypes signature.
+P = C.c_void_p
+SIGNATURES = {
+    "kdgb_abi_version": (C.c_int, []),
+    "kdgb_status_string": (C.c_char_p, [C.c_int]),
+    "kdgb_last_error": (C.c_char_p, []),
+    "kdgb_build_params_default": (None, [C.POINTER(BuildParams)]),
+    "kdgb_trace_params_default": (None, [C.POINTER(TraceParams)]),
+    "kdgb_build": (C.c_int, [P, C.c_int32, C.POINTER(BuildParams), C.POINTER(C.c_void_p), P]),
+    "kdgb_rebuild": (C.c_int, [P, P, C.c_int32, C.POINTER(BuildParams), P]),
+    "kdgb_tree_upload": (C.c_int, [C.POINTER(TreeView), P, C.c_int32, C.POINTER(C.c_void_p), P]),
+    "kdgb_tree_destroy": (C.c_int, [P]),
+    "kdgb_tree_view_get": (C.c_int, [P, C.POINTER(TreeView)]),
+    "kdgb_tree_download": (C.c_int, [P, C.POINTER(TreeView)]),
+    "kdgb_tree_stats": (C.c_int, [P, C.POINTER(BuildStats)]),
+    "kdgb_trace": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P]),
+    "kdgb_trace_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, C.c_int32, P, P, P]),
+    "kdgb_trace_primary_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P, P, P]),
+    "kdgb_trace_brute": (C.c_int, [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, P]),
+}
+
+_lib = None
+
+
+class KdgbError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        L = lib()
+        msg = L.kdgb_status_string(status).decode()
+        detail = L.kdgb_last_error().decode()
+        super().__init__(f"{where}: {msg} ({detail})")
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def lib():
+    """The loaded libkdgb.so.  Raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"libkdgb.so is not built ({path}); run __graft_entry__.build() first")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int, where: str) -> None:
+    if status != OK:
+        raise KdgbError(status, where)
+
+
+def build_params(**kw) -> BuildParams:
+    p = BuildParams()
+    lib().kdgb_build_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def trace_params(**kw) -> TraceParams:
+    p = TraceParams()
+    lib().kdgb_trace_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p

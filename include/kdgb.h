@@ -1,0 +1,214 @@
+/*
+ * kdgb.h -- C ABI of the GB300 kd-tree builder and ray tracer.
+ *
+ * Drop-in for the tree-build and trace path of OpenEngineDK/
+ * extensions-PhotonMapping.  The reference exposes that path as C++ classes
+ * (TriangleMap, KDNode/TriangleNode, IRayTracer and its three tracers); each
+ * entry point below names the reference interface it replaces.  The C++
+ * plugin shims in kdgb_plugin.hpp keep the reference class names on top of
+ * this ABI.
+ *
+ * Conventions
+ *  - Every function returns an int status (KDGB_OK = 0) and never throws.
+ *    kdgb_status_string() names a status, kdgb_last_error() gives the detail
+ *    of the last failure on the calling thread.
+ *  - Pointers named *_dev are device pointers; everything is stream ordered
+ *    on the cudaStream_t passed in (0 = legacy default stream).  Calls that
+ *    must size their output (kdgb_build) synchronise that stream.
+ *  - A kdgb_tree handle may be traced from several streams at once; building
+ *    or destroying it must not overlap other use of the same handle.
+ *  - Triangles are T*9 floats (v0.xyz v1.xyz v2.xyz); rays are n*3 float
+ *    origins and n*3 float directions; hit outputs are SoA.
+ *  - Arithmetic: fp32, each multiply/add rounded separately (no FMA
+ *    contraction), IEEE division and square root, so results match the CPU
+ *    restatement of the reference bit for bit.
+ */
+#ifndef KDGB_H
+#define KDGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *kdgb_stream_t; /* same type as cudaStream_t */
+
+#if defined(__GNUC__)
+#define KDGB_API __attribute__((visibility("default")))
+#else
+#define KDGB_API
+#endif
+
+#define KDGB_ABI_VERSION 1
+
+/* Utils/CUDA/Utils.h:18: the reference's "infinity" is the integer
+ * 0x7f800000 converted to float. */
+#define KDGB_FINF 2139095040.0f
+
+typedef enum kdgb_status {
+    KDGB_OK = 0,
+    KDGB_ERR_INVALID_ARGUMENT = 1,
+    KDGB_ERR_CUDA = 2,
+    KDGB_ERR_OUT_OF_MEMORY = 3,
+    KDGB_ERR_CAPACITY = 4,      /* a fixed-size pool or queue is full */
+    KDGB_ERR_DEGENERATE = 5,    /* upper build did not terminate within max_levels */
+    KDGB_ERR_NONFINITE = 6,     /* NaN or Inf vertex coordinate */
+    KDGB_ERR_TIMEOUT = 7,       /* a bounded device-side wait gave up */
+    KDGB_ERR_UNSUPPORTED = 8,
+    KDGB_ERR_NO_DEVICE = 9
+} kdgb_status;
+
+/* KDNode.h:59-62 */
+enum { KDGB_LEAF = 0, KDGB_X = 1, KDGB_Y = 2, KDGB_Z = 3 };
+
+/* TriangleMap.h:33 LowerAlgorithm (BALANCED not provided). */
+enum { KDGB_LOWER_BITMAP = 0, KDGB_LOWER_SAH = 1 };
+
+/* Build modes.  REFERENCE reproduces TriangleMap::Create bit for bit.
+ * TUNED runs median/empty-space splits for the top `upper_levels` levels and
+ * a binned SAH (traversal_cost, intersection_cost, leaf_size) below them. */
+enum { KDGB_BUILD_REFERENCE = 0, KDGB_BUILD_TUNED = 1 };
+
+/* Tracers: Raytracer (kd-restart), ShortStack, BruteTracer. */
+enum { KDGB_TRACER_RESTART = 0, KDGB_TRACER_SHORTSTACK = 1, KDGB_TRACER_BRUTE = 2 };
+
+/* Exact-tie rule between triangles hit at the same t.  LOWEST_ID is the
+ * default; REF_LAST keeps the reference's `t <= tBest` (IRayTracer.h:133),
+ * where the last triangle tested wins. */
+enum { KDGB_TIE_LOWEST_ID = 0, KDGB_TIE_REF_LAST = 1 };
+
+typedef struct kdgb_build_params {
+    int32_t mode;                  /* KDGB_BUILD_* */
+    int32_t lower;                 /* KDGB_LOWER_* (REFERENCE mode), TriangleMap.cu:46 default BITMAP */
+    int32_t split_empty_space;     /* TriangleMapUpperCreator.cu:31 default 1 */
+    int32_t propagate_aabbs;       /* TriangleMap.cu:47 default 1 */
+    float   empty_space_threshold; /* TriangleMapUpperCreator.cu:28 default 0.35 */
+    float   traversal_cost;        /* TriangleMap.cu:48 default 24 */
+    float   intersection_cost;     /* 1 = reference SAH rule */
+    int32_t min_leaf;              /* SAH never splits nodes with <= min_leaf triangles (0 = reference) */
+    int32_t esc_zmax_as_x;         /* 1 = EmptySpaceSplitting.h:172-181 behaviour (max-z face cut on x) */
+    int32_t max_levels;            /* upper-phase level guard, default 64 */
+    int32_t leaf_size;             /* KDNode.h:21 KDNODE_MAX_LOWER_SIZE, default 32, <= 32 */
+    int32_t upper_levels;          /* TUNED: median/empty-space levels before SAH, default 8 */
+    int32_t sah_bins;              /* TUNED: SAH bins per axis, default 32 */
+} kdgb_build_params;
+
+typedef struct kdgb_trace_params {
+    int32_t tracer;          /* KDGB_TRACER_* */
+    int32_t leaf_skipping;   /* IRayTracer.cu:33 default 1 */
+    int32_t tie;             /* KDGB_TIE_* */
+    int32_t stack_depth;     /* ShortStack.cu:25 SHORT_STACK_SIZE, 1..8, default 4 */
+    int32_t max_iterations;  /* per-ray restart/pop guard, 0 = unlimited */
+    int32_t block_size;      /* threads per block, 0 = library choice */
+    int32_t tile_width;      /* >0: rays are a row-major image of this width; threads walk
+                                4x8 pixel packets (IRayTracer.h:67-76) */
+} kdgb_trace_params;
+
+/* SoA device arrays of a tree, mirroring the KDNode / TriangleNode getters
+ * (Scene/KDNode.h:85-94, Scene/TriangleNode.h:30-31) and
+ * TriangleMap::GetPrimitiveIndices (TriangleMap.h:79).  For
+ * kdgb_tree_upload the same struct carries HOST pointers. */
+typedef struct kdgb_tree_view {
+    int32_t n_nodes;
+    int32_t n_refs;          /* length of prim_indices */
+    int32_t n_upper_leaves;  /* length of leaf_ids */
+    int32_t n_tris;
+    int8_t  *info;           /* n_nodes */
+    float   *split;          /* n_nodes */
+    float   *aabb_min;       /* n_nodes * 4 (float4, w = 0) */
+    float   *aabb_max;       /* n_nodes * 4 */
+    int32_t *prim_index;     /* n_nodes */
+    int32_t *bitmap;         /* n_nodes (KDNode::amount / bitmap) */
+    int32_t *children;       /* n_nodes * 2 (int2) */
+    float   *area;           /* n_nodes */
+    int32_t *parent;         /* n_nodes */
+    int32_t *prim_indices;   /* n_refs */
+    int32_t *leaf_ids;       /* n_upper_leaves */
+    float   *p0, *p1, *p2;   /* n_tris * 4 each, GeometryList SoA (GeometryList.h:41) */
+} kdgb_tree_view;
+
+typedef struct kdgb_tree kdgb_tree;
+
+typedef struct kdgb_build_stats {
+    int32_t upper_levels;
+    int32_t lower_levels;
+    int32_t n_nodes;
+    int32_t n_refs;
+    int32_t n_leaves;
+    int32_t max_depth;
+    float   build_ms;         /* device time of the last build (CUDA events) */
+} kdgb_build_stats;
+
+KDGB_API int         kdgb_abi_version(void);
+KDGB_API const char *kdgb_status_string(int status);
+KDGB_API const char *kdgb_last_error(void);
+KDGB_API void        kdgb_build_params_default(kdgb_build_params *p);
+KDGB_API void        kdgb_trace_params_default(kdgb_trace_params *p);
+
+/* Replaces TriangleMap::Create (Utils/CUDA/TriangleMap.cu:51-62): builds the
+ * tree over n_tris device triangles.  The handle owns copies of the geometry
+ * and all tree arrays.  Synchronises `stream` once per tree level. */
+KDGB_API int kdgb_build(const float *tri_v_dev, int32_t n_tris, const kdgb_build_params *params,
+               kdgb_tree **out, kdgb_stream_t stream);
+
+/* Rebuilds an existing handle in place (same as TriangleMap::Create called
+ * again each frame, PhotonRenderingView.cpp:45-60), reusing its memory. */
+KDGB_API int kdgb_rebuild(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris,
+                 const kdgb_build_params *params, kdgb_stream_t stream);
+
+/* Creates a handle from tree arrays held in HOST memory (e.g. a tree built
+ * on the CPU) plus host triangles; used to trace an externally built tree. */
+KDGB_API int kdgb_tree_upload(const kdgb_tree_view *host_arrays, const float *tri_v_host, int32_t n_tris,
+                     kdgb_tree **out, kdgb_stream_t stream);
+
+KDGB_API int kdgb_tree_destroy(kdgb_tree *tree);
+
+/* Replaces the KDNode / TriangleNode getters: device SoA pointers, valid
+ * until the next kdgb_rebuild or kdgb_tree_destroy of this handle. */
+KDGB_API int kdgb_tree_view_get(const kdgb_tree *tree, kdgb_tree_view *view);
+
+/* Copies the SoA arrays into caller-owned HOST buffers (the fields of
+ * `host_dst` that are non-NULL; sizes from kdgb_tree_view_get) and waits for
+ * the copy.  Replaces the cudaMemcpy-per-field inspection of
+ * KDNode::ToString / TriangleMap::PrintNode (KDNode.cu:64-119,
+ * TriangleMap.cu:118-162). */
+KDGB_API int kdgb_tree_download(const kdgb_tree *tree, kdgb_tree_view *host_dst);
+
+KDGB_API int kdgb_tree_stats(const kdgb_tree *tree, kdgb_build_stats *stats);
+
+/* Replaces IRayTracer::Trace (IRayTracer.h:47) of RayTracer (Raytracer.cu:295),
+ * ShortStack (ShortStack.cu:231) and BruteTracer (BruteTracer.cu:123): first
+ * hit of n rays; the uchar4 canvas output becomes hit id (-1 = miss), t, u, v.
+ * Misses write t = +inf, u = v = 0. */
+KDGB_API int kdgb_trace(const kdgb_tree *tree, const kdgb_trace_params *params,
+               const float *ray_o_dev, const float *ray_d_dev, int32_t n,
+               int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
+               kdgb_stream_t stream);
+
+/* Replaces RayTracer's ShadowRay (Raytracer.cu:108-163): occluded[i] = 1 when
+ * the segment from `light` (3 host floats) toward point i is blocked. */
+KDGB_API int kdgb_trace_shadow(const kdgb_tree *tree, const kdgb_trace_params *params,
+                      const float *points_dev, int32_t n, const float light[3],
+                      int32_t *occluded_dev, kdgb_stream_t stream);
+
+/* Primary rays followed by one shadow ray per hit toward `light`, fused in
+ * one launch; the shadow origin is p = o + t*d (separately rounded).
+ * occluded is 0 for misses. */
+KDGB_API int kdgb_trace_primary_shadow(const kdgb_tree *tree, const kdgb_trace_params *params,
+                              const float *ray_o_dev, const float *ray_d_dev, int32_t n,
+                              const float light[3],
+                              int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
+                              int32_t *occluded_dev, kdgb_stream_t stream);
+
+/* Replaces BruteTracer::Trace without a tree (BruteTracer.cu:54-96), with
+ * the 4096-triangle cap of BruteTracer.cu:50 lifted. */
+KDGB_API int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie,
+                     const float *ray_o_dev, const float *ray_d_dev, int32_t n,
+                     int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
+                     kdgb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

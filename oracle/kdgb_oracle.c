@@ -1,0 +1,1141 @@
+/*
+ * kdgb_oracle.c -- CPU restatement of the reference kd-tree build and ray
+ * traversal.  TEST INFRASTRUCTURE: the checker for the CUDA library and the
+ * timed CPU baseline; never linked into the product.  Parity unpinned (the
+ * reference does not compile here and ships no golden vectors); every
+ * function cites the reference lines it restates.
+ *
+ * Build: gcc -O3 -ffp-contract=off -fopenmp -fPIC -shared (see Makefile).
+ * -ffp-contract=off keeps every multiply and add separately rounded, the
+ * evaluation order the CUDA kernels use as well.
+ */
+#include "kdgb_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OR_ERR_ARG      (-1)
+#define OR_ERR_ALLOC    (-2)
+#define OR_ERR_LEVELS   (-3)
+#define OR_ERR_SPLIT    (-4)
+#define OR_ERR_NONFINITE (-5)
+
+const char *or_error_string(int code)
+{
+    switch (code) {
+    case 0: return "ok";
+    case OR_ERR_ARG: return "invalid argument";
+    case OR_ERR_ALLOC: return "allocation failed";
+    case OR_ERR_LEVELS: return "upper build exceeded max_levels (degenerate input)";
+    case OR_ERR_SPLIT: return "split produced fewer references than its input";
+    case OR_ERR_NONFINITE: return "non-finite vertex coordinate";
+    default: return "unknown error";
+    }
+}
+
+typedef struct { float x, y, z; } v3;
+typedef struct { float x, y, z, w; } f4;
+
+static inline float i2f(int32_t i) { float f; memcpy(&f, &i, 4); return f; }
+static inline int32_t f2i(float f) { int32_t i; memcpy(&i, &f, 4); return i; }
+
+/* min / max as used by the reference (CUDA fminf/fmaxf on finite data).  Ties
+ * between -0 and +0 are resolved by IEEE totalOrder (-0 < +0) so the result
+ * does not depend on reduction order; the CUDA kernels use the same order. */
+static inline float kmin(float a, float b)
+{
+    if (a < b) return a;
+    if (b < a) return b;
+    return signbit(a) ? a : b;
+}
+static inline float kmax(float a, float b)
+{
+    if (a > b) return a;
+    if (b > a) return b;
+    return signbit(a) ? b : a;
+}
+
+static inline v3 mk3(float x, float y, float z) { v3 r = {x, y, z}; return r; }
+static inline v3 sub3(v3 a, v3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+/* Evaluation order of the un-vendored CUDA-SDK helpers: left to right. */
+static inline float dot3(v3 a, v3 b)
+{
+    float s = a.x * b.x;
+    s = s + a.y * b.y;
+    s = s + a.z * b.z;
+    return s;
+}
+static inline v3 cross3(v3 a, v3 b)
+{
+    return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static inline v3 ld3(const float *p) { return mk3(p[0], p[1], p[2]); }
+
+/* ------------------------------------------------------------------------ */
+/* Intersection primitives                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* IRayTracer.h:60-65 AdjustRayDirection. */
+static inline v3 adjust_dir(v3 d)
+{
+    const float ooeps = 0x1p-80f; /* exp2f(-80.0) */
+    d.x = fabsf(d.x) > ooeps ? d.x : copysignf(ooeps, d.x);
+    d.y = fabsf(d.y) > ooeps ? d.y : copysignf(ooeps, d.y);
+    d.z = fabsf(d.z) > ooeps ? d.z : copysignf(ooeps, d.z);
+    return d;
+}
+
+static inline v3 inv3(v3 d) { return mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z); }
+
+/* IRayTracer.h:111-145 MoellerTrumbore, host branch (IEEE 1.0f/x).  `tie`
+ * selects the reference's `t <= tBest` (last tested wins) or lowest id. */
+static inline void mt_test(const float *tri, int prim, v3 o, v3 d, int tie,
+                           int *prim_hit, float th[3])
+{
+    const float *tp = tri + (size_t)prim * 9;
+    const v3 v0 = ld3(tp), v1 = ld3(tp + 3), v2 = ld3(tp + 6);
+    const v3 e1 = sub3(v1, v0);
+    const v3 e2 = sub3(v2, v0);
+    const v3 p = cross3(d, e2);
+    const v3 t = sub3(o, v0);
+    const v3 q = cross3(t, e1);
+    const float inv_det = 1.0f / dot3(p, e1);
+    const float ht = inv_det * dot3(q, e2);
+    if (0.0f <= ht && ht <= th[0]) {
+        const float hu = inv_det * dot3(p, t);
+        const float hv = inv_det * dot3(q, d);
+        if (hu >= 0.0f && hv >= 0.0f && hu + hv <= 1.0f) {
+            if (tie == OR_TIE_REF_LAST || *prim_hit == -1 || ht < th[0] || prim < *prim_hit) {
+                *prim_hit = prim;
+                th[0] = ht; th[1] = hu; th[2] = hv;
+            }
+        }
+    }
+}
+
+int or_moeller_trumbore(const float v0[3], const float v1[3], const float v2[3],
+                        const float o[3], const float d[3], float t_max, float out[3])
+{
+    float tri[9];
+    memcpy(tri, v0, 12); memcpy(tri + 3, v1, 12); memcpy(tri + 6, v2, 12);
+    float th[3] = {t_max, 0.0f, 0.0f};
+    int hit = -1;
+    mt_test(tri, 0, ld3(o), ld3(d), OR_TIE_REF_LAST, &hit, th);
+    out[0] = th[0]; out[1] = th[1]; out[2] = th[2];
+    return hit == 0;
+}
+
+/* IRayTracer.h:147-168 RayBoxIntersection<true>. */
+static inline int ray_box(v3 o, v3 inv, const float *bmin, const float *bmax)
+{
+    v3 lo = mk3((bmin[0] - o.x) * inv.x, (bmin[1] - o.y) * inv.y, (bmin[2] - o.z) * inv.z);
+    v3 hi = mk3((bmax[0] - o.x) * inv.x, (bmax[1] - o.y) * inv.y, (bmax[2] - o.z) * inv.z);
+    float n = kmin(lo.x, hi.x);
+    n = kmax(n, kmin(lo.y, hi.y));
+    n = kmax(n, kmin(lo.z, hi.z));
+    float f = kmax(hi.x, lo.x);
+    f = kmin(f, kmax(lo.y, hi.y));
+    f = kmin(f, kmax(lo.z, hi.z));
+    return n <= f;
+}
+
+static inline float axis_of(v3 a, int axis)
+{
+    return axis == OR_X ? a.x : (axis == OR_Y ? a.y : a.z);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tracers                                                                   */
+/* ------------------------------------------------------------------------ */
+
+static inline void write_miss(int32_t i, int32_t *hit, float *t, float *u, float *v)
+{
+    hit[i] = -1; t[i] = INFINITY; u[i] = 0.0f; v[i] = 0.0f;
+}
+
+/* Leaf test shared by the kd tracers: bitmap order LSB first (Utils.h:198-204,
+ * Raytracer.cu:199-215). */
+static inline int leaf_test(const or_tree *tr, const float *tri, int node, v3 o, v3 d,
+                            int tie, float th[3])
+{
+    const int pi = tr->prim_index[node];
+    uint32_t bm = (uint32_t)tr->bitmap[node];
+    int prim_hit = -1;
+    while (bm) {
+        const int i = __builtin_ctz(bm);
+        const int prim = tr->prim_indices[pi + i];
+        mt_test(tri, prim, o, d, tie, &prim_hit, th);
+        bm &= bm - 1u;
+    }
+    return prim_hit;
+}
+
+/* Raytracer.cu:57-106 TraceNode<true> + Raytracer.cu:165-262 KDRestart,
+ * stopped at the first leaf that reports a hit (shading left out). */
+static void trace_restart_one(const or_tree *tr, const float *tri, const or_trace_params *p,
+                              v3 o, v3 din, int32_t *hit, float *ot, float *ou, float *ov)
+{
+    const v3 d = adjust_dir(din);
+    const v3 inv = inv3(d);
+    float th[3] = {0.0f, 0.0f, 0.0f};
+    long iters = 0;
+    do {
+        float t_next = OR_FINF;
+        int node = 0;
+        int8_t axis = tr->info[0];
+        while ((axis & 3) != OR_LEAF) {
+            const float sv = tr->split[node];
+            const int l = tr->children[2 * node], r = tr->children[2 * node + 1];
+            const float ori = axis_of(o, axis), dir = axis_of(inv, axis);
+            const float t_split = (sv - ori) * dir;
+            if (th[0] < t_split) {
+                node = 0 < dir ? l : r;
+                t_next = kmin(t_split, t_next);
+            } else {
+                node = 0 < dir ? r : l;
+            }
+            axis = tr->info[node];
+        }
+        th[0] = t_next * 1.00001f;
+        if (!p->leaf_skipping || ray_box(o, inv, tr->aabb_min + 4 * (size_t)node,
+                                          tr->aabb_max + 4 * (size_t)node)) {
+            const int h = leaf_test(tr, tri, node, o, d, p->tie, th);
+            if (h != -1) { *hit = h; *ot = th[0]; *ou = th[1]; *ov = th[2]; return; }
+        }
+        if (p->max_iterations > 0 && ++iters >= p->max_iterations) break;
+    } while (th[0] < OR_FINF);
+    *hit = -1; *ot = INFINITY; *ou = 0.0f; *ov = 0.0f;
+}
+
+/* ShortStack.h:27-98 ring buffer; ShortStack.cu:58-194 TraceNode and
+ * ShortStackTrace, first hit.  The direction is inverted in place before the
+ * descent and re-inverted after it, every outer iteration (ShortStack.cu:134,148). */
+static void trace_shortstack_one(const or_tree *tr, const float *tri, const or_trace_params *p,
+                                 v3 o, v3 din, int32_t *hit, float *ot, float *ou, float *ov)
+{
+    enum { MAXN = 64 };
+    int sn[MAXN]; float st[MAXN];
+    const int N = p->stack_depth;
+    int nxt = 0, cnt = 0;
+    v3 d = adjust_dir(din);
+    float th[3] = {0.0f, 0.0f, 0.0f};
+    long iters = 0;
+    do {
+        int node; float t_next;
+        if (cnt == 0) {
+            node = 0; t_next = OR_FINF;
+        } else {
+            nxt = (nxt == 0 ? N : nxt) - 1;
+            cnt--;
+            node = sn[nxt]; t_next = st[nxt];
+        }
+        int8_t info = tr->info[node];
+        d = inv3(d);
+        while ((info & 3) != OR_LEAF) {
+            const float sv = tr->split[node];
+            const int l = tr->children[2 * node], r = tr->children[2 * node + 1];
+            const int axis = info & 3;
+            const float ori = axis_of(o, axis), dir = axis_of(d, axis);
+            const float t_split = (sv - ori) * dir;
+            const int lower = 0 < dir ? l : r;
+            const int upper = 0 < dir ? r : l;
+            if (th[0] < t_split) {
+                node = lower;
+                if (t_split < t_next) {
+                    sn[nxt] = upper; st[nxt] = t_next;
+                    nxt = nxt == N - 1 ? 0 : nxt + 1;
+                    cnt = cnt == N ? N : cnt + 1;
+                }
+                t_next = kmin(t_split, t_next);
+            } else {
+                node = upper;
+            }
+            info = tr->info[node];
+        }
+        d = inv3(d);
+        th[0] = t_next * 1.00001f;
+        if (!p->leaf_skipping || ray_box(o, inv3(d), tr->aabb_min + 4 * (size_t)node,
+                                          tr->aabb_max + 4 * (size_t)node)) {
+            const int h = leaf_test(tr, tri, node, o, d, p->tie, th);
+            if (h != -1) { *hit = h; *ot = th[0]; *ou = th[1]; *ov = th[2]; return; }
+        }
+        if (p->max_iterations > 0 && ++iters >= p->max_iterations) break;
+    } while (th[0] < OR_FINF);
+    *hit = -1; *ot = INFINITY; *ou = 0.0f; *ov = 0.0f;
+}
+
+/* BruteTracer.cu:54-96 Exhaustive (first hit, no direction clamp, the
+ * 4096-triangle cap of BruteTracer.cu:50 lifted). */
+static void trace_brute_one(const float *tri, int32_t T, int tie, v3 o, v3 d,
+                            int32_t *hit, float *ot, float *ou, float *ov)
+{
+    float th[3] = {OR_FINF, 0.0f, 0.0f};
+    int prim_hit = -1;
+    for (int prim = 0; prim < T; ++prim) mt_test(tri, prim, o, d, tie, &prim_hit, th);
+    if (th[0] < OR_FINF) { *hit = prim_hit; *ot = th[0]; *ou = th[1]; *ov = th[2]; }
+    else { *hit = -1; *ot = INFINITY; *ou = 0.0f; *ov = 0.0f; }
+}
+
+static int set_threads(int32_t threads)
+{
+#ifdef _OPENMP
+    return threads > 0 ? threads : omp_get_max_threads();
+#else
+    (void)threads;
+    return 1;
+#endif
+}
+
+int or_trace(const or_tree *tr, const float *tri, int32_t T, const or_trace_params *p,
+             const float *ray_o, const float *ray_d, int32_t n,
+             int32_t *hit, float *t, float *u, float *v, int32_t threads)
+{
+    if (!p || n < 0 || (n > 0 && (!ray_o || !ray_d || !hit || !t || !u || !v))) return OR_ERR_ARG;
+    if (p->tracer == OR_TRACER_BRUTE)
+        return or_trace_brute(tri, T, p->tie, ray_o, ray_d, n, hit, t, u, v, threads);
+    if (!tr || tr->n_nodes <= 0) return OR_ERR_ARG;
+    if (p->tracer == OR_TRACER_SHORTSTACK && (p->stack_depth < 1 || p->stack_depth > 64)) return OR_ERR_ARG;
+    const int nt = set_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(static, 64) num_threads(nt)
+    for (int32_t i = 0; i < n; ++i) {
+        const v3 o = ld3(ray_o + 3 * (size_t)i), d = ld3(ray_d + 3 * (size_t)i);
+        if (p->tracer == OR_TRACER_SHORTSTACK)
+            trace_shortstack_one(tr, tri, p, o, d, hit + i, t + i, u + i, v + i);
+        else
+            trace_restart_one(tr, tri, p, o, d, hit + i, t + i, u + i, v + i);
+    }
+    return 0;
+}
+
+int or_trace_brute(const float *tri, int32_t T, int32_t tie,
+                   const float *ray_o, const float *ray_d, int32_t n,
+                   int32_t *hit, float *t, float *u, float *v, int32_t threads)
+{
+    if (n < 0 || T < 0) return OR_ERR_ARG;
+    const int nt = set_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(static, 64) num_threads(nt)
+    for (int32_t i = 0; i < n; ++i) {
+        const v3 o = ld3(ray_o + 3 * (size_t)i), d = ld3(ray_d + 3 * (size_t)i);
+        trace_brute_one(tri, T, tie, o, d, hit + i, t + i, u + i, v + i);
+    }
+    return 0;
+}
+
+/* The same Moeller-Trumbore in double precision (an accuracy reference for
+ * the fp32 results, not a restatement of reference arithmetic). */
+int or_trace_brute_f64(const float *tri, int32_t T,
+                       const float *ray_o, const float *ray_d, int32_t n,
+                       int32_t *hit, double *t, double *u, double *v, int32_t threads)
+{
+    if (n < 0 || T < 0) return OR_ERR_ARG;
+    const int nt = set_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(static, 64) num_threads(nt)
+    for (int32_t i = 0; i < n; ++i) {
+        const double ox = ray_o[3 * (size_t)i], oy = ray_o[3 * (size_t)i + 1], oz = ray_o[3 * (size_t)i + 2];
+        const double dx = ray_d[3 * (size_t)i], dy = ray_d[3 * (size_t)i + 1], dz = ray_d[3 * (size_t)i + 2];
+        double best = (double)OR_FINF, bu = 0.0, bv = 0.0;
+        int bh = -1;
+        for (int prim = 0; prim < T; ++prim) {
+            const float *tp = tri + (size_t)prim * 9;
+            const double e1x = (double)tp[3] - tp[0], e1y = (double)tp[4] - tp[1], e1z = (double)tp[5] - tp[2];
+            const double e2x = (double)tp[6] - tp[0], e2y = (double)tp[7] - tp[1], e2z = (double)tp[8] - tp[2];
+            const double px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+            const double sx = ox - tp[0], sy = oy - tp[1], sz = oz - tp[2];
+            const double qx = sy * e1z - sz * e1y, qy = sz * e1x - sx * e1z, qz = sx * e1y - sy * e1x;
+            const double det = px * e1x + py * e1y + pz * e1z;
+            if (det == 0.0) continue;
+            const double inv = 1.0 / det;
+            const double tt = inv * (qx * e2x + qy * e2y + qz * e2z);
+            if (!(0.0 <= tt && tt <= best)) continue;
+            const double uu = inv * (px * sx + py * sy + pz * sz);
+            const double vv = inv * (qx * dx + qy * dy + qz * dz);
+            if (uu >= 0.0 && vv >= 0.0 && uu + vv <= 1.0) {
+                if (bh == -1 || tt < best) { bh = prim; best = tt; bu = uu; bv = vv; }
+            }
+        }
+        if (bh != -1 && best < (double)OR_FINF) { hit[i] = bh; t[i] = best; u[i] = bu; v[i] = bv; }
+        else { hit[i] = -1; t[i] = INFINITY; u[i] = 0.0; v[i] = 0.0; }
+    }
+    return 0;
+}
+
+/* Raytracer.cu:108-163 ShadowRay<false,true>: a ray from the light toward the
+ * point (direction = point - light, not normalised, not clamped); the leaf is
+ * skipped once its exit t reaches 0.999; any hit means shadow. */
+int or_trace_shadow(const or_tree *tr, const float *tri, int32_t T,
+                    const float *points, int32_t n, const float light[3],
+                    int32_t *occluded, int32_t threads)
+{
+    (void)T;
+    if (!tr || tr->n_nodes <= 0 || n < 0) return OR_ERR_ARG;
+    const int nt = set_threads(threads);
+    (void)nt;
+    const v3 lp = ld3(light);
+#pragma omp parallel for schedule(static, 64) num_threads(nt)
+    for (int32_t i = 0; i < n; ++i) {
+        const v3 pt = ld3(points + 3 * (size_t)i);
+        const v3 d = sub3(pt, lp);
+        const v3 inv = inv3(d);
+        float t_min = 0.0f;
+        int occ = 0;
+        do {
+            float t_next = OR_FINF;
+            int node = 0;
+            int8_t axis = tr->info[0];
+            while ((axis & 3) != OR_LEAF) {
+                const float sv = tr->split[node];
+                const int l = tr->children[2 * node], r = tr->children[2 * node + 1];
+                const float ori = axis_of(lp, axis), dir = axis_of(inv, axis);
+                const float t_split = (sv - ori) * dir;
+                if (t_min < t_split) {
+                    node = 0 < dir ? l : r;
+                    t_next = kmin(t_split, t_next);
+                } else {
+                    node = 0 < dir ? r : l;
+                }
+                axis = tr->info[node];
+            }
+            t_min = t_next * 1.00001f;
+            if (t_min >= 0.999f) break;
+            float th[3] = {t_min, 0.0f, 0.0f};
+            if (leaf_test(tr, tri, node, lp, d, OR_TIE_REF_LAST, th) != -1) { occ = 1; break; }
+        } while (t_min < 0.999f);
+        occluded[i] = occ;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Build                                                                     */
+/* ------------------------------------------------------------------------ */
+
+void or_build_params_default(or_build_params *p)
+{
+    p->lower = OR_LOWER_BITMAP;
+    p->split_empty_space = 1;
+    p->propagate_aabbs = 1;
+    p->empty_space_threshold = 0.35f;
+    p->traversal_cost = 24.0f;
+    p->intersection_cost = 1.0f;
+    p->min_leaf = 0;
+    p->esc_zmax_as_x = 1;
+    p->max_levels = 64;
+    p->leaf_size = 32;
+}
+
+void or_trace_params_default(or_trace_params *p)
+{
+    p->tracer = OR_TRACER_RESTART;
+    p->leaf_skipping = 1;
+    p->tie = OR_TIE_LOWEST_ID;
+    p->stack_depth = 4;
+    p->max_iterations = 0;
+}
+
+void or_geometry_from_tris(const float *tri, int32_t T, float *p0, float *p1, float *p2)
+{
+    for (int32_t i = 0; i < T; ++i)
+        for (int k = 0; k < 3; ++k) {
+            float *dst = k == 0 ? p0 : (k == 1 ? p1 : p2);
+            dst[4 * (size_t)i + 0] = tri[9 * (size_t)i + 3 * k + 0];
+            dst[4 * (size_t)i + 1] = tri[9 * (size_t)i + 3 * k + 1];
+            dst[4 * (size_t)i + 2] = tri[9 * (size_t)i + 3 * k + 2];
+            dst[4 * (size_t)i + 3] = 1.0f;
+        }
+}
+
+/* Growable node store (TriangleNode SoA).  New nodes are zero-filled; the
+ * reference leaves fields it never writes (leaf splitPos/children, the boxes
+ * of empty-space chain nodes, ...) uninitialised, which this restatement
+ * defines as zero. */
+typedef struct nodes {
+    int32_t n, cap;
+    int8_t *info; float *split; f4 *bmin; f4 *bmax;
+    int32_t *pidx; int32_t *amt; int32_t *ch; float *area; int32_t *parent;
+} nodes;
+
+static void *grow(void *p, size_t old_elems, size_t new_elems, size_t esz)
+{
+    void *q = realloc(p, new_elems * esz);
+    if (!q) return NULL;
+    memset((char *)q + old_elems * esz, 0, (new_elems - old_elems) * esz);
+    return q;
+}
+
+static int nodes_resize(nodes *s, int32_t n)
+{
+    if (n > s->cap) {
+        int32_t nc = s->cap ? s->cap : 64;
+        while (nc < n) nc *= 2;
+#define G(f, T_, k) do { void *q = grow(s->f, (size_t)s->cap * (k), (size_t)nc * (k), sizeof(T_)); if (!q) return OR_ERR_ALLOC; s->f = q; } while (0)
+        G(info, int8_t, 1); G(split, float, 1); G(bmin, f4, 1); G(bmax, f4, 1);
+        G(pidx, int32_t, 1); G(amt, int32_t, 1); G(ch, int32_t, 2); G(area, float, 1); G(parent, int32_t, 1);
+#undef G
+        s->cap = nc;
+    }
+    s->n = n;
+    return 0;
+}
+
+static void nodes_free(nodes *s)
+{
+    free(s->info); free(s->split); free(s->bmin); free(s->bmax); free(s->pidx);
+    free(s->amt); free(s->ch); free(s->area); free(s->parent);
+    memset(s, 0, sizeof(*s));
+}
+
+static inline float f4c(f4 a, int axis) { return axis == OR_X ? a.x : (axis == OR_Y ? a.y : a.z); }
+
+typedef struct ivec { int32_t *a; size_t n, cap; } ivec;
+static int ivec_push(ivec *v, int32_t x)
+{
+    if (v->n == v->cap) {
+        size_t nc = v->cap ? v->cap * 2 : 256;
+        int32_t *q = realloc(v->a, nc * sizeof(int32_t));
+        if (!q) return OR_ERR_ALLOC;
+        v->a = q; v->cap = nc;
+    }
+    v->a[v->n++] = x;
+    return 0;
+}
+
+/* Exclusive scan of in[0..n) into out[0..n]; out[n] = total. */
+static void excl_scan(const int32_t *in, int64_t n, int32_t *out)
+{
+    int32_t s = 0;
+    for (int64_t i = 0; i < n; ++i) { out[i] = s; s += in[i]; }
+    out[n] = s;
+}
+
+/*
+ * Upper ("large node") phase: TriangleMapUpperCreator.cu:110-183 (Create),
+ * :185-205 (ProcessNodes), :241-318 (ReduceAabb), :320-368 (CreateEmptySplits),
+ * :467-759 (CreateChildren, BOX method); kernels TriangleUpper.h:10-52,
+ * ReduceSegments.h:230-371,466-484, EmptySpaceSplitting.h:10-184,299-368,
+ * TriangleUpperChildren.h:10-62,144-395.  The 256-reference segments of the
+ * reference only schedule its reduction; the tight box of a node is the
+ * exact min/max over its references, which is what is computed here.
+ */
+static int build_upper(const float *tri, int32_t T, const or_build_params *p, nodes *nd,
+                       f4 **fmin_out, f4 **fmax_out, int32_t *nfinal_out, ivec *leaf_ids,
+                       int32_t *levels_out)
+{
+    const int LS = p->leaf_size;
+    int rc = 0;
+    f4 *cmin = NULL, *cmax = NULL, *nmin = NULL, *nmax = NULL, *fmin = NULL, *fmax = NULL;
+    f4 *pmin = NULL, *pmax = NULL;
+    int32_t *side = NULL, *saddr = NULL, *lside = NULL, *laddr = NULL, *owner = NULL;
+    int32_t *csize = NULL, *lnode = NULL, *lnaddr = NULL, *req = NULL, *eaddr = NULL;
+    int8_t *planes = NULL;
+    int32_t nfinal = 0, ncap_final = 0;
+
+    /* Root node (TriangleMapUpperCreator.cu:128-136). */
+    if ((rc = nodes_resize(nd, 1))) goto out;
+    nd->pidx[0] = 0; nd->amt[0] = T; nd->parent[0] = 0;
+    memset(&nd->bmin[0], 0, sizeof(f4)); memset(&nd->bmax[0], 0, sizeof(f4));
+
+    /* CalcPrimitiveAabb (TriangleUpper.h:10-28). */
+    int64_t N = T;
+    cmin = malloc(sizeof(f4) * (size_t)(N > 0 ? N : 1));
+    cmax = malloc(sizeof(f4) * (size_t)(N > 0 ? N : 1));
+    if (!cmin || !cmax) { rc = OR_ERR_ALLOC; goto out; }
+    for (int32_t i = 0; i < T; ++i) {
+        const float *tp = tri + 9 * (size_t)i;
+        for (int k = 0; k < 9; ++k) if (!isfinite(tp[k])) { rc = OR_ERR_NONFINITE; goto out; }
+        float mnx = tp[0], mny = tp[1], mnz = tp[2], mxx = tp[0], mxy = tp[1], mxz = tp[2];
+        mnx = kmin(mnx, tp[3]); mny = kmin(mny, tp[4]); mnz = kmin(mnz, tp[5]);
+        mxx = kmax(mxx, tp[3]); mxy = kmax(mxy, tp[4]); mxz = kmax(mxz, tp[5]);
+        f4 a = {kmin(mnx, tp[6]), kmin(mny, tp[7]), kmin(mnz, tp[8]), i2f(i)};
+        f4 b = {kmax(mxx, tp[6]), kmax(mxy, tp[7]), kmax(mxz, tp[8]), 0.0f};
+        cmin[i] = a; cmax[i] = b;
+    }
+
+    int32_t active = 0, R = 1, level = 0;
+    while (R > 0) {
+        if (level >= p->max_levels) { rc = OR_ERR_LEVELS; goto out; }
+        ++level;
+
+        /* ReduceAabb (TriangleMapUpperCreator.cu:241-318). */
+        free(pmin); free(pmax);
+        pmin = malloc(sizeof(f4) * (size_t)R); pmax = malloc(sizeof(f4) * (size_t)R);
+        if (!pmin || !pmax) { rc = OR_ERR_ALLOC; goto out; }
+        for (int32_t k = 0; k < R; ++k) { pmin[k] = nd->bmin[active + k]; pmax[k] = nd->bmax[active + k]; }
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int32_t k = 0; k < R; ++k) {
+            const int32_t s = nd->pidx[active + k], a = nd->amt[active + k];
+            float x0 = OR_FINF, y0 = OR_FINF, z0 = OR_FINF, x1 = -OR_FINF, y1 = -OR_FINF, z1 = -OR_FINF;
+            for (int32_t r = s; r < s + a; ++r) {
+                x0 = kmin(x0, cmin[r].x); y0 = kmin(y0, cmin[r].y); z0 = kmin(z0, cmin[r].z);
+                x1 = kmax(x1, cmax[r].x); y1 = kmax(y1, cmax[r].y); z1 = kmax(z1, cmax[r].z);
+            }
+            f4 a0 = {x0, y0, z0, 0.0f}, a1 = {x1, y1, z1, 0.0f};
+            nd->bmin[active + k] = a0; nd->bmax[active + k] = a1;
+        }
+
+        /* CreateEmptySplits, not at the root (TriangleMapUpperCreator.cu:302-303,
+         * EmptySpaceSplitting.h:10-184). */
+        if (p->split_empty_space && active != 0) {
+            free(planes); free(req); free(eaddr);
+            planes = calloc((size_t)R, 1); req = calloc((size_t)R, sizeof(int32_t));
+            eaddr = calloc((size_t)R + 1, sizeof(int32_t));
+            if (!planes || !req || !eaddr) { rc = OR_ERR_ALLOC; goto out; }
+            const float thr = p->empty_space_threshold;
+            int any = 0;
+            for (int32_t k = 0; k < R; ++k) {
+                const f4 a = pmin[k], b = pmax[k];
+                const f4 rmn = nd->bmin[active + k], rmx = nd->bmax[active + k];
+                int pl = 0, nr = 0;
+                if (rmn.x - a.x > thr * (b.x - a.x)) { pl |= 1; nr += 2; }
+                if (rmn.y - a.y > thr * (b.y - a.y)) { pl |= 2; nr += 2; }
+                if (rmn.z - a.z > thr * (b.z - a.z)) { pl |= 4; nr += 2; }
+                if (b.x - rmx.x > thr * (b.x - a.x)) { pl |= 8; nr += 2; }
+                if (b.y - rmx.y > thr * (b.y - a.y)) { pl |= 16; nr += 2; }
+                if (b.z - rmx.z > thr * (b.z - a.z)) { pl |= 32; nr += 2; }
+                planes[k] = (int8_t)pl; req[k] = nr;
+                if (pl) any = 1;
+            }
+            if (any) {
+                excl_scan(req, R, eaddr);
+                const int32_t empty_nodes = eaddr[R];
+                const int32_t base = nd->n;
+                if ((rc = nodes_resize(nd, nd->n + empty_nodes))) goto out;
+                for (int32_t k = 0; k < R; ++k) {
+                    int pl = planes[k];
+                    if (pl == 0) continue;
+                    const int32_t leaf = active + k;
+                    int32_t par = nd->parent[leaf];
+                    const int32_t start = base + eaddr[k];
+                    if (nd->ch[2 * par] == leaf) nd->ch[2 * par] = start;
+                    else nd->ch[2 * par + 1] = start;
+                    const f4 mn = nd->bmin[leaf], mx = nd->bmax[leaf];
+                    par = start;
+                    static const int8_t lo_axis[3] = {OR_X, OR_Y, OR_Z};
+                    for (int b = 0; b < 3; ++b) {
+                        if (pl & (1 << b)) {
+                            pl -= (1 << b);
+                            nd->info[par] = lo_axis[b];
+                            nd->split[par] = f4c(mn, lo_axis[b]);
+                            const int32_t l = par + 1, r = pl ? l + 1 : leaf;
+                            nd->ch[2 * par] = l; nd->ch[2 * par + 1] = r;
+                            nd->info[l] = OR_LEAF; nd->amt[l] = 0;
+                            par = r;
+                        }
+                    }
+                    for (int b = 3; b < 5; ++b) {
+                        if (pl & (1 << b)) {
+                            pl -= (1 << b);
+                            nd->info[par] = lo_axis[b - 3];
+                            nd->split[par] = f4c(mx, lo_axis[b - 3]);
+                            const int32_t r = par + 1, l = pl ? r + 1 : leaf;
+                            nd->ch[2 * par] = l; nd->ch[2 * par + 1] = r;
+                            nd->info[r] = OR_LEAF; nd->amt[r] = 0;
+                            par = l;
+                        }
+                    }
+                    if (pl & 32) {
+                        /* EmptySpaceSplitting.h:172-181 cuts the max-z face on x at
+                         * maxPlane.x; esc_zmax_as_x = 0 uses z and maxPlane.z. */
+                        nd->info[par] = p->esc_zmax_as_x ? OR_X : OR_Z;
+                        nd->split[par] = p->esc_zmax_as_x ? mx.x : mx.z;
+                        const int32_t r = par + 1, l = leaf;
+                        nd->ch[2 * par] = l; nd->ch[2 * par + 1] = r;
+                        nd->info[r] = OR_LEAF; nd->amt[r] = 0;
+                    }
+                }
+            }
+        }
+
+        /* CalcUpperNodeSplitInfo (ReduceSegments.h:466-484). */
+        for (int32_t k = 0; k < R; ++k) {
+            const f4 mn = nd->bmin[active + k], mx = nd->bmax[active + k];
+            const float sx = mx.x - mn.x, sy = mx.y - mn.y, sz = mx.z - mn.z;
+            const float mdx = sx * 0.5f + mn.x, mdy = sy * 0.5f + mn.y, mdz = sz * 0.5f + mn.z;
+            const int y_above_x = sx < sy;
+            const float mxs = y_above_x ? sy : sx;
+            const float sp = y_above_x ? mdy : mdx;
+            const int8_t ax = y_above_x ? OR_Y : OR_X;
+            const int z_higher = mxs < sz;
+            nd->split[active + k] = z_higher ? mdz : sp;
+            nd->info[active + k] = z_higher ? OR_Z : ax;
+        }
+
+        /* CreateChildren (TriangleMapUpperCreator.cu:467-759). */
+        const int32_t child_start = nd->n;
+        if ((rc = nodes_resize(nd, nd->n + 2 * R))) goto out;
+        free(side); free(saddr); free(owner); free(csize);
+        side = malloc(sizeof(int32_t) * (size_t)(2 * N + 1));
+        saddr = malloc(sizeof(int32_t) * (size_t)(2 * N + 2));
+        owner = malloc(sizeof(int32_t) * (size_t)(N > 0 ? N : 1));
+        csize = malloc(sizeof(int32_t) * (size_t)(2 * R));
+        if (!side || !saddr || !owner || !csize) { rc = OR_ERR_ALLOC; goto out; }
+        for (int32_t k = 0; k < R; ++k) {
+            const int32_t s = nd->pidx[active + k], a = nd->amt[active + k];
+            for (int32_t r = s; r < s + a; ++r) owner[r] = k;
+        }
+        /* SetSplitSide (TriangleUpperChildren.h:10-62). */
+#pragma omp parallel for schedule(static)
+        for (int64_t r = 0; r < N; ++r) {
+            const int32_t node = active + owner[r];
+            const int axis = nd->info[node];
+            const float sp = nd->split[node];
+            side[r] = f4c(cmin[r], axis) <= sp;
+            side[N + r] = sp < f4c(cmax[r], axis);
+        }
+        side[2 * N] = 0;
+        excl_scan(side, 2 * N, saddr);
+        int64_t new_tris = saddr[2 * N];
+        if (new_tris < N) { rc = OR_ERR_SPLIT; goto out; }
+
+        /* CalcNodeChildSize (TriangleUpperChildren.h:144-162). */
+        int created_leafs = 0;
+        for (int32_t k = 0; k < R; ++k) {
+            const int32_t s = nd->pidx[active + k], a = nd->amt[active + k];
+            csize[2 * k] = saddr[s + a] - saddr[s];
+            csize[2 * k + 1] = saddr[s + a + N] - saddr[s + N];
+            if (csize[2 * k] < LS || csize[2 * k + 1] < LS) created_leafs = 1;
+        }
+
+        int32_t children_created;
+        if (created_leafs) {
+            free(lside); free(laddr);
+            lside = malloc(sizeof(int32_t) * (size_t)(2 * N + 1));
+            laddr = malloc(sizeof(int32_t) * (size_t)(2 * N + 2));
+            if (!lside || !laddr) { rc = OR_ERR_ALLOC; goto out; }
+            /* SetPrimitiveLeafSide (TriangleUpperChildren.h:164-186). */
+            for (int64_t r = 0; r < N; ++r) {
+                const int32_t k = owner[r];
+                lside[r] = (csize[2 * k] < LS) * side[r];
+                lside[N + r] = (csize[2 * k + 1] < LS) * side[N + r];
+            }
+            excl_scan(lside, 2 * N, laddr);
+            const int32_t leaf_tris = laddr[2 * N];
+            new_tris -= leaf_tris;
+            const int32_t upper = nfinal;
+            if (nfinal + leaf_tris > ncap_final) {
+                int32_t nc = ncap_final ? ncap_final : 1024;
+                while (nc < nfinal + leaf_tris) nc *= 2;
+                f4 *a = realloc(fmin, sizeof(f4) * (size_t)nc), *b;
+                if (!a) { rc = OR_ERR_ALLOC; goto out; }
+                fmin = a;
+                b = realloc(fmax, sizeof(f4) * (size_t)nc);
+                if (!b) { rc = OR_ERR_ALLOC; goto out; }
+                fmax = b;
+                ncap_final = nc;
+            }
+            nfinal += leaf_tris;
+            free(nmin); free(nmax);
+            nmin = malloc(sizeof(f4) * (size_t)(new_tris > 0 ? new_tris : 1));
+            nmax = malloc(sizeof(f4) * (size_t)(new_tris > 0 ? new_tris : 1));
+            if (!nmin || !nmax) { rc = OR_ERR_ALLOC; goto out; }
+            /* SplitTriangles, leaf variant (TriangleUpperChildren.h:329-383). */
+#pragma omp parallel for schedule(static)
+            for (int64_t r = 0; r < N; ++r) {
+                const int32_t node = active + owner[r];
+                const int axis = nd->info[node];
+                const float sp = nd->split[node];
+                const f4 a = cmin[r], b = cmax[r];
+                if (side[r] == 1) {
+                    f4 hi = {axis == OR_X ? kmin(sp, b.x) : b.x, axis == OR_Y ? kmin(sp, b.y) : b.y,
+                             axis == OR_Z ? kmin(sp, b.z) : b.z, b.w};
+                    if (lside[r]) { fmin[upper + laddr[r]] = a; fmax[upper + laddr[r]] = hi; }
+                    else { nmin[saddr[r] - laddr[r]] = a; nmax[saddr[r] - laddr[r]] = hi; }
+                }
+                const int64_t rr = r + N;
+                if (side[rr] == 1) {
+                    f4 lo = {axis == OR_X ? kmax(sp, a.x) : a.x, axis == OR_Y ? kmax(sp, a.y) : a.y,
+                             axis == OR_Z ? kmax(sp, a.z) : a.z, a.w};
+                    if (lside[rr]) { fmin[upper + laddr[rr]] = lo; fmax[upper + laddr[rr]] = b; }
+                    else { nmin[saddr[rr] - laddr[rr]] = lo; nmax[saddr[rr] - laddr[rr]] = b; }
+                }
+            }
+            /* MarkNodeLeafs + scan (TriangleUpperChildren.h:190-201,
+             * TriangleMapUpperCreator.cu:658-668). */
+            free(lnode); free(lnaddr);
+            lnode = malloc(sizeof(int32_t) * (size_t)(2 * R));
+            lnaddr = malloc(sizeof(int32_t) * (size_t)(2 * R + 1));
+            if (!lnode || !lnaddr) { rc = OR_ERR_ALLOC; goto out; }
+            for (int32_t k = 0; k < R; ++k) {
+                lnode[k] = csize[2 * k] < LS;
+                lnode[R + k] = csize[2 * k + 1] < LS;
+            }
+            excl_scan(lnode, 2 * R, lnaddr);
+            const int32_t leaf_nodes = lnaddr[2 * R];
+            /* CreateUpperChildren, leaf variant (TriangleUpperChildren.h:236-281). */
+            for (int32_t k = 0; k < R; ++k) {
+                const int32_t par = active + k;
+                const int32_t pi = nd->pidx[par];
+                int leaf = csize[2 * k] < LS;
+                int32_t la = lnaddr[k];
+                const int32_t lid = (leaf ? la : k - la + leaf_nodes) + child_start;
+                nd->pidx[lid] = leaf ? laddr[pi] + upper : saddr[pi] - laddr[pi];
+                nd->amt[lid] = csize[2 * k];
+                nd->parent[lid] = par;
+                const int32_t kk = k + R;
+                leaf = csize[2 * k + 1] < LS;
+                la = lnaddr[kk];
+                const int32_t rid = (leaf ? la : kk - la + leaf_nodes) + child_start;
+                nd->pidx[rid] = leaf ? laddr[pi + N] + upper : saddr[pi + N] - laddr[pi + N];
+                nd->amt[rid] = csize[2 * k + 1];
+                nd->parent[rid] = par;
+                nd->ch[2 * par] = lid; nd->ch[2 * par + 1] = rid;
+            }
+            children_created = 2 * R - leaf_nodes;
+            /* MarkLeafNodes (TriangleUpperChildren.h:385-395). */
+            for (int32_t i = 0; i < leaf_nodes; ++i)
+                if ((rc = ivec_push(leaf_ids, child_start + i))) goto out;
+        } else {
+            free(nmin); free(nmax);
+            nmin = malloc(sizeof(f4) * (size_t)(new_tris > 0 ? new_tris : 1));
+            nmax = malloc(sizeof(f4) * (size_t)(new_tris > 0 ? new_tris : 1));
+            if (!nmin || !nmax) { rc = OR_ERR_ALLOC; goto out; }
+            /* CreateUpperChildren (TriangleUpperChildren.h:203-234). */
+            for (int32_t k = 0; k < R; ++k) {
+                const int32_t par = active + k;
+                const int32_t lid = child_start + k, rid = lid + R;
+                const int32_t pi = nd->pidx[par];
+                nd->pidx[lid] = saddr[pi];
+                nd->pidx[rid] = saddr[pi + N];
+                nd->amt[lid] = csize[2 * k];
+                nd->amt[rid] = csize[2 * k + 1];
+                nd->ch[2 * par] = lid; nd->ch[2 * par + 1] = rid;
+                nd->parent[lid] = par; nd->parent[rid] = par;
+            }
+            /* SplitTriangles (TriangleUpperChildren.h:283-327). */
+#pragma omp parallel for schedule(static)
+            for (int64_t r = 0; r < N; ++r) {
+                const int32_t node = active + owner[r];
+                const int axis = nd->info[node];
+                const float sp = nd->split[node];
+                const f4 a = cmin[r], b = cmax[r];
+                if (side[r] == 1) {
+                    f4 hi = {axis == OR_X ? kmin(sp, b.x) : b.x, axis == OR_Y ? kmin(sp, b.y) : b.y,
+                             axis == OR_Z ? kmin(sp, b.z) : b.z, b.w};
+                    nmin[saddr[r]] = a; nmax[saddr[r]] = hi;
+                }
+                if (side[r + N] == 1) {
+                    f4 lo = {axis == OR_X ? kmax(sp, a.x) : a.x, axis == OR_Y ? kmax(sp, a.y) : a.y,
+                             axis == OR_Z ? kmax(sp, a.z) : a.z, a.w};
+                    nmin[saddr[r + N]] = lo; nmax[saddr[r + N]] = b;
+                }
+            }
+            children_created = 2 * R;
+        }
+
+        /* PropagateAabbToChildren<false> (EmptySpaceSplitting.h:299-331). */
+        if (p->split_empty_space) {
+            for (int32_t k = 0; k < R; ++k) {
+                const int32_t par = active + k;
+                const int axis = nd->info[par] & 3;
+                const float sp = nd->split[par];
+                const int32_t l = nd->ch[2 * par], r = nd->ch[2 * par + 1];
+                const f4 mn = nd->bmin[par], mx = nd->bmax[par];
+                f4 rmn = {axis == OR_X ? sp : mn.x, axis == OR_Y ? sp : mn.y, axis == OR_Z ? sp : mn.z, 0.0f};
+                f4 lmx = {axis == OR_X ? sp : mx.x, axis == OR_Y ? sp : mx.y, axis == OR_Z ? sp : mx.z, 0.0f};
+                nd->bmin[l] = mn; nd->bmin[r] = rmn;
+                nd->bmax[l] = lmx; nd->bmax[r] = mx;
+            }
+        }
+
+        f4 *t0 = cmin, *t1 = cmax;
+        cmin = nmin; cmax = nmax; nmin = t0; nmax = t1;
+        N = new_tris;
+        active = nd->n - children_created;
+        R = children_created;
+    }
+
+    /* PropagateParentAabb<true> when empty-space splitting is off
+     * (TriangleMapUpperCreator.cu:171-182, EmptySpaceSplitting.h:333-368). */
+    if (!p->split_empty_space && p->propagate_aabbs) {
+        for (size_t i = 0; i < leaf_ids->n; ++i) {
+            const int32_t c = leaf_ids->a[i];
+            const int32_t par = nd->parent[c];
+            const f4 mn = nd->bmin[par], mx = nd->bmax[par];
+            const int axis = nd->info[par] & 3;
+            const float sp = nd->split[par];
+            if (nd->ch[2 * par] == c) {
+                f4 a = {mn.x, mn.y, mn.z, 0.0f};
+                f4 b = {axis == OR_X ? sp : mx.x, axis == OR_Y ? sp : mx.y, axis == OR_Z ? sp : mx.z, 0.0f};
+                nd->bmin[c] = a; nd->bmax[c] = b;
+            } else {
+                f4 a = {axis == OR_X ? sp : mn.x, axis == OR_Y ? sp : mn.y, axis == OR_Z ? sp : mn.z, 0.0f};
+                f4 b = {mx.x, mx.y, mx.z, 0.0f};
+                nd->bmin[c] = a; nd->bmax[c] = b;
+            }
+        }
+    }
+
+    *fmin_out = fmin; *fmax_out = fmax; fmin = fmax = NULL;
+    *nfinal_out = nfinal;
+    *levels_out = level;
+out:
+    free(cmin); free(cmax); free(nmin); free(nmax); free(fmin); free(fmax);
+    free(pmin); free(pmax); free(side); free(saddr); free(lside); free(laddr);
+    free(owner); free(csize); free(lnode); free(lnaddr); free(req); free(eaddr); free(planes);
+    return rc;
+}
+
+/* Triangle area 0.5*|e1 x e2| (LowerTriangleMap.h:24-38). */
+static inline float tri_area(const float *tri, int32_t prim)
+{
+    const float *tp = tri + 9 * (size_t)prim;
+    const v3 v0 = ld3(tp), v1 = ld3(tp + 3), v2 = ld3(tp + 6);
+    const v3 c = cross3(sub3(v1, v0), sub3(v2, v0));
+    return 0.5f * sqrtf(dot3(c, c));
+}
+
+/* CalcAreaForSets (LowerTriangleMap.h:412-461). */
+static inline void calc_area_for_sets(const int32_t sets_in[4], int axis, int32_t set_index,
+                                      uint32_t area_idx, const float *areas,
+                                      float *opt, float *la, float *ra, uint32_t *ls, uint32_t *rs,
+                                      int *opt_axis, int32_t *split_index)
+{
+    uint32_t s[4] = {(uint32_t)sets_in[0] & area_idx, (uint32_t)sets_in[1] & area_idx,
+                     (uint32_t)sets_in[2] & area_idx, (uint32_t)sets_in[3] & area_idx};
+    float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t bits = area_idx;
+    while (bits) {
+        const int i = __builtin_ctz(bits);
+        const uint32_t m = 1u << i;
+        a[0] = a[0] + ((s[0] & m) ? areas[i] : 0.0f);
+        a[1] = a[1] + ((s[1] & m) ? areas[i] : 0.0f);
+        a[2] = a[2] + ((s[2] & m) ? areas[i] : 0.0f);
+        a[3] = a[3] + ((s[3] & m) ? areas[i] : 0.0f);
+        bits &= bits - 1u;
+    }
+    const float low = (float)__builtin_popcount(s[0]) * a[0] + (float)__builtin_popcount(s[1]) * a[1];
+    const float high = (float)__builtin_popcount(s[2]) * a[2] + (float)__builtin_popcount(s[3]) * a[3];
+    if (low < *opt) {
+        *ls = s[0]; *rs = s[1]; *la = a[0]; *ra = a[1];
+        *opt = low; *opt_axis = axis; *split_index = set_index;
+    }
+    if (high < *opt) {
+        *ls = s[2]; *rs = s[3]; *la = a[2]; *ra = a[3];
+        *opt = high; *opt_axis = axis; *split_index = (int32_t)((uint32_t)set_index | 0x80000000u);
+    }
+}
+
+/*
+ * Lower SAH phase: TriangleMapSAHCreator.cu:67-260 with kernels
+ * LowerTriangleMap.h:24-155 (areas, preprocessing, splitting planes) and
+ * :412-636 (CalcSAH, CreateLowerSAHChildren, PropagateAabbToChildren).
+ * With intersection_cost = 1 and min_leaf = 0 the split rule is the
+ * reference's `optimalArea < (bitcount - traversalCost) * nodeArea`.
+ */
+static int build_lower_sah(const float *tri, const or_build_params *p, nodes *nd,
+                           const f4 *fmin, const f4 *fmax, int32_t NF,
+                           const int32_t *prim_indices, const ivec *leaf_ids, int32_t *levels_out)
+{
+    int rc = 0;
+    float *areas = malloc(sizeof(float) * (size_t)(NF > 0 ? NF : 1));
+    int32_t *sts = malloc(sizeof(int32_t) * 12 * (size_t)(NF > 0 ? NF : 1));
+    int32_t *act = NULL, *ssplit = NULL, *saddr = NULL, *csets = NULL;
+    float *careas = NULL;
+    if (!areas || !sts) { rc = OR_ERR_ALLOC; goto out; }
+    for (int32_t i = 0; i < NF; ++i) areas[i] = tri_area(tri, prim_indices[i]);
+
+    /* PreprocesLowerNodes (LowerTriangleMap.h:56-81). */
+    const int32_t R0 = (int32_t)leaf_ids->n;
+    for (int32_t k = 0; k < R0; ++k) {
+        const int32_t leaf = leaf_ids->a[k];
+        const int32_t pi = nd->pidx[leaf], amt = nd->amt[leaf];
+        float area = 0.0f;
+        uint32_t bmp = 0;
+        for (int32_t i = 0; i < amt; ++i) {
+            const float a = areas[pi + i];
+            bmp += a > 0.0f ? (1u << i) : 0u;
+            area += a;
+        }
+        nd->area[leaf] = area;
+        nd->amt[leaf] = (int32_t)bmp;
+    }
+    /* CreateSplittingPlanes (LowerTriangleMap.h:84-155): sets per prim slot,
+     * per axis {lowLeft, lowRight, highLeft, highRight}. */
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int32_t k = 0; k < R0; ++k) {
+        const int32_t leaf = leaf_ids->a[k];
+        const int32_t pi = nd->pidx[leaf];
+        const uint32_t bmp = (uint32_t)nd->amt[leaf];
+        uint32_t tris = bmp;
+        while (tris) {
+            const int id = __builtin_ctz(tris);
+            const f4 lo = fmin[pi + id], hi = fmax[pi + id];
+            uint32_t sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sz[4] = {0, 0, 0, 0};
+            uint32_t b = bmp;
+            while (b) {
+                const int i = __builtin_ctz(b);
+                const uint32_t m = 1u << i;
+                const f4 mn = fmin[pi + i], mx = fmax[pi + i];
+                sx[0] |= mn.x <= lo.x ? m : 0; sx[1] |= lo.x < mx.x ? m : 0;
+                sx[2] |= mn.x <= hi.x ? m : 0; sx[3] |= hi.x < mx.x ? m : 0;
+                sy[0] |= mn.y <= lo.y ? m : 0; sy[1] |= lo.y < mx.y ? m : 0;
+                sy[2] |= mn.y <= hi.y ? m : 0; sy[3] |= hi.y < mx.y ? m : 0;
+                sz[0] |= mn.z <= lo.z ? m : 0; sz[1] |= lo.z < mx.z ? m : 0;
+                sz[2] |= mn.z <= hi.z ? m : 0; sz[3] |= hi.z < mx.z ? m : 0;
+                b &= b - 1u;
+            }
+            for (int c = 0; c < 4; ++c) {
+                sts[4 * (size_t)(pi + id) + c] = (int32_t)sx[c];
+                sts[4 * ((size_t)NF + pi + id) + c] = (int32_t)sy[c];
+                sts[4 * (2 * (size_t)NF + pi + id) + c] = (int32_t)sz[c];
+            }
+            tris &= tris - 1u;
+        }
+    }
+
+    int32_t R = R0, active = nd->n, lv = 0;
+    int use_idx = 1;
+    while (R > 0) {
+        ++lv;
+        free(act); free(ssplit); free(saddr); free(csets); free(careas);
+        act = malloc(sizeof(int32_t) * (size_t)R);
+        ssplit = malloc(sizeof(int32_t) * (size_t)R);
+        saddr = malloc(sizeof(int32_t) * (size_t)R + sizeof(int32_t));
+        csets = malloc(sizeof(int32_t) * 2 * (size_t)R);
+        careas = malloc(sizeof(float) * 2 * (size_t)R);
+        if (!act || !ssplit || !saddr || !csets || !careas) { rc = OR_ERR_ALLOC; goto out; }
+        for (int32_t k = 0; k < R; ++k) act[k] = use_idx ? leaf_ids->a[k] : active + k;
+
+        /* CalcSAH (LowerTriangleMap.h:463-555). */
+        const float ct = p->traversal_cost, ci = p->intersection_cost;
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int32_t k = 0; k < R; ++k) {
+            const int32_t par = act[k];
+            const int32_t pi = nd->pidx[par];
+            const uint32_t bmp = (uint32_t)nd->amt[par];
+            float area[32];
+            uint32_t b = bmp;
+            while (b) { const int i = __builtin_ctz(b); area[i] = areas[pi + i]; b &= b - 1u; }
+            float opt = OR_FINF, la = 0.0f, ra = 0.0f;
+            uint32_t ls = 0, rs = 0;
+            int axis = 0;
+            int32_t split_index = 0;
+            uint32_t tris = bmp;
+            while (tris) {
+                const int i = __builtin_ctz(tris);
+                calc_area_for_sets(sts + 4 * (size_t)(pi + i), OR_X, pi + i, bmp, area,
+                                   &opt, &la, &ra, &ls, &rs, &axis, &split_index);
+                calc_area_for_sets(sts + 4 * ((size_t)NF + pi + i), OR_Y, pi + i, bmp, area,
+                                   &opt, &la, &ra, &ls, &rs, &axis, &split_index);
+                calc_area_for_sets(sts + 4 * (2 * (size_t)NF + pi + i), OR_Z, pi + i, bmp, area,
+                                   &opt, &la, &ra, &ls, &rs, &axis, &split_index);
+                tris &= tris - 1u;
+            }
+            const float node_area = nd->area[par];
+            const int cnt = __builtin_popcount(bmp);
+            int split = (ci * opt) < ((ci * (float)cnt) - ct) * node_area;
+            if (cnt <= p->min_leaf) split = 0;
+            if (split) {
+                careas[2 * k] = la; careas[2 * k + 1] = ra;
+                csets[2 * k] = (int32_t)ls; csets[2 * k + 1] = (int32_t)rs;
+                f4 sp4;
+                if ((uint32_t)split_index & 0x80000000u) sp4 = fmax[(uint32_t)split_index ^ 0x80000000u];
+                else sp4 = fmin[split_index];
+                nd->split[par] = f4c(sp4, axis);
+            }
+            nd->info[par] = split ? (int8_t)axis : OR_LEAF;
+            ssplit[k] = split;
+        }
+        excl_scan(ssplit, R, saddr);
+        const int32_t splits = saddr[R];
+        const int32_t child_base = nd->n;
+        if ((rc = nodes_resize(nd, nd->n + 2 * splits))) goto out;
+        /* CreateLowerSAHChildren (LowerTriangleMap.h:557-600). */
+        for (int32_t k = 0; k < R; ++k) {
+            if (!ssplit[k]) continue;
+            const int32_t par = act[k];
+            const int32_t l = child_base + saddr[k], r = l + splits;
+            nd->area[l] = careas[2 * k]; nd->pidx[l] = nd->pidx[par]; nd->amt[l] = csets[2 * k];
+            nd->area[r] = careas[2 * k + 1]; nd->pidx[r] = nd->pidx[par]; nd->amt[r] = csets[2 * k + 1];
+            nd->ch[2 * par] = l; nd->ch[2 * par + 1] = r;
+        }
+        const int32_t created = 2 * splits;
+        /* PropagateAabbToChildren (LowerTriangleMap.h:602-636). */
+        if (p->propagate_aabbs && created > 0) {
+            for (int32_t k = 0; k < R; ++k) {
+                const int32_t par = act[k];
+                const int axis = nd->info[par] & 3;
+                if (axis == OR_LEAF) continue;
+                const float sp = nd->split[par];
+                const int32_t l = nd->ch[2 * par], r = nd->ch[2 * par + 1];
+                const f4 mn = nd->bmin[par], mx = nd->bmax[par];
+                f4 rmn = {axis == OR_X ? sp : mn.x, axis == OR_Y ? sp : mn.y, axis == OR_Z ? sp : mn.z, 0.0f};
+                f4 lmx = {axis == OR_X ? sp : mx.x, axis == OR_Y ? sp : mx.y, axis == OR_Z ? sp : mx.z, 0.0f};
+                nd->bmin[l] = mn; nd->bmin[r] = rmn;
+                nd->bmax[l] = lmx; nd->bmax[r] = mx;
+            }
+        }
+        use_idx = 0;
+        active = nd->n - created;
+        R = created;
+    }
+    *levels_out = lv;
+out:
+    free(areas); free(sts); free(act); free(ssplit); free(saddr); free(csets); free(careas);
+    return rc;
+}
+
+int or_build(const float *tri, int32_t T, const or_build_params *p, or_tree *out)
+{
+    if (!out || !p || T < 0 || (T > 0 && !tri)) return OR_ERR_ARG;
+    if (p->leaf_size < 1 || p->leaf_size > 32) return OR_ERR_ARG;
+    memset(out, 0, sizeof(*out));
+    nodes nd;
+    memset(&nd, 0, sizeof(nd));
+    ivec leaf_ids = {0};
+    f4 *fmin = NULL, *fmax = NULL;
+    int32_t NF = 0, up_levels = 0, lo_levels = 0;
+    int rc = build_upper(tri, T, p, &nd, &fmin, &fmax, &NF, &leaf_ids, &up_levels);
+    if (rc) goto fail;
+
+    /* ExtractIndexFromAabb (TriangleUpper.h:43-52). */
+    int32_t *prim_indices = malloc(sizeof(int32_t) * (size_t)(NF > 0 ? NF : 1));
+    if (!prim_indices) { rc = OR_ERR_ALLOC; goto fail; }
+    for (int32_t i = 0; i < NF; ++i) prim_indices[i] = f2i(fmin[i].w);
+
+    if (p->lower == OR_LOWER_SAH) {
+        rc = build_lower_sah(tri, p, &nd, fmin, fmax, NF, prim_indices, &leaf_ids, &lo_levels);
+        if (rc) { free(prim_indices); goto fail; }
+    } else {
+        /* TriangleMapBitmapCreator.cu:32-49 PreprocessLeafNodes. */
+        for (size_t k = 0; k < leaf_ids.n; ++k) {
+            const int32_t leaf = leaf_ids.a[k];
+            nd.info[leaf] = OR_LEAF;
+            nd.amt[leaf] = (int32_t)((1u << nd.amt[leaf]) - 1u);
+        }
+    }
+
+    out->n_nodes = nd.n;
+    out->n_refs = NF;
+    out->n_upper_leaves = (int32_t)leaf_ids.n;
+    out->upper_levels = up_levels;
+    out->lower_levels = lo_levels;
+    out->info = nd.info; out->split = nd.split;
+    out->aabb_min = (float *)nd.bmin; out->aabb_max = (float *)nd.bmax;
+    out->prim_index = nd.pidx; out->bitmap = nd.amt; out->children = nd.ch;
+    out->area = nd.area; out->parent = nd.parent;
+    out->prim_indices = prim_indices;
+    out->leaf_ids = leaf_ids.a ? leaf_ids.a : calloc(1, sizeof(int32_t));
+    out->prim_min = (float *)(fmin ? fmin : calloc(1, sizeof(f4)));
+    out->prim_max = (float *)(fmax ? fmax : calloc(1, sizeof(f4)));
+    return 0;
+fail:
+    nodes_free(&nd);
+    free(leaf_ids.a); free(fmin); free(fmax);
+    return rc;
+}
+
+void or_tree_free(or_tree *t)
+{
+    if (!t) return;
+    free(t->info); free(t->split); free(t->aabb_min); free(t->aabb_max); free(t->prim_index);
+    free(t->bitmap); free(t->children); free(t->area); free(t->parent); free(t->prim_indices);
+    free(t->leaf_ids); free(t->prim_min); free(t->prim_max);
+    memset(t, 0, sizeof(*t));
+}

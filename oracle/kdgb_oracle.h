@@ -1,0 +1,127 @@
+/*
+ * kdgb_oracle.h -- CPU restatement of the reference kd-tree build and ray
+ * traversal (OpenEngineDK/extensions-PhotonMapping, Utils/CUDA).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path
+ * and the timed CPU baseline in bench.py.  Nothing in the product library
+ * links, loads or calls it; the product fails loudly when its CUDA
+ * extension is missing instead of falling back here.
+ *
+ * Parity status: the reference cannot be compiled here (it needs OpenEngine
+ * core, extensions-CUDA, CUDPP and cutil, none of which are present) and it
+ * ships no tests, golden vectors or fixtures, so this restatement is
+ * "parity unpinned" against the reference's own outputs.  It follows the
+ * reference source line by line (citations on each function) with one
+ * documented evaluation order for the un-vendored float3 helpers:
+ *   dot(a,b)   = (a.x*b.x + a.y*b.y) + a.z*b.z
+ *   cross(a,b) = (a.y*b.z - a.z*b.y, a.z*b.x - a.x*b.z, a.x*b.y - a.y*b.x)
+ * every multiply and add rounded separately (no FMA contraction), IEEE
+ * division (the reference's host path, IRayTracer.h:127-128) and IEEE sqrt.
+ *
+ * All arrays are plain host memory.  Functions return 0 on success and a
+ * negative number on error (see or_error_string).
+ */
+#ifndef KDGB_ORACLE_H
+#define KDGB_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Utils/CUDA/Utils.h:18 -- the integer 0x7f800000 converted to float. */
+#define OR_FINF 2139095040.0f
+
+enum { OR_LEAF = 0, OR_X = 1, OR_Y = 2, OR_Z = 3 };
+enum { OR_LOWER_BITMAP = 0, OR_LOWER_SAH = 1 };
+enum { OR_TIE_LOWEST_ID = 0, OR_TIE_REF_LAST = 1 };
+enum { OR_TRACER_RESTART = 0, OR_TRACER_SHORTSTACK = 1, OR_TRACER_BRUTE = 2 };
+
+typedef struct or_build_params {
+    int32_t lower;                 /* OR_LOWER_BITMAP (reference default) or OR_LOWER_SAH */
+    int32_t split_empty_space;     /* TriangleMapUpperCreator.cu:31 default true */
+    int32_t propagate_aabbs;       /* TriangleMap.cu:47 default true */
+    float   empty_space_threshold; /* TriangleMapUpperCreator.cu:28 default 0.35 */
+    float   traversal_cost;        /* TriangleMap.cu:48 default 24 */
+    float   intersection_cost;     /* 1.0 reproduces the reference SAH rule exactly */
+    int32_t min_leaf;              /* SAH never splits nodes with <= min_leaf prims (0 = reference) */
+    int32_t esc_zmax_as_x;         /* 1 = reproduce EmptySpaceSplitting.h:172-181 (max-z face cut on x) */
+    int32_t max_levels;            /* guard against non-terminating upper loops */
+    int32_t leaf_size;             /* upper leaf threshold: children with < leaf_size refs become leaves (32) */
+} or_build_params;
+
+typedef struct or_tree {
+    int32_t n_nodes;
+    int32_t n_refs;          /* length of prim_indices */
+    int32_t n_upper_leaves;  /* length of leaf_ids */
+    int32_t upper_levels;    /* upper loop iterations */
+    int32_t lower_levels;    /* SAH loop iterations */
+    int8_t  *info;           /* KDNode.h:65   0 LEAF, 1 X, 2 Y, 3 Z */
+    float   *split;          /* KDNode.h:66 */
+    float   *aabb_min;       /* KDNode.h:67   float4 per node, w = 0 */
+    float   *aabb_max;
+    int32_t *prim_index;     /* KDNode.h:68 */
+    int32_t *bitmap;         /* KDNode.h:69   amount during the upper build, bitmap after */
+    int32_t *children;       /* KDNode.h:73   int2 per node */
+    float   *area;           /* TriangleNode.h:20 */
+    int32_t *parent;         /* TriangleNode.h:21 */
+    int32_t *prim_indices;   /* TriangleMap.h:55 */
+    int32_t *leaf_ids;       /* TriangleMap.h:57 */
+    float   *prim_min;       /* final clipped reference boxes (float4, w = tri id bits) */
+    float   *prim_max;
+} or_tree;
+
+typedef struct or_trace_params {
+    int32_t tracer;          /* OR_TRACER_* */
+    int32_t leaf_skipping;   /* IRayTracer.cu:33 default true */
+    int32_t tie;             /* OR_TIE_* */
+    int32_t stack_depth;     /* ShortStack.cu:25 default 4 */
+    int32_t max_iterations;  /* restart / pop guard per ray; 0 = unlimited */
+} or_trace_params;
+
+void or_build_params_default(or_build_params *p);
+void or_trace_params_default(or_trace_params *p);
+const char *or_error_string(int code);
+
+/* Builds the reference tree over T triangles (tri: T*9 floats, v0 v1 v2). */
+int or_build(const float *tri, int32_t T, const or_build_params *p, or_tree *out);
+void or_tree_free(or_tree *t);
+
+/* Triangle SoA as GeometryList.h:41 (p0,p1,p2 float4 with w = 1). */
+void or_geometry_from_tris(const float *tri, int32_t T, float *p0, float *p1, float *p2);
+
+/*
+ * First-hit trace of n rays.  Tree arrays are or_tree fields (may come from
+ * any builder).  ray_o / ray_d: n*3 floats.  Outputs hit id (-1 miss), t, u, v.
+ * `threads` = OpenMP threads (<= 0: all).
+ */
+int or_trace(const or_tree *tree, const float *tri, int32_t T,
+             const or_trace_params *p,
+             const float *ray_o, const float *ray_d, int32_t n,
+             int32_t *hit, float *t, float *u, float *v, int32_t threads);
+
+/* Brute force over all T triangles (BruteTracer.cu:54-96, cap lifted). */
+int or_trace_brute(const float *tri, int32_t T, int32_t tie,
+                   const float *ray_o, const float *ray_d, int32_t n,
+                   int32_t *hit, float *t, float *u, float *v, int32_t threads);
+
+/* FP64 brute force: same Moeller-Trumbore in double, lowest-id ties. */
+int or_trace_brute_f64(const float *tri, int32_t T,
+                       const float *ray_o, const float *ray_d, int32_t n,
+                       int32_t *hit, double *t, double *u, double *v, int32_t threads);
+
+/* Shadow rays (Raytracer.cu:108-163): occluded[i] = 1 when point i is in shadow. */
+int or_trace_shadow(const or_tree *tree, const float *tri, int32_t T,
+                    const float *points, int32_t n, const float light[3],
+                    int32_t *occluded, int32_t threads);
+
+/* Moeller-Trumbore restated (IRayTracer.h:111-145); exported for unit tests. */
+int or_moeller_trumbore(const float v0[3], const float v1[3], const float v2[3],
+                        const float o[3], const float d[3], float t_max,
+                        float out_tuv[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

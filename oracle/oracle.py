@@ -1,0 +1,241 @@
+"""ctypes front end of the CPU oracle (libkdgb_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+cpu_baseline / --impl reference legs of bench.py as the checker and the
+timed CPU baseline.  The product library never imports this module.
+The restatement is "parity unpinned": the reference cannot be compiled here
+and ships no golden vectors (see kdgb_oracle.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import platform
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libkdgb_oracle.so")
+
+LEAF, X, Y, Z = 0, 1, 2, 3
+LOWER_BITMAP, LOWER_SAH = 0, 1
+TIE_LOWEST_ID, TIE_REF_LAST = 0, 1
+TRACER_RESTART, TRACER_SHORTSTACK, TRACER_BRUTE = 0, 1, 2
+FINF = np.float32(2139095040.0)
+
+
+class BuildParams(C.Structure):
+    _fields_ = [("lower", C.c_int32), ("split_empty_space", C.c_int32),
+                ("propagate_aabbs", C.c_int32), ("empty_space_threshold", C.c_float),
+                ("traversal_cost", C.c_float), ("intersection_cost", C.c_float),
+                ("min_leaf", C.c_int32), ("esc_zmax_as_x", C.c_int32),
+                ("max_levels", C.c_int32), ("leaf_size", C.c_int32)]
+
+
+class TraceParams(C.Structure):
+    _fields_ = [("tracer", C.c_int32), ("leaf_skipping", C.c_int32), ("tie", C.c_int32),
+                ("stack_depth", C.c_int32), ("max_iterations", C.c_int32)]
+
+
+class _Tree(C.Structure):
+    _fields_ = [("n_nodes", C.c_int32), ("n_refs", C.c_int32), ("n_upper_leaves", C.c_int32),
+                ("upper_levels", C.c_int32), ("lower_levels", C.c_int32),
+                ("info", C.POINTER(C.c_int8)), ("split", C.POINTER(C.c_float)),
+                ("aabb_min", C.POINTER(C.c_float)), ("aabb_max", C.POINTER(C.c_float)),
+                ("prim_index", C.POINTER(C.c_int32)), ("bitmap", C.POINTER(C.c_int32)),
+                ("children", C.POINTER(C.c_int32)), ("area", C.POINTER(C.c_float)),
+                ("parent", C.POINTER(C.c_int32)), ("prim_indices", C.POINTER(C.c_int32)),
+                ("leaf_ids", C.POINTER(C.c_int32)), ("prim_min", C.POINTER(C.c_float)),
+                ("prim_max", C.POINTER(C.c_float))]
+
+
+_lib = None
+
+
+def build_library(force: bool = False) -> str:
+    """Compiles libkdgb_oracle.so with the committed Makefile (rebuilt when
+    the source changed or the library was built on another host arch)."""
+    stamp = os.path.join(_HERE, ".host_arch")
+    here = platform.machine()
+    if not (os.path.exists(stamp) and open(stamp).read().strip() == here):
+        force = True
+    if force or not os.path.exists(_LIB_PATH) or (
+            os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "kdgb_oracle.c"))):
+        subprocess.run(["make", "-s", "-C", _HERE, "-B" if force else "all"], check=True)
+        with open(stamp, "w") as f:
+            f.write(here + "\n")
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_library()
+        L = C.CDLL(_LIB_PATH)
+        P = C.c_void_p
+        L.or_build.argtypes = [P, C.c_int32, C.POINTER(BuildParams), C.POINTER(_Tree)]
+        L.or_tree_free.argtypes = [C.POINTER(_Tree)]
+        L.or_trace.argtypes = [C.POINTER(_Tree), P, C.c_int32, C.POINTER(TraceParams), P, P,
+                               C.c_int32, P, P, P, P, C.c_int32]
+        L.or_trace_brute.argtypes = [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32]
+        L.or_trace_brute_f64.argtypes = [P, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32]
+        L.or_trace_shadow.argtypes = [C.POINTER(_Tree), P, C.c_int32, P, C.c_int32, P, P, C.c_int32]
+        L.or_moeller_trumbore.argtypes = [P, P, P, P, P, C.c_float, P]
+        L.or_error_string.restype = C.c_char_p
+        L.or_build_params_default.argtypes = [C.POINTER(BuildParams)]
+        L.or_trace_params_default.argtypes = [C.POINTER(TraceParams)]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib().or_error_string(rc).decode())
+
+
+def build_params(**kw) -> BuildParams:
+    p = BuildParams()
+    lib().or_build_params_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def trace_params(**kw) -> TraceParams:
+    p = TraceParams()
+    lib().or_trace_params_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+@dataclass
+class Tree:
+    """Tree arrays in the reference's KDNode / TriangleNode SoA layout."""
+    info: np.ndarray
+    split: np.ndarray
+    aabb_min: np.ndarray
+    aabb_max: np.ndarray
+    prim_index: np.ndarray
+    bitmap: np.ndarray
+    children: np.ndarray
+    area: np.ndarray
+    parent: np.ndarray
+    prim_indices: np.ndarray
+    leaf_ids: np.ndarray
+    prim_min: np.ndarray
+    prim_max: np.ndarray
+    upper_levels: int = 0
+    lower_levels: int = 0
+
+    @property
+    def n_nodes(self) -> int:
+        return int(self.info.shape[0])
+
+    def as_struct(self):
+        s = _Tree()
+        s.n_nodes = self.n_nodes
+        s.n_refs = int(self.prim_indices.shape[0])
+        s.n_upper_leaves = int(self.leaf_ids.shape[0])
+        for name, ctype in [("info", C.c_int8), ("split", C.c_float), ("aabb_min", C.c_float),
+                            ("aabb_max", C.c_float), ("prim_index", C.c_int32), ("bitmap", C.c_int32),
+                            ("children", C.c_int32), ("area", C.c_float), ("parent", C.c_int32),
+                            ("prim_indices", C.c_int32), ("leaf_ids", C.c_int32),
+                            ("prim_min", C.c_float), ("prim_max", C.c_float)]:
+            arr = getattr(self, name)
+            setattr(s, name, arr.ctypes.data_as(C.POINTER(ctype)))
+        return s
+
+
+def _copy(ptr, n, dtype, shape=None):
+    if n == 0:
+        return np.zeros(shape if shape else (0,), dtype=dtype)
+    buf = np.ctypeslib.as_array(ptr, shape=(n,)).copy().astype(dtype, copy=False)
+    return buf.reshape(shape) if shape else buf
+
+
+def build(tris: np.ndarray, params: BuildParams | None = None, **kw) -> Tree:
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    p = params if params is not None else build_params(**kw)
+    t = _Tree()
+    _check(lib().or_build(_ptr(tris), tris.shape[0], C.byref(p), C.byref(t)))
+    try:
+        n, r, lf = t.n_nodes, t.n_refs, t.n_upper_leaves
+        out = Tree(info=_copy(t.info, n, np.int8), split=_copy(t.split, n, np.float32),
+                   aabb_min=_copy(t.aabb_min, 4 * n, np.float32, (n, 4)),
+                   aabb_max=_copy(t.aabb_max, 4 * n, np.float32, (n, 4)),
+                   prim_index=_copy(t.prim_index, n, np.int32), bitmap=_copy(t.bitmap, n, np.int32),
+                   children=_copy(t.children, 2 * n, np.int32, (n, 2)), area=_copy(t.area, n, np.float32),
+                   parent=_copy(t.parent, n, np.int32), prim_indices=_copy(t.prim_indices, r, np.int32),
+                   leaf_ids=_copy(t.leaf_ids, lf, np.int32),
+                   prim_min=_copy(t.prim_min, 4 * r, np.float32, (r, 4)),
+                   prim_max=_copy(t.prim_max, 4 * r, np.float32, (r, 4)),
+                   upper_levels=t.upper_levels, lower_levels=t.lower_levels)
+    finally:
+        lib().or_tree_free(C.byref(t))
+    return out
+
+
+def _rays(o, d):
+    o = np.ascontiguousarray(o, dtype=np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(d, dtype=np.float32).reshape(-1, 3)
+    assert o.shape == d.shape
+    return o, d
+
+
+def trace(tree: Tree | None, tris: np.ndarray, o, d, params: TraceParams | None = None,
+          threads: int = 0, **kw):
+    """First-hit trace; returns (hit int32, t, u, v float32)."""
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    o, d = _rays(o, d)
+    n = o.shape[0]
+    p = params if params is not None else trace_params(**kw)
+    hit = np.empty(n, np.int32)
+    t = np.empty(n, np.float32)
+    u = np.empty(n, np.float32)
+    v = np.empty(n, np.float32)
+    if p.tracer == TRACER_BRUTE:
+        _check(lib().or_trace_brute(_ptr(tris), tris.shape[0], p.tie, _ptr(o), _ptr(d), n,
+                                    _ptr(hit), _ptr(t), _ptr(u), _ptr(v), threads))
+    else:
+        s = tree.as_struct()
+        _check(lib().or_trace(C.byref(s), _ptr(tris), tris.shape[0], C.byref(p), _ptr(o), _ptr(d), n,
+                              _ptr(hit), _ptr(t), _ptr(u), _ptr(v), threads))
+    return hit, t, u, v
+
+
+def trace_brute_f64(tris, o, d, threads: int = 0):
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    o, d = _rays(o, d)
+    n = o.shape[0]
+    hit = np.empty(n, np.int32)
+    t = np.empty(n, np.float64)
+    u = np.empty(n, np.float64)
+    v = np.empty(n, np.float64)
+    _check(lib().or_trace_brute_f64(_ptr(tris), tris.shape[0], _ptr(o), _ptr(d), n,
+                                    _ptr(hit), _ptr(t), _ptr(u), _ptr(v), threads))
+    return hit, t, u, v
+
+
+def trace_shadow(tree: Tree, tris, points, light, threads: int = 0):
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+    lp = np.ascontiguousarray(light, dtype=np.float32).reshape(3)
+    occ = np.empty(pts.shape[0], np.int32)
+    s = tree.as_struct()
+    _check(lib().or_trace_shadow(C.byref(s), _ptr(tris), tris.shape[0], _ptr(pts), pts.shape[0],
+                                 _ptr(lp), _ptr(occ), threads))
+    return occ
+
+
+def moeller_trumbore(v0, v1, v2, o, d, t_max=float(FINF)):
+    arrs = [np.ascontiguousarray(x, dtype=np.float32).reshape(3) for x in (v0, v1, v2, o, d)]
+    out = np.zeros(3, np.float32)
+    hit = lib().or_moeller_trumbore(*[_ptr(a) for a in arrs], t_max, _ptr(out))
+    return bool(hit), out

@@ -1,0 +1,112 @@
+"""GPU build parity: the reference-mode build of libkdgb.so must produce the
+oracle's tree bit for bit (node arrays, leaf lists, reference order)."""
+import numpy as np
+import pytest
+
+from kdgb import scenes
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("info", "split", "children", "prim_index", "bitmap", "parent", "area", "aabb_min", "aabb_max",
+          "prim_indices", "leaf_ids")
+
+
+def tri_soup(n, seed, scale=0.05):
+    c = np.stack([scenes.uniform(seed, n, k) for k in range(3)], axis=1)
+    off = (np.stack([scenes.uniform(seed, n, 10 + k) for k in range(9)], axis=1) - 0.5) * scale
+    return np.ascontiguousarray((np.tile(c, 3) + off).astype(np.float32))
+
+
+def assert_same_tree(gpu, ref):
+    assert gpu.info.shape == ref.info.shape, (gpu.info.shape, ref.info.shape)
+    for f in FIELDS:
+        a, b = getattr(gpu, f), getattr(ref, f)
+        assert a.shape == b.shape, f
+        if a.dtype.kind == "f":
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f
+        else:
+            assert np.array_equal(a, b), f
+
+
+def scene(name):
+    if name == "c1":
+        return scenes.heightfield(64, 32, seed=1)[0]
+    if name == "clustered3k":
+        return scenes.clustered(3000, seed=4)
+    if name == "clustered60k":
+        return scenes.clustered(60000, seed=5)
+    if name == "soup":
+        return tri_soup(5000, 7)
+    if name == "degenerate":
+        t = tri_soup(600, 8)
+        t[::7, 3:6] = t[::7, 0:3]          # zero-area triangles
+        t[::11, 6:9] = t[::11, 3:6]
+        return t
+    raise KeyError(name)
+
+
+@pytest.mark.parametrize("name", ["c1", "clustered3k", "clustered60k", "soup", "degenerate"])
+@pytest.mark.parametrize("lower", [0, 1])
+def test_build_matches_oracle(kdgb_lib, cuda, oracle, name, lower):
+    tris = scene(name)
+    ref = oracle.build(tris, lower=lower)
+    with kdgb_lib.KDTree.build(tris, lower=lower) as tree:
+        assert_same_tree(tree.to_host(), ref)
+        st = tree.stats()
+        assert st.upper_levels == ref.upper_levels and st.n_nodes == ref.n_nodes
+
+
+@pytest.mark.parametrize("opts", [
+    dict(split_empty_space=0),
+    dict(split_empty_space=0, propagate_aabbs=0),
+    dict(esc_zmax_as_x=0),
+    dict(leaf_size=8),
+    dict(lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8),
+    dict(lower=1, propagate_aabbs=0),
+    dict(empty_space_threshold=0.1),
+])
+def test_build_options_match_oracle(kdgb_lib, cuda, oracle, opts):
+    tris = scenes.clustered(8000, seed=14)
+    ref = oracle.build(tris, **opts)
+    with kdgb_lib.KDTree.build(tris, **opts) as tree:
+        assert_same_tree(tree.to_host(), ref)
+
+
+@pytest.mark.parametrize("T", [0, 1, 2, 31, 32, 33, 257])
+def test_small_and_empty_builds(kdgb_lib, cuda, oracle, T):
+    tris = tri_soup(max(T, 1), 30)[:T]
+    ref = oracle.build(tris)
+    with kdgb_lib.KDTree.build(tris) as tree:
+        assert_same_tree(tree.to_host(), ref)
+
+
+def test_rebuild_reuses_handle(kdgb_lib, cuda, oracle):
+    a, b = scenes.clustered(20000, seed=1), scenes.heightfield(40, 30, seed=3)[0]
+    with kdgb_lib.KDTree.build(a) as tree:
+        tree.rebuild(b, lower=1)
+        assert_same_tree(tree.to_host(), oracle.build(b, lower=1))
+        tree.rebuild(a)
+        assert_same_tree(tree.to_host(), oracle.build(a))
+
+
+def test_nonfinite_is_an_error(kdgb_lib, cuda):
+    tris = scenes.clustered(1000, seed=2)
+    tris[10, 2] = np.inf
+    with pytest.raises(kdgb_lib.KdgbError) as e:
+        kdgb_lib.KDTree.build(tris)
+    assert e.value.status == 6
+
+
+def test_degenerate_duplicates_error(kdgb_lib, cuda):
+    tris = np.tile(np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32), (40, 1))
+    with pytest.raises(kdgb_lib.KdgbError) as e:
+        kdgb_lib.KDTree.build(tris, max_levels=20)
+    assert e.value.status == 5
+
+
+def test_invalid_params(kdgb_lib, cuda):
+    tris = scenes.clustered(100, seed=2)
+    for bad in (dict(leaf_size=33), dict(leaf_size=0), dict(lower=5), dict(mode=7)):
+        with pytest.raises(kdgb_lib.KdgbError) as e:
+            kdgb_lib.KDTree.build(tris, **bad)
+        assert e.value.status == 1
