@@ -1,6 +1,7 @@
 // C ABI of the kd-tree builder and tracers (include/kdgb.h).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -38,6 +39,10 @@ void setup_pool()
     });
 }
 }  // namespace
+
+static std::atomic<int64_t> g_launches{0};
+
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 
@@ -192,6 +197,8 @@ const char *kdgb_status_string(int status)
 }
 
 const char *kdgb_last_error(void) { return g_last_error.c_str(); }
+
+int64_t kdgb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 void kdgb_build_params_default(kdgb_build_params *p)
 {

@@ -29,7 +29,14 @@ int cuda_fail(cudaError_t e, const char *what);
         if (s_ != KDGB_OK) return s_;    \
     } while (0)
 
-#define KDGB_LAUNCH_CHECK() KDGB_CUDA(cudaGetLastError())
+// Counts kernel launches made by the library (instrumentation only).
+void note_launch(int n = 1);
+
+#define KDGB_LAUNCH_CHECK()              \
+    do {                                 \
+        ::kdgb::note_launch();           \
+        KDGB_CUDA(cudaGetLastError());   \
+    } while (0)
 
 // ---------------------------------------------------------------------------
 // Device arrays owned by a tree handle.  `cap` counts elements.

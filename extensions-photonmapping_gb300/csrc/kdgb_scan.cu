@@ -192,6 +192,7 @@ int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s)
     }
     cudaFreeAsync(partial, s);
     if (e != cudaSuccess) return cuda_fail(e, "scan kernels");
+    note_launch(3);
     return KDGB_OK;
 }
 

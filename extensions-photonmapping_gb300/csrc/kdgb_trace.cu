@@ -390,6 +390,7 @@ int pack_for_traversal(Tree &t, cudaStream_t s)
         if (n > 0) {
             k_leaf_counts<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.bitmap.p, cnt);
             if ((e = cudaGetLastError()) != cudaSuccess) { rc = cuda_fail(e, "k_leaf_counts"); break; }
+            note_launch();
         }
         if ((rc = scan_exclusive<1>(cnt, off, n, s)) != KDGB_OK) break;
         if ((e = cudaMemcpyAsync(&total, off + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
@@ -406,6 +407,7 @@ int pack_for_traversal(Tree &t, cudaStream_t s)
             k_pack_tris<<<blocks_for((int64_t)n * 32, kPackBlock), kPackBlock, 0, s>>>(
                 n, t.info.p, t.bitmap.p, t.pidx.p, t.prim_indices.p, t.p0.p, t.p1.p, t.p2.p, off, t.ttri.p);
             if ((e = cudaGetLastError()) != cudaSuccess) { rc = cuda_fail(e, "pack kernels"); break; }
+            note_launch(2);
         }
     } while (0);
     cudaFreeAsync(cnt, s);

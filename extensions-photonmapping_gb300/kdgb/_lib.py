@@ -65,6 +65,7 @@ SIGNATURES = {
     "kdgb_abi_version": (C.c_int, []),
     "kdgb_status_string": (C.c_char_p, [C.c_int]),
     "kdgb_last_error": (C.c_char_p, []),
+    "kdgb_launch_count": (C.c_int64, []),
     "kdgb_build_params_default": (None, [C.POINTER(BuildParams)]),
     "kdgb_trace_params_default": (None, [C.POINTER(TraceParams)]),
     "kdgb_build": (C.c_int, [P, C.c_int32, C.POINTER(BuildParams), C.POINTER(C.c_void_p), P]),

@@ -143,6 +143,9 @@ typedef struct kdgb_build_stats {
 KDGB_API int         kdgb_abi_version(void);
 KDGB_API const char *kdgb_status_string(int status);
 KDGB_API const char *kdgb_last_error(void);
+/* Number of kernel launches this library has issued since it was loaded
+ * (instrumentation; no counterpart in the reference). */
+KDGB_API int64_t     kdgb_launch_count(void);
 KDGB_API void        kdgb_build_params_default(kdgb_build_params *p);
 KDGB_API void        kdgb_trace_params_default(kdgb_trace_params *p);
 
