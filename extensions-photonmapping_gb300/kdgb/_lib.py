@@ -79,7 +79,10 @@ SIGNATURES = {
     "kdgb_trace_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, C.c_int32, P, P, P]),
     "kdgb_trace_primary_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P, P, P]),
     "kdgb_trace_brute": (C.c_int, [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, P]),
+    "kdgb_trace_brute_noalloc": (C.c_int, [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, P]),
 }
+
+NOALLOC_MAX_TRIS = 65536  # KDGB_NOALLOC_MAX_TRIS
 
 _lib = None
 

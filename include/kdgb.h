@@ -211,6 +211,29 @@ KDGB_API int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t ti
                      int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
                      kdgb_stream_t stream);
 
+/* Largest triangle count kdgb_trace_brute_noalloc accepts. */
+#define KDGB_NOALLOC_MAX_TRIS 65536
+
+/* No counterpart in the reference.  The same first-hit brute-force trace as
+ * kdgb_trace_brute, for callers that cannot allocate device memory while
+ * they run: a frame loop that must not stall on cudaMalloc's implicit device
+ * synchronisation, or a host application whose own allocator has already
+ * reserved the device's memory.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine; its scratch is a fixed device array of
+ * KDGB_NOALLOC_MAX_TRIS packed triangles (3 MiB) inside the library, held by
+ * every GPU that loads the library until the process exits.
+ *  - n_tris > KDGB_NOALLOC_MAX_TRIS is rejected with KDGB_ERR_CAPACITY.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current and caches it; make
+ *    that first call before any stream capture.
+ *  - All calls share the one array and each call overwrites the part it
+ *    uses; calls whose work overlaps on the GPU (other streams, other host
+ *    threads) race on it and must be serialised by the caller. */
+KDGB_API int kdgb_trace_brute_noalloc(const float *tri_v_dev, int32_t n_tris, int32_t tie,
+                                      const float *ray_o_dev, const float *ray_d_dev, int32_t n,
+                                      int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
+                                      kdgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
