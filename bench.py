@@ -266,9 +266,11 @@ def main():
         flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("kdgb_timed_step")
         e0.record(stream)
         step((t0, t1))
         e1.record(stream)
+        torch.cuda.nvtx.range_pop()
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
         trace_ms.append(t0.elapsed_time(t1))
