@@ -94,6 +94,8 @@ template int ensure<float4>(DevArray<float4> &, int64_t, cudaStream_t, int64_t, 
 template int ensure<int32_t>(DevArray<int32_t> &, int64_t, cudaStream_t, int64_t, bool);
 template int ensure<int2>(DevArray<int2> &, int64_t, cudaStream_t, int64_t, bool);
 template int ensure<int4>(DevArray<int4> &, int64_t, cudaStream_t, int64_t, bool);
+template int ensure<unsigned>(DevArray<unsigned> &, int64_t, cudaStream_t, int64_t, bool);
+template int ensure<float2>(DevArray<float2> &, int64_t, cudaStream_t, int64_t, bool);
 
 static void release_all(Tree &t, cudaStream_t s)
 {
@@ -102,6 +104,18 @@ static void release_all(Tree &t, cudaStream_t s)
     release(t.pidx, s); release(t.bitmap, s); release(t.parent, s); release(t.children, s);
     release(t.area, s); release(t.prim_indices, s); release(t.leaf_ids, s);
     release(t.tnode, s); release(t.ttri, s);
+    Workspace &w = t.ws;
+    release(w.cmin, s); release(w.cmax, s); release(w.nmin, s); release(w.nmax, s); release(w.fmin, s);
+    release(w.fmax, s); release(w.pmin, s); release(w.pmax, s); release(w.keys, s); release(w.planes, s);
+    release(w.req, s); release(w.eaddr, s); release(w.cnt, s); release(w.lanes, s); release(w.lbase, s);
+    release(w.chunksum, s); release(w.chunkoff, s); release(w.stats, s); release(w.scan, s); release(w.misc0, s);
+    release(w.misc1, s); release(w.areas, s); release(w.sts, s); release(w.ssplit, s); release(w.saddr, s);
+    release(w.roff, s); release(w.careas, s); release(w.csets, s); release(w.ranges, s);
+    if (w.host) {
+        cudaStreamSynchronize(s);
+        cudaFreeHost(w.host);
+        w.host = nullptr;
+    }
 }
 
 static int check_device()

@@ -18,6 +18,7 @@
 //    scalar copies, and no level allocates more than it needs.
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <vector>
 
 #include "kdgb_internal.cuh"
@@ -105,40 +106,113 @@ __global__ void k_level_init(int32_t R, int32_t active, const float4 *__restrict
     cnt[2 * k + 1] = 0;
 }
 
+// The per-reference passes (k_reduce, k_count, k_scatter) walk the reference
+// array in warp chunks of kRows rows of 32 consecutive references.  Owners
+// are sorted, so most rows belong to one node: a warp keeps per-lane
+// accumulators while the owner stays the same and only reduces and issues
+// atomics when it changes, which keeps atomic traffic to a few per node per
+// chunk even at the root, where every reference has the same owner.
+constexpr int kRows = 16;
+constexpr int kChunk = 32 * kRows;                   // references per warp
+constexpr int kWarps = kBlock / 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+inline int64_t chunks_for(int64_t n) { return (n + kChunk - 1) / kChunk; }
+inline unsigned chunk_blocks(int64_t nch) { return (unsigned)((nch + kWarps - 1) / kWarps); }
+
+__device__ __forceinline__ void keys_atomic(unsigned *keys, int o, const unsigned (&k)[6])
+{
+    unsigned *kk = keys + 6 * (int64_t)o;
+    atomicMin(kk + 0, k[0]); atomicMin(kk + 1, k[1]); atomicMin(kk + 2, k[2]);
+    atomicMax(kk + 3, k[3]); atomicMax(kk + 4, k[4]); atomicMax(kk + 5, k[5]);
+}
+
+__device__ __forceinline__ void keys_reduce(unsigned mask, unsigned (&k)[6])
+{
+    k[0] = __reduce_min_sync(mask, k[0]); k[1] = __reduce_min_sync(mask, k[1]); k[2] = __reduce_min_sync(mask, k[2]);
+    k[3] = __reduce_max_sync(mask, k[3]); k[4] = __reduce_max_sync(mask, k[4]); k[5] = __reduce_max_sync(mask, k[5]);
+}
+
+__device__ __forceinline__ void keys_neutral(unsigned (&k)[6])
+{
+    k[0] = k[1] = k[2] = 0xffffffffu;
+    k[3] = k[4] = k[5] = 0u;
+}
+
 // Tight node boxes: exact min/max over each node's references, as the
 // segmented reduction ReduceSegmentsUnrolled + FinalSegmentedReduce
-// (ReduceSegments.h:230-371) computes.
+// (ReduceSegments.h:230-371) computes.  Keys are order-preserving uint32
+// images of the floats, so atomicMin/atomicMax give exact results in any order.
 __global__ void __launch_bounds__(kBlock) k_reduce(int64_t N, const float4 *__restrict__ cmin,
                                                   const float4 *__restrict__ cmax,
                                                   unsigned *__restrict__ keys)
 {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned lane = threadIdx.x & 31;
-    int owner = -1;
-    unsigned k[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
-    if (r < N) {
-        const float4 a = cmin[r], b = cmax[r];
-        owner = __float_as_int(b.w);
-        k[0] = fkey(a.x); k[1] = fkey(a.y); k[2] = fkey(a.z);
-        k[3] = fkey(b.x); k[4] = fkey(b.y); k[5] = fkey(b.z);
-    }
-    const int o0 = __shfl_sync(0xffffffffu, owner, 0);
-    if (__all_sync(0xffffffffu, owner == o0) && o0 >= 0) {
-        const unsigned m0 = __reduce_min_sync(0xffffffffu, k[0]);
-        const unsigned m1 = __reduce_min_sync(0xffffffffu, k[1]);
-        const unsigned m2 = __reduce_min_sync(0xffffffffu, k[2]);
-        const unsigned x0 = __reduce_max_sync(0xffffffffu, k[3]);
-        const unsigned x1 = __reduce_max_sync(0xffffffffu, k[4]);
-        const unsigned x2 = __reduce_max_sync(0xffffffffu, k[5]);
-        if (lane == 0) {
-            unsigned *kk = keys + 6 * (int64_t)o0;
-            atomicMin(kk + 0, m0); atomicMin(kk + 1, m1); atomicMin(kk + 2, m2);
-            atomicMax(kk + 3, x0); atomicMax(kk + 4, x1); atomicMax(kk + 5, x2);
+    __shared__ int s_owner[kWarps];
+    __shared__ unsigned s_keys[kWarps][6];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kChunk;
+    int cw = -1;
+    unsigned acc[6];
+    keys_neutral(acc);
+    for (int row = 0; row < kRows; ++row) {
+        const int64_t r0 = base + row * 32;
+        if (r0 >= N) break;
+        const int64_t r = r0 + lane;
+        int o = -1;
+        unsigned k[6];
+        keys_neutral(k);
+        if (r < N) {
+            const float4 a = cmin[r], b = cmax[r];
+            o = __float_as_int(b.w);
+            k[0] = fkey(a.x); k[1] = fkey(a.y); k[2] = fkey(a.z);
+            k[3] = fkey(b.x); k[4] = fkey(b.y); k[5] = fkey(b.z);
         }
-    } else if (owner >= 0) {
-        unsigned *kk = keys + 6 * (int64_t)owner;
-        atomicMin(kk + 0, k[0]); atomicMin(kk + 1, k[1]); atomicMin(kk + 2, k[2]);
-        atomicMax(kk + 3, k[3]); atomicMax(kk + 4, k[4]); atomicMax(kk + 5, k[5]);
+        const unsigned m = __match_any_sync(kFull, o);
+        if (m == kFull && o == cw) {
+            acc[0] = min(acc[0], k[0]); acc[1] = min(acc[1], k[1]); acc[2] = min(acc[2], k[2]);
+            acc[3] = max(acc[3], k[3]); acc[4] = max(acc[4], k[4]); acc[5] = max(acc[5], k[5]);
+            continue;
+        }
+        if (cw >= 0) {
+            keys_reduce(kFull, acc);
+            if (lane == 0) keys_atomic(keys, cw, acc);
+        }
+        if (m == kFull && o >= 0) {
+            cw = o;
+            for (int j = 0; j < 6; ++j) acc[j] = k[j];
+        } else {
+            if (o >= 0) {
+                keys_reduce(m, k);
+                if (lane == (unsigned)(__ffs(m) - 1)) keys_atomic(keys, o, k);
+            }
+            cw = -1;
+            keys_neutral(acc);
+        }
+    }
+    if (cw >= 0) keys_reduce(kFull, acc);
+    if (lane == 0) {
+        s_owner[warp] = cw;
+        for (int j = 0; j < 6; ++j) s_keys[warp][j] = acc[j];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // Consecutive warps cover consecutive chunks: merge equal owners.
+        int o = -1;
+        unsigned k[6];
+        keys_neutral(k);
+        for (int w = 0; w < kWarps; ++w) {
+            const int ow = s_owner[w];
+            if (ow < 0) continue;
+            if (ow != o) {
+                if (o >= 0) keys_atomic(keys, o, k);
+                o = ow;
+                for (int j = 0; j < 6; ++j) k[j] = s_keys[w][j];
+            } else {
+                for (int j = 0; j < 3; ++j) k[j] = min(k[j], s_keys[w][j]);
+                for (int j = 3; j < 6; ++j) k[j] = max(k[j], s_keys[w][j]);
+            }
+        }
+        if (o >= 0) keys_atomic(keys, o, k);
     }
 }
 
@@ -247,40 +321,62 @@ __device__ __forceinline__ void ref_flags(const float4 &a, const float4 &b, int 
     Rf = sp < axis_of4(b, axis);
 }
 
-// Per-node left/right counts and per-block totals of the flags.
+// Per-node left/right counts and per-chunk totals of the flags (the chunk
+// totals are scanned into each warp chunk's global offsets for k_scatter).
 __global__ void __launch_bounds__(kBlock) k_count(int64_t N, int32_t active, const float4 *__restrict__ cmin,
                                                  const float4 *__restrict__ cmax, const float *__restrict__ split,
                                                  const int8_t *__restrict__ info, int32_t *__restrict__ cnt,
-                                                 int32_t *__restrict__ blocksum)
+                                                 int32_t *__restrict__ chunksum)
 {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int owner = -1, L = 0, Rf = 0;
-    if (r < N) {
-        const float4 a = cmin[r], b = cmax[r];
-        owner = __float_as_int(b.w);
-        const int node = active + owner;
-        ref_flags(a, b, info[node], split[node], L, Rf);
-    }
-    const int o0 = __shfl_sync(0xffffffffu, owner, 0);
-    const int wl = __reduce_add_sync(0xffffffffu, L), wr = __reduce_add_sync(0xffffffffu, Rf);
-    if (__all_sync(0xffffffffu, owner == o0) && o0 >= 0) {
-        if (lane == 0) {
-            atomicAdd(cnt + 2 * o0, wl);
-            atomicAdd(cnt + 2 * o0 + 1, wr);
+    const unsigned lane = threadIdx.x & 31;
+    const int64_t chunk = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t base = chunk * kChunk;
+    if (base >= N) return;  // warp-uniform
+    int cw = -1, al = 0, ar = 0, tl = 0, tr = 0;
+    for (int row = 0; row < kRows; ++row) {
+        const int64_t r0 = base + row * 32;
+        if (r0 >= N) break;
+        const int64_t r = r0 + lane;
+        int o = -1, L = 0, Rf = 0;
+        if (r < N) {
+            const float4 a = cmin[r], b = cmax[r];
+            o = __float_as_int(b.w);
+            const int node = active + o;
+            ref_flags(a, b, info[node], split[node], L, Rf);
         }
-    } else if (owner >= 0) {
-        if (L) atomicAdd(cnt + 2 * owner, 1);
-        if (Rf) atomicAdd(cnt + 2 * owner + 1, 1);
+        tl += L;
+        tr += Rf;
+        const unsigned m = __match_any_sync(kFull, o);
+        if (m == kFull && o == cw) {
+            al += L;
+            ar += Rf;
+            continue;
+        }
+        if (cw >= 0) {
+            al = __reduce_add_sync(kFull, al);
+            ar = __reduce_add_sync(kFull, ar);
+            if (lane == 0) { atomicAdd(cnt + 2 * cw, al); atomicAdd(cnt + 2 * cw + 1, ar); }
+        }
+        if (m == kFull && o >= 0) {
+            cw = o; al = L; ar = Rf;
+        } else {
+            if (o >= 0) {
+                const int gl = __reduce_add_sync(m, L), gr = __reduce_add_sync(m, Rf);
+                if (lane == (unsigned)(__ffs(m) - 1)) { atomicAdd(cnt + 2 * o, gl); atomicAdd(cnt + 2 * o + 1, gr); }
+            }
+            cw = -1; al = 0; ar = 0;
+        }
     }
-    __shared__ int32_t s[2][kBlock / 32];
-    if (lane == 0) { s[0][warp] = wl; s[1][warp] = wr; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int32_t tl = 0, tr = 0;
-        for (int w = 0; w < kBlock / 32; ++w) { tl += s[0][w]; tr += s[1][w]; }
-        blocksum[2 * (int64_t)blockIdx.x] = tl;
-        blocksum[2 * (int64_t)blockIdx.x + 1] = tr;
+    if (cw >= 0) {
+        al = __reduce_add_sync(kFull, al);
+        ar = __reduce_add_sync(kFull, ar);
+        if (lane == 0) { atomicAdd(cnt + 2 * cw, al); atomicAdd(cnt + 2 * cw + 1, ar); }
+    }
+    tl = __reduce_add_sync(kFull, tl);
+    tr = __reduce_add_sync(kFull, tr);
+    if (lane == 0) {
+        chunksum[2 * chunk] = tl;
+        chunksum[2 * chunk + 1] = tr;
     }
 }
 
@@ -297,39 +393,14 @@ __global__ void k_node_lanes(int32_t R, int32_t LS, const int32_t *__restrict__ 
     o[0] = l; o[1] = r; o[2] = ll ? l : 0; o[3] = rl ? r : 0; o[4] = ll; o[5] = rl;
 }
 
-// Partition + compaction of the references with clipping to the split plane
-// (SplitTriangles, TriangleUpperChildren.h:283-383).  Destination = node base
-// + rank of the reference among the node's left (right) references.
-__global__ void __launch_bounds__(kBlock) k_scatter(
-    int64_t N, int32_t R, int32_t active, int32_t LS, int32_t upper,
-    const float4 *__restrict__ cmin, const float4 *__restrict__ cmax, const float *__restrict__ split,
-    const int8_t *__restrict__ info, const int32_t *__restrict__ blockoff, const int32_t *__restrict__ lbase,
-    float4 *__restrict__ nmin, float4 *__restrict__ nmax, float4 *__restrict__ fmin, float4 *__restrict__ fmax)
+// Writes one reference to its child (or final leaf) slot: destination = node
+// base + rank among the node's left (right) references.
+__device__ __forceinline__ void scatter_one(int32_t R, int owner, int32_t LS, int32_t upper, int L, int Rf, int axis,
+                                            float sp, float4 a, float4 b, int32_t pl, int32_t pr,
+                                            const int32_t *__restrict__ lbase, float4 *__restrict__ nmin,
+                                            float4 *__restrict__ nmax, float4 *__restrict__ fmin,
+                                            float4 *__restrict__ fmax)
 {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int owner = -1, L = 0, Rf = 0, axis = 0;
-    float sp = 0.0f;
-    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-    if (r < N) {
-        a = cmin[r];
-        b = cmax[r];
-        owner = __float_as_int(b.w);
-        const int node = active + owner;
-        axis = info[node];
-        sp = split[node];
-        ref_flags(a, b, axis, sp, L, Rf);
-    }
-    const unsigned bl = __ballot_sync(0xffffffffu, L), br = __ballot_sync(0xffffffffu, Rf);
-    const unsigned below = (1u << lane) - 1u;
-    __shared__ int32_t s[2][kBlock / 32];
-    if (lane == 0) { s[0][warp] = __popc(bl); s[1][warp] = __popc(br); }
-    __syncthreads();
-    int32_t pl = blockoff[2 * (int64_t)blockIdx.x] + __popc(bl & below);
-    int32_t pr = blockoff[2 * (int64_t)blockIdx.x + 1] + __popc(br & below);
-    for (unsigned w = 0; w < warp; ++w) { pl += s[0][w]; pr += s[1][w]; }
-    if (owner < 0) return;
-
     const int32_t *lb = lbase + 6 * (int64_t)owner;
     const int32_t *tot = lbase + 6 * (int64_t)R;
     const int32_t total_l = tot[0], leaf_l = tot[2], leafnodes_l = tot[4];
@@ -362,6 +433,45 @@ __global__ void __launch_bounds__(kBlock) k_scatter(
             nmin[dst] = lo;
             nmax[dst] = make_float4(b.x, b.y, b.z, __int_as_float(R + owner - (leafnodes_l + lb[5])));
         }
+    }
+}
+
+// Partition + compaction of the references with clipping to the split plane
+// (SplitTriangles, TriangleUpperChildren.h:283-383).  Destination = node base
+// + rank of the reference among the node's left (right) references.
+__global__ void __launch_bounds__(kBlock) k_scatter(
+    int64_t N, int32_t R, int32_t active, int32_t LS, int32_t upper,
+    const float4 *__restrict__ cmin, const float4 *__restrict__ cmax, const float *__restrict__ split,
+    const int8_t *__restrict__ info, const int32_t *__restrict__ chunkoff, const int32_t *__restrict__ lbase,
+    float4 *__restrict__ nmin, float4 *__restrict__ nmax, float4 *__restrict__ fmin, float4 *__restrict__ fmax)
+{
+    const unsigned lane = threadIdx.x & 31;
+    const int64_t chunk = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t base = chunk * kChunk;
+    if (base >= N) return;  // warp-uniform
+    const unsigned below = (1u << lane) - 1u;
+    int32_t off_l = chunkoff[2 * chunk], off_r = chunkoff[2 * chunk + 1];
+    for (int row = 0; row < kRows; ++row) {
+        const int64_t r0 = base + row * 32;
+        if (r0 >= N) break;
+        const int64_t r = r0 + lane;
+        int owner = -1, L = 0, Rf = 0, axis = 0;
+        float sp = 0.0f;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+        if (r < N) {
+            a = cmin[r];
+            b = cmax[r];
+            owner = __float_as_int(b.w);
+            const int node = active + owner;
+            axis = info[node];
+            sp = split[node];
+            ref_flags(a, b, axis, sp, L, Rf);
+        }
+        const unsigned bl = __ballot_sync(kFull, L), br = __ballot_sync(kFull, Rf);
+        const int32_t pl = off_l + __popc(bl & below), pr = off_r + __popc(br & below);
+        off_l += __popc(bl);
+        off_r += __popc(br);
+        if (owner >= 0) scatter_one(R, owner, LS, upper, L, Rf, axis, sp, a, b, pl, pr, lbase, nmin, nmax, fmin, fmax);
     }
 }
 
@@ -521,11 +631,11 @@ __global__ void k_sah_planes(int32_t nl, const int32_t *__restrict__ leaf_ids, c
     float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
     if (mine) { lo = fmin[pi + lane]; hi = fmax[pi + lane]; }
     unsigned sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sz[4] = {0, 0, 0, 0};
-    for (int j = 0; j < 32; ++j) {
+    for (unsigned bits = bmp; bits; bits &= bits - 1u) {  // bmp is warp-uniform
+        const int j = __ffs(bits) - 1;
         const float mnx = __shfl_sync(0xffffffffu, lo.x, j), mny = __shfl_sync(0xffffffffu, lo.y, j);
         const float mnz = __shfl_sync(0xffffffffu, lo.z, j), mxx = __shfl_sync(0xffffffffu, hi.x, j);
         const float mxy = __shfl_sync(0xffffffffu, hi.y, j), mxz = __shfl_sync(0xffffffffu, hi.z, j);
-        if (!((bmp >> j) & 1u)) continue;
         const unsigned m = 1u << j;
         sx[0] |= mnx <= lo.x ? m : 0; sx[1] |= lo.x < mxx ? m : 0;
         sx[2] |= mnx <= hi.x ? m : 0; sx[3] |= hi.x < mxx ? m : 0;
@@ -548,30 +658,20 @@ struct SahPick {
     int32_t idx;
 };
 
-// CalcAreaForSets (LowerTriangleMap.h:412-461) for one candidate slot.
-__device__ __forceinline__ void area_for_sets(int4 set, int axis, int32_t set_index, unsigned bmp,
-                                              const float a_lane, SahPick &best)
+// CalcAreaForSets (LowerTriangleMap.h:412-461) for the planes of one slot:
+// a0..a3 are the area sums of the four sets (accumulated in bit order by the
+// caller); low and high plane costs are tried in the reference's order.
+__device__ __forceinline__ void pick_planes(const unsigned (&s)[4], const float (&a)[4], int axis, int32_t set_index,
+                                            SahPick &best)
 {
-    unsigned s0 = (unsigned)set.x & bmp, s1 = (unsigned)set.y & bmp, s2 = (unsigned)set.z & bmp,
-             s3 = (unsigned)set.w & bmp;
-    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
-    for (int j = 0; j < 32; ++j) {
-        const float aj = __shfl_sync(0xffffffffu, a_lane, j);
-        if (!((bmp >> j) & 1u)) continue;
-        const unsigned m = 1u << j;
-        a0 = __fadd_rn(a0, (s0 & m) ? aj : 0.0f);
-        a1 = __fadd_rn(a1, (s1 & m) ? aj : 0.0f);
-        a2 = __fadd_rn(a2, (s2 & m) ? aj : 0.0f);
-        a3 = __fadd_rn(a3, (s3 & m) ? aj : 0.0f);
-    }
-    const float low = __fadd_rn(__fmul_rn((float)__popc(s0), a0), __fmul_rn((float)__popc(s1), a1));
-    const float high = __fadd_rn(__fmul_rn((float)__popc(s2), a2), __fmul_rn((float)__popc(s3), a3));
+    const float low = __fadd_rn(__fmul_rn((float)__popc(s[0]), a[0]), __fmul_rn((float)__popc(s[1]), a[1]));
+    const float high = __fadd_rn(__fmul_rn((float)__popc(s[2]), a[2]), __fmul_rn((float)__popc(s[3]), a[3]));
     if (low < best.cost) {
-        best.cost = low; best.ls = s0; best.rs = s1; best.la = a0; best.ra = a1;
+        best.cost = low; best.ls = s[0]; best.rs = s[1]; best.la = a[0]; best.ra = a[1];
         best.axis = axis; best.idx = set_index;
     }
     if (high < best.cost) {
-        best.cost = high; best.ls = s2; best.rs = s3; best.la = a2; best.ra = a3;
+        best.cost = high; best.ls = s[2]; best.rs = s[3]; best.la = a[2]; best.ra = a[3];
         best.axis = axis; best.idx = (int32_t)((unsigned)set_index | 0x80000000u);
     }
 }
@@ -601,9 +701,24 @@ __global__ void k_calc_sah(int32_t R, const int32_t *__restrict__ ids, int32_t a
     const int4 sy = mine ? sts[F + pi + lane] : zero4;
     const int4 sz = mine ? sts[2 * F + pi + lane] : zero4;
     SahPick mb = best;
-    area_for_sets(sx, KDGB_X, pi + lane, bmp, a_lane, mb);
-    area_for_sets(sy, KDGB_Y, pi + lane, bmp, a_lane, mb);
-    area_for_sets(sz, KDGB_Z, pi + lane, bmp, a_lane, mb);
+    // One pass over the node's references in bit order accumulates the area
+    // sums of all twelve sets (3 axes x {lowLeft, lowRight, highLeft, highRight}).
+    unsigned st[3][4] = {{(unsigned)sx.x & bmp, (unsigned)sx.y & bmp, (unsigned)sx.z & bmp, (unsigned)sx.w & bmp},
+                         {(unsigned)sy.x & bmp, (unsigned)sy.y & bmp, (unsigned)sy.z & bmp, (unsigned)sy.w & bmp},
+                         {(unsigned)sz.x & bmp, (unsigned)sz.y & bmp, (unsigned)sz.z & bmp, (unsigned)sz.w & bmp}};
+    float ar[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    for (unsigned bits = bmp; bits; bits &= bits - 1u) {  // bmp is warp-uniform
+        const int j = __ffs(bits) - 1;
+        const float aj = __shfl_sync(0xffffffffu, a_lane, j);
+        const unsigned m = 1u << j;
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) ar[x][c] = __fadd_rn(ar[x][c], (st[x][c] & m) ? aj : 0.0f);
+    }
+    pick_planes(st[0], ar[0], KDGB_X, pi + lane, mb);
+    pick_planes(st[1], ar[1], KDGB_Y, pi + lane, mb);
+    pick_planes(st[2], ar[2], KDGB_Z, pi + lane, mb);
     if (!mine) mb.cost = KDGB_FINF, mb.idx = -1;
     // Warp argmin on (cost, lane); only lanes whose cost beat fInfinity count.
     float c = mine && mb.cost < KDGB_FINF ? mb.cost : INFINITY;
@@ -664,27 +779,6 @@ __global__ void k_sah_children(int32_t R, const int32_t *__restrict__ ids, int32
 // Host side.
 // ---------------------------------------------------------------------------
 
-struct Pinned {
-    int32_t *p = nullptr;
-    ~Pinned() { if (p) cudaFreeHost(p); }
-};
-
-template <class T>
-struct Scratch {
-    T *p = nullptr;
-    cudaStream_t s = 0;
-    ~Scratch() { if (p) cudaFreeAsync(p, s); }
-};
-
-template <class T>
-int alloc_scratch(Scratch<T> &a, int64_t n, cudaStream_t s)
-{
-    if (a.p) { cudaFreeAsync(a.p, s); a.p = nullptr; }
-    a.s = s;
-    KDGB_CUDA(cudaMallocAsync(&a.p, sizeof(T) * (size_t)(n > 0 ? n : 1), s));
-    return KDGB_OK;
-}
-
 int grow_nodes(Tree &t, int64_t need, cudaStream_t s)
 {
     const int64_t keep = t.n_nodes;
@@ -705,49 +799,52 @@ int grow_nodes(Tree &t, int64_t need, cudaStream_t s)
 
 #define NODE_ARGS t.info.p, t.split.p, t.bmin.p, t.bmax.p, t.pidx.p, t.bitmap.p, t.children.p, t.area.p, t.parent.p
 
-int lower_sah(Tree &t, const kdgb_build_params &p, const float4 *fmin, const float4 *fmax, int32_t F,
-              cudaStream_t s, int32_t *host_rec)
+int host_record(Workspace &ws)
 {
+    if (!ws.host) KDGB_CUDA(cudaMallocHost(&ws.host, kHostRec * sizeof(int32_t)));
+    return KDGB_OK;
+}
+
+int lower_sah(Tree &t, const kdgb_build_params &p, const float4 *fmin, const float4 *fmax, int32_t F,
+              cudaStream_t s)
+{
+    Workspace &w = t.ws;
     const int32_t nl = t.n_upper_leaves;
-    Scratch<float> areas;
-    Scratch<int4> sts;
-    KDGB_CHECK(alloc_scratch(areas, F, s));
-    KDGB_CHECK(alloc_scratch(sts, 3 * (int64_t)F, s));
+    KDGB_CHECK(grab(w.areas, F, s));
+    KDGB_CHECK(grab(w.sts, 3 * (int64_t)F, s));
     if (F > 0) {
-        k_areas<<<blocks_for(F), kBlock, 0, s>>>(F, t.prim_indices.p, t.p0.p, t.p1.p, t.p2.p, areas.p);
+        k_areas<<<blocks_for(F), kBlock, 0, s>>>(F, t.prim_indices.p, t.p0.p, t.p1.p, t.p2.p, w.areas.p);
         KDGB_LAUNCH_CHECK();
     }
     if (nl > 0) {
-        k_sah_preprocess<<<blocks_for(nl), kBlock, 0, s>>>(nl, t.leaf_ids.p, t.pidx.p, t.bitmap.p, t.area.p, areas.p);
+        k_sah_preprocess<<<blocks_for(nl), kBlock, 0, s>>>(nl, t.leaf_ids.p, t.pidx.p, t.bitmap.p, t.area.p,
+                                                           w.areas.p);
         KDGB_LAUNCH_CHECK();
         k_sah_planes<<<blocks_for((int64_t)nl * 32), kBlock, 0, s>>>(nl, t.leaf_ids.p, t.pidx.p, t.bitmap.p, fmin,
-                                                                   fmax, F, sts.p);
+                                                                   fmax, F, w.sts.p);
         KDGB_LAUNCH_CHECK();
     }
     int32_t R = nl, active = t.n_nodes, lv = 0;
     const int32_t *ids = t.leaf_ids.p;
-    Scratch<int32_t> ssplit, saddr;
-    Scratch<float2> careas;
-    Scratch<int2> csets;
     while (R > 0) {
         ++lv;
-        KDGB_CHECK(alloc_scratch(ssplit, R, s));
-        KDGB_CHECK(alloc_scratch(saddr, R + 1, s));
-        KDGB_CHECK(alloc_scratch(careas, R, s));
-        KDGB_CHECK(alloc_scratch(csets, R, s));
+        KDGB_CHECK(grab(w.ssplit, R, s));
+        KDGB_CHECK(grab(w.saddr, (int64_t)R + 1, s));
+        KDGB_CHECK(grab(w.careas, R, s));
+        KDGB_CHECK(grab(w.csets, R, s));
         k_calc_sah<<<blocks_for((int64_t)R * 32), kBlock, 0, s>>>(
-            R, ids, active, t.pidx.p, t.bitmap.p, t.area.p, areas.p, fmin, fmax, sts.p, F, p.traversal_cost,
-            p.intersection_cost, p.min_leaf, t.info.p, t.split.p, ssplit.p, careas.p, csets.p);
+            R, ids, active, t.pidx.p, t.bitmap.p, t.area.p, w.areas.p, fmin, fmax, w.sts.p, F, p.traversal_cost,
+            p.intersection_cost, p.min_leaf, t.info.p, t.split.p, w.ssplit.p, w.careas.p, w.csets.p);
         KDGB_LAUNCH_CHECK();
-        KDGB_CHECK(scan_exclusive<1>(ssplit.p, saddr.p, R, s));
-        KDGB_CUDA(cudaMemcpyAsync(host_rec, saddr.p + R, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        KDGB_CHECK(scan_exclusive<1>(w.ssplit.p, w.saddr.p, R, s, &w.scan));
+        KDGB_CUDA(cudaMemcpyAsync(w.host, w.saddr.p + R, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         KDGB_CUDA(cudaStreamSynchronize(s));
-        const int32_t splits = host_rec[0];
+        const int32_t splits = w.host[0];
         const int32_t child_base = t.n_nodes;
         KDGB_CHECK(grow_nodes(t, (int64_t)t.n_nodes + 2 * (int64_t)splits, s));
         if (splits > 0) {
-            k_sah_children<<<blocks_for(R), kBlock, 0, s>>>(R, ids, active, child_base, ssplit.p, saddr.p, careas.p,
-                                                           csets.p, p.propagate_aabbs, NODE_ARGS);
+            k_sah_children<<<blocks_for(R), kBlock, 0, s>>>(R, ids, active, child_base, w.ssplit.p, w.saddr.p,
+                                                           w.careas.p, w.csets.p, p.propagate_aabbs, NODE_ARGS);
             KDGB_LAUNCH_CHECK();
         }
         t.n_nodes += 2 * splits;
@@ -768,38 +865,37 @@ int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s)
     KDGB_CHECK(ensure(t.p2, T, s));
     t.n_tris = T;
     if (T == 0) return KDGB_OK;
-    Scratch<int> err;
-    KDGB_CHECK(alloc_scratch(err, 1, s));
-    KDGB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
-    k_load_geometry<<<blocks_for(T), kBlock, 0, s>>>(tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, nullptr, nullptr, err.p);
+    Workspace &w = t.ws;
+    KDGB_CHECK(host_record(w));
+    KDGB_CHECK(grab(w.stats, 16, s));
+    KDGB_CUDA(cudaMemsetAsync(w.stats.p, 0, sizeof(int), s));
+    k_load_geometry<<<blocks_for(T), kBlock, 0, s>>>(tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, nullptr, nullptr, w.stats.p);
     KDGB_LAUNCH_CHECK();
-    int h = 0;
-    KDGB_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    KDGB_CUDA(cudaMemcpyAsync(w.host, w.stats.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     KDGB_CUDA(cudaStreamSynchronize(s));
-    if (h) return fail(KDGB_ERR_NONFINITE, "non-finite vertex coordinate");
+    if (w.host[0]) return fail(KDGB_ERR_NONFINITE, "non-finite vertex coordinate");
     return KDGB_OK;
 }
 
 int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p, cudaStream_t s)
 {
     const int32_t LS = p.leaf_size;
-    Pinned rec;
-    KDGB_CUDA(cudaMallocHost(&rec.p, 16 * sizeof(int32_t)));
+    Workspace &w = t.ws;
+    KDGB_CHECK(host_record(w));
+    int32_t *rec = w.host;
 
     // Geometry, primitive boxes and the root node.
     KDGB_CHECK(ensure(t.p0, T, s));
     KDGB_CHECK(ensure(t.p1, T, s));
     KDGB_CHECK(ensure(t.p2, T, s));
     t.n_tris = T;
-    Scratch<float4> cmin, cmax, nmin, nmax, fmin, fmax;
-    KDGB_CHECK(alloc_scratch(cmin, T, s));
-    KDGB_CHECK(alloc_scratch(cmax, T, s));
-    Scratch<int32_t> stats;
-    KDGB_CHECK(alloc_scratch(stats, 16, s));
-    KDGB_CUDA(cudaMemsetAsync(stats.p, 0, 16 * sizeof(int32_t), s));
+    KDGB_CHECK(grab(w.cmin, T, s));
+    KDGB_CHECK(grab(w.cmax, T, s));
+    KDGB_CHECK(grab(w.stats, 16, s));
+    KDGB_CUDA(cudaMemsetAsync(w.stats.p, 0, 16 * sizeof(int32_t), s));
     if (T > 0) {
-        k_load_geometry<<<blocks_for(T), kBlock, 0, s>>>(tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, cmin.p, cmax.p,
-                                                        stats.p + 15);
+        k_load_geometry<<<blocks_for(T), kBlock, 0, s>>>(tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, w.cmin.p, w.cmax.p,
+                                                        w.stats.p + 15);
         KDGB_LAUNCH_CHECK();
     }
     t.n_nodes = 0;
@@ -808,93 +904,81 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
     KDGB_LAUNCH_CHECK();
     t.n_nodes = 1;
 
-    int64_t N = T, F = 0, fcap = 0;
+    int64_t N = T, F = 0;
     int32_t active = 0, R = 1, level = 0;
     std::vector<int2> leaf_ranges;
     std::vector<int32_t> leaf_off;
     int32_t n_leaf_ids = 0;
 
-    Scratch<float4> pmin, pmax;
-    Scratch<unsigned> keys;
-    Scratch<int8_t> planes;
-    Scratch<int32_t> req, eaddr, cnt, lanes, lbase, blocksum, blockoff;
-
     while (R > 0) {
         if (level >= p.max_levels) return fail(KDGB_ERR_DEGENERATE, "upper build exceeded max_levels");
         ++level;
         const bool do_ess = p.split_empty_space && active != 0;
-        const int64_t nb = (N + kBlock - 1) / kBlock;
+        const int64_t nch = chunks_for(N);
+        const unsigned ngrid = chunk_blocks(nch);
         KDGB_CHECK(grow_nodes(t, (int64_t)t.n_nodes + 14 * (int64_t)R, s));
-        KDGB_CHECK(alloc_scratch(pmin, R, s));
-        KDGB_CHECK(alloc_scratch(pmax, R, s));
-        KDGB_CHECK(alloc_scratch(keys, 6 * (int64_t)R, s));
-        KDGB_CHECK(alloc_scratch(cnt, 2 * (int64_t)R, s));
-        KDGB_CHECK(alloc_scratch(lanes, 6 * (int64_t)R, s));
-        KDGB_CHECK(alloc_scratch(lbase, 6 * ((int64_t)R + 1), s));
-        KDGB_CHECK(alloc_scratch(blocksum, 2 * nb, s));
-        KDGB_CHECK(alloc_scratch(blockoff, 2 * (nb + 1), s));
-        KDGB_CHECK(alloc_scratch(nmin, 2 * N, s));
-        KDGB_CHECK(alloc_scratch(nmax, 2 * N, s));
-        if (F + 2 * N > fcap) {
-            const int64_t ncap = (F + 2 * N) * 3 / 2 + 1024;
-            Scratch<float4> a, b;
-            KDGB_CHECK(alloc_scratch(a, ncap, s));
-            KDGB_CHECK(alloc_scratch(b, ncap, s));
-            if (F > 0) {
-                KDGB_CUDA(cudaMemcpyAsync(a.p, fmin.p, sizeof(float4) * F, cudaMemcpyDeviceToDevice, s));
-                KDGB_CUDA(cudaMemcpyAsync(b.p, fmax.p, sizeof(float4) * F, cudaMemcpyDeviceToDevice, s));
-            }
-            std::swap(a.p, fmin.p);
-            std::swap(b.p, fmax.p);
-            fmin.s = fmax.s = s;
-            fcap = ncap;
+        KDGB_CHECK(grab(w.pmin, R, s));
+        KDGB_CHECK(grab(w.pmax, R, s));
+        KDGB_CHECK(grab(w.keys, 6 * (int64_t)R, s));
+        KDGB_CHECK(grab(w.cnt, 2 * (int64_t)R, s));
+        KDGB_CHECK(grab(w.lanes, 6 * (int64_t)R, s));
+        KDGB_CHECK(grab(w.lbase, 6 * ((int64_t)R + 1), s));
+        KDGB_CHECK(grab(w.chunksum, 2 * nch, s));
+        KDGB_CHECK(grab(w.chunkoff, 2 * (nch + 1), s));
+        KDGB_CHECK(grab(w.nmin, 2 * N, s));
+        KDGB_CHECK(grab(w.nmax, 2 * N, s));
+        if (F + 2 * N > w.fmin.cap) {
+            const int64_t want = (F + 2 * N) * 3 / 2 + 1024;
+            KDGB_CHECK(ensure(w.fmin, want, s, F));
+            KDGB_CHECK(ensure(w.fmax, want, s, F));
         }
 
-        k_level_init<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.bmin.p, t.bmax.p, pmin.p, pmax.p, keys.p, cnt.p);
+        k_level_init<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.bmin.p, t.bmax.p, w.pmin.p, w.pmax.p, w.keys.p,
+                                                      w.cnt.p);
         KDGB_LAUNCH_CHECK();
         if (N > 0) {
-            k_reduce<<<(unsigned)nb, kBlock, 0, s>>>(N, cmin.p, cmax.p, keys.p);
+            k_reduce<<<ngrid, kBlock, 0, s>>>(N, w.cmin.p, w.cmax.p, w.keys.p);
             KDGB_LAUNCH_CHECK();
         }
         if (do_ess) {
-            KDGB_CHECK(alloc_scratch(planes, R, s));
-            KDGB_CHECK(alloc_scratch(req, R, s));
-            KDGB_CHECK(alloc_scratch(eaddr, (int64_t)R + 1, s));
+            KDGB_CHECK(grab(w.planes, R, s));
+            KDGB_CHECK(grab(w.req, R, s));
+            KDGB_CHECK(grab(w.eaddr, (int64_t)R + 1, s));
         }
-        k_node_split<<<blocks_for(R), kBlock, 0, s>>>(R, active, do_ess, p.empty_space_threshold, pmin.p, pmax.p,
-                                                      keys.p, t.bmin.p, t.bmax.p, t.split.p, t.info.p,
-                                                      do_ess ? planes.p : nullptr, do_ess ? req.p : nullptr);
+        k_node_split<<<blocks_for(R), kBlock, 0, s>>>(R, active, do_ess, p.empty_space_threshold, w.pmin.p, w.pmax.p,
+                                                      w.keys.p, t.bmin.p, t.bmax.p, t.split.p, t.info.p,
+                                                      do_ess ? w.planes.p : nullptr, do_ess ? w.req.p : nullptr);
         KDGB_LAUNCH_CHECK();
         if (do_ess) {
-            KDGB_CHECK(scan_exclusive<1>(req.p, eaddr.p, R, s));
-            k_ess_chain<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.n_nodes, p.esc_zmax_as_x, planes.p, eaddr.p,
+            KDGB_CHECK(scan_exclusive<1>(w.req.p, w.eaddr.p, R, s, &w.scan));
+            k_ess_chain<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.n_nodes, p.esc_zmax_as_x, w.planes.p, w.eaddr.p,
                                                          NODE_ARGS);
             KDGB_LAUNCH_CHECK();
         }
         if (N > 0) {
-            k_count<<<(unsigned)nb, kBlock, 0, s>>>(N, active, cmin.p, cmax.p, t.split.p, t.info.p, cnt.p,
-                                                    blocksum.p);
+            k_count<<<ngrid, kBlock, 0, s>>>(N, active, w.cmin.p, w.cmax.p, t.split.p, t.info.p, w.cnt.p,
+                                             w.chunksum.p);
             KDGB_LAUNCH_CHECK();
         }
-        KDGB_CHECK(scan_exclusive<2>(blocksum.p, blockoff.p, nb, s));
-        k_node_lanes<<<blocks_for(R), kBlock, 0, s>>>(R, LS, cnt.p, lanes.p);
+        KDGB_CHECK(scan_exclusive<2>(w.chunksum.p, w.chunkoff.p, nch, s, &w.scan));
+        k_node_lanes<<<blocks_for(R), kBlock, 0, s>>>(R, LS, w.cnt.p, w.lanes.p);
         KDGB_LAUNCH_CHECK();
-        KDGB_CHECK(scan_exclusive<6>(lanes.p, lbase.p, R, s));
+        KDGB_CHECK(scan_exclusive<6>(w.lanes.p, w.lbase.p, R, s, &w.scan));
         if (N > 0) {
-            k_scatter<<<(unsigned)nb, kBlock, 0, s>>>(N, R, active, LS, (int32_t)F, cmin.p, cmax.p, t.split.p,
-                                                      t.info.p, blockoff.p, lbase.p, nmin.p, nmax.p, fmin.p, fmax.p);
+            k_scatter<<<ngrid, kBlock, 0, s>>>(N, R, active, LS, (int32_t)F, w.cmin.p, w.cmax.p, t.split.p, t.info.p,
+                                               w.chunkoff.p, w.lbase.p, w.nmin.p, w.nmax.p, w.fmin.p, w.fmax.p);
             KDGB_LAUNCH_CHECK();
         }
-        k_children<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.n_nodes, do_ess ? eaddr.p + R : nullptr, LS,
-                                                    (int32_t)F, p.split_empty_space, lbase.p, NODE_ARGS, stats.p);
+        k_children<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.n_nodes, do_ess ? w.eaddr.p + R : nullptr, LS,
+                                                    (int32_t)F, p.split_empty_space, w.lbase.p, NODE_ARGS, w.stats.p);
         KDGB_LAUNCH_CHECK();
-        KDGB_CUDA(cudaMemcpyAsync(rec.p, stats.p, 16 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        KDGB_CUDA(cudaMemcpyAsync(rec, w.stats.p, 16 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         KDGB_CUDA(cudaStreamSynchronize(s));
-        if (rec.p[15]) return fail(KDGB_ERR_NONFINITE, "non-finite vertex coordinate");
+        if (rec[15]) return fail(KDGB_ERR_NONFINITE, "non-finite vertex coordinate");
 
-        const int32_t empty = rec.p[0];
-        const int64_t total_l = rec.p[1], total_r = rec.p[2], leaf_l = rec.p[3], leaf_r = rec.p[4];
-        const int32_t leaf_nodes = rec.p[5] + rec.p[6];
+        const int32_t empty = rec[0];
+        const int64_t total_l = rec[1], total_r = rec[2], leaf_l = rec[3], leaf_r = rec[4];
+        const int32_t leaf_nodes = rec[5] + rec[6];
         if (total_l + total_r < N) return fail(KDGB_ERR_DEGENERATE, "split produced fewer references than its input");
         const int32_t child_start = t.n_nodes + empty;
         if (leaf_nodes > 0) {
@@ -905,8 +989,8 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
         t.n_nodes += empty + 2 * R;
         F += leaf_l + leaf_r;
         const int32_t created = 2 * R - leaf_nodes;
-        std::swap(cmin.p, nmin.p);
-        std::swap(cmax.p, nmax.p);
+        std::swap(w.cmin, w.nmin);
+        std::swap(w.cmax, w.nmax);
         N = total_l + total_r - leaf_l - leaf_r;
         active = t.n_nodes - created;
         R = created;
@@ -920,18 +1004,26 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
     KDGB_CHECK(ensure(t.prim_indices, F, s));
     if (n_leaf_ids > 0) {
         const int nr = (int)leaf_ranges.size();
-        Scratch<int2> dr;
-        Scratch<int32_t> doff;
-        KDGB_CHECK(alloc_scratch(dr, nr, s));
-        KDGB_CHECK(alloc_scratch(doff, nr, s));
-        KDGB_CUDA(cudaMemcpyAsync(dr.p, leaf_ranges.data(), sizeof(int2) * nr, cudaMemcpyHostToDevice, s));
-        KDGB_CUDA(cudaMemcpyAsync(doff.p, leaf_off.data(), sizeof(int32_t) * nr, cudaMemcpyHostToDevice, s));
-        k_leaf_ids<<<blocks_for(n_leaf_ids), kBlock, 0, s>>>(dr.p, nr, doff.p, n_leaf_ids, t.leaf_ids.p);
+        if (2 * nr + nr > kHostRec) {
+            // More leaf-producing levels than the pinned record holds: copy
+            // from pageable memory (synchronous for the host).
+            KDGB_CHECK(grab(w.ranges, nr, s));
+            KDGB_CHECK(grab(w.roff, nr, s));
+            KDGB_CUDA(cudaMemcpy(w.ranges.p, leaf_ranges.data(), sizeof(int2) * nr, cudaMemcpyHostToDevice));
+            KDGB_CUDA(cudaMemcpy(w.roff.p, leaf_off.data(), sizeof(int32_t) * nr, cudaMemcpyHostToDevice));
+        } else {
+            KDGB_CHECK(grab(w.ranges, nr, s));
+            KDGB_CHECK(grab(w.roff, nr, s));
+            std::memcpy(rec, leaf_ranges.data(), sizeof(int2) * nr);
+            std::memcpy(rec + 2 * nr, leaf_off.data(), sizeof(int32_t) * nr);
+            KDGB_CUDA(cudaMemcpyAsync(w.ranges.p, rec, sizeof(int2) * nr, cudaMemcpyHostToDevice, s));
+            KDGB_CUDA(cudaMemcpyAsync(w.roff.p, rec + 2 * nr, sizeof(int32_t) * nr, cudaMemcpyHostToDevice, s));
+        }
+        k_leaf_ids<<<blocks_for(n_leaf_ids), kBlock, 0, s>>>(w.ranges.p, nr, w.roff.p, n_leaf_ids, t.leaf_ids.p);
         KDGB_LAUNCH_CHECK();
-        KDGB_CUDA(cudaStreamSynchronize(s));  // host tables go out of scope
     }
     if (F > 0) {
-        k_extract_indices<<<blocks_for(F), kBlock, 0, s>>>((int32_t)F, fmin.p, t.prim_indices.p);
+        k_extract_indices<<<blocks_for(F), kBlock, 0, s>>>((int32_t)F, w.fmin.p, t.prim_indices.p);
         KDGB_LAUNCH_CHECK();
     }
     if (!p.split_empty_space && p.propagate_aabbs && n_leaf_ids > 0) {
@@ -942,7 +1034,10 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
 
     t.stats.lower_levels = 0;
     if (p.lower == KDGB_LOWER_SAH) {
-        KDGB_CHECK(lower_sah(t, p, fmin.p, fmax.p, (int32_t)F, s, rec.p));
+        // The SAH loop reuses the pinned record: wait until the range tables
+        // above have been read from it.
+        KDGB_CUDA(cudaStreamSynchronize(s));
+        KDGB_CHECK(lower_sah(t, p, w.fmin.p, w.fmax.p, (int32_t)F, s));
     } else if (n_leaf_ids > 0) {
         k_bitmap_leaves<<<blocks_for(n_leaf_ids), kBlock, 0, s>>>(n_leaf_ids, t.leaf_ids.p, t.info.p, t.bitmap.p);
         KDGB_LAUNCH_CHECK();

@@ -56,6 +56,31 @@ int ensure(DevArray<T> &a, int64_t n, cudaStream_t s, int64_t keep = 0, bool zer
 template <class T>
 void release(DevArray<T> &a, cudaStream_t s);
 
+// Scratch storage: grows geometrically (x1.5) and never keeps contents.
+template <class T>
+int grab(DevArray<T> &a, int64_t n, cudaStream_t s)
+{
+    if (a.p && n <= a.cap) return KDGB_OK;
+    const int64_t want = a.cap + a.cap / 2 > n ? a.cap + a.cap / 2 : n;
+    return ensure(a, want, s, 0, false);
+}
+
+// Per-handle build workspace, reused by every level and every rebuild so the
+// steady state issues no device allocations.
+struct Workspace {
+    DevArray<float4> cmin, cmax, nmin, nmax, fmin, fmax, pmin, pmax;
+    DevArray<unsigned> keys;
+    DevArray<int8_t> planes;
+    DevArray<int32_t> req, eaddr, cnt, lanes, lbase, chunksum, chunkoff, stats, scan, misc0, misc1;
+    DevArray<float> areas;
+    DevArray<int4> sts;
+    DevArray<int32_t> ssplit, saddr, roff;
+    DevArray<float2> careas;
+    DevArray<int2> csets, ranges;
+    int32_t *host = nullptr;  // pinned record buffer (kHostRec ints)
+};
+constexpr int kHostRec = 256;
+
 struct Tree {
     int32_t n_tris = 0;
     int32_t n_nodes = 0;
@@ -80,6 +105,8 @@ struct Tree {
     // triangle records (v0, e1, e2, id) of 48 bytes.
     DevArray<int4> tnode;
     DevArray<float4> ttri;
+
+    Workspace ws;
 };
 
 // Builders (kdgb_build.cu).  tri_v_dev: T*9 floats.
@@ -93,9 +120,10 @@ int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s);
 int pack_for_traversal(Tree &t, cudaStream_t s);
 
 // Device-wide exclusive scan of n records of K int32 lanes (lanes scanned
-// independently).  out has n+1 records; record n holds the totals.
+// independently).  out has n+1 records; record n holds the totals.  `ws`
+// (optional) holds the per-tile partials; without it they are allocated.
 template <int K>
-int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s);
+int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws = nullptr);
 
 // ---------------------------------------------------------------------------
 // Device helpers.

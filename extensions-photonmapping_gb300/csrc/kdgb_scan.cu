@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kThreads) scan_down_kernel(const int32_t *__re
 }  // namespace
 
 template <int K>
-int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s)
+int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws)
 {
     if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "scan: negative length");
     if (n == 0) {
@@ -179,7 +179,12 @@ int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s)
         return KDGB_OK;
     }
     int32_t *partial = nullptr;
-    KDGB_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * K * (size_t)nb, s));
+    if (ws) {
+        KDGB_CHECK(grab(*ws, K * nb, s));
+        partial = ws->p;
+    } else {
+        KDGB_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * K * (size_t)nb, s));
+    }
     scan_reduce_kernel<K><<<(unsigned)nb, kThreads, 0, s>>>(in, n, partial);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) {
@@ -190,14 +195,14 @@ int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s)
         scan_down_kernel<K><<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, partial);
         e = cudaGetLastError();
     }
-    cudaFreeAsync(partial, s);
+    if (!ws) cudaFreeAsync(partial, s);
     if (e != cudaSuccess) return cuda_fail(e, "scan kernels");
     note_launch(3);
     return KDGB_OK;
 }
 
-template int scan_exclusive<1>(const int32_t *, int32_t *, int64_t, cudaStream_t);
-template int scan_exclusive<2>(const int32_t *, int32_t *, int64_t, cudaStream_t);
-template int scan_exclusive<6>(const int32_t *, int32_t *, int64_t, cudaStream_t);
+template int scan_exclusive<1>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
+template int scan_exclusive<2>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
+template int scan_exclusive<6>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
 
 }  // namespace kdgb

@@ -56,28 +56,32 @@ __global__ void k_pack_nodes(int32_t n, const int8_t *__restrict__ info, const f
     }
 }
 
-// One warp per leaf: lane j handles bitmap bit j (LSB-first order).
+// One thread per node; a leaf writes its records in bitmap order (LSB first).
 __global__ void k_pack_tris(int32_t n, const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
                             const int32_t *__restrict__ pidx, const int32_t *__restrict__ prim_indices,
                             const float4 *__restrict__ p0, const float4 *__restrict__ p1,
                             const float4 *__restrict__ p2, const int32_t *__restrict__ off,
                             float4 *__restrict__ ttri)
 {
-    const int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned lane = threadIdx.x & 31;
+    const int32_t node = blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= n) return;
     if ((info[node] & 3) != KDGB_LEAF) return;
-    const unsigned bmp = (unsigned)bitmap[node];
-    if (!((bmp >> lane) & 1u)) return;
-    const int32_t rec = off[node] + __popc(bmp & ((1u << lane) - 1u));
-    const int32_t prim = prim_indices[pidx[node] + lane];
-    const float4 a = p0[prim], b = p1[prim], c = p2[prim];
-    const float3 v0 = make_float3(a.x, a.y, a.z);
-    const float3 e1 = sub3(make_float3(b.x, b.y, b.z), v0);
-    const float3 e2 = sub3(make_float3(c.x, c.y, c.z), v0);
-    ttri[3 * (int64_t)rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
-    ttri[3 * (int64_t)rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
-    ttri[3 * (int64_t)rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
+    unsigned bmp = (unsigned)bitmap[node];
+    const int32_t pi = pidx[node];
+    int64_t rec = off[node];
+    while (bmp) {
+        const int j = __ffs(bmp) - 1;
+        bmp &= bmp - 1u;
+        const int32_t prim = prim_indices[pi + j];
+        const float4 a = p0[prim], b = p1[prim], c = p2[prim];
+        const float3 v0 = make_float3(a.x, a.y, a.z);
+        const float3 e1 = sub3(make_float3(b.x, b.y, b.z), v0);
+        const float3 e2 = sub3(make_float3(c.x, c.y, c.z), v0);
+        ttri[3 * rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
+        ttri[3 * rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
+        ttri[3 * rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
+        ++rec;
+    }
 }
 
 struct Ctx {
@@ -380,39 +384,32 @@ __global__ void __launch_bounds__(kBruteBlock) k_brute(const float4 *__restrict_
 int pack_for_traversal(Tree &t, cudaStream_t s)
 {
     const int32_t n = t.n_nodes;
-    int32_t *cnt = nullptr, *off = nullptr;
-    KDGB_CUDA(cudaMallocAsync(&cnt, sizeof(int32_t) * (size_t)(n > 0 ? n : 1), s));
-    cudaError_t e = cudaMallocAsync(&off, sizeof(int32_t) * ((size_t)n + 1), s);
-    if (e != cudaSuccess) { cudaFreeAsync(cnt, s); return cuda_fail(e, "cudaMallocAsync"); }
-    int rc = KDGB_OK;
-    int32_t total = 0;
-    do {
-        if (n > 0) {
-            k_leaf_counts<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.bitmap.p, cnt);
-            if ((e = cudaGetLastError()) != cudaSuccess) { rc = cuda_fail(e, "k_leaf_counts"); break; }
-            note_launch();
-        }
-        if ((rc = scan_exclusive<1>(cnt, off, n, s)) != KDGB_OK) break;
-        if ((e = cudaMemcpyAsync(&total, off + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-            (e = cudaStreamSynchronize(s)) != cudaSuccess) {
-            rc = cuda_fail(e, "pack: total");
-            break;
-        }
-        if ((rc = ensure(t.tnode, n, s)) != KDGB_OK) break;
-        if ((rc = ensure(t.ttri, 3 * (int64_t)total, s)) != KDGB_OK) break;
-        t.n_leaf_tris = total;
-        if (n > 0) {
-            k_pack_nodes<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.split.p, t.children.p, off,
-                                                                         t.tnode.p);
-            k_pack_tris<<<blocks_for((int64_t)n * 32, kPackBlock), kPackBlock, 0, s>>>(
-                n, t.info.p, t.bitmap.p, t.pidx.p, t.prim_indices.p, t.p0.p, t.p1.p, t.p2.p, off, t.ttri.p);
-            if ((e = cudaGetLastError()) != cudaSuccess) { rc = cuda_fail(e, "pack kernels"); break; }
-            note_launch(2);
-        }
-    } while (0);
-    cudaFreeAsync(cnt, s);
-    cudaFreeAsync(off, s);
-    return rc;
+    Workspace &w = t.ws;
+    KDGB_CHECK(grab(w.misc0, n, s));
+    KDGB_CHECK(grab(w.misc1, (int64_t)n + 1, s));
+    if (!w.host) KDGB_CUDA(cudaMallocHost(&w.host, kHostRec * sizeof(int32_t)));
+    int32_t *cnt = w.misc0.p, *off = w.misc1.p;
+    if (n > 0) {
+        k_leaf_counts<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.bitmap.p, cnt);
+        KDGB_LAUNCH_CHECK();
+    }
+    KDGB_CHECK(scan_exclusive<1>(cnt, off, n, s, &w.scan));
+    KDGB_CUDA(cudaMemcpyAsync(w.host + kHostRec - 1, off + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    KDGB_CUDA(cudaStreamSynchronize(s));
+    const int32_t total = w.host[kHostRec - 1];
+    KDGB_CHECK(ensure(t.tnode, n, s));
+    KDGB_CHECK(ensure(t.ttri, 3 * (int64_t)total, s));
+    t.n_leaf_tris = total;
+    if (n > 0) {
+        k_pack_nodes<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.split.p, t.children.p, off,
+                                                                     t.tnode.p);
+        KDGB_LAUNCH_CHECK();
+        k_pack_tris<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.bitmap.p, t.pidx.p,
+                                                                    t.prim_indices.p, t.p0.p, t.p1.p, t.p2.p, off,
+                                                                    t.ttri.p);
+        KDGB_LAUNCH_CHECK();
+    }
+    return KDGB_OK;
 }
 
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
