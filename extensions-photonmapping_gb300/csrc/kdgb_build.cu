@@ -112,9 +112,10 @@ __global__ void k_level_init(int32_t R, int32_t active, const float4 *__restrict
 // accumulators while the owner stays the same and only reduces and issues
 // atomics when it changes, which keeps atomic traffic to a few per node per
 // chunk even at the root, where every reference has the same owner.
-constexpr int kRows = 16;
+constexpr int kRows = 4;
 constexpr int kChunk = 32 * kRows;                   // references per warp
 constexpr int kWarps = kBlock / 32;
+constexpr int kLanes = 7;  // per-node scan lanes (see k_node_lanes)
 constexpr unsigned kFull = 0xffffffffu;
 
 inline int64_t chunks_for(int64_t n) { return (n + kChunk - 1) / kChunk; }
@@ -154,16 +155,22 @@ __global__ void __launch_bounds__(kBlock) k_reduce(int64_t N, const float4 *__re
     int cw = -1;
     unsigned acc[6];
     keys_neutral(acc);
+    // Issue every row's loads before using any of them.
+    float4 ra[kRows], rb[kRows];
+#pragma unroll
     for (int row = 0; row < kRows; ++row) {
-        const int64_t r0 = base + row * 32;
-        if (r0 >= N) break;
-        const int64_t r = r0 + lane;
-        int o = -1;
+        const int64_t r = base + row * 32 + lane;
+        if (r < N) { ra[row] = cmin[r]; rb[row] = cmax[r]; }
+        else { rb[row].w = __int_as_float(-1); }
+    }
+#pragma unroll
+    for (int row = 0; row < kRows; ++row) {
+        if (base + row * 32 >= N) break;
+        const int o = __float_as_int(rb[row].w);
         unsigned k[6];
         keys_neutral(k);
-        if (r < N) {
-            const float4 a = cmin[r], b = cmax[r];
-            o = __float_as_int(b.w);
+        if (o >= 0) {
+            const float4 a = ra[row], b = rb[row];
             k[0] = fkey(a.x); k[1] = fkey(a.y); k[2] = fkey(a.z);
             k[3] = fkey(b.x); k[4] = fkey(b.y); k[5] = fkey(b.z);
         }
@@ -223,7 +230,7 @@ __global__ void k_node_split(int32_t R, int32_t active, int do_ess, float thr,
                              const float4 *__restrict__ pmin, const float4 *__restrict__ pmax,
                              const unsigned *__restrict__ keys, float4 *__restrict__ bmin,
                              float4 *__restrict__ bmax, float *__restrict__ split, int8_t *__restrict__ info,
-                             int8_t *__restrict__ planes, int32_t *__restrict__ req)
+                             int8_t *__restrict__ planes, int32_t *__restrict__ lanes)
 {
     const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= R) return;
@@ -242,7 +249,9 @@ __global__ void k_node_split(int32_t R, int32_t active, int do_ess, float thr,
         if (__fsub_rn(b.y, mx.y) > __fmul_rn(thr, __fsub_rn(b.y, a.y))) { pl |= 16; nr += 2; }
         if (__fsub_rn(b.z, mx.z) > __fmul_rn(thr, __fsub_rn(b.z, a.z))) { pl |= 32; nr += 2; }
         planes[k] = (int8_t)pl;
-        req[k] = nr;
+        lanes[kLanes * (int64_t)k + 6] = nr;
+    } else {
+        lanes[kLanes * (int64_t)k + 6] = 0;
     }
     const float sx = __fsub_rn(mx.x, mn.x), sy = __fsub_rn(mx.y, mn.y), sz = __fsub_rn(mx.z, mn.z);
     const float mdx = __fadd_rn(__fmul_rn(sx, 0.5f), mn.x);
@@ -257,19 +266,213 @@ __global__ void k_node_split(int32_t R, int32_t active, int do_ess, float thr,
     info[active + k] = z_higher ? (int8_t)KDGB_Z : ax;
 }
 
-// EmptySpaceSplitting2 (EmptySpaceSplitting.h:74-184): a chain of split
-// nodes, each with an empty leaf, between the parent and the active node.
-__global__ void k_ess_chain(int32_t R, int32_t active, int32_t base, int zmax_as_x,
-                            const int8_t *__restrict__ planes, const int32_t *__restrict__ eaddr,
-                            int8_t *info, float *split, float4 *bmin, float4 *bmax, int32_t *pidx,
-                            int32_t *amt, int2 *ch, float *area, int32_t *parent)
+__device__ __forceinline__ void ref_flags(const float4 &a, const float4 &b, int axis, float sp, int &L, int &Rf)
+{
+    // SetSplitSide (TriangleUpperChildren.h:10-62): left = min <= split,
+    // right = split < max.
+    L = axis_of4(a, axis) <= sp;
+    Rf = sp < axis_of4(b, axis);
+}
+
+// Per-node left/right counts and per-chunk totals of the flags (the chunk
+// totals are scanned into each warp chunk's global offsets for k_scatter).
+__global__ void __launch_bounds__(kBlock) k_count(int64_t N, int32_t active, const float4 *__restrict__ cmin,
+                                                 const float4 *__restrict__ cmax, const float *__restrict__ split,
+                                                 const int8_t *__restrict__ info, int32_t *__restrict__ cnt,
+                                                 int32_t *__restrict__ chunksum)
+{
+    __shared__ int s_owner[kWarps], s_l[kWarps], s_r[kWarps];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t chunk = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t base = chunk * kChunk;
+    int cw = -1, al = 0, ar = 0, tl = 0, tr = 0;
+    float4 ra[kRows], rb[kRows];
+#pragma unroll
+    for (int row = 0; row < kRows; ++row) {
+        const int64_t r = base + row * 32 + lane;
+        if (r < N) { ra[row] = cmin[r]; rb[row] = cmax[r]; }
+        else { rb[row].w = __int_as_float(-1); }
+    }
+    int ax[kRows];
+    float sp[kRows];
+#pragma unroll
+    for (int row = 0; row < kRows; ++row) {
+        const int o = __float_as_int(rb[row].w);
+        ax[row] = o >= 0 ? info[active + o] : 0;
+        sp[row] = o >= 0 ? split[active + o] : 0.0f;
+    }
+#pragma unroll
+    for (int row = 0; row < kRows; ++row) {
+        if (base + row * 32 >= N) break;
+        const int o = __float_as_int(rb[row].w);
+        int L = 0, Rf = 0;
+        if (o >= 0) ref_flags(ra[row], rb[row], ax[row], sp[row], L, Rf);
+        tl += L;
+        tr += Rf;
+        const unsigned m = __match_any_sync(kFull, o);
+        if (m == kFull && o == cw) {
+            al += L;
+            ar += Rf;
+            continue;
+        }
+        if (cw >= 0) {
+            al = __reduce_add_sync(kFull, al);
+            ar = __reduce_add_sync(kFull, ar);
+            if (lane == 0) { atomicAdd(cnt + 2 * cw, al); atomicAdd(cnt + 2 * cw + 1, ar); }
+        }
+        if (m == kFull && o >= 0) {
+            cw = o; al = L; ar = Rf;
+        } else {
+            if (o >= 0) {
+                const int gl = __reduce_add_sync(m, L), gr = __reduce_add_sync(m, Rf);
+                if (lane == (unsigned)(__ffs(m) - 1)) { atomicAdd(cnt + 2 * o, gl); atomicAdd(cnt + 2 * o + 1, gr); }
+            }
+            cw = -1; al = 0; ar = 0;
+        }
+    }
+    if (cw >= 0) {
+        al = __reduce_add_sync(kFull, al);
+        ar = __reduce_add_sync(kFull, ar);
+    }
+    tl = __reduce_add_sync(kFull, tl);
+    tr = __reduce_add_sync(kFull, tr);
+    if (lane == 0) {
+        if (base < N) {
+            chunksum[2 * chunk] = tl;
+            chunksum[2 * chunk + 1] = tr;
+        }
+        s_owner[warp] = cw;
+        s_l[warp] = al;
+        s_r[warp] = ar;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // Consecutive warps cover consecutive chunks: merge equal owners.
+        int o = -1, l = 0, r = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            const int ow = s_owner[w];
+            if (ow < 0) continue;
+            if (ow != o) {
+                if (o >= 0) { atomicAdd(cnt + 2 * o, l); atomicAdd(cnt + 2 * o + 1, r); }
+                o = ow; l = s_l[w]; r = s_r[w];
+            } else {
+                l += s_l[w]; r += s_r[w];
+            }
+        }
+        if (o >= 0) { atomicAdd(cnt + 2 * o, l); atomicAdd(cnt + 2 * o + 1, r); }
+    }
+}
+
+// Six scan lanes per node: left/right sizes, left/right references that go
+// to leaves, and the left/right leaf-node flags (CalcNodeChildSize,
+// SetPrimitiveLeafSide, MarkNodeLeafs: TriangleUpperChildren.h:144-201).
+__global__ void k_node_lanes(int32_t R, int32_t LS, const int32_t *__restrict__ cnt, int32_t *__restrict__ lanes)
 {
     const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= R) return;
-    int pl = planes[k];
-    if (pl == 0) return;
+    const int32_t l = cnt[2 * k], r = cnt[2 * k + 1];
+    const int ll = l < LS, rl = r < LS;
+    int32_t *o = lanes + kLanes * (int64_t)k;
+    o[0] = l; o[1] = r; o[2] = ll ? l : 0; o[3] = rl ? r : 0; o[4] = ll; o[5] = rl;
+}
+
+// Writes one reference to its child (or final leaf) slot: destination = node
+// base + rank among the node's left (right) references.
+__device__ __forceinline__ void scatter_one(int32_t R, int owner, int32_t LS, int32_t upper, int L, int Rf, int axis,
+                                            float sp, float4 a, float4 b, int32_t pl, int32_t pr,
+                                            const int32_t *__restrict__ lbase, float4 *__restrict__ nmin,
+                                            float4 *__restrict__ nmax, float4 *__restrict__ fmin,
+                                            float4 *__restrict__ fmax)
+{
+    const int32_t *lb = lbase + kLanes * (int64_t)owner;
+    const int32_t *tot = lbase + kLanes * (int64_t)R;
+    const int32_t total_l = tot[0], leaf_l = tot[2], leafnodes_l = tot[4];
+    if (L) {
+        const int32_t rank = pl - lb[0];
+        const float4 hi = make_float4(axis == KDGB_X ? kmin(sp, b.x) : b.x, axis == KDGB_Y ? kmin(sp, b.y) : b.y,
+                                      axis == KDGB_Z ? kmin(sp, b.z) : b.z, 0.0f);
+        const int32_t lcount = (lbase + kLanes * (int64_t)(owner + 1))[0] - lb[0];
+        if (lcount < LS) {
+            const int64_t dst = (int64_t)upper + lb[2] + rank;
+            fmin[dst] = a;
+            fmax[dst] = hi;
+        } else {
+            const int64_t dst = (int64_t)(lb[0] - lb[2]) + rank;
+            nmin[dst] = a;
+            nmax[dst] = make_float4(hi.x, hi.y, hi.z, __int_as_float(owner - lb[4]));
+        }
+    }
+    if (Rf) {
+        const int32_t rank = pr - lb[1];
+        const float4 lo = make_float4(axis == KDGB_X ? kmax(sp, a.x) : a.x, axis == KDGB_Y ? kmax(sp, a.y) : a.y,
+                                      axis == KDGB_Z ? kmax(sp, a.z) : a.z, a.w);
+        const int32_t rcount = (lbase + kLanes * (int64_t)(owner + 1))[1] - lb[1];
+        if (rcount < LS) {
+            const int64_t dst = (int64_t)upper + leaf_l + lb[3] + rank;
+            fmin[dst] = lo;
+            fmax[dst] = make_float4(b.x, b.y, b.z, 0.0f);
+        } else {
+            const int64_t dst = (int64_t)(total_l - leaf_l) + (lb[1] - lb[3]) + rank;
+            nmin[dst] = lo;
+            nmax[dst] = make_float4(b.x, b.y, b.z, __int_as_float(R + owner - (leafnodes_l + lb[5])));
+        }
+    }
+}
+
+// Partition + compaction of the references with clipping to the split plane
+// (SplitTriangles, TriangleUpperChildren.h:283-383).  Destination = node base
+// + rank of the reference among the node's left (right) references.
+__global__ void __launch_bounds__(kBlock) k_scatter(
+    int64_t N, int32_t R, int32_t active, int32_t LS, int32_t upper,
+    const float4 *__restrict__ cmin, const float4 *__restrict__ cmax, const float *__restrict__ split,
+    const int8_t *__restrict__ info, const int32_t *__restrict__ chunkoff, const int32_t *__restrict__ lbase,
+    float4 *__restrict__ nmin, float4 *__restrict__ nmax, float4 *__restrict__ fmin, float4 *__restrict__ fmax)
+{
+    const unsigned lane = threadIdx.x & 31;
+    const int64_t chunk = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t base = chunk * kChunk;
+    if (base >= N) return;  // warp-uniform
+    const unsigned below = (1u << lane) - 1u;
+    int32_t off_l = chunkoff[2 * chunk], off_r = chunkoff[2 * chunk + 1];
+    float4 ra[kRows], rb[kRows];
+#pragma unroll
+    for (int row = 0; row < kRows; ++row) {
+        const int64_t r = base + row * 32 + lane;
+        if (r < N) { ra[row] = cmin[r]; rb[row] = cmax[r]; }
+        else { rb[row].w = __int_as_float(-1); }
+    }
+    int ax[kRows];
+    float sps[kRows];
+#pragma unroll
+    for (int row = 0; row < kRows; ++row) {
+        const int o = __float_as_int(rb[row].w);
+        ax[row] = o >= 0 ? info[active + o] : 0;
+        sps[row] = o >= 0 ? split[active + o] : 0.0f;
+    }
+#pragma unroll
+    for (int row = 0; row < kRows; ++row) {
+        if (base + row * 32 >= N) break;
+        const int owner = __float_as_int(rb[row].w);
+        const int axis = ax[row];
+        const float sp = sps[row];
+        const float4 a = ra[row], b = rb[row];
+        int L = 0, Rf = 0;
+        if (owner >= 0) ref_flags(a, b, axis, sp, L, Rf);
+        const unsigned bl = __ballot_sync(kFull, L), br = __ballot_sync(kFull, Rf);
+        const int32_t pl = off_l + __popc(bl & below), pr = off_r + __popc(br & below);
+        off_l += __popc(bl);
+        off_r += __popc(br);
+        if (owner >= 0) scatter_one(R, owner, LS, upper, L, Rf, axis, sp, a, b, pl, pr, lbase, nmin, nmax, fmin, fmax);
+    }
+}
+
+// EmptySpaceSplitting2 (EmptySpaceSplitting.h:74-184): a chain of split
+// nodes, each with an empty leaf, between the parent and the active node.
+__device__ __forceinline__ void ess_chain(int32_t k, int32_t active, int32_t start, int pl, int zmax_as_x,
+                                          int8_t *info, float *split, float4 *bmin, float4 *bmax, int32_t *pidx,
+                                          int32_t *amt, int2 *ch, float *area, int32_t *parent)
+{
     const int32_t leaf = active + k;
-    const int32_t start = base + eaddr[k];
     const int nn = 2 * __popc(pl);
     for (int j = 0; j < nn; ++j) zero_node(start + j, info, split, bmin, bmax, pidx, amt, ch, area, parent);
     const int32_t par0 = parent[leaf];
@@ -313,196 +516,47 @@ __global__ void k_ess_chain(int32_t R, int32_t active, int32_t base, int zmax_as
     }
 }
 
-__device__ __forceinline__ void ref_flags(const float4 &a, const float4 &b, int axis, float sp, int &L, int &Rf)
-{
-    // SetSplitSide (TriangleUpperChildren.h:10-62): left = min <= split,
-    // right = split < max.
-    L = axis_of4(a, axis) <= sp;
-    Rf = sp < axis_of4(b, axis);
-}
-
-// Per-node left/right counts and per-chunk totals of the flags (the chunk
-// totals are scanned into each warp chunk's global offsets for k_scatter).
-__global__ void __launch_bounds__(kBlock) k_count(int64_t N, int32_t active, const float4 *__restrict__ cmin,
-                                                 const float4 *__restrict__ cmax, const float *__restrict__ split,
-                                                 const int8_t *__restrict__ info, int32_t *__restrict__ cnt,
-                                                 int32_t *__restrict__ chunksum)
-{
-    const unsigned lane = threadIdx.x & 31;
-    const int64_t chunk = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t base = chunk * kChunk;
-    if (base >= N) return;  // warp-uniform
-    int cw = -1, al = 0, ar = 0, tl = 0, tr = 0;
-    for (int row = 0; row < kRows; ++row) {
-        const int64_t r0 = base + row * 32;
-        if (r0 >= N) break;
-        const int64_t r = r0 + lane;
-        int o = -1, L = 0, Rf = 0;
-        if (r < N) {
-            const float4 a = cmin[r], b = cmax[r];
-            o = __float_as_int(b.w);
-            const int node = active + o;
-            ref_flags(a, b, info[node], split[node], L, Rf);
-        }
-        tl += L;
-        tr += Rf;
-        const unsigned m = __match_any_sync(kFull, o);
-        if (m == kFull && o == cw) {
-            al += L;
-            ar += Rf;
-            continue;
-        }
-        if (cw >= 0) {
-            al = __reduce_add_sync(kFull, al);
-            ar = __reduce_add_sync(kFull, ar);
-            if (lane == 0) { atomicAdd(cnt + 2 * cw, al); atomicAdd(cnt + 2 * cw + 1, ar); }
-        }
-        if (m == kFull && o >= 0) {
-            cw = o; al = L; ar = Rf;
-        } else {
-            if (o >= 0) {
-                const int gl = __reduce_add_sync(m, L), gr = __reduce_add_sync(m, Rf);
-                if (lane == (unsigned)(__ffs(m) - 1)) { atomicAdd(cnt + 2 * o, gl); atomicAdd(cnt + 2 * o + 1, gr); }
-            }
-            cw = -1; al = 0; ar = 0;
-        }
-    }
-    if (cw >= 0) {
-        al = __reduce_add_sync(kFull, al);
-        ar = __reduce_add_sync(kFull, ar);
-        if (lane == 0) { atomicAdd(cnt + 2 * cw, al); atomicAdd(cnt + 2 * cw + 1, ar); }
-    }
-    tl = __reduce_add_sync(kFull, tl);
-    tr = __reduce_add_sync(kFull, tr);
-    if (lane == 0) {
-        chunksum[2 * chunk] = tl;
-        chunksum[2 * chunk + 1] = tr;
-    }
-}
-
-// Six scan lanes per node: left/right sizes, left/right references that go
-// to leaves, and the left/right leaf-node flags (CalcNodeChildSize,
-// SetPrimitiveLeafSide, MarkNodeLeafs: TriangleUpperChildren.h:144-201).
-__global__ void k_node_lanes(int32_t R, int32_t LS, const int32_t *__restrict__ cnt, int32_t *__restrict__ lanes)
+// CreateUpperChildren (TriangleUpperChildren.h:203-281), the empty-space
+// chain of EmptySpaceSplitting2 (its nodes come first, at base + lane-6
+// offsets) and, with empty-space splitting on, PropagateAabbToChildren
+// (EmptySpaceSplitting.h:299-331).  Non-leaf children are the next level's
+// active nodes: their tight-box keys, counts and propagated boxes are reset
+// here (AabbMemset, ReduceSegments.h:328-335) so the next level needs no
+// separate init launch.
+__global__ void k_children(int32_t R, int32_t active, int32_t base, int do_ess, int zmax_as_x, int32_t LS,
+                           int32_t upper, int propagate, const int8_t *__restrict__ planes,
+                           const int32_t *__restrict__ lbase, int8_t *info, float *split, float4 *bmin,
+                           float4 *bmax, int32_t *pidx, int32_t *amt, int2 *ch, float *area, int32_t *parent,
+                           int32_t *stats, unsigned *__restrict__ next_keys, int32_t *__restrict__ next_cnt,
+                           float4 *__restrict__ next_pmin, float4 *__restrict__ next_pmax)
 {
     const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= R) return;
-    const int32_t l = cnt[2 * k], r = cnt[2 * k + 1];
-    const int ll = l < LS, rl = r < LS;
-    int32_t *o = lanes + 6 * (int64_t)k;
-    o[0] = l; o[1] = r; o[2] = ll ? l : 0; o[3] = rl ? r : 0; o[4] = ll; o[5] = rl;
-}
-
-// Writes one reference to its child (or final leaf) slot: destination = node
-// base + rank among the node's left (right) references.
-__device__ __forceinline__ void scatter_one(int32_t R, int owner, int32_t LS, int32_t upper, int L, int Rf, int axis,
-                                            float sp, float4 a, float4 b, int32_t pl, int32_t pr,
-                                            const int32_t *__restrict__ lbase, float4 *__restrict__ nmin,
-                                            float4 *__restrict__ nmax, float4 *__restrict__ fmin,
-                                            float4 *__restrict__ fmax)
-{
-    const int32_t *lb = lbase + 6 * (int64_t)owner;
-    const int32_t *tot = lbase + 6 * (int64_t)R;
-    const int32_t total_l = tot[0], leaf_l = tot[2], leafnodes_l = tot[4];
-    if (L) {
-        const int32_t rank = pl - lb[0];
-        const float4 hi = make_float4(axis == KDGB_X ? kmin(sp, b.x) : b.x, axis == KDGB_Y ? kmin(sp, b.y) : b.y,
-                                      axis == KDGB_Z ? kmin(sp, b.z) : b.z, 0.0f);
-        const int32_t lcount = (lbase + 6 * (int64_t)(owner + 1))[0] - lb[0];
-        if (lcount < LS) {
-            const int64_t dst = (int64_t)upper + lb[2] + rank;
-            fmin[dst] = a;
-            fmax[dst] = hi;
-        } else {
-            const int64_t dst = (int64_t)(lb[0] - lb[2]) + rank;
-            nmin[dst] = a;
-            nmax[dst] = make_float4(hi.x, hi.y, hi.z, __int_as_float(owner - lb[4]));
-        }
-    }
-    if (Rf) {
-        const int32_t rank = pr - lb[1];
-        const float4 lo = make_float4(axis == KDGB_X ? kmax(sp, a.x) : a.x, axis == KDGB_Y ? kmax(sp, a.y) : a.y,
-                                      axis == KDGB_Z ? kmax(sp, a.z) : a.z, a.w);
-        const int32_t rcount = (lbase + 6 * (int64_t)(owner + 1))[1] - lb[1];
-        if (rcount < LS) {
-            const int64_t dst = (int64_t)upper + leaf_l + lb[3] + rank;
-            fmin[dst] = lo;
-            fmax[dst] = make_float4(b.x, b.y, b.z, 0.0f);
-        } else {
-            const int64_t dst = (int64_t)(total_l - leaf_l) + (lb[1] - lb[3]) + rank;
-            nmin[dst] = lo;
-            nmax[dst] = make_float4(b.x, b.y, b.z, __int_as_float(R + owner - (leafnodes_l + lb[5])));
-        }
-    }
-}
-
-// Partition + compaction of the references with clipping to the split plane
-// (SplitTriangles, TriangleUpperChildren.h:283-383).  Destination = node base
-// + rank of the reference among the node's left (right) references.
-__global__ void __launch_bounds__(kBlock) k_scatter(
-    int64_t N, int32_t R, int32_t active, int32_t LS, int32_t upper,
-    const float4 *__restrict__ cmin, const float4 *__restrict__ cmax, const float *__restrict__ split,
-    const int8_t *__restrict__ info, const int32_t *__restrict__ chunkoff, const int32_t *__restrict__ lbase,
-    float4 *__restrict__ nmin, float4 *__restrict__ nmax, float4 *__restrict__ fmin, float4 *__restrict__ fmax)
-{
-    const unsigned lane = threadIdx.x & 31;
-    const int64_t chunk = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t base = chunk * kChunk;
-    if (base >= N) return;  // warp-uniform
-    const unsigned below = (1u << lane) - 1u;
-    int32_t off_l = chunkoff[2 * chunk], off_r = chunkoff[2 * chunk + 1];
-    for (int row = 0; row < kRows; ++row) {
-        const int64_t r0 = base + row * 32;
-        if (r0 >= N) break;
-        const int64_t r = r0 + lane;
-        int owner = -1, L = 0, Rf = 0, axis = 0;
-        float sp = 0.0f;
-        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-        if (r < N) {
-            a = cmin[r];
-            b = cmax[r];
-            owner = __float_as_int(b.w);
-            const int node = active + owner;
-            axis = info[node];
-            sp = split[node];
-            ref_flags(a, b, axis, sp, L, Rf);
-        }
-        const unsigned bl = __ballot_sync(kFull, L), br = __ballot_sync(kFull, Rf);
-        const int32_t pl = off_l + __popc(bl & below), pr = off_r + __popc(br & below);
-        off_l += __popc(bl);
-        off_r += __popc(br);
-        if (owner >= 0) scatter_one(R, owner, LS, upper, L, Rf, axis, sp, a, b, pl, pr, lbase, nmin, nmax, fmin, fmax);
-    }
-}
-
-// CreateUpperChildren (TriangleUpperChildren.h:203-281) and, with empty-space
-// splitting on, PropagateAabbToChildren (EmptySpaceSplitting.h:299-331).
-__global__ void k_children(int32_t R, int32_t active, int32_t base, const int32_t *__restrict__ empty_total,
-                           int32_t LS, int32_t upper, int propagate, const int32_t *__restrict__ lbase,
-                           int8_t *info, float *split, float4 *bmin, float4 *bmax, int32_t *pidx,
-                           int32_t *amt, int2 *ch, float *area, int32_t *parent, int32_t *stats)
-{
-    const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int32_t empty = empty_total ? *empty_total : 0;
-    const int32_t *tot = lbase + 6 * (int64_t)R;
+    const int32_t *tot = lbase + kLanes * (int64_t)R;
+    const int32_t empty = tot[6];
     if (k == 0) {
         stats[0] = empty;
         for (int j = 0; j < 6; ++j) stats[1 + j] = tot[j];
     }
     if (k >= R) return;
+    const int32_t *lb = lbase + kLanes * (int64_t)k;
+    const int32_t *nb = lbase + kLanes * (int64_t)(k + 1);
+    if (do_ess) {
+        const int pl = planes[k];
+        if (pl) ess_chain(k, active, base + lb[6], pl, zmax_as_x, info, split, bmin, bmax, pidx, amt, ch, area, parent);
+    }
     const int32_t child_start = base + empty;
     const int32_t total_l = tot[0], leaf_l = tot[2], ln_l = tot[4], leaf_nodes = tot[4] + tot[5];
-    const int32_t *lb = lbase + 6 * (int64_t)k;
-    const int32_t *nb = lbase + 6 * (int64_t)(k + 1);
     const int32_t l = nb[0] - lb[0], r = nb[1] - lb[1];
     const int32_t par = active + k;
 
     const bool lleaf = l < LS;
     const int32_t la = lb[4];
-    const int32_t lid = child_start + (lleaf ? la : k - la + leaf_nodes);
+    const int32_t lnext = k - la;
+    const int32_t lid = child_start + (lleaf ? la : lnext + leaf_nodes);
     const bool rleaf = r < LS;
     const int32_t ra = ln_l + lb[5];
-    const int32_t rid = child_start + (rleaf ? ra : (R + k) - ra + leaf_nodes);
+    const int32_t rnext = (R + k) - ra;
+    const int32_t rid = child_start + (rleaf ? ra : rnext + leaf_nodes);
 
     zero_node(lid, info, split, bmin, bmax, pidx, amt, ch, area, parent);
     zero_node(rid, info, split, bmin, bmax, pidx, amt, ch, area, parent);
@@ -513,14 +567,38 @@ __global__ void k_children(int32_t R, int32_t active, int32_t base, const int32_
     parent[lid] = par;
     parent[rid] = par;
     ch[par] = make_int2(lid, rid);
+    float4 lmin = make_float4(0.f, 0.f, 0.f, 0.f), lmax = lmin, rmin = lmin, rmax = lmin;
     if (propagate) {
         const int axis = info[par] & 3;
         const float sp = split[par];
         const float4 mn = bmin[par], mx = bmax[par];
-        bmin[lid] = mn;
-        bmin[rid] = make_float4(axis == KDGB_X ? sp : mn.x, axis == KDGB_Y ? sp : mn.y, axis == KDGB_Z ? sp : mn.z, 0.0f);
-        bmax[lid] = make_float4(axis == KDGB_X ? sp : mx.x, axis == KDGB_Y ? sp : mx.y, axis == KDGB_Z ? sp : mx.z, 0.0f);
-        bmax[rid] = mx;
+        lmin = mn;
+        rmin = make_float4(axis == KDGB_X ? sp : mn.x, axis == KDGB_Y ? sp : mn.y, axis == KDGB_Z ? sp : mn.z, 0.0f);
+        lmax = make_float4(axis == KDGB_X ? sp : mx.x, axis == KDGB_Y ? sp : mx.y, axis == KDGB_Z ? sp : mx.z, 0.0f);
+        rmax = mx;
+        bmin[lid] = lmin;
+        bmin[rid] = rmin;
+        bmax[lid] = lmax;
+        bmax[rid] = rmax;
+    }
+    const unsigned lo = fkey(KDGB_FINF), hi = fkey(-KDGB_FINF);
+    if (!lleaf) {
+        unsigned *kk = next_keys + 6 * (int64_t)lnext;
+        kk[0] = kk[1] = kk[2] = lo;
+        kk[3] = kk[4] = kk[5] = hi;
+        next_cnt[2 * lnext] = 0;
+        next_cnt[2 * lnext + 1] = 0;
+        next_pmin[lnext] = lmin;
+        next_pmax[lnext] = lmax;
+    }
+    if (!rleaf) {
+        unsigned *kk = next_keys + 6 * (int64_t)rnext;
+        kk[0] = kk[1] = kk[2] = lo;
+        kk[3] = kk[4] = kk[5] = hi;
+        next_cnt[2 * rnext] = 0;
+        next_cnt[2 * rnext + 1] = 0;
+        next_pmin[rnext] = rmin;
+        next_pmax[rnext] = rmax;
     }
 }
 
@@ -779,6 +857,15 @@ __global__ void k_sah_children(int32_t R, const int32_t *__restrict__ ids, int32
 // Host side.
 // ---------------------------------------------------------------------------
 
+// Grows a per-node array that carries `keep` live entries into a level.
+template <class T>
+int reserve_keep(DevArray<T> &a, int64_t n, int64_t keep, cudaStream_t s)
+{
+    if (a.p && n <= a.cap) return KDGB_OK;
+    const int64_t want = a.cap + a.cap / 2 > n ? a.cap + a.cap / 2 : n;
+    return ensure(a, want, s, a.p ? keep : 0);
+}
+
 int grow_nodes(Tree &t, int64_t need, cudaStream_t s)
 {
     const int64_t keep = t.n_nodes;
@@ -917,12 +1004,15 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
         const int64_t nch = chunks_for(N);
         const unsigned ngrid = chunk_blocks(nch);
         KDGB_CHECK(grow_nodes(t, (int64_t)t.n_nodes + 14 * (int64_t)R, s));
-        KDGB_CHECK(grab(w.pmin, R, s));
-        KDGB_CHECK(grab(w.pmax, R, s));
-        KDGB_CHECK(grab(w.keys, 6 * (int64_t)R, s));
-        KDGB_CHECK(grab(w.cnt, 2 * (int64_t)R, s));
-        KDGB_CHECK(grab(w.lanes, 6 * (int64_t)R, s));
-        KDGB_CHECK(grab(w.lbase, 6 * ((int64_t)R + 1), s));
+        // Per-node arrays hold this level's R entries (written by the
+        // previous level's k_children) and room for the next level's <= 2R.
+        KDGB_CHECK(reserve_keep(w.pmin, 2 * (int64_t)R, R, s));
+        KDGB_CHECK(reserve_keep(w.pmax, 2 * (int64_t)R, R, s));
+        KDGB_CHECK(reserve_keep(w.keys, 12 * (int64_t)R, 6 * (int64_t)R, s));
+        KDGB_CHECK(reserve_keep(w.cnt, 4 * (int64_t)R, 2 * (int64_t)R, s));
+        KDGB_CHECK(grab(w.lanes, kLanes * (int64_t)R, s));
+        KDGB_CHECK(grab(w.lbase, kLanes * ((int64_t)R + 1), s));
+        KDGB_CHECK(grab(w.planes, R, s));
         KDGB_CHECK(grab(w.chunksum, 2 * nch, s));
         KDGB_CHECK(grab(w.chunkoff, 2 * (nch + 1), s));
         KDGB_CHECK(grab(w.nmin, 2 * N, s));
@@ -933,28 +1023,19 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
             KDGB_CHECK(ensure(w.fmax, want, s, F));
         }
 
-        k_level_init<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.bmin.p, t.bmax.p, w.pmin.p, w.pmax.p, w.keys.p,
-                                                      w.cnt.p);
-        KDGB_LAUNCH_CHECK();
+        if (level == 1) {
+            k_level_init<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.bmin.p, t.bmax.p, w.pmin.p, w.pmax.p,
+                                                          w.keys.p, w.cnt.p);
+            KDGB_LAUNCH_CHECK();
+        }
         if (N > 0) {
             k_reduce<<<ngrid, kBlock, 0, s>>>(N, w.cmin.p, w.cmax.p, w.keys.p);
             KDGB_LAUNCH_CHECK();
         }
-        if (do_ess) {
-            KDGB_CHECK(grab(w.planes, R, s));
-            KDGB_CHECK(grab(w.req, R, s));
-            KDGB_CHECK(grab(w.eaddr, (int64_t)R + 1, s));
-        }
         k_node_split<<<blocks_for(R), kBlock, 0, s>>>(R, active, do_ess, p.empty_space_threshold, w.pmin.p, w.pmax.p,
-                                                      w.keys.p, t.bmin.p, t.bmax.p, t.split.p, t.info.p,
-                                                      do_ess ? w.planes.p : nullptr, do_ess ? w.req.p : nullptr);
+                                                      w.keys.p, t.bmin.p, t.bmax.p, t.split.p, t.info.p, w.planes.p,
+                                                      w.lanes.p);
         KDGB_LAUNCH_CHECK();
-        if (do_ess) {
-            KDGB_CHECK(scan_exclusive<1>(w.req.p, w.eaddr.p, R, s, &w.scan));
-            k_ess_chain<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.n_nodes, p.esc_zmax_as_x, w.planes.p, w.eaddr.p,
-                                                         NODE_ARGS);
-            KDGB_LAUNCH_CHECK();
-        }
         if (N > 0) {
             k_count<<<ngrid, kBlock, 0, s>>>(N, active, w.cmin.p, w.cmax.p, t.split.p, t.info.p, w.cnt.p,
                                              w.chunksum.p);
@@ -963,14 +1044,15 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
         KDGB_CHECK(scan_exclusive<2>(w.chunksum.p, w.chunkoff.p, nch, s, &w.scan));
         k_node_lanes<<<blocks_for(R), kBlock, 0, s>>>(R, LS, w.cnt.p, w.lanes.p);
         KDGB_LAUNCH_CHECK();
-        KDGB_CHECK(scan_exclusive<6>(w.lanes.p, w.lbase.p, R, s, &w.scan));
+        KDGB_CHECK(scan_exclusive<kLanes>(w.lanes.p, w.lbase.p, R, s, &w.scan));
         if (N > 0) {
             k_scatter<<<ngrid, kBlock, 0, s>>>(N, R, active, LS, (int32_t)F, w.cmin.p, w.cmax.p, t.split.p, t.info.p,
                                                w.chunkoff.p, w.lbase.p, w.nmin.p, w.nmax.p, w.fmin.p, w.fmax.p);
             KDGB_LAUNCH_CHECK();
         }
-        k_children<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.n_nodes, do_ess ? w.eaddr.p + R : nullptr, LS,
-                                                    (int32_t)F, p.split_empty_space, w.lbase.p, NODE_ARGS, w.stats.p);
+        k_children<<<blocks_for(R), kBlock, 0, s>>>(R, active, t.n_nodes, do_ess, p.esc_zmax_as_x, LS, (int32_t)F,
+                                                    p.split_empty_space, w.planes.p, w.lbase.p, NODE_ARGS, w.stats.p,
+                                                    w.keys.p, w.cnt.p, w.pmin.p, w.pmax.p);
         KDGB_LAUNCH_CHECK();
         KDGB_CUDA(cudaMemcpyAsync(rec, w.stats.p, 16 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         KDGB_CUDA(cudaStreamSynchronize(s));

@@ -204,5 +204,6 @@ int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, D
 template int scan_exclusive<1>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
 template int scan_exclusive<2>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
 template int scan_exclusive<6>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
+template int scan_exclusive<7>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
 
 }  // namespace kdgb
