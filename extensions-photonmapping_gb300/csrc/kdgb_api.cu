@@ -20,6 +20,8 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
                   int32_t *occ, cudaStream_t s);
 int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, int32_t T, int tie, const float *o,
                  const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv, cudaStream_t s);
+int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_params &ph, int64_t n,
+                  int32_t *seg_hit, float *seg_t, cudaStream_t s);
 
 namespace {
 thread_local std::string g_last_error;
@@ -488,6 +490,37 @@ int kdgb_trace_primary_shadow(const kdgb_tree *tree, const kdgb_trace_params *pa
         return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
     return trace_launch(tree->t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, occluded_dev, light,
                         (cudaStream_t)stream);
+}
+
+void kdgb_photon_params_default(kdgb_photon_params *p)
+{
+    if (!p) return;
+    p->light[0] = 0.5f;
+    p->light[1] = 0.5f;
+    p->light[2] = 0.5f;
+    p->seed = 3;
+    p->bounces = 3;
+    p->survival = 0.7f;
+}
+
+int kdgb_trace_photons(const kdgb_tree *tree, const kdgb_trace_params *params, const kdgb_photon_params *photons,
+                       int32_t n_photons, int32_t *seg_hit_dev, float *seg_t_dev, kdgb_stream_t stream)
+{
+    if (!tree || !photons) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    if (n_photons < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "negative photon count");
+    p.tile_width = 0;
+    KDGB_CHECK(validate_trace_params(p, n_photons));
+    if (p.tracer == KDGB_TRACER_BRUTE) return fail(KDGB_ERR_UNSUPPORTED, "photon tracing needs a kd tracer");
+    if (photons->bounces < 0 || photons->bounces > 64) return fail(KDGB_ERR_INVALID_ARGUMENT, "bounces must be in 0..64");
+    if (!(photons->survival >= 0.0f && photons->survival <= 1.0f))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "survival must be in [0, 1]");
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(photons->light[k])) return fail(KDGB_ERR_INVALID_ARGUMENT, "non-finite light");
+    if (n_photons == 0) return KDGB_OK;
+    if (!seg_hit_dev || !seg_t_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL output buffer");
+    return photon_launch(tree->t, p, *photons, n_photons, seg_hit_dev, seg_t_dev, (cudaStream_t)stream);
 }
 
 int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie, const float *ray_o_dev,

@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include "kdgb_internal.cuh"
+#include "kdgb_photon.cuh"
 
 namespace kdgb {
 
@@ -379,6 +380,72 @@ __global__ void __launch_bounds__(kBruteBlock) k_brute(const float4 *__restrict_
     }
 }
 
+// Photon tracing (the incoherent workload): each photon leaves the light in
+// a uniform direction drawn from Philox4x32-10 (key = seed, counter =
+// (photon, 0)), and after every hit it survives Russian roulette with
+// probability `survival` and continues in a cosine-weighted direction around
+// the hit triangle's normal (counter = (photon, bounce)), from the hit point
+// pushed 1e-4 along the normal.  Segment k of photon i is written to
+// [i * (bounces + 1) + k]: the hit id (-1 = miss) and t, or -2 when the
+// photon had already ended.
+struct PhotonArgs {
+    Ctx c;
+    const float4 *p0, *p1, *p2;
+    float3 light;
+    uint2 key;
+    int64_t n;
+    int bounces;
+    float survival;
+    int tie, depth, maxit;
+    int32_t *seg_hit;
+    float *seg_t;
+};
+
+template <int TRACER, bool SKIP>
+__global__ void k_photons(PhotonArgs a)
+{
+    extern __shared__ int2 stack_smem[];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int S = a.bounces + 1;
+    const int64_t base = i * S;
+    const unsigned lo = (unsigned)i, hi = (unsigned)(i >> 32);
+    uint4 r = philox4x32_10(make_uint4(lo, hi, 0u, 0u), a.key);
+    float3 o = a.light;
+    float3 d = sample_sphere(u24(r.x), u24(r.y));
+    int k = 0;
+    while (k < S) {
+        float t = 0.0f, u = 0.0f, v = 0.0f;
+        int h;
+        if (TRACER == KDGB_TRACER_SHORTSTACK)
+            h = trace_shortstack<SKIP>(a.c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u,
+                                       v);
+        else
+            h = trace_restart<SKIP>(a.c, o, d, a.tie, a.maxit, t, u, v);
+        a.seg_hit[base + k] = h;
+        a.seg_t[base + k] = h >= 0 ? t : INFINITY;
+        ++k;
+        if (h < 0 || k == S) break;
+        r = philox4x32_10(make_uint4(lo, hi, (unsigned)k, 0u), a.key);
+        if (!(u24(r.z) < a.survival)) break;
+        const float4 A = a.p0[h], B = a.p1[h], C = a.p2[h];
+        const float3 v0 = make_float3(A.x, A.y, A.z);
+        const float3 cr = cross3(sub3(make_float3(B.x, B.y, B.z), v0), sub3(make_float3(C.x, C.y, C.z), v0));
+        const float inv = __frcp_rn(__fsqrt_rn(dot3(cr, cr)));
+        float3 nrm = make_float3(__fmul_rn(cr.x, inv), __fmul_rn(cr.y, inv), __fmul_rn(cr.z, inv));
+        if (dot3(nrm, d) > 0.0f) nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+        const float3 p = make_float3(__fadd_rn(o.x, __fmul_rn(t, d.x)), __fadd_rn(o.y, __fmul_rn(t, d.y)),
+                                     __fadd_rn(o.z, __fmul_rn(t, d.z)));
+        o = make_float3(__fadd_rn(p.x, __fmul_rn(1e-4f, nrm.x)), __fadd_rn(p.y, __fmul_rn(1e-4f, nrm.y)),
+                        __fadd_rn(p.z, __fmul_rn(1e-4f, nrm.z)));
+        d = sample_cosine(nrm, u24(r.x), u24(r.y));
+    }
+    for (; k < S; ++k) {
+        a.seg_hit[base + k] = -2;
+        a.seg_t[base + k] = INFINITY;
+    }
+}
+
 }  // namespace
 
 int pack_for_traversal(Tree &t, cudaStream_t s)
@@ -472,6 +539,40 @@ int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, int32_t T
                  const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv, cudaStream_t s)
 {
     k_brute<<<blocks_for(n, kBruteBlock), kBruteBlock, 0, s>>>(p0, p1, p2, T, tie, o, d, n, hit, tt, uu, vv);
+    KDGB_LAUNCH_CHECK();
+    return KDGB_OK;
+}
+
+int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_params &ph, int64_t n,
+                  int32_t *seg_hit, float *seg_t, cudaStream_t s)
+{
+    PhotonArgs a;
+    a.c.node = t.tnode.p;
+    a.c.bmin = t.bmin.p;
+    a.c.bmax = t.bmax.p;
+    a.c.tri = t.ttri.p;
+    a.p0 = t.p0.p; a.p1 = t.p1.p; a.p2 = t.p2.p;
+    a.light = make_float3(ph.light[0], ph.light[1], ph.light[2]);
+    a.key = make_uint2((unsigned)(ph.seed & 0xffffffffu), (unsigned)(ph.seed >> 32));
+    a.n = n;
+    a.bounces = ph.bounces;
+    a.survival = ph.survival;
+    a.tie = p.tie;
+    a.depth = p.stack_depth;
+    a.maxit = p.max_iterations > 0 ? p.max_iterations : kDefaultMaxIterations;
+    a.seg_hit = seg_hit;
+    a.seg_t = seg_t;
+    const int bs = p.block_size > 0 ? p.block_size : 128;
+    const unsigned grid = blocks_for(n, bs);
+    const bool skip = p.leaf_skipping != 0;
+    if (p.tracer == KDGB_TRACER_SHORTSTACK) {
+        const size_t smem = sizeof(int2) * (size_t)p.stack_depth * bs;
+        if (skip) k_photons<KDGB_TRACER_SHORTSTACK, true><<<grid, bs, smem, s>>>(a);
+        else k_photons<KDGB_TRACER_SHORTSTACK, false><<<grid, bs, smem, s>>>(a);
+    } else {
+        if (skip) k_photons<KDGB_TRACER_RESTART, true><<<grid, bs, 0, s>>>(a);
+        else k_photons<KDGB_TRACER_RESTART, false><<<grid, bs, 0, s>>>(a);
+    }
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }

@@ -23,11 +23,11 @@ import numpy as np
 from . import scenes
 from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ERR_NO_DEVICE, FINF, LEAF, LOWER_BITMAP, LOWER_SAH,
                    TIE_LOWEST_ID, TIE_REF_LAST, TRACER_BRUTE, TRACER_RESTART, TRACER_SHORTSTACK, X, Y, Z,
-                   BuildParams, BuildStats, KdgbError, TraceParams, TreeView, build_params, check, lib,
-                   library_path, trace_params)
+                   BuildParams, BuildStats, KdgbError, PhotonParams, TraceParams, TreeView, build_params, check,
+                   lib, library_path, photon_params, trace_params)
 
 __all__ = ["KDTree", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
-           "trace_params", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
+           "trace_params", "photon_params", "PhotonParams", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
            "BUILD_REFERENCE", "BUILD_TUNED", "TRACER_RESTART", "TRACER_SHORTSTACK", "TRACER_BRUTE",
            "TIE_LOWEST_ID", "TIE_REF_LAST", "FINF", "lib", "library_path"]
 
@@ -227,6 +227,26 @@ class KDTree:
                                               _ptr(u), _ptr(v), _ptr(occ), C.c_void_p(_stream(stream))),
               "kdgb_trace_primary_shadow")
         return hit, t, u, v, occ
+
+
+def _trace_photons(self, n_photons: int, params: TraceParams | None = None, photons=None, stream=None, out=None,
+                   **kw):
+    """Photon segments: (hit int32, t float32) CUDA tensors of shape
+    (n_photons, bounces + 1)."""
+    torch = _torch()
+    p = params if params is not None else trace_params(**kw)
+    ph = photons if photons is not None else photon_params()
+    S = ph.bounces + 1
+    if out is None:
+        out = (torch.empty((n_photons, S), dtype=torch.int32, device="cuda"),
+               torch.empty((n_photons, S), dtype=torch.float32, device="cuda"))
+    hit, t = out
+    check(lib().kdgb_trace_photons(self._h, C.byref(p), C.byref(ph), n_photons, _ptr(hit), _ptr(t),
+                                   C.c_void_p(_stream(stream))), "kdgb_trace_photons")
+    return hit, t
+
+
+KDTree.trace_photons = _trace_photons
 
 
 def trace_brute(tris, o, d, tie: int = TIE_LOWEST_ID, stream=None):

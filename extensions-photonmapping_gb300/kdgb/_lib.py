@@ -53,6 +53,10 @@ class TreeView(C.Structure):
                 ("p2", C.c_void_p)]
 
 
+class PhotonParams(C.Structure):
+    _fields_ = [("light", C.c_float * 3), ("seed", C.c_uint64), ("bounces", C.c_int32), ("survival", C.c_float)]
+
+
 class BuildStats(C.Structure):
     _fields_ = [("upper_levels", C.c_int32), ("lower_levels", C.c_int32), ("n_nodes", C.c_int32),
                 ("n_refs", C.c_int32), ("n_leaves", C.c_int32), ("max_depth", C.c_int32),
@@ -78,6 +82,8 @@ SIGNATURES = {
     "kdgb_trace": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P]),
     "kdgb_trace_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, C.c_int32, P, P, P]),
     "kdgb_trace_primary_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P, P, P]),
+    "kdgb_photon_params_default": (None, [C.POINTER(PhotonParams)]),
+    "kdgb_trace_photons": (C.c_int, [P, C.POINTER(TraceParams), C.POINTER(PhotonParams), C.c_int32, P, P, P]),
     "kdgb_trace_brute": (C.c_int, [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, P]),
     "kdgb_trace_brute_noalloc": (C.c_int, [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, P]),
 }
@@ -128,6 +134,19 @@ def build_params(**kw) -> BuildParams:
         if not hasattr(p, k):
             raise AttributeError(k)
         setattr(p, k, v)
+    return p
+
+
+def photon_params(**kw) -> PhotonParams:
+    p = PhotonParams()
+    lib().kdgb_photon_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k == "light":
+            p.light = (C.c_float * 3)(*[float(x) for x in v])
+        elif not hasattr(p, k):
+            raise AttributeError(k)
+        else:
+            setattr(p, k, v)
     return p
 
 

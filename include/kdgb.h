@@ -204,6 +204,27 @@ KDGB_API int kdgb_trace_primary_shadow(const kdgb_tree *tree, const kdgb_trace_p
                               int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
                               int32_t *occluded_dev, kdgb_stream_t stream);
 
+typedef struct kdgb_photon_params {
+    float    light[3];   /* point light position (photon origin) */
+    uint64_t seed;       /* Philox4x32-10 key */
+    int32_t  bounces;    /* diffuse bounces after the first hit (3) */
+    float    survival;   /* Russian-roulette survival probability (0.7) */
+} kdgb_photon_params;
+
+KDGB_API void kdgb_photon_params_default(kdgb_photon_params *p);
+
+/* Photon tracing (no reference counterpart; the reference's PhotonMapping
+ * name never got a photon pass): n photons leave `light` in uniform
+ * directions and bounce diffusely (cosine-weighted around the hit normal)
+ * with Russian roulette, all random numbers from a counter-based
+ * Philox4x32-10 stream (key = seed, counter = (photon, bounce)).  Each
+ * segment is traced with the kd tracer in `params` (restart or short-stack).
+ * Outputs n*(bounces+1) segments: hit id (-1 miss, -2 photon already ended)
+ * and t (+inf when no hit). */
+KDGB_API int kdgb_trace_photons(const kdgb_tree *tree, const kdgb_trace_params *params,
+                                const kdgb_photon_params *photons, int32_t n_photons,
+                                int32_t *seg_hit_dev, float *seg_t_dev, kdgb_stream_t stream);
+
 /* Replaces BruteTracer::Trace without a tree (BruteTracer.cu:54-96), with
  * the 4096-triangle cap of BruteTracer.cu:50 lifted. */
 KDGB_API int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie,

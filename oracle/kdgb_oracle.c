@@ -413,6 +413,119 @@ int or_trace_shadow(const or_tree *tr, const float *tri, int32_t T,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Photons                                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Philox4x32-10 (Salmon et al., SC 2011). */
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
+        const uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static inline float u24(uint32_t x) { return (float)(x >> 8) * 0x1p-24f; }
+
+/* sin / cos of 2*pi*u: quadrant reduction on u, Taylor polynomials on
+ * [-pi/4, pi/4]; the same operation order as the CUDA sampler. */
+static inline void sincos_2pi(float u, float *s, float *c)
+{
+    const float u4 = u * 4.0f;
+    const float k = floorf(u4 + 0.5f);
+    const float x = (u4 - k) * 1.57079632679489662f;
+    const float x2 = x * x;
+    float ps = 1.0f - x2 * 0.0238095238095238095f;
+    ps = 1.0f - (x2 * 0.05f) * ps;
+    ps = 1.0f - (x2 * 0.166666666666666667f) * ps;
+    const float sx = x * ps;
+    float pc = 1.0f - x2 * 0.0178571428571428571f;
+    pc = 1.0f - (x2 * 0.0333333333333333333f) * pc;
+    pc = 1.0f - (x2 * 0.0833333333333333333f) * pc;
+    const float cx = 1.0f - (x2 * 0.5f) * pc;
+    const int q = ((int)k) & 3;
+    *s = q == 0 ? sx : (q == 1 ? cx : (q == 2 ? -sx : -cx));
+    *c = q == 0 ? cx : (q == 1 ? -sx : (q == 2 ? -cx : sx));
+}
+
+static inline v3 sample_sphere(float u0, float u1)
+{
+    const float z = 1.0f - 2.0f * u0;
+    const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    float s, c;
+    sincos_2pi(u1, &s, &c);
+    return mk3(r * c, r * s, z);
+}
+
+/* Cosine-weighted direction around n; basis of Duff et al., JCGT 2017. */
+static inline v3 sample_cosine(v3 n, float u0, float u1)
+{
+    const float r = sqrtf(u0);
+    float s, c;
+    sincos_2pi(u1, &s, &c);
+    const float x = r * c, y = r * s;
+    const float z = sqrtf(fmaxf(0.0f, 1.0f - u0));
+    const float sign = copysignf(1.0f, n.z);
+    const float a = -1.0f / (sign + n.z);
+    const float b = (n.x * n.y) * a;
+    const v3 t = mk3(1.0f + ((sign * n.x) * n.x) * a, sign * b, -(sign * n.x));
+    const v3 bt = mk3(b, sign + (n.y * n.y) * a, -n.y);
+    return mk3((t.x * x + bt.x * y) + n.x * z, (t.y * x + bt.y * y) + n.y * z, (t.z * x + bt.z * y) + n.z * z);
+}
+
+int or_trace_photons(const or_tree *tr, const float *tri, int32_t T, const or_trace_params *p,
+                     const or_photon_params *ph, int32_t n, int32_t *seg_hit, float *seg_t, int32_t threads)
+{
+    (void)T;
+    if (!tr || !p || !ph || n < 0 || ph->bounces < 0) return OR_ERR_ARG;
+    if (p->tracer != OR_TRACER_RESTART && p->tracer != OR_TRACER_SHORTSTACK) return OR_ERR_ARG;
+    const int nt = set_threads(threads);
+    (void)nt;
+    const int S = ph->bounces + 1;
+    const uint32_t key[2] = {(uint32_t)(ph->seed & 0xffffffffu), (uint32_t)(ph->seed >> 32)};
+    const v3 light = ld3(ph->light);
+#pragma omp parallel for schedule(static, 64) num_threads(nt)
+    for (int32_t i = 0; i < n; ++i) {
+        const int64_t base = (int64_t)i * S;
+        uint32_t ctr[4] = {(uint32_t)i, 0u, 0u, 0u}, r[4];
+        or_philox4x32_10(ctr, key, r);
+        v3 o = light;
+        v3 d = sample_sphere(u24(r[0]), u24(r[1]));
+        int k = 0;
+        while (k < S) {
+            int32_t h;
+            float t, u, v;
+            if (p->tracer == OR_TRACER_SHORTSTACK) trace_shortstack_one(tr, tri, p, o, d, &h, &t, &u, &v);
+            else trace_restart_one(tr, tri, p, o, d, &h, &t, &u, &v);
+            seg_hit[base + k] = h;
+            seg_t[base + k] = h >= 0 ? t : INFINITY;
+            ++k;
+            if (h < 0 || k == S) break;
+            ctr[2] = (uint32_t)k;
+            or_philox4x32_10(ctr, key, r);
+            if (!(u24(r[2]) < ph->survival)) break;
+            const float *tp = tri + 9 * (size_t)h;
+            const v3 v0 = ld3(tp);
+            const v3 cr = cross3(sub3(ld3(tp + 3), v0), sub3(ld3(tp + 6), v0));
+            const float inv = 1.0f / sqrtf(dot3(cr, cr));
+            v3 nrm = mk3(cr.x * inv, cr.y * inv, cr.z * inv);
+            if (dot3(nrm, d) > 0.0f) nrm = mk3(-nrm.x, -nrm.y, -nrm.z);
+            const v3 pt = mk3(o.x + t * d.x, o.y + t * d.y, o.z + t * d.z);
+            o = mk3(pt.x + 1e-4f * nrm.x, pt.y + 1e-4f * nrm.y, pt.z + 1e-4f * nrm.z);
+            d = sample_cosine(nrm, u24(r[0]), u24(r[1]));
+        }
+        for (; k < S; ++k) { seg_hit[base + k] = -2; seg_t[base + k] = INFINITY; }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Build                                                                     */
 /* ------------------------------------------------------------------------ */
 

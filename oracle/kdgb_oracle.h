@@ -116,6 +116,22 @@ int or_trace_shadow(const or_tree *tree, const float *tri, int32_t T,
                     const float *points, int32_t n, const float light[3],
                     int32_t *occluded, int32_t threads);
 
+/* Photon tracing: CPU restatement of kdgb_trace_photons (Philox4x32-10
+ * emission + cosine-weighted diffuse bounces + Russian roulette).  The
+ * reference has no photon pass; this is the checker of the CUDA version. */
+typedef struct or_photon_params {
+    float    light[3];
+    uint64_t seed;
+    int32_t  bounces;
+    float    survival;
+} or_photon_params;
+
+int or_trace_photons(const or_tree *tree, const float *tri, int32_t T, const or_trace_params *p,
+                     const or_photon_params *ph, int32_t n, int32_t *seg_hit, float *seg_t, int32_t threads);
+
+/* Philox4x32-10 block (exported for tests). */
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
 /* Moeller-Trumbore restated (IRayTracer.h:111-145); exported for unit tests. */
 int or_moeller_trumbore(const float v0[3], const float v1[3], const float v2[3],
                         const float o[3], const float d[3], float t_max,

@@ -234,6 +234,39 @@ def trace_shadow(tree: Tree, tris, points, light, threads: int = 0):
     return occ
 
 
+class PhotonParams(C.Structure):
+    _fields_ = [("light", C.c_float * 3), ("seed", C.c_uint64), ("bounces", C.c_int32), ("survival", C.c_float)]
+
+
+def trace_photons(tree: Tree, tris, n: int, light=(0.5, 0.5, 0.5), seed: int = 3, bounces: int = 3,
+                  survival: float = 0.7, threads: int = 0, **kw):
+    """Photon segments (hit, t) of shape (n, bounces + 1)."""
+    L = lib()
+    L.or_trace_photons.argtypes = [C.POINTER(_Tree), C.c_void_p, C.c_int32, C.POINTER(TraceParams),
+                                   C.POINTER(PhotonParams), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    p = trace_params(**kw)
+    ph = PhotonParams()
+    ph.light = (C.c_float * 3)(*[float(x) for x in light])
+    ph.seed, ph.bounces, ph.survival = seed, bounces, survival
+    hit = np.empty((n, bounces + 1), np.int32)
+    t = np.empty((n, bounces + 1), np.float32)
+    s = tree.as_struct()
+    _check(L.or_trace_photons(C.byref(s), _ptr(tris), tris.shape[0], C.byref(p), C.byref(ph), n, _ptr(hit),
+                              _ptr(t), threads))
+    return hit, t
+
+
+def philox4x32_10(ctr, key):
+    L = lib()
+    L.or_philox4x32_10.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, np.uint32)
+    L.or_philox4x32_10(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
 def moeller_trumbore(v0, v1, v2, o, d, t_max=float(FINF)):
     arrs = [np.ascontiguousarray(x, dtype=np.float32).reshape(3) for x in (v0, v1, v2, o, d)]
     out = np.zeros(3, np.float32)
