@@ -249,6 +249,26 @@ def _trace_photons(self, n_photons: int, params: TraceParams | None = None, phot
 KDTree.trace_photons = _trace_photons
 
 
+def backward(vertices, indices, o, d, hit, dL_dt, dL_du, dL_dv, out=None, stream=None):
+    """dL/dvertex (V, 3) float32 for an indexed mesh, reusing the forward's
+    hit ids (kdgb_backward); `out` is accumulated into when given."""
+    torch = _torch()
+    verts = _dev(vertices, torch.float32, 3)
+    idx = _dev(indices, torch.int32).reshape(-1)
+    o = _dev(o, torch.float32, 3)
+    d = _dev(d, torch.float32, 3)
+    hit = _dev(hit, torch.int32).reshape(-1)
+    gt = _dev(dL_dt, torch.float32).reshape(-1)
+    gu = _dev(dL_du, torch.float32).reshape(-1)
+    gv = _dev(dL_dv, torch.float32).reshape(-1)
+    if out is None:
+        out = torch.zeros_like(verts)
+    check(lib().kdgb_backward(_ptr(verts), verts.shape[0], _ptr(idx), idx.numel() // 3, _ptr(o), _ptr(d),
+                              o.shape[0], _ptr(hit), _ptr(gt), _ptr(gu), _ptr(gv), _ptr(out),
+                              C.c_void_p(_stream(stream))), "kdgb_backward")
+    return out
+
+
 def trace_brute(tris, o, d, tie: int = TIE_LOWEST_ID, stream=None):
     """BruteTracer over device triangles, without a tree."""
     torch = _torch()

@@ -225,6 +225,19 @@ KDGB_API int kdgb_trace_photons(const kdgb_tree *tree, const kdgb_trace_params *
                                 const kdgb_photon_params *photons, int32_t n_photons,
                                 int32_t *seg_hit_dev, float *seg_t_dev, kdgb_stream_t stream);
 
+/* Adjoint of first-hit t, u, v with respect to vertex positions (no
+ * reference counterpart).  vertices: n_vertices*3 floats; indices:
+ * n_tris*3 vertex ids (the index buffer of CUDAMeshNode, CUDAMeshNode.h:36);
+ * hit: the triangle ids a forward trace recorded for the n rays (reused, not
+ * re-traced; -1 = no contribution); dL_dt/du/dv: upstream gradients per ray.
+ * ADDS dL/dvertex (n_vertices*3) into dL_dvertex_dev with warp-aggregated
+ * float atomics (summation order, hence the last bits, are not
+ * deterministic). */
+KDGB_API int kdgb_backward(const float *vertices_dev, int32_t n_vertices, const uint32_t *indices_dev,
+                           int32_t n_tris, const float *ray_o_dev, const float *ray_d_dev, int32_t n,
+                           const int32_t *hit_dev, const float *dL_dt_dev, const float *dL_du_dev,
+                           const float *dL_dv_dev, float *dL_dvertex_dev, kdgb_stream_t stream);
+
 /* Replaces BruteTracer::Trace without a tree (BruteTracer.cu:54-96), with
  * the 4096-triangle cap of BruteTracer.cu:50 lifted. */
 KDGB_API int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie,
