@@ -238,6 +238,24 @@ KDGB_API int kdgb_backward(const float *vertices_dev, int32_t n_vertices, const 
                            const int32_t *hit_dev, const float *dL_dt_dev, const float *dL_du_dev,
                            const float *dL_dv_dev, float *dL_dvertex_dev, kdgb_stream_t stream);
 
+/* Replaces GeometryList::AddMesh(CUDAMeshNode*) (GeometryList.cu:318-341,
+ * kernel AddMeshKernel :197-232): gathers n_indices/3 triangles of an
+ * indexed mesh (vertices: n_vertices float4) and applies the row-major
+ * model matrix `model` (16 host floats, NULL = identity) to each vertex,
+ * writing the T x 9 triangle buffer kdgb_build takes.  An index outside the
+ * vertex buffer yields a NaN triangle (kdgb_build then reports
+ * KDGB_ERR_NONFINITE). */
+KDGB_API int kdgb_geometry_gather(const float *vertices_dev, int32_t n_vertices, const uint32_t *indices_dev,
+                                  int32_t n_indices, const float model[16], float *tri_v_out_dev,
+                                  kdgb_stream_t stream);
+
+/* Replaces OscCUDAMeshNode::Handle (OscCUDAMeshNode.cu:96-107, kernel
+ * UpdateSurface :75-94): moves the (detail+1)^2 float4 vertices and normals
+ * of the oscillating height field to time `time` (the reference passes its
+ * accumulated microseconds / 700000). */
+KDGB_API int kdgb_osc_update_surface(float *vertices_dev, float *normals_dev, int32_t detail, float height,
+                                     float time, kdgb_stream_t stream);
+
 /* Replaces BruteTracer::Trace without a tree (BruteTracer.cu:54-96), with
  * the 4096-triangle cap of BruteTracer.cu:50 lifted. */
 KDGB_API int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie,

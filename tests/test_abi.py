@@ -69,6 +69,22 @@ def test_no_device_is_an_error_not_a_crash(kdgb_lib):
     assert b"no CUDA device" in L.kdgb_last_error()
 
 
+def test_cpp_plugin_header_compiles_and_links(kdgb_lib, tmp_path):
+    """include/kdgb_plugin.hpp (reference class names over the C ABI) builds
+    with g++ against libkdgb.so (the program is run by the GPU tests)."""
+    import shutil
+    import subprocess
+    cuda_home = "/usr/local/cuda"
+    if not shutil.which("g++") or not os.path.isdir(os.path.join(cuda_home, "include")):
+        pytest.skip("g++ or the CUDA headers are missing")
+    libdir = os.path.dirname(kdgb_lib.library_path())
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), "-I",
+                        os.path.join(cuda_home, "include"), os.path.join(ROOT, "tests", "helpers", "plugin_demo.cpp"),
+                        "-L", libdir, "-lkdgb", "-L", os.path.join(cuda_home, "lib64"), "-lcudart",
+                        "-o", str(tmp_path / "plugin_demo")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_null_arguments_rejected(kdgb_lib):
     L = kdgb_lib.lib()
     assert L.kdgb_build(None, 1, None, None, None) == 1
