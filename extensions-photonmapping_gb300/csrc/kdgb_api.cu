@@ -15,7 +15,8 @@
 namespace kdgb {
 
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
-                 int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s);
+                 int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s,
+                 const int32_t *ray_mesh = nullptr, int32_t rays_per_mesh = 0);
 int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, int64_t n, const float *light,
                   int32_t *occ, cudaStream_t s);
 int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, int32_t T, int tie, const float *o,
@@ -105,7 +106,7 @@ static void release_all(Tree &t, cudaStream_t s)
     release(t.info, s); release(t.split, s); release(t.bmin, s); release(t.bmax, s);
     release(t.pidx, s); release(t.bitmap, s); release(t.parent, s); release(t.children, s);
     release(t.area, s); release(t.prim_indices, s); release(t.leaf_ids, s);
-    release(t.tnode, s); release(t.ttri, s);
+    release(t.tnode, s); release(t.ttri, s); release(t.mesh_off, s);
     Workspace &w = t.ws;
     release(w.cmin, s); release(w.cmax, s); release(w.nmin, s); release(w.nmax, s); release(w.fmin, s);
     release(w.fmax, s); release(w.pmin, s); release(w.pmax, s); release(w.keys, s); release(w.planes, s);
@@ -143,8 +144,8 @@ static int validate_build_params(const kdgb_build_params &p)
     if (!std::isfinite(p.empty_space_threshold) || !std::isfinite(p.traversal_cost) ||
         !std::isfinite(p.intersection_cost))
         return fail(KDGB_ERR_INVALID_ARGUMENT, "non-finite cost parameter");
-    if (p.mode == KDGB_BUILD_TUNED && (p.upper_levels < 0 || p.sah_bins < 2 || p.sah_bins > 256))
-        return fail(KDGB_ERR_INVALID_ARGUMENT, "tuned build: upper_levels >= 0, sah_bins in 2..256");
+    if (p.mode == KDGB_BUILD_TUNED && (p.upper_levels < 0 || p.sah_bins < 2 || p.sah_bins > 32))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "tuned build: upper_levels >= 0, sah_bins in 2..32");
     return KDGB_OK;
 }
 
@@ -163,14 +164,25 @@ static int validate_trace_params(const kdgb_trace_params &p, int64_t n)
     return KDGB_OK;
 }
 
-static int do_build(Tree &t, const float *tri_v_dev, int32_t n_tris, const kdgb_build_params &p, cudaStream_t s)
+static int do_build(Tree &t, const float *tri_v_dev, int32_t n_tris, const kdgb_build_params &p, cudaStream_t s,
+                    const int32_t *mesh_off_host = nullptr, int32_t n_meshes = 1)
 {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     KDGB_CUDA(cudaEventCreate(&e0));
     KDGB_CUDA(cudaEventCreate(&e1));
     cudaEventRecord(e0, s);
-    int rc = p.mode == KDGB_BUILD_TUNED ? build_tuned(t, tri_v_dev, n_tris, p, s)
-                                        : build_reference(t, tri_v_dev, n_tris, p, s);
+    int rc = KDGB_OK;
+    t.n_meshes = n_meshes > 1 ? n_meshes : 1;
+    if (n_meshes > 1) {
+        rc = ensure(t.mesh_off, (int64_t)n_meshes + 1, s);
+        if (rc == KDGB_OK) {
+            const cudaError_t e = cudaMemcpyAsync(t.mesh_off.p, mesh_off_host, sizeof(int32_t) * (n_meshes + 1),
+                                                  cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) rc = cuda_fail(e, "mesh offsets");
+        }
+    }
+    if (rc == KDGB_OK)
+        rc = build_reference(t, tri_v_dev, n_tris, p, s, n_meshes > 1 ? t.mesh_off.p : nullptr, t.n_meshes);
     if (rc == KDGB_OK) rc = pack_for_traversal(t, s);
     cudaEventRecord(e1, s);
     if (rc == KDGB_OK) {
@@ -454,6 +466,7 @@ int kdgb_trace(const kdgb_tree *tree, const kdgb_trace_params *params, const flo
     if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev)
         return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
     const Tree &t = tree->t;
+    if (t.n_meshes > 1) return fail(KDGB_ERR_INVALID_ARGUMENT, "batched tree: use kdgb_trace_batch");
     cudaStream_t s = (cudaStream_t)stream;
     if (p.tracer == KDGB_TRACER_BRUTE)
         return brute_launch(t.p0.p, t.p1.p, t.p2.p, t.n_tris, p.tie, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev,
@@ -472,6 +485,7 @@ int kdgb_trace_shadow(const kdgb_tree *tree, const kdgb_trace_params *params, co
     KDGB_CHECK(validate_trace_params(p, n));
     if (n == 0) return KDGB_OK;
     if (!points_dev || !occluded_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL buffer");
+    if (tree->t.n_meshes > 1) return fail(KDGB_ERR_UNSUPPORTED, "shadow rays of a batched tree");
     return shadow_launch(tree->t, p, points_dev, n, light, occluded_dev, (cudaStream_t)stream);
 }
 
@@ -488,6 +502,7 @@ int kdgb_trace_primary_shadow(const kdgb_tree *tree, const kdgb_trace_params *pa
     if (n == 0) return KDGB_OK;
     if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev || !occluded_dev)
         return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    if (tree->t.n_meshes > 1) return fail(KDGB_ERR_UNSUPPORTED, "shadow rays of a batched tree");
     return trace_launch(tree->t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, occluded_dev, light,
                         (cudaStream_t)stream);
 }
@@ -520,7 +535,63 @@ int kdgb_trace_photons(const kdgb_tree *tree, const kdgb_trace_params *params, c
         if (!std::isfinite(photons->light[k])) return fail(KDGB_ERR_INVALID_ARGUMENT, "non-finite light");
     if (n_photons == 0) return KDGB_OK;
     if (!seg_hit_dev || !seg_t_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL output buffer");
+    if (tree->t.n_meshes > 1) return fail(KDGB_ERR_UNSUPPORTED, "photons in a batched tree");
     return photon_launch(tree->t, p, *photons, n_photons, seg_hit_dev, seg_t_dev, (cudaStream_t)stream);
+}
+
+int kdgb_build_batch(const float *tri_v_dev, const int32_t *mesh_offsets, int32_t n_meshes,
+                     const kdgb_build_params *params, kdgb_tree **out, kdgb_stream_t stream)
+{
+    if (!out) return fail(KDGB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (n_meshes < 1 || !mesh_offsets) return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_build_batch: no meshes");
+    if (mesh_offsets[0] != 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_build_batch: mesh_offsets[0] must be 0");
+    for (int32_t m = 0; m < n_meshes; ++m)
+        if (mesh_offsets[m + 1] < mesh_offsets[m])
+            return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_build_batch: mesh_offsets must be non-decreasing");
+    const int32_t n_tris = mesh_offsets[n_meshes];
+    if (n_tris > 0 && !tri_v_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad triangle buffer");
+    KDGB_CHECK(check_device());
+    kdgb_build_params p;
+    if (params) p = *params; else kdgb_build_params_default(&p);
+    KDGB_CHECK(validate_build_params(p));
+    kdgb_tree *h = new (std::nothrow) kdgb_tree();
+    if (!h) return fail(KDGB_ERR_OUT_OF_MEMORY, "host allocation");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int rc = do_build(h->t, tri_v_dev, n_tris, p, s, mesh_offsets, n_meshes);
+    if (rc != KDGB_OK) {
+        release_all(h->t, s);
+        cudaStreamSynchronize(s);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return KDGB_OK;
+}
+
+int kdgb_trace_batch(const kdgb_tree *tree, const kdgb_trace_params *params, const float *ray_o_dev,
+                     const float *ray_d_dev, const int32_t *ray_mesh_dev, int32_t rays_per_mesh, int32_t n,
+                     int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev, kdgb_stream_t stream)
+{
+    if (!tree) return fail(KDGB_ERR_INVALID_ARGUMENT, "tree is NULL");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "negative ray count");
+    p.tile_width = 0;
+    KDGB_CHECK(validate_trace_params(p, n));
+    if (p.tracer == KDGB_TRACER_BRUTE) return fail(KDGB_ERR_UNSUPPORTED, "batched tracing needs a kd tracer");
+    if (!ray_mesh_dev && rays_per_mesh < 1)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_trace_batch: ray_mesh_dev or rays_per_mesh > 0 required");
+    if (!ray_mesh_dev && (int64_t)rays_per_mesh * tree->t.n_meshes < n)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_trace_batch: more rays than n_meshes * rays_per_mesh");
+    if (n == 0) return KDGB_OK;
+    if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    if (tree->t.n_meshes == 1)
+        return trace_launch(tree->t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, nullptr, nullptr,
+                            (cudaStream_t)stream);
+    return trace_launch(tree->t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, nullptr, nullptr,
+                        (cudaStream_t)stream, ray_mesh_dev, rays_per_mesh);
 }
 
 int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie, const float *ray_o_dev,
@@ -544,9 +615,3 @@ int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie, const 
 
 }  // extern "C"
 
-namespace kdgb {
-int build_tuned(Tree &, const float *, int32_t, const kdgb_build_params &, cudaStream_t)
-{
-    return fail(KDGB_ERR_UNSUPPORTED, "tuned build not available in this library build");
-}
-}  // namespace kdgb

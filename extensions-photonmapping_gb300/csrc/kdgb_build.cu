@@ -34,10 +34,21 @@ inline unsigned blocks_for(int64_t n, int b = kBlock) { return (unsigned)((n + b
 // ---------------------------------------------------------------------------
 // Geometry and primitive boxes (CalcPrimitiveAabb, TriangleUpper.h:10-28).
 // ---------------------------------------------------------------------------
+// Index of the mesh owning triangle i (mesh m owns [off[m], off[m+1])).
+__device__ __forceinline__ int mesh_of(const int32_t *__restrict__ off, int M, int32_t i)
+{
+    int lo = 0, hi = M - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 __global__ void k_load_geometry(const float *__restrict__ tri, int32_t T, float4 *__restrict__ p0,
                                 float4 *__restrict__ p1, float4 *__restrict__ p2,
                                 float4 *__restrict__ cmin, float4 *__restrict__ cmax,
-                                int *__restrict__ err)
+                                int *__restrict__ err, const int32_t *__restrict__ mesh_off = nullptr, int M = 1)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= T) return;
@@ -56,8 +67,10 @@ __global__ void k_load_geometry(const float *__restrict__ tri, int32_t T, float4
         float mnx = kmin(v[0], v[3]), mny = kmin(v[1], v[4]), mnz = kmin(v[2], v[5]);
         float mxx = kmax(v[0], v[3]), mxy = kmax(v[1], v[4]), mxz = kmax(v[2], v[5]);
         cmin[i] = make_float4(kmin(mnx, v[6]), kmin(mny, v[7]), kmin(mnz, v[8]), __int_as_float(i));
-        // w carries the local index of the owning active node (0 = root).
-        cmax[i] = make_float4(kmax(mxx, v[6]), kmax(mxy, v[7]), kmax(mxz, v[8]), __int_as_float(0));
+        // w carries the local index of the owning active node: the root of
+        // the triangle's mesh (0 for a single mesh).
+        const int owner = M > 1 ? mesh_of(mesh_off, M, i) : 0;
+        cmax[i] = make_float4(kmax(mxx, v[6]), kmax(mxy, v[7]), kmax(mxz, v[8]), __int_as_float(owner));
     }
 }
 
@@ -75,13 +88,19 @@ __device__ __forceinline__ void zero_node(int32_t j, int8_t *info, float *split,
     parent[j] = 0;
 }
 
-__global__ void k_init_root(int32_t T, int8_t *info, float *split, float4 *bmin, float4 *bmax,
-                            int32_t *pidx, int32_t *amt, int2 *ch, float *area, int32_t *parent)
+// Roots (TriangleMapUpperCreator.cu:128-136): node m is the root of mesh m,
+// covering references [off[m], off[m+1]) (a single mesh: node 0, all of them).
+__global__ void k_init_roots(int32_t T, int M, const int32_t *__restrict__ mesh_off, int8_t *info, float *split,
+                             float4 *bmin, float4 *bmax, int32_t *pidx, int32_t *amt, int2 *ch, float *area,
+                             int32_t *parent)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        zero_node(0, info, split, bmin, bmax, pidx, amt, ch, area, parent);
-        amt[0] = T;  // TriangleMapUpperCreator.cu:128-136
-    }
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    zero_node(m, info, split, bmin, bmax, pidx, amt, ch, area, parent);
+    const int32_t a = M > 1 ? mesh_off[m] : 0, b = M > 1 ? mesh_off[m + 1] : T;
+    pidx[m] = a;
+    amt[m] = b - a;
+    parent[m] = m;
 }
 
 // ---------------------------------------------------------------------------
@@ -374,6 +393,120 @@ __global__ void k_node_lanes(int32_t R, int32_t LS, const int32_t *__restrict__ 
     const int ll = l < LS, rl = r < LS;
     int32_t *o = lanes + kLanes * (int64_t)k;
     o[0] = l; o[1] = r; o[2] = ll ? l : 0; o[3] = rl ? r : 0; o[4] = ll; o[5] = rl;
+}
+
+// ---------------------------------------------------------------------------
+// Tuned mode: binned SAH for the upper levels below `upper_levels` (new in
+// this build; the reference splits every upper level at the median).  Per
+// node and axis with extent > 0: B equal bins over the tight box; each
+// reference adds 1 to the bin of its box min (left histogram) and of its box
+// max (right histogram).  The plane at bin boundary k has NL = left counts
+// below k, NR = right counts from k up and cost AL*NL + AR*NR (half box
+// areas); the first strict minimum over (axis X,Y,Z; k = 1..B-1) wins,
+// skipping planes that leave a side empty or keep every reference on both
+// sides; without a qualifying plane the median split stays.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int sah_bin(float x, float mn, float scale, int B)
+{
+    const int b = (int)__fmul_rn(__fsub_rn(x, mn), scale);
+    return b < 0 ? 0 : (b > B - 1 ? B - 1 : b);
+}
+
+// Histograms hist[((node * 3 + axis) * 2 + side) * B + bin]; lanes of a
+// warp with the same (owner, axis, side, bin) add once.
+__global__ void __launch_bounds__(kBlock) k_sah_bin(int64_t N, int32_t active, int B, const float4 *__restrict__ cmin,
+                                                   const float4 *__restrict__ cmax, const float4 *__restrict__ bmin,
+                                                   const float4 *__restrict__ bmax, int32_t *__restrict__ hist)
+{
+    const unsigned lane = threadIdx.x & 31;
+    const int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kChunk;
+    for (int row = 0; row < kRows; ++row) {
+        if (base + row * 32 >= N) break;
+        const int64_t r = base + row * 32 + lane;
+        int o = -1;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a, mn = a, mx = a;
+        if (r < N) {
+            a = cmin[r];
+            b = cmax[r];
+            o = __float_as_int(b.w);
+            mn = bmin[active + o];
+            mx = bmax[active + o];
+        }
+        for (int ax = 0; ax < 3; ++ax) {
+            const float lo = ax == 0 ? mn.x : (ax == 1 ? mn.y : mn.z);
+            const float ext = __fsub_rn(ax == 0 ? mx.x : (ax == 1 ? mx.y : mx.z), lo);
+            const bool valid = o >= 0 && ext > 0.0f;
+            const float scale = valid ? __fdiv_rn((float)B, ext) : 0.0f;
+            for (int side = 0; side < 2; ++side) {
+                const float4 &src = side == 0 ? a : b;
+                const float x = ax == 0 ? src.x : (ax == 1 ? src.y : src.z);
+                const int bin = valid ? sah_bin(x, lo, scale, B) : 0;
+                // Key: (owner, bin); invalid lanes get a key no valid lane has.
+                const long long key = valid ? ((long long)o << 8 | bin) : -1ll;
+                const unsigned m = __match_any_sync(kFull, key);
+                if (valid && lane == (unsigned)(__ffs(m) - 1))
+                    atomicAdd(hist + (((int64_t)o * 3 + ax) * 2 + side) * B + bin, __popc(m));
+            }
+        }
+    }
+}
+
+// One warp per node, lane k-1 evaluates the plane at bin boundary k.
+__global__ void k_sah_split(int32_t R, int32_t active, int B, const float4 *__restrict__ bmin,
+                            const float4 *__restrict__ bmax, const int32_t *__restrict__ amt,
+                            const int32_t *__restrict__ hist, float *__restrict__ split, int8_t *__restrict__ info)
+{
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= R) return;
+    const int32_t node = active + (int32_t)gw;
+    const int32_t a = amt[node];
+    const float4 mn4 = bmin[node], mx4 = bmax[node];
+    const float mnv[3] = {mn4.x, mn4.y, mn4.z}, mxv[3] = {mx4.x, mx4.y, mx4.z};
+    const float ext[3] = {__fsub_rn(mxv[0], mnv[0]), __fsub_rn(mxv[1], mnv[1]), __fsub_rn(mxv[2], mnv[2])};
+    float best = INFINITY, best_sp = 0.0f;
+    int best_ax = -1;
+    for (int ax = 0; ax < 3; ++ax) {
+        if (!(ext[ax] > 0.0f)) continue;  // warp-uniform
+        const int32_t *h = hist + ((int64_t)gw * 3 + ax) * 2 * B;
+        const int32_t lo = lane < B ? h[lane] : 0, hi = lane < B ? h[B + lane] : 0;
+        int32_t plo = lo, phi = hi;  // inclusive prefix sums over bins
+        for (int s = 1; s < 32; s <<= 1) {
+            const int32_t x = __shfl_up_sync(kFull, plo, s), y = __shfl_up_sync(kFull, phi, s);
+            if (lane >= s) { plo += x; phi += y; }
+        }
+        const int32_t total_hi = __shfl_sync(kFull, phi, 31);
+        const int k = lane + 1;
+        float cost = INFINITY, pk = 0.0f;
+        if (k < B) {
+            const int32_t nl = plo, nr = total_hi - phi;
+            const float w = __fdiv_rn(ext[ax], (float)B);
+            pk = __fadd_rn(mnv[ax], __fmul_rn((float)k, w));
+            float le[3] = {ext[0], ext[1], ext[2]}, re[3] = {ext[0], ext[1], ext[2]};
+            le[ax] = __fsub_rn(pk, mnv[ax]);
+            re[ax] = __fsub_rn(mxv[ax], pk);
+            const float al = __fadd_rn(__fadd_rn(__fmul_rn(le[0], le[1]), __fmul_rn(le[1], le[2])), __fmul_rn(le[2], le[0]));
+            const float ar = __fadd_rn(__fadd_rn(__fmul_rn(re[0], re[1]), __fmul_rn(re[1], re[2])), __fmul_rn(re[2], re[0]));
+            const float c = __fadd_rn(__fmul_rn(al, (float)nl), __fmul_rn(ar, (float)nr));
+            if (nl > 0 && nr > 0 && !(nl == a && nr == a)) cost = c;
+        }
+        // First minimum in k order within the axis, then strictly better
+        // than the previous axes.
+        float c = cost;
+        int kk = k;
+        for (int s = 16; s > 0; s >>= 1) {
+            const float c2 = __shfl_xor_sync(kFull, c, s);
+            const int k2 = __shfl_xor_sync(kFull, kk, s);
+            if (c2 < c || (c2 == c && k2 < kk)) { c = c2; kk = k2; }
+        }
+        const float sp = __shfl_sync(kFull, pk, kk - 1);
+        if (c < best) { best = c; best_ax = ax; best_sp = sp; }
+    }
+    if (lane == 0 && best_ax >= 0) {
+        info[node] = (int8_t)(best_ax + 1);
+        split[node] = best_sp;
+    }
 }
 
 // Writes one reference to its child (or final leaf) slot: destination = node
@@ -964,8 +1097,10 @@ int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s)
     return KDGB_OK;
 }
 
-int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p, cudaStream_t s)
+int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p, cudaStream_t s,
+                    const int32_t *mesh_off_dev, int32_t M)
 {
+    if (M < 1) M = 1;
     const int32_t LS = p.leaf_size;
     Workspace &w = t.ws;
     KDGB_CHECK(host_record(w));
@@ -982,17 +1117,17 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
     KDGB_CUDA(cudaMemsetAsync(w.stats.p, 0, 16 * sizeof(int32_t), s));
     if (T > 0) {
         k_load_geometry<<<blocks_for(T), kBlock, 0, s>>>(tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, w.cmin.p, w.cmax.p,
-                                                        w.stats.p + 15);
+                                                        w.stats.p + 15, mesh_off_dev, M);
         KDGB_LAUNCH_CHECK();
     }
     t.n_nodes = 0;
-    KDGB_CHECK(grow_nodes(t, 1, s));
-    k_init_root<<<1, 32, 0, s>>>(T, NODE_ARGS);
+    KDGB_CHECK(grow_nodes(t, M, s));
+    k_init_roots<<<blocks_for(M), kBlock, 0, s>>>(T, M, mesh_off_dev, NODE_ARGS);
     KDGB_LAUNCH_CHECK();
-    t.n_nodes = 1;
+    t.n_nodes = M;
 
     int64_t N = T, F = 0;
-    int32_t active = 0, R = 1, level = 0;
+    int32_t active = 0, R = M, level = 0;
     std::vector<int2> leaf_ranges;
     std::vector<int32_t> leaf_off;
     int32_t n_leaf_ids = 0;
@@ -1000,7 +1135,10 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
     while (R > 0) {
         if (level >= p.max_levels) return fail(KDGB_ERR_DEGENERATE, "upper build exceeded max_levels");
         ++level;
-        const bool do_ess = p.split_empty_space && active != 0;
+        // Tuned mode: median/empty-space splits on the first upper_levels
+        // levels, binned SAH below them.
+        const bool sah_level = p.mode == KDGB_BUILD_TUNED && level > p.upper_levels;
+        const bool do_ess = p.split_empty_space && active != 0 && !sah_level;
         const int64_t nch = chunks_for(N);
         const unsigned ngrid = chunk_blocks(nch);
         KDGB_CHECK(grow_nodes(t, (int64_t)t.n_nodes + 14 * (int64_t)R, s));
@@ -1036,6 +1174,16 @@ int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build
                                                       w.keys.p, t.bmin.p, t.bmax.p, t.split.p, t.info.p, w.planes.p,
                                                       w.lanes.p);
         KDGB_LAUNCH_CHECK();
+        if (sah_level && N > 0) {
+            const int B = p.sah_bins;
+            KDGB_CHECK(grab(w.misc0, (int64_t)R * 6 * B, s));
+            KDGB_CUDA(cudaMemsetAsync(w.misc0.p, 0, sizeof(int32_t) * (size_t)R * 6 * B, s));
+            k_sah_bin<<<ngrid, kBlock, 0, s>>>(N, active, B, w.cmin.p, w.cmax.p, t.bmin.p, t.bmax.p, w.misc0.p);
+            KDGB_LAUNCH_CHECK();
+            k_sah_split<<<blocks_for((int64_t)R * 32), kBlock, 0, s>>>(R, active, B, t.bmin.p, t.bmax.p, t.bitmap.p,
+                                                                      w.misc0.p, t.split.p, t.info.p);
+            KDGB_LAUNCH_CHECK();
+        }
         if (N > 0) {
             k_count<<<ngrid, kBlock, 0, s>>>(N, active, w.cmin.p, w.cmax.p, t.split.p, t.info.p, w.cnt.p,
                                              w.chunksum.p);

@@ -87,7 +87,9 @@ struct Tree {
     int32_t n_refs = 0;
     int32_t n_upper_leaves = 0;
     int32_t n_leaf_tris = 0;     // rows of the leaf-ordered triangle records
+    int32_t n_meshes = 1;        // forest roots (kdgb_build_batch)
     kdgb_build_stats stats{};
+    DevArray<int32_t> mesh_off;  // n_meshes + 1 triangle offsets (batches only)
 
     // Geometry (GeometryList SoA) and the packed triangle array used by builds.
     DevArray<float4> p0, p1, p2;
@@ -109,11 +111,11 @@ struct Tree {
     Workspace ws;
 };
 
-// Builders (kdgb_build.cu).  tri_v_dev: T*9 floats.
+// Builder (kdgb_build.cu), both modes.  tri_v_dev: T*9 floats.  With M > 1
+// the triangles are M meshes (mesh m = [mesh_off[m], mesh_off[m+1]), device
+// offsets) built as one forest whose root of mesh m is node m.
 int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p,
-                    cudaStream_t s);
-int build_tuned(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p,
-                cudaStream_t s);
+                    cudaStream_t s, const int32_t *mesh_off_dev = nullptr, int32_t M = 1);
 int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s);
 
 // Traversal layout from the SoA arrays (kdgb_trace.cu).

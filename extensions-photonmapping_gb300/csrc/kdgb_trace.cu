@@ -90,6 +90,7 @@ struct Ctx {
     const float4 *__restrict__ bmin;
     const float4 *__restrict__ bmax;
     const float4 *__restrict__ tri;
+    int root;  // root node of the ray's tree (forest of a batch: its mesh index)
 };
 
 // Moeller-Trumbore on one packed record (IRayTracer.h:111-145).
@@ -156,8 +157,8 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
     int iters = 0;
     do {
         float tnext = KDGB_FINF;
-        int node = 0;
-        int4 nd = __ldg(c.node);
+        int node = c.root;
+        int4 nd = __ldg(c.node + c.root);
         while (nd.w != KDGB_LEAF) {
             const float ori = axis_of(o, nd.w), dir = axis_of(inv, nd.w);
             const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
@@ -196,7 +197,7 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
         int node;
         float tnext;
         if (cnt == 0) {
-            node = 0;
+            node = c.root;
             tnext = KDGB_FINF;
         } else {
             nxt = (nxt == 0 ? depth : nxt) - 1;
@@ -248,8 +249,8 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit)
     int iters = 0;
     do {
         float tnext = KDGB_FINF;
-        int node = 0;
-        int4 nd = __ldg(c.node);
+        int node = c.root;
+        int4 nd = __ldg(c.node + c.root);
         while (nd.w != KDGB_LEAF) {
             const float ori = axis_of(lp, nd.w), dir = axis_of(inv, nd.w);
             const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
@@ -295,6 +296,11 @@ struct TraceArgs {
     int32_t *occ;
     float3 light;
     int tie, depth, maxit, tile_width;
+    // Batches: ray i belongs to mesh ray_mesh[i] (or i / rays_per_mesh when
+    // ray_mesh is NULL); its tree's root is node m and hit ids are returned
+    // relative to the mesh's first triangle mesh_off[m].
+    const int32_t *mesh_off, *ray_mesh;
+    int32_t rays_per_mesh, n_meshes;
 };
 
 template <int TRACER, bool SKIP, bool SHADOW>
@@ -305,14 +311,22 @@ __global__ void k_trace(TraceArgs a)
     if (id >= a.n) return;
     const int64_t i = ray_index(id, a.tile_width);
     const float3 o = ld3(a.o, i), d = ld3(a.d, i);
+    Ctx c = a.c;
+    int32_t id_off = 0;
+    if (a.mesh_off) {
+        int m = a.ray_mesh ? a.ray_mesh[i] : (int)(i / a.rays_per_mesh);
+        m = m < 0 ? 0 : (m >= a.n_meshes ? a.n_meshes - 1 : m);
+        c.root = m;
+        id_off = a.mesh_off[m];
+    }
     float t = 0.0f, u = 0.0f, v = 0.0f;
     int h;
     if (TRACER == KDGB_TRACER_SHORTSTACK)
-        h = trace_shortstack<SKIP>(a.c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u, v);
+        h = trace_shortstack<SKIP>(c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u, v);
     else
-        h = trace_restart<SKIP>(a.c, o, d, a.tie, a.maxit, t, u, v);
+        h = trace_restart<SKIP>(c, o, d, a.tie, a.maxit, t, u, v);
     if (h < 0) { t = INFINITY; u = 0.0f; v = 0.0f; }
-    a.hit[i] = h;
+    a.hit[i] = h >= 0 ? h - id_off : h;
     a.t[i] = t;
     a.u[i] = u;
     a.v[i] = v;
@@ -321,7 +335,7 @@ __global__ void k_trace(TraceArgs a)
         if (h >= 0) {
             const float3 p = make_float3(__fadd_rn(o.x, __fmul_rn(t, d.x)), __fadd_rn(o.y, __fmul_rn(t, d.y)),
                                          __fadd_rn(o.z, __fmul_rn(t, d.z)));
-            occ = trace_shadow(a.c, a.light, p, a.maxit);
+            occ = trace_shadow(c, a.light, p, a.maxit);
         }
         a.occ[i] = occ;
     }
@@ -480,13 +494,25 @@ int pack_for_traversal(Tree &t, cudaStream_t s)
 }
 
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
-                 int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s)
+                 int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s,
+                 const int32_t *ray_mesh, int32_t rays_per_mesh)
 {
     TraceArgs a;
     a.c.node = t.tnode.p;
     a.c.bmin = t.bmin.p;
     a.c.bmax = t.bmax.p;
     a.c.tri = t.ttri.p;
+    a.c.root = 0;
+    a.mesh_off = nullptr;
+    a.ray_mesh = nullptr;
+    a.rays_per_mesh = 1;
+    a.n_meshes = 1;
+    if (t.n_meshes > 1) {
+        a.mesh_off = t.mesh_off.p;
+        a.ray_mesh = ray_mesh;
+        a.rays_per_mesh = rays_per_mesh > 0 ? rays_per_mesh : 1;
+        a.n_meshes = t.n_meshes;
+    }
     a.o = o; a.d = d; a.n = n;
     a.hit = hit; a.t = tt; a.u = uu; a.v = vv; a.occ = occ;
     a.light = light ? make_float3(light[0], light[1], light[2]) : make_float3(0.f, 0.f, 0.f);
@@ -523,6 +549,11 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
     a.c.bmin = t.bmin.p;
     a.c.bmax = t.bmax.p;
     a.c.tri = t.ttri.p;
+    a.c.root = 0;
+    a.mesh_off = nullptr;
+    a.ray_mesh = nullptr;
+    a.rays_per_mesh = 1;
+    a.n_meshes = 1;
     a.o = pts; a.d = nullptr; a.n = n;
     a.hit = nullptr; a.t = a.u = a.v = nullptr; a.occ = occ;
     a.light = make_float3(light[0], light[1], light[2]);
@@ -551,6 +582,7 @@ int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_p
     a.c.bmin = t.bmin.p;
     a.c.bmax = t.bmax.p;
     a.c.tri = t.ttri.p;
+    a.c.root = 0;
     a.p0 = t.p0.p; a.p1 = t.p1.p; a.p2 = t.p2.p;
     a.light = make_float3(ph.light[0], ph.light[1], ph.light[2]);
     a.key = make_uint2((unsigned)(ph.seed & 0xffffffffu), (unsigned)(ph.seed >> 32));

@@ -249,6 +249,42 @@ def _trace_photons(self, n_photons: int, params: TraceParams | None = None, phot
 KDTree.trace_photons = _trace_photons
 
 
+def _build_batch(cls, tris, mesh_offsets, params: BuildParams | None = None, stream=None, **kw) -> "KDTree":
+    """One forest over meshes stored back to back (kdgb_build_batch);
+    mesh_offsets has n_meshes + 1 entries."""
+    tri = _dev(tris, _torch().float32, 9)
+    off = np.ascontiguousarray(mesh_offsets, dtype=np.int32)
+    p = params if params is not None else build_params(**kw)
+    h = C.c_void_p()
+    check(lib().kdgb_build_batch(_ptr(tri), off.ctypes.data_as(C.c_void_p), off.shape[0] - 1, C.byref(p),
+                                 C.byref(h), C.c_void_p(_stream(stream))), "kdgb_build_batch")
+    tree = cls(h, tri.shape[0])
+    tree.mesh_offsets = off
+    return tree
+
+
+def _trace_batch(self, o, d, ray_mesh=None, rays_per_mesh: int = 0, params: TraceParams | None = None, stream=None,
+                 out=None, **kw):
+    """Rays of a batch (kdgb_trace_batch): hit ids relative to each mesh."""
+    torch = _torch()
+    o = _dev(o, torch.float32, 3)
+    d = _dev(d, torch.float32, 3)
+    rm = _dev(ray_mesh, torch.int32).reshape(-1) if ray_mesh is not None else None
+    n = o.shape[0]
+    p = params if params is not None else trace_params(**kw)
+    if out is None:
+        out = (torch.empty(n, dtype=torch.int32, device=o.device), torch.empty(n, dtype=torch.float32, device=o.device),
+               torch.empty(n, dtype=torch.float32, device=o.device), torch.empty(n, dtype=torch.float32, device=o.device))
+    hit, t, u, v = out
+    check(lib().kdgb_trace_batch(self._h, C.byref(p), _ptr(o), _ptr(d), _ptr(rm), rays_per_mesh, n, _ptr(hit),
+                                 _ptr(t), _ptr(u), _ptr(v), C.c_void_p(_stream(stream))), "kdgb_trace_batch")
+    return hit, t, u, v
+
+
+KDTree.build_batch = classmethod(_build_batch)
+KDTree.trace_batch = _trace_batch
+
+
 def backward(vertices, indices, o, d, hit, dL_dt, dL_du, dL_dv, out=None, stream=None):
     """dL/dvertex (V, 3) float32 for an indexed mesh, reusing the forward's
     hit ids (kdgb_backward); `out` is accumulated into when given."""

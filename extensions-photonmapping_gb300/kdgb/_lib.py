@@ -84,6 +84,8 @@ SIGNATURES = {
     "kdgb_trace_primary_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P, P, P]),
     "kdgb_photon_params_default": (None, [C.POINTER(PhotonParams)]),
     "kdgb_trace_photons": (C.c_int, [P, C.POINTER(TraceParams), C.POINTER(PhotonParams), C.c_int32, P, P, P]),
+    "kdgb_build_batch": (C.c_int, [P, P, C.c_int32, C.POINTER(BuildParams), C.POINTER(C.c_void_p), P]),
+    "kdgb_trace_batch": (C.c_int, [P, C.POINTER(TraceParams), P, P, P, C.c_int32, C.c_int32, P, P, P, P, P]),
     "kdgb_geometry_gather": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, P]),
     "kdgb_osc_update_surface": (C.c_int, [P, P, C.c_int32, C.c_float, C.c_float, P]),
     "kdgb_backward": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, C.c_int32, P, P, P, P, P, P]),

@@ -66,8 +66,9 @@ enum { KDGB_LEAF = 0, KDGB_X = 1, KDGB_Y = 2, KDGB_Z = 3 };
 enum { KDGB_LOWER_BITMAP = 0, KDGB_LOWER_SAH = 1 };
 
 /* Build modes.  REFERENCE reproduces TriangleMap::Create bit for bit.
- * TUNED runs median/empty-space splits for the top `upper_levels` levels and
- * a binned SAH (traversal_cost, intersection_cost, leaf_size) below them. */
+ * TUNED runs the reference's median/empty-space splits for the top
+ * `upper_levels` levels and a binned SAH (sah_bins bins per axis) for the
+ * remaining upper levels; the lower phase is chosen by `lower` as before. */
 enum { KDGB_BUILD_REFERENCE = 0, KDGB_BUILD_TUNED = 1 };
 
 /* Tracers: Raytracer (kd-restart), ShortStack, BruteTracer. */
@@ -91,7 +92,7 @@ typedef struct kdgb_build_params {
     int32_t max_levels;            /* upper-phase level guard, default 64 */
     int32_t leaf_size;             /* KDNode.h:21 KDNODE_MAX_LOWER_SIZE, default 32, <= 32 */
     int32_t upper_levels;          /* TUNED: median/empty-space levels before SAH, default 8 */
-    int32_t sah_bins;              /* TUNED: SAH bins per axis, default 32 */
+    int32_t sah_bins;              /* TUNED: SAH bins per axis, 2..32, default 32 */
 } kdgb_build_params;
 
 typedef struct kdgb_trace_params {
@@ -224,6 +225,25 @@ KDGB_API void kdgb_photon_params_default(kdgb_photon_params *p);
 KDGB_API int kdgb_trace_photons(const kdgb_tree *tree, const kdgb_trace_params *params,
                                 const kdgb_photon_params *photons, int32_t n_photons,
                                 int32_t *seg_hit_dev, float *seg_t_dev, kdgb_stream_t stream);
+
+/* Batched build (no reference counterpart; the reference builds one scene
+ * per TriangleMap): n_meshes independent meshes stored back to back in
+ * tri_v_dev (mesh m = triangles [mesh_offsets[m], mesh_offsets[m+1]),
+ * mesh_offsets: n_meshes+1 HOST ints) are built as one forest in a single
+ * level loop: every level processes the active nodes of all meshes at once.
+ * The root of mesh m is node m; each mesh's tree is the tree kdgb_build
+ * makes for that mesh alone (same splits, leaves and reference order, node
+ * ids interleaved).  Trace it with kdgb_trace_batch. */
+KDGB_API int kdgb_build_batch(const float *tri_v_dev, const int32_t *mesh_offsets, int32_t n_meshes,
+                              const kdgb_build_params *params, kdgb_tree **out, kdgb_stream_t stream);
+
+/* Traces rays of a batch: ray i belongs to mesh ray_mesh_dev[i], or to mesh
+ * i / rays_per_mesh when ray_mesh_dev is NULL.  Hit ids are relative to the
+ * mesh's first triangle. */
+KDGB_API int kdgb_trace_batch(const kdgb_tree *tree, const kdgb_trace_params *params,
+                              const float *ray_o_dev, const float *ray_d_dev, const int32_t *ray_mesh_dev,
+                              int32_t rays_per_mesh, int32_t n, int32_t *hit_dev, float *t_dev, float *u_dev,
+                              float *v_dev, kdgb_stream_t stream);
 
 /* Adjoint of first-hit t, u, v with respect to vertex positions (no
  * reference counterpart).  vertices: n_vertices*3 floats; indices:

@@ -541,6 +541,9 @@ void or_build_params_default(or_build_params *p)
     p->esc_zmax_as_x = 1;
     p->max_levels = 64;
     p->leaf_size = 32;
+    p->mode = 0;
+    p->upper_levels = 8;
+    p->sah_bins = 32;
 }
 
 void or_trace_params_default(or_trace_params *p)
@@ -627,6 +630,73 @@ static void excl_scan(const int32_t *in, int64_t n, int32_t *out)
     out[n] = s;
 }
 
+/* Half surface area of a box with edge lengths e0, e1, e2. */
+static inline float half_area(float e0, float e1, float e2) { return (e0 * e1 + e1 * e2) + e2 * e0; }
+
+/* Binned SAH over the references [s, s + a) inside tight box (mn, mx): B
+ * equal bins per axis with extent > 0; a reference counts in the bin of its
+ * box min (left histogram) and of its box max (right histogram); the plane at
+ * bin boundary k has NL = sum of left counts below k and NR = sum of right
+ * counts from k up, cost AL*NL + AR*NR with half box areas.  The first
+ * strict minimum over (axis X, Y, Z; k = 1..B-1) wins; planes that leave a
+ * side empty or put every reference on both sides are skipped.  Returns 0
+ * when no plane qualifies (the median split is kept). */
+static int sah_binned_split(const f4 *cmin, const f4 *cmax, int32_t s, int32_t a, f4 mn, f4 mx, int B,
+                            int *axis_out, float *split_out)
+{
+    int32_t lo[3][256], hi[3][256];
+    const float mnv[3] = {mn.x, mn.y, mn.z}, mxv[3] = {mx.x, mx.y, mx.z};
+    float ext[3], scale[3];
+    int valid[3];
+    for (int ax = 0; ax < 3; ++ax) {
+        ext[ax] = mxv[ax] - mnv[ax];
+        valid[ax] = ext[ax] > 0.0f;
+        scale[ax] = valid[ax] ? (float)B / ext[ax] : 0.0f;
+        for (int b = 0; b < B; ++b) lo[ax][b] = hi[ax][b] = 0;
+    }
+    for (int32_t r = s; r < s + a; ++r) {
+        const float lv[3] = {cmin[r].x, cmin[r].y, cmin[r].z}, hv[3] = {cmax[r].x, cmax[r].y, cmax[r].z};
+        for (int ax = 0; ax < 3; ++ax) {
+            if (!valid[ax]) continue;
+            int bl = (int)((lv[ax] - mnv[ax]) * scale[ax]);
+            int bh = (int)((hv[ax] - mnv[ax]) * scale[ax]);
+            bl = bl < 0 ? 0 : (bl > B - 1 ? B - 1 : bl);
+            bh = bh < 0 ? 0 : (bh > B - 1 ? B - 1 : bh);
+            lo[ax][bl]++;
+            hi[ax][bh]++;
+        }
+    }
+    float best = INFINITY, best_sp = 0.0f;
+    int best_ax = -1;
+    for (int ax = 0; ax < 3; ++ax) {
+        if (!valid[ax]) continue;
+        const float w = ext[ax] / (float)B;
+        int32_t total_hi = 0;
+        for (int b = 0; b < B; ++b) total_hi += hi[ax][b];
+        int32_t nl = 0, hi_below = 0;
+        for (int k = 1; k < B; ++k) {
+            nl += lo[ax][k - 1];
+            hi_below += hi[ax][k - 1];
+            const int32_t nr = total_hi - hi_below;
+            const float pk = mnv[ax] + (float)k * w;
+            float le[3] = {ext[0], ext[1], ext[2]}, re[3] = {ext[0], ext[1], ext[2]};
+            le[ax] = pk - mnv[ax];
+            re[ax] = mxv[ax] - pk;
+            const float al = half_area(le[0], le[1], le[2]), ar = half_area(re[0], re[1], re[2]);
+            const float cost = al * (float)nl + ar * (float)nr;
+            if (nl > 0 && nr > 0 && !(nl == a && nr == a) && cost < best) {
+                best = cost;
+                best_ax = ax;
+                best_sp = pk;
+            }
+        }
+    }
+    if (best_ax < 0) return 0;
+    *axis_out = best_ax + 1;
+    *split_out = best_sp;
+    return 1;
+}
+
 /*
  * Upper ("large node") phase: TriangleMapUpperCreator.cu:110-183 (Create),
  * :185-205 (ProcessNodes), :241-318 (ReduceAabb), :320-368 (CreateEmptySplits),
@@ -693,8 +763,9 @@ static int build_upper(const float *tri, int32_t T, const or_build_params *p, no
         }
 
         /* CreateEmptySplits, not at the root (TriangleMapUpperCreator.cu:302-303,
-         * EmptySpaceSplitting.h:10-184). */
-        if (p->split_empty_space && active != 0) {
+         * EmptySpaceSplitting.h:10-184); in tuned mode only on the median levels. */
+        const int sah_level = p->mode == 1 && level > p->upper_levels;
+        if (p->split_empty_space && active != 0 && !sah_level) {
             free(planes); free(req); free(eaddr);
             planes = calloc((size_t)R, 1); req = calloc((size_t)R, sizeof(int32_t));
             eaddr = calloc((size_t)R + 1, sizeof(int32_t));
@@ -777,6 +848,20 @@ static int build_upper(const float *tri, int32_t T, const or_build_params *p, no
             const int z_higher = mxs < sz;
             nd->split[active + k] = z_higher ? mdz : sp;
             nd->info[active + k] = z_higher ? OR_Z : ax;
+        }
+        /* Tuned mode below the median levels: binned SAH split (new in this
+         * build; the reference splits every upper level at the median). */
+        if (sah_level) {
+#pragma omp parallel for schedule(dynamic, 8)
+            for (int32_t k = 0; k < R; ++k) {
+                int axis;
+                float sp;
+                if (sah_binned_split(cmin, cmax, nd->pidx[active + k], nd->amt[active + k], nd->bmin[active + k],
+                                     nd->bmax[active + k], p->sah_bins, &axis, &sp)) {
+                    nd->info[active + k] = (int8_t)axis;
+                    nd->split[active + k] = sp;
+                }
+            }
         }
 
         /* CreateChildren (TriangleMapUpperCreator.cu:467-759). */
@@ -1198,6 +1283,7 @@ int or_build(const float *tri, int32_t T, const or_build_params *p, or_tree *out
 {
     if (!out || !p || T < 0 || (T > 0 && !tri)) return OR_ERR_ARG;
     if (p->leaf_size < 1 || p->leaf_size > 32) return OR_ERR_ARG;
+    if (p->mode == 1 && (p->sah_bins < 2 || p->sah_bins > 32 || p->upper_levels < 0)) return OR_ERR_ARG;
     memset(out, 0, sizeof(*out));
     nodes nd;
     memset(&nd, 0, sizeof(nd));

@@ -49,6 +49,9 @@ typedef struct or_build_params {
     int32_t esc_zmax_as_x;         /* 1 = reproduce EmptySpaceSplitting.h:172-181 (max-z face cut on x) */
     int32_t max_levels;            /* guard against non-terminating upper loops */
     int32_t leaf_size;             /* upper leaf threshold: children with < leaf_size refs become leaves (32) */
+    int32_t mode;                  /* 0 reference, 1 tuned (binned SAH below upper_levels) */
+    int32_t upper_levels;          /* tuned: median / empty-space levels before the binned SAH */
+    int32_t sah_bins;              /* tuned: bins per axis */
 } or_build_params;
 
 typedef struct or_tree {

@@ -31,7 +31,8 @@ class BuildParams(C.Structure):
                 ("propagate_aabbs", C.c_int32), ("empty_space_threshold", C.c_float),
                 ("traversal_cost", C.c_float), ("intersection_cost", C.c_float),
                 ("min_leaf", C.c_int32), ("esc_zmax_as_x", C.c_int32),
-                ("max_levels", C.c_int32), ("leaf_size", C.c_int32)]
+                ("max_levels", C.c_int32), ("leaf_size", C.c_int32), ("mode", C.c_int32),
+                ("upper_levels", C.c_int32), ("sah_bins", C.c_int32)]
 
 
 class TraceParams(C.Structure):

@@ -125,7 +125,9 @@ def test_backward_accumulates_and_ignores_misses(kdgb_lib, cuda, c5):
                            c5["a"])
     g2 = kdgb_lib.backward(c5["verts"], c5["idx"].astype(np.uint32), c5["o"], c5["d"], c5["hit"], c5["w"], c5["a"],
                            c5["a"], out=g1.clone())
-    assert torch.allclose(g2, 2 * g1, rtol=1e-5, atol=1e-5)
+    # Float atomics: the summation order differs between calls, so compare in
+    # norm (vertices whose contributions cancel have large relative noise).
+    assert float((g2 - 2 * g1).norm() / (2 * g1).norm()) < 1e-6
     none = np.full_like(c5["hit"], -1)
     g0 = kdgb_lib.backward(c5["verts"], c5["idx"].astype(np.uint32), c5["o"], c5["d"], none, c5["w"], c5["a"],
                            c5["a"])

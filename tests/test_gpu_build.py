@@ -72,6 +72,29 @@ def test_build_options_match_oracle(kdgb_lib, cuda, oracle, opts):
         assert_same_tree(tree.to_host(), ref)
 
 
+TUNED = dict(mode=1, upper_levels=8, sah_bins=32, lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
+
+
+@pytest.mark.parametrize("name", ["c1", "clustered3k", "clustered60k", "soup", "degenerate"])
+def test_tuned_build_matches_oracle(kdgb_lib, cuda, oracle, name):
+    """Tuned mode (median/empty-space for 8 levels, then binned SAH) is new
+    in this build; the oracle restates it, so the trees must be identical."""
+    tris = scene(name)
+    ref = oracle.build(tris, **TUNED)
+    with kdgb_lib.KDTree.build(tris, **TUNED) as tree:
+        assert_same_tree(tree.to_host(), ref)
+
+
+@pytest.mark.parametrize("opts", [dict(upper_levels=0), dict(upper_levels=3, sah_bins=8), dict(sah_bins=2),
+                                  dict(upper_levels=40)])
+def test_tuned_build_options(kdgb_lib, cuda, oracle, opts):
+    kw = dict(TUNED, **opts)
+    tris = scenes.clustered(20000, seed=16)
+    ref = oracle.build(tris, **kw)
+    with kdgb_lib.KDTree.build(tris, **kw) as tree:
+        assert_same_tree(tree.to_host(), ref)
+
+
 @pytest.mark.parametrize("T", [0, 1, 2, 31, 32, 33, 257])
 def test_small_and_empty_builds(kdgb_lib, cuda, oracle, T):
     tris = tri_soup(max(T, 1), 30)[:T]

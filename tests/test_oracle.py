@@ -104,6 +104,29 @@ def test_tree_invariants(oracle, scene, lower):
         assert used[area > 0].all()
 
 
+@pytest.mark.parametrize("upper", [0, 4, 8])
+def test_tuned_tree_invariants_and_hits(oracle, upper):
+    tris = scenes.clustered(20000, seed=17)
+    kw = dict(mode=1, upper_levels=upper, lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
+    tree = oracle.build(tris, **kw)
+    used, area = check_tree(tree, tris)
+    assert used[area > 0].all()
+    lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
+    o, d = scenes.random_rays(3000, 18, lo, hi)
+    hb = oracle.trace(None, tris, o, d, tracer=2)[0]
+    for tracer in (0, 1):
+        assert (oracle.trace(tree, tris, o, d, tracer=tracer)[0] == hb).mean() >= 0.999
+
+
+def test_tuned_differs_from_reference_below_median_levels(oracle):
+    tris = scenes.clustered(20000, seed=19)
+    a = oracle.build(tris, mode=1, upper_levels=8)
+    b = oracle.build(tris)
+    assert a.n_nodes != b.n_nodes or not np.array_equal(a.split, b.split)
+    c = oracle.build(tris, mode=1, upper_levels=64)  # never reaches the SAH levels
+    assert np.array_equal(c.split, b.split) and np.array_equal(c.children, b.children)
+
+
 def test_upper_leaf_boxes_contain_references(oracle):
     tris = scenes.clustered(3000, seed=9)
     tree = oracle.build(tris)
