@@ -1,8 +1,10 @@
 """Benchmark of the kd-tree build + trace path on one GB300 (or N replicas).
 
-Workload (one "step" = one frame of the 1M-triangle clustered scene):
+Default workload (one "step" = one frame of the 1M-triangle clustered scene):
   * rebuild the kd tree over 1,000,000 device-resident triangles
-    (64 Gaussian clusters, 2 ground-plane triangles, 2000 thin triangles);
+    (64 Gaussian clusters, 2 ground-plane triangles, 2000 thin triangles) by
+    launching the tree's rebuild graph (kdgb_graph_launch: the whole level
+    loop on the device, no host round trip);
   * trace 1920x1080 primary rays with the short-stack tracer (depth 8) and,
     fused in the same kernel, one shadow ray per hit toward (0.5, 3, 0.5).
 Metric: rays traced (primary + shadow) per second of the whole step, build
@@ -15,6 +17,15 @@ torchrun each rank runs an independent replica (weak scaling).
 
 --impl reference times the reference's algorithms on the host cores: the CPU
 restatement in oracle/ (the reference itself does not compile here).
+
+--workload selects the other measured configurations (one JSON line each):
+  small    4096-triangle height field, 256x256 rays: kd-restart and brute force
+  photons  262,144-triangle clustered scene, 16M photons x 3 diffuse bounces,
+           kd-restart vs short-stack, Msegments/s
+  batched  512 clustered meshes (log-uniform 1k..200k triangles, ~22M total),
+           64k rays per mesh: one graph (forest build + trace) vs a per-mesh
+           launch loop, parameters from the autotuner
+  adjoint  100k-triangle height field (316x158), 512x512 rays: backward pass
 """
 from __future__ import annotations
 
@@ -37,8 +48,11 @@ WIDTH, HEIGHT = 1920, 1080
 LIGHT = (0.5, 3.0, 0.5)
 SCENE_SEED = 2
 BUILD = dict(lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
-BUILD_DESC = "reference upper (median + empty space to <32 refs) + SAH lower Ct=1 Ci=1.5 min_leaf=8"
+BUILD_DESC = ("reference upper (median + empty space to <32 refs) + SAH lower Ct=1 Ci=1.5 min_leaf=8, "
+              "rebuilt by one graph launch")
 STACK_DEPTH = 8
+HEADROOM = 1.1
+FLUSH_BYTES = 512 << 20
 
 
 def parse():
@@ -47,9 +61,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "small", "photons", "batched", "adjoint"])
     ap.add_argument("--tris", type=int, default=N_TRIS)
     ap.add_argument("--width", type=int, default=WIDTH)
     ap.add_argument("--height", type=int, default=HEIGHT)
+    ap.add_argument("--host-build", action="store_true", help="rebuild with the host-driven level loop")
+    ap.add_argument("--profile", action="store_true",
+                    help="one build and two traces, nothing timed (for ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -137,8 +155,8 @@ def measured_peak_gbs():
 
 
 def committed_traffic():
-    """DRAM bytes per trace launch from the committed ncu summary, scaled by
-    the units it covers; None when no capture has been committed."""
+    """DRAM bytes per trace launch from the committed ncu summary; None when
+    no capture has been committed."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
@@ -146,13 +164,18 @@ def committed_traffic():
         return json.load(f)
 
 
+def oracle_module():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.lib()
+    return O
+
+
 def cpu_baseline(tris, o, d, sample_stride=16, threads=0):
     """The oracle (reference algorithms restated in C, OpenMP) on the host
     cores: full build + traced sample of every `sample_stride`-th ray."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
+    O = oracle_module()
     from kdgb import scenes
-    O.lib()
     t0 = time.perf_counter()
     tree = O.build(tris, **BUILD)
     t_build = time.perf_counter() - t0
@@ -178,10 +201,8 @@ def run_reference(args, world, rank):
     """--impl reference: the oracle on all host cores, full frames."""
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
+    O = oracle_module()
     from kdgb import scenes
-    O.lib()
     tris, o, d = workload(args)
     cores = os.cpu_count() or 1
 
@@ -205,7 +226,8 @@ def run_reference(args, world, rank):
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "clustered-1M-tris 1920x1080 primary + shadow, short-stack depth 8",
-                       "tris": args.tris, "rays": args.width * args.height, "build": BUILD_DESC},
+                       "tris": args.tris, "rays": args.width * args.height,
+                       "build": "reference upper + SAH lower Ct=1 Ci=1.5 min_leaf=8 (host loop)"},
             "cpu_baseline": {"value": val, "unit": "Mrays/s", "cores": cores, "kind": "port",
                              "sample": "full frames: CPU restatement of the reference build + short-stack + "
                                        "shadow rays, OpenMP over all host cores"},
@@ -213,15 +235,26 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def main():
-    args = parse()
-    world, rank, local, pg = dist_setup(args)
-    if args.impl == "reference":
-        run_reference(args, world, rank)
-        return
+def time_steps(step, steps, stream, flush=None):
+    """Per-step device milliseconds (CUDA events on `stream`), L2 flushed
+    between steps outside the events."""
+    import torch
+    out = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return out
+
+
+def run_frame(args, world, rank, local, pg):
     import torch
     import kdgb
-    from kdgb import _lib
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -234,23 +267,41 @@ def main():
     bp = kdgb.build_params(**BUILD)
     tp = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH, tile_width=args.width)
     tree = kdgb.KDTree.build(tris_d, bp)
+    graph = None if args.host_build else kdgb.Graph(tree, tris_d, params=bp, headroom=HEADROOM)
     outs = (torch.empty(n, dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.float32, device=dev),
             torch.empty(n, dtype=torch.float32, device=dev), torch.empty(n, dtype=torch.float32, device=dev),
             torch.empty(n, dtype=torch.int32, device=dev))
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
 
+    def build():
+        if graph is not None:
+            graph.launch()
+        else:
+            tree.rebuild(tris_d, bp)
+
     def step(ev=None):
-        tree.rebuild(tris_d, bp)
+        build()
         if ev:
             ev[0].record(stream)
         tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
         if ev:
             ev[1].record(stream)
 
+    if args.profile:
+        build()
+        tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
+        tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
+        torch.cuda.synchronize()
+        if graph is not None and graph.status() != 0:
+            raise RuntimeError("graph rebuild failed")
+        return
+
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
+    if graph is not None:
+        kdgb.check(graph.status(), "graph rebuild")
     n_hits = int((outs[0] >= 0).sum().item())
     rays_per_step = n + n_hits
     st = tree.stats()
@@ -277,6 +328,8 @@ def main():
     torch.cuda.synchronize()
     clocks = sampler.stop()
     launches = L.kdgb_launch_count() - launches0
+    if graph is not None:
+        kdgb.check(graph.status(), "graph rebuild")
     total_ms = float(sum(step_ms))
     if pg:
         t = torch.tensor([total_ms], device=dev)
@@ -297,6 +350,8 @@ def main():
             "traffic": traffic.get("trace_dram_bytes_per_launch") if traffic else None,
             "kernel": "k_trace<SHORTSTACK,leaf-skip,shadow>", "algorithmic_bytes_per_launch": alg_bytes,
             "peak_source": f"{peak_kind} hbm_gbs"}
+    if traffic:
+        roof["traffic_source"] = traffic.get("source")
 
     # End to end through the public API with host buffers.
     e2e = None
@@ -345,7 +400,8 @@ def main():
                 "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic (seeded clustered scene, pinhole camera)",
                 "config": {"workload": "clustered-1M-tris 1920x1080 primary + shadow, short-stack depth 8",
-                           "tris": T, "rays_primary": n, "rays_shadow": n_hits, "build": BUILD_DESC,
+                           "tris": T, "rays_primary": n, "rays_shadow": n_hits,
+                           "build": BUILD_DESC if graph is not None else BUILD_DESC.split(",")[0] + " (host loop)",
                            "l2": "512 MB buffer written between timed steps",
                            "parallelism": f"replicas x{world}"},
                 "build_ms": statistics.mean(s - t for s, t in zip(step_ms, trace_ms)),
@@ -355,7 +411,245 @@ def main():
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clocks}
         print(json.dumps(line), flush=True)
+    if graph is not None:
+        graph.close()
     tree.close()
+
+
+# ---------------------------------------------------------------------------
+# Other configurations (single GPU, rank 0 only).
+# ---------------------------------------------------------------------------
+
+SMALL_BUILD = dict(lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
+
+
+def line_common(args, metric, value, unit, higher, ms, workload_desc, extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": higher, "scaling": "weak",
+         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": workload_desc}}
+    d.update(extra)
+    return d
+
+
+def run_small(args):
+    """4096-triangle height field, 256x256 pinhole rays: SAH build, kd-restart
+    and brute force."""
+    import torch
+    import kdgb
+    from kdgb import scenes
+    tris = scenes.heightfield(64, 32, seed=1)[0]
+    o, d = scenes.camera_rays(256, 256)
+    n = o.shape[0]
+    td, od, dd = (torch.from_numpy(x).cuda() for x in (tris, o, d))
+    stream = torch.cuda.current_stream()
+    bp = kdgb.build_params(**SMALL_BUILD)
+    tree = kdgb.KDTree.build(td, bp)
+    graph = kdgb.Graph(tree, td, params=bp, headroom=HEADROOM)
+    tp = kdgb.trace_params(tracer=kdgb.TRACER_RESTART)
+    outs = tuple(torch.empty(n, dtype=dt, device="cuda") for dt in (torch.int32, torch.float32, torch.float32,
+                                                                      torch.float32))
+    W = max(args.warmup, 3)
+    res = {}
+    for name, fn in (("host_build", lambda: tree.rebuild(td, bp)), ("graph_build", graph.launch),
+                     ("restart", lambda: tree.trace(od, dd, tp, out=outs)),
+                     ("brute", lambda: kdgb.trace_brute(td, od, dd))):
+        time_steps(fn, W, stream)
+        res[name] = statistics.median(time_steps(fn, args.steps, stream))
+    kdgb.check(graph.status(), "graph rebuild")
+    step_ms = res["graph_build"] + res["restart"]
+    cpu = None
+    if not args.no_cpu_baseline:
+        O = oracle_module()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            ot = O.build(tris, **SMALL_BUILD)
+        tb = (time.perf_counter() - t0) / 5
+        t0 = time.perf_counter()
+        for _ in range(5):
+            O.trace(ot, tris, o, d, tracer=O.TRACER_RESTART)
+        tt = (time.perf_counter() - t0) / 5
+        t0 = time.perf_counter()
+        O.trace(None, tris, o[::16], d[::16], tracer=O.TRACER_BRUTE)
+        tbr = (time.perf_counter() - t0) * 16
+        cpu = {"value": n / (tb + tt) / 1e6, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "oracle build + kd-restart over all 65,536 rays (5 runs); brute force over every 16th ray",
+               "build_ms": tb * 1e3, "restart_mrays_s": n / tt / 1e6, "brute_mrays_s": n / tbr / 1e6}
+    print(json.dumps(line_common(
+        args, "kd-restart Mrays/s per step (4096-tri SAH build + 256x256 primary rays)", n / (step_ms / 1e3) / 1e6,
+        "Mrays/s", True, step_ms, "heightfield-64x32 (4096 tris) 256x256 rays, SAH Ct=1 Ci=1.5 leaf 8",
+        {"build_ms_graph": res["graph_build"], "build_ms_host": res["host_build"],
+         "restart_trace_ms": res["restart"], "restart_mrays_s": n / (res["restart"] / 1e3) / 1e6,
+         "brute_trace_ms": res["brute"], "brute_mrays_s": n / (res["brute"] / 1e3) / 1e6, "cpu_baseline": cpu})),
+        flush=True)
+    graph.close()
+    tree.close()
+
+
+def run_photons(args):
+    """Incoherent load: 16M photons from a point light, 3 cosine-weighted
+    bounces with Russian roulette (p = 0.7), Philox stream; kd-restart vs
+    short-stack on a 262,144-triangle clustered scene."""
+    import torch
+    import kdgb
+    from kdgb import scenes
+    T, P = 262144, 16 << 20
+    tris = scenes.clustered(T, seed=SCENE_SEED)
+    td = torch.from_numpy(tris).cuda()
+    stream = torch.cuda.current_stream()
+    tree = kdgb.KDTree.build(td, **BUILD)
+    ph = kdgb.photon_params(seed=3, bounces=3, survival=0.7)
+    out = (torch.empty((P, 4), dtype=torch.int32, device="cuda"), torch.empty((P, 4), dtype=torch.float32,
+                                                                              device="cuda"))
+    W = max(args.warmup, 3)
+    res = {}
+    for name, tp in (("restart", kdgb.trace_params(tracer=kdgb.TRACER_RESTART)),
+                     ("shortstack", kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH))):
+        fn = lambda tp=tp: tree.trace_photons(P, tp, photons=ph, out=out)
+        time_steps(fn, W, stream)
+        res[name] = statistics.median(time_steps(fn, args.steps, stream))
+    segs = int((out[0] != -2).sum().item())
+    best = min(res, key=res.get)
+    cpu = None
+    if not args.no_cpu_baseline:
+        O = oracle_module()
+        ot = O.build(tris, **BUILD)
+        sample = 1 << 18
+        t0 = time.perf_counter()
+        h, _ = O.trace_photons(ot, tris, sample, seed=3, bounces=3, survival=0.7, tracer=O.TRACER_SHORTSTACK,
+                               stack_depth=STACK_DEPTH)
+        dt = time.perf_counter() - t0
+        cpu = {"value": int((h != -2).sum()) / dt / 1e6, "unit": "Msegments/s", "cores": os.cpu_count(),
+               "kind": "port", "sample": f"first {sample} photons, short-stack, OpenMP over all host cores"}
+    print(json.dumps(line_common(
+        args, "photon segments Msegments/s (262k-tri clustered, 16M photons x 3 bounces)",
+        segs / (res[best] / 1e3) / 1e6, "Msegments/s", True, res[best],
+        "clustered-262144-tris, 16M photons from (0.5,0.5,0.5), 3 bounces, RR p=0.7",
+        {"segments": segs, "restart_ms": res["restart"], "shortstack_ms": res["shortstack"],
+         "restart_msegments_s": segs / (res["restart"] / 1e3) / 1e6,
+         "shortstack_msegments_s": segs / (res["shortstack"] / 1e3) / 1e6, "best": best, "cpu_baseline": cpu})),
+        flush=True)
+    tree.close()
+
+
+def batched_workload(n_meshes=512, lo=1000, hi=200000, rays_per_mesh=65536, seed=40):
+    from kdgb import scenes
+    u = scenes.uniform(seed, n_meshes, 0)
+    sizes = np.exp(np.log(lo) + (np.log(hi) - np.log(lo)) * u).astype(np.int64)
+    meshes = [scenes.clustered(int(s), seed=seed + 1 + m) for m, s in enumerate(sizes)]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
+    o = np.empty((n_meshes * rays_per_mesh, 3), np.float32)
+    d = np.empty_like(o)
+    for m, t in enumerate(meshes):
+        v = t.reshape(-1, 3)
+        ro, rd = scenes.random_rays(rays_per_mesh, seed + 1000 + m, v.min(0), v.max(0))
+        o[m * rays_per_mesh:(m + 1) * rays_per_mesh] = ro
+        d[m * rays_per_mesh:(m + 1) * rays_per_mesh] = rd
+    return meshes, off, o, d
+
+
+def run_batched(args):
+    """512 meshes: one graph (forest build + batched trace) vs a per-mesh loop
+    of rebuild + trace launches, both with the autotuner's parameters."""
+    import torch
+    import kdgb
+    R = 65536
+    meshes, off, o, d = batched_workload(rays_per_mesh=R)
+    M = len(meshes)
+    tris = np.concatenate(meshes)
+    td, od, dd = (torch.from_numpy(x).cuda() for x in (tris, o, d))
+    stream = torch.cuda.current_stream()
+    base_b = kdgb.build_params(**BUILD)
+    base_t = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH)
+    t0 = time.perf_counter()
+    tuned = kdgb.autotune(td, od, dd, mesh_offsets=off, rays_per_mesh=R, build=base_b, trace=base_t,
+                          builds_per_trace=1.0, reps=2)
+    tune_s = time.perf_counter() - t0
+    bp, tp = tuned.build, tuned.trace
+    tp.tile_width = 0
+    forest = kdgb.KDTree.build_batch(td, off, bp)
+    graph = kdgb.Graph(forest, td, mesh_offsets=off, params=bp, headroom=HEADROOM, o=od, d=dd, rays_per_mesh=R,
+                       trace=tp)
+    W = max(args.warmup, 3)
+    time_steps(graph.launch, W, stream)
+    g_ms = time_steps(graph.launch, args.steps, stream)
+    kdgb.check(graph.status(), "graph rebuild")
+    hits = int((graph.out[0] >= 0).sum().item())
+
+    # Per-mesh launch loop: one handle per mesh, host-driven rebuild + trace.
+    views = [td[off[m]:off[m + 1]] for m in range(M)]
+    trees = [kdgb.KDTree.build(views[m], bp) for m in range(M)]
+    louts = [tuple(torch.empty(R, dtype=dt, device="cuda") for dt in (torch.int32, torch.float32, torch.float32,
+                                                                      torch.float32)) for _ in range(M)]
+    oviews = [(od[m * R:(m + 1) * R], dd[m * R:(m + 1) * R]) for m in range(M)]
+
+    def loop():
+        for m in range(M):
+            trees[m].rebuild(views[m], bp)
+            trees[m].trace(oviews[m][0], oviews[m][1], tp, out=louts[m])
+
+    time_steps(loop, 1, stream)
+    l_ms = time_steps(loop, max(2, args.steps // 3), stream)
+    same = all(torch.equal(louts[m][0], graph.out[0][m * R:(m + 1) * R]) for m in range(M))
+    g, lp = statistics.median(g_ms), statistics.median(l_ms)
+    print(json.dumps(line_common(
+        args, "batched build+trace of 512 meshes, meshes/s (one graph launch)", M / (g / 1e3), "meshes/s", True, g,
+        "512 clustered meshes log-uniform [1k,200k] tris (%d total), 64k random rays each, SAH" % tris.shape[0],
+        {"rays_mrays_s": M * R / (g / 1e3) / 1e6, "per_mesh_loop_ms": lp, "per_mesh_loop_meshes_s": M / (lp / 1e3),
+         "speedup_vs_loop": lp / g, "hits": hits, "loop_hits_identical": bool(same),
+         "autotune": {"leaf_size": bp.leaf_size, "sah_bins": bp.sah_bins, "stack_depth": tp.stack_depth,
+                      "block_size": tp.block_size, "objective_ms": tuned.objective, "baseline_ms": tuned.baseline,
+                      "trials": tuned.trials, "seconds": tune_s}})), flush=True)
+    graph.close()
+    forest.close()
+    for t in trees:
+        t.close()
+
+
+def run_adjoint(args):
+    """Backward pass of t and barycentrics w.r.t. the vertices of a 100k
+    triangle height field for 512x512 rays with fixed forward hits."""
+    import torch
+    import kdgb
+    from kdgb import scenes
+    tris, verts, idx = scenes.heightfield(316, 158, seed=5)
+    o, d = scenes.camera_rays(512, 512)
+    n = o.shape[0]
+    stream = torch.cuda.current_stream()
+    td = torch.from_numpy(tris).cuda()
+    vd = torch.from_numpy(np.ascontiguousarray(verts, dtype=np.float32)).cuda()
+    idd = torch.from_numpy(np.ascontiguousarray(idx, dtype=np.int32)).cuda()
+    od, dd = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    tree = kdgb.KDTree.build(td, **SMALL_BUILD)
+    hit, t, u, v = tree.trace(od, dd)
+    g = torch.Generator(device="cpu").manual_seed(7)
+    w = torch.randn(n, generator=g).cuda()
+    wv = torch.randn(n, generator=g).cuda()
+    grad = torch.zeros_like(vd)
+    fn = lambda: kdgb.backward(vd, idd, od, dd, hit, w, wv, wv, out=grad)
+    W = max(args.warmup, 3)
+    time_steps(fn, W, stream)
+    b_ms = statistics.median(time_steps(fn, args.steps, stream))
+    f_ms = statistics.median(time_steps(lambda: tree.trace(od, dd), args.steps, stream))
+    print(json.dumps(line_common(
+        args, "adjoint backward ms (100k-tri height field, 512x512 rays)", b_ms, "ms", False, b_ms,
+        "heightfield-316x158 (%d tris), 512x512 rays, loss sum w*t + v*(u+v)" % tris.shape[0],
+        {"forward_trace_ms": f_ms, "hits": int((hit >= 0).sum().item()),
+         "backward_mrays_s": n / (b_ms / 1e3) / 1e6})), flush=True)
+    tree.close()
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    if args.workload == "frame":
+        run_frame(args, world, rank, local, pg)
+    elif rank == 0:
+        import torch
+        torch.cuda.set_device(local)
+        {"small": run_small, "photons": run_photons, "batched": run_batched, "adjoint": run_adjoint}[args.workload](args)
     if pg:
         pg.destroy_process_group()
 

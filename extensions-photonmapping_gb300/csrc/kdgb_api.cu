@@ -1,6 +1,7 @@
 // C ABI of the kd-tree builder and tracers (include/kdgb.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -99,6 +100,7 @@ template int ensure<int2>(DevArray<int2> &, int64_t, cudaStream_t, int64_t, bool
 template int ensure<int4>(DevArray<int4> &, int64_t, cudaStream_t, int64_t, bool);
 template int ensure<unsigned>(DevArray<unsigned> &, int64_t, cudaStream_t, int64_t, bool);
 template int ensure<float2>(DevArray<float2> &, int64_t, cudaStream_t, int64_t, bool);
+template int ensure<BuildState>(DevArray<BuildState> &, int64_t, cudaStream_t, int64_t, bool);
 
 static void release_all(Tree &t, cudaStream_t s)
 {
@@ -108,12 +110,16 @@ static void release_all(Tree &t, cudaStream_t s)
     release(t.area, s); release(t.prim_indices, s); release(t.leaf_ids, s);
     release(t.tnode, s); release(t.ttri, s); release(t.mesh_off, s);
     Workspace &w = t.ws;
-    release(w.cmin, s); release(w.cmax, s); release(w.nmin, s); release(w.nmax, s); release(w.fmin, s);
-    release(w.fmax, s); release(w.pmin, s); release(w.pmax, s); release(w.keys, s); release(w.planes, s);
-    release(w.req, s); release(w.eaddr, s); release(w.cnt, s); release(w.lanes, s); release(w.lbase, s);
-    release(w.chunksum, s); release(w.chunkoff, s); release(w.stats, s); release(w.scan, s); release(w.misc0, s);
-    release(w.misc1, s); release(w.areas, s); release(w.sts, s); release(w.ssplit, s); release(w.saddr, s);
-    release(w.roff, s); release(w.careas, s); release(w.csets, s); release(w.ranges, s);
+    for (int b = 0; b < 2; ++b) {
+        release(w.rmin[b], s);
+        release(w.rmax[b], s);
+    }
+    release(w.fmin, s); release(w.fmax, s); release(w.pmin, s); release(w.pmax, s); release(w.keys, s);
+    release(w.planes, s); release(w.cnt, s); release(w.lanes, s); release(w.lbase, s); release(w.chunksum, s);
+    release(w.chunkoff, s); release(w.stats, s); release(w.scan, s); release(w.misc0, s); release(w.misc1, s);
+    release(w.hist, s); release(w.areas, s); release(w.sts, s); release(w.ssplit, s); release(w.saddr, s);
+    release(w.roff, s); release(w.careas, s); release(w.csets, s); release(w.ranges, s); release(w.state, s);
+    t.plan = BuildPlan();
     if (w.host) {
         cudaStreamSynchronize(s);
         cudaFreeHost(w.host);
@@ -149,6 +155,16 @@ static int validate_build_params(const kdgb_build_params &p)
     return KDGB_OK;
 }
 
+static int validate_offsets(const int32_t *mesh_offsets, int32_t n_meshes, const char *who)
+{
+    if (n_meshes < 1 || !mesh_offsets) return fail(KDGB_ERR_INVALID_ARGUMENT, std::string(who) + ": no meshes");
+    if (mesh_offsets[0] != 0) return fail(KDGB_ERR_INVALID_ARGUMENT, std::string(who) + ": mesh_offsets[0] must be 0");
+    for (int32_t m = 0; m < n_meshes; ++m)
+        if (mesh_offsets[m + 1] < mesh_offsets[m])
+            return fail(KDGB_ERR_INVALID_ARGUMENT, std::string(who) + ": mesh_offsets must be non-decreasing");
+    return KDGB_OK;
+}
+
 static int validate_trace_params(const kdgb_trace_params &p, int64_t n)
 {
     if (p.tracer < KDGB_TRACER_RESTART || p.tracer > KDGB_TRACER_BRUTE)
@@ -181,9 +197,7 @@ static int do_build(Tree &t, const float *tri_v_dev, int32_t n_tris, const kdgb_
             if (e != cudaSuccess) rc = cuda_fail(e, "mesh offsets");
         }
     }
-    if (rc == KDGB_OK)
-        rc = build_reference(t, tri_v_dev, n_tris, p, s, n_meshes > 1 ? t.mesh_off.p : nullptr, t.n_meshes);
-    if (rc == KDGB_OK) rc = pack_for_traversal(t, s);
+    if (rc == KDGB_OK) rc = build_tree(t, tri_v_dev, n_tris, p, s, n_meshes > 1 ? t.mesh_off.p : nullptr, t.n_meshes);
     cudaEventRecord(e1, s);
     if (rc == KDGB_OK) {
         cudaError_t e = cudaEventSynchronize(e1);
@@ -202,6 +216,17 @@ static int do_build(Tree &t, const float *tri_v_dev, int32_t n_tris, const kdgb_
 }  // namespace kdgb
 
 using namespace kdgb;
+
+struct kdgb_graph {
+    kdgb_tree *tree = nullptr;
+    cudaStream_t cs = nullptr, body = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t signature = 0;
+    GraphKernels kernels;
+    int64_t trace_kernels = 0;
+    int64_t per_launch = 0;  // kernels one launch runs at the plan's level counts
+};
 
 extern "C" {
 
@@ -544,11 +569,7 @@ int kdgb_build_batch(const float *tri_v_dev, const int32_t *mesh_offsets, int32_
 {
     if (!out) return fail(KDGB_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
-    if (n_meshes < 1 || !mesh_offsets) return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_build_batch: no meshes");
-    if (mesh_offsets[0] != 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_build_batch: mesh_offsets[0] must be 0");
-    for (int32_t m = 0; m < n_meshes; ++m)
-        if (mesh_offsets[m + 1] < mesh_offsets[m])
-            return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_build_batch: mesh_offsets must be non-decreasing");
+    KDGB_CHECK(validate_offsets(mesh_offsets, n_meshes, "kdgb_build_batch"));
     const int32_t n_tris = mesh_offsets[n_meshes];
     if (n_tris > 0 && !tri_v_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad triangle buffer");
     KDGB_CHECK(check_device());
@@ -567,6 +588,20 @@ int kdgb_build_batch(const float *tri_v_dev, const int32_t *mesh_offsets, int32_
     }
     *out = h;
     return KDGB_OK;
+}
+
+int kdgb_rebuild_batch(kdgb_tree *tree, const float *tri_v_dev, const int32_t *mesh_offsets, int32_t n_meshes,
+                       const kdgb_build_params *params, kdgb_stream_t stream)
+{
+    if (!tree) return fail(KDGB_ERR_INVALID_ARGUMENT, "tree is NULL");
+    KDGB_CHECK(validate_offsets(mesh_offsets, n_meshes, "kdgb_rebuild_batch"));
+    const int32_t n_tris = mesh_offsets[n_meshes];
+    if (n_tris > 0 && !tri_v_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad triangle buffer");
+    KDGB_CHECK(check_device());
+    kdgb_build_params p;
+    if (params) p = *params; else kdgb_build_params_default(&p);
+    KDGB_CHECK(validate_build_params(p));
+    return do_build(tree->t, tri_v_dev, n_tris, p, (cudaStream_t)stream, mesh_offsets, n_meshes);
 }
 
 int kdgb_trace_batch(const kdgb_tree *tree, const kdgb_trace_params *params, const float *ray_o_dev,
@@ -613,5 +648,125 @@ int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie, const 
     return rc;
 }
 
+int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris, const int32_t *mesh_offsets,
+                      int32_t n_meshes, const kdgb_build_params *params, float headroom,
+                      const kdgb_trace_params *trace, const float *ray_o_dev, const float *ray_d_dev,
+                      const int32_t *ray_mesh_dev, int32_t rays_per_mesh, int32_t n_rays, int32_t *hit_dev,
+                      float *t_dev, float *u_dev, float *v_dev, kdgb_graph **out, kdgb_stream_t stream)
+{
+    if (!out) return fail(KDGB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (!tree) return fail(KDGB_ERR_INVALID_ARGUMENT, "tree is NULL");
+    Tree &t = tree->t;
+    if (!t.plan.valid) return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_graph_create: build the tree once first");
+    if (!(headroom >= 1.0f) || !(headroom <= 64.0f))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_graph_create: headroom must be in [1, 64]");
+    if (n_meshes < 1) return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_graph_create: n_meshes must be >= 1");
+    if (n_meshes > 1) {
+        KDGB_CHECK(validate_offsets(mesh_offsets, n_meshes, "kdgb_graph_create"));
+        if (mesh_offsets[n_meshes] != n_tris)
+            return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_graph_create: mesh_offsets[n_meshes] != n_tris");
+    }
+    if (n_tris < 0 || (n_tris > 0 && !tri_v_dev)) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad triangle buffer");
+    KDGB_CHECK(check_device());
+    kdgb_build_params p;
+    if (params) p = *params; else kdgb_build_params_default(&p);
+    KDGB_CHECK(validate_build_params(p));
+    kdgb_trace_params tp;
+    if (trace) tp = *trace; else kdgb_trace_params_default(&tp);
+    if (n_rays < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "negative ray count");
+    if (n_rays > 0) {
+        if (n_meshes > 1) tp.tile_width = 0;
+        KDGB_CHECK(validate_trace_params(tp, n_rays));
+        if (tp.tracer == KDGB_TRACER_BRUTE) return fail(KDGB_ERR_UNSUPPORTED, "graph traces need a kd tracer");
+        if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev)
+            return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+        if (n_meshes > 1 && !ray_mesh_dev && (rays_per_mesh < 1 || (int64_t)rays_per_mesh * n_meshes < n_rays))
+            return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_graph_create: ray_mesh_dev or enough rays_per_mesh needed");
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    // Offsets and every fixed buffer, before capture.
+    t.n_meshes = n_meshes;
+    if (n_meshes > 1) {
+        KDGB_CHECK(ensure(t.mesh_off, (int64_t)n_meshes + 1, s));
+        KDGB_CUDA(cudaMemcpyAsync(t.mesh_off.p, mesh_offsets, sizeof(int32_t) * (n_meshes + 1),
+                                  cudaMemcpyHostToDevice, s));
+    }
+    KDGB_CHECK(reserve_for_graph(t, n_tris, p, n_meshes, headroom, s));
+    KDGB_CUDA(cudaStreamSynchronize(s));
+
+    kdgb_graph *g = new (std::nothrow) kdgb_graph();
+    if (!g) return fail(KDGB_ERR_OUT_OF_MEMORY, "host allocation");
+    g->tree = tree;
+    int rc = KDGB_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&g->cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->body, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda_fail(e, "graph streams");
+    if (rc == KDGB_OK) {
+        e = cudaStreamBeginCapture(g->cs, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamBeginCapture");
+    }
+    const int64_t launches0 = kdgb_launch_count();
+    if (rc == KDGB_OK) {
+        rc = capture_build(t, tri_v_dev, n_tris, p, g->cs, g->body, n_meshes > 1 ? t.mesh_off.p : nullptr,
+                           n_meshes, g->kernels);
+        const int64_t before_trace = kdgb_launch_count();
+        if (rc == KDGB_OK && n_rays > 0)
+            rc = trace_launch(t, tp, ray_o_dev, ray_d_dev, n_rays, hit_dev, t_dev, u_dev, v_dev, nullptr, nullptr,
+                              g->cs, n_meshes > 1 ? ray_mesh_dev : nullptr, n_meshes > 1 ? rays_per_mesh : 0);
+        g->trace_kernels = kdgb_launch_count() - before_trace;
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(g->cs, &graph);
+        g->graph = graph;
+        if (rc == KDGB_OK && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamEndCapture");
+    }
+    // Capture launched nothing: take the recorded kernels off the counter.
+    note_launch((int)-(kdgb_launch_count() - launches0));
+    if (rc == KDGB_OK) {
+        e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaGraphInstantiate");
+    }
+    {
+        const GraphKernels &k = g->kernels;
+        g->per_launch = k.fixed + k.upper_body * t.plan.levels + g->trace_kernels +
+                        (p.lower == KDGB_LOWER_SAH ? k.lower_body * std::max(1, t.plan.low_levels) : 0);
+    }
+    if (rc != KDGB_OK) {
+        kdgb_graph_destroy(g);
+        return rc;
+    }
+    g->signature = layout_signature(t);
+    *out = g;
+    return KDGB_OK;
+}
+
+int kdgb_graph_launch(kdgb_graph *graph, kdgb_stream_t stream)
+{
+    if (!graph || !graph->exec) return fail(KDGB_ERR_INVALID_ARGUMENT, "graph is NULL");
+    if (layout_signature(graph->tree->t) != graph->signature)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "the tree's buffers changed since the graph was created");
+    KDGB_CUDA(cudaGraphLaunch(graph->exec, (cudaStream_t)stream));
+    note_launch((int)graph->per_launch);
+    return KDGB_OK;
+}
+
+int kdgb_graph_status(kdgb_graph *graph, kdgb_stream_t stream)
+{
+    if (!graph) return fail(KDGB_ERR_INVALID_ARGUMENT, "graph is NULL");
+    return read_build_state(graph->tree->t, (cudaStream_t)stream);
+}
+
+int kdgb_graph_destroy(kdgb_graph *graph)
+{
+    if (!graph) return KDGB_OK;
+    if (graph->exec) cudaGraphExecDestroy(graph->exec);
+    if (graph->graph) cudaGraphDestroy(graph->graph);
+    if (graph->body) cudaStreamDestroy(graph->body);
+    if (graph->cs) cudaStreamDestroy(graph->cs);
+    delete graph;
+    return KDGB_OK;
+}
+
 }  // extern "C"
+
 

@@ -65,18 +65,59 @@ int grab(DevArray<T> &a, int64_t n, cudaStream_t s)
     return ensure(a, want, s, 0, false);
 }
 
+// Device-resident counters of a build in progress.  Every build kernel reads
+// its sizes here, so one launch sequence runs either under host control
+// (exact grids, one readback per level) or captured once into a CUDA graph
+// whose level loops are conditional WHILE nodes.  Only the single-thread
+// advance kernels write it.
+struct BuildState {
+    int64_t N;            // references of the current upper level
+    int64_t F;            // leaf references written so far
+    int32_t R;            // active nodes of the current upper level
+    int32_t active;       // id of the first active node
+    int32_t n_nodes;      // nodes written so far
+    int32_t level;        // upper levels completed
+    int32_t nch;          // warp chunks covering the N references
+    int32_t n_leaf_ids;   // upper leaves so far
+    int32_t n_ranges;     // upper levels that produced leaves
+    int32_t err;          // first failure (a kdgb_status), 0 while healthy
+    int32_t err_detail;   // which check failed (see kdgb_build.cu)
+    int32_t nonfinite;    // set when a vertex coordinate is NaN or Inf
+    int32_t low_R;        // active nodes of the current SAH lower level
+    int32_t low_active;   // first of them when low_first == 0
+    int32_t low_levels;   // SAH lower levels completed
+    int32_t low_first;    // 1 while the lower level is the upper leaves
+    int32_t n_leaf_tris;  // leaf records of the traversal layout
+    int32_t pad;
+};
+
+// Sizes seen by the last host-driven build of a handle; a graph rebuild
+// sizes its fixed buffers from them.
+struct BuildPlan {
+    bool valid = false;
+    int64_t max_N = 0, F = 0, nodes = 0, max_R = 0, leaves = 0, max_low_R = 0, leaf_tris = 0;
+    int32_t levels = 0, low_levels = 0;
+};
+
+// Kernels a captured build records: outside the loops and per loop body.
+struct GraphKernels {
+    int64_t fixed = 0, upper_body = 0, lower_body = 0;
+};
+
 // Per-handle build workspace, reused by every level and every rebuild so the
-// steady state issues no device allocations.
+// steady state issues no device allocations.  References ping-pong between
+// rmin/rmax[0] and [1] by level parity.
 struct Workspace {
-    DevArray<float4> cmin, cmax, nmin, nmax, fmin, fmax, pmin, pmax;
+    DevArray<float4> rmin[2], rmax[2], fmin, fmax, pmin, pmax;
     DevArray<unsigned> keys;
     DevArray<int8_t> planes;
-    DevArray<int32_t> req, eaddr, cnt, lanes, lbase, chunksum, chunkoff, stats, scan, misc0, misc1;
+    DevArray<int32_t> cnt, lanes, lbase, chunksum, chunkoff, stats, scan, misc0, misc1, hist;
     DevArray<float> areas;
     DevArray<int4> sts;
     DevArray<int32_t> ssplit, saddr, roff;
     DevArray<float2> careas;
     DevArray<int2> csets, ranges;
+    DevArray<BuildState> state;
     int32_t *host = nullptr;  // pinned record buffer (kHostRec ints)
 };
 constexpr int kHostRec = 256;
@@ -109,23 +150,50 @@ struct Tree {
     DevArray<float4> ttri;
 
     Workspace ws;
+    BuildPlan plan;
 };
 
-// Builder (kdgb_build.cu), both modes.  tri_v_dev: T*9 floats.  With M > 1
-// the triangles are M meshes (mesh m = [mesh_off[m], mesh_off[m+1]), device
-// offsets) built as one forest whose root of mesh m is node m.
-int build_reference(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p,
-                    cudaStream_t s, const int32_t *mesh_off_dev = nullptr, int32_t M = 1);
+// Builder (kdgb_build.cu), both modes, host-driven.  tri_v_dev: T*9 floats.
+// With M > 1 the triangles are M meshes (mesh m = [mesh_off[m],
+// mesh_off[m+1]), device offsets) built as one forest whose root of mesh m is
+// node m.  Also builds the traversal layout and records t.plan.
+int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p, cudaStream_t s,
+               const int32_t *mesh_off_dev = nullptr, int32_t M = 1);
+
+// The same build recorded into the graph being captured on `cs`: fixed
+// buffers sized from t.plan x headroom, level loops as WHILE nodes, no host
+// synchronisation.  `body` is a second stream used to capture loop bodies.
+int capture_build(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p, cudaStream_t cs,
+                  cudaStream_t body, const int32_t *mesh_off_dev, int32_t M, GraphKernels &counts);
+
+// Allocates every buffer capture_build uses, before capture starts.
+int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M, double headroom, cudaStream_t s);
+
+// Copies the device build counters into the host mirrors of t (synchronises
+// s).  Returns the build's failure status, if any.
+int read_build_state(Tree &t, cudaStream_t s);
+
 int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s);
 
-// Traversal layout from the SoA arrays (kdgb_trace.cu).
+// Traversal layout from the SoA arrays of a tree whose host counts are
+// current (kdgb_tree_upload).
 int pack_for_traversal(Tree &t, cudaStream_t s);
 
 // Device-wide exclusive scan of n records of K int32 lanes (lanes scanned
 // independently).  out has n+1 records; record n holds the totals.  `ws`
 // (optional) holds the per-tile partials; without it they are allocated.
+// With n_dev set, the kernels read the length there (at most n, which then
+// only sizes the grids and the partials).
 template <int K>
-int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws = nullptr);
+int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws = nullptr,
+                   const int32_t *n_dev = nullptr);
+
+// Partials (int32 elements) a scan of n records of K lanes needs.
+int64_t scan_partials_needed(int K, int64_t n);
+
+// Hash of every device buffer's address and capacity: a captured graph is
+// valid while this is unchanged.
+uint64_t layout_signature(const Tree &t);
 
 // ---------------------------------------------------------------------------
 // Device helpers.

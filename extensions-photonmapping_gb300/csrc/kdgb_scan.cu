@@ -5,7 +5,10 @@
 // reduce-then-scan over records of K independent lanes: one pass of block
 // totals, one single-block scan of the totals, one pass that rescans each
 // block with its offset.  It needs no inter-block waiting, so it cannot
-// hang, and has no size cap below 2^31 records.
+// hang, and has no size cap below 2^31 records.  The length may live in
+// device memory (a build counter): the grids are then sized for an upper
+// bound and blocks past the real length do nothing, so the scan can be
+// captured once into a graph and replayed for any length up to the bound.
 #include "kdgb_internal.cuh"
 
 namespace kdgb {
@@ -60,8 +63,11 @@ __device__ __forceinline__ void block_scan(int32_t (&v)[K], int32_t (&total)[K])
 
 template <int K>
 __global__ void __launch_bounds__(kThreads) scan_reduce_kernel(const int32_t *__restrict__ in, int64_t n,
+                                                               const int32_t *__restrict__ n_dev,
                                                                int32_t *__restrict__ partial)
 {
+    if (n_dev) n = *n_dev;
+    if ((int64_t)blockIdx.x * kTile >= n) return;  // block-uniform
     const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
     int32_t s[K];
 #pragma unroll
@@ -85,9 +91,13 @@ __global__ void __launch_bounds__(kThreads) scan_reduce_kernel(const int32_t *__
 // Single block: exclusive scan of nb partial records in place; writes the
 // grand totals to `totals`.
 template <int K>
-__global__ void __launch_bounds__(kThreads) scan_partials_kernel(int32_t *__restrict__ partial, int64_t nb,
-                                                                 int32_t *__restrict__ totals)
+__global__ void __launch_bounds__(kThreads) scan_partials_kernel(int32_t *__restrict__ partial, int64_t n,
+                                                                 const int32_t *__restrict__ n_dev,
+                                                                 int32_t *__restrict__ out)
 {
+    if (n_dev) n = *n_dev;
+    const int64_t nb = (n + kTile - 1) / kTile;
+    int32_t *totals = out + n * K;
     int32_t carry[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) carry[k] = 0;
@@ -126,8 +136,11 @@ __global__ void __launch_bounds__(kThreads) scan_partials_kernel(int32_t *__rest
 
 template <int K>
 __global__ void __launch_bounds__(kThreads) scan_down_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
-                                                             int64_t n, const int32_t *__restrict__ partial)
+                                                             int64_t n, const int32_t *__restrict__ n_dev,
+                                                             const int32_t *__restrict__ partial)
 {
+    if (n_dev) n = *n_dev;
+    if (blockIdx.x > 0 && (int64_t)blockIdx.x * kTile >= n) return;  // block-uniform
     const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
     int32_t vals[kItems][K];
     int32_t s[K];
@@ -164,8 +177,11 @@ __global__ void __launch_bounds__(kThreads) scan_down_kernel(const int32_t *__re
 
 }  // namespace
 
+int64_t scan_partials_needed(int K, int64_t n) { return K * ((n + kTile - 1) / kTile); }
+
 template <int K>
-int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws)
+int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws,
+                   const int32_t *n_dev)
 {
     if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "scan: negative length");
     if (n == 0) {
@@ -174,7 +190,8 @@ int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, D
     }
     const int64_t nb = (n + kTile - 1) / kTile;
     if (nb == 1) {
-        scan_down_kernel<K><<<1, kThreads, 0, s>>>(in, out, n, nullptr);
+        // One tile: block 0 scans and writes the totals record itself.
+        scan_down_kernel<K><<<1, kThreads, 0, s>>>(in, out, n, n_dev, nullptr);
         KDGB_LAUNCH_CHECK();
         return KDGB_OK;
     }
@@ -185,14 +202,14 @@ int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, D
     } else {
         KDGB_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * K * (size_t)nb, s));
     }
-    scan_reduce_kernel<K><<<(unsigned)nb, kThreads, 0, s>>>(in, n, partial);
+    scan_reduce_kernel<K><<<(unsigned)nb, kThreads, 0, s>>>(in, n, n_dev, partial);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) {
-        scan_partials_kernel<K><<<1, kThreads, 0, s>>>(partial, nb, out + n * K);
+        scan_partials_kernel<K><<<1, kThreads, 0, s>>>(partial, n, n_dev, out);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
-        scan_down_kernel<K><<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, partial);
+        scan_down_kernel<K><<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, n_dev, partial);
         e = cudaGetLastError();
     }
     if (!ws) cudaFreeAsync(partial, s);
@@ -201,9 +218,13 @@ int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, D
     return KDGB_OK;
 }
 
-template int scan_exclusive<1>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
-template int scan_exclusive<2>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
-template int scan_exclusive<6>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
-template int scan_exclusive<7>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *);
+template int scan_exclusive<1>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *,
+                                   const int32_t *);
+template int scan_exclusive<2>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *,
+                                   const int32_t *);
+template int scan_exclusive<6>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *,
+                                   const int32_t *);
+template int scan_exclusive<7>(const int32_t *, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *,
+                                   const int32_t *);
 
 }  // namespace kdgb

@@ -10,7 +10,7 @@
 // (IRayTracer.h:147-168).  Divisions are IEEE (__frcp_rn), products and sums
 // separately rounded, so hit ids match the CPU restatement bit for bit.
 //
-// Memory layout read by the tracers (built by pack_for_traversal):
+// Memory layout read by the tracers (built by the pack kernels of kdgb_build.cu):
 //   tnode[i]  int4  interior: {split bits, left, right, axis}
 //                   leaf:     {first record, record count, 0, 0}
 //   ttri[3r..3r+2]  float4 x3 per leaf record, in leaf order:
@@ -28,62 +28,12 @@ namespace kdgb {
 
 namespace {
 
-constexpr int kPackBlock = 256;
 constexpr int kMaxStack = 8;
 // Hard cap on restarts/pops per ray when the caller passes 0, so that a
 // pathological ray cannot keep a thread alive forever.
 constexpr int kDefaultMaxIterations = 1 << 22;
 
 inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
-
-__global__ void k_leaf_counts(int32_t n, const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
-                              int32_t *__restrict__ cnt)
-{
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) cnt[i] = info[i] == KDGB_LEAF ? __popc((unsigned)bitmap[i]) : 0;
-}
-
-__global__ void k_pack_nodes(int32_t n, const int8_t *__restrict__ info, const float *__restrict__ split,
-                             const int2 *__restrict__ ch, const int32_t *__restrict__ off, int4 *__restrict__ tnode)
-{
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int a = info[i] & 3;
-    if (a == KDGB_LEAF) {
-        tnode[i] = make_int4(off[i], off[i + 1] - off[i], 0, 0);
-    } else {
-        const int2 c = ch[i];
-        tnode[i] = make_int4(__float_as_int(split[i]), c.x, c.y, a);
-    }
-}
-
-// One thread per node; a leaf writes its records in bitmap order (LSB first).
-__global__ void k_pack_tris(int32_t n, const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
-                            const int32_t *__restrict__ pidx, const int32_t *__restrict__ prim_indices,
-                            const float4 *__restrict__ p0, const float4 *__restrict__ p1,
-                            const float4 *__restrict__ p2, const int32_t *__restrict__ off,
-                            float4 *__restrict__ ttri)
-{
-    const int32_t node = blockIdx.x * blockDim.x + threadIdx.x;
-    if (node >= n) return;
-    if ((info[node] & 3) != KDGB_LEAF) return;
-    unsigned bmp = (unsigned)bitmap[node];
-    const int32_t pi = pidx[node];
-    int64_t rec = off[node];
-    while (bmp) {
-        const int j = __ffs(bmp) - 1;
-        bmp &= bmp - 1u;
-        const int32_t prim = prim_indices[pi + j];
-        const float4 a = p0[prim], b = p1[prim], c = p2[prim];
-        const float3 v0 = make_float3(a.x, a.y, a.z);
-        const float3 e1 = sub3(make_float3(b.x, b.y, b.z), v0);
-        const float3 e2 = sub3(make_float3(c.x, c.y, c.z), v0);
-        ttri[3 * rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
-        ttri[3 * rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
-        ttri[3 * rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
-        ++rec;
-    }
-}
 
 struct Ctx {
     const int4 *__restrict__ node;
@@ -301,6 +251,10 @@ struct TraceArgs {
     // relative to the mesh's first triangle mesh_off[m].
     const int32_t *mesh_off, *ray_mesh;
     int32_t rays_per_mesh, n_meshes;
+    // Nonzero when the tree's last build failed (a graph rebuild that
+    // outgrew its buffers): every ray then reports a miss without reading
+    // the tree.
+    const int32_t *build_err;
 };
 
 template <int TRACER, bool SKIP, bool SHADOW>
@@ -310,6 +264,14 @@ __global__ void k_trace(TraceArgs a)
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= a.n) return;
     const int64_t i = ray_index(id, a.tile_width);
+    if (a.build_err && *a.build_err) {
+        a.hit[i] = -1;
+        a.t[i] = INFINITY;
+        a.u[i] = 0.0f;
+        a.v[i] = 0.0f;
+        if (SHADOW) a.occ[i] = 0;
+        return;
+    }
     const float3 o = ld3(a.o, i), d = ld3(a.d, i);
     Ctx c = a.c;
     int32_t id_off = 0;
@@ -345,6 +307,10 @@ __global__ void k_shadow(TraceArgs a)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
+    if (a.build_err && *a.build_err) {
+        a.occ[i] = 0;
+        return;
+    }
     a.occ[i] = trace_shadow(a.c, a.light, ld3(a.o, i), a.maxit);
 }
 
@@ -413,6 +379,7 @@ struct PhotonArgs {
     int tie, depth, maxit;
     int32_t *seg_hit;
     float *seg_t;
+    const int32_t *build_err;  // as TraceArgs::build_err
 };
 
 template <int TRACER, bool SKIP>
@@ -423,6 +390,13 @@ __global__ void k_photons(PhotonArgs a)
     if (i >= a.n) return;
     const int S = a.bounces + 1;
     const int64_t base = i * S;
+    if (a.build_err && *a.build_err) {
+        for (int k = 0; k < S; ++k) {
+            a.seg_hit[base + k] = -2;
+            a.seg_t[base + k] = INFINITY;
+        }
+        return;
+    }
     const unsigned lo = (unsigned)i, hi = (unsigned)(i >> 32);
     uint4 r = philox4x32_10(make_uint4(lo, hi, 0u, 0u), a.key);
     float3 o = a.light;
@@ -462,36 +436,6 @@ __global__ void k_photons(PhotonArgs a)
 
 }  // namespace
 
-int pack_for_traversal(Tree &t, cudaStream_t s)
-{
-    const int32_t n = t.n_nodes;
-    Workspace &w = t.ws;
-    KDGB_CHECK(grab(w.misc0, n, s));
-    KDGB_CHECK(grab(w.misc1, (int64_t)n + 1, s));
-    if (!w.host) KDGB_CUDA(cudaMallocHost(&w.host, kHostRec * sizeof(int32_t)));
-    int32_t *cnt = w.misc0.p, *off = w.misc1.p;
-    if (n > 0) {
-        k_leaf_counts<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.bitmap.p, cnt);
-        KDGB_LAUNCH_CHECK();
-    }
-    KDGB_CHECK(scan_exclusive<1>(cnt, off, n, s, &w.scan));
-    KDGB_CUDA(cudaMemcpyAsync(w.host + kHostRec - 1, off + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    KDGB_CUDA(cudaStreamSynchronize(s));
-    const int32_t total = w.host[kHostRec - 1];
-    KDGB_CHECK(ensure(t.tnode, n, s));
-    KDGB_CHECK(ensure(t.ttri, 3 * (int64_t)total, s));
-    t.n_leaf_tris = total;
-    if (n > 0) {
-        k_pack_nodes<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.split.p, t.children.p, off,
-                                                                     t.tnode.p);
-        KDGB_LAUNCH_CHECK();
-        k_pack_tris<<<blocks_for(n, kPackBlock), kPackBlock, 0, s>>>(n, t.info.p, t.bitmap.p, t.pidx.p,
-                                                                    t.prim_indices.p, t.p0.p, t.p1.p, t.p2.p, off,
-                                                                    t.ttri.p);
-        KDGB_LAUNCH_CHECK();
-    }
-    return KDGB_OK;
-}
 
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
                  int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s,
@@ -507,6 +451,7 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
     a.ray_mesh = nullptr;
     a.rays_per_mesh = 1;
     a.n_meshes = 1;
+    a.build_err = t.ws.state.p ? &t.ws.state.p->err : nullptr;
     if (t.n_meshes > 1) {
         a.mesh_off = t.mesh_off.p;
         a.ray_mesh = ray_mesh;
@@ -554,6 +499,7 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
     a.ray_mesh = nullptr;
     a.rays_per_mesh = 1;
     a.n_meshes = 1;
+    a.build_err = t.ws.state.p ? &t.ws.state.p->err : nullptr;
     a.o = pts; a.d = nullptr; a.n = n;
     a.hit = nullptr; a.t = a.u = a.v = nullptr; a.occ = occ;
     a.light = make_float3(light[0], light[1], light[2]);
@@ -594,6 +540,7 @@ int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_p
     a.maxit = p.max_iterations > 0 ? p.max_iterations : kDefaultMaxIterations;
     a.seg_hit = seg_hit;
     a.seg_t = seg_t;
+    a.build_err = t.ws.state.p ? &t.ws.state.p->err : nullptr;
     const int bs = p.block_size > 0 ? p.block_size : 128;
     const unsigned grid = blocks_for(n, bs);
     const bool skip = p.leaf_skipping != 0;

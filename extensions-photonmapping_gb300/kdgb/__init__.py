@@ -21,12 +21,12 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import scenes
-from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ERR_NO_DEVICE, FINF, LEAF, LOWER_BITMAP, LOWER_SAH,
+from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ERR_CAPACITY, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, FINF, LEAF, LOWER_BITMAP, LOWER_SAH,
                    TIE_LOWEST_ID, TIE_REF_LAST, TRACER_BRUTE, TRACER_RESTART, TRACER_SHORTSTACK, X, Y, Z,
-                   BuildParams, BuildStats, KdgbError, PhotonParams, TraceParams, TreeView, build_params, check,
+                   AutotuneResult, BuildParams, BuildStats, KdgbError, PhotonParams, TraceParams, TreeView, build_params, check,
                    lib, library_path, photon_params, trace_params)
 
-__all__ = ["KDTree", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
+__all__ = ["KDTree", "Graph", "autotune", "AutotuneResult", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
            "trace_params", "photon_params", "PhotonParams", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
            "BUILD_REFERENCE", "BUILD_TUNED", "TRACER_RESTART", "TRACER_SHORTSTACK", "TRACER_BRUTE",
            "TIE_LOWEST_ID", "TIE_REF_LAST", "FINF", "lib", "library_path"]
@@ -281,8 +281,103 @@ def _trace_batch(self, o, d, ray_mesh=None, rays_per_mesh: int = 0, params: Trac
     return hit, t, u, v
 
 
+def _rebuild_batch(self, tris, mesh_offsets, params: BuildParams | None = None, stream=None, **kw) -> None:
+    """Rebuilds this handle as a batch (kdgb_rebuild_batch)."""
+    tri = _dev(tris, _torch().float32, 9)
+    off = np.ascontiguousarray(mesh_offsets, dtype=np.int32)
+    p = params if params is not None else build_params(**kw)
+    check(lib().kdgb_rebuild_batch(self._h, _ptr(tri), off.ctypes.data_as(C.c_void_p), off.shape[0] - 1,
+                                   C.byref(p), C.c_void_p(_stream(stream))), "kdgb_rebuild_batch")
+    self.n_tris = tri.shape[0]
+    self.mesh_offsets = off
+
+
 KDTree.build_batch = classmethod(_build_batch)
+KDTree.rebuild_batch = _rebuild_batch
 KDTree.trace_batch = _trace_batch
+
+
+class Graph:
+    """A rebuild of a tree (and optionally a trace) recorded as one CUDA
+    graph (kdgb_graph_create).  The triangle, ray and output tensors are
+    recorded by address: refill them in place, then launch()."""
+
+    def __init__(self, tree: KDTree, tris, mesh_offsets=None, params: BuildParams | None = None,
+                 headroom: float = 1.25, o=None, d=None, ray_mesh=None, rays_per_mesh: int = 0,
+                 trace: TraceParams | None = None, out=None, stream=None, **kw):
+        torch = _torch()
+        self.tree = tree
+        self.tris = _dev(tris, torch.float32, 9)
+        off = None if mesh_offsets is None else np.ascontiguousarray(mesh_offsets, dtype=np.int32)
+        n_meshes = 1 if off is None else off.shape[0] - 1
+        p = params if params is not None else build_params(**kw)
+        tp = trace if trace is not None else trace_params()
+        self.o = self.d = self.ray_mesh = None
+        self.out = None
+        n = 0
+        if o is not None:
+            self.o = _dev(o, torch.float32, 3)
+            self.d = _dev(d, torch.float32, 3)
+            self.ray_mesh = _dev(ray_mesh, torch.int32).reshape(-1) if ray_mesh is not None else None
+            n = self.o.shape[0]
+            dev = self.o.device
+            self.out = out if out is not None else (
+                torch.empty(n, dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.float32, device=dev),
+                torch.empty(n, dtype=torch.float32, device=dev), torch.empty(n, dtype=torch.float32, device=dev))
+        hit, t, u, v = self.out if self.out is not None else (None, None, None, None)
+        g = C.c_void_p()
+        check(lib().kdgb_graph_create(tree._h, _ptr(self.tris), self.tris.shape[0],
+                                      off.ctypes.data_as(C.c_void_p) if off is not None else None, n_meshes,
+                                      C.byref(p), headroom, C.byref(tp), _ptr(self.o), _ptr(self.d),
+                                      _ptr(self.ray_mesh), rays_per_mesh, n, _ptr(hit), _ptr(t), _ptr(u), _ptr(v),
+                                      C.byref(g), C.c_void_p(_stream(stream))), "kdgb_graph_create")
+        self._g = g
+
+    def launch(self, stream=None) -> None:
+        check(lib().kdgb_graph_launch(self._g, C.c_void_p(_stream(stream))), "kdgb_graph_launch")
+
+    def status(self, stream=None) -> int:
+        """Synchronises and returns the last launch's build status (0 = ok)."""
+        return lib().kdgb_graph_status(self._g, C.c_void_p(_stream(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_g", None):
+            lib().kdgb_graph_destroy(self._g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def autotune(tris, o=None, d=None, mesh_offsets=None, ray_mesh=None, rays_per_mesh: int = 0,
+             build: BuildParams | None = None, trace: TraceParams | None = None, builds_per_trace: float = 1.0,
+             reps: int = 3, stream=None) -> AutotuneResult:
+    """kdgb_autotune: the leaf threshold, SAH bins, short-stack depth and
+    block size that minimise builds_per_trace * rebuild_ms + trace_ms."""
+    torch = _torch()
+    tri = _dev(tris, torch.float32, 9)
+    off = None if mesh_offsets is None else np.ascontiguousarray(mesh_offsets, dtype=np.int32)
+    n_meshes = 1 if off is None else off.shape[0] - 1
+    od = _dev(o, torch.float32, 3) if o is not None else None
+    dd = _dev(d, torch.float32, 3) if d is not None else None
+    rm = _dev(ray_mesh, torch.int32).reshape(-1) if ray_mesh is not None else None
+    n = od.shape[0] if od is not None else 0
+    bp = build if build is not None else build_params()
+    tp = trace if trace is not None else trace_params()
+    res = AutotuneResult()
+    check(lib().kdgb_autotune(_ptr(tri), tri.shape[0], off.ctypes.data_as(C.c_void_p) if off is not None else None,
+                              n_meshes, _ptr(od), _ptr(dd), _ptr(rm), rays_per_mesh, n, C.byref(bp), C.byref(tp),
+                              builds_per_trace, reps, C.byref(res), C.c_void_p(_stream(stream))), "kdgb_autotune")
+    return res
 
 
 def backward(vertices, indices, o, d, hit, dL_dt, dL_du, dL_dv, out=None, stream=None):

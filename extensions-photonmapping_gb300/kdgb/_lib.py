@@ -57,6 +57,11 @@ class PhotonParams(C.Structure):
     _fields_ = [("light", C.c_float * 3), ("seed", C.c_uint64), ("bounces", C.c_int32), ("survival", C.c_float)]
 
 
+class AutotuneResult(C.Structure):
+    _fields_ = [("build", BuildParams), ("trace", TraceParams), ("build_ms", C.c_float), ("trace_ms", C.c_float),
+                ("baseline", C.c_float), ("objective", C.c_float), ("trials", C.c_int32)]
+
+
 class BuildStats(C.Structure):
     _fields_ = [("upper_levels", C.c_int32), ("lower_levels", C.c_int32), ("n_nodes", C.c_int32),
                 ("n_refs", C.c_int32), ("n_leaves", C.c_int32), ("max_depth", C.c_int32),
@@ -85,7 +90,16 @@ SIGNATURES = {
     "kdgb_photon_params_default": (None, [C.POINTER(PhotonParams)]),
     "kdgb_trace_photons": (C.c_int, [P, C.POINTER(TraceParams), C.POINTER(PhotonParams), C.c_int32, P, P, P]),
     "kdgb_build_batch": (C.c_int, [P, P, C.c_int32, C.POINTER(BuildParams), C.POINTER(C.c_void_p), P]),
+    "kdgb_rebuild_batch": (C.c_int, [P, P, P, C.c_int32, C.POINTER(BuildParams), P]),
     "kdgb_trace_batch": (C.c_int, [P, C.POINTER(TraceParams), P, P, P, C.c_int32, C.c_int32, P, P, P, P, P]),
+    "kdgb_graph_create": (C.c_int, [P, P, C.c_int32, P, C.c_int32, C.POINTER(BuildParams), C.c_float,
+                                    C.POINTER(TraceParams), P, P, P, C.c_int32, C.c_int32, P, P, P, P,
+                                    C.POINTER(C.c_void_p), P]),
+    "kdgb_graph_launch": (C.c_int, [P, P]),
+    "kdgb_autotune": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, P, C.c_int32, C.c_int32, C.POINTER(BuildParams),
+                                C.POINTER(TraceParams), C.c_float, C.c_int32, C.POINTER(AutotuneResult), P]),
+    "kdgb_graph_status": (C.c_int, [P, P]),
+    "kdgb_graph_destroy": (C.c_int, [P]),
     "kdgb_geometry_gather": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, P]),
     "kdgb_osc_update_surface": (C.c_int, [P, P, C.c_int32, C.c_float, C.c_float, P]),
     "kdgb_backward": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, C.c_int32, P, P, P, P, P, P]),

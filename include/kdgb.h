@@ -237,6 +237,11 @@ KDGB_API int kdgb_trace_photons(const kdgb_tree *tree, const kdgb_trace_params *
 KDGB_API int kdgb_build_batch(const float *tri_v_dev, const int32_t *mesh_offsets, int32_t n_meshes,
                               const kdgb_build_params *params, kdgb_tree **out, kdgb_stream_t stream);
 
+/* Rebuilds a tree handle as a batch (same meaning as kdgb_build_batch),
+ * reusing its device buffers. */
+KDGB_API int kdgb_rebuild_batch(kdgb_tree *tree, const float *tri_v_dev, const int32_t *mesh_offsets,
+                                int32_t n_meshes, const kdgb_build_params *params, kdgb_stream_t stream);
+
 /* Traces rays of a batch: ray i belongs to mesh ray_mesh_dev[i], or to mesh
  * i / rays_per_mesh when ray_mesh_dev is NULL.  Hit ids are relative to the
  * mesh's first triangle. */
@@ -244,6 +249,70 @@ KDGB_API int kdgb_trace_batch(const kdgb_tree *tree, const kdgb_trace_params *pa
                               const float *ray_o_dev, const float *ray_d_dev, const int32_t *ray_mesh_dev,
                               int32_t rays_per_mesh, int32_t n, int32_t *hit_dev, float *t_dev, float *u_dev,
                               float *v_dev, kdgb_stream_t stream);
+
+/* Graph rebuilds (no reference counterpart: TriangleMap::Create waits on the
+ * device at every level of its host loop, TriangleMapUpperCreator.cu:
+ * 110-759).  A kdgb_graph records one complete rebuild of `tree` -- and,
+ * with n_rays > 0, a trace of its rays -- into a CUDA graph.  Launching it
+ * rebuilds with no host synchronisation and no device allocation: the level
+ * loops are conditional WHILE graph nodes driven by device-side counters.
+ *  - The tree must have completed a kdgb_build / kdgb_rebuild (or batch
+ *    build) first; the graph's fixed buffers are that build's sizes times
+ *    `headroom` (1 to 64; 1.25 leaves 25% for geometry that changes
+ *    between launches).
+ *  - tri_v_dev (n_tris triangles; n_meshes > 1: a batch with HOST
+ *    mesh_offsets as in kdgb_build_batch), the rays and the outputs are
+ *    recorded by address: refill them in place between launches.  The trace
+ *    is kdgb_trace (one mesh) or kdgb_trace_batch (ray_mesh_dev /
+ *    rays_per_mesh) with `trace`; kd tracers only.
+ *  - A rebuild that would outgrow a buffer stops and leaves the tree invalid
+ *    (its traces report misses); kdgb_graph_status then returns
+ *    KDGB_ERR_CAPACITY.  Rebuild with kdgb_rebuild / kdgb_rebuild_batch and
+ *    create the graph again.
+ *  - kdgb_graph_status synchronises the stream, returns the last launch's
+ *    build status and refreshes the tree's host-side counts
+ *    (kdgb_tree_stats, kdgb_tree_view_get are stale until then).
+ *  - A host-driven rebuild that reallocates any of the tree's buffers
+ *    invalidates the graph: kdgb_graph_launch then returns
+ *    KDGB_ERR_INVALID_ARGUMENT.  Destroy graphs before their tree. */
+typedef struct kdgb_graph kdgb_graph;
+
+KDGB_API int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris,
+                               const int32_t *mesh_offsets, int32_t n_meshes, const kdgb_build_params *params,
+                               float headroom, const kdgb_trace_params *trace, const float *ray_o_dev,
+                               const float *ray_d_dev, const int32_t *ray_mesh_dev, int32_t rays_per_mesh,
+                               int32_t n_rays, int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
+                               kdgb_graph **out, kdgb_stream_t stream);
+KDGB_API int kdgb_graph_launch(kdgb_graph *graph, kdgb_stream_t stream);
+KDGB_API int kdgb_graph_status(kdgb_graph *graph, kdgb_stream_t stream);
+KDGB_API int kdgb_graph_destroy(kdgb_graph *graph);
+
+/* Autotuner (no reference counterpart).  Picks leaf_size (16/24/32),
+ * sah_bins (8/16/32, tuned mode only), stack_depth (2/4/8, short-stack
+ * only) and block_size (64/128/256) for a workload by coordinate descent
+ * from `build` / `trace`, scoring each candidate by
+ * builds_per_trace * rebuild_ms + trace_ms (median of `reps` timed runs on
+ * `stream`; 1 = rebuild every frame, 0 = a static scene).  The workload is
+ * one mesh (n_meshes = 1, mesh_offsets NULL) or a batch (HOST mesh_offsets
+ * as in kdgb_build_batch, rays by ray_mesh_dev or rays_per_mesh); n_rays
+ * may be 0 to tune the build alone.  Candidates that fail (a tree that does
+ * not terminate within 4 levels more than the starting one, or no memory)
+ * are skipped.  Synchronises the stream; allocates a temporary tree. */
+typedef struct kdgb_autotune_result {
+    kdgb_build_params build; /* chosen build parameters */
+    kdgb_trace_params trace; /* chosen trace parameters */
+    float build_ms;          /* rebuild time of the choice */
+    float trace_ms;          /* trace time of the choice */
+    float baseline;          /* objective of the starting parameters */
+    float objective;         /* objective of the choice (<= baseline) */
+    int32_t trials;          /* candidates measured */
+} kdgb_autotune_result;
+
+KDGB_API int kdgb_autotune(const float *tri_v_dev, int32_t n_tris, const int32_t *mesh_offsets, int32_t n_meshes,
+                           const float *ray_o_dev, const float *ray_d_dev, const int32_t *ray_mesh_dev,
+                           int32_t rays_per_mesh, int32_t n_rays, const kdgb_build_params *build,
+                           const kdgb_trace_params *trace, float builds_per_trace, int32_t reps,
+                           kdgb_autotune_result *out, kdgb_stream_t stream);
 
 /* Adjoint of first-hit t, u, v with respect to vertex positions (no
  * reference counterpart).  vertices: n_vertices*3 floats; indices:
