@@ -48,8 +48,12 @@ WIDTH, HEIGHT = 1920, 1080
 LIGHT = (0.5, 3.0, 0.5)
 SCENE_SEED = 2
 BUILD = dict(lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
-BUILD_DESC = ("reference upper (median + empty space to <32 refs) + SAH lower Ct=1 Ci=1.5 min_leaf=8, "
-              "rebuilt by one graph launch")
+BUILD_DESC = "reference upper (median + empty space to <32 refs) + SAH lower Ct=1 Ci=1.5 min_leaf=8"
+# The frame's configuration: median/empty-space splits on the top 8 levels, then SAH (binned, 32 bins, down to
+# nodes of < 32 references), then the reference's SAH lower phase (Ct=1, Ci=1.5, leaf threshold 8).
+BUILD_TUNED = dict(BUILD, mode=1, upper_levels=8, sah_bins=32)
+BUILD_TUNED_DESC = ("median + empty space on the top 8 levels, binned SAH (32 bins) below to <32 refs, "
+                    "then SAH lower Ct=1 Ci=1.5 min_leaf=8")
 STACK_DEPTH = 8
 HEADROOM = 1.1
 FLUSH_BYTES = 512 << 20
@@ -66,6 +70,8 @@ def parse():
     ap.add_argument("--width", type=int, default=WIDTH)
     ap.add_argument("--height", type=int, default=HEIGHT)
     ap.add_argument("--host-build", action="store_true", help="rebuild with the host-driven level loop")
+    ap.add_argument("--build", default="tuned", choices=["tuned", "reference"],
+                    help="tuned: the frame's configuration; reference: the reference's creators")
     ap.add_argument("--profile", action="store_true",
                     help="one build and two traces, nothing timed (for ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -155,13 +161,16 @@ def measured_peak_gbs():
 
 
 def committed_traffic():
-    """DRAM bytes per trace launch from the committed ncu summary; None when
-    no capture has been committed."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+    """DRAM bytes (read + write) per launch of the trace kernel from the
+    committed ncu summary; None when no capture has been committed."""
+    path = os.path.join(ROOT, "profiles", "k_trace_clustered1M_frame.md")
     if not os.path.exists(path):
         return None
+    import re
     with open(path) as f:
-        return json.load(f)
+        m = re.search(r"^traffic_bytes_per_launch = (\d+)$", f.read(), re.M)
+    return {"trace_dram_bytes_per_launch": int(m.group(1)), "source": "profiles/k_trace_clustered1M_frame.md"} \
+        if m else None
 
 
 def oracle_module():
@@ -192,8 +201,9 @@ def cpu_baseline(tris, o, d, sample_stride=16, threads=0):
     rays = n_sample * scale
     cores = threads if threads > 0 else (os.cpu_count() or 1)
     return {"value": rays / step_s / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
-            "sample": f"full CPU build ({t_build * 1e3:.0f} ms) + every {sample_stride}th primary ray and its "
-                      f"shadow ray ({t_trace * 1e3:.0f} ms), extrapolated to the frame",
+            "sample": f"full CPU build with the reference's creators ({t_build * 1e3:.0f} ms) + every "
+                      f"{sample_stride}th primary ray and its shadow ray ({t_trace * 1e3:.0f} ms), extrapolated "
+                      f"to the frame",
             "build_ms": t_build * 1e3}
 
 
@@ -264,7 +274,8 @@ def run_frame(args, world, rank, local, pg):
     tris_d = torch.from_numpy(tris).to(dev)
     o_d = torch.from_numpy(o).to(dev)
     d_d = torch.from_numpy(d).to(dev)
-    bp = kdgb.build_params(**BUILD)
+    build_kw, build_desc = (BUILD_TUNED, BUILD_TUNED_DESC) if args.build == "tuned" else (BUILD, BUILD_DESC)
+    bp = kdgb.build_params(**build_kw)
     tp = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH, tile_width=args.width)
     tree = kdgb.KDTree.build(tris_d, bp)
     graph = None if args.host_build else kdgb.Graph(tree, tris_d, params=bp, headroom=HEADROOM)
@@ -401,7 +412,8 @@ def run_frame(args, world, rank, local, pg):
                 "dtype": "f32", "data": "synthetic (seeded clustered scene, pinhole camera)",
                 "config": {"workload": "clustered-1M-tris 1920x1080 primary + shadow, short-stack depth 8",
                            "tris": T, "rays_primary": n, "rays_shadow": n_hits,
-                           "build": BUILD_DESC if graph is not None else BUILD_DESC.split(",")[0] + " (host loop)",
+                           "build": build_desc + (", rebuilt by one graph launch" if graph is not None else
+                                                  ", host-driven level loop"),
                            "l2": "512 MB buffer written between timed steps",
                            "parallelism": f"replicas x{world}"},
                 "build_ms": statistics.mean(s - t for s, t in zip(step_ms, trace_ms)),

@@ -39,7 +39,7 @@ constexpr int kBlock = 256;
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
-// The per-reference passes (k_reduce, k_count, k_scatter, k_sah_bin) walk
+// The per-reference passes (k_reduce, k_count, k_scatter) walk
 // the reference array in warp chunks of kRows rows of 32 consecutive
 // references, kWarps consecutive chunks per block tile.  Owners are sorted,
 // so most rows belong to one node: a warp keeps per-lane accumulators while
@@ -99,7 +99,7 @@ struct BuildArgs {
     int32_t *prim_indices, *leaf_ids;
     float4 *pmin, *pmax;
     unsigned *keys;
-    int32_t *cnt, *lanes, *lbase, *chunksum, *chunkoff, *hist;
+    int32_t *cnt, *lanes, *lbase, *chunksum, *chunkoff;
     int8_t *planes;
     int2 *ranges;
     int32_t *roff;
@@ -128,9 +128,11 @@ __device__ __forceinline__ bool sah_level(const BuildArgs &a, const BuildState *
     return a.tuned && st->level + 1 > a.upper_levels;
 }
 
+// Empty-space splitting runs on every level but the first, in tuned mode
+// too (ahead of the binned SAH split of the remaining box).
 __device__ __forceinline__ bool do_ess(const BuildArgs &a, const BuildState *st)
 {
-    return a.ess && st->active != 0 && !sah_level(a, st);
+    return a.ess && st->active != 0;
 }
 
 #define GRID_STRIDE(i, n) \
@@ -529,117 +531,151 @@ __device__ __forceinline__ int sah_bin(float x, float mn, float scale, int B)
     return b < 0 ? 0 : (b > B - 1 ? B - 1 : b);
 }
 
-__global__ void k_sah_clear(const BuildArgs a)
-{
-    const BuildState *st = a.st;
-    if (!sah_level(a, st)) return;
-    const int64_t n = (int64_t)st->R * 6 * a.B;
-    GRID_STRIDE(i, n) a.hist[i] = 0;
-}
+// Nodes with at least this many references are binned by a whole block,
+// smaller ones by one warp.
+constexpr int kSahBlockRefs = 2048;
 
-// Histograms hist[((node * 3 + axis) * 2 + side) * B + bin]; lanes of a
-// warp with the same (owner, axis, side, bin) add once.
-__global__ void __launch_bounds__(kBlock) k_sah_bin(const BuildArgs a)
+// Bins the references [first, first + cnt) of one node into h[(axis * 2 +
+// side) * 32 + bin] (shared memory, zeroed by the caller); threads `tid` of
+// `nthreads` share the range.
+__device__ __forceinline__ void sah_fill(const float4 *__restrict__ cmin, const float4 *__restrict__ cmax,
+                                         int64_t first, int32_t cnt, const float (&lo)[3], const float (&scale)[3],
+                                         const bool (&valid)[3], int B, int *h, int tid, int nthreads)
 {
-    const BuildState *st = a.st;
-    if (!sah_level(a, st)) return;
-    const int64_t N = st->N;
-    const int32_t active = st->active;
-    const int B = a.B;
-    const int cur = st->level & 1;
-    const float4 *__restrict__ cmin = a.rmin[cur];
-    const float4 *__restrict__ cmax = a.rmax[cur];
-    const unsigned lane = threadIdx.x & 31;
-    WARP_STRIDE(chunk, chunks_for(N)) {
-        const int64_t base = chunk * kChunk;
-        for (int row = 0; row < kRows; ++row) {
-            if (base + row * 32 >= N) break;
-            const int64_t r = base + row * 32 + lane;
-            int o = -1;
-            float4 lo4 = make_float4(0.f, 0.f, 0.f, 0.f), hi4 = lo4, mn = lo4, mx = lo4;
-            if (r < N) {
-                lo4 = cmin[r];
-                hi4 = cmax[r];
-                o = __float_as_int(hi4.w);
-                mn = a.bmin[active + o];
-                mx = a.bmax[active + o];
-            }
-            for (int ax = 0; ax < 3; ++ax) {
-                const float lo = ax == 0 ? mn.x : (ax == 1 ? mn.y : mn.z);
-                const float ext = __fsub_rn(ax == 0 ? mx.x : (ax == 1 ? mx.y : mx.z), lo);
-                const bool valid = o >= 0 && ext > 0.0f;
-                const float scale = valid ? __fdiv_rn((float)B, ext) : 0.0f;
-                for (int side = 0; side < 2; ++side) {
-                    const float4 &src = side == 0 ? lo4 : hi4;
-                    const float x = ax == 0 ? src.x : (ax == 1 ? src.y : src.z);
-                    const int bin = valid ? sah_bin(x, lo, scale, B) : 0;
-                    // Key: (owner, bin); invalid lanes get a key no valid lane has.
-                    const long long key = valid ? ((long long)o << 8 | bin) : -1ll;
-                    const unsigned m = __match_any_sync(kFull, key);
-                    if (valid && lane == (unsigned)(__ffs(m) - 1))
-                        atomicAdd(a.hist + (((int64_t)o * 3 + ax) * 2 + side) * B + bin, __popc(m));
-                }
-            }
+    for (int32_t i = tid; i < cnt; i += nthreads) {
+        const float4 p = cmin[first + i], q = cmax[first + i];
+        const float pv[3] = {p.x, p.y, p.z}, qv[3] = {q.x, q.y, q.z};
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            if (!valid[ax]) continue;
+            atomicAdd(h + (ax * 2 + 0) * 32 + sah_bin(pv[ax], lo[ax], scale[ax], B), 1);
+            atomicAdd(h + (ax * 2 + 1) * 32 + sah_bin(qv[ax], lo[ax], scale[ax], B), 1);
         }
     }
 }
 
-// One warp per node, lane k-1 evaluates the plane at bin boundary k.
-__global__ void k_sah_split(const BuildArgs a)
+// One warp evaluates the planes of a node from its histograms: lane k-1
+// takes the plane at bin boundary k; the first strict minimum over (axis,
+// k) wins.  Lane 0 writes the split.
+__device__ __forceinline__ void sah_pick(const BuildArgs &a, int32_t node, int32_t cnt, const float (&mnv)[3],
+                                         const float (&mxv)[3], const float (&ext)[3], const int *h, int lane)
 {
+    const int B = a.B;
+    float best = INFINITY, best_sp = 0.0f;
+    int best_ax = -1;
+    for (int ax = 0; ax < 3; ++ax) {
+        if (!(ext[ax] > 0.0f)) continue;  // warp-uniform
+        const int32_t lo = lane < B ? h[(ax * 2 + 0) * 32 + lane] : 0;
+        const int32_t hi = lane < B ? h[(ax * 2 + 1) * 32 + lane] : 0;
+        int32_t plo = lo, phi = hi;  // inclusive prefix sums over bins
+        for (int s = 1; s < 32; s <<= 1) {
+            const int32_t x = __shfl_up_sync(kFull, plo, s), y = __shfl_up_sync(kFull, phi, s);
+            if (lane >= s) { plo += x; phi += y; }
+        }
+        const int32_t total_hi = __shfl_sync(kFull, phi, 31);
+        const int k = lane + 1;
+        float cost = INFINITY, pk = 0.0f;
+        if (k < B) {
+            const int32_t nl = plo, nr = total_hi - phi;
+            const float w = __fdiv_rn(ext[ax], (float)B);
+            pk = __fadd_rn(mnv[ax], __fmul_rn((float)k, w));
+            float le[3] = {ext[0], ext[1], ext[2]}, re[3] = {ext[0], ext[1], ext[2]};
+            le[ax] = __fsub_rn(pk, mnv[ax]);
+            re[ax] = __fsub_rn(mxv[ax], pk);
+            const float al = __fadd_rn(__fadd_rn(__fmul_rn(le[0], le[1]), __fmul_rn(le[1], le[2])), __fmul_rn(le[2], le[0]));
+            const float ar = __fadd_rn(__fadd_rn(__fmul_rn(re[0], re[1]), __fmul_rn(re[1], re[2])), __fmul_rn(re[2], re[0]));
+            const float c = __fadd_rn(__fmul_rn(al, (float)nl), __fmul_rn(ar, (float)nr));
+            if (nl > 0 && nr > 0 && !(nl == cnt && nr == cnt)) cost = c;
+        }
+        // First minimum in k order within the axis, then strictly better
+        // than the previous axes.
+        float c = cost;
+        int kk = k;
+        for (int s = 16; s > 0; s >>= 1) {
+            const float c2 = __shfl_xor_sync(kFull, c, s);
+            const int k2 = __shfl_xor_sync(kFull, kk, s);
+            if (c2 < c || (c2 == c && k2 < kk)) { c = c2; kk = k2; }
+        }
+        const float sp = __shfl_sync(kFull, pk, kk - 1);
+        if (c < best) { best = c; best_ax = ax; best_sp = sp; }
+    }
+    if (lane == 0 && best_ax >= 0) {
+        a.info[node] = (int8_t)(best_ax + 1);
+        a.split[node] = best_sp;
+    }
+}
+
+struct SahNode {
+    int32_t node, cnt;
+    int64_t first;
+    float mnv[3], mxv[3], ext[3], scale[3];
+    bool valid[3];
+};
+
+// An active node's references are contiguous: [pidx, pidx + amt) of the
+// current reference buffer (k_begin / k_children place them so).
+__device__ __forceinline__ SahNode sah_node(const BuildArgs &a, int32_t node)
+{
+    SahNode n;
+    n.node = node;
+    n.cnt = a.amt[node];
+    n.first = a.pidx[node];
+    const float4 mn4 = a.bmin[node], mx4 = a.bmax[node];
+    n.mnv[0] = mn4.x; n.mnv[1] = mn4.y; n.mnv[2] = mn4.z;
+    n.mxv[0] = mx4.x; n.mxv[1] = mx4.y; n.mxv[2] = mx4.z;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        n.ext[ax] = __fsub_rn(n.mxv[ax], n.mnv[ax]);
+        n.valid[ax] = n.ext[ax] > 0.0f;
+        n.scale[ax] = n.valid[ax] ? __fdiv_rn((float)a.B, n.ext[ax]) : 0.0f;
+    }
+    return n;
+}
+
+// Binned SAH of the active nodes below kSahBlockRefs references: one warp
+// per node, histograms in shared memory.
+__global__ void __launch_bounds__(kBlock) k_sah_warp(const BuildArgs a)
+{
+    __shared__ int s_hist[kWarps][6 * 32];
     const BuildState *st = a.st;
     if (!sah_level(a, st)) return;
     const int32_t R = st->R, active = st->active;
-    const int B = a.B;
-    const int lane = threadIdx.x & 31;
+    const int cur = st->level & 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int *h = s_hist[warp];
     WARP_STRIDE(gw, R) {
         const int32_t node = active + (int32_t)gw;
-        const int32_t cnt = a.amt[node];
-        const float4 mn4 = a.bmin[node], mx4 = a.bmax[node];
-        const float mnv[3] = {mn4.x, mn4.y, mn4.z}, mxv[3] = {mx4.x, mx4.y, mx4.z};
-        const float ext[3] = {__fsub_rn(mxv[0], mnv[0]), __fsub_rn(mxv[1], mnv[1]), __fsub_rn(mxv[2], mnv[2])};
-        float best = INFINITY, best_sp = 0.0f;
-        int best_ax = -1;
-        for (int ax = 0; ax < 3; ++ax) {
-            if (!(ext[ax] > 0.0f)) continue;  // warp-uniform
-            const int32_t *h = a.hist + (gw * 3 + ax) * 2 * B;
-            const int32_t lo = lane < B ? h[lane] : 0, hi = lane < B ? h[B + lane] : 0;
-            int32_t plo = lo, phi = hi;  // inclusive prefix sums over bins
-            for (int s = 1; s < 32; s <<= 1) {
-                const int32_t x = __shfl_up_sync(kFull, plo, s), y = __shfl_up_sync(kFull, phi, s);
-                if (lane >= s) { plo += x; phi += y; }
-            }
-            const int32_t total_hi = __shfl_sync(kFull, phi, 31);
-            const int k = lane + 1;
-            float cost = INFINITY, pk = 0.0f;
-            if (k < B) {
-                const int32_t nl = plo, nr = total_hi - phi;
-                const float w = __fdiv_rn(ext[ax], (float)B);
-                pk = __fadd_rn(mnv[ax], __fmul_rn((float)k, w));
-                float le[3] = {ext[0], ext[1], ext[2]}, re[3] = {ext[0], ext[1], ext[2]};
-                le[ax] = __fsub_rn(pk, mnv[ax]);
-                re[ax] = __fsub_rn(mxv[ax], pk);
-                const float al = __fadd_rn(__fadd_rn(__fmul_rn(le[0], le[1]), __fmul_rn(le[1], le[2])), __fmul_rn(le[2], le[0]));
-                const float ar = __fadd_rn(__fadd_rn(__fmul_rn(re[0], re[1]), __fmul_rn(re[1], re[2])), __fmul_rn(re[2], re[0]));
-                const float c = __fadd_rn(__fmul_rn(al, (float)nl), __fmul_rn(ar, (float)nr));
-                if (nl > 0 && nr > 0 && !(nl == cnt && nr == cnt)) cost = c;
-            }
-            // First minimum in k order within the axis, then strictly better
-            // than the previous axes.
-            float c = cost;
-            int kk = k;
-            for (int s = 16; s > 0; s >>= 1) {
-                const float c2 = __shfl_xor_sync(kFull, c, s);
-                const int k2 = __shfl_xor_sync(kFull, kk, s);
-                if (c2 < c || (c2 == c && k2 < kk)) { c = c2; kk = k2; }
-            }
-            const float sp = __shfl_sync(kFull, pk, kk - 1);
-            if (c < best) { best = c; best_ax = ax; best_sp = sp; }
-        }
-        if (lane == 0 && best_ax >= 0) {
-            a.info[node] = (int8_t)(best_ax + 1);
-            a.split[node] = best_sp;
-        }
+        if (a.amt[node] >= kSahBlockRefs) continue;  // warp-uniform
+        const SahNode n = sah_node(a, node);
+        for (int j = lane; j < 6 * 32; j += 32) h[j] = 0;
+        __syncwarp();
+        sah_fill(a.rmin[cur], a.rmax[cur], n.first, n.cnt, n.mnv, n.scale, n.valid, a.B, h, lane, 32);
+        __syncwarp();
+        sah_pick(a, node, n.cnt, n.mnv, n.mxv, n.ext, h, lane);
+        __syncwarp();
+    }
+}
+
+// The same for nodes of kSahBlockRefs references or more: one block per node.
+__global__ void __launch_bounds__(kBlock) k_sah_block(const BuildArgs a)
+{
+    __shared__ int s_hist[6 * 32];
+    const BuildState *st = a.st;
+    if (!sah_level(a, st)) return;
+    const int32_t R = st->R, active = st->active;
+    const int cur = st->level & 1;
+    const int lane = threadIdx.x & 31;
+    for (int32_t k = blockIdx.x; k < R; k += gridDim.x) {
+        const int32_t node = active + k;
+        if (a.amt[node] < kSahBlockRefs) continue;  // block-uniform
+        const SahNode n = sah_node(a, node);
+        for (int j = threadIdx.x; j < 6 * 32; j += blockDim.x) s_hist[j] = 0;
+        __syncthreads();
+        sah_fill(a.rmin[cur], a.rmax[cur], n.first, n.cnt, n.mnv, n.scale, n.valid, a.B, s_hist, threadIdx.x,
+                 blockDim.x);
+        __syncthreads();
+        if (threadIdx.x < 32) sah_pick(a, node, n.cnt, n.mnv, n.mxv, n.ext, s_hist, lane);
+        __syncthreads();
     }
 }
 
@@ -1445,7 +1481,6 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.cap.R = std::min({w.pmin.cap, w.pmax.cap, w.keys.cap / 6, w.cnt.cap / 2});
     a.chunksum = w.chunksum.p;
     a.chunkoff = w.chunkoff.p;
-    a.hist = w.hist.p;
     a.ranges = w.ranges.p;
     a.roff = w.roff.p;
     a.cap.ranges = std::min(w.ranges.cap, w.roff.cap);
@@ -1490,13 +1525,10 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
     k_node_split<<<gR, kBlock, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
     if (tuned_levels) {
-        k_sah_clear<<<L.grid(e.R * 6 * a.B, kBlock, 2), kBlock, 0, s>>>(a);
+        k_sah_block<<<L.grid(std::min<int64_t>(e.R, ceil_div(e.N, kSahBlockRefs)) * kBlock, kBlock, 2), kBlock, 0,
+                      s>>>(a);
         KDGB_LAUNCH_CHECK();
-        if (e.N > 0) {
-            k_sah_bin<<<gW, kBlock, 0, s>>>(a);
-            KDGB_LAUNCH_CHECK();
-        }
-        k_sah_split<<<L.grid(e.R * 32, kBlock), kBlock, 0, s>>>(a);
+        k_sah_warp<<<L.grid(e.R * 32, kBlock), kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
     if (e.N > 0) {
@@ -1641,7 +1673,6 @@ void graph_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, const
     a.cap.refs[0] = std::min(a.cap.refs[0], chunk_refs);
     a.cap.refs[1] = std::min(a.cap.refs[1], chunk_refs);
     a.cap.R = std::min({a.cap.R, w.lanes.cap / kLanes, w.lbase.cap / kLanes - 1, w.planes.cap});
-    if (p.mode == KDGB_BUILD_TUNED) a.cap.R = std::min(a.cap.R, w.hist.cap / (6 * (int64_t)p.sah_bins));
     a.cap.leaves = t.leaf_ids.cap;
     a.cap.low_R = std::min({w.ssplit.cap, w.saddr.cap - 1, w.careas.cap, w.csets.cap});
     a.cap.fin = std::min({a.cap.fin, t.prim_indices.cap, w.areas.cap, w.sts.cap / 3});
@@ -1671,7 +1702,7 @@ uint64_t layout_signature(const Tree &t)
     MIX(t.tnode); MIX(t.ttri); MIX(t.mesh_off);
     MIX(w.rmin[0]); MIX(w.rmin[1]); MIX(w.rmax[0]); MIX(w.rmax[1]); MIX(w.fmin); MIX(w.fmax); MIX(w.pmin);
     MIX(w.pmax); MIX(w.keys); MIX(w.planes); MIX(w.cnt); MIX(w.lanes); MIX(w.lbase); MIX(w.chunksum);
-    MIX(w.chunkoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.hist); MIX(w.areas); MIX(w.sts);
+    MIX(w.chunkoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.areas); MIX(w.sts);
     MIX(w.ssplit); MIX(w.saddr); MIX(w.roff); MIX(w.careas); MIX(w.csets); MIX(w.ranges); MIX(w.state);
 #undef MIX
     return h;
@@ -1789,7 +1820,6 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
         KDGB_CHECK(grab(w.planes, R, s));
         KDGB_CHECK(grab(w.chunksum, 2 * chunks_for(N), s));
         KDGB_CHECK(grab(w.chunkoff, 2 * (chunks_for(N) + 1), s));
-        if (tuned_level) KDGB_CHECK(grab(w.hist, R * 6 * p.sah_bins, s));
         const Extents e{N, R, F, n_nodes, 0, 0};
         KDGB_CHECK(emit_upper_level(make_args(t, p, T, M, mesh_off_dev), L, e, tuned_level, w, s));
         KDGB_CHECK(fetch_state(t, st, s));
@@ -1882,7 +1912,6 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.planes, R, s));
     KDGB_CHECK(ensure(w.chunksum, 2 * chunks_for(refs), s));
     KDGB_CHECK(ensure(w.chunkoff, 2 * (chunks_for(refs) + 1), s));
-    KDGB_CHECK(ensure(w.hist, p.mode == KDGB_BUILD_TUNED ? R * 6 * p.sah_bins : 1, s));
     KDGB_CHECK(ensure(w.ranges, (int64_t)p.max_levels + 1, s));
     KDGB_CHECK(ensure(w.roff, (int64_t)p.max_levels + 1, s));
     KDGB_CHECK(ensure(t.leaf_ids, leaves, s));

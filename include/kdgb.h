@@ -66,9 +66,11 @@ enum { KDGB_LEAF = 0, KDGB_X = 1, KDGB_Y = 2, KDGB_Z = 3 };
 enum { KDGB_LOWER_BITMAP = 0, KDGB_LOWER_SAH = 1 };
 
 /* Build modes.  REFERENCE reproduces TriangleMap::Create bit for bit.
- * TUNED runs the reference's median/empty-space splits for the top
- * `upper_levels` levels and a binned SAH (sah_bins bins per axis) for the
- * remaining upper levels; the lower phase is chosen by `lower` as before. */
+ * TUNED splits the top `upper_levels` levels at the reference's spatial
+ * median and the remaining upper levels by a binned SAH (sah_bins bins per
+ * axis, down to nodes of < leaf_size references), with the reference's
+ * empty-space cuts on every level but the root; the lower phase is chosen
+ * by `lower` as before. */
 enum { KDGB_BUILD_REFERENCE = 0, KDGB_BUILD_TUNED = 1 };
 
 /* Tracers: Raytracer (kd-restart), ShortStack, BruteTracer. */

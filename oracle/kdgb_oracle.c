@@ -763,9 +763,10 @@ static int build_upper(const float *tri, int32_t T, const or_build_params *p, no
         }
 
         /* CreateEmptySplits, not at the root (TriangleMapUpperCreator.cu:302-303,
-         * EmptySpaceSplitting.h:10-184); in tuned mode only on the median levels. */
+         * EmptySpaceSplitting.h:10-184); in tuned mode on every level, before
+         * the median or the binned SAH split of the remaining box. */
         const int sah_level = p->mode == 1 && level > p->upper_levels;
-        if (p->split_empty_space && active != 0 && !sah_level) {
+        if (p->split_empty_space && active != 0) {
             free(planes); free(req); free(eaddr);
             planes = calloc((size_t)R, 1); req = calloc((size_t)R, sizeof(int32_t));
             eaddr = calloc((size_t)R + 1, sizeof(int32_t));
@@ -849,8 +850,8 @@ static int build_upper(const float *tri, int32_t T, const or_build_params *p, no
             nd->split[active + k] = z_higher ? mdz : sp;
             nd->info[active + k] = z_higher ? OR_Z : ax;
         }
-        /* Tuned mode below the median levels: binned SAH split (new in this
-         * build; the reference splits every upper level at the median). */
+        /* Tuned mode below the median levels: binned SAH split (no reference
+         * counterpart; the reference splits every upper level at the median). */
         if (sah_level) {
 #pragma omp parallel for schedule(dynamic, 8)
             for (int32_t k = 0; k < R; ++k) {

@@ -77,8 +77,9 @@ TUNED = dict(mode=1, upper_levels=8, sah_bins=32, lower=1, traversal_cost=1.0, i
 
 @pytest.mark.parametrize("name", ["c1", "clustered3k", "clustered60k", "soup", "degenerate"])
 def test_tuned_build_matches_oracle(kdgb_lib, cuda, oracle, name):
-    """Tuned mode (median/empty-space for 8 levels, then binned SAH) is new
-    in this build; the oracle restates it, so the trees must be identical."""
+    """Tuned mode (median for 8 levels, then binned SAH; empty-space cuts on
+    every level) has no reference counterpart; the oracle restates it, so the
+    trees must be identical."""
     tris = scene(name)
     ref = oracle.build(tris, **TUNED)
     with kdgb_lib.KDTree.build(tris, **TUNED) as tree:
