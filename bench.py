@@ -180,13 +180,14 @@ def oracle_module():
     return O
 
 
-def cpu_baseline(tris, o, d, sample_stride=16, threads=0):
-    """The oracle (reference algorithms restated in C, OpenMP) on the host
-    cores: full build + traced sample of every `sample_stride`-th ray."""
+def cpu_baseline(tris, o, d, build_kw, sample_stride=16, threads=0):
+    """The oracle (the build and tracers restated in C, OpenMP) on the host
+    cores: full build with the GPU arm's parameters + traced sample of every
+    `sample_stride`-th ray."""
     O = oracle_module()
     from kdgb import scenes
     t0 = time.perf_counter()
-    tree = O.build(tris, **BUILD)
+    tree = O.build(tris, **build_kw)
     t_build = time.perf_counter() - t0
     idx = np.arange(0, o.shape[0], sample_stride)
     t0 = time.perf_counter()
@@ -201,7 +202,7 @@ def cpu_baseline(tris, o, d, sample_stride=16, threads=0):
     rays = n_sample * scale
     cores = threads if threads > 0 else (os.cpu_count() or 1)
     return {"value": rays / step_s / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
-            "sample": f"full CPU build with the reference's creators ({t_build * 1e3:.0f} ms) + every "
+            "sample": f"full CPU build, same parameters as the GPU arm ({t_build * 1e3:.0f} ms) + every "
                       f"{sample_stride}th primary ray and its shadow ray ({t_trace * 1e3:.0f} ms), extrapolated "
                       f"to the frame",
             "build_ms": t_build * 1e3}
@@ -401,9 +402,31 @@ def run_frame(args, world, rank, local, pg):
         e2e = {"value": rays_per_step * world / (e2e_ms / 1e3) / 1e6, "unit": "Mrays/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
 
+    # The other build configuration on the same inputs, for context.
+    variant = None
+    if graph is not None and not args.profile:
+        alt_kw, alt_desc = (BUILD, BUILD_DESC) if args.build == "tuned" else (BUILD_TUNED, BUILD_TUNED_DESC)
+        alt_bp = kdgb.build_params(**alt_kw)
+        alt_tree = kdgb.KDTree.build(tris_d, alt_bp)
+        alt_graph = kdgb.Graph(alt_tree, tris_d, params=alt_bp, headroom=HEADROOM)
+
+        def alt_step():
+            alt_graph.launch()
+            alt_tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
+
+        time_steps(alt_step, 3, stream)
+        alt_ms = statistics.median(time_steps(alt_step, args.steps, stream, flush))
+        kdgb.check(alt_graph.status(), "graph rebuild")
+        alt_rays = n + int((outs[0] >= 0).sum().item())  # primary + one shadow ray per hit
+        alt_st = alt_tree.stats()
+        variant = {"build": alt_desc, "ms_per_step": alt_ms, "value": alt_rays / (alt_ms / 1e3) / 1e6,
+                   "tree": {"nodes": alt_st.n_nodes, "refs": alt_st.n_refs}}
+        alt_graph.close()
+        alt_tree.close()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(tris, o, d)
+        cpu = cpu_baseline(tris, o, d, build_kw)
 
     if rank == 0:
         line = {"metric": "kd traversal Mrays/s per frame (1M-tri build + primary + shadow)", "value": value,
@@ -421,7 +444,7 @@ def run_frame(args, world, rank, local, pg):
                 "tree": {"nodes": st.n_nodes, "refs": st.n_refs, "upper_levels": st.upper_levels,
                          "lower_levels": st.lower_levels},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clocks}
+                "clocks": clocks, "other_build": variant}
         print(json.dumps(line), flush=True)
     if graph is not None:
         graph.close()

@@ -51,6 +51,9 @@ constexpr int kChunk = 32 * kRows;  // references per warp chunk
 constexpr int kWarps = kBlock / 32;
 constexpr int kTileRefs = kChunk * kWarps;  // references per block tile
 constexpr int kLanes = 7;                   // per-node scan lanes (see k_node_lanes)
+// Tuned levels: nodes with at least this many references are binned by a
+// whole block (k_sah_block), smaller ones by one warp (k_sah_warp).
+constexpr int kSahBlockRefs = 2048;
 constexpr unsigned kFull = 0xffffffffu;
 
 __host__ __device__ inline int64_t chunks_for(int64_t n) { return (n + kChunk - 1) / kChunk; }
@@ -99,7 +102,7 @@ struct BuildArgs {
     int32_t *prim_indices, *leaf_ids;
     float4 *pmin, *pmax;
     unsigned *keys;
-    int32_t *cnt, *lanes, *lbase, *chunksum, *chunkoff;
+    int32_t *cnt, *lanes, *lbase, *chunksum, *chunkoff, *big;
     int8_t *planes;
     int2 *ranges;
     int32_t *roff;
@@ -356,7 +359,7 @@ __global__ void k_node_split(const BuildArgs a)
 {
     const BuildState *st = a.st;
     const int32_t R = st->R, active = st->active;
-    const bool ess = do_ess(a, st);
+    const bool ess = do_ess(a, st), sah = sah_level(a, st);
     const float thr = a.thr;
     GRID_STRIDE(k64, R) {
         const int32_t k = (int32_t)k64;
@@ -390,6 +393,7 @@ __global__ void k_node_split(const BuildArgs a)
         const bool z_higher = mxs < sz;
         a.split[active + k] = z_higher ? mdz : sp;
         a.info[active + k] = z_higher ? (int8_t)KDGB_Z : ax;
+        if (sah && a.amt[active + k] >= kSahBlockRefs) a.big[atomicAdd(&a.st->n_big, 1)] = k;
     }
 }
 
@@ -531,18 +535,18 @@ __device__ __forceinline__ int sah_bin(float x, float mn, float scale, int B)
     return b < 0 ? 0 : (b > B - 1 ? B - 1 : b);
 }
 
-// Nodes with at least this many references are binned by a whole block,
-// smaller ones by one warp.
-constexpr int kSahBlockRefs = 2048;
 
 // Bins the references [first, first + cnt) of one node into h[(axis * 2 +
-// side) * 32 + bin] (shared memory, zeroed by the caller); threads `tid` of
-// `nthreads` share the range.
+// side) * 32 + bin] (shared memory, zeroed by the caller).  A warp walks the
+// range in rows of 32 references, `warps` warps interleaved (warp `wid`
+// takes rows wid, wid + warps, ...), with one shared atomic per reference,
+// axis and side (cheaper here than merging equal bins with match_any).
 __device__ __forceinline__ void sah_fill(const float4 *__restrict__ cmin, const float4 *__restrict__ cmax,
                                          int64_t first, int32_t cnt, const float (&lo)[3], const float (&scale)[3],
-                                         const bool (&valid)[3], int B, int *h, int tid, int nthreads)
+                                         const bool (&valid)[3], int B, int *h, int wid, int warps)
 {
-    for (int32_t i = tid; i < cnt; i += nthreads) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t i = wid * 32 + lane; i < cnt; i += warps * 32) {
         const float4 p = cmin[first + i], q = cmax[first + i];
         const float pv[3] = {p.x, p.y, p.z}, qv[3] = {q.x, q.y, q.z};
 #pragma unroll
@@ -649,32 +653,38 @@ __global__ void __launch_bounds__(kBlock) k_sah_warp(const BuildArgs a)
         const SahNode n = sah_node(a, node);
         for (int j = lane; j < 6 * 32; j += 32) h[j] = 0;
         __syncwarp();
-        sah_fill(a.rmin[cur], a.rmax[cur], n.first, n.cnt, n.mnv, n.scale, n.valid, a.B, h, lane, 32);
+        sah_fill(a.rmin[cur], a.rmax[cur], n.first, n.cnt, n.mnv, n.scale, n.valid, a.B, h, 0, 1);
         __syncwarp();
         sah_pick(a, node, n.cnt, n.mnv, n.mxv, n.ext, h, lane);
         __syncwarp();
     }
 }
 
-// The same for nodes of kSahBlockRefs references or more: one block per node.
+// The same for nodes of kSahBlockRefs references or more: one block per node,
+// a private histogram per warp, summed before the plane search.
 __global__ void __launch_bounds__(kBlock) k_sah_block(const BuildArgs a)
 {
-    __shared__ int s_hist[6 * 32];
+    __shared__ int s_hist[kWarps][6 * 32];
     const BuildState *st = a.st;
     if (!sah_level(a, st)) return;
-    const int32_t R = st->R, active = st->active;
+    const int32_t nb = st->n_big, active = st->active;
     const int cur = st->level & 1;
-    const int lane = threadIdx.x & 31;
-    for (int32_t k = blockIdx.x; k < R; k += gridDim.x) {
-        const int32_t node = active + k;
-        if (a.amt[node] < kSahBlockRefs) continue;  // block-uniform
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int32_t k = blockIdx.x; k < nb; k += gridDim.x) {
+        const int32_t node = active + a.big[k];
         const SahNode n = sah_node(a, node);
-        for (int j = threadIdx.x; j < 6 * 32; j += blockDim.x) s_hist[j] = 0;
+        for (int j = lane; j < 6 * 32; j += 32) s_hist[warp][j] = 0;
+        __syncwarp();
+        sah_fill(a.rmin[cur], a.rmax[cur], n.first, n.cnt, n.mnv, n.scale, n.valid, a.B, s_hist[warp], warp, kWarps);
         __syncthreads();
-        sah_fill(a.rmin[cur], a.rmax[cur], n.first, n.cnt, n.mnv, n.scale, n.valid, a.B, s_hist, threadIdx.x,
-                 blockDim.x);
+        if (threadIdx.x < 6 * 32) {
+            int sum = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) sum += s_hist[w][threadIdx.x];
+            s_hist[0][threadIdx.x] = sum;
+        }
         __syncthreads();
-        if (threadIdx.x < 32) sah_pick(a, node, n.cnt, n.mnv, n.mxv, n.ext, s_hist, lane);
+        if (warp == 0) sah_pick(a, node, n.cnt, n.mnv, n.mxv, n.ext, s_hist[0], lane);
         __syncthreads();
     }
 }
@@ -957,6 +967,7 @@ __global__ void k_advance(const BuildArgs a)
         st->active = st->n_nodes - created;
         st->R = created;
         st->level += 1;
+        st->n_big = 0;
         if (created > 0 && st->level >= a.max_levels) { set_err(st, KDGB_ERR_DEGENERATE, kErrMaxLevels); break; }
         more = created > 0;
     } while (0);
@@ -1173,6 +1184,8 @@ __global__ void k_calc_sah(const BuildArgs a)
                                {(unsigned)sy.x & bmp, (unsigned)sy.y & bmp, (unsigned)sy.z & bmp, (unsigned)sy.w & bmp},
                                {(unsigned)sz.x & bmp, (unsigned)sz.y & bmp, (unsigned)sz.z & bmp, (unsigned)sz.w & bmp}};
         float ar[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+        // Only members are added (predicated adds): skipping a +0 term is
+        // exact, so the sums equal the reference's bit-order accumulation.
         for (unsigned bits = bmp; bits; bits &= bits - 1u) {  // bmp is warp-uniform
             const int j = __ffs(bits) - 1;
             const float aj = __shfl_sync(kFull, a_lane, j);
@@ -1180,7 +1193,8 @@ __global__ void k_calc_sah(const BuildArgs a)
 #pragma unroll
             for (int x = 0; x < 3; ++x)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) ar[x][c] = __fadd_rn(ar[x][c], (sets[x][c] & m) ? aj : 0.0f);
+                for (int c = 0; c < 4; ++c)
+                    if (sets[x][c] & m) ar[x][c] = __fadd_rn(ar[x][c], aj);
         }
         pick_planes(sets[0], ar[0], KDGB_X, pi + lane, mb);
         pick_planes(sets[1], ar[1], KDGB_Y, pi + lane, mb);
@@ -1481,6 +1495,7 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.cap.R = std::min({w.pmin.cap, w.pmax.cap, w.keys.cap / 6, w.cnt.cap / 2});
     a.chunksum = w.chunksum.p;
     a.chunkoff = w.chunkoff.p;
+    a.big = w.big.p;
     a.ranges = w.ranges.p;
     a.roff = w.roff.p;
     a.cap.ranges = std::min(w.ranges.cap, w.roff.cap);
@@ -1702,7 +1717,7 @@ uint64_t layout_signature(const Tree &t)
     MIX(t.tnode); MIX(t.ttri); MIX(t.mesh_off);
     MIX(w.rmin[0]); MIX(w.rmin[1]); MIX(w.rmax[0]); MIX(w.rmax[1]); MIX(w.fmin); MIX(w.fmax); MIX(w.pmin);
     MIX(w.pmax); MIX(w.keys); MIX(w.planes); MIX(w.cnt); MIX(w.lanes); MIX(w.lbase); MIX(w.chunksum);
-    MIX(w.chunkoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.areas); MIX(w.sts);
+    MIX(w.chunkoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.big); MIX(w.areas); MIX(w.sts);
     MIX(w.ssplit); MIX(w.saddr); MIX(w.roff); MIX(w.careas); MIX(w.csets); MIX(w.ranges); MIX(w.state);
 #undef MIX
     return h;
@@ -1820,6 +1835,7 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
         KDGB_CHECK(grab(w.planes, R, s));
         KDGB_CHECK(grab(w.chunksum, 2 * chunks_for(N), s));
         KDGB_CHECK(grab(w.chunkoff, 2 * (chunks_for(N) + 1), s));
+        KDGB_CHECK(grab(w.big, std::min<int64_t>(R, N / kSahBlockRefs) + 1, s));
         const Extents e{N, R, F, n_nodes, 0, 0};
         KDGB_CHECK(emit_upper_level(make_args(t, p, T, M, mesh_off_dev), L, e, tuned_level, w, s));
         KDGB_CHECK(fetch_state(t, st, s));
@@ -1912,6 +1928,7 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.planes, R, s));
     KDGB_CHECK(ensure(w.chunksum, 2 * chunks_for(refs), s));
     KDGB_CHECK(ensure(w.chunkoff, 2 * (chunks_for(refs) + 1), s));
+    KDGB_CHECK(ensure(w.big, refs / kSahBlockRefs + 1, s));
     KDGB_CHECK(ensure(w.ranges, (int64_t)p.max_levels + 1, s));
     KDGB_CHECK(ensure(w.roff, (int64_t)p.max_levels + 1, s));
     KDGB_CHECK(ensure(t.leaf_ids, leaves, s));

@@ -88,7 +88,7 @@ struct BuildState {
     int32_t low_levels;   // SAH lower levels completed
     int32_t low_first;    // 1 while the lower level is the upper leaves
     int32_t n_leaf_tris;  // leaf records of the traversal layout
-    int32_t pad;
+    int32_t n_big;        // tuned levels: active nodes listed for block-wide SAH binning
 };
 
 // Sizes seen by the last host-driven build of a handle; a graph rebuild
@@ -111,7 +111,7 @@ struct Workspace {
     DevArray<float4> rmin[2], rmax[2], fmin, fmax, pmin, pmax;
     DevArray<unsigned> keys;
     DevArray<int8_t> planes;
-    DevArray<int32_t> cnt, lanes, lbase, chunksum, chunkoff, stats, scan, misc0, misc1, hist;
+    DevArray<int32_t> cnt, lanes, lbase, chunksum, chunkoff, stats, scan, misc0, misc1, big;
     DevArray<float> areas;
     DevArray<int4> sts;
     DevArray<int32_t> ssplit, saddr, roff;

@@ -43,18 +43,32 @@ struct Ctx {
     int root;  // root node of the ray's tree (forest of a batch: its mesh index)
 };
 
-// Moeller-Trumbore on one packed record (IRayTracer.h:111-145).
+// True when x = RN(RN(1/det) * n) is certainly negative and nonzero:
+// det and n have opposite signs, n != 0, and |det| <= 2^64, |n| >= 2^-64 so
+// the product cannot round to -0 (a -0 would pass the `>= 0` tests).
+// det = +-0 gives +-inf, whose product with n is negative as well.
+__device__ __forceinline__ bool surely_negative(float det, float n)
+{
+    return n != 0.0f && (signbit(det) != signbit(n)) && fabsf(det) <= 0x1p64f && fabsf(n) >= 0x1p-64f;
+}
+
+// Moeller-Trumbore on one packed record (IRayTracer.h:111-145).  Triangles
+// whose u or v is certainly negative are rejected before the IEEE
+// reciprocal; every accepted value is computed exactly as the reference does.
 __device__ __forceinline__ void mt_test(float3 v0, float3 e1, float3 e2, int id, float3 o, float3 d, int tie,
                                         int &hit, float &tb, float &ub, float &vb)
 {
     const float3 p = cross3(d, e2);
     const float3 t = sub3(o, v0);
     const float3 q = cross3(t, e1);
-    const float inv_det = __frcp_rn(dot3(p, e1));
+    const float det = dot3(p, e1);
+    const float pt = dot3(p, t), qd = dot3(q, d);
+    if (surely_negative(det, pt) || surely_negative(det, qd)) return;
+    const float inv_det = __frcp_rn(det);
     const float ht = __fmul_rn(inv_det, dot3(q, e2));
     if (0.0f <= ht && ht <= tb) {
-        const float hu = __fmul_rn(inv_det, dot3(p, t));
-        const float hv = __fmul_rn(inv_det, dot3(q, d));
+        const float hu = __fmul_rn(inv_det, pt);
+        const float hv = __fmul_rn(inv_det, qd);
         if (hu >= 0.0f && hv >= 0.0f && __fadd_rn(hu, hv) <= 1.0f) {
             if (tie == KDGB_TIE_REF_LAST || hit == -1 || ht < tb || id < hit) {
                 hit = id; tb = ht; ub = hu; vb = hv;
@@ -143,6 +157,17 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
     float3 d = adjust_dir(din);
     float th = 0.0f;
     int iters = 0;
+    // The reference inverts d before each descent and back after it, so d
+    // becomes rcp(rcp(d)) after the first iteration.  When
+    // rcp(rcp(rcp(d))) == rcp(d) the sequence is at its fixed point from
+    // then on: every descent and slab test uses inv1 = rcp(d) and every
+    // triangle test d1 = rcp(inv1).  That holds for all finite nonzero
+    // floats except six values next to FLT_MAX (checked exhaustively); it is
+    // tested per ray, and rays that miss it take the reference's loop.
+    const float3 inv1 = inv3(d), d1 = inv3(inv1), inv2 = inv3(d1);
+    const bool fixed = __float_as_uint(inv2.x) == __float_as_uint(inv1.x) &&
+                       __float_as_uint(inv2.y) == __float_as_uint(inv1.y) &&
+                       __float_as_uint(inv2.z) == __float_as_uint(inv1.z);
     do {
         int node;
         float tnext;
@@ -157,7 +182,7 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
             tnext = __int_as_float(e.y);
         }
         int4 nd = __ldg(c.node + node);
-        d = inv3(d);
+        d = fixed ? inv1 : inv3(d);
         while (nd.w != KDGB_LEAF) {
             const float ori = axis_of(o, nd.w), dir = axis_of(d, nd.w);
             const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
@@ -176,9 +201,9 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
             }
             nd = __ldg(c.node + node);
         }
-        d = inv3(d);
+        d = fixed ? d1 : inv3(d);
         th = __fmul_rn(tnext, 1.00001f);
-        if (!SKIP || ray_box(o, inv3(d), __ldg(c.bmin + node), __ldg(c.bmax + node))) {
+        if (!SKIP || ray_box(o, fixed ? inv1 : inv3(d), __ldg(c.bmin + node), __ldg(c.bmax + node))) {
             float tb = th, ub = 0.0f, vb = 0.0f;
             const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
             if (h != -1) { t = tb; u = ub; v = vb; return h; }
