@@ -14,8 +14,8 @@
 //    seven-lane node scan, and a reference's destination is its node base
 //    plus its rank inside the node (ballot scan + chunk offset), which equals
 //    the reference's 2N+1-element scans (TriangleMapUpperCreator.cu:557,631);
-//  * every size lives in a device-resident BuildState that single-thread
-//    advance kernels update at the end of each level, and every kernel
+//  * every size lives in a device-resident BuildState that the last block of
+//    each level's closing kernel updates, and every kernel
 //    loops over the counts it reads there.  The host-driven build reads the
 //    state once per level to size buffers and grids exactly; the graph build
 //    (capture_build) records the same launch sequence once, with fixed
@@ -50,7 +50,7 @@ constexpr int kRows = 4;
 constexpr int kChunk = 32 * kRows;  // references per warp chunk
 constexpr int kWarps = kBlock / 32;
 constexpr int kTileRefs = kChunk * kWarps;  // references per block tile
-constexpr int kLanes = 7;                   // per-node scan lanes (see k_node_lanes)
+constexpr int kLanes = 7;                   // per-node scan lanes (see NodeLanes)
 // Tuned levels: nodes with at least this many references are binned by a
 // whole block (k_sah_block), smaller ones by one warp (k_sah_warp).
 constexpr int kSahBlockRefs = 2048;
@@ -102,7 +102,7 @@ struct BuildArgs {
     int32_t *prim_indices, *leaf_ids;
     float4 *pmin, *pmax;
     unsigned *keys;
-    int32_t *cnt, *lanes, *lbase, *chunksum, *chunkoff, *big;
+    int32_t *cnt, *ess_cnt, *lbase, *chunksum, *tilesum, *tileoff, *big;
     int8_t *planes;
     int2 *ranges;
     int32_t *roff;
@@ -233,7 +233,7 @@ __global__ void k_begin(const BuildArgs a)
         s.N = a.T;
         s.R = a.M;
         s.n_nodes = a.M;
-        s.nch = (int32_t)chunks_for(a.T);
+        s.ntiles = (int32_t)ceil_div(a.T, kTileRefs);
         *st = s;
     }
 }
@@ -378,9 +378,9 @@ __global__ void k_node_split(const BuildArgs a)
             if (__fsub_rn(hi.y, mx.y) > __fmul_rn(thr, __fsub_rn(hi.y, lo.y))) { pl |= 16; nr += 2; }
             if (__fsub_rn(hi.z, mx.z) > __fmul_rn(thr, __fsub_rn(hi.z, lo.z))) { pl |= 32; nr += 2; }
             a.planes[k] = (int8_t)pl;
-            a.lanes[kLanes * (int64_t)k + 6] = nr;
+            a.ess_cnt[k] = nr;
         } else {
-            a.lanes[kLanes * (int64_t)k + 6] = 0;
+            a.ess_cnt[k] = 0;
         }
         const float sx = __fsub_rn(mx.x, mn.x), sy = __fsub_rn(mx.y, mn.y), sz = __fsub_rn(mx.z, mn.z);
         const float mdx = __fadd_rn(__fmul_rn(sx, 0.5f), mn.x);
@@ -405,11 +405,12 @@ __device__ __forceinline__ void ref_flags(const float4 &lo, const float4 &hi, in
     Rf = sp < axis_of4(hi, axis);
 }
 
-// Per-node left/right counts and per-chunk totals of the flags (the chunk
-// totals are scanned into each warp chunk's global offsets for k_scatter).
+// Per-node left/right counts, per-chunk totals of the flags and per-tile
+// totals (the tile totals are scanned into tile offsets; k_scatter adds the
+// chunk totals of the earlier warps of its tile).
 __global__ void __launch_bounds__(kBlock) k_count(const BuildArgs a)
 {
-    __shared__ int s_owner[kWarps], s_l[kWarps], s_r[kWarps];
+    __shared__ int s_owner[kWarps], s_l[kWarps], s_r[kWarps], s_tl[kWarps], s_tr[kWarps];
     const BuildState *st = a.st;
     const int64_t N = st->N;
     const int32_t active = st->active;
@@ -481,8 +482,16 @@ __global__ void __launch_bounds__(kBlock) k_count(const BuildArgs a)
             s_owner[warp] = cw;
             s_l[warp] = al;
             s_r[warp] = ar;
+            s_tl[warp] = tl;
+            s_tr[warp] = tr;
         }
         __syncthreads();
+        if (threadIdx.x == 32) {
+            int sl = 0, sr = 0;
+            for (int w = 0; w < kWarps; ++w) { sl += s_tl[w]; sr += s_tr[w]; }
+            a.tilesum[2 * tile] = sl;
+            a.tilesum[2 * tile + 1] = sr;
+        }
         if (threadIdx.x == 0) {
             // Consecutive warps cover consecutive chunks: merge equal owners.
             int o = -1, l = 0, r = 0;
@@ -499,21 +508,6 @@ __global__ void __launch_bounds__(kBlock) k_count(const BuildArgs a)
             if (o >= 0) { atomicAdd(cnt + 2 * o, l); atomicAdd(cnt + 2 * o + 1, r); }
         }
         __syncthreads();
-    }
-}
-
-// Seven scan lanes per node: left/right sizes, left/right references that go
-// to leaves, the left/right leaf-node flags (CalcNodeChildSize,
-// SetPrimitiveLeafSide, MarkNodeLeafs: TriangleUpperChildren.h:144-201) and
-// the empty-space node count written by k_node_split.
-__global__ void k_node_lanes(const BuildArgs a)
-{
-    const int32_t R = a.st->R, LS = a.LS;
-    GRID_STRIDE(k, R) {
-        const int32_t l = a.cnt[2 * k], r = a.cnt[2 * k + 1];
-        const int ll = l < LS, rl = r < LS;
-        int32_t *o = a.lanes + kLanes * k;
-        o[0] = l; o[1] = r; o[2] = ll ? l : 0; o[3] = rl ? r : 0; o[4] = ll; o[5] = rl;
     }
 }
 
@@ -752,11 +746,14 @@ __device__ __forceinline__ void scatter_one(const BuildArgs &a, int32_t R, int o
 
 // Partition + compaction of the references with clipping to the split plane
 // (SplitTriangles, TriangleUpperChildren.h:283-383).  Destination = node base
-// + rank of the reference among the node's left (right) references.
+// + rank of the reference among the node's left (right) references; a warp's
+// first rank is its tile's offset plus the chunk totals of the tile's earlier
+// warps.
 __global__ void __launch_bounds__(kBlock) k_scatter(const BuildArgs a)
 {
+    __shared__ int32_t s_off[kWarps][2];
     const BuildState *st = a.st;
-    if (!level_fits(a, st, node_totals(a, st))) return;  // k_advance records the failure
+    if (!level_fits(a, st, node_totals(a, st))) return;  // advance_upper records the failure
     const int64_t N = st->N;
     const int32_t R = st->R, active = st->active, upper = (int32_t)st->F;
     const int cur = st->level & 1;
@@ -764,11 +761,28 @@ __global__ void __launch_bounds__(kBlock) k_scatter(const BuildArgs a)
     const float4 *__restrict__ cmax = a.rmax[cur];
     float4 *__restrict__ nmin = a.rmin[cur ^ 1];
     float4 *__restrict__ nmax = a.rmax[cur ^ 1];
-    const unsigned lane = threadIdx.x & 31;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
-    WARP_STRIDE(chunk, chunks_for(N)) {
+    const int64_t ntiles = ceil_div(N, kTileRefs);
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (threadIdx.x == 0) {
+            int32_t ol = a.tileoff[2 * tile], orr = a.tileoff[2 * tile + 1];
+            for (int w = 0; w < kWarps; ++w) {
+                s_off[w][0] = ol;
+                s_off[w][1] = orr;
+                const int64_t ch = tile * kWarps + w;
+                if (ch * kChunk < N) {
+                    ol += a.chunksum[2 * ch];
+                    orr += a.chunksum[2 * ch + 1];
+                }
+            }
+        }
+        __syncthreads();
+        const int64_t chunk = tile * kWarps + warp;
         const int64_t base = chunk * kChunk;
-        int32_t off_l = a.chunkoff[2 * chunk], off_r = a.chunkoff[2 * chunk + 1];
+        int32_t off_l = s_off[warp][0], off_r = s_off[warp][1];
+        __syncthreads();  // s_off is rewritten by the next tile
+        if (base >= N) continue;  // warp-uniform
         float4 ra[kRows], rb[kRows];
 #pragma unroll
         for (int row = 0; row < kRows; ++row) {
@@ -850,6 +864,63 @@ __device__ __forceinline__ void ess_chain(const BuildArgs &a, int32_t k, int32_t
     }
 }
 
+// Called by every thread at the end of a level-closing kernel: true in one
+// thread of the block that finishes last (all other blocks are done with the
+// state then), which also resets the counter for the next level.
+__device__ __forceinline__ bool last_block(BuildState *st)
+{
+    __shared__ bool s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&st->done, 1) == (int)gridDim.x - 1;
+        if (s_last) st->done = 0;
+    }
+    __syncthreads();
+    return s_last && threadIdx.x == 0;
+}
+
+// End of an upper level (run by one thread of the level's last block):
+// records the level's leaf range, advances the counters to the next level
+// and decides whether the loop continues.
+__device__ void advance_upper(const BuildArgs &a, BuildState *st)
+{
+    int more = 0;
+    do {
+        if (st->err) break;
+        if (st->nonfinite) { set_err(st, KDGB_ERR_NONFINITE, kErrNonfinite); break; }
+        const int32_t R = st->R;
+        const int32_t *tot = node_totals(a, st);
+        if (!level_fits(a, st, tot)) { set_err(st, KDGB_ERR_CAPACITY, kErrUpperCapacity); break; }
+        const int32_t leaf_nodes = tot[4] + tot[5];
+        if (leaf_nodes > 0 && (st->n_ranges >= a.cap.ranges || (int64_t)st->n_leaf_ids + leaf_nodes > a.cap.leaves)) {
+            set_err(st, KDGB_ERR_CAPACITY, kErrLeafCapacity);
+            break;
+        }
+        const int64_t tl = tot[0], tr = tot[1], ll = tot[2], lr = tot[3];
+        if (tl + tr < st->N) { set_err(st, KDGB_ERR_DEGENERATE, kErrFewerRefs); break; }
+        const int32_t empty = tot[6];
+        if (leaf_nodes > 0) {
+            a.ranges[st->n_ranges] = make_int2(st->n_nodes + empty, leaf_nodes);
+            a.roff[st->n_ranges] = st->n_leaf_ids;
+            st->n_ranges += 1;
+            st->n_leaf_ids += leaf_nodes;
+        }
+        st->n_nodes += empty + 2 * R;
+        st->F += ll + lr;
+        const int32_t created = 2 * R - leaf_nodes;
+        st->N = tl + tr - ll - lr;
+        st->ntiles = (int32_t)ceil_div(st->N, kTileRefs);
+        st->active = st->n_nodes - created;
+        st->R = created;
+        st->level += 1;
+        st->n_big = 0;
+        if (created > 0 && st->level >= a.max_levels) { set_err(st, KDGB_ERR_DEGENERATE, kErrMaxLevels); break; }
+        more = created > 0;
+    } while (0);
+    if (a.use_cond) cudaGraphSetConditional(a.upper_cond, more ? 1u : 0u);
+}
+
 // CreateUpperChildren (TriangleUpperChildren.h:203-281), the empty-space
 // chain of EmptySpaceSplitting2 (its nodes come first, at base + lane-6
 // offsets) and, with empty-space splitting on, PropagateAabbToChildren
@@ -857,13 +928,15 @@ __device__ __forceinline__ void ess_chain(const BuildArgs &a, int32_t k, int32_t
 // it whenever empty-space splitting is on, whatever propagateAabbs says).  Non-leaf children are the next level's
 // active nodes: their tight-box keys, counts and propagated boxes are reset
 // here (AabbMemset, ReduceSegments.h:328-335) so the next level needs no
-// separate init launch.
+// separate init launch.  The block that finishes last closes the level
+// (advance_upper).
 __global__ void k_children(const BuildArgs a)
 {
-    const BuildState *st = a.st;
+    BuildState *st = a.st;
     const int32_t *tot = node_totals(a, st);
-    if (!level_fits(a, st, tot)) return;  // k_advance records the failure
-    const int32_t R = st->R, active = st->active, base = st->n_nodes, upper = (int32_t)st->F, LS = a.LS;
+    const bool fits = level_fits(a, st, tot);  // when not, advance_upper records the failure
+    const int32_t R = fits ? st->R : 0, active = st->active, base = st->n_nodes, upper = (int32_t)st->F;
+    const int32_t LS = a.LS;
     const bool ess = do_ess(a, st);
     const int32_t empty = tot[6];
     const int32_t child_start = base + empty;
@@ -931,47 +1004,7 @@ __global__ void k_children(const BuildArgs a)
             a.pmax[rnext] = rmax;
         }
     }
-}
-
-// End of an upper level: records the level's leaf range, advances the
-// counters to the next level and decides whether the loop continues.
-__global__ void k_advance(const BuildArgs a)
-{
-    BuildState *st = a.st;
-    int more = 0;
-    do {
-        if (st->err) break;
-        if (st->nonfinite) { set_err(st, KDGB_ERR_NONFINITE, kErrNonfinite); break; }
-        const int32_t R = st->R;
-        const int32_t *tot = node_totals(a, st);
-        if (!level_fits(a, st, tot)) { set_err(st, KDGB_ERR_CAPACITY, kErrUpperCapacity); break; }
-        const int32_t leaf_nodes = tot[4] + tot[5];
-        if (leaf_nodes > 0 && (st->n_ranges >= a.cap.ranges || (int64_t)st->n_leaf_ids + leaf_nodes > a.cap.leaves)) {
-            set_err(st, KDGB_ERR_CAPACITY, kErrLeafCapacity);
-            break;
-        }
-        const int64_t tl = tot[0], tr = tot[1], ll = tot[2], lr = tot[3];
-        if (tl + tr < st->N) { set_err(st, KDGB_ERR_DEGENERATE, kErrFewerRefs); break; }
-        const int32_t empty = tot[6];
-        if (leaf_nodes > 0) {
-            a.ranges[st->n_ranges] = make_int2(st->n_nodes + empty, leaf_nodes);
-            a.roff[st->n_ranges] = st->n_leaf_ids;
-            st->n_ranges += 1;
-            st->n_leaf_ids += leaf_nodes;
-        }
-        st->n_nodes += empty + 2 * R;
-        st->F += ll + lr;
-        const int32_t created = 2 * R - leaf_nodes;
-        st->N = tl + tr - ll - lr;
-        st->nch = (int32_t)chunks_for(st->N);
-        st->active = st->n_nodes - created;
-        st->R = created;
-        st->level += 1;
-        st->n_big = 0;
-        if (created > 0 && st->level >= a.max_levels) { set_err(st, KDGB_ERR_DEGENERATE, kErrMaxLevels); break; }
-        more = created > 0;
-    } while (0);
-    if (a.use_cond) cudaGraphSetConditional(a.upper_cond, more ? 1u : 0u);
+    if (last_block(st)) advance_upper(a, st);
 }
 
 // MarkLeafNodes (TriangleUpperChildren.h:385-395) over all levels at once:
@@ -1231,15 +1264,38 @@ __device__ __forceinline__ bool lower_fits(const BuildArgs &a, const BuildState 
     return (int64_t)st->n_nodes + 2 * (int64_t)splits <= a.cap.nodes;
 }
 
+// End of a SAH lower level (one thread of the level's last block).
+__device__ void advance_lower(const BuildArgs &a, BuildState *st)
+{
+    int more = 0;
+    do {
+        if (st->err) break;
+        const int32_t R = st->low_R;
+        if (R == 0) break;
+        const int32_t splits = a.saddr[R];
+        if (!lower_fits(a, st, splits) || 2 * (int64_t)splits > a.cap.low_R) {
+            set_err(st, KDGB_ERR_CAPACITY, kErrLowerCapacity);
+            break;
+        }
+        st->low_levels += 1;
+        st->n_nodes += 2 * splits;
+        st->low_active = st->n_nodes - 2 * splits;
+        st->low_R = 2 * splits;
+        st->low_first = 0;
+        more = splits > 0;
+    } while (0);
+    if (a.use_cond) cudaGraphSetConditional(a.lower_cond, more ? 1u : 0u);
+}
+
 // CreateLowerSAHChildren (LowerTriangleMap.h:557-600) and, when enabled,
 // PropagateAabbToChildren (LowerTriangleMap.h:602-636).
 __global__ void k_sah_children(const BuildArgs a)
 {
-    const BuildState *st = a.st;
-    if (st->err) return;
-    const int32_t R = st->low_R;
-    const int32_t splits = a.saddr[R];
-    if (!lower_fits(a, st, splits)) return;  // k_lower_advance records the failure
+    BuildState *st = a.st;
+    const int32_t splits = a.saddr[st->low_R];
+    // After a failure, or when the children do not fit (advance_lower
+    // records that), no block writes.
+    const int32_t R = (st->err || !lower_fits(a, st, splits)) ? 0 : st->low_R;
     const int32_t *__restrict__ ids = st->low_first ? a.leaf_ids : nullptr;
     const int32_t active = st->low_active, child_base = st->n_nodes;
     GRID_STRIDE(k64, R) {
@@ -1266,29 +1322,7 @@ __global__ void k_sah_children(const BuildArgs a)
             a.bmax[r] = mx;
         }
     }
-}
-
-__global__ void k_lower_advance(const BuildArgs a)
-{
-    BuildState *st = a.st;
-    int more = 0;
-    do {
-        if (st->err) break;
-        const int32_t R = st->low_R;
-        if (R == 0) break;
-        const int32_t splits = a.saddr[R];
-        if (!lower_fits(a, st, splits) || 2 * (int64_t)splits > a.cap.low_R) {
-            set_err(st, KDGB_ERR_CAPACITY, kErrLowerCapacity);
-            break;
-        }
-        st->low_levels += 1;
-        st->n_nodes += 2 * splits;
-        st->low_active = st->n_nodes - 2 * splits;
-        st->low_R = 2 * splits;
-        st->low_first = 0;
-        more = splits > 0;
-    } while (0);
-    if (a.use_cond) cudaGraphSetConditional(a.lower_cond, more ? 1u : 0u);
+    if (last_block(st)) advance_lower(a, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -1488,13 +1522,14 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.pmax = w.pmax.p;
     a.keys = w.keys.p;
     a.cnt = w.cnt.p;
-    a.lanes = w.lanes.p;
+    a.ess_cnt = w.ess.p;
     a.lbase = w.lbase.p;
     a.planes = w.planes.p;
     // Next-level node entries are written by k_children into these four.
     a.cap.R = std::min({w.pmin.cap, w.pmax.cap, w.keys.cap / 6, w.cnt.cap / 2});
     a.chunksum = w.chunksum.p;
-    a.chunkoff = w.chunkoff.p;
+    a.tilesum = w.tilesum.p;
+    a.tileoff = w.tileoff.p;
     a.big = w.big.p;
     a.ranges = w.ranges.p;
     a.roff = w.roff.p;
@@ -1531,7 +1566,7 @@ int emit_begin(const BuildArgs &a, const Launcher &L, const float *tri_v_dev, cu
 int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bool tuned_levels, Workspace &w,
                      cudaStream_t s)
 {
-    const unsigned gN = L.grid(e.N, kTileRefs), gW = L.grid(chunks_for(e.N) * 32, kBlock);
+    const unsigned gN = L.grid(e.N, kTileRefs);
     const unsigned gR = L.grid(e.R, kBlock, 2);
     if (e.N > 0) {
         k_reduce<<<gN, kBlock, 0, s>>>(a);
@@ -1550,17 +1585,14 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
         k_count<<<gN, kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
-    KDGB_CHECK(scan_exclusive<2>(a.chunksum, a.chunkoff, chunks_for(e.N), s, &w.scan, &a.st->nch));
-    k_node_lanes<<<gR, kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
-    KDGB_CHECK(scan_exclusive<kLanes>(a.lanes, a.lbase, e.R, s, &w.scan, &a.st->R));
+    KDGB_CHECK(scan_exclusive<2>(a.tilesum, a.tileoff, ceil_div(e.N, kTileRefs), s, &w.scan, &a.st->ntiles));
+    const NodeLanes lanes{a.cnt, a.ess_cnt, a.LS};
+    KDGB_CHECK((scan_exclusive_in<kLanes, NodeLanes>(lanes, a.lbase, e.R, s, &w.scan, &a.st->R)));
     if (e.N > 0) {
-        k_scatter<<<gW, kBlock, 0, s>>>(a);
+        k_scatter<<<gN, kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
     k_children<<<gR, kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
-    k_advance<<<1, 1, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
@@ -1598,8 +1630,6 @@ int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, Wo
     KDGB_LAUNCH_CHECK();
     KDGB_CHECK(scan_exclusive<1>(a.ssplit, a.saddr, e.low_R, s, &w.scan, &a.st->low_R));
     k_sah_children<<<L.grid(e.low_R, kBlock, 2), kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
-    k_lower_advance<<<1, 1, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
@@ -1684,10 +1714,11 @@ void graph_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, const
 {
     Workspace &w = t.ws;
     a = make_args(t, p, T, M, mesh_off);
-    const int64_t chunk_refs = std::min(w.chunksum.cap / 2, w.chunkoff.cap / 2 - 1) * kChunk;
+    const int64_t chunk_refs = std::min({w.chunksum.cap / 2 * kChunk, w.tilesum.cap / 2 * kTileRefs,
+                                         (w.tileoff.cap / 2 - 1) * kTileRefs});
     a.cap.refs[0] = std::min(a.cap.refs[0], chunk_refs);
     a.cap.refs[1] = std::min(a.cap.refs[1], chunk_refs);
-    a.cap.R = std::min({a.cap.R, w.lanes.cap / kLanes, w.lbase.cap / kLanes - 1, w.planes.cap});
+    a.cap.R = std::min({a.cap.R, w.ess.cap, w.lbase.cap / kLanes - 1, w.planes.cap});
     a.cap.leaves = t.leaf_ids.cap;
     a.cap.low_R = std::min({w.ssplit.cap, w.saddr.cap - 1, w.careas.cap, w.csets.cap});
     a.cap.fin = std::min({a.cap.fin, t.prim_indices.cap, w.areas.cap, w.sts.cap / 3});
@@ -1716,8 +1747,8 @@ uint64_t layout_signature(const Tree &t)
     MIX(t.bitmap); MIX(t.parent); MIX(t.children); MIX(t.area); MIX(t.prim_indices); MIX(t.leaf_ids);
     MIX(t.tnode); MIX(t.ttri); MIX(t.mesh_off);
     MIX(w.rmin[0]); MIX(w.rmin[1]); MIX(w.rmax[0]); MIX(w.rmax[1]); MIX(w.fmin); MIX(w.fmax); MIX(w.pmin);
-    MIX(w.pmax); MIX(w.keys); MIX(w.planes); MIX(w.cnt); MIX(w.lanes); MIX(w.lbase); MIX(w.chunksum);
-    MIX(w.chunkoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.big); MIX(w.areas); MIX(w.sts);
+    MIX(w.pmax); MIX(w.keys); MIX(w.planes); MIX(w.cnt); MIX(w.ess); MIX(w.lbase); MIX(w.chunksum);
+    MIX(w.tilesum); MIX(w.tileoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.big); MIX(w.areas); MIX(w.sts);
     MIX(w.ssplit); MIX(w.saddr); MIX(w.roff); MIX(w.careas); MIX(w.csets); MIX(w.ranges); MIX(w.state);
 #undef MIX
     return h;
@@ -1830,11 +1861,12 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
         KDGB_CHECK(reserve_keep(w.pmax, 2 * R, R, s));
         KDGB_CHECK(reserve_keep(w.keys, 12 * R, 6 * R, s));
         KDGB_CHECK(reserve_keep(w.cnt, 4 * R, 2 * R, s));
-        KDGB_CHECK(grab(w.lanes, kLanes * R, s));
+        KDGB_CHECK(grab(w.ess, R, s));
         KDGB_CHECK(grab(w.lbase, kLanes * (R + 1), s));
         KDGB_CHECK(grab(w.planes, R, s));
         KDGB_CHECK(grab(w.chunksum, 2 * chunks_for(N), s));
-        KDGB_CHECK(grab(w.chunkoff, 2 * (chunks_for(N) + 1), s));
+        KDGB_CHECK(grab(w.tilesum, 2 * ceil_div(N, kTileRefs), s));
+        KDGB_CHECK(grab(w.tileoff, 2 * (ceil_div(N, kTileRefs) + 1), s));
         KDGB_CHECK(grab(w.big, std::min<int64_t>(R, N / kSahBlockRefs) + 1, s));
         const Extents e{N, R, F, n_nodes, 0, 0};
         KDGB_CHECK(emit_upper_level(make_args(t, p, T, M, mesh_off_dev), L, e, tuned_level, w, s));
@@ -1923,11 +1955,12 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.pmax, R, s));
     KDGB_CHECK(ensure(w.keys, 6 * R, s));
     KDGB_CHECK(ensure(w.cnt, 2 * R, s));
-    KDGB_CHECK(ensure(w.lanes, kLanes * R, s));
+    KDGB_CHECK(ensure(w.ess, R, s));
     KDGB_CHECK(ensure(w.lbase, kLanes * (R + 1), s));
     KDGB_CHECK(ensure(w.planes, R, s));
     KDGB_CHECK(ensure(w.chunksum, 2 * chunks_for(refs), s));
-    KDGB_CHECK(ensure(w.chunkoff, 2 * (chunks_for(refs) + 1), s));
+    KDGB_CHECK(ensure(w.tilesum, 2 * ceil_div(refs, kTileRefs), s));
+    KDGB_CHECK(ensure(w.tileoff, 2 * (ceil_div(refs, kTileRefs) + 1), s));
     KDGB_CHECK(ensure(w.big, refs / kSahBlockRefs + 1, s));
     KDGB_CHECK(ensure(w.ranges, (int64_t)p.max_levels + 1, s));
     KDGB_CHECK(ensure(w.roff, (int64_t)p.max_levels + 1, s));
@@ -1947,7 +1980,7 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     BuildArgs a;
     Extents e;
     graph_args(t, p, T, M, nullptr, a, e);
-    const int64_t parts = std::max({scan_partials_needed(2, chunks_for(e.N)), scan_partials_needed(kLanes, e.R),
+    const int64_t parts = std::max({scan_partials_needed(2, ceil_div(e.N, kTileRefs)), scan_partials_needed(kLanes, e.R),
                                     scan_partials_needed(1, e.low_R), scan_partials_needed(1, e.nodes),
                                     (int64_t)1});
     KDGB_CHECK(ensure(w.scan, parts, s));

@@ -68,8 +68,8 @@ int grab(DevArray<T> &a, int64_t n, cudaStream_t s)
 // Device-resident counters of a build in progress.  Every build kernel reads
 // its sizes here, so one launch sequence runs either under host control
 // (exact grids, one readback per level) or captured once into a CUDA graph
-// whose level loops are conditional WHILE nodes.  Only the single-thread
-// advance kernels write it.
+// whose level loops are conditional WHILE nodes.  Only one thread of the
+// block that finishes a level last writes it (advance_upper/advance_lower).
 struct BuildState {
     int64_t N;            // references of the current upper level
     int64_t F;            // leaf references written so far
@@ -77,7 +77,7 @@ struct BuildState {
     int32_t active;       // id of the first active node
     int32_t n_nodes;      // nodes written so far
     int32_t level;        // upper levels completed
-    int32_t nch;          // warp chunks covering the N references
+    int32_t ntiles;       // block tiles (kTileRefs references) covering the N references
     int32_t n_leaf_ids;   // upper leaves so far
     int32_t n_ranges;     // upper levels that produced leaves
     int32_t err;          // first failure (a kdgb_status), 0 while healthy
@@ -89,6 +89,8 @@ struct BuildState {
     int32_t low_first;    // 1 while the lower level is the upper leaves
     int32_t n_leaf_tris;  // leaf records of the traversal layout
     int32_t n_big;        // tuned levels: active nodes listed for block-wide SAH binning
+    int32_t done;         // blocks of the current level-closing kernel that have finished
+    int32_t pad;
 };
 
 // Sizes seen by the last host-driven build of a handle; a graph rebuild
@@ -111,7 +113,7 @@ struct Workspace {
     DevArray<float4> rmin[2], rmax[2], fmin, fmax, pmin, pmax;
     DevArray<unsigned> keys;
     DevArray<int8_t> planes;
-    DevArray<int32_t> cnt, lanes, lbase, chunksum, chunkoff, stats, scan, misc0, misc1, big;
+    DevArray<int32_t> cnt, ess, lbase, chunksum, tilesum, tileoff, stats, scan, misc0, misc1, big;
     DevArray<float> areas;
     DevArray<int4> sts;
     DevArray<int32_t> ssplit, saddr, roff;
@@ -179,14 +181,54 @@ int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s);
 // current (kdgb_tree_upload).
 int pack_for_traversal(Tree &t, cudaStream_t s);
 
+// Scan inputs: a loader fills the K lanes of record r.
+template <int K>
+struct ScanArray {
+    const int32_t *in;  // n records of K consecutive ints
+#ifdef __CUDACC__
+    __device__ __forceinline__ void load(int64_t r, int32_t (&v)[K]) const
+    {
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = in[r * K + k];
+    }
+#endif
+};
+
+// The seven per-node lanes of an upper level, computed from the node's
+// left/right reference counts and its empty-space node count (see
+// k_count and k_node_split): left, right, left references that go to a leaf,
+// right references that go to a leaf, left-is-leaf, right-is-leaf, empty-space
+// nodes (CalcNodeChildSize, SetPrimitiveLeafSide, MarkNodeLeafs:
+// TriangleUpperChildren.h:144-201).
+struct NodeLanes {
+    const int32_t *cnt;  // 2 per node
+    const int32_t *ess;  // 1 per node
+    int32_t LS;          // leaf threshold
+#ifdef __CUDACC__
+    __device__ __forceinline__ void load(int64_t k, int32_t (&v)[7]) const
+    {
+        const int32_t l = cnt[2 * k], r = cnt[2 * k + 1];
+        const int ll = l < LS, rl = r < LS;
+        v[0] = l; v[1] = r; v[2] = ll ? l : 0; v[3] = rl ? r : 0; v[4] = ll; v[5] = rl; v[6] = ess[k];
+    }
+#endif
+};
+
 // Device-wide exclusive scan of n records of K int32 lanes (lanes scanned
 // independently).  out has n+1 records; record n holds the totals.  `ws`
 // (optional) holds the per-tile partials; without it they are allocated.
 // With n_dev set, the kernels read the length there (at most n, which then
 // only sizes the grids and the partials).
+template <int K, class In>
+int scan_exclusive_in(const In &in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws = nullptr,
+                      const int32_t *n_dev = nullptr);
+
 template <int K>
-int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws = nullptr,
-                   const int32_t *n_dev = nullptr);
+inline int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws = nullptr,
+                          const int32_t *n_dev = nullptr)
+{
+    return scan_exclusive_in<K, ScanArray<K>>(ScanArray<K>{in}, out, n, s, ws, n_dev);
+}
 
 // Partials (int32 elements) a scan of n records of K lanes needs.
 int64_t scan_partials_needed(int K, int64_t n);
