@@ -24,6 +24,9 @@ int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, int32_t T
                  const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv, cudaStream_t s);
 int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_params &ph, int64_t n,
                   int32_t *seg_hit, float *seg_t, cudaStream_t s);
+int shade_launch(const Tree &t, const kdgb_trace_params &p, const float *n0, const float *n1, const float *n2,
+                 const uint8_t *c0, const kdgb_light &light, int max_bounces, const float *o, const float *d, int64_t n,
+                 uint8_t *rgba, cudaStream_t s);
 
 namespace {
 thread_local std::string g_last_error;
@@ -562,6 +565,48 @@ int kdgb_trace_photons(const kdgb_tree *tree, const kdgb_trace_params *params, c
     if (!seg_hit_dev || !seg_t_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL output buffer");
     if (tree->t.n_meshes > 1) return fail(KDGB_ERR_UNSUPPORTED, "photons in a batched tree");
     return photon_launch(tree->t, p, *photons, n_photons, seg_hit_dev, seg_t_dev, (cudaStream_t)stream);
+}
+
+void kdgb_light_default(kdgb_light *light)
+{
+    if (!light) return;
+    // Raytracer.cu:43-51: light at (0, 4, 0) with colour (1, 0.92, 0.8)
+    // scaled 0.3 / 0.7 / 0.3 for ambient / diffuse / specular.
+    const float col[3] = {1.0f, 0.92f, 0.8f};
+    light->position[0] = 0.0f;
+    light->position[1] = 4.0f;
+    light->position[2] = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        light->ambient[k] = col[k] * 0.3f;
+        light->diffuse[k] = col[k] * 0.7f;
+        light->specular[k] = col[k] * 0.3f;
+    }
+}
+
+int kdgb_trace_shaded(const kdgb_tree *tree, const kdgb_trace_params *params, const float *n0_dev,
+                      const float *n1_dev, const float *n2_dev, const uint8_t *c0_dev, const kdgb_light *light,
+                      int32_t max_bounces, const float *ray_o_dev, const float *ray_d_dev, int32_t n,
+                      uint8_t *rgba_dev, kdgb_stream_t stream)
+{
+    if (!tree) return fail(KDGB_ERR_INVALID_ARGUMENT, "tree is NULL");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "negative ray count");
+    KDGB_CHECK(validate_trace_params(p, n));
+    if (max_bounces < 0 || max_bounces > 1024) return fail(KDGB_ERR_INVALID_ARGUMENT, "max_bounces must be in 0..1024");
+    kdgb_light L;
+    if (light) L = *light; else kdgb_light_default(&L);
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(L.position[k]) || !std::isfinite(L.ambient[k]) || !std::isfinite(L.diffuse[k]) ||
+            !std::isfinite(L.specular[k]))
+            return fail(KDGB_ERR_INVALID_ARGUMENT, "non-finite light");
+    if (tree->t.n_meshes > 1) return fail(KDGB_ERR_UNSUPPORTED, "shading a batched tree");
+    if (n == 0) return KDGB_OK;
+    if (!ray_o_dev || !ray_d_dev || !rgba_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    if (tree->t.n_tris > 0 && (!n0_dev || !n1_dev || !n2_dev || !c0_dev))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL normal or colour buffer");
+    return shade_launch(tree->t, p, n0_dev, n1_dev, n2_dev, c0_dev, L, max_bounces > 0 ? max_bounces : 64, ray_o_dev,
+                        ray_d_dev, n, rgba_dev, (cudaStream_t)stream);
 }
 
 int kdgb_build_batch(const float *tri_v_dev, const int32_t *mesh_offsets, int32_t n_meshes,

@@ -7,6 +7,10 @@
 // 41-47), each summed left to right.  The output is the T x 9 triangle buffer
 // kdgb_build consumes.
 //
+// kdgb_geometry_gather_attributes is its normal and colour half (n0/n1/n2
+// and c0 of the GeometryList, GeometryList.cu:224-230), which the shading
+// loop reads.
+//
 // kdgb_osc_update_surface restates UpdateSurface of OscCUDAMeshNode
 // (Scene/OscCUDAMeshNode.cu:75-94): heights and normals of the oscillating
 // grid for one time value.
@@ -51,6 +55,42 @@ __global__ void k_gather(const float4 *__restrict__ verts, int32_t n_verts, cons
         o[3 * k + 0] = dot4(M.m + 0, v);
         o[3 * k + 1] = dot4(M.m + 4, v);
         o[3 * k + 2] = dot4(M.m + 8, v);
+    }
+}
+
+struct Mat33 {
+    float m[9];  // row major
+};
+
+// The normal and colour half of AddMeshKernel: per triangle, the three
+// vertex normals times the normal matrix (three row dot products, left to
+// right, w = 0) and the first vertex's colour.  An index outside the vertex
+// buffer gives NaN normals and a zero colour.
+__global__ void k_gather_attributes(const float4 *__restrict__ normals, const uchar4 *__restrict__ colors,
+                                    int32_t n_verts, const unsigned *__restrict__ idx, int32_t n_tris, Mat33 N,
+                                    float4 *__restrict__ n0, float4 *__restrict__ n1, float4 *__restrict__ n2,
+                                    uchar4 *__restrict__ c0)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_tris) return;
+    float4 *outs[3] = {n0, n1, n2};
+    for (int k = 0; k < 3; ++k) {
+        const unsigned vi = idx[3 * (int64_t)i + k];
+        if (vi >= (unsigned)n_verts) {
+            const float nan = __int_as_float(0x7fc00000);
+            outs[k][i] = make_float4(nan, nan, nan, 0.0f);
+            if (k == 0) c0[i] = make_uchar4(0, 0, 0, 0);
+            continue;
+        }
+        const float4 v = normals[vi];
+        float r[3];
+        for (int row = 0; row < 3; ++row) {
+            float s = __fmul_rn(N.m[3 * row + 0], v.x);
+            s = __fadd_rn(s, __fmul_rn(N.m[3 * row + 1], v.y));
+            r[row] = __fadd_rn(s, __fmul_rn(N.m[3 * row + 2], v.z));
+        }
+        outs[k][i] = make_float4(r[0], r[1], r[2], 0.0f);
+        if (k == 0) c0[i] = colors[vi];
     }
 }
 
@@ -114,6 +154,27 @@ extern "C" int kdgb_osc_update_surface(float *vertices_dev, float *normals_dev, 
     const dim3 grid((detail + 15) / 16, (detail + 15) / 16, 1);
     k_osc<<<grid, block, 0, (cudaStream_t)stream>>>(reinterpret_cast<float4 *>(vertices_dev),
                                                     reinterpret_cast<float4 *>(normals_dev), d, height, time);
+    KDGB_LAUNCH_CHECK();
+    return KDGB_OK;
+}
+
+extern "C" int kdgb_geometry_gather_attributes(const float *normals_dev, const uint8_t *colors_dev, int32_t n_vertices,
+                                               const uint32_t *indices_dev, int32_t n_indices,
+                                               const float normal_matrix[9], float *n0_out_dev, float *n1_out_dev,
+                                               float *n2_out_dev, uint8_t *c0_out_dev, kdgb_stream_t stream)
+{
+    if (n_vertices < 0 || n_indices < 0 || n_indices % 3 != 0)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_geometry_gather_attributes: index count must be a multiple of 3");
+    const int32_t n_tris = n_indices / 3;
+    if (n_tris == 0) return KDGB_OK;
+    if (!normals_dev || !colors_dev || !indices_dev || !n0_out_dev || !n1_out_dev || !n2_out_dev || !c0_out_dev)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_geometry_gather_attributes: NULL buffer");
+    Mat33 N;
+    for (int k = 0; k < 9; ++k) N.m[k] = normal_matrix ? normal_matrix[k] : (k % 4 == 0 ? 1.0f : 0.0f);
+    k_gather_attributes<<<(n_tris + kGeoBlock - 1) / kGeoBlock, kGeoBlock, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float4 *>(normals_dev), reinterpret_cast<const uchar4 *>(colors_dev), n_vertices,
+        indices_dev, n_tris, N, reinterpret_cast<float4 *>(n0_out_dev), reinterpret_cast<float4 *>(n1_out_dev),
+        reinterpret_cast<float4 *>(n2_out_dev), reinterpret_cast<uchar4 *>(c0_out_dev));
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }

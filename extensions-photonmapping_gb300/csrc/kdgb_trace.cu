@@ -113,10 +113,12 @@ __device__ __forceinline__ int leaf_test(const Ctx &c, int4 leaf, float3 o, floa
 
 // kd-restart, first hit (Raytracer.cu:57-106, 165-262).
 template <bool SKIP>
-__device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int maxit, float &t, float &u, float &v)
+__device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int maxit, float &t, float &u, float &v,
+                             float3 *dused = nullptr)
 {
     const float3 d = adjust_dir(din);
     const float3 inv = inv3(d);
+    if (dused) *dused = d;
     float tmin = 0.0f;
     int iters = 0;
     do {
@@ -151,7 +153,7 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
 // after it (ShortStack.cu:134,148), exactly as the reference does.
 template <bool SKIP>
 __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int depth, int maxit, int2 *st,
-                                int stride, float &t, float &u, float &v)
+                                int stride, float &t, float &u, float &v, float3 *dused = nullptr)
 {
     int nxt = 0, cnt = 0;
     float3 d = adjust_dir(din);
@@ -206,7 +208,11 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
         if (!SKIP || ray_box(o, fixed ? inv1 : inv3(d), __ldg(c.bmin + node), __ldg(c.bmax + node))) {
             float tb = th, ub = 0.0f, vb = 0.0f;
             const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
-            if (h != -1) { t = tb; u = ub; v = vb; return h; }
+            if (h != -1) {
+                t = tb; u = ub; v = vb;
+                if (dused) *dused = d;
+                return h;
+            }
         }
         if (++iters >= maxit) break;
     } while (th < KDGB_FINF);
@@ -459,6 +465,180 @@ __global__ void k_photons(PhotonArgs a)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Shading (Raytracer.cu:165-262, ShortStack.cu:100-190, BruteTracer.cu:54-96
+// with ColorKernels.h:15-85), into a headless RGBA8 buffer instead of the
+// OpenGL canvas.  The un-vendored vector helpers are evaluated left to right
+// with IEEE 1/sqrt in normalize (their host branch) and the specular power is
+// this library's own series restatement, operation for operation the one of
+// the CPU restatement, so the pixels match it bit for bit.
+// ---------------------------------------------------------------------------
+
+// x^y for x in [0, 1], y >= 0: 2^(y log2 x); log2 from the atanh series
+// ln m = 2 s (1 + s^2/3 + ... + s^10/11), s = (m-1)/(m+1), m in
+// [sqrt(1/2), sqrt(2)); 2^f from the Taylor series of e^(f ln 2) to the 8th
+// power, f in [-1/2, 1/2]; within 2e-5 relative (the fp32 product y log2 x
+// dominates at large y).
+__device__ __forceinline__ float kpow(float x, float y)
+{
+    if (y == 0.0f) return 1.0f;
+    if (!(x > 0.0f)) return 0.0f;
+    if (x >= 1.0f) return 1.0f;
+    int e = 0;
+    if (x < 0x1p-126f) { x = __fmul_rn(x, 0x1p24f); e = -24; }
+    const int b = __float_as_int(x);
+    e += ((b >> 23) & 0xff) - 127;
+    float m = __int_as_float((b & 0x007fffff) | 0x3f800000);
+    if (m > 1.41421356f) { m = __fmul_rn(m, 0.5f); e += 1; }
+    const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+    const float s2 = __fmul_rn(s, s);
+    float poly = 0.0909090909f;
+    poly = __fadd_rn(0.111111111f, __fmul_rn(s2, poly));
+    poly = __fadd_rn(0.142857143f, __fmul_rn(s2, poly));
+    poly = __fadd_rn(0.2f, __fmul_rn(s2, poly));
+    poly = __fadd_rn(0.333333333f, __fmul_rn(s2, poly));
+    poly = __fadd_rn(1.0f, __fmul_rn(s2, poly));
+    const float ln_m = __fmul_rn(__fmul_rn(2.0f, s), poly);
+    const float z = __fmul_rn(y, __fadd_rn((float)e, __fmul_rn(ln_m, 1.44269504f)));
+    if (z < -150.0f) return 0.0f;
+    const float n = floorf(__fadd_rn(z, 0.5f));
+    const float g = __fmul_rn(__fsub_rn(z, n), 0.693147181f);
+    float q = 2.48015873e-5f;
+    q = __fadd_rn(1.98412698e-4f, __fmul_rn(g, q));
+    q = __fadd_rn(1.38888889e-3f, __fmul_rn(g, q));
+    q = __fadd_rn(8.33333333e-3f, __fmul_rn(g, q));
+    q = __fadd_rn(4.16666667e-2f, __fmul_rn(g, q));
+    q = __fadd_rn(0.166666667f, __fmul_rn(g, q));
+    q = __fadd_rn(0.5f, __fmul_rn(g, q));
+    q = __fadd_rn(1.0f, __fmul_rn(g, q));
+    q = __fadd_rn(1.0f, __fmul_rn(g, q));
+    const int ni = (int)n, n1 = ni / 2, n2 = ni - n1;
+    return __fmul_rn(__fmul_rn(q, __int_as_float((n1 + 127) << 23)), __int_as_float((n2 + 127) << 23));
+}
+
+__device__ __forceinline__ float3 nrm3(float3 v)
+{
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(v, v)));
+    return make_float3(__fmul_rn(v.x, inv), __fmul_rn(v.y, inv), __fmul_rn(v.z, inv));
+}
+__device__ __forceinline__ float sat(float x) { return x > 0.0f ? (x < 1.0f ? x : 1.0f) : 0.0f; }
+__device__ __forceinline__ float clamp01(float x) { return fmaxf(0.0f, fminf(x, 1.0f)); }
+__device__ __forceinline__ unsigned to_u8(float x)
+{
+    const float y = truncf(__fmul_rn(x, 255.0f));
+    return (unsigned)(y > 0.0f ? (y < 255.0f ? y : 255.0f) : 0.0f);
+}
+
+struct Light {
+    float3 pos, amb, dif, spec;
+};
+
+// PhongLighting (ColorKernels.h:15-41), shadow = 1.
+__device__ __forceinline__ float4 phong(float4 c, float3 n, float3 pt, float3 origin, const Light &L)
+{
+    const float3 ld = nrm3(sub3(L.pos, pt));
+    const float diffuse = sat(__fmul_rn(dot3(ld, n), 1.0f));
+    const float k = __fmul_rn(2.0f, dot3(n, ld));
+    const float3 refl = nrm3(make_float3(__fsub_rn(__fmul_rn(k, n.x), ld.x), __fsub_rn(__fmul_rn(k, n.y), ld.y),
+                                         __fsub_rn(__fmul_rn(k, n.z), ld.z)));
+    const float stemp = sat(dot3(nrm3(sub3(origin, pt)), refl));
+    const float sp = __fsub_rn(1.0f, c.w);
+    const float specular = __fmul_rn(sp, kpow(stemp, __fmul_rn(128.0f, sp)));
+    const float lx = __fadd_rn(__fmul_rn(c.x, __fadd_rn(L.amb.x, __fmul_rn(L.dif.x, diffuse))),
+                               __fmul_rn(__fmul_rn(__fmul_rn(L.spec.x, specular), 10.0f), 1.0f));
+    const float ly = __fadd_rn(__fmul_rn(c.y, __fadd_rn(L.amb.y, __fmul_rn(L.dif.y, diffuse))),
+                               __fmul_rn(__fmul_rn(__fmul_rn(L.spec.y, specular), 10.0f), 1.0f));
+    const float lz = __fadd_rn(__fmul_rn(c.z, __fadd_rn(L.amb.z, __fmul_rn(L.dif.z, diffuse))),
+                               __fmul_rn(__fmul_rn(__fmul_rn(L.spec.z, specular), 10.0f), 1.0f));
+    return make_float4(clamp01(lx), clamp01(ly), clamp01(lz), c.w < specular ? specular : c.w);
+}
+
+struct ShadeArgs {
+    Ctx c;
+    const float4 *p0, *p1, *p2;   // geometry, for brute force
+    int32_t T;
+    const float4 *n0, *n1, *n2;   // vertex normals per triangle
+    const uchar4 *c0;             // colour per triangle
+    Light L;
+    const float *o, *d;
+    int64_t n;
+    uchar4 *rgba;
+    int tie, depth, maxit, max_bounces, tile_width;
+    const int32_t *build_err;
+};
+
+// Exhaustive (BruteTracer.cu:54-96) from one thread: first hit over all
+// triangles, no direction clamp.
+__device__ __forceinline__ int brute_hit(const ShadeArgs &a, float3 o, float3 d, float &t, float &u, float &v)
+{
+    int hit = -1;
+    float tb = KDGB_FINF, ub = 0.0f, vb = 0.0f;
+    for (int32_t i = 0; i < a.T; ++i) {
+        const float4 A = __ldg(a.p0 + i), B = __ldg(a.p1 + i), C = __ldg(a.p2 + i);
+        const float3 v0 = make_float3(A.x, A.y, A.z);
+        mt_test(v0, sub3(make_float3(B.x, B.y, B.z), v0), sub3(make_float3(C.x, C.y, C.z), v0), i, o, d, a.tie, hit,
+                tb, ub, vb);
+    }
+    if (!(tb < KDGB_FINF)) return -1;
+    t = tb; u = ub; v = vb;
+    return hit;
+}
+
+template <int TRACER, bool SKIP>
+__global__ void k_shade(ShadeArgs a)
+{
+    extern __shared__ int2 stack_smem[];
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.n) return;
+    const int64_t i = ray_index(id, a.tile_width);
+    float4 col = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!(a.build_err && *a.build_err)) {
+        float3 o = ld3(a.o, i), d = ld3(a.d, i);
+        if (TRACER != KDGB_TRACER_BRUTE) d = adjust_dir(d);
+        for (int b = 0; b < a.max_bounces; ++b) {
+            float t = 0.0f, u = 0.0f, v = 0.0f;
+            float3 dh = d;
+            int h;
+            if (TRACER == KDGB_TRACER_SHORTSTACK)
+                h = trace_shortstack<SKIP>(a.c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x,
+                                           t, u, v, &dh);
+            else if (TRACER == KDGB_TRACER_RESTART)
+                h = trace_restart<SKIP>(a.c, o, d, a.tie, a.maxit, t, u, v, &dh);
+            else
+                h = brute_hit(a, o, d, t, u, v);
+            if (h < 0) break;
+            d = dh;
+            // Lighting (ColorKernels.h:43-78).
+            const float3 pt = make_float3(__fadd_rn(o.x, __fmul_rn(t, d.x)), __fadd_rn(o.y, __fmul_rn(t, d.y)),
+                                          __fadd_rn(o.z, __fmul_rn(t, d.z)));
+            const float w = __fsub_rn(__fsub_rn(1.0f, u), v);
+            const float4 A = __ldg(a.n0 + h), B = __ldg(a.n1 + h), C = __ldg(a.n2 + h);
+            const float3 nrm = nrm3(make_float3(
+                __fadd_rn(__fadd_rn(__fmul_rn(w, A.x), __fmul_rn(u, B.x)), __fmul_rn(v, C.x)),
+                __fadd_rn(__fadd_rn(__fmul_rn(w, A.y), __fmul_rn(u, B.y)), __fmul_rn(v, C.y)),
+                __fadd_rn(__fadd_rn(__fmul_rn(w, A.z), __fmul_rn(u, B.z)), __fmul_rn(v, C.z))));
+            const uchar4 cc = a.c0[h];
+            float4 c = make_float4(__fdiv_rn((float)cc.x, 255.0f), __fdiv_rn((float)cc.y, 255.0f),
+                                   __fdiv_rn((float)cc.z, 255.0f), __fdiv_rn((float)cc.w, 255.0f));
+            const float k = __fmul_rn(2.0f, dot3(nrm, make_float3(-d.x, -d.y, -d.z)));
+            const float3 nd = nrm3(make_float3(__fadd_rn(__fmul_rn(k, nrm.x), d.x), __fadd_rn(__fmul_rn(k, nrm.y), d.y),
+                                               __fadd_rn(__fmul_rn(k, nrm.z), d.z)));
+            c = phong(c, nrm, pt, o, a.L);
+            o = make_float3(__fadd_rn(pt.x, __fmul_rn(0.00001f, nd.x)), __fadd_rn(pt.y, __fmul_rn(0.00001f, nd.y)),
+                            __fadd_rn(pt.z, __fmul_rn(0.00001f, nd.z)));
+            d = nd;
+            // BlendColor (ColorKernels.h:80-85).
+            const float kk = __fmul_rn(__fsub_rn(1.0f, col.w), c.w);
+            col = make_float4(__fadd_rn(col.x, __fmul_rn(kk, c.x)), __fadd_rn(col.y, __fmul_rn(kk, c.y)),
+                              __fadd_rn(col.z, __fmul_rn(kk, c.z)), __fadd_rn(col.w, __fmul_rn(kk, 1.0f)));
+            if (TRACER != KDGB_TRACER_BRUTE) d = adjust_dir(d);
+            if (!(col.w < 0.97f)) break;
+        }
+    }
+    a.rgba[i] = make_uchar4((unsigned char)to_u8(col.x), (unsigned char)to_u8(col.y), (unsigned char)to_u8(col.z),
+                            (unsigned char)to_u8(col.w));
+}
+
 }  // namespace
 
 
@@ -576,6 +756,51 @@ int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_p
     } else {
         if (skip) k_photons<KDGB_TRACER_RESTART, true><<<grid, bs, 0, s>>>(a);
         else k_photons<KDGB_TRACER_RESTART, false><<<grid, bs, 0, s>>>(a);
+    }
+    KDGB_LAUNCH_CHECK();
+    return KDGB_OK;
+}
+
+int shade_launch(const Tree &t, const kdgb_trace_params &p, const float *n0, const float *n1, const float *n2,
+                 const uint8_t *c0, const kdgb_light &light, int max_bounces, const float *o, const float *d, int64_t n,
+                 uint8_t *rgba, cudaStream_t s)
+{
+    ShadeArgs a;
+    a.c.node = t.tnode.p;
+    a.c.bmin = t.bmin.p;
+    a.c.bmax = t.bmax.p;
+    a.c.tri = t.ttri.p;
+    a.c.root = 0;
+    a.p0 = t.p0.p; a.p1 = t.p1.p; a.p2 = t.p2.p;
+    a.T = t.n_tris;
+    a.n0 = reinterpret_cast<const float4 *>(n0);
+    a.n1 = reinterpret_cast<const float4 *>(n1);
+    a.n2 = reinterpret_cast<const float4 *>(n2);
+    a.c0 = reinterpret_cast<const uchar4 *>(c0);
+    a.L.pos = make_float3(light.position[0], light.position[1], light.position[2]);
+    a.L.amb = make_float3(light.ambient[0], light.ambient[1], light.ambient[2]);
+    a.L.dif = make_float3(light.diffuse[0], light.diffuse[1], light.diffuse[2]);
+    a.L.spec = make_float3(light.specular[0], light.specular[1], light.specular[2]);
+    a.o = o; a.d = d; a.n = n;
+    a.rgba = reinterpret_cast<uchar4 *>(rgba);
+    a.tie = p.tie;
+    a.depth = p.stack_depth;
+    a.maxit = p.max_iterations > 0 ? p.max_iterations : kDefaultMaxIterations;
+    a.max_bounces = max_bounces;
+    a.tile_width = p.tile_width;
+    a.build_err = t.ws.state.p ? &t.ws.state.p->err : nullptr;
+    const int bs = p.block_size > 0 ? p.block_size : 128;
+    const unsigned grid = blocks_for(n, bs);
+    const bool skip = p.leaf_skipping != 0;
+    if (p.tracer == KDGB_TRACER_SHORTSTACK) {
+        const size_t smem = sizeof(int2) * (size_t)p.stack_depth * bs;
+        if (skip) k_shade<KDGB_TRACER_SHORTSTACK, true><<<grid, bs, smem, s>>>(a);
+        else k_shade<KDGB_TRACER_SHORTSTACK, false><<<grid, bs, smem, s>>>(a);
+    } else if (p.tracer == KDGB_TRACER_RESTART) {
+        if (skip) k_shade<KDGB_TRACER_RESTART, true><<<grid, bs, 0, s>>>(a);
+        else k_shade<KDGB_TRACER_RESTART, false><<<grid, bs, 0, s>>>(a);
+    } else {
+        k_shade<KDGB_TRACER_BRUTE, false><<<grid, bs, 0, s>>>(a);
     }
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;

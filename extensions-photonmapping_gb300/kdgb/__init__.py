@@ -23,10 +23,10 @@ import numpy as np
 from . import scenes
 from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ERR_CAPACITY, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, FINF, LEAF, LOWER_BITMAP, LOWER_SAH,
                    TIE_LOWEST_ID, TIE_REF_LAST, TRACER_BRUTE, TRACER_RESTART, TRACER_SHORTSTACK, X, Y, Z,
-                   AutotuneResult, BuildParams, BuildStats, KdgbError, PhotonParams, TraceParams, TreeView, build_params, check,
+                   AutotuneResult, BuildParams, BuildStats, KdgbError, Light, light, PhotonParams, TraceParams, TreeView, build_params, check,
                    lib, library_path, photon_params, trace_params)
 
-__all__ = ["KDTree", "Graph", "autotune", "AutotuneResult", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
+__all__ = ["KDTree", "Graph", "autotune", "AutotuneResult", "Light", "light", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
            "trace_params", "photon_params", "PhotonParams", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
            "BUILD_REFERENCE", "BUILD_TUNED", "TRACER_RESTART", "TRACER_SHORTSTACK", "TRACER_BRUTE",
            "TIE_LOWEST_ID", "TIE_REF_LAST", "FINF", "lib", "library_path"]
@@ -247,6 +247,29 @@ def _trace_photons(self, n_photons: int, params: TraceParams | None = None, phot
 
 
 KDTree.trace_photons = _trace_photons
+
+
+def _trace_shaded(self, o, d, n0, n1, n2, c0, params: TraceParams | None = None, light_params: Light | None = None,
+                  max_bounces: int = 0, stream=None, out=None, **kw):
+    """Shaded pixels (kdgb_trace_shaded): (n, 4) uint8 CUDA tensor.  n0/n1/n2:
+    (T, 4) float32 vertex normals per triangle, c0: (T, 4) uint8 colours."""
+    torch = _torch()
+    o = _dev(o, torch.float32, 3)
+    d = _dev(d, torch.float32, 3)
+    n0, n1, n2 = (_dev(x, torch.float32, 4) for x in (n0, n1, n2))
+    c0 = _dev(c0, torch.uint8, 4)
+    n = o.shape[0]
+    p = params if params is not None else trace_params(**kw)
+    L = light_params if light_params is not None else light()
+    if out is None:
+        out = torch.empty((n, 4), dtype=torch.uint8, device=o.device)
+    check(lib().kdgb_trace_shaded(self._h, C.byref(p), _ptr(n0), _ptr(n1), _ptr(n2), _ptr(c0), C.byref(L),
+                                  max_bounces, _ptr(o), _ptr(d), n, _ptr(out), C.c_void_p(_stream(stream))),
+          "kdgb_trace_shaded")
+    return out
+
+
+KDTree.trace_shaded = _trace_shaded
 
 
 def _build_batch(cls, tris, mesh_offsets, params: BuildParams | None = None, stream=None, **kw) -> "KDTree":

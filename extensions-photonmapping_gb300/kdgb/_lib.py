@@ -62,6 +62,11 @@ class AutotuneResult(C.Structure):
                 ("baseline", C.c_float), ("objective", C.c_float), ("trials", C.c_int32)]
 
 
+class Light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("ambient", C.c_float * 3), ("diffuse", C.c_float * 3),
+                ("specular", C.c_float * 3)]
+
+
 class BuildStats(C.Structure):
     _fields_ = [("upper_levels", C.c_int32), ("lower_levels", C.c_int32), ("n_nodes", C.c_int32),
                 ("n_refs", C.c_int32), ("n_leaves", C.c_int32), ("max_depth", C.c_int32),
@@ -101,6 +106,10 @@ SIGNATURES = {
     "kdgb_graph_status": (C.c_int, [P, P]),
     "kdgb_graph_destroy": (C.c_int, [P]),
     "kdgb_geometry_gather": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, P]),
+    "kdgb_geometry_gather_attributes": (C.c_int, [P, P, C.c_int32, P, C.c_int32, P, P, P, P, P, P]),
+    "kdgb_light_default": (None, [C.POINTER(Light)]),
+    "kdgb_trace_shaded": (C.c_int, [P, C.POINTER(TraceParams), P, P, P, P, C.POINTER(Light), C.c_int32, P, P,
+                                    C.c_int32, P, P]),
     "kdgb_osc_update_surface": (C.c_int, [P, P, C.c_int32, C.c_float, C.c_float, P]),
     "kdgb_backward": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, C.c_int32, P, P, P, P, P, P]),
     "kdgb_trace_brute": (C.c_int, [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, P]),
@@ -167,6 +176,16 @@ def photon_params(**kw) -> PhotonParams:
         else:
             setattr(p, k, v)
     return p
+
+
+def light(**kw) -> Light:
+    L = Light()
+    lib().kdgb_light_default(C.byref(L))
+    for k, v in kw.items():
+        if not hasattr(L, k):
+            raise AttributeError(k)
+        setattr(L, k, (C.c_float * 3)(*[float(x) for x in v]))
+    return L
 
 
 def trace_params(**kw) -> TraceParams:

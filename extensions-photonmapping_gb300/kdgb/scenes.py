@@ -87,6 +87,55 @@ def heightfield(nx: int, ny: int, seed: int = 1, amplitude: float = 0.2):
     return np.ascontiguousarray(tris, dtype=np.float32), verts, idx
 
 
+def vertex_normals(verts: np.ndarray, idx: np.ndarray) -> np.ndarray:
+    """Per-vertex normals: the normalised sum of the adjacent faces' area
+    weighted normals, as (V, 4) float32 with w = 0."""
+    v = verts.astype(np.float64)
+    t = idx.astype(np.int64).reshape(-1, 3)
+    fn = np.cross(v[t[:, 1]] - v[t[:, 0]], v[t[:, 2]] - v[t[:, 0]])
+    acc = np.zeros_like(v)
+    for k in range(3):
+        np.add.at(acc, t[:, k], fn)
+    acc /= np.maximum(np.linalg.norm(acc, axis=1, keepdims=True), 1e-30)
+    return np.concatenate([acc, np.zeros((v.shape[0], 1))], axis=1).astype(np.float32)
+
+
+def shaded_box(nx: int = 32, ny: int = 16, seed: int = 1):
+    """A height field inside four mirror-like walls, for the shading loop:
+    returns (tris (T, 9), n0, n1, n2 (T, 4) float32 vertex normals per
+    triangle, c0 (T, 4) uint8 colours).  The height field's colours are
+    seeded with alphas of 255 (opaque), 128 and 0 (reflective), the walls
+    have alpha 40, so rays take several bounces."""
+    verts = heightfield_vertices(nx, ny, seed)
+    idx = grid_indices(nx, ny).astype(np.int64)
+    vn = vertex_normals(verts, idx)
+    tris = verts[idx].reshape(-1, 9)
+    nrm = vn[idx].reshape(-1, 3, 4)
+    T = tris.shape[0]
+    r = uniform(seed, 4 * T, stream=11).reshape(T, 4)
+    c0 = np.floor(r * 256.0).clip(0, 255).astype(np.uint8)
+    c0[:, 3] = np.array([255, 128, 0], np.uint8)[np.floor(r[:, 3] * 3).astype(np.int64).clip(0, 2)]
+    lo, hi, top = -0.1, 1.1, 1.5
+    corners = {"x0": [(lo, lo, 0), (lo, hi, 0), (lo, hi, top), (lo, lo, top)],
+               "x1": [(hi, lo, 0), (hi, lo, top), (hi, hi, top), (hi, hi, 0)],
+               "y0": [(lo, lo, 0), (lo, lo, top), (hi, lo, top), (hi, lo, 0)],
+               "y1": [(lo, hi, 0), (hi, hi, 0), (hi, hi, top), (lo, hi, top)]}
+    inward = {"x0": (1, 0, 0), "x1": (-1, 0, 0), "y0": (0, 1, 0), "y1": (0, -1, 0)}
+    wt, wn, wc = [], [], []
+    for k, q in corners.items():
+        a, b, c, d = (np.array(p, np.float32) for p in q)
+        n4 = np.array(inward[k] + (0,), np.float32)
+        for tri in ((a, b, c), (a, c, d)):
+            wt.append(np.concatenate(tri))
+            wn.append(np.stack([n4, n4, n4]))
+            wc.append(np.array([200, 210, 230, 40], np.uint8))
+    tris = np.concatenate([tris, np.array(wt, np.float32)])
+    nrm = np.concatenate([nrm, np.array(wn, np.float32)])
+    c0 = np.concatenate([c0, np.array(wc, np.uint8)])
+    n0, n1, n2 = (np.ascontiguousarray(nrm[:, k]) for k in range(3))
+    return np.ascontiguousarray(tris, dtype=np.float32), n0, n1, n2, np.ascontiguousarray(c0)
+
+
 def _frames(seed: int, n: int, stream: int):
     """Random orthonormal pairs (u, w) spanning a uniformly oriented plane."""
     nz = normal(seed, n, stream)

@@ -228,6 +228,37 @@ KDGB_API int kdgb_trace_photons(const kdgb_tree *tree, const kdgb_trace_params *
                                 const kdgb_photon_params *photons, int32_t n_photons,
                                 int32_t *seg_hit_dev, float *seg_t_dev, kdgb_stream_t stream);
 
+/* Light of the shading loop (the __constant__ d_light* of
+ * ColorKernels.h:10-13). */
+typedef struct kdgb_light {
+    float position[3];
+    float ambient[3];
+    float diffuse[3];
+    float specular[3];
+} kdgb_light;
+
+/* The tracers' constructor defaults (Raytracer.cu:43-51). */
+KDGB_API void kdgb_light_default(kdgb_light *light);
+
+/* Replaces the pixel output of RayTracer / ShortStack / BruteTracer ::Trace
+ * (Raytracer.cu:165-262, ShortStack.cu:100-190, BruteTracer.cu:54-96 with
+ * Lighting / PhongLighting / BlendColor, ColorKernels.h:15-85), writing an
+ * RGBA8 buffer instead of the OpenGL canvas.  Per ray: find the first hit,
+ * shade it (interpolated vertex normal, triangle colour, Phong light),
+ * blend it front to back, reflect the ray about the normal and continue from
+ * the hit point until the ray escapes, the blended alpha reaches 0.97 or
+ * max_bounces hits were shaded (0 = 64; the reference has no bound).
+ * n0/n1/n2: n_tris float4 vertex normals per triangle and c0: n_tris uchar4
+ * colours, the GeometryList layout (kdgb_geometry_gather_attributes fills
+ * them); light NULL = kdgb_light_default.  The vector helpers are evaluated
+ * left to right with IEEE 1/sqrt in normalize and the specular power is
+ * this library's series restatement of pow, so the pixels are
+ * deterministic and match the CPU restatement bit for bit. */
+KDGB_API int kdgb_trace_shaded(const kdgb_tree *tree, const kdgb_trace_params *params, const float *n0_dev,
+                               const float *n1_dev, const float *n2_dev, const uint8_t *c0_dev,
+                               const kdgb_light *light, int32_t max_bounces, const float *ray_o_dev,
+                               const float *ray_d_dev, int32_t n, uint8_t *rgba_dev, kdgb_stream_t stream);
+
 /* Batched build (no reference counterpart; the reference builds one scene
  * per TriangleMap): n_meshes independent meshes stored back to back in
  * tri_v_dev (mesh m = triangles [mesh_offsets[m], mesh_offsets[m+1]),
@@ -339,6 +370,16 @@ KDGB_API int kdgb_backward(const float *vertices_dev, int32_t n_vertices, const 
 KDGB_API int kdgb_geometry_gather(const float *vertices_dev, int32_t n_vertices, const uint32_t *indices_dev,
                                   int32_t n_indices, const float model[16], float *tri_v_out_dev,
                                   kdgb_stream_t stream);
+
+/* The normal and colour half of GeometryList::AddMesh (GeometryList.cu:
+ * 224-230): per triangle of the index buffer, the three vertex normals
+ * (n_vertices float4) times the row-major 3x3 normal matrix (NULL =
+ * identity; w = 0) into n0/n1/n2, and the first vertex's colour (n_vertices
+ * uchar4) into c0: the inputs of kdgb_trace_shaded. */
+KDGB_API int kdgb_geometry_gather_attributes(const float *normals_dev, const uint8_t *colors_dev, int32_t n_vertices,
+                                             const uint32_t *indices_dev, int32_t n_indices,
+                                             const float normal_matrix[9], float *n0_out_dev, float *n1_out_dev,
+                                             float *n2_out_dev, uint8_t *c0_out_dev, kdgb_stream_t stream);
 
 /* Replaces OscCUDAMeshNode::Handle (OscCUDAMeshNode.cu:96-107, kernel
  * UpdateSurface :75-94): moves the (detail+1)^2 float4 vertices and normals

@@ -177,12 +177,13 @@ static inline int leaf_test(const or_tree *tr, const float *tri, int node, v3 o,
 /* Raytracer.cu:57-106 TraceNode<true> + Raytracer.cu:165-262 KDRestart,
  * stopped at the first leaf that reports a hit (shading left out). */
 static void trace_restart_one(const or_tree *tr, const float *tri, const or_trace_params *p,
-                              v3 o, v3 din, int32_t *hit, float *ot, float *ou, float *ov)
+                              v3 o, v3 din, int32_t *hit, float *ot, float *ou, float *ov, v3 *dused)
 {
     const v3 d = adjust_dir(din);
     const v3 inv = inv3(d);
     float th[3] = {0.0f, 0.0f, 0.0f};
     long iters = 0;
+    if (dused) *dused = d;
     do {
         float t_next = OR_FINF;
         int node = 0;
@@ -215,7 +216,7 @@ static void trace_restart_one(const or_tree *tr, const float *tri, const or_trac
  * ShortStackTrace, first hit.  The direction is inverted in place before the
  * descent and re-inverted after it, every outer iteration (ShortStack.cu:134,148). */
 static void trace_shortstack_one(const or_tree *tr, const float *tri, const or_trace_params *p,
-                                 v3 o, v3 din, int32_t *hit, float *ot, float *ou, float *ov)
+                                 v3 o, v3 din, int32_t *hit, float *ot, float *ou, float *ov, v3 *dused)
 {
     enum { MAXN = 64 };
     int sn[MAXN]; float st[MAXN];
@@ -261,7 +262,11 @@ static void trace_shortstack_one(const or_tree *tr, const float *tri, const or_t
         if (!p->leaf_skipping || ray_box(o, inv3(d), tr->aabb_min + 4 * (size_t)node,
                                           tr->aabb_max + 4 * (size_t)node)) {
             const int h = leaf_test(tr, tri, node, o, d, p->tie, th);
-            if (h != -1) { *hit = h; *ot = th[0]; *ou = th[1]; *ov = th[2]; return; }
+            if (h != -1) {
+                *hit = h; *ot = th[0]; *ou = th[1]; *ov = th[2];
+                if (dused) *dused = d;
+                return;
+            }
         }
         if (p->max_iterations > 0 && ++iters >= p->max_iterations) break;
     } while (th[0] < OR_FINF);
@@ -305,9 +310,9 @@ int or_trace(const or_tree *tr, const float *tri, int32_t T, const or_trace_para
     for (int32_t i = 0; i < n; ++i) {
         const v3 o = ld3(ray_o + 3 * (size_t)i), d = ld3(ray_d + 3 * (size_t)i);
         if (p->tracer == OR_TRACER_SHORTSTACK)
-            trace_shortstack_one(tr, tri, p, o, d, hit + i, t + i, u + i, v + i);
+            trace_shortstack_one(tr, tri, p, o, d, hit + i, t + i, u + i, v + i, NULL);
         else
-            trace_restart_one(tr, tri, p, o, d, hit + i, t + i, u + i, v + i);
+            trace_restart_one(tr, tri, p, o, d, hit + i, t + i, u + i, v + i, NULL);
     }
     return 0;
 }
@@ -501,8 +506,8 @@ int or_trace_photons(const or_tree *tr, const float *tri, int32_t T, const or_tr
         while (k < S) {
             int32_t h;
             float t, u, v;
-            if (p->tracer == OR_TRACER_SHORTSTACK) trace_shortstack_one(tr, tri, p, o, d, &h, &t, &u, &v);
-            else trace_restart_one(tr, tri, p, o, d, &h, &t, &u, &v);
+            if (p->tracer == OR_TRACER_SHORTSTACK) trace_shortstack_one(tr, tri, p, o, d, &h, &t, &u, &v, NULL);
+            else trace_restart_one(tr, tri, p, o, d, &h, &t, &u, &v, NULL);
             seg_hit[base + k] = h;
             seg_t[base + k] = h >= 0 ? t : INFINITY;
             ++k;
@@ -521,6 +526,165 @@ int or_trace_photons(const or_tree *tr, const float *tri, int32_t T, const or_tr
             d = sample_cosine(nrm, u24(r[0]), u24(r[1]));
         }
         for (; k < S; ++k) { seg_hit[base + k] = -2; seg_t[base + k] = INFINITY; }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Shading (Raytracer.cu:165-262, ShortStack.cu:100-190, BruteTracer.cu:54-96, */
+/* ColorKernels.h:15-85)                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* x^y for x in [0, 1], y >= 0 (the specular term): 2^(y log2 x), log2 from
+ * the series ln m = 2 atanh((m-1)/(m+1)) = 2 s (1 + s^2/3 + s^4/5 + ...) on
+ * m in [sqrt(1/2), sqrt(2)), 2^f from the Taylor series of e^(f ln 2) on
+ * f in [-1/2, 1/2]; within 2e-5 relative (the fp32 product y log2 x
+ * dominates at large y).  The reference calls __powf on the
+ * device and powf on the host; this own restatement with every operation
+ * separately rounded is what the CUDA kernel computes as well. */
+float or_kpow(float x, float y)
+{
+    if (y == 0.0f) return 1.0f;
+    if (!(x > 0.0f)) return 0.0f;
+    if (x >= 1.0f) return 1.0f;
+    int e = 0;
+    if (x < 0x1p-126f) { x = x * 0x1p24f; e = -24; }
+    const int32_t b = f2i(x);
+    e += ((b >> 23) & 0xff) - 127;
+    float m = i2f((b & 0x007fffff) | 0x3f800000);
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float poly = 0.0909090909f;
+    poly = 0.111111111f + s2 * poly;
+    poly = 0.142857143f + s2 * poly;
+    poly = 0.2f + s2 * poly;
+    poly = 0.333333333f + s2 * poly;
+    poly = 1.0f + s2 * poly;
+    const float ln_m = (2.0f * s) * poly;
+    const float z = y * ((float)e + ln_m * 1.44269504f);
+    if (z < -150.0f) return 0.0f;
+    const float n = floorf(z + 0.5f);
+    const float g = (z - n) * 0.693147181f;
+    float q = 2.48015873e-5f;
+    q = 1.98412698e-4f + g * q;
+    q = 1.38888889e-3f + g * q;
+    q = 8.33333333e-3f + g * q;
+    q = 4.16666667e-2f + g * q;
+    q = 0.166666667f + g * q;
+    q = 0.5f + g * q;
+    q = 1.0f + g * q;
+    q = 1.0f + g * q;
+    const int ni = (int)n, n1 = ni / 2, n2 = ni - n1;
+    return (q * i2f((n1 + 127) << 23)) * i2f((n2 + 127) << 23);
+}
+
+/* normalize of the CUDA-SDK helpers with IEEE 1/sqrt (their host branch). */
+static inline v3 nrm3(v3 v)
+{
+    const float inv = 1.0f / sqrtf(dot3(v, v));
+    return mk3(v.x * inv, v.y * inv, v.z * inv);
+}
+static inline float sat(float x) { return x > 0.0f ? (x < 1.0f ? x : 1.0f) : 0.0f; }
+static inline float clamp01(float x) { return fmaxf(0.0f, fminf(x, 1.0f)); }
+static inline uint8_t to_u8(float x)
+{
+    const float y = truncf(x * 255.0f);
+    return (uint8_t)(y > 0.0f ? (y < 255.0f ? y : 255.0f) : 0.0f);
+}
+
+/* PhongLighting (ColorKernels.h:15-41) with shadow = 1. */
+static inline f4 phong(f4 c, v3 n, v3 pt, v3 origin, const or_light *L)
+{
+    const v3 lpos = ld3(L->position);
+    const v3 ld = nrm3(sub3(lpos, pt));
+    const float diffuse = sat(dot3(ld, n) * 1.0f);
+    const float k = 2.0f * dot3(n, ld);
+    const v3 refl = nrm3(mk3(k * n.x - ld.x, k * n.y - ld.y, k * n.z - ld.z));
+    const float stemp = sat(dot3(nrm3(sub3(origin, pt)), refl));
+    const float spec_prop = 1.0f - c.w;
+    const float specular = spec_prop * or_kpow(stemp, 128.0f * spec_prop);
+    const float *A = L->ambient, *D = L->diffuse, *S = L->specular;
+    const float lx = c.x * (A[0] + D[0] * diffuse) + ((S[0] * specular) * 10.0f) * 1.0f;
+    const float ly = c.y * (A[1] + D[1] * diffuse) + ((S[1] * specular) * 10.0f) * 1.0f;
+    const float lz = c.z * (A[2] + D[2] * diffuse) + ((S[2] * specular) * 10.0f) * 1.0f;
+    const float alpha = c.w < specular ? specular : c.w;
+    f4 r = {clamp01(lx), clamp01(ly), clamp01(lz), alpha};
+    return r;
+}
+
+/* Lighting (ColorKernels.h:43-78): colour of the hit, reflected direction,
+ * next origin 1e-5 along it. */
+static inline f4 lighting(float t, float u, float v, v3 *o, v3 *d, const float *n0, const float *n1,
+                          const float *n2, const uint8_t *c0, int prim, const or_light *L)
+{
+    const v3 pt = mk3(o->x + t * d->x, o->y + t * d->y, o->z + t * d->z);
+    const float w = (1.0f - u) - v;
+    const float *a = n0 + 4 * (size_t)prim, *b = n1 + 4 * (size_t)prim, *c = n2 + 4 * (size_t)prim;
+    const v3 n = nrm3(mk3((w * a[0] + u * b[0]) + v * c[0], (w * a[1] + u * b[1]) + v * c[1],
+                          (w * a[2] + u * b[2]) + v * c[2]));
+    const uint8_t *cc = c0 + 4 * (size_t)prim;
+    f4 col = {cc[0] / 255.0f, cc[1] / 255.0f, cc[2] / 255.0f, cc[3] / 255.0f};
+    const float k = 2.0f * dot3(n, mk3(-d->x, -d->y, -d->z));
+    const v3 nd = nrm3(mk3(k * n.x + d->x, k * n.y + d->y, k * n.z + d->z));
+    col = phong(col, n, pt, *o, L);
+    *o = mk3(pt.x + 0.00001f * nd.x, pt.y + 0.00001f * nd.y, pt.z + 0.00001f * nd.z);
+    *d = nd;
+    return col;
+}
+
+/* BlendColor (ColorKernels.h:80-85). */
+static inline f4 blend(f4 orig, f4 nc)
+{
+    const float k = (1.0f - orig.w) * nc.w;
+    f4 r = {orig.x + k * nc.x, orig.y + k * nc.y, orig.z + k * nc.z, orig.w + k * 1.0f};
+    return r;
+}
+
+void or_light_default(or_light *L)
+{
+    /* Raytracer.cu:43-51: light at (0,4,0), colour (1, 0.92, 0.8) scaled
+     * 0.3 / 0.7 / 0.3 for ambient / diffuse / specular. */
+    const float col[3] = {1.0f, 0.92f, 0.8f};
+    L->position[0] = 0.0f; L->position[1] = 4.0f; L->position[2] = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        L->ambient[k] = col[k] * 0.3f;
+        L->diffuse[k] = col[k] * 0.7f;
+        L->specular[k] = col[k] * 0.3f;
+    }
+}
+
+int or_trace_shaded(const or_tree *tr, const float *tri, int32_t T, const or_trace_params *p,
+                    const float *n0, const float *n1, const float *n2, const uint8_t *c0, const or_light *L,
+                    int32_t max_bounces, const float *ray_o, const float *ray_d, int32_t n, uint8_t *rgba,
+                    int32_t threads)
+{
+    if (!p || !L || !n0 || !n1 || !n2 || !c0 || n < 0 || max_bounces < 1 ||
+        (n > 0 && (!ray_o || !ray_d || !rgba)))
+        return OR_ERR_ARG;
+    if (p->tracer != OR_TRACER_BRUTE && (!tr || tr->n_nodes <= 0)) return OR_ERR_ARG;
+    const int nt = set_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(static, 64) num_threads(nt)
+    for (int32_t i = 0; i < n; ++i) {
+        v3 o = ld3(ray_o + 3 * (size_t)i), d = ld3(ray_d + 3 * (size_t)i);
+        if (p->tracer != OR_TRACER_BRUTE) d = adjust_dir(d);
+        f4 col = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int b = 0; b < max_bounces; ++b) {
+            int32_t h;
+            float t, u, v;
+            v3 dh = d;
+            if (p->tracer == OR_TRACER_BRUTE) trace_brute_one(tri, T, p->tie, o, d, &h, &t, &u, &v);
+            else if (p->tracer == OR_TRACER_SHORTSTACK) trace_shortstack_one(tr, tri, p, o, d, &h, &t, &u, &v, &dh);
+            else trace_restart_one(tr, tri, p, o, d, &h, &t, &u, &v, &dh);
+            if (h < 0) break;
+            d = dh;
+            col = blend(col, lighting(t, u, v, &o, &d, n0, n1, n2, c0, h, L));
+            if (p->tracer != OR_TRACER_BRUTE) d = adjust_dir(d);
+            if (!(col.w < 0.97f)) break;
+        }
+        uint8_t *px = rgba + 4 * (size_t)i;
+        px[0] = to_u8(col.x); px[1] = to_u8(col.y); px[2] = to_u8(col.z); px[3] = to_u8(col.w);
     }
     return 0;
 }

@@ -132,6 +132,27 @@ typedef struct or_photon_params {
 int or_trace_photons(const or_tree *tree, const float *tri, int32_t T, const or_trace_params *p,
                      const or_photon_params *ph, int32_t n, int32_t *seg_hit, float *seg_t, int32_t threads);
 
+/* Light of the shading loop (ColorKernels.h:10-13 constants). */
+typedef struct or_light {
+    float position[3], ambient[3], diffuse[3], specular[3];
+} or_light;
+
+/* The reference's defaults (Raytracer.cu:43-51). */
+void or_light_default(or_light *L);
+
+/* Shaded trace (Raytracer.cu:165-262 KDRestart, ShortStack.cu:100-190,
+ * BruteTracer.cu:54-96 Exhaustive with ColorKernels.h:15-85): per ray, hit,
+ * Phong-shade, reflect and continue until the ray escapes, the accumulated
+ * alpha reaches 0.97 or max_bounces hits were shaded.  n0/n1/n2: T float4
+ * vertex normals per triangle; c0: T uchar4 colours; rgba: n uchar4. */
+int or_trace_shaded(const or_tree *tr, const float *tri, int32_t T, const or_trace_params *p,
+                    const float *n0, const float *n1, const float *n2, const uint8_t *c0, const or_light *L,
+                    int32_t max_bounces, const float *ray_o, const float *ray_d, int32_t n, uint8_t *rgba,
+                    int32_t threads);
+
+/* The x^y of the specular term (exported for tests). */
+float or_kpow(float x, float y);
+
 /* Philox4x32-10 block (exported for tests). */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

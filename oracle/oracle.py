@@ -258,6 +258,48 @@ def trace_photons(tree: Tree, tris, n: int, light=(0.5, 0.5, 0.5), seed: int = 3
     return hit, t
 
 
+class Light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("ambient", C.c_float * 3), ("diffuse", C.c_float * 3),
+                ("specular", C.c_float * 3)]
+
+
+def light(**kw) -> Light:
+    L = Light()
+    lib().or_light_default(C.byref(L))
+    for k, v in kw.items():
+        setattr(L, k, (C.c_float * 3)(*[float(x) for x in v]))
+    return L
+
+
+def trace_shaded(tree: Tree | None, tris, o, d, n0, n1, n2, c0, light_params: Light | None = None,
+                 max_bounces: int = 64, threads: int = 0, **kw):
+    """Shaded RGBA8 pixels (n, 4) uint8 (or_trace_shaded)."""
+    L = lib()
+    L.or_trace_shaded.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(TraceParams), C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.POINTER(Light), C.c_int32, C.c_void_p, C.c_void_p,
+                                  C.c_int32, C.c_void_p, C.c_int32]
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    o, d = _rays(o, d)
+    n0, n1, n2 = (np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 4) for x in (n0, n1, n2))
+    c0 = np.ascontiguousarray(c0, dtype=np.uint8).reshape(-1, 4)
+    p = trace_params(**kw)
+    lp = light_params if light_params is not None else light()
+    out = np.empty((o.shape[0], 4), np.uint8)
+    s = tree.as_struct() if tree is not None else None
+    _check(L.or_trace_shaded(C.c_void_p(C.addressof(s)) if s is not None else None, _ptr(tris), tris.shape[0],
+                             C.byref(p), _ptr(n0), _ptr(n1), _ptr(n2), _ptr(c0), C.byref(lp), max_bounces, _ptr(o),
+                             _ptr(d), o.shape[0], _ptr(out), threads))
+    return out
+
+
+def kpow(x: float, y: float) -> float:
+    """The specular power restated from series (or_kpow)."""
+    L = lib()
+    L.or_kpow.argtypes = [C.c_float, C.c_float]
+    L.or_kpow.restype = C.c_float
+    return float(L.or_kpow(x, y))
+
+
 def philox4x32_10(ctr, key):
     L = lib()
     L.or_philox4x32_10.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
