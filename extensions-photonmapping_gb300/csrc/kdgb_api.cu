@@ -609,6 +609,35 @@ int kdgb_trace_shaded(const kdgb_tree *tree, const kdgb_trace_params *params, co
                         ray_d_dev, n, rgba_dev, (cudaStream_t)stream);
 }
 
+int kdgb_trace_brute_shaded(const float *tri_v_dev, int32_t n_tris, int32_t tie, const float *n0_dev,
+                            const float *n1_dev, const float *n2_dev, const uint8_t *c0_dev, const kdgb_light *light,
+                            int32_t max_bounces, const float *ray_o_dev, const float *ray_d_dev, int32_t n,
+                            uint8_t *rgba_dev, kdgb_stream_t stream)
+{
+    if (n_tris < 0 || n < 0 || (n_tris > 0 && !tri_v_dev)) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (tie != KDGB_TIE_LOWEST_ID && tie != KDGB_TIE_REF_LAST) return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown tie rule");
+    if (max_bounces < 0 || max_bounces > 1024) return fail(KDGB_ERR_INVALID_ARGUMENT, "max_bounces must be in 0..1024");
+    kdgb_light L;
+    if (light) L = *light; else kdgb_light_default(&L);
+    if (n == 0) return KDGB_OK;
+    if (!ray_o_dev || !ray_d_dev || !rgba_dev) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    if (n_tris > 0 && (!n0_dev || !n1_dev || !n2_dev || !c0_dev))
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL normal or colour buffer");
+    KDGB_CHECK(check_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    kdgb_trace_params p;
+    kdgb_trace_params_default(&p);
+    p.tracer = KDGB_TRACER_BRUTE;
+    p.tie = tie;
+    Tree t;
+    int rc = load_geometry(t, tri_v_dev, n_tris, s);
+    if (rc == KDGB_OK)
+        rc = shade_launch(t, p, n0_dev, n1_dev, n2_dev, c0_dev, L, max_bounces > 0 ? max_bounces : 64, ray_o_dev,
+                          ray_d_dev, n, rgba_dev, s);
+    release_all(t, s);
+    return rc;
+}
+
 int kdgb_build_batch(const float *tri_v_dev, const int32_t *mesh_offsets, int32_t n_meshes,
                      const kdgb_build_params *params, kdgb_tree **out, kdgb_stream_t stream)
 {

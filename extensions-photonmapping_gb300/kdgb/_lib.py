@@ -110,6 +110,8 @@ SIGNATURES = {
     "kdgb_light_default": (None, [C.POINTER(Light)]),
     "kdgb_trace_shaded": (C.c_int, [P, C.POINTER(TraceParams), P, P, P, P, C.POINTER(Light), C.c_int32, P, P,
                                     C.c_int32, P, P]),
+    "kdgb_trace_brute_shaded": (C.c_int, [P, C.c_int32, C.c_int32, P, P, P, P, C.POINTER(Light), C.c_int32, P, P,
+                                          C.c_int32, P, P]),
     "kdgb_osc_update_surface": (C.c_int, [P, P, C.c_int32, C.c_float, C.c_float, P]),
     "kdgb_backward": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, C.c_int32, P, P, P, P, P, P]),
     "kdgb_trace_brute": (C.c_int, [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, P]),

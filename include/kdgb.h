@@ -259,6 +259,14 @@ KDGB_API int kdgb_trace_shaded(const kdgb_tree *tree, const kdgb_trace_params *p
                                const kdgb_light *light, int32_t max_bounces, const float *ray_o_dev,
                                const float *ray_d_dev, int32_t n, uint8_t *rgba_dev, kdgb_stream_t stream);
 
+/* BruteTracer::Trace's pixels without a tree (BruteTracer.cu:54-96 with the
+ * shading of ColorKernels.h:15-85): as kdgb_trace_shaded with
+ * KDGB_TRACER_BRUTE over n_tris device triangles. */
+KDGB_API int kdgb_trace_brute_shaded(const float *tri_v_dev, int32_t n_tris, int32_t tie, const float *n0_dev,
+                                     const float *n1_dev, const float *n2_dev, const uint8_t *c0_dev,
+                                     const kdgb_light *light, int32_t max_bounces, const float *ray_o_dev,
+                                     const float *ray_d_dev, int32_t n, uint8_t *rgba_dev, kdgb_stream_t stream);
+
 /* Batched build (no reference counterpart; the reference builds one scene
  * per TriangleMap): n_meshes independent meshes stored back to back in
  * tri_v_dev (mesh m = triangles [mesh_offsets[m], mesh_offsets[m+1]),

@@ -190,31 +190,57 @@ namespace CUDA {
 class GeometryList {
 public:
     // AddMesh(CUDAMeshNode*, model matrix) (GeometryList.cu:318-341); the
-    // matrix is row major and applied as Matrix44f * float4.
-    void AddMesh(const Scene::CUDAMeshNode &mesh, const float model[16] = nullptr, cudaStream_t s = 0)
+    // model matrix is row major and applied as Matrix44f * float4, the
+    // normal matrix (row major 3x3, NULL = identity) to the normals.  Fills
+    // the triangle buffer and the per-triangle normals n0/n1/n2 and colour
+    // c0 (GeometryList.h:41-47).
+    void AddMesh(const Scene::CUDAMeshNode &mesh, const float model[16] = nullptr,
+                 const float normal_matrix[9] = nullptr, cudaStream_t s = 0)
     {
         const int32_t tris = (int32_t)mesh.GetSize() / 3;
         const size_t old = (size_t)size_;
-        if ((size_t)(size_ + tris) * 9 > tri_.n) {
-            detail::DeviceBuffer<float> bigger;
-            bigger.resize((size_t)(size_ + tris) * 9 * 2);
-            if (old) detail::cuda(cudaMemcpy(bigger.p, tri_.p, old * 9 * sizeof(float), cudaMemcpyDeviceToDevice),
-                                  "cudaMemcpy");
-            std::swap(bigger.p, tri_.p);
-            std::swap(bigger.n, tri_.n);
+        if ((size_t)(size_ + tris) > cap_) {
+            const size_t cap = (size_t)(size_ + tris) * 2;
+            grow(tri_, old * 9, cap * 9);
+            grow(n0_, old * 4, cap * 4);
+            grow(n1_, old * 4, cap * 4);
+            grow(n2_, old * 4, cap * 4);
+            grow(c0_, old * 4, cap * 4);
+            cap_ = cap;
         }
         detail::check(kdgb_geometry_gather(reinterpret_cast<const float *>(mesh.GetVertexData()),
                                            (int32_t)mesh.GetVertexCount(), mesh.GetIndexData(), (int32_t)mesh.GetSize(),
                                            model, tri_.p + old * 9, s),
+                      "GeometryList::AddMesh");
+        detail::check(kdgb_geometry_gather_attributes(
+                          reinterpret_cast<const float *>(mesh.GetNormalData()),
+                          reinterpret_cast<const uint8_t *>(mesh.GetColorData()), (int32_t)mesh.GetVertexCount(),
+                          mesh.GetIndexData(), (int32_t)mesh.GetSize(), normal_matrix, n0_.p + old * 4, n1_.p + old * 4,
+                          n2_.p + old * 4, c0_.p + old * 4, s),
                       "GeometryList::AddMesh");
         size_ += tris;
     }
     void Clear() { size_ = 0; }
     int GetSize() const { return size_; }
     const float *GetTriangleData() const { return tri_.p; }
+    const float *GetNormal0Data() const { return n0_.p; }
+    const float *GetNormal1Data() const { return n1_.p; }
+    const float *GetNormal2Data() const { return n2_.p; }
+    const uint8_t *GetColor0Data() const { return c0_.p; }
 
 private:
-    detail::DeviceBuffer<float> tri_;
+    template <class T>
+    static void grow(detail::DeviceBuffer<T> &b, size_t keep, size_t n)
+    {
+        detail::DeviceBuffer<T> bigger;
+        bigger.resize(n);
+        if (keep) detail::cuda(cudaMemcpy(bigger.p, b.p, keep * sizeof(T), cudaMemcpyDeviceToDevice), "cudaMemcpy");
+        std::swap(bigger.p, b.p);
+        std::swap(bigger.n, b.n);
+    }
+    detail::DeviceBuffer<float> tri_, n0_, n1_, n2_;
+    detail::DeviceBuffer<uint8_t> c0_;
+    size_t cap_ = 0;
     int size_ = 0;
 };
 
@@ -309,6 +335,11 @@ public:
 
     virtual void Trace(const float *origins, const float *directions, int n, int *hit, float *t, float *u, float *v,
                        cudaStream_t s = 0) = 0;
+    // Trace(IRenderCanvas*, uchar4* canvasData) (Raytracer.cu:295): the
+    // shaded pixels of n rays (a width-wide image when Params().tile_width is
+    // set) into canvasData, with Light() as the scene light.
+    virtual void Trace(const float *origins, const float *directions, int n, uchar4 *canvasData,
+                       cudaStream_t s = 0) = 0;
 
     void SetIntersectionAlgorithm(const IntersectionAlgorithm a)
     {
@@ -319,6 +350,7 @@ public:
     bool GetLeafSkipping() const { return p_.leaf_skipping != 0; }
     float GetRenderTime() const { return renderTime_; }
     kdgb_trace_params &Params() { return p_; }
+    kdgb_light &Light() { return light_; }
 
 protected:
     void TraceTree(const kdgb_tree *tree, bool propagate, const float *o, const float *d, int n, int *hit, float *t,
@@ -326,20 +358,44 @@ protected:
     {
         kdgb_trace_params p = p_;
         if (!propagate) p.leaf_skipping = 0;  // Raytracer.cu:313
+        Timed([&] { return kdgb_trace(tree, &p, o, d, n, hit, t, u, v, s); }, "IRayTracer::Trace", s);
+    }
+    template <class F>
+    void Timed(F &&f, const char *where, cudaStream_t s)
+    {
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, s);
-        const int rc = kdgb_trace(tree, &p, o, d, n, hit, t, u, v, s);
+        const int rc = f();
         cudaEventRecord(e1, s);
         cudaEventSynchronize(e1);
         cudaEventElapsedTime(&renderTime_, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        detail::check(rc, "IRayTracer::Trace");
+        detail::check(rc, where);
+    }
+    void ShadeTree(const kdgb_tree *tree, bool propagate, const GeometryList *g, const float *o, const float *d, int n,
+                   uchar4 *canvas, cudaStream_t s)
+    {
+        kdgb_trace_params p = p_;
+        if (!propagate) p.leaf_skipping = 0;
+        Timed([&] {
+            return kdgb_trace_shaded(tree, &p, g->GetNormal0Data(), g->GetNormal1Data(), g->GetNormal2Data(),
+                                     g->GetColor0Data(), &light_, 0, o, d, n, reinterpret_cast<uint8_t *>(canvas), s);
+        }, "IRayTracer::Trace", s);
     }
     kdgb_trace_params p_;
+    kdgb_light light_ = DefaultLight();
     float renderTime_ = 0.0f;
+
+private:
+    static kdgb_light DefaultLight()
+    {
+        kdgb_light l;
+        kdgb_light_default(&l);
+        return l;
+    }
 };
 
 class RayTracer : public IRayTracer {
@@ -348,6 +404,10 @@ public:
     void Trace(const float *o, const float *d, int n, int *hit, float *t, float *u, float *v, cudaStream_t s = 0) override
     {
         TraceTree(map_->Handle(), map_->GetPropagateBoundingBox(), o, d, n, hit, t, u, v, s);
+    }
+    void Trace(const float *o, const float *d, int n, uchar4 *canvas, cudaStream_t s = 0) override
+    {
+        ShadeTree(map_->Handle(), map_->GetPropagateBoundingBox(), map_->GetGeometry(), o, d, n, canvas, s);
     }
 
 private:
@@ -360,6 +420,10 @@ public:
     void Trace(const float *o, const float *d, int n, int *hit, float *t, float *u, float *v, cudaStream_t s = 0) override
     {
         TraceTree(map_->Handle(), map_->GetPropagateBoundingBox(), o, d, n, hit, t, u, v, s);
+    }
+    void Trace(const float *o, const float *d, int n, uchar4 *canvas, cudaStream_t s = 0) override
+    {
+        ShadeTree(map_->Handle(), map_->GetPropagateBoundingBox(), map_->GetGeometry(), o, d, n, canvas, s);
     }
 
 private:
@@ -374,6 +438,15 @@ public:
     {
         detail::check(kdgb_trace_brute(geom_->GetTriangleData(), geom_->GetSize(), p_.tie, o, d, n, hit, t, u, v, s),
                       "BruteTracer::Trace");
+    }
+    void Trace(const float *o, const float *d, int n, uchar4 *canvas, cudaStream_t s = 0) override
+    {
+        const GeometryList *g = geom_;
+        Timed([&] {
+            return kdgb_trace_brute_shaded(g->GetTriangleData(), g->GetSize(), p_.tie, g->GetNormal0Data(),
+                                           g->GetNormal1Data(), g->GetNormal2Data(), g->GetColor0Data(), &light_, 0, o,
+                                           d, n, reinterpret_cast<uint8_t *>(canvas), s);
+        }, "BruteTracer::Trace", s);
     }
 
 private:

@@ -4,7 +4,9 @@
 // trace one frame.  Writes everything the test needs to compare with the
 // oracle to the file named by argv[1]:
 //   int32 T, int32 n, float tris[T*9], float o[n*3], float d[n*3],
-//   then for restart, short-stack, brute: int32 hit[n], float t[n].
+//   then for restart, short-stack, brute: int32 hit[n], float t[n],
+//   then float n0/n1/n2[T*4], uint8 c0[T*4] (the GeometryList attributes),
+//   then for restart, short-stack, brute: uint8 rgba[n*4] (shaded Trace).
 #include <cstdio>
 #include <vector>
 
@@ -85,6 +87,22 @@ int main(int argc, char **argv)
         cudaMemcpy(th.data(), t, 4 * n, cudaMemcpyDeviceToHost);
         std::fwrite(h.data(), 4, n, f);
         std::fwrite(th.data(), 4, n, f);
+    }
+    std::vector<float> nrm(4 * (size_t)T);
+    for (const float *src : {geom.GetNormal0Data(), geom.GetNormal1Data(), geom.GetNormal2Data()}) {
+        cudaMemcpy(nrm.data(), src, nrm.size() * 4, cudaMemcpyDeviceToHost);
+        std::fwrite(nrm.data(), 4, nrm.size(), f);
+    }
+    std::vector<unsigned char> bytes(4 * (size_t)T);
+    cudaMemcpy(bytes.data(), geom.GetColor0Data(), bytes.size(), cudaMemcpyDeviceToHost);
+    std::fwrite(bytes.data(), 1, bytes.size(), f);
+    uchar4 *canvas;
+    cudaMalloc(&canvas, 4 * n);
+    std::vector<unsigned char> px(4 * (size_t)n);
+    for (IRayTracer *tr : tracers) {
+        tr->Trace(od, dd, n, canvas);
+        cudaMemcpy(px.data(), canvas, px.size(), cudaMemcpyDeviceToHost);
+        std::fwrite(px.data(), 1, px.size(), f);
     }
     std::fclose(f);
     std::printf("plugin demo: %d triangles, %d nodes, build %.3f ms\n", T, map.GetNodes()->GetSize(),

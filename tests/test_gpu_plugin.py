@@ -45,14 +45,26 @@ def test_cpp_plugin_frame_matches_oracle(kdgb_lib, cuda, oracle, tmp_path):
         h = np.frombuffer(raw[off:off + 4 * n].tobytes(), np.int32); off += 4 * n
         t = np.frombuffer(raw[off:off + 4 * n].tobytes(), np.float32); off += 4 * n
         res.append((h, t))
+    nrm = []
+    for _ in range(3):
+        nrm.append(np.frombuffer(raw[off:off + 16 * T].tobytes(), np.float32).reshape(T, 4)); off += 16 * T
+    c0 = raw[off:off + 4 * T].reshape(T, 4); off += 4 * T
+    pixels = []
+    for _ in range(3):
+        pixels.append(raw[off:off + 4 * n].reshape(n, 4)); off += 4 * n
+    assert off == raw.shape[0]
     assert T == 2 * 48 * 48
     tree = oracle.build(tris, lower=1)  # TriangleMap defaults + SetLowerAlgorithm(SAH)
-    for (h, t), tracer in zip(res, (0, 1, 2)):
+    for (h, t), px, tracer in zip(res, pixels, (0, 1, 2)):
         hr, tr, _, _ = oracle.trace(tree, tris, o, d, tracer=tracer)
         assert np.array_equal(h, hr), tracer
         m = hr >= 0
         assert np.array_equal(t[m].view(np.uint32), tr[m].view(np.uint32))
         assert m.mean() > 0.5
+        want = oracle.trace_shaded(tree if tracer != 2 else None, tris, o, d, nrm[0], nrm[1], nrm[2], c0,
+                                   tracer=tracer)
+        assert np.array_equal(px, want), tracer
+        assert (px[m, 3] > 0).all()
 
 
 def test_geometry_gather_matches_numpy(kdgb_lib, cuda):
