@@ -20,8 +20,9 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
                  const int32_t *ray_mesh = nullptr, int32_t rays_per_mesh = 0);
 int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, int64_t n, const float *light,
                   int32_t *occ, cudaStream_t s);
-int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, int32_t T, int tie, const float *o,
-                 const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv, cudaStream_t s);
+int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, const float4 *woop, int32_t T, int tie,
+                 const float *o, const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv,
+                 cudaStream_t s);
 int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_params &ph, int64_t n,
                   int32_t *seg_hit, float *seg_t, cudaStream_t s);
 int shade_launch(const Tree &t, const kdgb_trace_params &p, const float *n0, const float *n1, const float *n2,
@@ -111,7 +112,8 @@ static void release_all(Tree &t, cudaStream_t s)
     release(t.info, s); release(t.split, s); release(t.bmin, s); release(t.bmax, s);
     release(t.pidx, s); release(t.bitmap, s); release(t.parent, s); release(t.children, s);
     release(t.area, s); release(t.prim_indices, s); release(t.leaf_ids, s);
-    release(t.tnode, s); release(t.ttri, s); release(t.mesh_off, s);
+    release(t.tnode, s); release(t.ttri, s); release(t.mesh_off, s); release(t.woop, s);
+    t.woop_valid = false;
     Workspace &w = t.ws;
     for (int b = 0; b < 2; ++b) {
         release(w.rmin[b], s);
@@ -178,6 +180,8 @@ static int validate_trace_params(const kdgb_trace_params &p, int64_t n)
         return fail(KDGB_ERR_INVALID_ARGUMENT, "block_size must be 0 or a multiple of 32 up to 1024");
     if (p.max_iterations < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "max_iterations must be >= 0");
     if (p.tile_width < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "tile_width must be >= 0");
+    if (p.intersection != KDGB_ISECT_MOELLER && p.intersection != KDGB_ISECT_WOOP)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown intersection algorithm");
     if (p.tile_width > 0 && (p.tile_width % 4 != 0 || n % ((int64_t)p.tile_width * 8) != 0))
         return fail(KDGB_ERR_INVALID_ARGUMENT, "tile_width needs width % 4 == 0 and height % 8 == 0");
     return KDGB_OK;
@@ -284,6 +288,7 @@ void kdgb_trace_params_default(kdgb_trace_params *p)
     p->max_iterations = 0;
     p->block_size = 0;
     p->tile_width = 0;
+    p->intersection = KDGB_ISECT_MOELLER;
 }
 
 int kdgb_build(const float *tri_v_dev, int32_t n_tris, const kdgb_build_params *params, kdgb_tree **out,
@@ -496,9 +501,15 @@ int kdgb_trace(const kdgb_tree *tree, const kdgb_trace_params *params, const flo
     const Tree &t = tree->t;
     if (t.n_meshes > 1) return fail(KDGB_ERR_INVALID_ARGUMENT, "batched tree: use kdgb_trace_batch");
     cudaStream_t s = (cudaStream_t)stream;
-    if (p.tracer == KDGB_TRACER_BRUTE)
-        return brute_launch(t.p0.p, t.p1.p, t.p2.p, t.n_tris, p.tie, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev,
-                            v_dev, s);
+    if (p.tracer == KDGB_TRACER_BRUTE) {
+        const float4 *woop = nullptr;
+        if (p.intersection == KDGB_ISECT_WOOP) {
+            KDGB_CHECK(woop_values(t, s));
+            woop = t.woop.p;
+        }
+        return brute_launch(t.p0.p, t.p1.p, t.p2.p, woop, t.n_tris, p.tie, ray_o_dev, ray_d_dev, n, hit_dev, t_dev,
+                            u_dev, v_dev, s);
+    }
     return trace_launch(t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, nullptr, nullptr, s);
 }
 
@@ -609,13 +620,16 @@ int kdgb_trace_shaded(const kdgb_tree *tree, const kdgb_trace_params *params, co
                         ray_d_dev, n, rgba_dev, (cudaStream_t)stream);
 }
 
-int kdgb_trace_brute_shaded(const float *tri_v_dev, int32_t n_tris, int32_t tie, const float *n0_dev,
-                            const float *n1_dev, const float *n2_dev, const uint8_t *c0_dev, const kdgb_light *light,
-                            int32_t max_bounces, const float *ray_o_dev, const float *ray_d_dev, int32_t n,
-                            uint8_t *rgba_dev, kdgb_stream_t stream)
+int kdgb_trace_brute_shaded(const float *tri_v_dev, int32_t n_tris, const kdgb_trace_params *params,
+                            const float *n0_dev, const float *n1_dev, const float *n2_dev, const uint8_t *c0_dev,
+                            const kdgb_light *light, int32_t max_bounces, const float *ray_o_dev,
+                            const float *ray_d_dev, int32_t n, uint8_t *rgba_dev, kdgb_stream_t stream)
 {
     if (n_tris < 0 || n < 0 || (n_tris > 0 && !tri_v_dev)) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad arguments");
-    if (tie != KDGB_TIE_LOWEST_ID && tie != KDGB_TIE_REF_LAST) return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown tie rule");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    p.tracer = KDGB_TRACER_BRUTE;
+    KDGB_CHECK(validate_trace_params(p, n));
     if (max_bounces < 0 || max_bounces > 1024) return fail(KDGB_ERR_INVALID_ARGUMENT, "max_bounces must be in 0..1024");
     kdgb_light L;
     if (light) L = *light; else kdgb_light_default(&L);
@@ -625,15 +639,40 @@ int kdgb_trace_brute_shaded(const float *tri_v_dev, int32_t n_tris, int32_t tie,
         return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL normal or colour buffer");
     KDGB_CHECK(check_device());
     cudaStream_t s = (cudaStream_t)stream;
-    kdgb_trace_params p;
-    kdgb_trace_params_default(&p);
-    p.tracer = KDGB_TRACER_BRUTE;
-    p.tie = tie;
     Tree t;
     int rc = load_geometry(t, tri_v_dev, n_tris, s);
     if (rc == KDGB_OK)
         rc = shade_launch(t, p, n0_dev, n1_dev, n2_dev, c0_dev, L, max_bounces > 0 ? max_bounces : 64, ray_o_dev,
                           ray_d_dev, n, rgba_dev, s);
+    release_all(t, s);
+    return rc;
+}
+
+int kdgb_trace_brute_ex(const float *tri_v_dev, int32_t n_tris, const kdgb_trace_params *params,
+                        const float *ray_o_dev, const float *ray_d_dev, int32_t n, int32_t *hit_dev, float *t_dev,
+                        float *u_dev, float *v_dev, kdgb_stream_t stream)
+{
+    if (n_tris < 0 || n < 0 || (n_tris > 0 && !tri_v_dev)) return fail(KDGB_ERR_INVALID_ARGUMENT, "bad arguments");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    p.tracer = KDGB_TRACER_BRUTE;
+    p.tile_width = 0;
+    KDGB_CHECK(validate_trace_params(p, n));
+    if (n == 0) return KDGB_OK;
+    if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    KDGB_CHECK(check_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    Tree t;
+    int rc = load_geometry(t, tri_v_dev, n_tris, s);
+    const float4 *woop = nullptr;
+    if (rc == KDGB_OK && p.intersection == KDGB_ISECT_WOOP) {
+        rc = woop_values(t, s);
+        woop = t.woop.p;
+    }
+    if (rc == KDGB_OK)
+        rc = brute_launch(t.p0.p, t.p1.p, t.p2.p, woop, n_tris, p.tie, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev,
+                          v_dev, s);
     release_all(t, s);
     return rc;
 }
@@ -717,7 +756,8 @@ int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t tie, const 
     Tree t;
     int rc = load_geometry(t, tri_v_dev, n_tris, s);
     if (rc == KDGB_OK)
-        rc = brute_launch(t.p0.p, t.p1.p, t.p2.p, n_tris, tie, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, s);
+        rc = brute_launch(t.p0.p, t.p1.p, t.p2.p, nullptr, n_tris, tie, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev,
+                          v_dev, s);
     release_all(t, s);
     return rc;
 }
@@ -767,6 +807,11 @@ int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris, c
                                   cudaMemcpyHostToDevice, s));
     }
     KDGB_CHECK(reserve_for_graph(t, n_tris, p, n_meshes, headroom, s));
+    if (n_rays > 0 && tp.intersection == KDGB_ISECT_WOOP) {
+        // The graph recomputes the Woop rows from the rebuilt geometry.
+        KDGB_CHECK(ensure(t.woop, 3 * (int64_t)std::max(n_tris, 1), s));
+        t.woop_valid = false;
+    }
     KDGB_CUDA(cudaStreamSynchronize(s));
 
     kdgb_graph *g = new (std::nothrow) kdgb_graph();
@@ -820,6 +865,7 @@ int kdgb_graph_launch(kdgb_graph *graph, kdgb_stream_t stream)
     if (layout_signature(graph->tree->t) != graph->signature)
         return fail(KDGB_ERR_INVALID_ARGUMENT, "the tree's buffers changed since the graph was created");
     KDGB_CUDA(cudaGraphLaunch(graph->exec, (cudaStream_t)stream));
+    graph->tree->t.woop_valid = false;  // the geometry may have moved
     note_launch((int)graph->per_launch);
     return KDGB_OK;
 }

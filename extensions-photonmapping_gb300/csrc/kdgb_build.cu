@@ -1698,6 +1698,7 @@ void apply_state(Tree &t, const BuildState &st)
 
 int geometry_arrays(Tree &t, int32_t T, cudaStream_t s)
 {
+    t.woop_valid = false;  // the Woop rows follow the geometry
     KDGB_CHECK(ensure(t.p0, T, s));
     KDGB_CHECK(ensure(t.p1, T, s));
     KDGB_CHECK(ensure(t.p2, T, s));

@@ -151,9 +151,17 @@ struct Tree {
     DevArray<int4> tnode;
     DevArray<float4> ttri;
 
+    // Woop transform rows (m0, m1, m2) per triangle, computed on the first
+    // Woop trace after a build (a cache: traces of a const handle fill it).
+    mutable DevArray<float4> woop;
+    mutable bool woop_valid = false;
+
     Workspace ws;
     BuildPlan plan;
 };
+
+// Makes t.woop current (kdgb_trace.cu).
+int woop_values(const Tree &t, cudaStream_t s);
 
 // Builder (kdgb_build.cu), both modes, host-driven.  tri_v_dev: T*9 floats.
 // With M > 1 the triangles are M meshes (mesh m = [mesh_off[m],

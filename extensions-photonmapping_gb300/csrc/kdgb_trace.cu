@@ -21,6 +21,8 @@
 // same fp32 values the reference computes per test.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kdgb_internal.cuh"
 #include "kdgb_photon.cuh"
 
@@ -40,6 +42,7 @@ struct Ctx {
     const float4 *__restrict__ bmin;
     const float4 *__restrict__ bmax;
     const float4 *__restrict__ tri;
+    const float4 *__restrict__ woop;  // per-triangle Woop values, or NULL for Moeller-Trumbore
     int root;  // root node of the ray's tree (forest of a batch: its mesh index)
 };
 
@@ -103,11 +106,56 @@ __device__ __forceinline__ bool ray_box(float3 o, float3 inv, float4 bmin, float
     return n <= f;
 }
 
+// Woop's test (IRayTracer.h:78-109) against the triangle's transform rows
+// m0, m1, m2 (GeometryList.cu:81-102): lambda = -(m2.o - m2.w) / (m2.d),
+// u = lambda (m0.d) + m0.o - m0.w, v likewise with m1.
+__device__ __forceinline__ float woop_lambda(float4 m2, float3 o, float3 d)
+{
+    const float3 n2 = make_float3(m2.x, m2.y, m2.z);
+    return __fdiv_rn(-__fsub_rn(dot3(n2, o), m2.w), dot3(n2, d));
+}
+
+__device__ __forceinline__ void woop_accept(float lambda, float4 m0, float4 m1, int id, float3 o, float3 d, int tie,
+                                            int &hit, float &tb, float &ub, float &vb)
+{
+    const float3 n0 = make_float3(m0.x, m0.y, m0.z), n1 = make_float3(m1.x, m1.y, m1.z);
+    const float hu = __fsub_rn(__fadd_rn(__fmul_rn(lambda, dot3(n0, d)), dot3(n0, o)), m0.w);
+    const float hv = __fsub_rn(__fadd_rn(__fmul_rn(lambda, dot3(n1, d)), dot3(n1, o)), m1.w);
+    if (hu >= -0.0f && hv >= -0.0f && __fadd_rn(hu, hv) <= 1.0f) {
+        if (tie == KDGB_TIE_REF_LAST || hit == -1 || lambda < tb || id < hit) {
+            hit = id; tb = lambda; ub = hu; vb = hv;
+        }
+    }
+}
+
+// The rows in registers (brute-force tiles).
+__device__ __forceinline__ void woop_test(float4 m0, float4 m1, float4 m2, int id, float3 o, float3 d, int tie,
+                                          int &hit, float &tb, float &ub, float &vb)
+{
+    const float lambda = woop_lambda(m2, o, d);
+    if (0.0f <= lambda && lambda <= tb) woop_accept(lambda, m0, m1, id, o, d, tie, hit, tb, ub, vb);
+}
+
+// The rows in global memory: m0 and m1 are loaded only when lambda passes.
+__device__ __forceinline__ void woop_test(const float4 *__restrict__ w, int id, float3 o, float3 d, int tie, int &hit,
+                                          float &tb, float &ub, float &vb)
+{
+    const float lambda = woop_lambda(__ldg(w + 2), o, d);
+    if (0.0f <= lambda && lambda <= tb) woop_accept(lambda, __ldg(w), __ldg(w + 1), id, o, d, tie, hit, tb, ub, vb);
+}
+
 __device__ __forceinline__ int leaf_test(const Ctx &c, int4 leaf, float3 o, float3 d, int tie, float &tb, float &ub,
                                          float &vb)
 {
     int hit = -1;
-    for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) mt_record(c.tri, r, o, d, tie, hit, tb, ub, vb);
+    if (c.woop) {
+        for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) {
+            const int id = __float_as_int(__ldg(c.tri + 3 * (int64_t)r + 2).y);
+            woop_test(c.woop + 3 * (int64_t)id, id, o, d, tie, hit, tb, ub, vb);
+        }
+    } else {
+        for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) mt_record(c.tri, r, o, d, tie, hit, tb, ub, vb);
+    }
     return hit;
 }
 
@@ -349,10 +397,12 @@ __global__ void k_shadow(TraceArgs a)
 // order; triangles are staged through shared memory one tile at a time.
 constexpr int kBruteBlock = 128;
 
+// With `woop` set the tiles hold the Woop rows (m0, m1, m2) instead.
 __global__ void __launch_bounds__(kBruteBlock) k_brute(const float4 *__restrict__ p0, const float4 *__restrict__ p1,
-                                                      const float4 *__restrict__ p2, int32_t T, int tie,
-                                                      const float *__restrict__ ro, const float *__restrict__ rd,
-                                                      int64_t n, int32_t *hit, float *ot, float *ou, float *ov)
+                                                      const float4 *__restrict__ p2, const float4 *__restrict__ woop,
+                                                      int32_t T, int tie, const float *__restrict__ ro,
+                                                      const float *__restrict__ rd, int64_t n, int32_t *hit,
+                                                      float *ot, float *ou, float *ov)
 {
     __shared__ float4 sa[kBruteBlock], sb[kBruteBlock], sc[kBruteBlock];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -363,7 +413,11 @@ __global__ void __launch_bounds__(kBruteBlock) k_brute(const float4 *__restrict_
     float tb = KDGB_FINF, ub = 0.0f, vb = 0.0f;
     for (int32_t base = 0; base < T; base += kBruteBlock) {
         const int32_t j = base + threadIdx.x;
-        if (j < T) {
+        if (j < T && woop) {
+            sa[threadIdx.x] = woop[3 * (int64_t)j];
+            sb[threadIdx.x] = woop[3 * (int64_t)j + 1];
+            sc[threadIdx.x] = woop[3 * (int64_t)j + 2];
+        } else if (j < T) {
             const float4 a = p0[j], b = p1[j], c = p2[j];
             const float3 v0 = make_float3(a.x, a.y, a.z);
             const float3 e1 = sub3(make_float3(b.x, b.y, b.z), v0);
@@ -374,7 +428,9 @@ __global__ void __launch_bounds__(kBruteBlock) k_brute(const float4 *__restrict_
         }
         __syncthreads();
         const int m = min(kBruteBlock, T - base);
-        if (live) {
+        if (live && woop) {
+            for (int k = 0; k < m; ++k) woop_test(sa[k], sb[k], sc[k], base + k, o, d, tie, h, tb, ub, vb);
+        } else if (live) {
             for (int k = 0; k < m; ++k) {
                 const float4 a = sa[k], b = sb[k], c = sc[k];
                 mt_test(make_float3(a.x, a.y, a.z), make_float3(a.w, b.x, b.y), make_float3(b.z, b.w, c.x),
@@ -574,6 +630,10 @@ __device__ __forceinline__ int brute_hit(const ShadeArgs &a, float3 o, float3 d,
     int hit = -1;
     float tb = KDGB_FINF, ub = 0.0f, vb = 0.0f;
     for (int32_t i = 0; i < a.T; ++i) {
+        if (a.c.woop) {
+            woop_test(a.c.woop + 3 * (int64_t)i, i, o, d, a.tie, hit, tb, ub, vb);
+            continue;
+        }
         const float4 A = __ldg(a.p0 + i), B = __ldg(a.p1 + i), C = __ldg(a.p2 + i);
         const float3 v0 = make_float3(A.x, A.y, A.z);
         mt_test(v0, sub3(make_float3(B.x, B.y, B.z), v0), sub3(make_float3(C.x, C.y, C.z), v0), i, o, d, a.tie, hit,
@@ -639,7 +699,61 @@ __global__ void k_shade(ShadeArgs a)
                             (unsigned char)to_u8(col.w));
 }
 
+// CreateWoopValues (GeometryList.cu:81-102): WoopTransformationMatrix
+// (IntersectionTests.h:438-467) of (p1, p2, p0), the inverse of the matrix
+// whose columns are a - c, b - c and (a - c) x (b - c) - c, rows scaled by
+// 1/det, each row's w = row . c.
+__global__ void k_woop_values(const float4 *__restrict__ p0, const float4 *__restrict__ p1,
+                              const float4 *__restrict__ p2, int32_t T, float4 *__restrict__ out)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= T) return;
+    const float4 A = p1[i], B = p2[i], C = p0[i];
+    const float3 a = make_float3(A.x, A.y, A.z), b = make_float3(B.x, B.y, B.z), c = make_float3(C.x, C.y, C.z);
+    const float3 m0 = sub3(a, c), m1 = sub3(b, c), m2 = sub3(cross3(m0, m1), c);
+    const float det = __fadd_rn(
+        __fadd_rn(__fmul_rn(m0.x, __fsub_rn(__fmul_rn(m1.y, m2.z), __fmul_rn(m1.z, m2.y))),
+                  __fmul_rn(m1.x, __fsub_rn(__fmul_rn(m2.y, m0.z), __fmul_rn(m2.z, m0.y)))),
+        __fmul_rn(m2.x, __fsub_rn(__fmul_rn(m0.y, m1.z), __fmul_rn(m0.z, m1.y))));
+    const float inv = __fdiv_rn(1.0f, det);
+    const float3 r0 = make_float3(__fmul_rn(__fsub_rn(__fmul_rn(m1.y, m2.z), __fmul_rn(m1.z, m2.y)), inv),
+                                  __fmul_rn(__fsub_rn(__fmul_rn(m2.x, m1.z), __fmul_rn(m2.z, m1.x)), inv),
+                                  __fmul_rn(__fsub_rn(__fmul_rn(m1.x, m2.y), __fmul_rn(m1.y, m2.x)), inv));
+    const float3 r1 = make_float3(__fmul_rn(__fsub_rn(__fmul_rn(m2.y, m0.z), __fmul_rn(m2.z, m0.y)), inv),
+                                  __fmul_rn(__fsub_rn(__fmul_rn(m0.x, m2.z), __fmul_rn(m0.z, m2.x)), inv),
+                                  __fmul_rn(__fsub_rn(__fmul_rn(m2.x, m0.y), __fmul_rn(m2.y, m0.x)), inv));
+    const float3 r2 = make_float3(__fmul_rn(__fsub_rn(__fmul_rn(m0.y, m1.z), __fmul_rn(m0.z, m1.y)), inv),
+                                  __fmul_rn(__fsub_rn(__fmul_rn(m1.x, m0.z), __fmul_rn(m1.z, m0.x)), inv),
+                                  __fmul_rn(__fsub_rn(__fmul_rn(m0.x, m1.y), __fmul_rn(m0.y, m1.x)), inv));
+    out[3 * (int64_t)i + 0] = make_float4(r0.x, r0.y, r0.z, dot3(r0, c));
+    out[3 * (int64_t)i + 1] = make_float4(r1.x, r1.y, r1.z, dot3(r1, c));
+    out[3 * (int64_t)i + 2] = make_float4(r2.x, r2.y, r2.z, dot3(r2, c));
+}
+
 }  // namespace
+
+int woop_values(const Tree &t, cudaStream_t s)
+{
+    if (t.woop_valid) return KDGB_OK;
+    KDGB_CHECK(ensure(t.woop, 3 * (int64_t)std::max(t.n_tris, 1), s));
+    if (t.n_tris > 0) {
+        k_woop_values<<<blocks_for(t.n_tris, 256), 256, 0, s>>>(t.p0.p, t.p1.p, t.p2.p, t.n_tris, t.woop.p);
+        KDGB_LAUNCH_CHECK();
+    }
+    t.woop_valid = true;
+    return KDGB_OK;
+}
+
+// Sets c.woop to the Woop rows for the trace parameters (NULL for
+// Moeller-Trumbore).
+static int woop_for(const Tree &t, const kdgb_trace_params &p, cudaStream_t s, Ctx &c)
+{
+    c.woop = nullptr;
+    if (p.intersection != KDGB_ISECT_WOOP) return KDGB_OK;
+    KDGB_CHECK(woop_values(t, s));
+    c.woop = t.woop.p;
+    return KDGB_OK;
+}
 
 
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
@@ -652,6 +766,7 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
     a.c.bmax = t.bmax.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
+    KDGB_CHECK(woop_for(t, p, s, a.c));
     a.mesh_off = nullptr;
     a.ray_mesh = nullptr;
     a.rays_per_mesh = 1;
@@ -700,6 +815,7 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
     a.c.bmax = t.bmax.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
+    KDGB_CHECK(woop_for(t, p, s, a.c));
     a.mesh_off = nullptr;
     a.ray_mesh = nullptr;
     a.rays_per_mesh = 1;
@@ -717,10 +833,11 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
     return KDGB_OK;
 }
 
-int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, int32_t T, int tie, const float *o,
-                 const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv, cudaStream_t s)
+int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, const float4 *woop, int32_t T, int tie,
+                 const float *o, const float *d, int64_t n, int32_t *hit, float *tt, float *uu, float *vv,
+                 cudaStream_t s)
 {
-    k_brute<<<blocks_for(n, kBruteBlock), kBruteBlock, 0, s>>>(p0, p1, p2, T, tie, o, d, n, hit, tt, uu, vv);
+    k_brute<<<blocks_for(n, kBruteBlock), kBruteBlock, 0, s>>>(p0, p1, p2, woop, T, tie, o, d, n, hit, tt, uu, vv);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
@@ -734,6 +851,7 @@ int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_p
     a.c.bmax = t.bmax.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
+    KDGB_CHECK(woop_for(t, p, s, a.c));
     a.p0 = t.p0.p; a.p1 = t.p1.p; a.p2 = t.p2.p;
     a.light = make_float3(ph.light[0], ph.light[1], ph.light[2]);
     a.key = make_uint2((unsigned)(ph.seed & 0xffffffffu), (unsigned)(ph.seed >> 32));
@@ -771,6 +889,7 @@ int shade_launch(const Tree &t, const kdgb_trace_params &p, const float *n0, con
     a.c.bmax = t.bmax.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
+    KDGB_CHECK(woop_for(t, p, s, a.c));
     a.p0 = t.p0.p; a.p1 = t.p1.p; a.p2 = t.p2.p;
     a.T = t.n_tris;
     a.n0 = reinterpret_cast<const float4 *>(n0);

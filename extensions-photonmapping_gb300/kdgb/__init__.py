@@ -21,7 +21,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import scenes
-from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ERR_CAPACITY, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, FINF, LEAF, LOWER_BITMAP, LOWER_SAH,
+from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ISECT_MOELLER, ISECT_WOOP, ERR_CAPACITY, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, FINF, LEAF, LOWER_BITMAP, LOWER_SAH,
                    TIE_LOWEST_ID, TIE_REF_LAST, TRACER_BRUTE, TRACER_RESTART, TRACER_SHORTSTACK, X, Y, Z,
                    AutotuneResult, BuildParams, BuildStats, KdgbError, Light, light, PhotonParams, TraceParams, TreeView, build_params, check,
                    lib, library_path, photon_params, trace_params)
@@ -29,7 +29,7 @@ from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ERR_CAPACITY, ERR_INVALID_ARGUM
 __all__ = ["KDTree", "Graph", "autotune", "AutotuneResult", "Light", "light", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
            "trace_params", "photon_params", "PhotonParams", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
            "BUILD_REFERENCE", "BUILD_TUNED", "TRACER_RESTART", "TRACER_SHORTSTACK", "TRACER_BRUTE",
-           "TIE_LOWEST_ID", "TIE_REF_LAST", "FINF", "lib", "library_path"]
+           "TIE_LOWEST_ID", "TIE_REF_LAST", "ISECT_MOELLER", "ISECT_WOOP", "FINF", "lib", "library_path"]
 
 
 def _torch():
@@ -528,8 +528,10 @@ class IRayTracer:
         return bool(self.params.leaf_skipping)
 
     def SetIntersectionAlgorithm(self, a: int) -> None:
-        if a != self.MOELLER:
-            raise KdgbError(8, "SetIntersectionAlgorithm: only MOELLER is provided")
+        self.params.intersection = ISECT_WOOP if a == self.WOOP else ISECT_MOELLER
+
+    def GetIntersectionAlgorithm(self) -> int:
+        return self.WOOP if self.params.intersection == ISECT_WOOP else self.MOELLER
 
     def GetRenderTime(self) -> float:
         return self.render_time

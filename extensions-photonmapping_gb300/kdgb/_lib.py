@@ -15,6 +15,7 @@ LOWER_BITMAP, LOWER_SAH = 0, 1
 BUILD_REFERENCE, BUILD_TUNED = 0, 1
 TRACER_RESTART, TRACER_SHORTSTACK, TRACER_BRUTE = 0, 1, 2
 TIE_LOWEST_ID, TIE_REF_LAST = 0, 1
+ISECT_MOELLER, ISECT_WOOP = 0, 1
 
 OK = 0
 ERR_INVALID_ARGUMENT = 1
@@ -41,7 +42,7 @@ class BuildParams(C.Structure):
 class TraceParams(C.Structure):
     _fields_ = [("tracer", C.c_int32), ("leaf_skipping", C.c_int32), ("tie", C.c_int32),
                 ("stack_depth", C.c_int32), ("max_iterations", C.c_int32), ("block_size", C.c_int32),
-                ("tile_width", C.c_int32)]
+                ("tile_width", C.c_int32), ("intersection", C.c_int32)]
 
 
 class TreeView(C.Structure):
@@ -110,8 +111,9 @@ SIGNATURES = {
     "kdgb_light_default": (None, [C.POINTER(Light)]),
     "kdgb_trace_shaded": (C.c_int, [P, C.POINTER(TraceParams), P, P, P, P, C.POINTER(Light), C.c_int32, P, P,
                                     C.c_int32, P, P]),
-    "kdgb_trace_brute_shaded": (C.c_int, [P, C.c_int32, C.c_int32, P, P, P, P, C.POINTER(Light), C.c_int32, P, P,
-                                          C.c_int32, P, P]),
+    "kdgb_trace_brute_shaded": (C.c_int, [P, C.c_int32, C.POINTER(TraceParams), P, P, P, P, C.POINTER(Light),
+                                          C.c_int32, P, P, C.c_int32, P, P]),
+    "kdgb_trace_brute_ex": (C.c_int, [P, C.c_int32, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P]),
     "kdgb_osc_update_surface": (C.c_int, [P, P, C.c_int32, C.c_float, C.c_float, P]),
     "kdgb_backward": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, C.c_int32, P, P, P, P, P, P]),
     "kdgb_trace_brute": (C.c_int, [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, P]),

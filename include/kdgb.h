@@ -40,7 +40,7 @@ typedef struct CUstream_st *kdgb_stream_t; /* same type as cudaStream_t */
 #define KDGB_API
 #endif
 
-#define KDGB_ABI_VERSION 1
+#define KDGB_ABI_VERSION 2
 
 /* Utils/CUDA/Utils.h:18: the reference's "infinity" is the integer
  * 0x7f800000 converted to float. */
@@ -76,6 +76,13 @@ enum { KDGB_BUILD_REFERENCE = 0, KDGB_BUILD_TUNED = 1 };
 /* Tracers: Raytracer (kd-restart), ShortStack, BruteTracer. */
 enum { KDGB_TRACER_RESTART = 0, KDGB_TRACER_SHORTSTACK = 1, KDGB_TRACER_BRUTE = 2 };
 
+/* Ray-triangle test (IRayTracer::SetIntersectionAlgorithm): Moeller-Trumbore
+ * (IRayTracer.h:111-145) or Woop's unit-triangle transform (IRayTracer.h:
+ * 78-109 with the per-triangle values of GeometryList.cu:81-102 /
+ * IntersectionTests.h:438-467), computed for a tree on its first Woop trace
+ * after each build. */
+enum { KDGB_ISECT_MOELLER = 0, KDGB_ISECT_WOOP = 1 };
+
 /* Exact-tie rule between triangles hit at the same t.  LOWEST_ID is the
  * default; REF_LAST keeps the reference's `t <= tBest` (IRayTracer.h:133),
  * where the last triangle tested wins. */
@@ -106,6 +113,7 @@ typedef struct kdgb_trace_params {
     int32_t block_size;      /* threads per block, 0 = library choice */
     int32_t tile_width;      /* >0: rays are a row-major image of this width; threads walk
                                 4x8 pixel packets (IRayTracer.h:67-76) */
+    int32_t intersection;    /* KDGB_ISECT_*, default MOELLER (IRayTracer.cu:33) */
 } kdgb_trace_params;
 
 /* SoA device arrays of a tree, mirroring the KDNode / TriangleNode getters
@@ -261,11 +269,19 @@ KDGB_API int kdgb_trace_shaded(const kdgb_tree *tree, const kdgb_trace_params *p
 
 /* BruteTracer::Trace's pixels without a tree (BruteTracer.cu:54-96 with the
  * shading of ColorKernels.h:15-85): as kdgb_trace_shaded with
- * KDGB_TRACER_BRUTE over n_tris device triangles. */
-KDGB_API int kdgb_trace_brute_shaded(const float *tri_v_dev, int32_t n_tris, int32_t tie, const float *n0_dev,
-                                     const float *n1_dev, const float *n2_dev, const uint8_t *c0_dev,
-                                     const kdgb_light *light, int32_t max_bounces, const float *ray_o_dev,
-                                     const float *ray_d_dev, int32_t n, uint8_t *rgba_dev, kdgb_stream_t stream);
+ * KDGB_TRACER_BRUTE over n_tris device triangles (params: tie and
+ * intersection are used). */
+KDGB_API int kdgb_trace_brute_shaded(const float *tri_v_dev, int32_t n_tris, const kdgb_trace_params *params,
+                                     const float *n0_dev, const float *n1_dev, const float *n2_dev,
+                                     const uint8_t *c0_dev, const kdgb_light *light, int32_t max_bounces,
+                                     const float *ray_o_dev, const float *ray_d_dev, int32_t n, uint8_t *rgba_dev,
+                                     kdgb_stream_t stream);
+
+/* kdgb_trace_brute with trace parameters (tie and intersection used), for
+ * BruteTracer with SetIntersectionAlgorithm(WOOP) (BruteTracer.cu:139). */
+KDGB_API int kdgb_trace_brute_ex(const float *tri_v_dev, int32_t n_tris, const kdgb_trace_params *params,
+                                 const float *ray_o_dev, const float *ray_d_dev, int32_t n, int32_t *hit_dev,
+                                 float *t_dev, float *u_dev, float *v_dev, kdgb_stream_t stream);
 
 /* Batched build (no reference counterpart; the reference builds one scene
  * per TriangleMap): n_meshes independent meshes stored back to back in

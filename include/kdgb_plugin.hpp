@@ -343,9 +343,12 @@ public:
 
     void SetIntersectionAlgorithm(const IntersectionAlgorithm a)
     {
-        if (a != MOELLER) throw Core::Exception("IRayTracer: only Moeller-Trumbore is provided");
+        p_.intersection = a == WOOP ? KDGB_ISECT_WOOP : KDGB_ISECT_MOELLER;
     }
-    IntersectionAlgorithm GetIntersectionAlgorithm() const { return MOELLER; }
+    IntersectionAlgorithm GetIntersectionAlgorithm() const
+    {
+        return p_.intersection == KDGB_ISECT_WOOP ? WOOP : MOELLER;
+    }
     void SetLeafSkipping(const bool s) { p_.leaf_skipping = s; }
     bool GetLeafSkipping() const { return p_.leaf_skipping != 0; }
     float GetRenderTime() const { return renderTime_; }
@@ -436,14 +439,14 @@ public:
     explicit BruteTracer(GeometryList *geom) : IRayTracer(KDGB_TRACER_BRUTE), geom_(geom) {}
     void Trace(const float *o, const float *d, int n, int *hit, float *t, float *u, float *v, cudaStream_t s = 0) override
     {
-        detail::check(kdgb_trace_brute(geom_->GetTriangleData(), geom_->GetSize(), p_.tie, o, d, n, hit, t, u, v, s),
+        detail::check(kdgb_trace_brute_ex(geom_->GetTriangleData(), geom_->GetSize(), &p_, o, d, n, hit, t, u, v, s),
                       "BruteTracer::Trace");
     }
     void Trace(const float *o, const float *d, int n, uchar4 *canvas, cudaStream_t s = 0) override
     {
         const GeometryList *g = geom_;
         Timed([&] {
-            return kdgb_trace_brute_shaded(g->GetTriangleData(), g->GetSize(), p_.tie, g->GetNormal0Data(),
+            return kdgb_trace_brute_shaded(g->GetTriangleData(), g->GetSize(), &p_, g->GetNormal0Data(),
                                            g->GetNormal1Data(), g->GetNormal2Data(), g->GetColor0Data(), &light_, 0, o,
                                            d, n, reinterpret_cast<uint8_t *>(canvas), s);
         }, "BruteTracer::Trace", s);

@@ -117,6 +117,56 @@ static inline void mt_test(const float *tri, int prim, v3 o, v3 d, int tie,
     }
 }
 
+/* WoopTransformationMatrix (IntersectionTests.h:438-467) of (p1, p2, p0) as
+ * CreateWoopValues (GeometryList.cu:81-102) calls it: the inverse of the
+ * matrix whose columns are a - c, b - c and (a - c) x (b - c) - c, rows scaled
+ * by 1/det, each row's w = row . c. */
+static void woop_rows(const float *tri, int prim, f4 m[3])
+{
+    const float *tp = tri + (size_t)prim * 9;
+    const v3 c = ld3(tp), a = ld3(tp + 3), b = ld3(tp + 6);
+    const v3 m0 = sub3(a, c), m1 = sub3(b, c), m2 = sub3(cross3(m0, m1), c);
+    const float det = (m0.x * (m1.y * m2.z - m1.z * m2.y) + m1.x * (m2.y * m0.z - m2.z * m0.y)) +
+                      m2.x * (m0.y * m1.z - m0.z * m1.y);
+    const float inv = 1.0f / det;
+    const v3 r0 = mk3((m1.y * m2.z - m1.z * m2.y) * inv, (m2.x * m1.z - m2.z * m1.x) * inv,
+                      (m1.x * m2.y - m1.y * m2.x) * inv);
+    const v3 r1 = mk3((m2.y * m0.z - m2.z * m0.y) * inv, (m0.x * m2.z - m0.z * m2.x) * inv,
+                      (m2.x * m0.y - m2.y * m0.x) * inv);
+    const v3 r2 = mk3((m0.y * m1.z - m0.z * m1.y) * inv, (m1.x * m0.z - m1.z * m0.x) * inv,
+                      (m0.x * m1.y - m0.y * m1.x) * inv);
+    const f4 w0 = {r0.x, r0.y, r0.z, dot3(r0, c)}, w1 = {r1.x, r1.y, r1.z, dot3(r1, c)},
+             w2 = {r2.x, r2.y, r2.z, dot3(r2, c)};
+    m[0] = w0; m[1] = w1; m[2] = w2;
+}
+
+/* Woop (IRayTracer.h:78-109): lambda = -(m2.o - m2.w) / (m2.d),
+ * u = lambda (m0.d) + m0.o - m0.w, v likewise with m1. */
+static inline void woop_test(const float *tri, int prim, v3 o, v3 d, int tie, int *prim_hit, float th[3])
+{
+    f4 m[3];
+    woop_rows(tri, prim, m);
+    const v3 n2 = mk3(m[2].x, m[2].y, m[2].z);
+    const float lambda = -(dot3(n2, o) - m[2].w) / dot3(n2, d);
+    if (0.0f <= lambda && lambda <= th[0]) {
+        const v3 n0 = mk3(m[0].x, m[0].y, m[0].z), n1 = mk3(m[1].x, m[1].y, m[1].z);
+        const float hu = (lambda * dot3(n0, d) + dot3(n0, o)) - m[0].w;
+        const float hv = (lambda * dot3(n1, d) + dot3(n1, o)) - m[1].w;
+        if (hu >= -0.0f && hv >= -0.0f && hu + hv <= 1.0f) {
+            if (tie == OR_TIE_REF_LAST || *prim_hit == -1 || lambda < th[0] || prim < *prim_hit) {
+                *prim_hit = prim;
+                th[0] = lambda; th[1] = hu; th[2] = hv;
+            }
+        }
+    }
+}
+
+static inline void isect(int woop, const float *tri, int prim, v3 o, v3 d, int tie, int *prim_hit, float th[3])
+{
+    if (woop) woop_test(tri, prim, o, d, tie, prim_hit, th);
+    else mt_test(tri, prim, o, d, tie, prim_hit, th);
+}
+
 int or_moeller_trumbore(const float v0[3], const float v1[3], const float v2[3],
                         const float o[3], const float d[3], float t_max, float out[3])
 {
@@ -160,7 +210,7 @@ static inline void write_miss(int32_t i, int32_t *hit, float *t, float *u, float
 /* Leaf test shared by the kd tracers: bitmap order LSB first (Utils.h:198-204,
  * Raytracer.cu:199-215). */
 static inline int leaf_test(const or_tree *tr, const float *tri, int node, v3 o, v3 d,
-                            int tie, float th[3])
+                            int tie, int woop, float th[3])
 {
     const int pi = tr->prim_index[node];
     uint32_t bm = (uint32_t)tr->bitmap[node];
@@ -168,7 +218,7 @@ static inline int leaf_test(const or_tree *tr, const float *tri, int node, v3 o,
     while (bm) {
         const int i = __builtin_ctz(bm);
         const int prim = tr->prim_indices[pi + i];
-        mt_test(tri, prim, o, d, tie, &prim_hit, th);
+        isect(woop, tri, prim, o, d, tie, &prim_hit, th);
         bm &= bm - 1u;
     }
     return prim_hit;
@@ -204,7 +254,7 @@ static void trace_restart_one(const or_tree *tr, const float *tri, const or_trac
         th[0] = t_next * 1.00001f;
         if (!p->leaf_skipping || ray_box(o, inv, tr->aabb_min + 4 * (size_t)node,
                                           tr->aabb_max + 4 * (size_t)node)) {
-            const int h = leaf_test(tr, tri, node, o, d, p->tie, th);
+            const int h = leaf_test(tr, tri, node, o, d, p->tie, p->intersection, th);
             if (h != -1) { *hit = h; *ot = th[0]; *ou = th[1]; *ov = th[2]; return; }
         }
         if (p->max_iterations > 0 && ++iters >= p->max_iterations) break;
@@ -261,7 +311,7 @@ static void trace_shortstack_one(const or_tree *tr, const float *tri, const or_t
         th[0] = t_next * 1.00001f;
         if (!p->leaf_skipping || ray_box(o, inv3(d), tr->aabb_min + 4 * (size_t)node,
                                           tr->aabb_max + 4 * (size_t)node)) {
-            const int h = leaf_test(tr, tri, node, o, d, p->tie, th);
+            const int h = leaf_test(tr, tri, node, o, d, p->tie, p->intersection, th);
             if (h != -1) {
                 *hit = h; *ot = th[0]; *ou = th[1]; *ov = th[2];
                 if (dused) *dused = d;
@@ -275,12 +325,12 @@ static void trace_shortstack_one(const or_tree *tr, const float *tri, const or_t
 
 /* BruteTracer.cu:54-96 Exhaustive (first hit, no direction clamp, the
  * 4096-triangle cap of BruteTracer.cu:50 lifted). */
-static void trace_brute_one(const float *tri, int32_t T, int tie, v3 o, v3 d,
+static void trace_brute_one(const float *tri, int32_t T, int tie, int woop, v3 o, v3 d,
                             int32_t *hit, float *ot, float *ou, float *ov)
 {
     float th[3] = {OR_FINF, 0.0f, 0.0f};
     int prim_hit = -1;
-    for (int prim = 0; prim < T; ++prim) mt_test(tri, prim, o, d, tie, &prim_hit, th);
+    for (int prim = 0; prim < T; ++prim) isect(woop, tri, prim, o, d, tie, &prim_hit, th);
     if (th[0] < OR_FINF) { *hit = prim_hit; *ot = th[0]; *ou = th[1]; *ov = th[2]; }
     else { *hit = -1; *ot = INFINITY; *ou = 0.0f; *ov = 0.0f; }
 }
@@ -301,7 +351,7 @@ int or_trace(const or_tree *tr, const float *tri, int32_t T, const or_trace_para
 {
     if (!p || n < 0 || (n > 0 && (!ray_o || !ray_d || !hit || !t || !u || !v))) return OR_ERR_ARG;
     if (p->tracer == OR_TRACER_BRUTE)
-        return or_trace_brute(tri, T, p->tie, ray_o, ray_d, n, hit, t, u, v, threads);
+        return or_trace_brute(tri, T, p->tie, p->intersection, ray_o, ray_d, n, hit, t, u, v, threads);
     if (!tr || tr->n_nodes <= 0) return OR_ERR_ARG;
     if (p->tracer == OR_TRACER_SHORTSTACK && (p->stack_depth < 1 || p->stack_depth > 64)) return OR_ERR_ARG;
     const int nt = set_threads(threads);
@@ -317,7 +367,7 @@ int or_trace(const or_tree *tr, const float *tri, int32_t T, const or_trace_para
     return 0;
 }
 
-int or_trace_brute(const float *tri, int32_t T, int32_t tie,
+int or_trace_brute(const float *tri, int32_t T, int32_t tie, int32_t intersection,
                    const float *ray_o, const float *ray_d, int32_t n,
                    int32_t *hit, float *t, float *u, float *v, int32_t threads)
 {
@@ -327,7 +377,7 @@ int or_trace_brute(const float *tri, int32_t T, int32_t tie,
 #pragma omp parallel for schedule(static, 64) num_threads(nt)
     for (int32_t i = 0; i < n; ++i) {
         const v3 o = ld3(ray_o + 3 * (size_t)i), d = ld3(ray_d + 3 * (size_t)i);
-        trace_brute_one(tri, T, tie, o, d, hit + i, t + i, u + i, v + i);
+        trace_brute_one(tri, T, tie, intersection, o, d, hit + i, t + i, u + i, v + i);
     }
     return 0;
 }
@@ -374,7 +424,7 @@ int or_trace_brute_f64(const float *tri, int32_t T,
 /* Raytracer.cu:108-163 ShadowRay<false,true>: a ray from the light toward the
  * point (direction = point - light, not normalised, not clamped); the leaf is
  * skipped once its exit t reaches 0.999; any hit means shadow. */
-int or_trace_shadow(const or_tree *tr, const float *tri, int32_t T,
+int or_trace_shadow(const or_tree *tr, const float *tri, int32_t T, int32_t intersection,
                     const float *points, int32_t n, const float light[3],
                     int32_t *occluded, int32_t threads)
 {
@@ -410,7 +460,7 @@ int or_trace_shadow(const or_tree *tr, const float *tri, int32_t T,
             t_min = t_next * 1.00001f;
             if (t_min >= 0.999f) break;
             float th[3] = {t_min, 0.0f, 0.0f};
-            if (leaf_test(tr, tri, node, lp, d, OR_TIE_REF_LAST, th) != -1) { occ = 1; break; }
+            if (leaf_test(tr, tri, node, lp, d, OR_TIE_REF_LAST, intersection, th) != -1) { occ = 1; break; }
         } while (t_min < 0.999f);
         occluded[i] = occ;
     }
@@ -674,7 +724,7 @@ int or_trace_shaded(const or_tree *tr, const float *tri, int32_t T, const or_tra
             int32_t h;
             float t, u, v;
             v3 dh = d;
-            if (p->tracer == OR_TRACER_BRUTE) trace_brute_one(tri, T, p->tie, o, d, &h, &t, &u, &v);
+            if (p->tracer == OR_TRACER_BRUTE) trace_brute_one(tri, T, p->tie, p->intersection, o, d, &h, &t, &u, &v);
             else if (p->tracer == OR_TRACER_SHORTSTACK) trace_shortstack_one(tr, tri, p, o, d, &h, &t, &u, &v, &dh);
             else trace_restart_one(tr, tri, p, o, d, &h, &t, &u, &v, &dh);
             if (h < 0) break;
@@ -717,6 +767,7 @@ void or_trace_params_default(or_trace_params *p)
     p->tie = OR_TIE_LOWEST_ID;
     p->stack_depth = 4;
     p->max_iterations = 0;
+    p->intersection = OR_ISECT_MOELLER;
 }
 
 void or_geometry_from_tris(const float *tri, int32_t T, float *p0, float *p1, float *p2)

@@ -81,7 +81,10 @@ typedef struct or_trace_params {
     int32_t tie;             /* OR_TIE_* */
     int32_t stack_depth;     /* ShortStack.cu:25 default 4 */
     int32_t max_iterations;  /* restart / pop guard per ray; 0 = unlimited */
+    int32_t intersection;    /* OR_ISECT_*: IRayTracer.cu:33 default Moeller-Trumbore */
 } or_trace_params;
+
+enum { OR_ISECT_MOELLER = 0, OR_ISECT_WOOP = 1 };
 
 void or_build_params_default(or_build_params *p);
 void or_trace_params_default(or_trace_params *p);
@@ -105,7 +108,7 @@ int or_trace(const or_tree *tree, const float *tri, int32_t T,
              int32_t *hit, float *t, float *u, float *v, int32_t threads);
 
 /* Brute force over all T triangles (BruteTracer.cu:54-96, cap lifted). */
-int or_trace_brute(const float *tri, int32_t T, int32_t tie,
+int or_trace_brute(const float *tri, int32_t T, int32_t tie, int32_t intersection,
                    const float *ray_o, const float *ray_d, int32_t n,
                    int32_t *hit, float *t, float *u, float *v, int32_t threads);
 
@@ -115,7 +118,7 @@ int or_trace_brute_f64(const float *tri, int32_t T,
                        int32_t *hit, double *t, double *u, double *v, int32_t threads);
 
 /* Shadow rays (Raytracer.cu:108-163): occluded[i] = 1 when point i is in shadow. */
-int or_trace_shadow(const or_tree *tree, const float *tri, int32_t T,
+int or_trace_shadow(const or_tree *tree, const float *tri, int32_t T, int32_t intersection,
                     const float *points, int32_t n, const float light[3],
                     int32_t *occluded, int32_t threads);
 

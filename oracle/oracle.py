@@ -23,6 +23,7 @@ LEAF, X, Y, Z = 0, 1, 2, 3
 LOWER_BITMAP, LOWER_SAH = 0, 1
 TIE_LOWEST_ID, TIE_REF_LAST = 0, 1
 TRACER_RESTART, TRACER_SHORTSTACK, TRACER_BRUTE = 0, 1, 2
+ISECT_MOELLER, ISECT_WOOP = 0, 1
 FINF = np.float32(2139095040.0)
 
 
@@ -37,7 +38,7 @@ class BuildParams(C.Structure):
 
 class TraceParams(C.Structure):
     _fields_ = [("tracer", C.c_int32), ("leaf_skipping", C.c_int32), ("tie", C.c_int32),
-                ("stack_depth", C.c_int32), ("max_iterations", C.c_int32)]
+                ("stack_depth", C.c_int32), ("max_iterations", C.c_int32), ("intersection", C.c_int32)]
 
 
 class _Tree(C.Structure):
@@ -80,9 +81,9 @@ def lib():
         L.or_tree_free.argtypes = [C.POINTER(_Tree)]
         L.or_trace.argtypes = [C.POINTER(_Tree), P, C.c_int32, C.POINTER(TraceParams), P, P,
                                C.c_int32, P, P, P, P, C.c_int32]
-        L.or_trace_brute.argtypes = [P, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32]
+        L.or_trace_brute.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32]
         L.or_trace_brute_f64.argtypes = [P, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32]
-        L.or_trace_shadow.argtypes = [C.POINTER(_Tree), P, C.c_int32, P, C.c_int32, P, P, C.c_int32]
+        L.or_trace_shadow.argtypes = [C.POINTER(_Tree), P, C.c_int32, C.c_int32, P, C.c_int32, P, P, C.c_int32]
         L.or_moeller_trumbore.argtypes = [P, P, P, P, P, C.c_float, P]
         L.or_error_string.restype = C.c_char_p
         L.or_build_params_default.argtypes = [C.POINTER(BuildParams)]
@@ -202,7 +203,7 @@ def trace(tree: Tree | None, tris: np.ndarray, o, d, params: TraceParams | None 
     u = np.empty(n, np.float32)
     v = np.empty(n, np.float32)
     if p.tracer == TRACER_BRUTE:
-        _check(lib().or_trace_brute(_ptr(tris), tris.shape[0], p.tie, _ptr(o), _ptr(d), n,
+        _check(lib().or_trace_brute(_ptr(tris), tris.shape[0], p.tie, p.intersection, _ptr(o), _ptr(d), n,
                                     _ptr(hit), _ptr(t), _ptr(u), _ptr(v), threads))
     else:
         s = tree.as_struct()
@@ -224,13 +225,13 @@ def trace_brute_f64(tris, o, d, threads: int = 0):
     return hit, t, u, v
 
 
-def trace_shadow(tree: Tree, tris, points, light, threads: int = 0):
+def trace_shadow(tree: Tree, tris, points, light, threads: int = 0, intersection: int = 0):
     tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
     pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
     lp = np.ascontiguousarray(light, dtype=np.float32).reshape(3)
     occ = np.empty(pts.shape[0], np.int32)
     s = tree.as_struct()
-    _check(lib().or_trace_shadow(C.byref(s), _ptr(tris), tris.shape[0], _ptr(pts), pts.shape[0],
+    _check(lib().or_trace_shadow(C.byref(s), _ptr(tris), tris.shape[0], intersection, _ptr(pts), pts.shape[0],
                                  _ptr(lp), _ptr(occ), threads))
     return occ
 
