@@ -148,13 +148,21 @@ static int validate_build_params(const kdgb_build_params &p)
 {
     if (p.mode != KDGB_BUILD_REFERENCE && p.mode != KDGB_BUILD_TUNED)
         return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown build mode");
-    if (p.lower != KDGB_LOWER_BITMAP && p.lower != KDGB_LOWER_SAH)
+    if (p.lower != KDGB_LOWER_BITMAP && p.lower != KDGB_LOWER_SAH && p.lower != KDGB_LOWER_BALANCED)
         return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown lower algorithm");
+    if (p.split_method == KDGB_SPLIT_SPLIT)
+        return fail(KDGB_ERR_UNSUPPORTED, "split method SPLIT is not implemented (as in the reference)");
+    if (p.split_method != KDGB_SPLIT_BOX && p.split_method != KDGB_SPLIT_DIVIDE)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown split method");
     if (p.leaf_size < 1 || p.leaf_size > 32) return fail(KDGB_ERR_INVALID_ARGUMENT, "leaf_size must be in 1..32");
     if (p.max_levels < 1 || p.max_levels > 4096) return fail(KDGB_ERR_INVALID_ARGUMENT, "max_levels out of range");
     if (!std::isfinite(p.empty_space_threshold) || !std::isfinite(p.traversal_cost) ||
         !std::isfinite(p.intersection_cost))
         return fail(KDGB_ERR_INVALID_ARGUMENT, "non-finite cost parameter");
+    // A negative cost lets the balanced rule split a node into itself and an
+    // empty child forever.
+    if (p.lower == KDGB_LOWER_BALANCED && p.traversal_cost < 0.0f)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "balanced lower creator needs traversal_cost >= 0");
     if (p.mode == KDGB_BUILD_TUNED && (p.upper_levels < 0 || p.sah_bins < 2 || p.sah_bins > 32))
         return fail(KDGB_ERR_INVALID_ARGUMENT, "tuned build: upper_levels >= 0, sah_bins in 2..32");
     return KDGB_OK;
@@ -276,6 +284,7 @@ void kdgb_build_params_default(kdgb_build_params *p)
     p->leaf_size = 32;
     p->upper_levels = 8;
     p->sah_bins = 32;
+    p->split_method = KDGB_SPLIT_BOX;
 }
 
 void kdgb_trace_params_default(kdgb_trace_params *p)
@@ -848,7 +857,7 @@ int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris, c
     {
         const GraphKernels &k = g->kernels;
         g->per_launch = k.fixed + k.upper_body * t.plan.levels + g->trace_kernels +
-                        (p.lower == KDGB_LOWER_SAH ? k.lower_body * std::max(1, t.plan.low_levels) : 0);
+                        (lower_loop(p) ? k.lower_body * std::max(1, t.plan.low_levels) : 0);
     }
     if (rc != KDGB_OK) {
         kdgb_graph_destroy(g);

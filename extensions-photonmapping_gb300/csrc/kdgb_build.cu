@@ -88,7 +88,7 @@ struct BuildArgs {
     BuildState *st;
     Caps cap;
     int32_t T, M, LS, B, upper_levels, max_levels, min_leaf;
-    int ess, zmax_as_x, propagate, tuned;
+    int ess, zmax_as_x, propagate, tuned, lower, divide;
     float thr, ct, ci;
     const int32_t *mesh_off;
     float4 *p0, *p1, *p2;
@@ -405,9 +405,71 @@ __device__ __forceinline__ void ref_flags(const float4 &lo, const float4 &hi, in
     Rf = sp < axis_of4(hi, axis);
 }
 
+// One separating axis of Akenine-Moeller's triangle/box test, step 3 (a
+// triangle edge crossed with a box axis), in the two coordinates (s, t)
+// perpendicular to the box axis: edge a->b, third vertex c, box half sizes
+// hs, ht, all relative to the box centre.  Expressions of a0XTests /
+// a1XTests / a2XTests (IntersectionTests.h:23-149) with their slack
+// r = (... + 1e-5) * 1.0001 (IntersectionTests.h:20-21), every operation
+// rounded separately.
+__device__ __forceinline__ bool sat_edge(float as, float at, float bs, float bt, float cs, float ct, float hs,
+                                         float ht)
+{
+    const float p0 = __fsub_rn(__fmul_rn(at, bs), __fmul_rn(as, bt));
+    const float p1 = __fsub_rn(__fmul_rn(__fsub_rn(bs, as), ct), __fmul_rn(__fsub_rn(bt, at), cs));
+    float r = __fadd_rn(__fmul_rn(ht, fabsf(__fsub_rn(bs, as))), __fmul_rn(hs, fabsf(__fsub_rn(bt, at))));
+    r = __fmul_rn(__fadd_rn(r, 0.00001f), 1.0001f);
+    return !((p0 > r && p1 > r) || (p0 < -r && p1 < -r));
+}
+
+// TriangleAabbIntersectionStep3 (IntersectionTests.h:378-395): the nine
+// edge-axis tests of the triangle against the box [lo, hi].
+__device__ __forceinline__ bool tri_box_step3(float3 v0, float3 v1, float3 v2, float3 lo, float3 hi)
+{
+    const float3 h = make_float3(__fmul_rn(__fsub_rn(hi.x, lo.x), 0.5f), __fmul_rn(__fsub_rn(hi.y, lo.y), 0.5f),
+                                 __fmul_rn(__fsub_rn(hi.z, lo.z), 0.5f));
+    const float3 c = make_float3(__fadd_rn(lo.x, h.x), __fadd_rn(lo.y, h.y), __fadd_rn(lo.z, h.z));
+    v0 = sub3(v0, c);
+    v1 = sub3(v1, c);
+    v2 = sub3(v2, c);
+    bool ok = true;
+    // box axis x: coordinates (y, z)
+    ok &= sat_edge(v0.y, v0.z, v1.y, v1.z, v2.y, v2.z, h.y, h.z);
+    ok &= sat_edge(v1.y, v1.z, v2.y, v2.z, v0.y, v0.z, h.y, h.z);
+    ok &= sat_edge(v2.y, v2.z, v0.y, v0.z, v1.y, v1.z, h.y, h.z);
+    // box axis y: coordinates (z, x)
+    ok &= sat_edge(v0.z, v0.x, v1.z, v1.x, v2.z, v2.x, h.z, h.x);
+    ok &= sat_edge(v1.z, v1.x, v2.z, v2.x, v0.z, v0.x, h.z, h.x);
+    ok &= sat_edge(v2.z, v2.x, v0.z, v0.x, v1.z, v1.x, h.z, h.x);
+    // box axis z: coordinates (x, y)
+    ok &= sat_edge(v0.x, v0.y, v1.x, v1.y, v2.x, v2.y, h.x, h.y);
+    ok &= sat_edge(v1.x, v1.y, v2.x, v2.y, v0.x, v0.y, h.x, h.y);
+    ok &= sat_edge(v2.x, v2.y, v0.x, v0.y, v1.x, v1.y, h.x, h.y);
+    return ok;
+}
+
+// SetDivideSide<false> (TriangleUpperChildren.h:64-142): a reference whose
+// box straddles the plane is tested with its triangle against the two halves
+// of the node's tight box; it may go to one side only, or to none when the
+// triangle misses the node box although its clipped box does not.
+__device__ __forceinline__ void divide_flags(const BuildArgs &a, int32_t prim, int32_t node, int axis, float sp,
+                                            int &L, int &Rf)
+{
+    const float4 q0 = __ldg(a.p0 + prim), q1 = __ldg(a.p1 + prim), q2 = __ldg(a.p2 + prim);
+    const float3 v0 = make_float3(q0.x, q0.y, q0.z), v1 = make_float3(q1.x, q1.y, q1.z),
+                 v2 = make_float3(q2.x, q2.y, q2.z);
+    const float4 mn = a.bmin[node], mx = a.bmax[node];
+    const float3 lo = make_float3(mn.x, mn.y, mn.z), hi = make_float3(mx.x, mx.y, mx.z);
+    const float3 lhi = make_float3(axis == KDGB_X ? sp : hi.x, axis == KDGB_Y ? sp : hi.y, axis == KDGB_Z ? sp : hi.z);
+    const float3 rlo = make_float3(axis == KDGB_X ? sp : lo.x, axis == KDGB_Y ? sp : lo.y, axis == KDGB_Z ? sp : lo.z);
+    L = tri_box_step3(v0, v1, v2, lo, lhi);
+    Rf = tri_box_step3(v0, v1, v2, rlo, hi);
+}
+
 // Per-node left/right counts, per-chunk totals of the flags and per-tile
 // totals (the tile totals are scanned into tile offsets; k_scatter adds the
 // chunk totals of the earlier warps of its tile).
+template <bool DIVIDE>
 __global__ void __launch_bounds__(kBlock) k_count(const BuildArgs a)
 {
     __shared__ int s_owner[kWarps], s_l[kWarps], s_r[kWarps], s_tl[kWarps], s_tr[kWarps];
@@ -445,6 +507,7 @@ __global__ void __launch_bounds__(kBlock) k_count(const BuildArgs a)
             const int o = __float_as_int(rb[row].w);
             int L = 0, Rf = 0;
             if (o >= 0) ref_flags(ra[row], rb[row], ax[row], sp[row], L, Rf);
+            if (DIVIDE && L && Rf) divide_flags(a, __float_as_int(ra[row].w), active + o, ax[row], sp[row], L, Rf);
             tl += L;
             tr += Rf;
             const unsigned m = __match_any_sync(kFull, o);
@@ -749,6 +812,7 @@ __device__ __forceinline__ void scatter_one(const BuildArgs &a, int32_t R, int o
 // + rank of the reference among the node's left (right) references; a warp's
 // first rank is its tile's offset plus the chunk totals of the tile's earlier
 // warps.
+template <bool DIVIDE>
 __global__ void __launch_bounds__(kBlock) k_scatter(const BuildArgs a)
 {
     __shared__ int32_t s_off[kWarps][2];
@@ -807,6 +871,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(const BuildArgs a)
             const float4 lo = ra[row], hi = rb[row];
             int L = 0, Rf = 0;
             if (owner >= 0) ref_flags(lo, hi, axis, sp, L, Rf);
+            if (DIVIDE && L && Rf) divide_flags(a, __float_as_int(lo.w), active + owner, axis, sp, L, Rf);
             const unsigned bl = __ballot_sync(kFull, L), br = __ballot_sync(kFull, Rf);
             const int32_t pl = off_l + __popc(bl & below), pr = off_r + __popc(br & below);
             off_l += __popc(bl);
@@ -898,7 +963,9 @@ __device__ void advance_upper(const BuildArgs &a, BuildState *st)
             break;
         }
         const int64_t tl = tot[0], tr = tot[1], ll = tot[2], lr = tot[3];
-        if (tl + tr < st->N) { set_err(st, KDGB_ERR_DEGENERATE, kErrFewerRefs); break; }
+        // Box sides keep every reference; DIVIDE may drop references whose
+        // triangle misses the node box.
+        if (!a.divide && tl + tr < st->N) { set_err(st, KDGB_ERR_DEGENERATE, kErrFewerRefs); break; }
         const int32_t empty = tot[6];
         if (leaf_nodes > 0) {
             a.ranges[st->n_ranges] = make_int2(st->n_nodes + empty, leaf_nodes);
@@ -1259,6 +1326,66 @@ __global__ void k_calc_sah(const BuildArgs a)
     }
 }
 
+// Balanced ("SSAH") lower creator: CalcSplit (LowerTriangleMap.h:299-369)
+// with CalcRelationForSets (:260-295), one warp per node.  Lane i weighs the
+// six planes of slot i by small^2 + large^2 of the two set sizes (integers,
+// so the order of evaluation cannot change the result); the warp keeps the
+// first minimum in (slot, axis, low/high) order, the reference's running
+// strict minimum from 32 * 32.  A node of n references splits when
+// (traversal_cost + weight) / n < n and a plane was found.  Children carry
+// no area (the creator never writes one).
+constexpr int kNoPlane = 32 * 32;
+
+__global__ void k_calc_balanced(const BuildArgs a)
+{
+    const BuildState *st = a.st;
+    if (st->err) return;
+    const int32_t R = st->low_R, active = st->low_active;
+    const int32_t *__restrict__ ids = st->low_first ? a.leaf_ids : nullptr;
+    const int64_t F = st->F;
+    const int lane = threadIdx.x & 31;
+    WARP_STRIDE(gw, R) {
+        const int32_t par = ids ? ids[gw] : active + (int32_t)gw;
+        const int32_t pi = a.pidx[par];
+        const unsigned bmp = (unsigned)a.amt[par];
+        int best = kNoPlane, axis = 0, high = 0;
+        unsigned ls = 0, rs = 0;
+        if ((bmp >> lane) & 1u) {
+#pragma unroll
+            for (int x = 0; x < 3; ++x) {
+                const int4 s4 = a.sts[x * F + pi + lane];
+                const unsigned s[4] = {(unsigned)s4.x & bmp, (unsigned)s4.y & bmp, (unsigned)s4.z & bmp,
+                                       (unsigned)s4.w & bmp};
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int c0 = __popc(s[2 * h]), c1 = __popc(s[2 * h + 1]);
+                    const int w = c0 * c0 + c1 * c1;
+                    if (w < best) { best = w; ls = s[2 * h]; rs = s[2 * h + 1]; axis = x + 1; high = h; }
+                }
+            }
+        }
+        int c = best, owner = lane;
+        for (int o = 16; o > 0; o >>= 1) {
+            const int c2 = __shfl_xor_sync(kFull, c, o);
+            const int w2 = __shfl_xor_sync(kFull, owner, o);
+            if (c2 < c || (c2 == c && w2 < owner)) { c = c2; owner = w2; }
+        }
+        if (lane == owner) {
+            const float n = (float)__popc(bmp);
+            const float ssah = __fdiv_rn(__fadd_rn(a.ct, (float)best), n);
+            const bool split_it = best < kNoPlane && ssah < n;
+            if (split_it) {
+                a.careas[gw] = make_float2(0.0f, 0.0f);
+                a.csets[gw] = make_int2((int)ls, (int)rs);
+                const float4 sp4 = high ? a.fmax[pi + lane] : a.fmin[pi + lane];
+                a.split[par] = axis_of4(sp4, axis);
+            }
+            a.info[par] = split_it ? (int8_t)axis : (int8_t)KDGB_LEAF;
+            a.ssplit[gw] = split_it;
+        }
+    }
+}
+
 __device__ __forceinline__ bool lower_fits(const BuildArgs &a, const BuildState *st, int32_t splits)
 {
     return (int64_t)st->n_nodes + 2 * (int64_t)splits <= a.cap.nodes;
@@ -1492,6 +1619,8 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.zmax_as_x = p.esc_zmax_as_x;
     a.propagate = p.propagate_aabbs;
     a.tuned = p.mode == KDGB_BUILD_TUNED;
+    a.lower = p.lower;
+    a.divide = p.split_method == KDGB_SPLIT_DIVIDE;
     a.thr = p.empty_space_threshold;
     a.ct = p.traversal_cost;
     a.ci = p.intersection_cost;
@@ -1582,14 +1711,16 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
         KDGB_LAUNCH_CHECK();
     }
     if (e.N > 0) {
-        k_count<<<gN, kBlock, 0, s>>>(a);
+        if (a.divide) k_count<true><<<gN, kBlock, 0, s>>>(a);
+        else k_count<false><<<gN, kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
     KDGB_CHECK(scan_exclusive<2>(a.tilesum, a.tileoff, ceil_div(e.N, kTileRefs), s, &w.scan, &a.st->ntiles));
     const NodeLanes lanes{a.cnt, a.ess_cnt, a.LS};
     KDGB_CHECK((scan_exclusive_in<kLanes, NodeLanes>(lanes, a.lbase, e.R, s, &w.scan, &a.st->R)));
     if (e.N > 0) {
-        k_scatter<<<gN, kBlock, 0, s>>>(a);
+        if (a.divide) k_scatter<true><<<gN, kBlock, 0, s>>>(a);
+        else k_scatter<false><<<gN, kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
     k_children<<<gR, kBlock, 0, s>>>(a);
@@ -1613,12 +1744,16 @@ int emit_after_upper(const BuildArgs &a, const Launcher &L, const Extents &e, co
         KDGB_LAUNCH_CHECK();
         k_sah_preprocess<<<L.grid(e.leaves, kBlock), kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
+    } else {
+        // Every reference of an upper leaf (PreprocessLeafNodes,
+        // LowerTriangleMap.h:40-53 and TriangleMapBitmapCreator.cu:32-49).
+        k_bitmap_leaves<<<L.grid(e.leaves, kBlock), kBlock, 0, s>>>(a);
+        KDGB_LAUNCH_CHECK();
+    }
+    if (lower_loop(p)) {
         k_sah_planes<<<L.grid(e.leaves * 32, kBlock), kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
         k_lower_begin<<<1, 1, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
-    } else {
-        k_bitmap_leaves<<<L.grid(e.leaves, kBlock), kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
     return KDGB_OK;
@@ -1626,7 +1761,8 @@ int emit_after_upper(const BuildArgs &a, const Launcher &L, const Extents &e, co
 
 int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, Workspace &w, cudaStream_t s)
 {
-    k_calc_sah<<<L.grid(e.low_R * 32, kBlock), kBlock, 0, s>>>(a);
+    if (a.lower == KDGB_LOWER_BALANCED) k_calc_balanced<<<L.grid(e.low_R * 32, kBlock), kBlock, 0, s>>>(a);
+    else k_calc_sah<<<L.grid(e.low_R * 32, kBlock), kBlock, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
     KDGB_CHECK(scan_exclusive<1>(a.ssplit, a.saddr, e.low_R, s, &w.scan, &a.st->low_R));
     k_sah_children<<<L.grid(e.low_R, kBlock, 2), kBlock, 0, s>>>(a);
@@ -1879,15 +2015,13 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
     const int64_t F = st.F, nl = st.n_leaf_ids;
     KDGB_CHECK(ensure(t.leaf_ids, nl, s));
     KDGB_CHECK(ensure(t.prim_indices, F, s));
-    if (p.lower == KDGB_LOWER_SAH) {
-        KDGB_CHECK(grab(w.areas, F, s));
-        KDGB_CHECK(grab(w.sts, 3 * F, s));
-    }
+    if (p.lower == KDGB_LOWER_SAH) KDGB_CHECK(grab(w.areas, F, s));
+    if (lower_loop(p)) KDGB_CHECK(grab(w.sts, 3 * F, s));
     {
         const Extents e{0, 0, F, st.n_nodes, nl, 0};
         KDGB_CHECK(emit_after_upper(make_args(t, p, T, M, mesh_off_dev), L, e, p, s));
     }
-    if (p.lower == KDGB_LOWER_SAH) {
+    if (lower_loop(p)) {
         KDGB_CHECK(fetch_state(t, st, s));
         while (st.low_R > 0) {
             const int64_t R = st.low_R;
@@ -2046,7 +2180,7 @@ int capture_build(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_p
     KDGB_CHECK(emit_after_upper(a, L, e, p, cs));
     c1 = kdgb_launch_count();
     counts.fixed += c1 - c0;
-    if (p.lower == KDGB_LOWER_SAH) {
+    if (lower_loop(p)) {
         KDGB_CHECK(capture_while(cs, body, [&](cudaGraphConditionalHandle h) {
             BuildArgs b = a;
             b.lower_cond = h;

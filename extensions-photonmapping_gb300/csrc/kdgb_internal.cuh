@@ -163,6 +163,13 @@ struct Tree {
 // Makes t.woop current (kdgb_trace.cu).
 int woop_values(const Tree &t, cudaStream_t s);
 
+// Lower creators that split the upper leaves level by level over bitmap
+// sets (SAH and balanced); BITMAP only converts the leaves.
+inline bool lower_loop(const kdgb_build_params &p)
+{
+    return p.lower == KDGB_LOWER_SAH || p.lower == KDGB_LOWER_BALANCED;
+}
+
 // Builder (kdgb_build.cu), both modes, host-driven.  tri_v_dev: T*9 floats.
 // With M > 1 the triangles are M meshes (mesh m = [mesh_off[m],
 // mesh_off[m+1]), device offsets) built as one forest whose root of mesh m is

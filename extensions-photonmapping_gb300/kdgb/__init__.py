@@ -21,13 +21,15 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import scenes
-from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ISECT_MOELLER, ISECT_WOOP, ERR_CAPACITY, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, FINF, LEAF, LOWER_BITMAP, LOWER_SAH,
+from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ISECT_MOELLER, ISECT_WOOP, ERR_CAPACITY, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, FINF, LEAF, LOWER_BALANCED, LOWER_BITMAP, LOWER_SAH,
+                   SPLIT_BOX, SPLIT_DIVIDE, SPLIT_SPLIT,
                    TIE_LOWEST_ID, TIE_REF_LAST, TRACER_BRUTE, TRACER_RESTART, TRACER_SHORTSTACK, X, Y, Z,
                    AutotuneResult, BuildParams, BuildStats, KdgbError, Light, light, PhotonParams, TraceParams, TreeView, build_params, check,
                    lib, library_path, photon_params, trace_params)
 
 __all__ = ["KDTree", "Graph", "autotune", "AutotuneResult", "Light", "light", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
            "trace_params", "photon_params", "PhotonParams", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
+           "LOWER_BALANCED", "SPLIT_BOX", "SPLIT_DIVIDE", "SPLIT_SPLIT",
            "BUILD_REFERENCE", "BUILD_TUNED", "TRACER_RESTART", "TRACER_SHORTSTACK", "TRACER_BRUTE",
            "TIE_LOWEST_ID", "TIE_REF_LAST", "ISECT_MOELLER", "ISECT_WOOP", "FINF", "lib", "library_path"]
 
@@ -463,13 +465,13 @@ class TriangleMap:
             self.tree.rebuild(self.geometry, self.params)
         self.construction_time = self.tree.stats().build_ms
 
+    _LOWER = {BITMAP: LOWER_BITMAP, BALANCED: LOWER_BALANCED, SAH: LOWER_SAH}
+
     def SetLowerAlgorithm(self, algo: int) -> None:
-        if algo == self.BALANCED:
-            raise KdgbError(8, "SetLowerAlgorithm(BALANCED)")
-        self.params.lower = LOWER_SAH if algo == self.SAH else LOWER_BITMAP
+        self.params.lower = self._LOWER[algo]
 
     def GetLowerAlgorithm(self) -> int:
-        return self.SAH if self.params.lower == LOWER_SAH else self.BITMAP
+        return {v: k for k, v in self._LOWER.items()}[self.params.lower]
 
     def SplitEmptySpace(self, s: bool) -> None:
         self.params.split_empty_space = int(bool(s))
@@ -478,11 +480,12 @@ class TriangleMap:
         return bool(self.params.split_empty_space)
 
     def SetSplitMethod(self, m: int) -> None:
-        if m != self.BOX:
-            raise KdgbError(8, "SetSplitMethod: only BOX is provided")
+        # SPLIT is accepted here and refused by Create(), where the reference
+        # throws NotImplemented (TriangleMapUpperCreator.cu:551-552).
+        self.params.split_method = {self.BOX: SPLIT_BOX, self.DIVIDE: SPLIT_DIVIDE, self.SPLIT: SPLIT_SPLIT}[m]
 
     def GetSplitMethod(self) -> int:
-        return self.BOX
+        return int(self.params.split_method)
 
     def SetPropagateBoundingBox(self, p: bool) -> None:
         self.params.propagate_aabbs = int(bool(p))

@@ -11,7 +11,8 @@ import os
 from . import _build
 
 LEAF, X, Y, Z = 0, 1, 2, 3
-LOWER_BITMAP, LOWER_SAH = 0, 1
+LOWER_BITMAP, LOWER_SAH, LOWER_BALANCED = 0, 1, 2
+SPLIT_BOX, SPLIT_DIVIDE, SPLIT_SPLIT = 0, 1, 2
 BUILD_REFERENCE, BUILD_TUNED = 0, 1
 TRACER_RESTART, TRACER_SHORTSTACK, TRACER_BRUTE = 0, 1, 2
 TIE_LOWEST_ID, TIE_REF_LAST = 0, 1
@@ -36,7 +37,7 @@ class BuildParams(C.Structure):
                 ("propagate_aabbs", C.c_int32), ("empty_space_threshold", C.c_float),
                 ("traversal_cost", C.c_float), ("intersection_cost", C.c_float), ("min_leaf", C.c_int32),
                 ("esc_zmax_as_x", C.c_int32), ("max_levels", C.c_int32), ("leaf_size", C.c_int32),
-                ("upper_levels", C.c_int32), ("sah_bins", C.c_int32)]
+                ("upper_levels", C.c_int32), ("sah_bins", C.c_int32), ("split_method", C.c_int32)]
 
 
 class TraceParams(C.Structure):

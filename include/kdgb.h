@@ -40,7 +40,7 @@ typedef struct CUstream_st *kdgb_stream_t; /* same type as cudaStream_t */
 #define KDGB_API
 #endif
 
-#define KDGB_ABI_VERSION 2
+#define KDGB_ABI_VERSION 3
 
 /* Utils/CUDA/Utils.h:18: the reference's "infinity" is the integer
  * 0x7f800000 converted to float. */
@@ -62,8 +62,20 @@ typedef enum kdgb_status {
 /* KDNode.h:59-62 */
 enum { KDGB_LEAF = 0, KDGB_X = 1, KDGB_Y = 2, KDGB_Z = 3 };
 
-/* TriangleMap.h:33 LowerAlgorithm (BALANCED not provided). */
-enum { KDGB_LOWER_BITMAP = 0, KDGB_LOWER_SAH = 1 };
+/* TriangleMap.h:33 LowerAlgorithm: BITMAP converts the upper leaves to
+ * bitmap leaves (TriangleMapBitmapCreator), SAH splits them by the surface
+ * area heuristic (TriangleMapSAHCreator), BALANCED by the reference's
+ * "SSAH" set-size rule (TriangleMapBalancedCreator: split when
+ * (traversal_cost + small^2 + large^2) / n < n; traversal_cost must be
+ * >= 0).  The values differ from the reference enum's order. */
+enum { KDGB_LOWER_BITMAP = 0, KDGB_LOWER_SAH = 1, KDGB_LOWER_BALANCED = 2 };
+
+/* TriangleMap.h:34 SplitMethod of the upper phase: BOX sides from the
+ * clipped reference boxes (SetSplitSide), DIVIDE also tests a straddling
+ * triangle against the two halves of the node box (SetDivideSide, may drop
+ * references whose triangle misses the node).  The reference's SPLIT is not
+ * implemented there either and is rejected (KDGB_ERR_UNSUPPORTED). */
+enum { KDGB_SPLIT_BOX = 0, KDGB_SPLIT_DIVIDE = 1, KDGB_SPLIT_SPLIT = 2 };
 
 /* Build modes.  REFERENCE reproduces TriangleMap::Create bit for bit.
  * TUNED splits the top `upper_levels` levels at the reference's spatial
@@ -90,7 +102,7 @@ enum { KDGB_TIE_LOWEST_ID = 0, KDGB_TIE_REF_LAST = 1 };
 
 typedef struct kdgb_build_params {
     int32_t mode;                  /* KDGB_BUILD_* */
-    int32_t lower;                 /* KDGB_LOWER_* (REFERENCE mode), TriangleMap.cu:46 default BITMAP */
+    int32_t lower;                 /* KDGB_LOWER_*, TriangleMap.cu:46 default BITMAP */
     int32_t split_empty_space;     /* TriangleMapUpperCreator.cu:31 default 1 */
     int32_t propagate_aabbs;       /* TriangleMap.cu:47 default 1 */
     float   empty_space_threshold; /* TriangleMapUpperCreator.cu:28 default 0.35 */
@@ -102,6 +114,7 @@ typedef struct kdgb_build_params {
     int32_t leaf_size;             /* KDNode.h:21 KDNODE_MAX_LOWER_SIZE, default 32, <= 32 */
     int32_t upper_levels;          /* TUNED: median/empty-space levels before SAH, default 8 */
     int32_t sah_bins;              /* TUNED: SAH bins per axis, 2..32, default 32 */
+    int32_t split_method;          /* KDGB_SPLIT_*, TriangleMapUpperCreator.cu:32 default BOX */
 } kdgb_build_params;
 
 typedef struct kdgb_trace_params {

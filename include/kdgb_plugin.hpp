@@ -276,18 +276,22 @@ public:
     LowerAlgorithm GetLowerAlgorithm() const { return lower_; }
     void SetLowerAlgorithm(const LowerAlgorithm l)
     {
-        if (l == BALANCED) throw Core::Exception("TriangleMap: the BALANCED lower creator is not provided");
         lower_ = l;
-        p_.lower = l == SAH ? KDGB_LOWER_SAH : KDGB_LOWER_BITMAP;
+        p_.lower = l == SAH ? KDGB_LOWER_SAH : (l == BALANCED ? KDGB_LOWER_BALANCED : KDGB_LOWER_BITMAP);
     }
     float GetConstructionTime() const { return constructionTime_; }
     void SplitEmptySpace(const bool s) { p_.split_empty_space = s; }
     bool IsSplittingEmptySpace() const { return p_.split_empty_space != 0; }
+    // SPLIT is stored and refused by Create(), where the reference throws
+    // NotImplemented (TriangleMapUpperCreator.cu:551-552).
     void SetSplitMethod(const SplitMethod m)
     {
-        if (m != BOX) throw Core::Exception("TriangleMap: only the BOX split method is provided");
+        p_.split_method = m == DIVIDE ? KDGB_SPLIT_DIVIDE : (m == SPLIT ? KDGB_SPLIT_SPLIT : KDGB_SPLIT_BOX);
     }
-    SplitMethod GetSplitMethod() const { return BOX; }
+    SplitMethod GetSplitMethod() const
+    {
+        return p_.split_method == KDGB_SPLIT_DIVIDE ? DIVIDE : (p_.split_method == KDGB_SPLIT_SPLIT ? SPLIT : BOX);
+    }
     void SetPropagateBoundingBox(const bool p) { p_.propagate_aabbs = p; }
     bool GetPropagateBoundingBox() const { return p_.propagate_aabbs != 0; }
     void SetTraversalCost(const float t) { p_.traversal_cost = t; }

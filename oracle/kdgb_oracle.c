@@ -758,6 +758,7 @@ void or_build_params_default(or_build_params *p)
     p->mode = 0;
     p->upper_levels = 8;
     p->sah_bins = 32;
+    p->split_method = OR_SPLIT_BOX;
 }
 
 void or_trace_params_default(or_trace_params *p)
@@ -921,6 +922,60 @@ static int sah_binned_split(const f4 *cmin, const f4 *cmax, int32_t s, int32_t a
  * reference only schedule its reduction; the tight box of a node is the
  * exact min/max over its references, which is what is computed here.
  */
+/* One separating axis of Akenine-Moeller's triangle/box test (step 3: a
+ * triangle edge crossed with a box axis), in the two coordinates (s, t)
+ * perpendicular to the box axis: edge a->b, third vertex c, box half sizes
+ * hs, ht, all relative to the box centre.  The slack r = (... + 1e-5) *
+ * 1.0001 is IntersectionTests.h:20-21 (GAMMA, EPSILON); the expressions
+ * follow a0XTests/a1XTests/a2XTests (IntersectionTests.h:23-149). */
+static inline int sat_edge(float as, float at, float bs, float bt, float cs, float ct, float hs, float ht)
+{
+    const float p0 = at * bs - as * bt;
+    const float p1 = (bs - as) * ct - (bt - at) * cs;
+    float r = ht * fabsf(bs - as) + hs * fabsf(bt - at) + 0.00001f;
+    r *= 1.0001f;
+    return !((p0 > r && p1 > r) || (p0 < -r && p1 < -r));
+}
+
+/* TriangleAabbIntersectionStep3 (IntersectionTests.h:378-395): the nine
+ * edge-axis tests against the box [lo, hi]. */
+static int tri_box_step3(v3 v0, v3 v1, v3 v2, v3 lo, v3 hi)
+{
+    const v3 h = mk3((hi.x - lo.x) * 0.5f, (hi.y - lo.y) * 0.5f, (hi.z - lo.z) * 0.5f);
+    const v3 c = mk3(lo.x + h.x, lo.y + h.y, lo.z + h.z);
+    v0 = sub3(v0, c); v1 = sub3(v1, c); v2 = sub3(v2, c);
+    int ok = 1;
+    /* box axis x: coordinates (y, z) */
+    ok &= sat_edge(v0.y, v0.z, v1.y, v1.z, v2.y, v2.z, h.y, h.z);
+    ok &= sat_edge(v1.y, v1.z, v2.y, v2.z, v0.y, v0.z, h.y, h.z);
+    ok &= sat_edge(v2.y, v2.z, v0.y, v0.z, v1.y, v1.z, h.y, h.z);
+    /* box axis y: coordinates (z, x) */
+    ok &= sat_edge(v0.z, v0.x, v1.z, v1.x, v2.z, v2.x, h.z, h.x);
+    ok &= sat_edge(v1.z, v1.x, v2.z, v2.x, v0.z, v0.x, h.z, h.x);
+    ok &= sat_edge(v2.z, v2.x, v0.z, v0.x, v1.z, v1.x, h.z, h.x);
+    /* box axis z: coordinates (x, y) */
+    ok &= sat_edge(v0.x, v0.y, v1.x, v1.y, v2.x, v2.y, h.x, h.y);
+    ok &= sat_edge(v1.x, v1.y, v2.x, v2.y, v0.x, v0.y, h.x, h.y);
+    ok &= sat_edge(v2.x, v2.y, v0.x, v0.y, v1.x, v1.y, h.x, h.y);
+    return ok;
+}
+
+/* SetDivideSide<false> (TriangleUpperChildren.h:64-142): a reference whose
+ * box straddles the plane is tested against the two halves of the node box
+ * with the triangle itself, and may go to one side only (or to none, when
+ * the triangle misses the node box although its clipped box does not). */
+static inline void divide_sides(const float *tri, int32_t prim, f4 bmin, f4 bmax, int axis, float sp,
+                                int32_t *left, int32_t *right)
+{
+    const float *tp = tri + 9 * (size_t)prim;
+    const v3 v0 = ld3(tp), v1 = ld3(tp + 3), v2 = ld3(tp + 6);
+    const v3 lo = mk3(bmin.x, bmin.y, bmin.z), hi = mk3(bmax.x, bmax.y, bmax.z);
+    const v3 lhi = mk3(axis == OR_X ? sp : hi.x, axis == OR_Y ? sp : hi.y, axis == OR_Z ? sp : hi.z);
+    const v3 rlo = mk3(axis == OR_X ? sp : lo.x, axis == OR_Y ? sp : lo.y, axis == OR_Z ? sp : lo.z);
+    *left = tri_box_step3(v0, v1, v2, lo, lhi);
+    *right = tri_box_step3(v0, v1, v2, rlo, hi);
+}
+
 static int build_upper(const float *tri, int32_t T, const or_build_params *p, nodes *nd,
                        f4 **fmin_out, f4 **fmax_out, int32_t *nfinal_out, ivec *leaf_ids,
                        int32_t *levels_out)
@@ -1093,7 +1148,9 @@ static int build_upper(const float *tri, int32_t T, const or_build_params *p, no
             const int32_t s = nd->pidx[active + k], a = nd->amt[active + k];
             for (int32_t r = s; r < s + a; ++r) owner[r] = k;
         }
-        /* SetSplitSide (TriangleUpperChildren.h:10-62). */
+        /* SetSplitSide (TriangleUpperChildren.h:10-62), or SetDivideSide<false>
+         * (TriangleUpperChildren.h:64-142) with the DIVIDE split method. */
+        const int divide = p->split_method == OR_SPLIT_DIVIDE;
 #pragma omp parallel for schedule(static)
         for (int64_t r = 0; r < N; ++r) {
             const int32_t node = active + owner[r];
@@ -1101,11 +1158,15 @@ static int build_upper(const float *tri, int32_t T, const or_build_params *p, no
             const float sp = nd->split[node];
             side[r] = f4c(cmin[r], axis) <= sp;
             side[N + r] = sp < f4c(cmax[r], axis);
+            if (divide && side[r] && side[N + r])
+                divide_sides(tri, f2i(cmin[r].w), nd->bmin[node], nd->bmax[node], axis, sp, &side[r], &side[N + r]);
         }
         side[2 * N] = 0;
         excl_scan(side, 2 * N, saddr);
         int64_t new_tris = saddr[2 * N];
-        if (new_tris < N) { rc = OR_ERR_SPLIT; goto out; }
+        /* Box sides keep every reference; DIVIDE may drop references whose
+         * triangle misses the node box. */
+        if (!divide && new_tris < N) { rc = OR_ERR_SPLIT; goto out; }
 
         /* CalcNodeChildSize (TriangleUpperChildren.h:144-162). */
         int created_leafs = 0;
@@ -1335,39 +1396,75 @@ static inline void calc_area_for_sets(const int32_t sets_in[4], int axis, int32_
     }
 }
 
+/* CalcRelationForSets (LowerTriangleMap.h:260-295): the node's sets of one
+ * plane pair, weighted by small^2 + large^2 of the two set sizes; the first
+ * strictly smaller weight wins. */
+static inline void relation_for_sets(const int32_t sets_in[4], uint32_t node_set, int axis, int32_t set_index,
+                                     int *weight, uint32_t *ls, uint32_t *rs, int *opt_axis, int32_t *split_index)
+{
+    const uint32_t s[4] = {(uint32_t)sets_in[0] & node_set, (uint32_t)sets_in[1] & node_set,
+                           (uint32_t)sets_in[2] & node_set, (uint32_t)sets_in[3] & node_set};
+    for (int h = 0; h < 2; ++h) {
+        const int a = __builtin_popcount(s[2 * h]), b = __builtin_popcount(s[2 * h + 1]);
+        const int small = a < b ? a : b, large = a < b ? b : a;
+        const int w = small * small + large * large;
+        if (w < *weight) {
+            *weight = w;
+            *ls = s[2 * h]; *rs = s[2 * h + 1];
+            *opt_axis = axis;
+            *split_index = h ? (int32_t)((uint32_t)set_index | 0x80000000u) : set_index;
+        }
+    }
+}
+
 /*
- * Lower SAH phase: TriangleMapSAHCreator.cu:67-260 with kernels
- * LowerTriangleMap.h:24-155 (areas, preprocessing, splitting planes) and
- * :412-636 (CalcSAH, CreateLowerSAHChildren, PropagateAabbToChildren).
- * With intersection_cost = 1 and min_leaf = 0 the split rule is the
- * reference's `optimalArea < (bitcount - traversalCost) * nodeArea`.
+ * Lower phase with bitmap sets, two creators:
+ *  - SAH: TriangleMapSAHCreator.cu:67-260 with kernels LowerTriangleMap.h:24-155
+ *    (areas, preprocessing, splitting planes) and :412-636 (CalcSAH,
+ *    CreateLowerSAHChildren, PropagateAabbToChildren).  With
+ *    intersection_cost = 1 and min_leaf = 0 the split rule is the
+ *    reference's `optimalArea < (bitcount - traversalCost) * nodeArea`.
+ *  - BALANCED ("SSAH"): TriangleMapBalancedCreator.cu:60-248 with
+ *    PreprocessLeafNodes (LowerTriangleMap.h:40-53), the same splitting
+ *    planes, CalcSplit (:299-369) and CreateChildren (:371-410).  Node areas
+ *    stay zero (the creator never writes them); TrimChildBitmaps never runs
+ *    (removeFalsePrimitives is fixed to false, TriangleMapBalancedCreator.cu:35).
  */
-static int build_lower_sah(const float *tri, const or_build_params *p, nodes *nd,
-                           const f4 *fmin, const f4 *fmax, int32_t NF,
-                           const int32_t *prim_indices, const ivec *leaf_ids, int32_t *levels_out)
+static int build_lower(const float *tri, const or_build_params *p, nodes *nd,
+                       const f4 *fmin, const f4 *fmax, int32_t NF,
+                       const int32_t *prim_indices, const ivec *leaf_ids, int32_t *levels_out)
 {
     int rc = 0;
+    const int balanced = p->lower == OR_LOWER_BALANCED;
     float *areas = malloc(sizeof(float) * (size_t)(NF > 0 ? NF : 1));
     int32_t *sts = malloc(sizeof(int32_t) * 12 * (size_t)(NF > 0 ? NF : 1));
     int32_t *act = NULL, *ssplit = NULL, *saddr = NULL, *csets = NULL;
     float *careas = NULL;
     if (!areas || !sts) { rc = OR_ERR_ALLOC; goto out; }
-    for (int32_t i = 0; i < NF; ++i) areas[i] = tri_area(tri, prim_indices[i]);
 
-    /* PreprocesLowerNodes (LowerTriangleMap.h:56-81). */
     const int32_t R0 = (int32_t)leaf_ids->n;
-    for (int32_t k = 0; k < R0; ++k) {
-        const int32_t leaf = leaf_ids->a[k];
-        const int32_t pi = nd->pidx[leaf], amt = nd->amt[leaf];
-        float area = 0.0f;
-        uint32_t bmp = 0;
-        for (int32_t i = 0; i < amt; ++i) {
-            const float a = areas[pi + i];
-            bmp += a > 0.0f ? (1u << i) : 0u;
-            area += a;
+    if (balanced) {
+        /* PreprocessLeafNodes (LowerTriangleMap.h:40-53): every reference. */
+        for (int32_t k = 0; k < R0; ++k) {
+            const int32_t leaf = leaf_ids->a[k];
+            nd->amt[leaf] = (int32_t)((1u << nd->amt[leaf]) - 1u);
         }
-        nd->area[leaf] = area;
-        nd->amt[leaf] = (int32_t)bmp;
+    } else {
+        for (int32_t i = 0; i < NF; ++i) areas[i] = tri_area(tri, prim_indices[i]);
+        /* PreprocesLowerNodes (LowerTriangleMap.h:56-81). */
+        for (int32_t k = 0; k < R0; ++k) {
+            const int32_t leaf = leaf_ids->a[k];
+            const int32_t pi = nd->pidx[leaf], amt = nd->amt[leaf];
+            float area = 0.0f;
+            uint32_t bmp = 0;
+            for (int32_t i = 0; i < amt; ++i) {
+                const float a = areas[pi + i];
+                bmp += a > 0.0f ? (1u << i) : 0u;
+                area += a;
+            }
+            nd->area[leaf] = area;
+            nd->amt[leaf] = (int32_t)bmp;
+        }
     }
     /* CreateSplittingPlanes (LowerTriangleMap.h:84-155): sets per prim slot,
      * per axis {lowLeft, lowRight, highLeft, highRight}. */
@@ -1416,8 +1513,47 @@ static int build_lower_sah(const float *tri, const or_build_params *p, nodes *nd
         if (!act || !ssplit || !saddr || !csets || !careas) { rc = OR_ERR_ALLOC; goto out; }
         for (int32_t k = 0; k < R; ++k) act[k] = use_idx ? leaf_ids->a[k] : active + k;
 
-        /* CalcSAH (LowerTriangleMap.h:463-555). */
         const float ct = p->traversal_cost, ci = p->intersection_cost;
+        if (balanced) {
+            /* CalcSplit (LowerTriangleMap.h:299-369). */
+#pragma omp parallel for schedule(dynamic, 16)
+            for (int32_t k = 0; k < R; ++k) {
+                const int32_t par = act[k];
+                const int32_t pi = nd->pidx[par];
+                const uint32_t bmp = (uint32_t)nd->amt[par];
+                int weight = 32 * 32, axis = 0;
+                uint32_t ls = 0, rs = 0;
+                int32_t split_index = 0;
+                uint32_t tris = bmp;
+                while (tris) {
+                    const int i = __builtin_ctz(tris);
+                    relation_for_sets(sts + 4 * (size_t)(pi + i), bmp, OR_X, pi + i, &weight, &ls, &rs, &axis,
+                                      &split_index);
+                    relation_for_sets(sts + 4 * ((size_t)NF + pi + i), bmp, OR_Y, pi + i, &weight, &ls, &rs, &axis,
+                                      &split_index);
+                    relation_for_sets(sts + 4 * (2 * (size_t)NF + pi + i), bmp, OR_Z, pi + i, &weight, &ls, &rs,
+                                      &axis, &split_index);
+                    tris &= tris - 1u;
+                }
+                /* A split needs a plane (the reference's sets are
+                 * uninitialised otherwise; with traversal_cost >= 0 no
+                 * split is possible without one). */
+                const float cnt = (float)__builtin_popcount(bmp);
+                const float ssah = (ct + (float)weight) / cnt;
+                const int split = weight < 32 * 32 && ssah < cnt;
+                if (split) {
+                    careas[2 * k] = 0.0f; careas[2 * k + 1] = 0.0f;
+                    csets[2 * k] = (int32_t)ls; csets[2 * k + 1] = (int32_t)rs;
+                    f4 sp4;
+                    if ((uint32_t)split_index & 0x80000000u) sp4 = fmax[(uint32_t)split_index ^ 0x80000000u];
+                    else sp4 = fmin[split_index];
+                    nd->split[par] = f4c(sp4, axis);
+                }
+                nd->info[par] = split ? (int8_t)axis : OR_LEAF;
+                ssplit[k] = split;
+            }
+        } else {
+        /* CalcSAH (LowerTriangleMap.h:463-555). */
 #pragma omp parallel for schedule(dynamic, 16)
         for (int32_t k = 0; k < R; ++k) {
             const int32_t par = act[k];
@@ -1456,11 +1592,13 @@ static int build_lower_sah(const float *tri, const or_build_params *p, nodes *nd
             nd->info[par] = split ? (int8_t)axis : OR_LEAF;
             ssplit[k] = split;
         }
+        }
         excl_scan(ssplit, R, saddr);
         const int32_t splits = saddr[R];
         const int32_t child_base = nd->n;
         if ((rc = nodes_resize(nd, nd->n + 2 * splits))) goto out;
-        /* CreateLowerSAHChildren (LowerTriangleMap.h:557-600). */
+        /* CreateLowerSAHChildren (LowerTriangleMap.h:557-600); CreateChildren
+         * (:371-410) is the same without areas. */
         for (int32_t k = 0; k < R; ++k) {
             if (!ssplit[k]) continue;
             const int32_t par = act[k];
@@ -1500,6 +1638,11 @@ int or_build(const float *tri, int32_t T, const or_build_params *p, or_tree *out
     if (!out || !p || T < 0 || (T > 0 && !tri)) return OR_ERR_ARG;
     if (p->leaf_size < 1 || p->leaf_size > 32) return OR_ERR_ARG;
     if (p->mode == 1 && (p->sah_bins < 2 || p->sah_bins > 32 || p->upper_levels < 0)) return OR_ERR_ARG;
+    if (p->lower < OR_LOWER_BITMAP || p->lower > OR_LOWER_BALANCED) return OR_ERR_ARG;
+    if (p->split_method != OR_SPLIT_BOX && p->split_method != OR_SPLIT_DIVIDE) return OR_ERR_ARG;
+    /* A negative cost lets the balanced rule split a node into itself and
+     * an empty child forever. */
+    if (p->lower == OR_LOWER_BALANCED && !(p->traversal_cost >= 0.0f)) return OR_ERR_ARG;
     memset(out, 0, sizeof(*out));
     nodes nd;
     memset(&nd, 0, sizeof(nd));
@@ -1514,8 +1657,8 @@ int or_build(const float *tri, int32_t T, const or_build_params *p, or_tree *out
     if (!prim_indices) { rc = OR_ERR_ALLOC; goto fail; }
     for (int32_t i = 0; i < NF; ++i) prim_indices[i] = f2i(fmin[i].w);
 
-    if (p->lower == OR_LOWER_SAH) {
-        rc = build_lower_sah(tri, p, &nd, fmin, fmax, NF, prim_indices, &leaf_ids, &lo_levels);
+    if (p->lower == OR_LOWER_SAH || p->lower == OR_LOWER_BALANCED) {
+        rc = build_lower(tri, p, &nd, fmin, fmax, NF, prim_indices, &leaf_ids, &lo_levels);
         if (rc) { free(prim_indices); goto fail; }
     } else {
         /* TriangleMapBitmapCreator.cu:32-49 PreprocessLeafNodes. */

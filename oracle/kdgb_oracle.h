@@ -34,12 +34,15 @@ extern "C" {
 #define OR_FINF 2139095040.0f
 
 enum { OR_LEAF = 0, OR_X = 1, OR_Y = 2, OR_Z = 3 };
-enum { OR_LOWER_BITMAP = 0, OR_LOWER_SAH = 1 };
+enum { OR_LOWER_BITMAP = 0, OR_LOWER_SAH = 1, OR_LOWER_BALANCED = 2 };
+/* TriangleMap::SplitMethod (TriangleMap.h:34); SPLIT is not implemented by
+ * the reference (TriangleMapUpperCreator.cu:551-552). */
+enum { OR_SPLIT_BOX = 0, OR_SPLIT_DIVIDE = 1 };
 enum { OR_TIE_LOWEST_ID = 0, OR_TIE_REF_LAST = 1 };
 enum { OR_TRACER_RESTART = 0, OR_TRACER_SHORTSTACK = 1, OR_TRACER_BRUTE = 2 };
 
 typedef struct or_build_params {
-    int32_t lower;                 /* OR_LOWER_BITMAP (reference default) or OR_LOWER_SAH */
+    int32_t lower;                 /* OR_LOWER_BITMAP (reference default), OR_LOWER_SAH or OR_LOWER_BALANCED */
     int32_t split_empty_space;     /* TriangleMapUpperCreator.cu:31 default true */
     int32_t propagate_aabbs;       /* TriangleMap.cu:47 default true */
     float   empty_space_threshold; /* TriangleMapUpperCreator.cu:28 default 0.35 */
@@ -52,6 +55,7 @@ typedef struct or_build_params {
     int32_t mode;                  /* 0 reference, 1 tuned (binned SAH below upper_levels) */
     int32_t upper_levels;          /* tuned: median / empty-space levels before the binned SAH */
     int32_t sah_bins;              /* tuned: bins per axis */
+    int32_t split_method;          /* OR_SPLIT_BOX (TriangleMapUpperCreator.cu:32 default) or OR_SPLIT_DIVIDE */
 } or_build_params;
 
 typedef struct or_tree {

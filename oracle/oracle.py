@@ -20,7 +20,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "libkdgb_oracle.so")
 
 LEAF, X, Y, Z = 0, 1, 2, 3
-LOWER_BITMAP, LOWER_SAH = 0, 1
+LOWER_BITMAP, LOWER_SAH, LOWER_BALANCED = 0, 1, 2
+SPLIT_BOX, SPLIT_DIVIDE = 0, 1
 TIE_LOWEST_ID, TIE_REF_LAST = 0, 1
 TRACER_RESTART, TRACER_SHORTSTACK, TRACER_BRUTE = 0, 1, 2
 ISECT_MOELLER, ISECT_WOOP = 0, 1
@@ -33,7 +34,7 @@ class BuildParams(C.Structure):
                 ("traversal_cost", C.c_float), ("intersection_cost", C.c_float),
                 ("min_leaf", C.c_int32), ("esc_zmax_as_x", C.c_int32),
                 ("max_levels", C.c_int32), ("leaf_size", C.c_int32), ("mode", C.c_int32),
-                ("upper_levels", C.c_int32), ("sah_bins", C.c_int32)]
+                ("upper_levels", C.c_int32), ("sah_bins", C.c_int32), ("split_method", C.c_int32)]
 
 
 class TraceParams(C.Structure):

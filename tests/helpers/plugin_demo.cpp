@@ -28,14 +28,17 @@ int main(int argc, char **argv)
     geom.AddMesh(osc, model);
 
     TriangleMap map(&geom);
-    map.SetLowerAlgorithm(TriangleMap::SAH);
+    // The SPLIT method is refused at Create(), as the reference's is.
+    map.SetSplitMethod(TriangleMap::SPLIT);
     bool threw = false;
     try {
-        map.SetLowerAlgorithm(TriangleMap::BALANCED);
+        map.Create();
     } catch (const Core::Exception &) {
         threw = true;
     }
     if (!threw) return 3;
+    map.SetSplitMethod(TriangleMap::BOX);
+    map.SetLowerAlgorithm(TriangleMap::SAH);
     map.Create();
     if (map.GetNodes()->GetSize() < 3) return 4;
 

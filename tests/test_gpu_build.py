@@ -1,5 +1,7 @@
-"""GPU build parity: the reference-mode build of libkdgb.so must produce the
-oracle's tree bit for bit (node arrays, leaf lists, reference order)."""
+"""GPU build parity: every build of libkdgb.so (reference and tuned modes,
+BITMAP / SAH / BALANCED lower creators, BOX / DIVIDE split methods) must
+produce the oracle's tree bit for bit (node arrays, leaf lists, reference
+order)."""
 import numpy as np
 import pytest
 
@@ -46,7 +48,7 @@ def scene(name):
 
 
 @pytest.mark.parametrize("name", ["c1", "clustered3k", "clustered60k", "soup", "degenerate"])
-@pytest.mark.parametrize("lower", [0, 1])
+@pytest.mark.parametrize("lower", [0, 1, 2])
 def test_build_matches_oracle(kdgb_lib, cuda, oracle, name, lower):
     tris = scene(name)
     ref = oracle.build(tris, lower=lower)
@@ -64,6 +66,9 @@ def test_build_matches_oracle(kdgb_lib, cuda, oracle, name, lower):
     dict(lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8),
     dict(lower=1, propagate_aabbs=0),
     dict(empty_space_threshold=0.1),
+    dict(lower=2, traversal_cost=16.0),
+    dict(lower=2, traversal_cost=0.0, propagate_aabbs=0),
+    dict(lower=2, leaf_size=12),
 ])
 def test_build_options_match_oracle(kdgb_lib, cuda, oracle, opts):
     tris = scenes.clustered(8000, seed=14)
@@ -96,11 +101,47 @@ def test_tuned_build_options(kdgb_lib, cuda, oracle, opts):
         assert_same_tree(tree.to_host(), ref)
 
 
+@pytest.mark.parametrize("name", ["c1", "clustered3k", "clustered60k", "soup", "degenerate"])
+@pytest.mark.parametrize("lower", [0, 2])
+def test_divide_build_matches_oracle(kdgb_lib, cuda, oracle, name, lower):
+    """The DIVIDE split method (triangle against the two half boxes of a
+    straddled node) builds the oracle's tree bit for bit."""
+    tris = scene(name)
+    kw = dict(split_method=1, lower=lower)
+    ref = oracle.build(tris, **kw)
+    with kdgb_lib.KDTree.build(tris, **kw) as tree:
+        assert_same_tree(tree.to_host(), ref)
+
+
+def test_divide_drops_references_and_traces_like_brute_force(kdgb_lib, cuda, oracle):
+    tris = tri_soup(20000, 31, scale=0.08)
+    o, d = scenes.camera_rays(96, 64)
+    with kdgb_lib.KDTree.build(tris) as box, kdgb_lib.KDTree.build(tris, split_method=1, lower=2) as div:
+        assert div.stats().n_refs < box.stats().n_refs
+        brute = [x.cpu().numpy() for x in kdgb_lib.trace_brute(tris, o, d)]
+        for tracer in (0, 1):
+            got = [x.cpu().numpy() for x in div.trace(o, d, tracer=tracer)]
+            assert np.array_equal(got[0], brute[0]), tracer
+            if tracer == 0:
+                assert np.array_equal(got[1].view(np.uint32), brute[1].view(np.uint32))
+            else:  # the short stack measures t from a moved origin
+                assert np.allclose(got[1], brute[1], rtol=1e-5)
+
+
+def test_tuned_divide_balanced_matches_oracle(kdgb_lib, cuda, oracle):
+    kw = dict(TUNED, split_method=1, lower=2, traversal_cost=16.0)
+    tris = scenes.clustered(30000, seed=19)
+    ref = oracle.build(tris, **kw)
+    with kdgb_lib.KDTree.build(tris, **kw) as tree:
+        assert_same_tree(tree.to_host(), ref)
+
+
 @pytest.mark.parametrize("T", [0, 1, 2, 31, 32, 33, 257])
-def test_small_and_empty_builds(kdgb_lib, cuda, oracle, T):
+@pytest.mark.parametrize("kw", [dict(), dict(lower=2, split_method=1)])
+def test_small_and_empty_builds(kdgb_lib, cuda, oracle, T, kw):
     tris = tri_soup(max(T, 1), 30)[:T]
-    ref = oracle.build(tris)
-    with kdgb_lib.KDTree.build(tris) as tree:
+    ref = oracle.build(tris, **kw)
+    with kdgb_lib.KDTree.build(tris, **kw) as tree:
         assert_same_tree(tree.to_host(), ref)
 
 
@@ -130,7 +171,12 @@ def test_degenerate_duplicates_error(kdgb_lib, cuda):
 
 def test_invalid_params(kdgb_lib, cuda):
     tris = scenes.clustered(100, seed=2)
-    for bad in (dict(leaf_size=33), dict(leaf_size=0), dict(lower=5), dict(mode=7)):
+    for bad in (dict(leaf_size=33), dict(leaf_size=0), dict(lower=5), dict(mode=7), dict(split_method=7),
+                dict(lower=2, traversal_cost=-1.0)):
         with pytest.raises(kdgb_lib.KdgbError) as e:
             kdgb_lib.KDTree.build(tris, **bad)
         assert e.value.status == 1
+    # The reference's SPLIT method throws NotImplemented.
+    with pytest.raises(kdgb_lib.KdgbError) as e:
+        kdgb_lib.KDTree.build(tris, split_method=2)
+    assert e.value.status == 8

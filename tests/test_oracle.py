@@ -86,7 +86,7 @@ def check_tree(tree, tris, leaf_size=32):
     return used, area
 
 
-@pytest.mark.parametrize("lower", [0, 1])
+@pytest.mark.parametrize("lower", [0, 1, 2])
 @pytest.mark.parametrize("scene", ["heightfield", "clustered", "soup"])
 def test_tree_invariants(oracle, scene, lower):
     if scene == "heightfield":
@@ -97,7 +97,7 @@ def test_tree_invariants(oracle, scene, lower):
         tris = tri_soup(2000, 7)
     tree = oracle.build(tris, lower=lower)
     used, area = check_tree(tree, tris)
-    if lower == 0:
+    if lower != 1:
         assert used.all()
     else:
         # The SAH lower phase drops zero-area triangles (LowerTriangleMap.h:74).
@@ -125,6 +125,70 @@ def test_tuned_differs_from_reference_below_median_levels(oracle):
     assert a.n_nodes != b.n_nodes or not np.array_equal(a.split, b.split)
     c = oracle.build(tris, mode=1, upper_levels=64)  # never reaches the SAH levels
     assert np.array_equal(c.split, b.split) and np.array_equal(c.children, b.children)
+
+
+def popc(x):
+    return bin(int(np.uint32(x))).count("1")
+
+
+@pytest.mark.parametrize("cost", [0.0, 16.0, 24.0])
+def test_balanced_split_rule(oracle, cost):
+    """Every balanced split divides a node's reference set into two covering
+    subsets with (cost + small^2 + large^2) / n < n (LowerTriangleMap.h:
+    299-369); every lower leaf has no plane that passes the rule."""
+    tris = scenes.clustered(4000, seed=21)
+    tree = oracle.build(tris, lower=2, traversal_cost=cost)
+    assert tree.lower_levels > 1
+    splits = 0
+    stack = [int(k) for k in tree.leaf_ids]
+    while stack:
+        k = stack.pop()
+        if tree.info[k] == 0:
+            continue
+        l, r = (int(c) for c in tree.children[k])
+        b, bl, br = (int(np.uint32(tree.bitmap[j])) for j in (k, l, r))
+        assert tree.prim_index[l] == tree.prim_index[r] == tree.prim_index[k]
+        assert bl | br == b and bl & ~b == 0 and br & ~b == 0
+        n, a, c = popc(b), popc(bl), popc(br)
+        assert np.float32(cost + (a * a + c * c)) / np.float32(n) < n
+        assert max(a, c) < n
+        splits += 1
+        stack += [l, r]
+    assert splits > 0
+    # Balanced trees keep every triangle and trace like brute force.
+    used, _ = check_tree(tree, tris)
+    assert used.all()
+    assert (tree.area == 0).all()
+
+
+@pytest.mark.parametrize("lower", [0, 2])
+def test_divide_keeps_triangles_and_traces_exactly(oracle, lower):
+    """DIVIDE (TriangleUpperChildren.h:64-142) drops references whose
+    triangle misses a half box, but never a triangle from every leaf: kd
+    traversal of the tree equals brute force."""
+    tris = tri_soup(6000, 23, scale=0.1)
+    box = oracle.build(tris, lower=lower)
+    div = oracle.build(tris, lower=lower, split_method=1)
+    assert div.prim_indices.shape[0] < box.prim_indices.shape[0]
+    used, _ = check_tree(div, tris)
+    assert used.all()
+    lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
+    o, d = scenes.random_rays(4000, 24, lo, hi)
+    hb, tb, _, _ = oracle.trace(None, tris, o, d, tracer=2)
+    for tracer in (0, 1):
+        h, t, _, _ = oracle.trace(div, tris, o, d, tracer=tracer)
+        assert np.array_equal(h, hb)
+        if tracer == 0:
+            assert np.array_equal(t.view(np.uint32), tb.view(np.uint32))
+        else:  # the short stack measures t from a moved origin
+            assert np.allclose(t, tb, rtol=1e-5)
+
+
+def test_split_method_and_lower_validation(oracle):
+    tris = scenes.clustered(200, seed=2)
+    for bad in (dict(split_method=2), dict(lower=3), dict(lower=2, traversal_cost=-1.0)):
+        with pytest.raises(RuntimeError, match="invalid argument"):
+            oracle.build(tris, **bad)
 
 
 def test_upper_leaf_boxes_contain_references(oracle):
@@ -180,7 +244,7 @@ def test_degenerate_duplicates_terminate(oracle):
 # ---------------------------------------------------------------------------
 
 @pytest.mark.parametrize("tracer", [0, 1])
-@pytest.mark.parametrize("lower", [0, 1])
+@pytest.mark.parametrize("lower", [0, 1, 2])
 def test_kd_tracers_match_brute_force(oracle, tracer, lower):
     tris = scenes.clustered(4000, seed=12)
     lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
