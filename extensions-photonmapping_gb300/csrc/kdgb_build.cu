@@ -52,7 +52,7 @@ constexpr int kWarps = kBlock / 32;
 constexpr int kTileRefs = kChunk * kWarps;  // references per block tile
 constexpr int kLanes = 7;                   // per-node scan lanes (see NodeLanes)
 // Tuned levels: nodes with at least this many references are binned by a
-// whole block (k_sah_block), smaller ones by one warp (k_sah_warp).
+// whole block, smaller ones by one warp (k_sah_bin).
 constexpr int kSahBlockRefs = 2048;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -261,8 +261,8 @@ __device__ __forceinline__ void keys_neutral(unsigned (&k)[6])
     k[3] = k[4] = k[5] = 0u;
 }
 
-// Tight node boxes: exact min/max over each node's references, as the
-// segmented reduction ReduceSegmentsUnrolled + FinalSegmentedReduce
+// Tight node boxes of the roots: exact min/max over each node's references,
+// as the segmented reduction ReduceSegmentsUnrolled + FinalSegmentedReduce
 // (ReduceSegments.h:230-371) computes.  Keys are order-preserving uint32
 // images of the floats, so atomicMin/atomicMax give exact results in any order.
 __global__ void __launch_bounds__(kBlock) k_reduce(const BuildArgs a)
@@ -468,10 +468,18 @@ __device__ __forceinline__ void divide_flags(const BuildArgs &a, int32_t prim, i
 
 // Per-node left/right counts, per-chunk totals of the flags and per-tile
 // totals (the tile totals are scanned into tile offsets; k_scatter adds the
-// chunk totals of the earlier warps of its tile).
+// chunk totals of the earlier warps of its tile).  Also resets the tight-box
+// keys of the next level's nodes (at most 2R of them) to the +-fInfinity box
+// (AabbMemset, ReduceSegments.h:328-335): k_node_split has consumed this
+// level's keys and k_scatter reduces the children's boxes into them.
 template <bool DIVIDE>
 __global__ void __launch_bounds__(kBlock) k_count(const BuildArgs a)
 {
+    {
+        const int64_t next = min(2 * (int64_t)a.st->R, a.cap.R);
+        const unsigned lo_key = fkey(KDGB_FINF), hi_key = fkey(-KDGB_FINF);
+        GRID_STRIDE(i, 6 * next) a.keys[i] = (i % 6) < 3 ? lo_key : hi_key;
+    }
     __shared__ int s_owner[kWarps], s_l[kWarps], s_r[kWarps], s_tl[kWarps], s_tr[kWarps];
     const BuildState *st = a.st;
     const int64_t N = st->N;
@@ -593,42 +601,58 @@ __device__ __forceinline__ int sah_bin(float x, float mn, float scale, int B)
 }
 
 
-// Bins the references [first, first + cnt) of one node into h[(axis * 2 +
-// side) * 32 + bin] (shared memory, zeroed by the caller).  A warp walks the
-// range in rows of 32 references, `warps` warps interleaved (warp `wid`
-// takes rows wid, wid + warps, ...), with one shared atomic per reference,
-// axis and side (cheaper here than merging equal bins with match_any).
-__device__ __forceinline__ void sah_fill(const float4 *__restrict__ cmin, const float4 *__restrict__ cmax,
-                                         int64_t first, int32_t cnt, const float (&lo)[3], const float (&scale)[3],
-                                         const bool (&valid)[3], int B, int *h, int wid, int warps)
+struct SahNode {
+    int32_t node, cnt;
+    int64_t first;
+    float mnv[3], mxv[3], ext[3], scale[3];
+    bool valid[3];
+};
+
+// Adds the references of rows row0, row0 + step, ... (32 references each)
+// of one node to the histograms h[(axis * 2 + side) * 32 + bin] (shared
+// memory private to the calling warp), one shared atomic per reference, axis
+// and side (cheaper than merging equal bins first).  kRows rows of loads are
+// in flight before any of them is binned.
+__device__ __forceinline__ void sah_rows(const float4 *__restrict__ cmin, const float4 *__restrict__ cmax,
+                                         const SahNode &n, int B, int row0, int step, int *h)
 {
     const int lane = threadIdx.x & 31;
-    for (int32_t i = wid * 32 + lane; i < cnt; i += warps * 32) {
-        const float4 p = cmin[first + i], q = cmax[first + i];
-        const float pv[3] = {p.x, p.y, p.z}, qv[3] = {q.x, q.y, q.z};
+    const int rows = (n.cnt + 31) >> 5;
+    for (int r0 = row0; r0 < rows; r0 += kRows * step) {
+        float4 p[kRows], q[kRows];
+        bool in[kRows];
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-            if (!valid[ax]) continue;
-            atomicAdd(h + (ax * 2 + 0) * 32 + sah_bin(pv[ax], lo[ax], scale[ax], B), 1);
-            atomicAdd(h + (ax * 2 + 1) * 32 + sah_bin(qv[ax], lo[ax], scale[ax], B), 1);
+        for (int u = 0; u < kRows; ++u) {
+            const int32_t i = (r0 + u * step) * 32 + lane;
+            in[u] = r0 + u * step < rows && i < n.cnt;
+            if (in[u]) { p[u] = cmin[n.first + i]; q[u] = cmax[n.first + i]; }
+        }
+#pragma unroll
+        for (int u = 0; u < kRows; ++u) {
+            if (!in[u]) continue;
+            const float pv[3] = {p[u].x, p[u].y, p[u].z}, qv[3] = {q[u].x, q[u].y, q[u].z};
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                if (!n.valid[ax]) continue;
+                atomicAdd(h + (ax * 2 + 0) * 32 + sah_bin(pv[ax], n.mnv[ax], n.scale[ax], B), 1);
+                atomicAdd(h + (ax * 2 + 1) * 32 + sah_bin(qv[ax], n.mnv[ax], n.scale[ax], B), 1);
+            }
         }
     }
 }
 
-// One warp evaluates the planes of a node from its histograms: lane k-1
-// takes the plane at bin boundary k; the first strict minimum over (axis,
-// k) wins.  Lane 0 writes the split.
-__device__ __forceinline__ void sah_pick(const BuildArgs &a, int32_t node, int32_t cnt, const float (&mnv)[3],
-                                         const float (&mxv)[3], const float (&ext)[3], const int *h, int lane)
+// One warp evaluates the planes of a node from its six histograms (lane j
+// holds bin j of each): lane k-1 takes the plane at bin boundary k; the first
+// strict minimum over (axis, k) wins.  Lane 0 writes the split.
+__device__ __forceinline__ void sah_pick(const BuildArgs &a, const SahNode &n, const int (&hv)[6], int lane)
 {
     const int B = a.B;
     float best = INFINITY, best_sp = 0.0f;
     int best_ax = -1;
     for (int ax = 0; ax < 3; ++ax) {
-        if (!(ext[ax] > 0.0f)) continue;  // warp-uniform
-        const int32_t lo = lane < B ? h[(ax * 2 + 0) * 32 + lane] : 0;
-        const int32_t hi = lane < B ? h[(ax * 2 + 1) * 32 + lane] : 0;
-        int32_t plo = lo, phi = hi;  // inclusive prefix sums over bins
+        if (!n.valid[ax]) continue;  // warp-uniform
+        int32_t plo = lane < B ? hv[ax * 2 + 0] : 0;  // inclusive prefix sums over bins
+        int32_t phi = lane < B ? hv[ax * 2 + 1] : 0;
         for (int s = 1; s < 32; s <<= 1) {
             const int32_t x = __shfl_up_sync(kFull, plo, s), y = __shfl_up_sync(kFull, phi, s);
             if (lane >= s) { plo += x; phi += y; }
@@ -638,15 +662,15 @@ __device__ __forceinline__ void sah_pick(const BuildArgs &a, int32_t node, int32
         float cost = INFINITY, pk = 0.0f;
         if (k < B) {
             const int32_t nl = plo, nr = total_hi - phi;
-            const float w = __fdiv_rn(ext[ax], (float)B);
-            pk = __fadd_rn(mnv[ax], __fmul_rn((float)k, w));
-            float le[3] = {ext[0], ext[1], ext[2]}, re[3] = {ext[0], ext[1], ext[2]};
-            le[ax] = __fsub_rn(pk, mnv[ax]);
-            re[ax] = __fsub_rn(mxv[ax], pk);
+            const float w = __fdiv_rn(n.ext[ax], (float)B);
+            pk = __fadd_rn(n.mnv[ax], __fmul_rn((float)k, w));
+            float le[3] = {n.ext[0], n.ext[1], n.ext[2]}, re[3] = {n.ext[0], n.ext[1], n.ext[2]};
+            le[ax] = __fsub_rn(pk, n.mnv[ax]);
+            re[ax] = __fsub_rn(n.mxv[ax], pk);
             const float al = __fadd_rn(__fadd_rn(__fmul_rn(le[0], le[1]), __fmul_rn(le[1], le[2])), __fmul_rn(le[2], le[0]));
             const float ar = __fadd_rn(__fadd_rn(__fmul_rn(re[0], re[1]), __fmul_rn(re[1], re[2])), __fmul_rn(re[2], re[0]));
             const float c = __fadd_rn(__fmul_rn(al, (float)nl), __fmul_rn(ar, (float)nr));
-            if (nl > 0 && nr > 0 && !(nl == cnt && nr == cnt)) cost = c;
+            if (nl > 0 && nr > 0 && !(nl == n.cnt && nr == n.cnt)) cost = c;
         }
         // First minimum in k order within the axis, then strictly better
         // than the previous axes.
@@ -661,17 +685,10 @@ __device__ __forceinline__ void sah_pick(const BuildArgs &a, int32_t node, int32
         if (c < best) { best = c; best_ax = ax; best_sp = sp; }
     }
     if (lane == 0 && best_ax >= 0) {
-        a.info[node] = (int8_t)(best_ax + 1);
-        a.split[node] = best_sp;
+        a.info[n.node] = (int8_t)(best_ax + 1);
+        a.split[n.node] = best_sp;
     }
 }
-
-struct SahNode {
-    int32_t node, cnt;
-    int64_t first;
-    float mnv[3], mxv[3], ext[3], scale[3];
-    bool valid[3];
-};
 
 // An active node's references are contiguous: [pidx, pidx + amt) of the
 // current reference buffer (k_begin / k_children place them so).
@@ -693,56 +710,58 @@ __device__ __forceinline__ SahNode sah_node(const BuildArgs &a, int32_t node)
     return n;
 }
 
-// Binned SAH of the active nodes below kSahBlockRefs references: one warp
-// per node, histograms in shared memory.
-__global__ void __launch_bounds__(kBlock) k_sah_warp(const BuildArgs a)
+// Binned SAH of the active nodes, one launch per tuned level.  First the
+// nodes of kSahBlockRefs references or more (listed by k_node_split), one
+// block each, taken from a work counter: every warp bins an interleaved
+// share of the rows into its own histograms, which are then summed.  Then
+// the smaller nodes, one warp each.
+__global__ void __launch_bounds__(kBlock) k_sah_bin(const BuildArgs a)
 {
     __shared__ int s_hist[kWarps][6 * 32];
-    const BuildState *st = a.st;
+    __shared__ int32_t s_big;
+    BuildState *st = a.st;
     if (!sah_level(a, st)) return;
-    const int32_t R = st->R, active = st->active;
+    const int32_t nb = st->n_big, R = st->R, active = st->active;
     const int cur = st->level & 1;
+    const float4 *__restrict__ cmin = a.rmin[cur];
+    const float4 *__restrict__ cmax = a.rmax[cur];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int *h = s_hist[warp];
+    int hv[6];
+    for (;;) {
+        if (threadIdx.x == 0) s_big = atomicAdd(&st->big_next, 1);
+        __syncthreads();
+        const int32_t k = s_big;
+        if (k >= nb) break;  // block-uniform
+        const SahNode n = sah_node(a, active + a.big[k]);
+        for (int j = lane; j < 6 * 32; j += 32) h[j] = 0;
+        __syncwarp();
+        sah_rows(cmin, cmax, n, a.B, warp, kWarps, h);
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (int j = 0; j < 6; ++j) {
+                int sum = 0;
+#pragma unroll
+                for (int w = 0; w < kWarps; ++w) sum += s_hist[w][j * 32 + lane];
+                hv[j] = sum;
+            }
+            sah_pick(a, n, hv, lane);
+        }
+        __syncthreads();  // s_hist and s_big are reused
+    }
     WARP_STRIDE(gw, R) {
         const int32_t node = active + (int32_t)gw;
         if (a.amt[node] >= kSahBlockRefs) continue;  // warp-uniform
         const SahNode n = sah_node(a, node);
         for (int j = lane; j < 6 * 32; j += 32) h[j] = 0;
         __syncwarp();
-        sah_fill(a.rmin[cur], a.rmax[cur], n.first, n.cnt, n.mnv, n.scale, n.valid, a.B, h, 0, 1);
+        sah_rows(cmin, cmax, n, a.B, 0, 1, h);
         __syncwarp();
-        sah_pick(a, node, n.cnt, n.mnv, n.mxv, n.ext, h, lane);
-        __syncwarp();
-    }
-}
-
-// The same for nodes of kSahBlockRefs references or more: one block per node,
-// a private histogram per warp, summed before the plane search.
-__global__ void __launch_bounds__(kBlock) k_sah_block(const BuildArgs a)
-{
-    __shared__ int s_hist[kWarps][6 * 32];
-    const BuildState *st = a.st;
-    if (!sah_level(a, st)) return;
-    const int32_t nb = st->n_big, active = st->active;
-    const int cur = st->level & 1;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int32_t k = blockIdx.x; k < nb; k += gridDim.x) {
-        const int32_t node = active + a.big[k];
-        const SahNode n = sah_node(a, node);
-        for (int j = lane; j < 6 * 32; j += 32) s_hist[warp][j] = 0;
-        __syncwarp();
-        sah_fill(a.rmin[cur], a.rmax[cur], n.first, n.cnt, n.mnv, n.scale, n.valid, a.B, s_hist[warp], warp, kWarps);
-        __syncthreads();
-        if (threadIdx.x < 6 * 32) {
-            int sum = 0;
 #pragma unroll
-            for (int w = 0; w < kWarps; ++w) sum += s_hist[w][threadIdx.x];
-            s_hist[0][threadIdx.x] = sum;
-        }
-        __syncthreads();
-        if (warp == 0) sah_pick(a, node, n.cnt, n.mnv, n.mxv, n.ext, s_hist[0], lane);
-        __syncthreads();
+        for (int j = 0; j < 6; ++j) hv[j] = h[j * 32 + lane];
+        sah_pick(a, n, hv, lane);
+        __syncwarp();
     }
 }
 
@@ -768,7 +787,7 @@ __device__ __forceinline__ bool level_fits(const BuildArgs &a, const BuildState 
 // Writes one reference to its child (or final leaf) slot: destination = node
 // base + rank among the node's left (right) references.
 __device__ __forceinline__ void scatter_one(const BuildArgs &a, int32_t R, int owner, int32_t upper, int L, int Rf,
-                                            int axis, float sp, float4 lo, float4 hi, int32_t pl, int32_t pr,
+                                            float4 lo, float4 hi, float4 h, float4 l, int32_t pl, int32_t pr,
                                             float4 *__restrict__ nmin, float4 *__restrict__ nmax)
 {
     const int32_t LS = a.LS;
@@ -777,8 +796,6 @@ __device__ __forceinline__ void scatter_one(const BuildArgs &a, int32_t R, int o
     const int32_t total_l = tot[0], leaf_l = tot[2], leafnodes_l = tot[4];
     if (L) {
         const int32_t rank = pl - lb[0];
-        const float4 h = make_float4(axis == KDGB_X ? kmin(sp, hi.x) : hi.x, axis == KDGB_Y ? kmin(sp, hi.y) : hi.y,
-                                     axis == KDGB_Z ? kmin(sp, hi.z) : hi.z, 0.0f);
         const int32_t lcount = (a.lbase + kLanes * (int64_t)(owner + 1))[0] - lb[0];
         if (lcount < LS) {
             const int64_t dst = (int64_t)upper + lb[2] + rank;
@@ -792,8 +809,6 @@ __device__ __forceinline__ void scatter_one(const BuildArgs &a, int32_t R, int o
     }
     if (Rf) {
         const int32_t rank = pr - lb[1];
-        const float4 l = make_float4(axis == KDGB_X ? kmax(sp, lo.x) : lo.x, axis == KDGB_Y ? kmax(sp, lo.y) : lo.y,
-                                     axis == KDGB_Z ? kmax(sp, lo.z) : lo.z, lo.w);
         const int32_t rcount = (a.lbase + kLanes * (int64_t)(owner + 1))[1] - lb[1];
         if (rcount < LS) {
             const int64_t dst = (int64_t)upper + leaf_l + lb[3] + rank;
@@ -807,15 +822,51 @@ __device__ __forceinline__ void scatter_one(const BuildArgs &a, int32_t R, int o
     }
 }
 
+// Tight-box keys of a child's references: min corner in k[0..2], max corner
+// in k[3..5]; neutral when the reference does not go to that child.
+__device__ __forceinline__ void box_keys(bool in, const float4 &mn, const float4 &mx, unsigned (&k)[6])
+{
+    if (in) {
+        k[0] = fkey(mn.x); k[1] = fkey(mn.y); k[2] = fkey(mn.z);
+        k[3] = fkey(mx.x); k[4] = fkey(mx.y); k[5] = fkey(mx.z);
+    } else {
+        keys_neutral(k);
+    }
+}
+
+__device__ __forceinline__ void keys_merge(unsigned (&acc)[6], const unsigned (&k)[6])
+{
+    acc[0] = min(acc[0], k[0]); acc[1] = min(acc[1], k[1]); acc[2] = min(acc[2], k[2]);
+    acc[3] = max(acc[3], k[3]); acc[4] = max(acc[4], k[4]); acc[5] = max(acc[5], k[5]);
+}
+
+// Adds the reduced child keys of parent o to the next level's tight boxes:
+// only non-leaf children are next-level nodes (local ids as in k_children).
+// A neutral min key (no finite float maps to it) means no contribution.
+__device__ __forceinline__ void child_keys_atomic(const BuildArgs &a, int32_t R, int o, const unsigned (&kl)[6],
+                                                  const unsigned (&kr)[6])
+{
+    const int32_t *lb = a.lbase + kLanes * (int64_t)o, *nb = lb + kLanes;
+    const int32_t *tot = a.lbase + kLanes * (int64_t)R;
+    if (kl[0] != 0xffffffffu && nb[0] - lb[0] >= a.LS) keys_atomic(a.keys, o - lb[4], kl);
+    if (kr[0] != 0xffffffffu && nb[1] - lb[1] >= a.LS) keys_atomic(a.keys, R + o - (tot[4] + lb[5]), kr);
+}
+
 // Partition + compaction of the references with clipping to the split plane
 // (SplitTriangles, TriangleUpperChildren.h:283-383).  Destination = node base
 // + rank of the reference among the node's left (right) references; a warp's
 // first rank is its tile's offset plus the chunk totals of the tile's earlier
-// warps.
+// warps.  The same pass reduces the next level's tight boxes (the segmented
+// AABB reduction of ReduceSegments.h:230-371 for the children): references
+// are sorted by parent, so a warp keeps running key minima/maxima while its
+// rows belong to one parent and issues atomics only when the parent changes;
+// the warps of a block merge equal parents before their atomics.
 template <bool DIVIDE>
 __global__ void __launch_bounds__(kBlock) k_scatter(const BuildArgs a)
 {
     __shared__ int32_t s_off[kWarps][2];
+    __shared__ int s_owner[kWarps];
+    __shared__ unsigned s_keys[kWarps][12];
     const BuildState *st = a.st;
     if (!level_fits(a, st, node_totals(a, st))) return;  // advance_upper records the failure
     const int64_t N = st->N;
@@ -845,39 +896,109 @@ __global__ void __launch_bounds__(kBlock) k_scatter(const BuildArgs a)
         const int64_t chunk = tile * kWarps + warp;
         const int64_t base = chunk * kChunk;
         int32_t off_l = s_off[warp][0], off_r = s_off[warp][1];
-        __syncthreads();  // s_off is rewritten by the next tile
-        if (base >= N) continue;  // warp-uniform
-        float4 ra[kRows], rb[kRows];
+        int run = -1;  // parent whose whole rows this warp is accumulating
+        unsigned al[6], ar[6];
+        keys_neutral(al);
+        keys_neutral(ar);
+        if (base < N) {  // warp-uniform
+            float4 ra[kRows], rb[kRows];
 #pragma unroll
-        for (int row = 0; row < kRows; ++row) {
-            const int64_t r = base + row * 32 + lane;
-            if (r < N) { ra[row] = cmin[r]; rb[row] = cmax[r]; }
-            else { rb[row].w = __int_as_float(-1); }
-        }
-        int ax[kRows];
-        float sps[kRows];
+            for (int row = 0; row < kRows; ++row) {
+                const int64_t r = base + row * 32 + lane;
+                if (r < N) { ra[row] = cmin[r]; rb[row] = cmax[r]; }
+                else { ra[row] = make_float4(0.f, 0.f, 0.f, 0.f); rb[row] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)); }
+            }
+            int ax[kRows];
+            float sps[kRows];
 #pragma unroll
-        for (int row = 0; row < kRows; ++row) {
-            const int o = __float_as_int(rb[row].w);
-            ax[row] = o >= 0 ? a.info[active + o] : 0;
-            sps[row] = o >= 0 ? a.split[active + o] : 0.0f;
-        }
+            for (int row = 0; row < kRows; ++row) {
+                const int o = __float_as_int(rb[row].w);
+                ax[row] = o >= 0 ? a.info[active + o] : 0;
+                sps[row] = o >= 0 ? a.split[active + o] : 0.0f;
+            }
 #pragma unroll
-        for (int row = 0; row < kRows; ++row) {
-            if (base + row * 32 >= N) break;
-            const int owner = __float_as_int(rb[row].w);
-            const int axis = ax[row];
-            const float sp = sps[row];
-            const float4 lo = ra[row], hi = rb[row];
-            int L = 0, Rf = 0;
-            if (owner >= 0) ref_flags(lo, hi, axis, sp, L, Rf);
-            if (DIVIDE && L && Rf) divide_flags(a, __float_as_int(lo.w), active + owner, axis, sp, L, Rf);
-            const unsigned bl = __ballot_sync(kFull, L), br = __ballot_sync(kFull, Rf);
-            const int32_t pl = off_l + __popc(bl & below), pr = off_r + __popc(br & below);
-            off_l += __popc(bl);
-            off_r += __popc(br);
-            if (owner >= 0) scatter_one(a, R, owner, upper, L, Rf, axis, sp, lo, hi, pl, pr, nmin, nmax);
+            for (int row = 0; row < kRows; ++row) {
+                if (base + row * 32 >= N) break;
+                const int owner = __float_as_int(rb[row].w);
+                const int axis = ax[row];
+                const float sp = sps[row];
+                const float4 lo = ra[row], hi = rb[row];
+                int L = 0, Rf = 0;
+                if (owner >= 0) ref_flags(lo, hi, axis, sp, L, Rf);
+                if (DIVIDE && L && Rf) divide_flags(a, __float_as_int(lo.w), active + owner, axis, sp, L, Rf);
+                const unsigned bl = __ballot_sync(kFull, L), br = __ballot_sync(kFull, Rf);
+                const int32_t pl = off_l + __popc(bl & below), pr = off_r + __popc(br & below);
+                off_l += __popc(bl);
+                off_r += __popc(br);
+                // Clipped boxes: the left child's max and the right child's min.
+                const float4 h = make_float4(axis == KDGB_X ? kmin(sp, hi.x) : hi.x,
+                                             axis == KDGB_Y ? kmin(sp, hi.y) : hi.y,
+                                             axis == KDGB_Z ? kmin(sp, hi.z) : hi.z, 0.0f);
+                const float4 l = make_float4(axis == KDGB_X ? kmax(sp, lo.x) : lo.x,
+                                             axis == KDGB_Y ? kmax(sp, lo.y) : lo.y,
+                                             axis == KDGB_Z ? kmax(sp, lo.z) : lo.z, lo.w);
+                if (owner >= 0) scatter_one(a, R, owner, upper, L, Rf, lo, hi, h, l, pl, pr, nmin, nmax);
+                unsigned kl[6], kr[6];
+                box_keys(L, lo, h, kl);
+                box_keys(Rf, l, hi, kr);
+                const unsigned m = __match_any_sync(kFull, owner);
+                if (m == kFull && owner == run) {
+                    keys_merge(al, kl);
+                    keys_merge(ar, kr);
+                    continue;
+                }
+                if (run >= 0) {
+                    keys_reduce(kFull, al);
+                    keys_reduce(kFull, ar);
+                    if (lane == 0) child_keys_atomic(a, R, run, al, ar);
+                }
+                if (m == kFull && owner >= 0) {
+                    run = owner;
+                    for (int j = 0; j < 6; ++j) { al[j] = kl[j]; ar[j] = kr[j]; }
+                } else {
+                    if (owner >= 0) {
+                        keys_reduce(m, kl);
+                        keys_reduce(m, kr);
+                        if (lane == (unsigned)(__ffs(m) - 1)) child_keys_atomic(a, R, owner, kl, kr);
+                    }
+                    run = -1;
+                    keys_neutral(al);
+                    keys_neutral(ar);
+                }
+            }
+            if (run >= 0) {
+                keys_reduce(kFull, al);
+                keys_reduce(kFull, ar);
+            }
         }
+        if (lane == 0) {
+            s_owner[warp] = run;
+            for (int j = 0; j < 6; ++j) { s_keys[warp][j] = al[j]; s_keys[warp][6 + j] = ar[j]; }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // Consecutive warps cover consecutive chunks: merge equal parents.
+            int o = -1;
+            unsigned kl[6], kr[6];
+            keys_neutral(kl);
+            keys_neutral(kr);
+            for (int w = 0; w < kWarps; ++w) {
+                const int ow = s_owner[w];
+                if (ow < 0) continue;
+                unsigned wl[6], wr[6];
+                for (int j = 0; j < 6; ++j) { wl[j] = s_keys[w][j]; wr[j] = s_keys[w][6 + j]; }
+                if (ow != o) {
+                    if (o >= 0) child_keys_atomic(a, R, o, kl, kr);
+                    o = ow;
+                    for (int j = 0; j < 6; ++j) { kl[j] = wl[j]; kr[j] = wr[j]; }
+                } else {
+                    keys_merge(kl, wl);
+                    keys_merge(kr, wr);
+                }
+            }
+            if (o >= 0) child_keys_atomic(a, R, o, kl, kr);
+        }
+        __syncthreads();  // s_off, s_owner and s_keys are rewritten by the next tile
     }
 }
 
@@ -982,6 +1103,7 @@ __device__ void advance_upper(const BuildArgs &a, BuildState *st)
         st->R = created;
         st->level += 1;
         st->n_big = 0;
+        st->big_next = 0;
         if (created > 0 && st->level >= a.max_levels) { set_err(st, KDGB_ERR_DEGENERATE, kErrMaxLevels); break; }
         more = created > 0;
     } while (0);
@@ -992,10 +1114,11 @@ __device__ void advance_upper(const BuildArgs &a, BuildState *st)
 // chain of EmptySpaceSplitting2 (its nodes come first, at base + lane-6
 // offsets) and, with empty-space splitting on, PropagateAabbToChildren
 // (EmptySpaceSplitting.h:299-331; TriangleMapUpperCreator.cu:731-733 runs
-// it whenever empty-space splitting is on, whatever propagateAabbs says).  Non-leaf children are the next level's
-// active nodes: their tight-box keys, counts and propagated boxes are reset
-// here (AabbMemset, ReduceSegments.h:328-335) so the next level needs no
-// separate init launch.  The block that finishes last closes the level
+// it whenever empty-space splitting is on, whatever propagateAabbs says).
+// Non-leaf children are the next level's active nodes: their counts and
+// propagated boxes are reset here (their tight-box keys were reset by
+// k_count and filled by k_scatter), so the next level needs no separate
+// init launch.  The block that finishes last closes the level
 // (advance_upper).
 __global__ void k_children(const BuildArgs a)
 {
@@ -1008,7 +1131,6 @@ __global__ void k_children(const BuildArgs a)
     const int32_t empty = tot[6];
     const int32_t child_start = base + empty;
     const int32_t total_l = tot[0], leaf_l = tot[2], ln_l = tot[4], leaf_nodes = tot[4] + tot[5];
-    const unsigned lo_key = fkey(KDGB_FINF), hi_key = fkey(-KDGB_FINF);
     GRID_STRIDE(k64, R) {
         const int32_t k = (int32_t)k64;
         const int32_t *lb = a.lbase + kLanes * (int64_t)k;
@@ -1053,18 +1175,12 @@ __global__ void k_children(const BuildArgs a)
             a.bmax[rid] = rmax;
         }
         if (!lleaf) {
-            unsigned *kq = a.keys + 6 * (int64_t)lnext;
-            kq[0] = kq[1] = kq[2] = lo_key;
-            kq[3] = kq[4] = kq[5] = hi_key;
             a.cnt[2 * lnext] = 0;
             a.cnt[2 * lnext + 1] = 0;
             a.pmin[lnext] = lmin;
             a.pmax[lnext] = lmax;
         }
         if (!rleaf) {
-            unsigned *kq = a.keys + 6 * (int64_t)rnext;
-            kq[0] = kq[1] = kq[2] = lo_key;
-            kq[3] = kq[4] = kq[5] = hi_key;
             a.cnt[2 * rnext] = 0;
             a.cnt[2 * rnext + 1] = 0;
             a.pmin[rnext] = rmin;
@@ -1269,6 +1385,13 @@ __global__ void k_calc_sah(const BuildArgs a)
         const int32_t par = ids ? ids[gw] : active + (int32_t)gw;
         const int32_t pi = a.pidx[par];
         const unsigned bmp = (unsigned)a.amt[par];
+        if (__popc(bmp) <= a.min_leaf) {  // never split: skip the plane costs
+            if (lane == 0) {
+                a.info[par] = (int8_t)KDGB_LEAF;
+                a.ssplit[gw] = 0;
+            }
+            continue;
+        }
         const bool mine = (bmp >> lane) & 1u;
         const float a_lane = mine ? a.areas[pi + lane] : 0.0f;
         SahPick mb;
@@ -1688,6 +1811,9 @@ int emit_begin(const BuildArgs &a, const Launcher &L, const float *tri_v_dev, cu
         k_load_geometry<<<L.grid(a.T, kBlock), kBlock, 0, s>>>(tri_v_dev, a.T, a.p0, a.p1, a.p2, a.rmin[0],
                                                                a.rmax[0], &a.st->nonfinite, a.mesh_off, a.M);
         KDGB_LAUNCH_CHECK();
+        // The roots' tight boxes; later levels get theirs from k_scatter.
+        k_reduce<<<L.grid(a.T, kTileRefs), kBlock, 0, s>>>(a);
+        KDGB_LAUNCH_CHECK();
     }
     return KDGB_OK;
 }
@@ -1697,17 +1823,12 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
 {
     const unsigned gN = L.grid(e.N, kTileRefs);
     const unsigned gR = L.grid(e.R, kBlock, 2);
-    if (e.N > 0) {
-        k_reduce<<<gN, kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
-    }
     k_node_split<<<gR, kBlock, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
     if (tuned_levels) {
-        k_sah_block<<<L.grid(std::min<int64_t>(e.R, ceil_div(e.N, kSahBlockRefs)) * kBlock, kBlock, 2), kBlock, 0,
-                      s>>>(a);
-        KDGB_LAUNCH_CHECK();
-        k_sah_warp<<<L.grid(e.R * 32, kBlock), kBlock, 0, s>>>(a);
+        // Enough blocks for one per large node and one warp per node.
+        const int64_t big = std::min<int64_t>(e.R, ceil_div(e.N, kSahBlockRefs));
+        k_sah_bin<<<L.grid(std::max<int64_t>(big * kBlock, e.R * 32), kBlock), kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
     if (e.N > 0) {
@@ -1715,9 +1836,9 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
         else k_count<false><<<gN, kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
-    KDGB_CHECK(scan_exclusive<2>(a.tilesum, a.tileoff, ceil_div(e.N, kTileRefs), s, &w.scan, &a.st->ntiles));
+    KDGB_CHECK(scan_exclusive<2>(a.tilesum, a.tileoff, ceil_div(e.N, kTileRefs), s, &w.scan, &a.st->ntiles, &a.st->err));
     const NodeLanes lanes{a.cnt, a.ess_cnt, a.LS};
-    KDGB_CHECK((scan_exclusive_in<kLanes, NodeLanes>(lanes, a.lbase, e.R, s, &w.scan, &a.st->R)));
+    KDGB_CHECK((scan_exclusive_in<kLanes, NodeLanes>(lanes, a.lbase, e.R, s, &w.scan, &a.st->R, &a.st->err)));
     if (e.N > 0) {
         if (a.divide) k_scatter<true><<<gN, kBlock, 0, s>>>(a);
         else k_scatter<false><<<gN, kBlock, 0, s>>>(a);
@@ -1764,7 +1885,7 @@ int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, Wo
     if (a.lower == KDGB_LOWER_BALANCED) k_calc_balanced<<<L.grid(e.low_R * 32, kBlock), kBlock, 0, s>>>(a);
     else k_calc_sah<<<L.grid(e.low_R * 32, kBlock), kBlock, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
-    KDGB_CHECK(scan_exclusive<1>(a.ssplit, a.saddr, e.low_R, s, &w.scan, &a.st->low_R));
+    KDGB_CHECK(scan_exclusive<1>(a.ssplit, a.saddr, e.low_R, s, &w.scan, &a.st->low_R, &a.st->err));
     k_sah_children<<<L.grid(e.low_R, kBlock, 2), kBlock, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
@@ -1775,7 +1896,7 @@ int emit_pack_counts(const BuildArgs &a, const Launcher &L, const Extents &e, Wo
 {
     k_leaf_counts<<<L.grid(e.nodes, kBlock), kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.info, a.amt, a.lcnt);
     KDGB_LAUNCH_CHECK();
-    KDGB_CHECK(scan_exclusive<1>(a.lcnt, a.loff, e.nodes, s, &w.scan, &a.st->n_nodes));
+    KDGB_CHECK(scan_exclusive<1>(a.lcnt, a.loff, e.nodes, s, &w.scan, &a.st->n_nodes, &a.st->err));
     k_pack_finish<<<1, 1, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
@@ -2118,7 +2239,7 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     const int64_t parts = std::max({scan_partials_needed(2, ceil_div(e.N, kTileRefs)), scan_partials_needed(kLanes, e.R),
                                     scan_partials_needed(1, e.low_R), scan_partials_needed(1, e.nodes),
                                     (int64_t)1});
-    KDGB_CHECK(ensure(w.scan, parts, s));
+    KDGB_CHECK(ensure(w.scan, parts, s, 0, true));  // zeroed scan state
     return KDGB_OK;
 }
 

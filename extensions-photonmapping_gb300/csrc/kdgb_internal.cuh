@@ -90,7 +90,7 @@ struct BuildState {
     int32_t n_leaf_tris;  // leaf records of the traversal layout
     int32_t n_big;        // tuned levels: active nodes listed for block-wide SAH binning
     int32_t done;         // blocks of the current level-closing kernel that have finished
-    int32_t pad;
+    int32_t big_next;     // tuned levels: work counter over the listed nodes
 };
 
 // Sizes seen by the last host-driven build of a handle; a graph rebuild
@@ -230,22 +230,24 @@ struct NodeLanes {
 };
 
 // Device-wide exclusive scan of n records of K int32 lanes (lanes scanned
-// independently).  out has n+1 records; record n holds the totals.  `ws`
-// (optional) holds the per-tile partials; without it they are allocated.
-// With n_dev set, the kernels read the length there (at most n, which then
-// only sizes the grids and the partials).
+// independently), one launch.  out has n+1 records; record n holds the
+// totals.  `ws` holds the scan's control words and tile status; it persists
+// between scans and is grown (zeroed) here when too small.  With n_dev set,
+// the kernel reads the length there (at most n, which then only sizes the
+// grid and the status).  A bounded wait that gives up stores
+// KDGB_ERR_TIMEOUT in *err (when given) if it is still 0.
 template <int K, class In>
-int scan_exclusive_in(const In &in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws = nullptr,
-                      const int32_t *n_dev = nullptr);
+int scan_exclusive_in(const In &in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws,
+                      const int32_t *n_dev = nullptr, int32_t *err = nullptr);
 
 template <int K>
-inline int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws = nullptr,
-                          const int32_t *n_dev = nullptr)
+inline int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws,
+                          const int32_t *n_dev = nullptr, int32_t *err = nullptr)
 {
-    return scan_exclusive_in<K, ScanArray<K>>(ScanArray<K>{in}, out, n, s, ws, n_dev);
+    return scan_exclusive_in<K, ScanArray<K>>(ScanArray<K>{in}, out, n, s, ws, n_dev, err);
 }
 
-// Partials (int32 elements) a scan of n records of K lanes needs.
+// Workspace (int32 elements) a scan of n records of K lanes needs.
 int64_t scan_partials_needed(int K, int64_t n);
 
 // Hash of every device buffer's address and capacity: a captured graph is

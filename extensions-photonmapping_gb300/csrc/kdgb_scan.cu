@@ -3,16 +3,25 @@
 // The reference scans with CUDPP (TriangleMapUpperCreator.cu:58-76, one plan
 // of 262,144 elements, return codes ignored).  This replacement scans records
 // of K independent lanes read through a loader (a plain array, or lanes
-// computed on the fly from other arrays).  Up to kSingleMax records one
-// block of 1024 threads scans everything in a single launch; above that a
-// reduce-then-scan takes three launches (block totals, a single-block scan
-// of the totals, a rescan of each block with its offset).  No block ever
-// waits for another, so the scan cannot hang, and it has no size cap below
-// 2^31 records.  The length may live in device memory (a build counter): the
-// grids are then sized for an upper bound and blocks past the real length do
-// nothing, so the scan can be captured once into a graph and replayed for
-// any length up to the bound.
+// computed on the fly from other arrays) in ONE launch, whatever the length:
+// a single-pass scan with decoupled look-back.  Each block takes a tile of
+// kTile records in the order blocks start (a ticket counter), scans it,
+// publishes the tile's totals at once and then the inclusive prefix once it
+// knows its predecessors' prefix, which it assembles by looking back over
+// the published tiles (32 at a time, one lane each).  A block only ever
+// waits for tiles whose blocks started before it and publish without
+// waiting, so every wait ends; each wait is still bounded and a scan that
+// gives up records KDGB_ERR_TIMEOUT.  Status flags carry the invocation's
+// epoch, so the status array is never cleared between scans; the last block
+// of an invocation resets the ticket counter and advances the epoch.
+//
+// The length may live in device memory (a build counter): the grid is then
+// sized for an upper bound and tiles past the real length do nothing, so the
+// scan can be captured once into a graph and replayed for any length up to
+// the bound.
 #include "kdgb_internal.cuh"
+
+#include <algorithm>
 
 namespace kdgb {
 
@@ -21,9 +30,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kItems = 4;
 constexpr int kTile = kThreads * kItems;
-constexpr int kSingleThreads = 1024;
-constexpr int kSingleTile = kSingleThreads * kItems;
-constexpr int64_t kSingleMax = 16384;
+constexpr unsigned kFull = 0xffffffffu;
 
 // Exclusive block scan of one value per lane per thread.  Returns the block
 // total of every lane in `total`.
@@ -89,162 +96,167 @@ __device__ __forceinline__ void load_items(const In &in, int64_t base, int64_t n
     }
 }
 
-// One block, any n: segments of kSingleTile records with a running carry;
-// writes the totals record out[n].
-template <int K, class In>
-__global__ void __launch_bounds__(kSingleThreads) scan_single_kernel(const In in, int32_t *__restrict__ out, int64_t n,
-                                                                     const int32_t *__restrict__ n_dev)
+// Scan state in the workspace array: kCtl control words, then kStatus ints
+// per tile: the tile totals (K <= 7 lanes, written once), the inclusive
+// prefix (8 + k) and a flag word (epoch << 2 | kind) at kFlag.  Totals and
+// prefix live apart, so a reader that saw either kind reads values that no
+// later store of the same epoch changes.
+constexpr int kCtl = 4;  // ticket, finished blocks, epoch, spare
+constexpr int kStatus = 16;
+constexpr int kIncl = 8;
+constexpr int kFlag = 15;
+constexpr unsigned kAggregate = 1, kPrefix = 2;
+constexpr int kSpinLimit = 1 << 22;
+
+__device__ __forceinline__ unsigned load_flag(const int32_t *p)
 {
+    return *(const volatile unsigned *)p;
+}
+
+template <int K, class In>
+__global__ void __launch_bounds__(kThreads) scan_lookback_kernel(const In in, int32_t *__restrict__ out, int64_t n,
+                                                                 const int32_t *__restrict__ n_dev, int32_t *ws,
+                                                                 int32_t *err)
+{
+    __shared__ int64_t s_tile;
+    __shared__ int32_t s_excl[K];
+    unsigned *ctl = (unsigned *)ws;
+    int32_t *status = ws + kCtl;
     if (n_dev) n = *n_dev;
-    int32_t carry[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) carry[k] = 0;
-    for (int64_t start = 0; start < n; start += kSingleTile) {
-        const int64_t base = start + (int64_t)threadIdx.x * kItems;
+    const unsigned epoch = *(volatile unsigned *)(ctl + 2) & 0x3fffffffu;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ctl + 0, 1u);
+    __syncthreads();
+    const int64_t tile = s_tile, ntiles = (n + kTile - 1) / kTile;
+    if (tile < ntiles) {
+        const int64_t base = tile * kTile + (int64_t)threadIdx.x * kItems;
         int32_t vals[kItems][K], s[K], tot[K];
         load_items<K>(in, base, n, vals, s);
-        block_scan<K, kSingleThreads>(s, tot);
+        block_scan<K, kThreads>(s, tot);
+        int32_t *mine = status + kStatus * tile;
+        if (threadIdx.x == 0) {
+            // Publish the tile totals (for tile 0 they are the inclusive prefix).
+            const int off = tile == 0 ? kIncl : 0;
+#pragma unroll
+            for (int k = 0; k < K; ++k) ((volatile int32_t *)mine)[off + k] = tot[k];
+            __threadfence();
+            ((volatile unsigned *)mine)[kFlag] = (epoch << 2) | (tile == 0 ? kPrefix : kAggregate);
+        }
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            int32_t excl[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) excl[k] = 0;
+            int64_t j = tile - 1;  // nearest unread predecessor
+            while (j >= 0) {      // warp-uniform
+                const int64_t t = j - lane;
+                unsigned f = 0;
+                bool dead = false;
+                if (t >= 0) {
+                    int spins = 0;
+                    f = load_flag(status + kStatus * t + kFlag);
+                    while ((f >> 2) != epoch || (f & 3u) == 0) {
+                        if (++spins > kSpinLimit) {
+                            if (err) atomicCAS(err, 0, KDGB_ERR_TIMEOUT);
+                            f = (epoch << 2) | kPrefix;  // give up: count it as a zero prefix
+                            dead = true;
+                            break;
+                        }
+                        __nanosleep(64);
+                        f = load_flag(status + kStatus * t + kFlag);
+                    }
+                }
+                __threadfence();
+                // Lanes up to the first prefix (nearest predecessor first) count.
+                const unsigned pm = __ballot_sync(kFull, t >= 0 && (f & 3u) == kPrefix);
+                const int stop = pm ? __ffs(pm) - 1 : 31;
+                const bool use = t >= 0 && lane <= stop && !dead;
+                const int off = (f & 3u) == kPrefix ? kIncl : 0;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    int32_t v = use ? ((const volatile int32_t *)(status + kStatus * t))[off + k] : 0;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+                    excl[k] += v;
+                }
+                if (pm) break;
+                j -= 32;
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) s_excl[k] = excl[k];
+                if (tile > 0) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) ((volatile int32_t *)mine)[kIncl + k] = excl[k] + tot[k];
+                    __threadfence();
+                    ((volatile unsigned *)mine)[kFlag] = (epoch << 2) | kPrefix;
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < K; ++k) s[k] += s_excl[k];
 #pragma unroll
         for (int i = 0; i < kItems; ++i) {
 #pragma unroll
             for (int k = 0; k < K; ++k) {
-                if (base + i < n) out[(base + i) * K + k] = carry[k] + s[k];
+                if (base + i < n) out[(base + i) * K + k] = s[k];
                 s[k] += vals[i][k];
             }
         }
+        if (tile == ntiles - 1 && threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) carry[k] += tot[k];
-    }
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) out[n * K + k] = carry[k];
-    }
-}
-
-template <int K, class In>
-__global__ void __launch_bounds__(kThreads) scan_reduce_kernel(const In in, int64_t n,
-                                                               const int32_t *__restrict__ n_dev,
-                                                               int32_t *__restrict__ partial)
-{
-    if (n_dev) n = *n_dev;
-    if ((int64_t)blockIdx.x * kTile >= n) return;  // block-uniform
-    const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
-    int32_t vals[kItems][K], s[K], tot[K];
-    load_items<K>(in, base, n, vals, s);
-    block_scan<K, kThreads>(s, tot);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) partial[(int64_t)blockIdx.x * K + k] = tot[k];
-    }
-}
-
-// Single block: exclusive scan of the block partials in place; writes the
-// grand totals to out[n].
-template <int K>
-__global__ void __launch_bounds__(kSingleThreads) scan_partials_kernel(int32_t *__restrict__ partial, int64_t n,
-                                                                       const int32_t *__restrict__ n_dev,
-                                                                       int32_t *__restrict__ out)
-{
-    if (n_dev) n = *n_dev;
-    const int64_t nb = (n + kTile - 1) / kTile;
-    int32_t carry[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) carry[k] = 0;
-    const ScanArray<K> in{partial};
-    for (int64_t start = 0; start < nb; start += kSingleTile) {
-        const int64_t b = start + (int64_t)threadIdx.x * kItems;
-        int32_t vals[kItems][K], s[K], tot[K];
-        load_items<K>(in, b, nb, vals, s);
-        block_scan<K, kSingleThreads>(s, tot);
-#pragma unroll
-        for (int i = 0; i < kItems; ++i) {
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                if (b + i < nb) partial[(b + i) * K + k] = carry[k] + s[k];
-                s[k] += vals[i][k];
-            }
+            for (int k = 0; k < K; ++k) out[n * K + k] = s_excl[k] + tot[k];
         }
-#pragma unroll
-        for (int k = 0; k < K; ++k) carry[k] += tot[k];
+    } else if (tile == 0 && threadIdx.x < K) {
+        out[threadIdx.x] = 0;  // n == 0: the totals record only
     }
+    // The last block to finish resets the tickets and opens the next epoch.
     if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) out[n * K + k] = carry[k];
-    }
-}
-
-template <int K, class In>
-__global__ void __launch_bounds__(kThreads) scan_down_kernel(const In in, int32_t *__restrict__ out, int64_t n,
-                                                             const int32_t *__restrict__ n_dev,
-                                                             const int32_t *__restrict__ partial)
-{
-    if (n_dev) n = *n_dev;
-    if ((int64_t)blockIdx.x * kTile >= n) return;  // block-uniform
-    const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
-    int32_t vals[kItems][K], s[K], tot[K];
-    load_items<K>(in, base, n, vals, s);
-    block_scan<K, kThreads>(s, tot);
-#pragma unroll
-    for (int k = 0; k < K; ++k) s[k] += partial[(int64_t)blockIdx.x * K + k];
-#pragma unroll
-    for (int i = 0; i < kItems; ++i) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            if (base + i < n) out[(base + i) * K + k] = s[k];
-            s[k] += vals[i][k];
+        __threadfence();
+        if (atomicAdd(ctl + 1, 1u) == gridDim.x - 1) {
+            ctl[0] = 0;
+            ctl[1] = 0;
+            ctl[2] = (epoch + 1) & 0x3fffffffu;
+            __threadfence();
         }
     }
 }
 
 }  // namespace
 
-int64_t scan_partials_needed(int K, int64_t n) { return n <= kSingleMax ? 0 : K * ((n + kTile - 1) / kTile); }
+int64_t scan_partials_needed(int K, int64_t n)
+{
+    (void)K;
+    return kCtl + kStatus * ((n + kTile - 1) / kTile);
+}
 
 template <int K, class In>
 int scan_exclusive_in(const In &in, int32_t *out, int64_t n, cudaStream_t s, DevArray<int32_t> *ws,
-                      const int32_t *n_dev)
+                      const int32_t *n_dev, int32_t *err)
 {
+    static_assert(K <= 7, "a tile status holds K lanes twice and a flag");
     if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "scan: negative length");
-    if (n == 0) {
-        KDGB_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t) * K, s));
-        return KDGB_OK;
+    if (!ws) return fail(KDGB_ERR_INVALID_ARGUMENT, "scan: no workspace");
+    const int64_t need = scan_partials_needed(K, n);
+    if (!ws->p || need > ws->cap) {
+        // New state is zeroed (no flag matches any epoch); the control words
+        // carry over.  Grows geometrically.
+        const int64_t want = std::max<int64_t>(need, ws->cap + ws->cap / 2);
+        KDGB_CHECK(ensure(*ws, want, s, ws->p ? kCtl : 0, true));
     }
-    if (n <= kSingleMax) {
-        scan_single_kernel<K, In><<<1, kSingleThreads, 0, s>>>(in, out, n, n_dev);
-        KDGB_LAUNCH_CHECK();
-        return KDGB_OK;
-    }
-    const int64_t nb = (n + kTile - 1) / kTile;
-    int32_t *partial = nullptr;
-    if (ws) {
-        KDGB_CHECK(grab(*ws, K * nb, s));
-        partial = ws->p;
-    } else {
-        KDGB_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * K * (size_t)nb, s));
-    }
-    scan_reduce_kernel<K, In><<<(unsigned)nb, kThreads, 0, s>>>(in, n, n_dev, partial);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) {
-        scan_partials_kernel<K><<<1, kSingleThreads, 0, s>>>(partial, n, n_dev, out);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) {
-        scan_down_kernel<K, In><<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, n_dev, partial);
-        e = cudaGetLastError();
-    }
-    if (!ws) cudaFreeAsync(partial, s);
-    if (e != cudaSuccess) return cuda_fail(e, "scan kernels");
-    note_launch(3);
+    const int64_t nb = std::max<int64_t>(1, (n + kTile - 1) / kTile);
+    scan_lookback_kernel<K, In><<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, n_dev, ws->p, err);
+    KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
 
 template int scan_exclusive_in<1, ScanArray<1>>(const ScanArray<1> &, int32_t *, int64_t, cudaStream_t,
-                                             DevArray<int32_t> *, const int32_t *);
+                                             DevArray<int32_t> *, const int32_t *, int32_t *);
 template int scan_exclusive_in<2, ScanArray<2>>(const ScanArray<2> &, int32_t *, int64_t, cudaStream_t,
-                                             DevArray<int32_t> *, const int32_t *);
+                                             DevArray<int32_t> *, const int32_t *, int32_t *);
 template int scan_exclusive_in<7, ScanArray<7>>(const ScanArray<7> &, int32_t *, int64_t, cudaStream_t,
-                                             DevArray<int32_t> *, const int32_t *);
+                                             DevArray<int32_t> *, const int32_t *, int32_t *);
 template int scan_exclusive_in<7, NodeLanes>(const NodeLanes &, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *,
-                                          const int32_t *);
+                                          const int32_t *, int32_t *);
 
 }  // namespace kdgb
