@@ -53,7 +53,7 @@ constexpr int kTileRefs = kChunk * kWarps;  // references per block tile
 constexpr int kLanes = 7;                   // per-node scan lanes (see NodeLanes)
 // Tuned levels: nodes with at least this many references are binned by a
 // whole block, smaller ones by one warp (k_sah_bin).
-constexpr int kSahBlockRefs = 2048;
+constexpr int kSahBlockRefs = 512;
 constexpr unsigned kFull = 0xffffffffu;
 
 __host__ __device__ inline int64_t chunks_for(int64_t n) { return (n + kChunk - 1) / kChunk; }
@@ -1307,18 +1307,32 @@ __global__ void k_sah_planes(const BuildArgs a)
         float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
         if (mine) { lo = a.fmin[pi + lane]; hi = a.fmax[pi + lane]; }
         unsigned sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sz[4] = {0, 0, 0, 0};
-        for (unsigned bits = bmp; bits; bits &= bits - 1u) {  // bmp is warp-uniform
-            const int j = __ffs(bits) - 1;
-            const float mnx = __shfl_sync(kFull, lo.x, j), mny = __shfl_sync(kFull, lo.y, j);
-            const float mnz = __shfl_sync(kFull, lo.z, j), mxx = __shfl_sync(kFull, hi.x, j);
-            const float mxy = __shfl_sync(kFull, hi.y, j), mxz = __shfl_sync(kFull, hi.z, j);
-            const unsigned m = 1u << j;
-            sx[0] |= mnx <= lo.x ? m : 0; sx[1] |= lo.x < mxx ? m : 0;
-            sx[2] |= mnx <= hi.x ? m : 0; sx[3] |= hi.x < mxx ? m : 0;
-            sy[0] |= mny <= lo.y ? m : 0; sy[1] |= lo.y < mxy ? m : 0;
-            sy[2] |= mny <= hi.y ? m : 0; sy[3] |= hi.y < mxy ? m : 0;
-            sz[0] |= mnz <= lo.z ? m : 0; sz[1] |= lo.z < mxz ? m : 0;
-            sz[2] |= mnz <= hi.z ? m : 0; sz[3] |= hi.z < mxz ? m : 0;
+        for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; two members per iteration
+            int jj[2];
+            unsigned mm[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                jj[q] = bits ? __ffs(bits) - 1 : 0;
+                mm[q] = bits ? 1u << jj[q] : 0u;
+                bits &= bits - 1u;
+            }
+            float mnx[2], mny[2], mnz[2], mxx[2], mxy[2], mxz[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                mnx[q] = __shfl_sync(kFull, lo.x, jj[q]); mny[q] = __shfl_sync(kFull, lo.y, jj[q]);
+                mnz[q] = __shfl_sync(kFull, lo.z, jj[q]); mxx[q] = __shfl_sync(kFull, hi.x, jj[q]);
+                mxy[q] = __shfl_sync(kFull, hi.y, jj[q]); mxz[q] = __shfl_sync(kFull, hi.z, jj[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const unsigned m = mm[q];
+                sx[0] |= mnx[q] <= lo.x ? m : 0; sx[1] |= lo.x < mxx[q] ? m : 0;
+                sx[2] |= mnx[q] <= hi.x ? m : 0; sx[3] |= hi.x < mxx[q] ? m : 0;
+                sy[0] |= mny[q] <= lo.y ? m : 0; sy[1] |= lo.y < mxy[q] ? m : 0;
+                sy[2] |= mny[q] <= hi.y ? m : 0; sy[3] |= hi.y < mxy[q] ? m : 0;
+                sz[0] |= mnz[q] <= lo.z ? m : 0; sz[1] |= lo.z < mxz[q] ? m : 0;
+                sz[2] |= mnz[q] <= hi.z ? m : 0; sz[3] |= hi.z < mxz[q] ? m : 0;
+            }
         }
         if (mine) {
             a.sts[pi + lane] = make_int4(sx[0], sx[1], sx[2], sx[3]);

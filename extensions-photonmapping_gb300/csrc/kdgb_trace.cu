@@ -159,31 +159,125 @@ __device__ __forceinline__ int leaf_test(const Ctx &c, int4 leaf, float3 o, floa
     return hit;
 }
 
+// Remembered descents for kd-restart.  A restart descends from the root
+// with tmin' = tnext * 1.00001, larger than the tmin of the previous
+// descent, so it repeats every decision of that descent (far ones stay far,
+// near ones whose split distance exceeds tmin' stay near) down to the
+// topmost near decision whose split distance is <= tmin', and turns to the
+// far child there.  Keeping the near decisions of the current descent as
+// (node, prefix minimum of their split distances from the root) lets the
+// descent resume at that node with the prefix minimum above it as tnext:
+// the leaves visited and their tnext values are exactly those of the full
+// restart.  The deepest `cap` (a power of two) near decisions are kept (a
+// ring in shared memory, entry slot s at e[s * stride]); when the turning
+// node lies above them (`base`, the minimum over the dropped ones, is <=
+// tmin') the descent starts again from the root.
+constexpr int kMemo = 16;  // capacity where the shared region is sized for it
+
+struct Memo {
+    int2 *e;
+    int stride, cap, head, cnt;
+    float base;
+    __device__ __forceinline__ void reset()
+    {
+        head = 0;
+        cnt = 0;
+        base = KDGB_FINF;
+    }
+    __device__ __forceinline__ int2 &at(int i) const { return e[((head + i) & (cap - 1)) * stride]; }
+    __device__ __forceinline__ void push(int node, float pm)
+    {
+        if (cnt == cap) {  // drop the shallowest; it is the deepest dropped so far
+            base = __int_as_float(at(0).y);
+            head = (head + 1) & (cap - 1);
+            --cnt;
+        }
+        at(cnt) = make_int2(node, __float_as_int(pm));
+        ++cnt;
+    }
+};
+
+// The largest power of two <= n (n >= 1): the memo capacity of a region of
+// n entries.
+__device__ __forceinline__ int memo_cap(int n) { return 1 << (31 - __clz(n)); }
+
+// Per-thread int2 entries of the tracers' shared-memory region: the short
+// stack (ShortStack; its depth, so the region takes no L1 beyond it) or the
+// remembered descents (kd-restart), then those of the shadow rays.
+__host__ __device__ __forceinline__ int stack_entries(int tracer, int depth)
+{
+    return tracer == KDGB_TRACER_SHORTSTACK ? depth : kMemo;
+}
+
+// Descends from `node` (record nd) to a leaf, as the reference's kd-restart
+// loop does (Raytracer.cu:73-86); near decisions are remembered in m when
+// given.
+__device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 inv, float tmin, int &node, int4 &nd,
+                                                float &tnext, Memo *m)
+{
+    while (nd.w != KDGB_LEAF) {
+        const float ori = axis_of(o, nd.w), dir = axis_of(inv, nd.w);
+        const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
+        if (tmin < ts) {
+            tnext = kmin(ts, tnext);
+            if (m) m->push(node, tnext);
+            node = 0 < dir ? nd.y : nd.z;
+        } else {
+            node = 0 < dir ? nd.z : nd.y;
+        }
+        nd = __ldg(c.node + node);
+    }
+}
+
+// Where the next kd-restart descent starts: the far child of the topmost
+// remembered near decision whose distance is <= tmin (prefix minima fall
+// with depth, so it is the first entry whose minimum is <= tmin), or the
+// root.
+__device__ __forceinline__ void restart_from(const Ctx &c, float3 inv, float tmin, int &node, int4 &nd, float &tnext,
+                                             Memo *m)
+{
+    if (m && m->cnt > 0 && tmin < m->base) {
+        int lo = 0, hi = m->cnt - 1;  // the deepest entry's minimum is the last tnext <= tmin
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__int_as_float(m->at(mid).y) <= tmin) hi = mid; else lo = mid + 1;
+        }
+        const int2 e = m->at(lo);
+        tnext = lo > 0 ? __int_as_float(m->at(lo - 1).y) : m->base;
+        m->cnt = lo;
+        nd = __ldg(c.node + e.x);
+        node = 0 < axis_of(inv, nd.w) ? nd.z : nd.y;
+        nd = __ldg(c.node + node);
+        return;
+    }
+    if (m) m->reset();
+    node = c.root;
+    nd = __ldg(c.node + c.root);
+    tnext = KDGB_FINF;
+}
+
 // kd-restart, first hit (Raytracer.cu:57-106, 165-262).
+// With memo storage (mem, stride, cap) the descents are remembered (see Memo).
 template <bool SKIP>
 __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int maxit, float &t, float &u, float &v,
-                             float3 *dused = nullptr)
+                             float3 *dused = nullptr, int2 *mem = nullptr, int stride = 0, int cap = kMemo)
 {
     const float3 d = adjust_dir(din);
     const float3 inv = inv3(d);
     if (dused) *dused = d;
     float tmin = 0.0f;
     int iters = 0;
+    Memo memo;
+    memo.e = mem;
+    memo.stride = stride;
+    memo.cap = cap;
+    memo.reset();
+    Memo *m = mem ? &memo : nullptr;
+    int node = c.root;
+    int4 nd = __ldg(c.node + c.root);
+    float tnext = KDGB_FINF;
     do {
-        float tnext = KDGB_FINF;
-        int node = c.root;
-        int4 nd = __ldg(c.node + c.root);
-        while (nd.w != KDGB_LEAF) {
-            const float ori = axis_of(o, nd.w), dir = axis_of(inv, nd.w);
-            const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
-            if (tmin < ts) {
-                node = 0 < dir ? nd.y : nd.z;
-                tnext = kmin(ts, tnext);
-            } else {
-                node = 0 < dir ? nd.z : nd.y;
-            }
-            nd = __ldg(c.node + node);
-        }
+        restart_descend(c, o, inv, tmin, node, nd, tnext, m);
         tmin = __fmul_rn(tnext, 1.00001f);
         if (!SKIP || ray_box(o, inv, __ldg(c.bmin + node), __ldg(c.bmax + node))) {
             float tb = tmin, ub = 0.0f, vb = 0.0f;
@@ -191,7 +285,9 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
             if (h != -1) { t = tb; u = ub; v = vb; return h; }
         }
         if (++iters >= maxit) break;
-    } while (tmin < KDGB_FINF);
+        if (!(tmin < KDGB_FINF)) break;
+        restart_from(c, inv, tmin, node, nd, tnext, m);
+    } while (true);
     return -1;
 }
 
@@ -270,33 +366,32 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
 // ShadowRay (Raytracer.cu:108-163): from the light toward the point, the
 // direction neither normalised nor clamped; leaves whose exit reaches 0.999
 // are not tested; any hit occludes.
-__device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit)
+// With memo storage (mem, stride, cap) the descents are remembered (see Memo).
+__device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 *mem = nullptr, int stride = 0,
+                            int cap = kMemo)
 {
     const float3 d = sub3(pt, lp);
     const float3 inv = inv3(d);
     float tmin = 0.0f;
     int iters = 0;
+    Memo memo;
+    memo.e = mem;
+    memo.stride = stride;
+    memo.cap = cap;
+    memo.reset();
+    Memo *m = mem ? &memo : nullptr;
+    int node = c.root;
+    int4 nd = __ldg(c.node + c.root);
+    float tnext = KDGB_FINF;
     do {
-        float tnext = KDGB_FINF;
-        int node = c.root;
-        int4 nd = __ldg(c.node + c.root);
-        while (nd.w != KDGB_LEAF) {
-            const float ori = axis_of(lp, nd.w), dir = axis_of(inv, nd.w);
-            const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
-            if (tmin < ts) {
-                node = 0 < dir ? nd.y : nd.z;
-                tnext = kmin(ts, tnext);
-            } else {
-                node = 0 < dir ? nd.z : nd.y;
-            }
-            nd = __ldg(c.node + node);
-        }
+        restart_descend(c, lp, inv, tmin, node, nd, tnext, m);
         tmin = __fmul_rn(tnext, 1.00001f);
         if (tmin >= 0.999f) return 0;
         float tb = tmin, ub = 0.0f, vb = 0.0f;
         if (leaf_test(c, nd, lp, d, KDGB_TIE_REF_LAST, tb, ub, vb) != -1) return 1;
         if (++iters >= maxit) break;
-    } while (tmin < 0.999f);
+        restart_from(c, inv, tmin, node, nd, tnext, m);
+    } while (true);
     return 0;
 }
 
@@ -304,6 +399,11 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit)
 __device__ __forceinline__ int64_t ray_index(int64_t id, int tile_width)
 {
     if (tile_width <= 0) return id;
+    if (id < 0x7fffffff) {  // 32-bit arithmetic for image-sized launches
+        const int32_t i = (int32_t)id, cell = i >> 5, cols = tile_width >> 2;
+        const int32_t by = cell / cols, bx = cell - by * cols;
+        return (int64_t)(bx * 4 + (i & 3)) + (int64_t)(by * 8 + ((i & 31) >> 2)) * tile_width;
+    }
     const int64_t cell = id / 32;
     const int64_t cols = tile_width / 4;
     const int64_t bx = cell % cols, by = cell / cols;
@@ -336,61 +436,98 @@ struct TraceArgs {
     const int32_t *build_err;
 };
 
+// A shadow ray waiting in a block's queue: the hit point, the tree root and
+// the ray it belongs to.
+struct ShadowItem {
+    float4 p;  // w = root bits
+    int64_t ray;
+    int64_t pad;
+};
+
+// Dynamic shared memory: the per-thread regions of stack_entries() int2
+// (short stack or remembered descents) followed, with shadow rays, by a
+// queue of blockDim ShadowItem.
 template <int TRACER, bool SKIP, bool SHADOW>
 __global__ void k_trace(TraceArgs a)
 {
-    extern __shared__ int2 stack_smem[];
+    extern __shared__ __align__(16) unsigned char trace_smem[];
+    int2 *stack_smem = (int2 *)trace_smem;
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= a.n) return;
-    const int64_t i = ray_index(id, a.tile_width);
-    if (a.build_err && *a.build_err) {
-        a.hit[i] = -1;
-        a.t[i] = INFINITY;
-        a.u[i] = 0.0f;
-        a.v[i] = 0.0f;
-        if (SHADOW) a.occ[i] = 0;
+    const bool live = id < a.n;
+    const int64_t i = live ? ray_index(id, a.tile_width) : 0;
+    if (a.build_err && *a.build_err) {  // grid-uniform
+        if (live) {
+            a.hit[i] = -1;
+            a.t[i] = INFINITY;
+            a.u[i] = 0.0f;
+            a.v[i] = 0.0f;
+            if (SHADOW) a.occ[i] = 0;
+        }
         return;
     }
-    const float3 o = ld3(a.o, i), d = ld3(a.d, i);
+    float3 o = make_float3(0.f, 0.f, 0.f), d = o;
     Ctx c = a.c;
-    int32_t id_off = 0;
-    if (a.mesh_off) {
-        int m = a.ray_mesh ? a.ray_mesh[i] : (int)(i / a.rays_per_mesh);
-        m = m < 0 ? 0 : (m >= a.n_meshes ? a.n_meshes - 1 : m);
-        c.root = m;
-        id_off = a.mesh_off[m];
-    }
     float t = 0.0f, u = 0.0f, v = 0.0f;
-    int h;
-    if (TRACER == KDGB_TRACER_SHORTSTACK)
-        h = trace_shortstack<SKIP>(c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u, v);
-    else
-        h = trace_restart<SKIP>(c, o, d, a.tie, a.maxit, t, u, v);
-    if (h < 0) { t = INFINITY; u = 0.0f; v = 0.0f; }
-    a.hit[i] = h >= 0 ? h - id_off : h;
-    a.t[i] = t;
-    a.u[i] = u;
-    a.v[i] = v;
+    int h = -1;
+    if (live) {
+        o = ld3(a.o, i);
+        d = ld3(a.d, i);
+        int32_t id_off = 0;
+        if (a.mesh_off) {
+            int m = a.ray_mesh ? a.ray_mesh[i] : (int)(i / a.rays_per_mesh);
+            m = m < 0 ? 0 : (m >= a.n_meshes ? a.n_meshes - 1 : m);
+            c.root = m;
+            id_off = a.mesh_off[m];
+        }
+        if (TRACER == KDGB_TRACER_SHORTSTACK)
+            h = trace_shortstack<SKIP>(c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u,
+                                       v);
+        else
+            h = trace_restart<SKIP>(c, o, d, a.tie, a.maxit, t, u, v, nullptr, stack_smem + threadIdx.x, blockDim.x);
+        if (h < 0) { t = INFINITY; u = 0.0f; v = 0.0f; }
+        a.hit[i] = h >= 0 ? h - id_off : h;
+        a.t[i] = t;
+        a.u[i] = u;
+        a.v[i] = v;
+    }
     if (SHADOW) {
-        int occ = 0;
+        // The block's shadow rays (one per primary hit) are packed onto its
+        // first threads, so warps stay full while they are traced.
+        __shared__ int s_count;
+        ShadowItem *queue = (ShadowItem *)(trace_smem + sizeof(int2) * stack_entries(TRACER, a.depth) * blockDim.x);
+        if (threadIdx.x == 0) s_count = 0;
+        __syncthreads();
         if (h >= 0) {
             const float3 p = make_float3(__fadd_rn(o.x, __fmul_rn(t, d.x)), __fadd_rn(o.y, __fmul_rn(t, d.y)),
                                          __fadd_rn(o.z, __fmul_rn(t, d.z)));
-            occ = trace_shadow(c, a.light, p, a.maxit);
+            const int slot = atomicAdd(&s_count, 1);
+            queue[slot].p = make_float4(p.x, p.y, p.z, __int_as_float(c.root));
+            queue[slot].ray = i;
+        } else if (live) {
+            a.occ[i] = 0;
         }
-        a.occ[i] = occ;
+        __syncthreads();
+        if ((int)threadIdx.x < s_count) {
+            const ShadowItem q = queue[threadIdx.x];
+            Ctx cs = a.c;
+            cs.root = __float_as_int(q.p.w);
+            a.occ[q.ray] = trace_shadow(cs, a.light, make_float3(q.p.x, q.p.y, q.p.z), a.maxit,
+                                        stack_smem + threadIdx.x, blockDim.x,
+                                        memo_cap(stack_entries(TRACER, a.depth)));
+        }
     }
 }
 
 __global__ void k_shadow(TraceArgs a)
 {
+    extern __shared__ int2 memo_smem[];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     if (a.build_err && *a.build_err) {
         a.occ[i] = 0;
         return;
     }
-    a.occ[i] = trace_shadow(a.c, a.light, ld3(a.o, i), a.maxit);
+    a.occ[i] = trace_shadow(a.c, a.light, ld3(a.o, i), a.maxit, memo_smem + threadIdx.x, blockDim.x);
 }
 
 // Brute force (BruteTracer.cu:54-96): every ray tests every triangle in id
@@ -496,7 +633,7 @@ __global__ void k_photons(PhotonArgs a)
             h = trace_shortstack<SKIP>(a.c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u,
                                        v);
         else
-            h = trace_restart<SKIP>(a.c, o, d, a.tie, a.maxit, t, u, v);
+            h = trace_restart<SKIP>(a.c, o, d, a.tie, a.maxit, t, u, v, nullptr, stack_smem + threadIdx.x, blockDim.x);
         a.seg_hit[base + k] = h;
         a.seg_t[base + k] = h >= 0 ? t : INFINITY;
         ++k;
@@ -663,7 +800,7 @@ __global__ void k_shade(ShadeArgs a)
                 h = trace_shortstack<SKIP>(a.c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x,
                                            t, u, v, &dh);
             else if (TRACER == KDGB_TRACER_RESTART)
-                h = trace_restart<SKIP>(a.c, o, d, a.tie, a.maxit, t, u, v, &dh);
+                h = trace_restart<SKIP>(a.c, o, d, a.tie, a.maxit, t, u, v, &dh, stack_smem + threadIdx.x, blockDim.x);
             else
                 h = brute_hit(a, o, d, t, u, v);
             if (h < 0) break;
@@ -789,19 +926,20 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
     const unsigned grid = blocks_for(n, bs);
     const bool skip = p.leaf_skipping != 0;
     const bool shadow = occ != nullptr;
-    size_t smem = 0;
+    const size_t smem = sizeof(int2) * (size_t)stack_entries(p.tracer, p.stack_depth) * bs +
+                        (shadow ? sizeof(ShadowItem) * (size_t)bs : 0);
+    void (*kernel)(TraceArgs);
     if (p.tracer == KDGB_TRACER_SHORTSTACK) {
-        smem = sizeof(int2) * (size_t)p.stack_depth * bs;
-        if (skip && shadow) k_trace<KDGB_TRACER_SHORTSTACK, true, true><<<grid, bs, smem, s>>>(a);
-        else if (skip) k_trace<KDGB_TRACER_SHORTSTACK, true, false><<<grid, bs, smem, s>>>(a);
-        else if (shadow) k_trace<KDGB_TRACER_SHORTSTACK, false, true><<<grid, bs, smem, s>>>(a);
-        else k_trace<KDGB_TRACER_SHORTSTACK, false, false><<<grid, bs, smem, s>>>(a);
+        kernel = skip ? (shadow ? k_trace<KDGB_TRACER_SHORTSTACK, true, true> : k_trace<KDGB_TRACER_SHORTSTACK, true, false>)
+                      : (shadow ? k_trace<KDGB_TRACER_SHORTSTACK, false, true>
+                                : k_trace<KDGB_TRACER_SHORTSTACK, false, false>);
     } else {
-        if (skip && shadow) k_trace<KDGB_TRACER_RESTART, true, true><<<grid, bs, 0, s>>>(a);
-        else if (skip) k_trace<KDGB_TRACER_RESTART, true, false><<<grid, bs, 0, s>>>(a);
-        else if (shadow) k_trace<KDGB_TRACER_RESTART, false, true><<<grid, bs, 0, s>>>(a);
-        else k_trace<KDGB_TRACER_RESTART, false, false><<<grid, bs, 0, s>>>(a);
+        kernel = skip ? (shadow ? k_trace<KDGB_TRACER_RESTART, true, true> : k_trace<KDGB_TRACER_RESTART, true, false>)
+                      : (shadow ? k_trace<KDGB_TRACER_RESTART, false, true> : k_trace<KDGB_TRACER_RESTART, false, false>);
     }
+    // Large blocks with deep stacks need more than the default 48 KB.
+    if (smem > 48 * 1024) KDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<grid, bs, smem, s>>>(a);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
@@ -828,7 +966,10 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
     a.maxit = p.max_iterations > 0 ? p.max_iterations : kDefaultMaxIterations;
     a.tile_width = 0;
     const int bs = p.block_size > 0 ? p.block_size : 128;
-    k_shadow<<<blocks_for(n, bs), bs, 0, s>>>(a);
+    const size_t smem = sizeof(int2) * (size_t)kMemo * bs;
+    if (smem > 48 * 1024)
+        KDGB_CUDA(cudaFuncSetAttribute(k_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_shadow<<<blocks_for(n, bs), bs, smem, s>>>(a);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
@@ -867,13 +1008,16 @@ int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_p
     const int bs = p.block_size > 0 ? p.block_size : 128;
     const unsigned grid = blocks_for(n, bs);
     const bool skip = p.leaf_skipping != 0;
-    if (p.tracer == KDGB_TRACER_SHORTSTACK) {
-        const size_t smem = sizeof(int2) * (size_t)p.stack_depth * bs;
-        if (skip) k_photons<KDGB_TRACER_SHORTSTACK, true><<<grid, bs, smem, s>>>(a);
-        else k_photons<KDGB_TRACER_SHORTSTACK, false><<<grid, bs, smem, s>>>(a);
-    } else {
-        if (skip) k_photons<KDGB_TRACER_RESTART, true><<<grid, bs, 0, s>>>(a);
-        else k_photons<KDGB_TRACER_RESTART, false><<<grid, bs, 0, s>>>(a);
+    {
+        const size_t smem = sizeof(int2) * (size_t)stack_entries(p.tracer, p.stack_depth) * bs;
+        void (*kernel)(PhotonArgs);
+        if (p.tracer == KDGB_TRACER_SHORTSTACK)
+            kernel = skip ? k_photons<KDGB_TRACER_SHORTSTACK, true> : k_photons<KDGB_TRACER_SHORTSTACK, false>;
+        else
+            kernel = skip ? k_photons<KDGB_TRACER_RESTART, true> : k_photons<KDGB_TRACER_RESTART, false>;
+        if (smem > 48 * 1024)
+            KDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kernel<<<grid, bs, smem, s>>>(a);
     }
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
@@ -911,13 +1055,16 @@ int shade_launch(const Tree &t, const kdgb_trace_params &p, const float *n0, con
     const int bs = p.block_size > 0 ? p.block_size : 128;
     const unsigned grid = blocks_for(n, bs);
     const bool skip = p.leaf_skipping != 0;
-    if (p.tracer == KDGB_TRACER_SHORTSTACK) {
-        const size_t smem = sizeof(int2) * (size_t)p.stack_depth * bs;
-        if (skip) k_shade<KDGB_TRACER_SHORTSTACK, true><<<grid, bs, smem, s>>>(a);
-        else k_shade<KDGB_TRACER_SHORTSTACK, false><<<grid, bs, smem, s>>>(a);
-    } else if (p.tracer == KDGB_TRACER_RESTART) {
-        if (skip) k_shade<KDGB_TRACER_RESTART, true><<<grid, bs, 0, s>>>(a);
-        else k_shade<KDGB_TRACER_RESTART, false><<<grid, bs, 0, s>>>(a);
+    if (p.tracer == KDGB_TRACER_SHORTSTACK || p.tracer == KDGB_TRACER_RESTART) {
+        const size_t smem = sizeof(int2) * (size_t)stack_entries(p.tracer, p.stack_depth) * bs;
+        void (*kernel)(ShadeArgs);
+        if (p.tracer == KDGB_TRACER_SHORTSTACK)
+            kernel = skip ? k_shade<KDGB_TRACER_SHORTSTACK, true> : k_shade<KDGB_TRACER_SHORTSTACK, false>;
+        else
+            kernel = skip ? k_shade<KDGB_TRACER_RESTART, true> : k_shade<KDGB_TRACER_RESTART, false>;
+        if (smem > 48 * 1024)
+            KDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kernel<<<grid, bs, smem, s>>>(a);
     } else {
         k_shade<KDGB_TRACER_BRUTE, false><<<grid, bs, 0, s>>>(a);
     }

@@ -106,7 +106,10 @@ def test_shadow_rays(kdgb_lib, cuda, oracle, clustered):
 
 
 @pytest.mark.parametrize("tracer", [0, 1])
-def test_fused_primary_shadow(kdgb_lib, cuda, oracle, clustered, tracer):
+@pytest.mark.parametrize("block_size", [0, 64, 1024])
+def test_fused_primary_shadow(kdgb_lib, cuda, oracle, clustered, tracer, block_size):
+    """Shadow rays are packed onto a block's first threads; 1024-thread
+    blocks need more than 48 KB of shared memory."""
     tris, tree, o, d = clustered
     light = (0.5, 3.0, 0.5)
     ref = oracle.trace(tree, tris, o, d, tracer=tracer, stack_depth=8)
@@ -114,7 +117,7 @@ def test_fused_primary_shadow(kdgb_lib, cuda, oracle, clustered, tracer):
     occ_ref = oracle.trace_shadow(tree, tris, pts, light)
     occ_ref[ref[0] < 0] = 0
     with kdgb_lib.KDTree.upload(tree, tris) as gt:
-        h, t, u, v, occ = gt.trace_primary_shadow(o, d, light, tracer=tracer, stack_depth=8)
+        h, t, u, v, occ = gt.trace_primary_shadow(o, d, light, tracer=tracer, stack_depth=8, block_size=block_size)
         assert_hits_equal((h, t, u, v), ref)
         assert np.array_equal(np_(occ), occ_ref)
 
