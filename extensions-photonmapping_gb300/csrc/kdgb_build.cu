@@ -1850,9 +1850,11 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
         else k_count<false><<<gN, kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
-    KDGB_CHECK(scan_exclusive<2>(a.tilesum, a.tileoff, ceil_div(e.N, kTileRefs), s, &w.scan, &a.st->ntiles, &a.st->err));
+    // Tile offsets and node bases: independent scans, one launch.
     const NodeLanes lanes{a.cnt, a.ess_cnt, a.LS};
-    KDGB_CHECK((scan_exclusive_in<kLanes, NodeLanes>(lanes, a.lbase, e.R, s, &w.scan, &a.st->R, &a.st->err)));
+    KDGB_CHECK((scan_exclusive_pair<2, ScanArray<2>, kLanes, NodeLanes>(
+        ScanArray<2>{a.tilesum}, a.tileoff, ceil_div(e.N, kTileRefs), &a.st->ntiles, lanes, a.lbase, e.R, &a.st->R, s,
+        &w.scan, &a.st->err)));
     if (e.N > 0) {
         if (a.divide) k_scatter<true><<<gN, kBlock, 0, s>>>(a);
         else k_scatter<false><<<gN, kBlock, 0, s>>>(a);
@@ -2250,7 +2252,7 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     BuildArgs a;
     Extents e;
     graph_args(t, p, T, M, nullptr, a, e);
-    const int64_t parts = std::max({scan_partials_needed(2, ceil_div(e.N, kTileRefs)), scan_partials_needed(kLanes, e.R),
+    const int64_t parts = std::max({scan_pair_needed(ceil_div(e.N, kTileRefs), e.R),
                                     scan_partials_needed(1, e.low_R), scan_partials_needed(1, e.nodes),
                                     (int64_t)1});
     KDGB_CHECK(ensure(w.scan, parts, s, 0, true));  // zeroed scan state

@@ -250,6 +250,15 @@ inline int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream
 // Workspace (int32 elements) a scan of n records of K lanes needs.
 int64_t scan_partials_needed(int K, int64_t n);
 
+// Two independent scans (as scan_exclusive_in each) in one launch.
+template <int K1, class In1, int K2, class In2>
+int scan_exclusive_pair(const In1 &in1, int32_t *out1, int64_t n1, const int32_t *n1_dev, const In2 &in2,
+                        int32_t *out2, int64_t n2, const int32_t *n2_dev, cudaStream_t s, DevArray<int32_t> *ws,
+                        int32_t *err = nullptr);
+
+// Workspace (int32 elements) a scan pair of n1 and n2 records needs.
+int64_t scan_pair_needed(int64_t n1, int64_t n2);
+
 // Hash of every device buffer's address and capacity: a captured graph is
 // valid while this is unchanged.
 uint64_t layout_signature(const Tree &t);

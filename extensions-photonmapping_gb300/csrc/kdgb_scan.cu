@@ -113,105 +113,115 @@ __device__ __forceinline__ unsigned load_flag(const int32_t *p)
     return *(const volatile unsigned *)p;
 }
 
+// One tile of a single-pass scan, run by a whole block: tile `tile` of the
+// n records of `in`, with its status in `status` (tiles of this scan only).
 template <int K, class In>
-__global__ void __launch_bounds__(kThreads) scan_lookback_kernel(const In in, int32_t *__restrict__ out, int64_t n,
-                                                                 const int32_t *__restrict__ n_dev, int32_t *ws,
-                                                                 int32_t *err)
+__device__ __forceinline__ void scan_tile(const In &in, int32_t *__restrict__ out, int64_t n, int64_t tile,
+                                          int32_t *status, unsigned epoch, int32_t *err)
 {
-    __shared__ int64_t s_tile;
     __shared__ int32_t s_excl[K];
-    unsigned *ctl = (unsigned *)ws;
-    int32_t *status = ws + kCtl;
-    if (n_dev) n = *n_dev;
-    const unsigned epoch = *(volatile unsigned *)(ctl + 2) & 0x3fffffffu;
-    if (threadIdx.x == 0) s_tile = atomicAdd(ctl + 0, 1u);
-    __syncthreads();
-    const int64_t tile = s_tile, ntiles = (n + kTile - 1) / kTile;
-    if (tile < ntiles) {
-        const int64_t base = tile * kTile + (int64_t)threadIdx.x * kItems;
-        int32_t vals[kItems][K], s[K], tot[K];
-        load_items<K>(in, base, n, vals, s);
-        block_scan<K, kThreads>(s, tot);
-        int32_t *mine = status + kStatus * tile;
-        if (threadIdx.x == 0) {
-            // Publish the tile totals (for tile 0 they are the inclusive prefix).
-            const int off = tile == 0 ? kIncl : 0;
+    const int64_t ntiles = (n + kTile - 1) / kTile;
+    if (tile >= ntiles) {  // block-uniform
+        if (tile == 0 && threadIdx.x < K) out[threadIdx.x] = 0;  // n == 0: the totals record only
+        return;
+    }
+    const int64_t base = tile * kTile + (int64_t)threadIdx.x * kItems;
+    int32_t vals[kItems][K], s[K], tot[K];
+    load_items<K>(in, base, n, vals, s);
+    block_scan<K, kThreads>(s, tot);
+    int32_t *mine = status + kStatus * tile;
+    if (threadIdx.x == 0) {
+        // Publish the tile totals (for tile 0 they are the inclusive prefix).
+        const int off = tile == 0 ? kIncl : 0;
 #pragma unroll
-            for (int k = 0; k < K; ++k) ((volatile int32_t *)mine)[off + k] = tot[k];
-            __threadfence();
-            ((volatile unsigned *)mine)[kFlag] = (epoch << 2) | (tile == 0 ? kPrefix : kAggregate);
-        }
-        if (threadIdx.x < 32) {
-            const int lane = threadIdx.x;
-            int32_t excl[K];
+        for (int k = 0; k < K; ++k) ((volatile int32_t *)mine)[off + k] = tot[k];
+        __threadfence();
+        ((volatile unsigned *)mine)[kFlag] = (epoch << 2) | (tile == 0 ? kPrefix : kAggregate);
+    }
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        int32_t excl[K];
 #pragma unroll
-            for (int k = 0; k < K; ++k) excl[k] = 0;
-            int64_t j = tile - 1;  // nearest unread predecessor
-            while (j >= 0) {      // warp-uniform
-                const int64_t t = j - lane;
-                unsigned f = 0;
-                bool dead = false;
-                if (t >= 0) {
-                    int spins = 0;
-                    f = load_flag(status + kStatus * t + kFlag);
-                    while ((f >> 2) != epoch || (f & 3u) == 0) {
-                        if (++spins > kSpinLimit) {
-                            if (err) atomicCAS(err, 0, KDGB_ERR_TIMEOUT);
-                            f = (epoch << 2) | kPrefix;  // give up: count it as a zero prefix
-                            dead = true;
-                            break;
-                        }
-                        __nanosleep(64);
-                        f = load_flag(status + kStatus * t + kFlag);
+        for (int k = 0; k < K; ++k) excl[k] = 0;
+        int64_t j = tile - 1;  // nearest unread predecessor
+        while (j >= 0) {      // warp-uniform
+            const int64_t t = j - lane;
+            unsigned f = 0;
+            bool dead = false;
+            if (t >= 0) {
+                int spins = 0;
+                f = load_flag(status + kStatus * t + kFlag);
+                while ((f >> 2) != epoch || (f & 3u) == 0) {
+                    if (++spins > kSpinLimit) {
+                        if (err) atomicCAS(err, 0, KDGB_ERR_TIMEOUT);
+                        f = (epoch << 2) | kPrefix;  // give up: count it as a zero prefix
+                        dead = true;
+                        break;
                     }
-                }
-                __threadfence();
-                // Lanes up to the first prefix (nearest predecessor first) count.
-                const unsigned pm = __ballot_sync(kFull, t >= 0 && (f & 3u) == kPrefix);
-                const int stop = pm ? __ffs(pm) - 1 : 31;
-                const bool use = t >= 0 && lane <= stop && !dead;
-                const int off = (f & 3u) == kPrefix ? kIncl : 0;
-#pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    int32_t v = use ? ((const volatile int32_t *)(status + kStatus * t))[off + k] : 0;
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-                    excl[k] += v;
-                }
-                if (pm) break;
-                j -= 32;
-            }
-            if (lane == 0) {
-#pragma unroll
-                for (int k = 0; k < K; ++k) s_excl[k] = excl[k];
-                if (tile > 0) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) ((volatile int32_t *)mine)[kIncl + k] = excl[k] + tot[k];
-                    __threadfence();
-                    ((volatile unsigned *)mine)[kFlag] = (epoch << 2) | kPrefix;
+                    __nanosleep(64);
+                    f = load_flag(status + kStatus * t + kFlag);
                 }
             }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < K; ++k) s[k] += s_excl[k];
-#pragma unroll
-        for (int i = 0; i < kItems; ++i) {
+            __threadfence();
+            // Lanes up to the first prefix (nearest predecessor first) count.
+            const unsigned pm = __ballot_sync(kFull, t >= 0 && (f & 3u) == kPrefix);
+            const int stop = pm ? __ffs(pm) - 1 : 31;
+            const bool use = t >= 0 && lane <= stop && !dead;
+            const int off = (f & 3u) == kPrefix ? kIncl : 0;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
-                if (base + i < n) out[(base + i) * K + k] = s[k];
-                s[k] += vals[i][k];
+                int32_t v = use ? ((const volatile int32_t *)(status + kStatus * t))[off + k] : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+                excl[k] += v;
+            }
+            if (pm) break;
+            j -= 32;
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) s_excl[k] = excl[k];
+            if (tile > 0) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) ((volatile int32_t *)mine)[kIncl + k] = excl[k] + tot[k];
+                __threadfence();
+                ((volatile unsigned *)mine)[kFlag] = (epoch << 2) | kPrefix;
             }
         }
-        if (tile == ntiles - 1 && threadIdx.x == 0) {
-#pragma unroll
-            for (int k = 0; k < K; ++k) out[n * K + k] = s_excl[k] + tot[k];
-        }
-    } else if (tile == 0 && threadIdx.x < K) {
-        out[threadIdx.x] = 0;  // n == 0: the totals record only
     }
-    // The last block to finish resets the tickets and opens the next epoch.
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] += s_excl[k];
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (base + i < n) out[(base + i) * K + k] = s[k];
+            s[k] += vals[i][k];
+        }
+    }
+    if (tile == ntiles - 1 && threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[n * K + k] = s_excl[k] + tot[k];
+    }
+}
+
+// Takes a ticket (tiles in the order blocks start) and reads the epoch.
+__device__ __forceinline__ int64_t scan_ticket(int32_t *ws, unsigned &epoch)
+{
+    __shared__ int64_t s_tile;
+    unsigned *ctl = (unsigned *)ws;
+    epoch = *(volatile unsigned *)(ctl + 2) & 0x3fffffffu;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ctl + 0, 1u);
+    __syncthreads();
+    return s_tile;
+}
+
+// The last block to finish resets the tickets and opens the next epoch.
+__device__ __forceinline__ void scan_finish(int32_t *ws, unsigned epoch)
+{
     if (threadIdx.x == 0) {
+        unsigned *ctl = (unsigned *)ws;
         __threadfence();
         if (atomicAdd(ctl + 1, 1u) == gridDim.x - 1) {
             ctl[0] = 0;
@@ -220,6 +230,36 @@ __global__ void __launch_bounds__(kThreads) scan_lookback_kernel(const In in, in
             __threadfence();
         }
     }
+}
+
+template <int K, class In>
+__global__ void __launch_bounds__(kThreads) scan_lookback_kernel(const In in, int32_t *__restrict__ out, int64_t n,
+                                                                 const int32_t *__restrict__ n_dev, int32_t *ws,
+                                                                 int32_t *err)
+{
+    if (n_dev) n = *n_dev;
+    unsigned epoch;
+    const int64_t tile = scan_ticket(ws, epoch);
+    scan_tile<K>(in, out, n, tile, ws + kCtl, epoch, err);
+    scan_finish(ws, epoch);
+}
+
+// Two independent scans in one launch: tickets below nb1 take tiles of the
+// first, the rest tiles of the second (its status follows the first's).
+template <int K1, class In1, int K2, class In2>
+__global__ void __launch_bounds__(kThreads) scan_pair_kernel(const In1 in1, int32_t *__restrict__ out1, int64_t n1,
+                                                             const int32_t *__restrict__ n1_dev, int64_t nb1,
+                                                             const In2 in2, int32_t *__restrict__ out2, int64_t n2,
+                                                             const int32_t *__restrict__ n2_dev, int32_t *ws,
+                                                             int32_t *err)
+{
+    if (n1_dev) n1 = *n1_dev;
+    if (n2_dev) n2 = *n2_dev;
+    unsigned epoch;
+    const int64_t ticket = scan_ticket(ws, epoch);
+    if (ticket < nb1) scan_tile<K1>(in1, out1, n1, ticket, ws + kCtl, epoch, err);
+    else scan_tile<K2>(in2, out2, n2, ticket - nb1, ws + kCtl + kStatus * nb1, epoch, err);
+    scan_finish(ws, epoch);
 }
 
 }  // namespace
@@ -249,6 +289,38 @@ int scan_exclusive_in(const In &in, int32_t *out, int64_t n, cudaStream_t s, Dev
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
+
+template <int K1, class In1, int K2, class In2>
+int scan_exclusive_pair(const In1 &in1, int32_t *out1, int64_t n1, const int32_t *n1_dev, const In2 &in2,
+                        int32_t *out2, int64_t n2, const int32_t *n2_dev, cudaStream_t s, DevArray<int32_t> *ws,
+                        int32_t *err)
+{
+    static_assert(K1 <= 7 && K2 <= 7, "a tile status holds K lanes twice and a flag");
+    if (n1 < 0 || n2 < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "scan: negative length");
+    if (!ws) return fail(KDGB_ERR_INVALID_ARGUMENT, "scan: no workspace");
+    const int64_t nb1 = std::max<int64_t>(1, (n1 + kTile - 1) / kTile);
+    const int64_t nb2 = std::max<int64_t>(1, (n2 + kTile - 1) / kTile);
+    const int64_t need = kCtl + kStatus * (nb1 + nb2);
+    if (!ws->p || need > ws->cap) {
+        const int64_t want = std::max<int64_t>(need, ws->cap + ws->cap / 2);
+        KDGB_CHECK(ensure(*ws, want, s, ws->p ? kCtl : 0, true));
+    }
+    scan_pair_kernel<K1, In1, K2, In2><<<(unsigned)(nb1 + nb2), kThreads, 0, s>>>(in1, out1, n1, n1_dev, nb1, in2,
+                                                                                 out2, n2, n2_dev, ws->p, err);
+    KDGB_LAUNCH_CHECK();
+    return KDGB_OK;
+}
+
+int64_t scan_pair_needed(int64_t n1, int64_t n2)
+{
+    return kCtl + kStatus * (std::max<int64_t>(1, (n1 + kTile - 1) / kTile) +
+                             std::max<int64_t>(1, (n2 + kTile - 1) / kTile));
+}
+
+template int scan_exclusive_pair<2, ScanArray<2>, 7, NodeLanes>(const ScanArray<2> &, int32_t *, int64_t,
+                                                               const int32_t *, const NodeLanes &, int32_t *,
+                                                               int64_t, const int32_t *, cudaStream_t,
+                                                               DevArray<int32_t> *, int32_t *);
 
 template int scan_exclusive_in<1, ScanArray<1>>(const ScanArray<1> &, int32_t *, int64_t, cudaStream_t,
                                              DevArray<int32_t> *, const int32_t *, int32_t *);
