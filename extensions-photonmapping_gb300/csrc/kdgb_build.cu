@@ -473,7 +473,7 @@ __device__ __forceinline__ void divide_flags(const BuildArgs &a, int32_t prim, i
 // (AabbMemset, ReduceSegments.h:328-335): k_node_split has consumed this
 // level's keys and k_scatter reduces the children's boxes into them.
 template <bool DIVIDE>
-__global__ void __launch_bounds__(kBlock) k_count(const BuildArgs a)
+__global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_count(const BuildArgs a)
 {
     {
         const int64_t next = min(2 * (int64_t)a.st->R, a.cap.R);
@@ -715,7 +715,7 @@ __device__ __forceinline__ SahNode sah_node(const BuildArgs &a, int32_t node)
 // block each, taken from a work counter: every warp bins an interleaved
 // share of the rows into its own histograms, which are then summed.  Then
 // the smaller nodes, one warp each.
-__global__ void __launch_bounds__(kBlock) k_sah_bin(const BuildArgs a)
+__global__ void __launch_bounds__(kBlock, 4) k_sah_bin(const BuildArgs a)
 {
     __shared__ int s_hist[kWarps][6 * 32];
     __shared__ int32_t s_big;
@@ -862,7 +862,7 @@ __device__ __forceinline__ void child_keys_atomic(const BuildArgs &a, int32_t R,
 // rows belong to one parent and issues atomics only when the parent changes;
 // the warps of a block merge equal parents before their atomics.
 template <bool DIVIDE>
-__global__ void __launch_bounds__(kBlock) k_scatter(const BuildArgs a)
+__global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_scatter(const BuildArgs a)
 {
     __shared__ int32_t s_off[kWarps][2];
     __shared__ int s_owner[kWarps];

@@ -159,6 +159,28 @@ __device__ __forceinline__ int leaf_test(const Ctx &c, int4 leaf, float3 o, floa
     return hit;
 }
 
+// Whether any triangle of the leaf is hit within [0, tb] (the reference's
+// shadow test, REF_LAST acceptance): the first accepted triangle settles it,
+// so the loop stops there with the result testing all of them gives.
+__device__ __forceinline__ bool leaf_any(const Ctx &c, int4 leaf, float3 o, float3 d, float tb)
+{
+    int hit = -1;
+    float ub = 0.0f, vb = 0.0f;
+    if (c.woop) {
+        for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) {
+            const int id = __float_as_int(__ldg(c.tri + 3 * (int64_t)r + 2).y);
+            woop_test(c.woop + 3 * (int64_t)id, id, o, d, KDGB_TIE_REF_LAST, hit, tb, ub, vb);
+            if (hit != -1) return true;
+        }
+    } else {
+        for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) {
+            mt_record(c.tri, r, o, d, KDGB_TIE_REF_LAST, hit, tb, ub, vb);
+            if (hit != -1) return true;
+        }
+    }
+    return false;
+}
+
 // Remembered descents for kd-restart.  A restart descends from the root
 // with tmin' = tnext * 1.00001, larger than the tmin of the previous
 // descent, so it repeats every decision of that descent (far ones stay far,
@@ -387,8 +409,7 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 
         restart_descend(c, lp, inv, tmin, node, nd, tnext, m);
         tmin = __fmul_rn(tnext, 1.00001f);
         if (tmin >= 0.999f) return 0;
-        float tb = tmin, ub = 0.0f, vb = 0.0f;
-        if (leaf_test(c, nd, lp, d, KDGB_TIE_REF_LAST, tb, ub, vb) != -1) return 1;
+        if (leaf_any(c, nd, lp, d, tmin)) return 1;
         if (++iters >= maxit) break;
         restart_from(c, inv, tmin, node, nd, tnext, m);
     } while (true);
