@@ -1631,7 +1631,9 @@ __global__ void k_pack_nodes(int32_t n_host, const int32_t *n_dev, const int32_t
     }
 }
 
-// One thread per node; a leaf writes its records in bitmap order (LSB first).
+// One warp per node; lane j of a leaf writes the record of bitmap bit j at
+// the leaf's offset + the rank of j among the set bits (bitmap order, LSB
+// first), so a leaf's gathers are all in flight at once.
 __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t *err, int64_t cap_tris,
                             const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
                             const int32_t *__restrict__ pidx, const int32_t *__restrict__ prim_indices,
@@ -1641,24 +1643,21 @@ __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t 
 {
     const int32_t n = n_dev ? *n_dev : n_host;
     if (!pack_ok(n, err, off, cap_tris)) return;
-    GRID_STRIDE(node, n) {
-        if ((info[node] & 3) != KDGB_LEAF) continue;
-        unsigned bmp = (unsigned)bitmap[node];
-        const int32_t pi = pidx[node];
-        int64_t rec = off[node];
-        while (bmp) {
-            const int j = __ffs(bmp) - 1;
-            bmp &= bmp - 1u;
-            const int32_t prim = prim_indices[pi + j];
-            const float4 pa = p0[prim], pb = p1[prim], pc = p2[prim];
-            const float3 v0 = make_float3(pa.x, pa.y, pa.z);
-            const float3 e1 = sub3(make_float3(pb.x, pb.y, pb.z), v0);
-            const float3 e2 = sub3(make_float3(pc.x, pc.y, pc.z), v0);
-            ttri[3 * rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
-            ttri[3 * rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
-            ttri[3 * rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
-            ++rec;
-        }
+    const unsigned lane = threadIdx.x & 31;
+    WARP_STRIDE(w, n) {
+        const int32_t node = (int32_t)w;
+        if ((info[node] & 3) != KDGB_LEAF) continue;  // warp-uniform
+        const unsigned bmp = (unsigned)bitmap[node];
+        if (!((bmp >> lane) & 1u)) continue;
+        const int64_t rec = off[node] + __popc(bmp & ((1u << lane) - 1u));
+        const int32_t prim = prim_indices[pidx[node] + lane];
+        const float4 pa = p0[prim], pb = p1[prim], pc = p2[prim];
+        const float3 v0 = make_float3(pa.x, pa.y, pa.z);
+        const float3 e1 = sub3(make_float3(pb.x, pb.y, pb.z), v0);
+        const float3 e2 = sub3(make_float3(pc.x, pc.y, pc.z), v0);
+        ttri[3 * rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
+        ttri[3 * rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
+        ttri[3 * rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
     }
 }
 
@@ -1924,7 +1923,8 @@ int emit_pack(const BuildArgs &a, const Launcher &L, const Extents &e, cudaStrea
     k_pack_nodes<<<g, kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info, a.split, a.ch, a.loff,
                                       a.tnode);
     KDGB_LAUNCH_CHECK();
-    k_pack_tris<<<g, kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info, a.amt, a.pidx,
+    k_pack_tris<<<L.grid(e.nodes * 32, kBlock), kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info,
+                                                                 a.amt, a.pidx,
                                      a.prim_indices, a.p0, a.p1, a.p2, a.loff, a.ttri);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
@@ -2080,8 +2080,9 @@ int pack_for_traversal(Tree &t, cudaStream_t s)
         k_pack_nodes<<<g, kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p, t.split.p, t.children.p, off,
                                           t.tnode.p);
         KDGB_LAUNCH_CHECK();
-        k_pack_tris<<<g, kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p, t.bitmap.p, t.pidx.p,
-                                         t.prim_indices.p, t.p0.p, t.p1.p, t.p2.p, off, t.ttri.p);
+        k_pack_tris<<<L.grid((int64_t)n * 32, kBlock), kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p,
+                                                                        t.bitmap.p, t.pidx.p, t.prim_indices.p,
+                                                                        t.p0.p, t.p1.p, t.p2.p, off, t.ttri.p);
         KDGB_LAUNCH_CHECK();
     }
     return KDGB_OK;
