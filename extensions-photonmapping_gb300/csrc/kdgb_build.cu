@@ -100,10 +100,13 @@ struct BuildArgs {
     int2 *ch;
     float *area;
     int32_t *prim_indices, *leaf_ids;
-    float4 *pmin, *pmax;
     unsigned *keys;
-    int32_t *cnt, *ess_cnt, *lbase, *chunksum, *tilesum, *tileoff, *big;
-    int8_t *planes;
+    int32_t *cnt, *lbase, *chunksum, *tilesum, *tileoff, *big;
+    // Empty-space planes and node counts of a level, in buffer (level & 1)
+    // (st->level counts the completed levels): k_children writes the next
+    // level's while it reads the current one's.
+    int32_t *ess_cnt[2];
+    int8_t *planes[2];
     int2 *ranges;
     int32_t *roff;
     float *areas;
@@ -219,8 +222,6 @@ __global__ void k_begin(const BuildArgs a)
         a.pidx[m] = b0;
         a.amt[m] = b1 - b0;
         a.parent[m] = m;
-        a.pmin[m] = make_float4(0.f, 0.f, 0.f, 0.f);
-        a.pmax[m] = make_float4(0.f, 0.f, 0.f, 0.f);
         unsigned *kk = a.keys + 6 * (int64_t)m;
         kk[0] = kk[1] = kk[2] = lo;
         kk[3] = kk[4] = kk[5] = hi;
@@ -352,48 +353,60 @@ __global__ void __launch_bounds__(kBlock) k_reduce(const BuildArgs a)
     }
 }
 
-// Writes the tight boxes, the empty-space planes (CalcEmptySpaceSplits,
-// EmptySpaceSplitting.h:10-70) and the spatial-median split of the longest
-// axis (CalcUpperNodeSplitInfo, ReduceSegments.h:466-484).
+// One active node's tight box (from its keys), empty-space planes against
+// its propagated box [lo, hi] (CalcEmptySpaceSplits,
+// EmptySpaceSplitting.h:10-70) and spatial-median split of the longest axis
+// (CalcUpperNodeSplitInfo, ReduceSegments.h:466-484); nodes of a binned-SAH
+// level with at least kSahBlockRefs references are listed for block-wide
+// binning.  k is the node's index in its level, node its id.
+__device__ __forceinline__ void node_split_one(const BuildArgs &a, int32_t k, int32_t node, bool ess, float4 lo,
+                                               float4 hi, bool sah, int8_t *planes, int32_t *ess_cnt)
+{
+    const float thr = a.thr;
+    const unsigned *kk = a.keys + 6 * (int64_t)k;
+    const float3 mn = make_float3(funkey(kk[0]), funkey(kk[1]), funkey(kk[2]));
+    const float3 mx = make_float3(funkey(kk[3]), funkey(kk[4]), funkey(kk[5]));
+    a.bmin[node] = make_float4(mn.x, mn.y, mn.z, 0.0f);
+    a.bmax[node] = make_float4(mx.x, mx.y, mx.z, 0.0f);
+    if (ess) {
+        int pl = 0, nr = 0;
+        if (__fsub_rn(mn.x, lo.x) > __fmul_rn(thr, __fsub_rn(hi.x, lo.x))) { pl |= 1; nr += 2; }
+        if (__fsub_rn(mn.y, lo.y) > __fmul_rn(thr, __fsub_rn(hi.y, lo.y))) { pl |= 2; nr += 2; }
+        if (__fsub_rn(mn.z, lo.z) > __fmul_rn(thr, __fsub_rn(hi.z, lo.z))) { pl |= 4; nr += 2; }
+        if (__fsub_rn(hi.x, mx.x) > __fmul_rn(thr, __fsub_rn(hi.x, lo.x))) { pl |= 8; nr += 2; }
+        if (__fsub_rn(hi.y, mx.y) > __fmul_rn(thr, __fsub_rn(hi.y, lo.y))) { pl |= 16; nr += 2; }
+        if (__fsub_rn(hi.z, mx.z) > __fmul_rn(thr, __fsub_rn(hi.z, lo.z))) { pl |= 32; nr += 2; }
+        planes[k] = (int8_t)pl;
+        ess_cnt[k] = nr;
+    } else {
+        ess_cnt[k] = 0;
+    }
+    const float sx = __fsub_rn(mx.x, mn.x), sy = __fsub_rn(mx.y, mn.y), sz = __fsub_rn(mx.z, mn.z);
+    const float mdx = __fadd_rn(__fmul_rn(sx, 0.5f), mn.x);
+    const float mdy = __fadd_rn(__fmul_rn(sy, 0.5f), mn.y);
+    const float mdz = __fadd_rn(__fmul_rn(sz, 0.5f), mn.z);
+    const bool y_above_x = sx < sy;
+    const float mxs = y_above_x ? sy : sx;
+    const float sp = y_above_x ? mdy : mdx;
+    const int8_t ax = y_above_x ? KDGB_Y : KDGB_X;
+    const bool z_higher = mxs < sz;
+    a.split[node] = z_higher ? mdz : sp;
+    a.info[node] = z_higher ? (int8_t)KDGB_Z : ax;
+    if (sah && a.amt[node] >= kSahBlockRefs) a.big[atomicAdd(&a.st->n_big, 1)] = k;
+}
+
+// The roots' splits (the first level; no empty-space cuts at the root).
+// Later levels get theirs from k_children of the level before.
 __global__ void k_node_split(const BuildArgs a)
 {
     const BuildState *st = a.st;
     const int32_t R = st->R, active = st->active;
     const bool ess = do_ess(a, st), sah = sah_level(a, st);
-    const float thr = a.thr;
+    const int b = st->level & 1;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     GRID_STRIDE(k64, R) {
         const int32_t k = (int32_t)k64;
-        const unsigned *kk = a.keys + 6 * (int64_t)k;
-        const float3 mn = make_float3(funkey(kk[0]), funkey(kk[1]), funkey(kk[2]));
-        const float3 mx = make_float3(funkey(kk[3]), funkey(kk[4]), funkey(kk[5]));
-        a.bmin[active + k] = make_float4(mn.x, mn.y, mn.z, 0.0f);
-        a.bmax[active + k] = make_float4(mx.x, mx.y, mx.z, 0.0f);
-        if (ess) {
-            const float4 lo = a.pmin[k], hi = a.pmax[k];
-            int pl = 0, nr = 0;
-            if (__fsub_rn(mn.x, lo.x) > __fmul_rn(thr, __fsub_rn(hi.x, lo.x))) { pl |= 1; nr += 2; }
-            if (__fsub_rn(mn.y, lo.y) > __fmul_rn(thr, __fsub_rn(hi.y, lo.y))) { pl |= 2; nr += 2; }
-            if (__fsub_rn(mn.z, lo.z) > __fmul_rn(thr, __fsub_rn(hi.z, lo.z))) { pl |= 4; nr += 2; }
-            if (__fsub_rn(hi.x, mx.x) > __fmul_rn(thr, __fsub_rn(hi.x, lo.x))) { pl |= 8; nr += 2; }
-            if (__fsub_rn(hi.y, mx.y) > __fmul_rn(thr, __fsub_rn(hi.y, lo.y))) { pl |= 16; nr += 2; }
-            if (__fsub_rn(hi.z, mx.z) > __fmul_rn(thr, __fsub_rn(hi.z, lo.z))) { pl |= 32; nr += 2; }
-            a.planes[k] = (int8_t)pl;
-            a.ess_cnt[k] = nr;
-        } else {
-            a.ess_cnt[k] = 0;
-        }
-        const float sx = __fsub_rn(mx.x, mn.x), sy = __fsub_rn(mx.y, mn.y), sz = __fsub_rn(mx.z, mn.z);
-        const float mdx = __fadd_rn(__fmul_rn(sx, 0.5f), mn.x);
-        const float mdy = __fadd_rn(__fmul_rn(sy, 0.5f), mn.y);
-        const float mdz = __fadd_rn(__fmul_rn(sz, 0.5f), mn.z);
-        const bool y_above_x = sx < sy;
-        const float mxs = y_above_x ? sy : sx;
-        const float sp = y_above_x ? mdy : mdx;
-        const int8_t ax = y_above_x ? KDGB_Y : KDGB_X;
-        const bool z_higher = mxs < sz;
-        a.split[active + k] = z_higher ? mdz : sp;
-        a.info[active + k] = z_higher ? (int8_t)KDGB_Z : ax;
-        if (sah && a.amt[active + k] >= kSahBlockRefs) a.big[atomicAdd(&a.st->n_big, 1)] = k;
+        node_split_one(a, k, active + k, ess, zero, zero, sah, a.planes[b], a.ess_cnt[b]);
     }
 }
 
@@ -470,8 +483,9 @@ __device__ __forceinline__ void divide_flags(const BuildArgs &a, int32_t prim, i
 // totals (the tile totals are scanned into tile offsets; k_scatter adds the
 // chunk totals of the earlier warps of its tile).  Also resets the tight-box
 // keys of the next level's nodes (at most 2R of them) to the +-fInfinity box
-// (AabbMemset, ReduceSegments.h:328-335): k_node_split has consumed this
-// level's keys and k_scatter reduces the children's boxes into them.
+// (AabbMemset, ReduceSegments.h:328-335): this level's keys were consumed
+// when its splits were made, and k_scatter reduces the children's boxes into
+// them.
 template <bool DIVIDE>
 __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_count(const BuildArgs a)
 {
@@ -479,6 +493,12 @@ __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_count(const BuildArg
         const int64_t next = min(2 * (int64_t)a.st->R, a.cap.R);
         const unsigned lo_key = fkey(KDGB_FINF), hi_key = fkey(-KDGB_FINF);
         GRID_STRIDE(i, 6 * next) a.keys[i] = (i % 6) < 3 ? lo_key : hi_key;
+        // This level's list of large nodes has been binned; k_children lists
+        // the next level's.
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.st->n_big = 0;
+            a.st->big_next = 0;
+        }
     }
     __shared__ int s_owner[kWarps], s_l[kWarps], s_r[kWarps], s_tl[kWarps], s_tr[kWarps];
     const BuildState *st = a.st;
@@ -711,7 +731,7 @@ __device__ __forceinline__ SahNode sah_node(const BuildArgs &a, int32_t node)
 }
 
 // Binned SAH of the active nodes, one launch per tuned level.  First the
-// nodes of kSahBlockRefs references or more (listed by k_node_split), one
+// nodes of kSahBlockRefs references or more (listed with the splits), one
 // block each, taken from a work counter: every warp bins an interleaved
 // share of the rows into its own histograms, which are then summed.  Then
 // the smaller nodes, one warp each.
@@ -1102,8 +1122,6 @@ __device__ void advance_upper(const BuildArgs &a, BuildState *st)
         st->active = st->n_nodes - created;
         st->R = created;
         st->level += 1;
-        st->n_big = 0;
-        st->big_next = 0;
         if (created > 0 && st->level >= a.max_levels) { set_err(st, KDGB_ERR_DEGENERATE, kErrMaxLevels); break; }
         more = created > 0;
     } while (0);
@@ -1115,11 +1133,11 @@ __device__ void advance_upper(const BuildArgs &a, BuildState *st)
 // offsets) and, with empty-space splitting on, PropagateAabbToChildren
 // (EmptySpaceSplitting.h:299-331; TriangleMapUpperCreator.cu:731-733 runs
 // it whenever empty-space splitting is on, whatever propagateAabbs says).
-// Non-leaf children are the next level's active nodes: their counts and
-// propagated boxes are reset here (their tight-box keys were reset by
-// k_count and filled by k_scatter), so the next level needs no separate
-// init launch.  The block that finishes last closes the level
-// (advance_upper).
+// Non-leaf children are the next level's active nodes: their counts are
+// reset and their splits made here (node_split_one against the propagated
+// box; their tight-box keys were reset by k_count and filled by k_scatter),
+// so the next level starts with its counting pass.  The block that finishes
+// last closes the level (advance_upper).
 __global__ void k_children(const BuildArgs a)
 {
     BuildState *st = a.st;
@@ -1128,6 +1146,13 @@ __global__ void k_children(const BuildArgs a)
     const int32_t R = fits ? st->R : 0, active = st->active, base = st->n_nodes, upper = (int32_t)st->F;
     const int32_t LS = a.LS;
     const bool ess = do_ess(a, st);
+    // The next level: never the root level, a binned-SAH level once
+    // upper_levels are done.
+    const bool sah_next = a.tuned && st->level + 2 > a.upper_levels;
+    const int cur = st->level & 1;
+    const int8_t *planes = a.planes[cur];
+    int8_t *planes_next = a.planes[cur ^ 1];
+    int32_t *ess_next = a.ess_cnt[cur ^ 1];
     const int32_t empty = tot[6];
     const int32_t child_start = base + empty;
     const int32_t total_l = tot[0], leaf_l = tot[2], ln_l = tot[4], leaf_nodes = tot[4] + tot[5];
@@ -1136,7 +1161,7 @@ __global__ void k_children(const BuildArgs a)
         const int32_t *lb = a.lbase + kLanes * (int64_t)k;
         const int32_t *nb = a.lbase + kLanes * (int64_t)(k + 1);
         if (ess) {
-            const int pl = a.planes[k];
+            const int pl = planes[k];
             if (pl) ess_chain(a, k, active, base + lb[6], pl);
         }
         const int32_t l = nb[0] - lb[0], r = nb[1] - lb[1];
@@ -1177,14 +1202,12 @@ __global__ void k_children(const BuildArgs a)
         if (!lleaf) {
             a.cnt[2 * lnext] = 0;
             a.cnt[2 * lnext + 1] = 0;
-            a.pmin[lnext] = lmin;
-            a.pmax[lnext] = lmax;
+            node_split_one(a, lnext, lid, a.ess, lmin, lmax, sah_next, planes_next, ess_next);
         }
         if (!rleaf) {
             a.cnt[2 * rnext] = 0;
             a.cnt[2 * rnext + 1] = 0;
-            a.pmin[rnext] = rmin;
-            a.pmax[rnext] = rmax;
+            node_split_one(a, rnext, rid, a.ess, rmin, rmax, sah_next, planes_next, ess_next);
         }
     }
     if (last_block(st)) advance_upper(a, st);
@@ -1783,15 +1806,16 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.cap.nodes = t.info.cap;
     a.prim_indices = t.prim_indices.p;
     a.leaf_ids = t.leaf_ids.p;
-    a.pmin = w.pmin.p;
-    a.pmax = w.pmax.p;
     a.keys = w.keys.p;
     a.cnt = w.cnt.p;
-    a.ess_cnt = w.ess.p;
     a.lbase = w.lbase.p;
-    a.planes = w.planes.p;
-    // Next-level node entries are written by k_children into these four.
-    a.cap.R = std::min({w.pmin.cap, w.pmax.cap, w.keys.cap / 6, w.cnt.cap / 2});
+    for (int b = 0; b < 2; ++b) {
+        a.ess_cnt[b] = w.ess[b].p;
+        a.planes[b] = w.planes[b].p;
+    }
+    // Next-level node entries are written by k_children into these.
+    a.cap.R = std::min({w.keys.cap / 6, w.cnt.cap / 2, w.ess[0].cap, w.ess[1].cap, w.planes[0].cap,
+                        w.planes[1].cap});
     a.chunksum = w.chunksum.p;
     a.tilesum = w.tilesum.p;
     a.tileoff = w.tileoff.p;
@@ -1828,6 +1852,9 @@ int emit_begin(const BuildArgs &a, const Launcher &L, const float *tri_v_dev, cu
         k_reduce<<<L.grid(a.T, kTileRefs), kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
+    // The roots' splits; later levels get theirs from k_children.
+    k_node_split<<<L.grid(a.M, kBlock), kBlock, 0, s>>>(a);
+    KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
 
@@ -1836,8 +1863,6 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
 {
     const unsigned gN = L.grid(e.N, kTileRefs);
     const unsigned gR = L.grid(e.R, kBlock, 2);
-    k_node_split<<<gR, kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
     if (tuned_levels) {
         // Enough blocks for one per large node and one warp per node.
         const int64_t big = std::min<int64_t>(e.R, ceil_div(e.N, kSahBlockRefs));
@@ -1850,7 +1875,7 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
         KDGB_LAUNCH_CHECK();
     }
     // Tile offsets and node bases: independent scans, one launch.
-    const NodeLanes lanes{a.cnt, a.ess_cnt, a.LS};
+    const NodeLanes lanes{a.cnt, {a.ess_cnt[0], a.ess_cnt[1]}, &a.st->level, a.LS};
     KDGB_CHECK((scan_exclusive_pair<2, ScanArray<2>, kLanes, NodeLanes>(
         ScanArray<2>{a.tilesum}, a.tileoff, ceil_div(e.N, kTileRefs), &a.st->ntiles, lanes, a.lbase, e.R, &a.st->R, s,
         &w.scan, &a.st->err)));
@@ -1992,7 +2017,7 @@ void graph_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, const
                                          (w.tileoff.cap / 2 - 1) * kTileRefs});
     a.cap.refs[0] = std::min(a.cap.refs[0], chunk_refs);
     a.cap.refs[1] = std::min(a.cap.refs[1], chunk_refs);
-    a.cap.R = std::min({a.cap.R, w.ess.cap, w.lbase.cap / kLanes - 1, w.planes.cap});
+    a.cap.R = std::min(a.cap.R, w.lbase.cap / kLanes - 1);
     a.cap.leaves = t.leaf_ids.cap;
     a.cap.low_R = std::min({w.ssplit.cap, w.saddr.cap - 1, w.careas.cap, w.csets.cap});
     a.cap.fin = std::min({a.cap.fin, t.prim_indices.cap, w.areas.cap, w.sts.cap / 3});
@@ -2020,8 +2045,9 @@ uint64_t layout_signature(const Tree &t)
     MIX(t.p0); MIX(t.p1); MIX(t.p2); MIX(t.info); MIX(t.split); MIX(t.bmin); MIX(t.bmax); MIX(t.pidx);
     MIX(t.bitmap); MIX(t.parent); MIX(t.children); MIX(t.area); MIX(t.prim_indices); MIX(t.leaf_ids);
     MIX(t.tnode); MIX(t.ttri); MIX(t.mesh_off);
-    MIX(w.rmin[0]); MIX(w.rmin[1]); MIX(w.rmax[0]); MIX(w.rmax[1]); MIX(w.fmin); MIX(w.fmax); MIX(w.pmin);
-    MIX(w.pmax); MIX(w.keys); MIX(w.planes); MIX(w.cnt); MIX(w.ess); MIX(w.lbase); MIX(w.chunksum);
+    MIX(w.rmin[0]); MIX(w.rmin[1]); MIX(w.rmax[0]); MIX(w.rmax[1]); MIX(w.fmin); MIX(w.fmax);
+    MIX(w.keys); MIX(w.planes[0]); MIX(w.planes[1]); MIX(w.cnt); MIX(w.ess[0]); MIX(w.ess[1]); MIX(w.lbase);
+    MIX(w.chunksum);
     MIX(w.tilesum); MIX(w.tileoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.big); MIX(w.areas); MIX(w.sts);
     MIX(w.ssplit); MIX(w.saddr); MIX(w.roff); MIX(w.careas); MIX(w.csets); MIX(w.ranges); MIX(w.state);
 #undef MIX
@@ -2100,8 +2126,9 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
     KDGB_CHECK(grab(w.rmin[0], T, s));
     KDGB_CHECK(grab(w.rmax[0], T, s));
     KDGB_CHECK(grow_nodes(t, M, 0, s));
-    KDGB_CHECK(reserve_keep(w.pmin, M, 0, s));
-    KDGB_CHECK(reserve_keep(w.pmax, M, 0, s));
+    KDGB_CHECK(grab(w.planes[0], M, s));
+    KDGB_CHECK(grab(w.ess[0], M, s));
+    KDGB_CHECK(grab(w.big, M + 1, s));
     KDGB_CHECK(reserve_keep(w.keys, 6 * (int64_t)M, 0, s));
     KDGB_CHECK(reserve_keep(w.cnt, 2 * (int64_t)M, 0, s));
     KDGB_CHECK(grab(w.ranges, (int64_t)p.max_levels + 1, s));
@@ -2132,17 +2159,24 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
             KDGB_CHECK(ensure(w.fmin, want, s, F));
             KDGB_CHECK(ensure(w.fmax, want, s, F));
         }
-        KDGB_CHECK(reserve_keep(w.pmin, 2 * R, R, s));
-        KDGB_CHECK(reserve_keep(w.pmax, 2 * R, R, s));
         KDGB_CHECK(reserve_keep(w.keys, 12 * R, 6 * R, s));
         KDGB_CHECK(reserve_keep(w.cnt, 4 * R, 2 * R, s));
-        KDGB_CHECK(grab(w.ess, R, s));
+        // This level's planes and counts are in [cur] (kept); k_children
+        // writes the next level's (<= 2R) into [nxt].  Both hold 2R, the
+        // capacity the level checks its children against.
+        const int cur = st.level & 1;
+        KDGB_CHECK(reserve_keep(w.ess[cur], 2 * R, R, s));
+        KDGB_CHECK(reserve_keep(w.planes[cur], 2 * R, R, s));
+        KDGB_CHECK(grab(w.ess[nxt], 2 * R, s));
+        KDGB_CHECK(grab(w.planes[nxt], 2 * R, s));
         KDGB_CHECK(grab(w.lbase, kLanes * (R + 1), s));
-        KDGB_CHECK(grab(w.planes, R, s));
         KDGB_CHECK(grab(w.chunksum, 2 * chunks_for(N), s));
         KDGB_CHECK(grab(w.tilesum, 2 * ceil_div(N, kTileRefs), s));
         KDGB_CHECK(grab(w.tileoff, 2 * (ceil_div(N, kTileRefs) + 1), s));
-        KDGB_CHECK(grab(w.big, std::min<int64_t>(R, N / kSahBlockRefs) + 1, s));
+        // This level's large-node list is kept; the next level's is listed
+        // by k_children.
+        KDGB_CHECK(reserve_keep(w.big, std::min<int64_t>(2 * R, 2 * N / kSahBlockRefs) + 1,
+                                std::min<int64_t>(R, N / kSahBlockRefs) + 1, s));
         const Extents e{N, R, F, n_nodes, 0, 0};
         KDGB_CHECK(emit_upper_level(make_args(t, p, T, M, mesh_off_dev), L, e, tuned_level, w, s));
         KDGB_CHECK(fetch_state(t, st, s));
@@ -2224,13 +2258,13 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.fmin, fin, s));
     KDGB_CHECK(ensure(w.fmax, fin, s));
     KDGB_CHECK(grow_nodes(t, nodes, 0, s));
-    KDGB_CHECK(ensure(w.pmin, R, s));
-    KDGB_CHECK(ensure(w.pmax, R, s));
     KDGB_CHECK(ensure(w.keys, 6 * R, s));
     KDGB_CHECK(ensure(w.cnt, 2 * R, s));
-    KDGB_CHECK(ensure(w.ess, R, s));
+    for (int b = 0; b < 2; ++b) {
+        KDGB_CHECK(ensure(w.ess[b], R, s));
+        KDGB_CHECK(ensure(w.planes[b], R, s));
+    }
     KDGB_CHECK(ensure(w.lbase, kLanes * (R + 1), s));
-    KDGB_CHECK(ensure(w.planes, R, s));
     KDGB_CHECK(ensure(w.chunksum, 2 * chunks_for(refs), s));
     KDGB_CHECK(ensure(w.tilesum, 2 * ceil_div(refs, kTileRefs), s));
     KDGB_CHECK(ensure(w.tileoff, 2 * (ceil_div(refs, kTileRefs) + 1), s));

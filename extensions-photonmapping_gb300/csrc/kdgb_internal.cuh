@@ -110,10 +110,11 @@ struct GraphKernels {
 // steady state issues no device allocations.  References ping-pong between
 // rmin/rmax[0] and [1] by level parity.
 struct Workspace {
-    DevArray<float4> rmin[2], rmax[2], fmin, fmax, pmin, pmax;
+    DevArray<float4> rmin[2], rmax[2], fmin, fmax;
     DevArray<unsigned> keys;
-    DevArray<int8_t> planes;
-    DevArray<int32_t> cnt, ess, lbase, chunksum, tilesum, tileoff, stats, scan, misc0, misc1, big;
+    DevArray<int8_t> planes[2];  // empty-space planes of a level, by level parity
+    DevArray<int32_t> ess[2];    // empty-space node counts of a level, by level parity
+    DevArray<int32_t> cnt, lbase, chunksum, tilesum, tileoff, stats, scan, misc0, misc1, big;
     DevArray<float> areas;
     DevArray<int4> sts;
     DevArray<int32_t> ssplit, saddr, roff;
@@ -216,15 +217,16 @@ struct ScanArray {
 // nodes (CalcNodeChildSize, SetPrimitiveLeafSide, MarkNodeLeafs:
 // TriangleUpperChildren.h:144-201).
 struct NodeLanes {
-    const int32_t *cnt;  // 2 per node
-    const int32_t *ess;  // 1 per node
-    int32_t LS;          // leaf threshold
+    const int32_t *cnt;     // 2 per node
+    const int32_t *ess[2];  // 1 per node, in ess[*level & 1]
+    const int32_t *level;   // completed upper levels (device)
+    int32_t LS;             // leaf threshold
 #ifdef __CUDACC__
     __device__ __forceinline__ void load(int64_t k, int32_t (&v)[7]) const
     {
         const int32_t l = cnt[2 * k], r = cnt[2 * k + 1];
         const int ll = l < LS, rl = r < LS;
-        v[0] = l; v[1] = r; v[2] = ll ? l : 0; v[3] = rl ? r : 0; v[4] = ll; v[5] = rl; v[6] = ess[k];
+        v[0] = l; v[1] = r; v[2] = ll ? l : 0; v[3] = rl ? r : 0; v[4] = ll; v[5] = rl; v[6] = ess[*level & 1][k];
     }
 #endif
 };
