@@ -372,12 +372,26 @@ def run_frame(args, world, rank, local, pg):
         h_o = torch.from_numpy(o).pin_memory()
         h_d = torch.from_numpy(d).pin_memory()
         h_out = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in outs]
+        # The rays are not needed until the trace: they are uploaded on a
+        # second stream while the tree is rebuilt (after the previous step's
+        # trace has read them).  Every step still copies all its inputs and
+        # reads back all its outputs inside the timed region.
+        side = torch.cuda.Stream(device=dev)
+        traced = torch.cuda.Event()
+        traced.record(stream)
 
         def e2e_step():
+            side.wait_event(traced)
+            with torch.cuda.stream(side):
+                o_d.copy_(h_o, non_blocking=True)
+                d_d.copy_(h_d, non_blocking=True)
+            rays_in = torch.cuda.Event()
+            rays_in.record(side)
             tris_d.copy_(h_tris, non_blocking=True)
-            o_d.copy_(h_o, non_blocking=True)
-            d_d.copy_(h_d, non_blocking=True)
-            step()
+            build()
+            stream.wait_event(rays_in)
+            tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
+            traced.record(stream)
             for hb, db in zip(h_out, outs):
                 hb.copy_(db, non_blocking=True)
 
