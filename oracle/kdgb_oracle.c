@@ -1,9 +1,11 @@
 /*
  * kdgb_oracle.c -- CPU restatement of the reference kd-tree build and ray
  * traversal.  TEST INFRASTRUCTURE: the checker for the CUDA library and the
- * timed CPU baseline; never linked into the product.  Parity unpinned (the
- * reference does not compile here and ships no golden vectors); every
- * function cites the reference lines it restates.
+ * timed CPU baseline; never linked into the product.  The intersection
+ * primitives are pinned bit for bit to the reference's own header-only code
+ * (oracle/refpin); the build and the traversal loops are parity unpinned
+ * (the reference's build does not compile here and it ships no golden
+ * vectors).  Every function cites the reference lines it restates.
  *
  * Build: gcc -O3 -ffp-contract=off -fopenmp -fPIC -shared (see Makefile).
  * -ffp-contract=off keeps every multiply and add separately rounded, the
@@ -1696,4 +1698,43 @@ void or_tree_free(or_tree *t)
     free(t->bitmap); free(t->children); free(t->area); free(t->parent); free(t->prim_indices);
     free(t->leaf_ids); free(t->prim_min); free(t->prim_max);
     memset(t, 0, sizeof(*t));
+}
+
+/* ------------------------------------------------------------------------ */
+/* Single-primitive entry points for the pin test against the reference's    */
+/* own header-only code (oracle/refpin, tests/test_refpin.py).               */
+/* ------------------------------------------------------------------------ */
+
+void or_pin_adjust_dir(float d[3])
+{
+    const v3 a = adjust_dir(ld3(d));
+    d[0] = a.x; d[1] = a.y; d[2] = a.z;
+}
+
+int or_pin_ray_box(const float o[3], const float inv[3], const float bmin[3], const float bmax[3])
+{
+    return ray_box(ld3(o), ld3(inv), bmin, bmax);
+}
+
+void or_pin_woop_rows(const float tri[9], float m[12])
+{
+    f4 r[3];
+    woop_rows(tri, 0, r);
+    for (int i = 0; i < 3; ++i) {
+        m[4 * i] = r[i].x; m[4 * i + 1] = r[i].y; m[4 * i + 2] = r[i].z; m[4 * i + 3] = r[i].w;
+    }
+}
+
+int or_pin_woop(const float tri[9], const float o[3], const float d[3], float t_max, float out[3])
+{
+    float th[3] = {t_max, 0.0f, 0.0f};
+    int hit = -1;
+    woop_test(tri, 0, ld3(o), ld3(d), OR_TIE_REF_LAST, &hit, th);
+    out[0] = th[0]; out[1] = th[1]; out[2] = th[2];
+    return hit == 0;
+}
+
+int or_pin_tri_box(const float tri[9], const float bmin[3], const float bmax[3])
+{
+    return tri_box_step3(ld3(tri), ld3(tri + 3), ld3(tri + 6), ld3(bmin), ld3(bmax));
 }

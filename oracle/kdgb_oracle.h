@@ -7,12 +7,17 @@
  * links, loads or calls it; the product fails loudly when its CUDA
  * extension is missing instead of falling back here.
  *
- * Parity status: the reference cannot be compiled here (it needs OpenEngine
- * core, extensions-CUDA, CUDPP and cutil, none of which are present) and it
- * ships no tests, golden vectors or fixtures, so this restatement is
- * "parity unpinned" against the reference's own outputs.  It follows the
- * reference source line by line (citations on each function) with one
- * documented evaluation order for the un-vendored float3 helpers:
+ * Parity status: the reference's build and tracers cannot be compiled here
+ * (they need OpenEngine core, extensions-CUDA, CUDPP and cutil, none of which
+ * are present) and it ships no tests, golden vectors or fixtures.  Its
+ * header-only intersection primitives do compile unmodified (oracle/refpin,
+ * host stand-ins for CUDA): Moeller-Trumbore, Woop (rows and test),
+ * AdjustRayDirection, RayBoxIntersection and TriangleAabbIntersectionStep3
+ * of this restatement are pinned to them bit for bit (or_pin_*, tested in
+ * tests/test_refpin.py).  The build and the traversal loops are "parity
+ * unpinned".  The restatement follows the reference source line by line
+ * (citations on each function) with one documented evaluation order for the
+ * un-vendored float3 helpers:
  *   dot(a,b)   = (a.x*b.x + a.y*b.y) + a.z*b.z
  *   cross(a,b) = (a.y*b.z - a.z*b.y, a.z*b.x - a.x*b.z, a.x*b.y - a.y*b.x)
  * every multiply and add rounded separately (no FMA contraction), IEEE
@@ -162,6 +167,17 @@ float or_kpow(float x, float y);
 
 /* Philox4x32-10 block (exported for tests). */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Single primitives for the pin test against the reference's own header-only
+ * code: AdjustRayDirection, RayBoxIntersection<true>, WoopTransformationMatrix
+ * of (p1, p2, p0), Woop (REF_LAST acceptance) and
+ * TriangleAabbIntersectionStep3, restated as the traversal and the build use
+ * them. */
+void or_pin_adjust_dir(float d[3]);
+int or_pin_ray_box(const float o[3], const float inv[3], const float bmin[3], const float bmax[3]);
+void or_pin_woop_rows(const float tri[9], float m[12]);
+int or_pin_woop(const float tri[9], const float o[3], const float d[3], float t_max, float out[3]);
+int or_pin_tri_box(const float tri[9], const float bmin[3], const float bmax[3]);
 
 /* Moeller-Trumbore restated (IRayTracer.h:111-145); exported for unit tests. */
 int or_moeller_trumbore(const float v0[3], const float v1[3], const float v2[3],

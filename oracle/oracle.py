@@ -3,8 +3,10 @@
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
 cpu_baseline / --impl reference legs of bench.py as the checker and the
 timed CPU baseline.  The product library never imports this module.
-The restatement is "parity unpinned": the reference cannot be compiled here
-and ships no golden vectors (see kdgb_oracle.h).
+Its intersection primitives are pinned bit for bit to the reference's own
+header-only code (refpin_lib, tests/test_refpin.py); the build and traversal
+loops are "parity unpinned": the reference's build cannot be compiled here and
+it ships no golden vectors (see kdgb_oracle.h).
 """
 from __future__ import annotations
 
@@ -317,3 +319,57 @@ def moeller_trumbore(v0, v1, v2, o, d, t_max=float(FINF)):
     out = np.zeros(3, np.float32)
     hit = lib().or_moeller_trumbore(*[_ptr(a) for a in arrs], t_max, _ptr(out))
     return bool(hit), out
+
+
+# ---------------------------------------------------------------------------
+# Pin test: the oracle's single primitives and the reference's own
+# header-only code compiled unmodified (oracle/refpin -> oracle/_ref).
+# ---------------------------------------------------------------------------
+_REFPIN_DIR = os.path.join(_HERE, "refpin")
+_REFPIN_LIB = os.path.join(_HERE, "_ref", "librefpin.so")
+_refpin = None
+
+
+def refpin_lib():
+    """Loads oracle/_ref/librefpin.so, building it with the committed recipe
+    first.  Returns None where the reference tree is not available (the
+    recipe then fails), so callers can skip."""
+    global _refpin
+    if _refpin is not None:
+        return _refpin
+    r = subprocess.run(["make", "-s", "-C", _REFPIN_DIR], capture_output=True, text=True)
+    if r.returncode != 0 or not os.path.exists(_REFPIN_LIB):
+        return None
+    L = C.CDLL(_REFPIN_LIB)
+    F = C.POINTER(C.c_float)
+    L.ref_moeller_trumbore.argtypes = [F, F, F, C.c_float, F]
+    L.ref_moeller_trumbore.restype = C.c_int
+    L.ref_adjust_dir.argtypes = [F]
+    L.ref_adjust_dir.restype = None
+    L.ref_ray_box.argtypes = [F, F, F, F]
+    L.ref_ray_box.restype = C.c_int
+    L.ref_woop_rows.argtypes = [F, F]
+    L.ref_woop_rows.restype = None
+    L.ref_woop.argtypes = [F, F, F, C.c_float, F]
+    L.ref_woop.restype = C.c_int
+    L.ref_tri_box_step3.argtypes = [F, F, F]
+    L.ref_tri_box_step3.restype = C.c_int
+    _refpin = L
+    return L
+
+
+def pin_functions():
+    """The oracle's counterparts of the reference's pinned primitives."""
+    L = lib()
+    F = C.POINTER(C.c_float)
+    L.or_pin_adjust_dir.argtypes = [F]
+    L.or_pin_adjust_dir.restype = None
+    L.or_pin_ray_box.argtypes = [F, F, F, F]
+    L.or_pin_ray_box.restype = C.c_int
+    L.or_pin_woop_rows.argtypes = [F, F]
+    L.or_pin_woop_rows.restype = None
+    L.or_pin_woop.argtypes = [F, F, F, C.c_float, F]
+    L.or_pin_woop.restype = C.c_int
+    L.or_pin_tri_box.argtypes = [F, F, F]
+    L.or_pin_tri_box.restype = C.c_int
+    return L

@@ -1,0 +1,144 @@
+"""The oracle's intersection primitives, checked bit for bit against the
+reference's OWN header-only code.
+
+`oracle/refpin/Makefile` compiles the reference's unmodified source with g++:
+Utils/CUDA/IRayTracer.h (AdjustRayDirection, Woop, MoellerTrumbore,
+RayBoxIntersection), Utils/CUDA/IntersectionTests.h (WoopTransformationMatrix,
+TriangleAabbIntersectionStep3), Utils/CUDA/Utils.h and Scene/KDNode.h. Host
+stand-ins for the CUDA types and the un-vendored vector helpers come from
+`oracle/refpin/include`. This pins the arithmetic of those primitives, as the
+oracle restates it, to the reference's source. The vector helpers themselves
+are not vendored by the reference; both sides use the documented evaluation
+order.
+
+The library is built into oracle/_ref where the reference tree is available.
+Elsewhere these tests skip.
+"""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def pins(oracle):
+    ref = oracle.refpin_lib()
+    if ref is None:
+        pytest.skip("the reference tree is not available to compile the pin library")
+    return ref, oracle.pin_functions()
+
+
+def f32p(a):
+    import ctypes as C
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def bits(a):
+    return np.asarray(a, np.float32).view(np.uint32)
+
+
+def hit_rays(rng, n, spread):
+    """Triangles of varied size and shape, and rays aimed at points in and around
+    them: inside, on edges and vertices, just outside, and from behind."""
+    tri = rng.normal(size=(n, 9)).astype(np.float32) * rng.choice([1e-3, 0.1, 1.0, 10.0], size=(n, 1)).astype(np.float32)
+    tri += rng.uniform(-5, 5, size=(n, 1)).astype(np.float32)
+    w = rng.uniform(-spread, 1 + spread, size=(n, 3)).astype(np.float32)
+    w[::7, 0] = 0.0                      # on an edge (barycentric 0)
+    w[::11] = np.array([1, 0, 0], np.float32)  # on a vertex
+    w /= np.where(np.abs(w.sum(1, keepdims=True)) < 1e-3, 1.0, w.sum(1, keepdims=True))
+    target = w[:, :1] * tri[:, 0:3] + w[:, 1:2] * tri[:, 3:6] + w[:, 2:3] * tri[:, 6:9]
+    o = (target + rng.normal(size=(n, 3)) * rng.uniform(0.1, 20, size=(n, 1))).astype(np.float32)
+    d = (target - o).astype(np.float32)
+    d[::5] *= rng.uniform(0.01, 100, size=(len(d[::5]), 1)).astype(np.float32)
+    d[::13, 1] = 0.0                     # axis-parallel components
+    return tri, o, d
+
+
+def test_moeller_trumbore_pinned(oracle, pins):
+    ref, _ = pins
+    rng = np.random.default_rng(101)
+    tri, o, d = hit_rays(rng, 20000, 0.05)
+    hits = 0
+    for i in range(tri.shape[0]):
+        t_max = np.float32(oracle.FINF) if i % 3 else np.float32(rng.uniform(0.5, 1.5))
+        out_r = np.zeros(3, np.float32)
+        h_r = ref.ref_moeller_trumbore(f32p(tri[i]), f32p(o[i]), f32p(d[i]), t_max, f32p(out_r))
+        h_o, out_o = oracle.moeller_trumbore(tri[i, 0:3], tri[i, 3:6], tri[i, 6:9], o[i], d[i], t_max)
+        assert bool(h_r) == h_o, i
+        assert np.array_equal(bits(out_r), bits(out_o)), i
+        hits += h_o
+    assert 0.3 * tri.shape[0] < hits < tri.shape[0]
+
+
+def test_woop_pinned(oracle, pins):
+    ref, ours = pins
+    rng = np.random.default_rng(102)
+    tri, o, d = hit_rays(rng, 20000, 0.05)
+    hits = 0
+    for i in range(tri.shape[0]):
+        m_r = np.zeros(12, np.float32)
+        m_o = np.zeros(12, np.float32)
+        ref.ref_woop_rows(f32p(tri[i]), f32p(m_r))
+        ours.or_pin_woop_rows(f32p(tri[i]), f32p(m_o))
+        assert np.array_equal(bits(m_r), bits(m_o)), i
+        t_max = np.float32(oracle.FINF)
+        out_r = np.zeros(3, np.float32)
+        out_o = np.zeros(3, np.float32)
+        h_r = ref.ref_woop(f32p(m_r), f32p(o[i]), f32p(d[i]), t_max, f32p(out_r))
+        h_o = ours.or_pin_woop(f32p(tri[i]), f32p(o[i]), f32p(d[i]), t_max, f32p(out_o))
+        assert h_r == h_o, i
+        assert np.array_equal(bits(out_r), bits(out_o)), i
+        hits += h_o
+    assert 0.3 * tri.shape[0] < hits < tri.shape[0]
+
+
+def test_adjust_direction_pinned(pins):
+    ref, ours = pins
+    rng = np.random.default_rng(103)
+    vals = np.concatenate([rng.normal(size=3000), [0.0, -0.0, 2.0 ** -80, -(2.0 ** -80), 2.0 ** -81, 2.0 ** -79,
+                                                   1e-30, -1e-30, 1e-24]]).astype(np.float32)
+    vals[:1000] *= np.float32(2.0 ** -79)
+    for i in range(0, len(vals) - 2):
+        a = vals[i:i + 3].copy()
+        b = a.copy()
+        ref.ref_adjust_dir(f32p(a))
+        ours.or_pin_adjust_dir(f32p(b))
+        assert np.array_equal(bits(a), bits(b)), i
+
+
+def test_ray_box_pinned(pins):
+    ref, ours = pins
+    rng = np.random.default_rng(104)
+    n = 40000
+    lo = rng.uniform(-2, 2, size=(n, 3)).astype(np.float32)
+    hi = (lo + rng.uniform(0, 1, size=(n, 3))).astype(np.float32)
+    hi[::9, 2] = lo[::9, 2]              # flat boxes
+    o = rng.uniform(-4, 4, size=(n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    # Half the rays aim at a point of the box (with some just past its faces).
+    aim = (lo + (hi - lo) * rng.uniform(-0.1, 1.1, size=(n, 3))).astype(np.float32)
+    d[::2] = (aim - o)[::2]
+    inv = (np.float32(1.0) / d).astype(np.float32)
+    res = np.zeros(2, np.int64)
+    for i in range(n):
+        r = ref.ref_ray_box(f32p(o[i]), f32p(inv[i]), f32p(lo[i]), f32p(hi[i]))
+        q = ours.or_pin_ray_box(f32p(o[i]), f32p(inv[i]), f32p(lo[i]), f32p(hi[i]))
+        assert r == q, i
+        res[r] += 1
+    assert res.min() > n // 10
+
+
+def test_triangle_box_step3_pinned(pins):
+    """TriangleAabbIntersectionStep3 decides the DIVIDE split method's sides."""
+    ref, ours = pins
+    rng = np.random.default_rng(105)
+    n = 40000
+    c = rng.uniform(-1, 1, size=(n, 3)).astype(np.float32)
+    tri = (np.tile(c, 3) + rng.normal(size=(n, 9)) * rng.choice([0.01, 0.2, 1.0], size=(n, 1))).astype(np.float32)
+    lo = (c + rng.normal(size=(n, 3)) * 0.3).astype(np.float32)
+    hi = (lo + rng.uniform(0, 0.8, size=(n, 3))).astype(np.float32)
+    counts = np.zeros(2, np.int64)
+    for i in range(n):
+        r = ref.ref_tri_box_step3(f32p(tri[i]), f32p(lo[i]), f32p(hi[i]))
+        q = ours.or_pin_tri_box(f32p(tri[i]), f32p(lo[i]), f32p(hi[i]))
+        assert r == q, i
+        counts[r] += 1
+    assert counts.min() > n // 20
