@@ -2,10 +2,11 @@
  * kdgb_oracle.c -- CPU restatement of the reference kd-tree build and ray
  * traversal.  TEST INFRASTRUCTURE: the checker for the CUDA library and the
  * timed CPU baseline; never linked into the product.  The intersection
- * primitives are pinned bit for bit to the reference's own header-only code
- * (oracle/refpin); the build and the traversal loops are parity unpinned
- * (the reference's build does not compile here and it ships no golden
- * vectors).  Every function cites the reference lines it restates.
+ * primitives and the lower SAH / balanced creators are pinned bit for bit to
+ * the reference's own code (oracle/refpin); the upper build and the traversal
+ * loops are parity unpinned (they do not compile here as a whole and the
+ * reference ships no golden vectors).  Every function cites the reference
+ * lines it restates.
  *
  * Build: gcc -O3 -ffp-contract=off -fopenmp -fPIC -shared (see Makefile).
  * -ffp-contract=off keeps every multiply and add separately rounded, the

@@ -14,8 +14,12 @@
  * host stand-ins for CUDA): Moeller-Trumbore, Woop (rows and test),
  * AdjustRayDirection, RayBoxIntersection and TriangleAabbIntersectionStep3
  * of this restatement are pinned to them bit for bit (or_pin_*, tested in
- * tests/test_refpin.py).  The build and the traversal loops are "parity
- * unpinned".  The restatement follows the reference source line by line
+ * tests/test_refpin.py).  The lower-phase kernels (LowerTriangleMap.h:
+ * CalcSAH, CreateLowerSAHChildren, CalcSplit, CreateChildren and their
+ * helpers) compile unmodified too and, replayed on the host one thread at a
+ * time from this restatement's upper leaves, reproduce its SAH and balanced
+ * lower trees bit for bit.  The upper build and the traversal loops are
+ * "parity unpinned".  The restatement follows the reference source line by line
  * (citations on each function) with one documented evaluation order for the
  * un-vendored float3 helpers:
  *   dot(a,b)   = (a.x*b.x + a.y*b.y) + a.z*b.z

@@ -3,10 +3,11 @@
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
 cpu_baseline / --impl reference legs of bench.py as the checker and the
 timed CPU baseline.  The product library never imports this module.
-Its intersection primitives are pinned bit for bit to the reference's own
-header-only code (refpin_lib, tests/test_refpin.py); the build and traversal
-loops are "parity unpinned": the reference's build cannot be compiled here and
-it ships no golden vectors (see kdgb_oracle.h).
+Its intersection primitives and lower SAH / balanced creators are pinned bit
+for bit to the reference's own code (refpin_lib, ref_lower,
+tests/test_refpin.py); the upper build and traversal loops are "parity
+unpinned": they cannot be compiled here as a whole and the reference ships no
+golden vectors (see kdgb_oracle.h).
 """
 from __future__ import annotations
 
@@ -373,3 +374,42 @@ def pin_functions():
     L.or_pin_tri_box.argtypes = [F, F, F]
     L.or_pin_tri_box.restype = C.c_int
     return L
+
+
+def ref_lower(tris: np.ndarray, upper: Tree, lower: int, traversal_cost: float, propagate: bool = True,
+              max_nodes: int | None = None):
+    """The reference's own lower creator (SAH or BALANCED, its kernels run on
+    the host by the pin library) over the upper phase of `upper`, a tree built
+    with the BITMAP lower creator (its upper part is the same for every lower
+    creator).  Returns the node arrays and the lower level count, or None when
+    the pin library is not available."""
+    L = refpin_lib()
+    if L is None:
+        return None
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    n0 = upper.n_nodes
+    cap = max_nodes if max_nodes is not None else 64 * max(n0, 1)
+    out = {
+        "info": np.zeros(cap, np.int8), "split": np.zeros(cap, np.float32),
+        "aabb_min": np.zeros((cap, 4), np.float32), "aabb_max": np.zeros((cap, 4), np.float32),
+        "prim_index": np.zeros(cap, np.int32), "bitmap": np.zeros(cap, np.int32),
+        "children": np.zeros((cap, 2), np.int32), "area": np.zeros(cap, np.float32),
+    }
+    for k, v in out.items():
+        v[:n0] = getattr(upper, k)
+    # The upper leaves hand their reference counts to the lower creator.
+    leaves = upper.leaf_ids
+    out["bitmap"][leaves] = [bin(int(np.uint32(b))).count("1") for b in upper.bitmap[leaves]]
+    out["info"][leaves] = 0
+    levels = C.c_int(0)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    L.ref_lower.restype = C.c_int
+    n = L.ref_lower(C.c_int(lower), C.c_int(int(propagate)), C.c_float(traversal_cost), P(tris), C.c_int(tris.shape[0]),
+                    C.c_int(n0), C.c_int(cap), P(out["info"]), P(out["split"]), P(out["aabb_min"]),
+                    P(out["aabb_max"]), P(out["prim_index"]), P(out["bitmap"]), P(out["children"]), P(out["area"]),
+                    P(np.ascontiguousarray(upper.prim_indices)), P(np.ascontiguousarray(upper.prim_min)),
+                    P(np.ascontiguousarray(upper.prim_max)), C.c_int(upper.prim_indices.shape[0]),
+                    P(np.ascontiguousarray(leaves)), C.c_int(leaves.shape[0]), C.byref(levels))
+    if n < 0:
+        raise RuntimeError("ref_lower: node capacity too small")
+    return {k: v[:n] for k, v in out.items()}, levels.value

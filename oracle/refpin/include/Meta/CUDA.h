@@ -95,3 +95,18 @@ struct KdgbPinDeviceProp {
     int warpSize;
 };
 static KdgbPinDeviceProp activeCudaDevice = {{1024, 1024, 64}, {2147483647, 65535, 65535}, 49152, 65536, 32};
+
+// Kernel execution on the host, one thread at a time (pin tests of the
+// reference's per-thread kernels): launch qualifiers vanish, the thread
+// coordinates are globals set by the caller, and shared memory is a static
+// host buffer.
+#define __constant__
+#define __launch_bounds__(...)
+struct uint3 { unsigned x, y, z; };
+struct dim3 { unsigned x, y, z; };
+extern uint3 threadIdx, blockIdx;
+extern dim3 blockDim, gridDim;
+inline void __syncthreads() {}
+static const int warpSize = 32;
+inline float length(float3 v) { return sqrtf(dot(v, v)); }
+inline float2 make_float2(float x, float y) { float2 r = {x, y}; return r; }

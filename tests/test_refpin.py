@@ -1,5 +1,5 @@
-"""The oracle's intersection primitives, checked bit for bit against the
-reference's OWN header-only code.
+"""The oracle's intersection primitives and lower creators, checked bit for
+bit against the reference's OWN code.
 
 `oracle/refpin/Makefile` compiles the reference's unmodified source with g++:
 Utils/CUDA/IRayTracer.h (AdjustRayDirection, Woop, MoellerTrumbore,
@@ -9,7 +9,9 @@ stand-ins for the CUDA types and the un-vendored vector helpers come from
 `oracle/refpin/include`. This pins the arithmetic of those primitives, as the
 oracle restates it, to the reference's source. The vector helpers themselves
 are not vendored by the reference; both sides use the documented evaluation
-order.
+order. `oracle/refpin/refpin_lower.cpp` adds the lower-phase kernels of
+Utils/CUDA/LowerTriangleMap.h and a host driver that replays their launches
+one thread at a time.
 
 The library is built into oracle/_ref where the reference tree is available.
 Elsewhere these tests skip.
@@ -142,3 +144,42 @@ def test_triangle_box_step3_pinned(pins):
         assert r == q, i
         counts[r] += 1
     assert counts.min() > n // 20
+
+
+LOWER_FIELDS = ("info", "split", "children", "prim_index", "bitmap", "area", "aabb_min", "aabb_max")
+
+
+@pytest.mark.parametrize("lower,cost,propagate", [(1, 24.0, 1), (1, 1.0, 1), (1, 1.0, 0), (2, 24.0, 1), (2, 16.0, 1),
+                                                  (2, 0.0, 0)])
+@pytest.mark.parametrize("scene", ["heightfield", "clustered", "soup"])
+def test_lower_creators_pinned(oracle, pins, lower, cost, propagate, scene):
+    """The whole lower phase: the reference's own kernels (CalcSurfaceArea,
+    PreprocesLowerNodes / PreprocessLeafNodes, CreateSplittingPlanes, CalcSAH /
+    CalcSplit, CreateLowerSAHChildren / CreateChildren, PropagateAabbToChildren;
+    LowerTriangleMap.h) run level by level on the host from the oracle's upper
+    leaves.  Every node the oracle's SAH and BALANCED creators make must come
+    out bit for bit the same."""
+    from kdgb import scenes
+    if scene == "heightfield":
+        tris = scenes.heightfield(64, 32, seed=1)[0]
+    elif scene == "clustered":
+        tris = scenes.clustered(6000, seed=4)
+    else:
+        rng = np.random.default_rng(7)
+        c = rng.random((3000, 1, 3)).astype(np.float32)
+        tris = (c + rng.normal(size=(3000, 3, 3)).astype(np.float32) * 0.02).reshape(-1, 9)
+        tris[::9, 3:6] = tris[::9, 0:3]  # zero-area triangles (dropped by the SAH creator)
+    kw = dict(traversal_cost=cost, propagate_aabbs=propagate)
+    upper = oracle.build(tris, lower=0, **kw)
+    ours = oracle.build(tris, lower=lower, **kw)
+    ref, levels = oracle.ref_lower(tris, upper, lower, cost, bool(propagate), max_nodes=ours.n_nodes + 16)
+    assert levels == ours.lower_levels
+    assert ref["info"].shape[0] == ours.n_nodes
+    for f in LOWER_FIELDS:
+        a, b = ref[f], getattr(ours, f)
+        if a.dtype.kind == "f":
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f
+        else:
+            assert np.array_equal(a, b), f
+    if lower == 2 or cost < 20:  # both creators split at these costs
+        assert ours.n_nodes > upper.n_nodes
