@@ -18,8 +18,11 @@
  * CalcSAH, CreateLowerSAHChildren, CalcSplit, CreateChildren and their
  * helpers) compile unmodified too and, replayed on the host one thread at a
  * time from this restatement's upper leaves, reproduce its SAH and balanced
- * lower trees bit for bit.  The upper build and the traversal loops are
- * "parity unpinned".  The restatement follows the reference source line by line
+ * lower trees bit for bit.  So do the tracer sources (Raytracer.cu,
+ * ShortStack.cu, BruteTracer.cu, compiled with nvcc and run on the host):
+ * shaded pixels, first hits and shadow rays match this restatement bit for
+ * bit (tests/test_refpin_trace.py).  The upper build is "parity unpinned".
+ * The restatement follows the reference source line by line
  * (citations on each function) with one documented evaluation order for the
  * un-vendored float3 helpers:
  *   dot(a,b)   = (a.x*b.x + a.y*b.y) + a.z*b.z

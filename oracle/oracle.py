@@ -3,11 +3,12 @@
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
 cpu_baseline / --impl reference legs of bench.py as the checker and the
 timed CPU baseline.  The product library never imports this module.
-Its intersection primitives and lower SAH / balanced creators are pinned bit
-for bit to the reference's own code (refpin_lib, ref_lower,
-tests/test_refpin.py); the upper build and traversal loops are "parity
-unpinned": they cannot be compiled here as a whole and the reference ships no
-golden vectors (see kdgb_oracle.h).
+Its intersection primitives, lower SAH / balanced creators, tracers, shading
+loop and shadow rays are pinned bit for bit to the reference's own code
+(refpin_lib, ref_lower, refpin_trace_lib, ref_trace, ref_shadow;
+tests/test_refpin.py, tests/test_refpin_trace.py); the upper build is "parity
+unpinned": it cannot be compiled here and the reference ships no golden
+vectors (see kdgb_oracle.h).
 """
 from __future__ import annotations
 
@@ -328,6 +329,8 @@ def moeller_trumbore(v0, v1, v2, o, d, t_max=float(FINF)):
 # ---------------------------------------------------------------------------
 _REFPIN_DIR = os.path.join(_HERE, "refpin")
 _REFPIN_LIB = os.path.join(_HERE, "_ref", "librefpin.so")
+_REFPIN_TRACE_LIB = os.path.join(_HERE, "_ref", "librefpin_trace.so")
+_refpin_trace = None
 _refpin = None
 
 
@@ -338,7 +341,7 @@ def refpin_lib():
     global _refpin
     if _refpin is not None:
         return _refpin
-    r = subprocess.run(["make", "-s", "-C", _REFPIN_DIR], capture_output=True, text=True)
+    r = subprocess.run(["make", "-s", "-C", _REFPIN_DIR, "../_ref/librefpin.so"], capture_output=True, text=True)
     if r.returncode != 0 or not os.path.exists(_REFPIN_LIB):
         return None
     L = C.CDLL(_REFPIN_LIB)
@@ -357,6 +360,130 @@ def refpin_lib():
     L.ref_tri_box_step3.restype = C.c_int
     _refpin = L
     return L
+
+
+class RefTraceScene(C.Structure):
+    """ref_trace_scene of oracle/refpin/refpin_trace.h."""
+    _fields_ = [("n_nodes", C.c_int32), ("info", C.c_void_p), ("split", C.c_void_p), ("children", C.c_void_p),
+                ("prim_index", C.c_void_p), ("bitmap", C.c_void_p), ("aabb_min", C.c_void_p),
+                ("aabb_max", C.c_void_p), ("prim_indices", C.c_void_p), ("n_tris", C.c_int32),
+                ("p0", C.c_void_p), ("p1", C.c_void_p), ("p2", C.c_void_p), ("n0", C.c_void_p),
+                ("n1", C.c_void_p), ("n2", C.c_void_p), ("c0", C.c_void_p)]
+
+
+def refpin_trace_lib():
+    """Loads oracle/_ref/librefpin_trace.so (the reference's Raytracer.cu,
+    ShortStack.cu and BruteTracer.cu compiled unmodified, their traversal
+    functions called on the host), building it with the committed recipe
+    first.  Returns None where the reference tree or nvcc is not available."""
+    global _refpin_trace
+    if _refpin_trace is not None:
+        return _refpin_trace
+    r = subprocess.run(["make", "-s", "-j4", "-C", _REFPIN_DIR, "../_ref/librefpin_trace.so"], capture_output=True,
+                       text=True)
+    if r.returncode != 0 or not os.path.exists(_REFPIN_TRACE_LIB):
+        return None
+    L = C.CDLL(_REFPIN_TRACE_LIB)
+    P, I = C.c_void_p, C.c_int
+    S = C.POINTER(RefTraceScene)
+    for name in ("ref_restart_set_light", "ref_shortstack_set_light", "ref_brute_set_light"):
+        getattr(L, name).argtypes = [P, P, P, P]
+        getattr(L, name).restype = None
+    L.ref_kdrestart.argtypes = [S, I, I, P, P, I, P, P, P]
+    L.ref_kdrestart.restype = None
+    L.ref_shortstack.argtypes = [S, I, I, P, P, I, P, P]
+    L.ref_shortstack.restype = None
+    L.ref_exhaustive.argtypes = [S, I, P, P, I, P]
+    L.ref_exhaustive.restype = None
+    L.ref_shadow.argtypes = [S, I, P, I, P, P]
+    L.ref_shadow.restype = None
+    L.ref_shortstack_depth.restype = I
+    L.ref_brute_max_prims.restype = I
+    L.ref_trace_set_pow.argtypes = [P]
+    L.ref_trace_set_pow.restype = None
+    _refpin_trace = L
+    return L
+
+
+def _f4(a, w):
+    a = np.asarray(a, np.float32).reshape(-1, 3)
+    return np.ascontiguousarray(np.concatenate([a, np.full((a.shape[0], 1), w, np.float32)], axis=1))
+
+
+def ref_trace(tracer: int, tree: Tree | None, tris, o, d, n0, n1, n2, c0, light_params: Light | None = None,
+              intersection: int = ISECT_MOELLER, leaf_skipping: bool = True, oracle_pow: bool = True):
+    """The reference's own shaded tracers, ray by ray on the host
+    (refpin_trace_lib): KDRestart (TRACER_RESTART), ShortStackTrace
+    (TRACER_SHORTSTACK) or Exhaustive (TRACER_BRUTE).  With oracle_pow the
+    specular power is the oracle's or_kpow (which the CUDA kernel computes
+    too); without it the C library's powf, the reference's host path.
+    Returns (rgba (n, 4) uint8, extra): extra is (first_prim, first_thit) for
+    kd-restart, last_thit for the short stack and None for brute force."""
+    L = refpin_trace_lib()
+    if L is None:
+        return None
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    keep = [_f4(tris[:, 0:3], 1.0), _f4(tris[:, 3:6], 1.0), _f4(tris[:, 6:9], 1.0)]
+    keep += [np.ascontiguousarray(x, np.float32).reshape(-1, 4) for x in (n0, n1, n2)]
+    keep.append(np.ascontiguousarray(c0, np.uint8).reshape(-1, 4))
+    sc = RefTraceScene()
+    sc.n_tris = tris.shape[0]
+    sc.p0, sc.p1, sc.p2, sc.n0, sc.n1, sc.n2, sc.c0 = (k.ctypes.data for k in keep)
+    if tree is not None:
+        sc.n_nodes = tree.n_nodes
+        for name in ("info", "split", "children", "prim_index", "bitmap", "aabb_min", "aabb_max",
+                     "prim_indices"):
+            arr = np.ascontiguousarray(getattr(tree, name))
+            keep.append(arr)
+            setattr(sc, name, arr.ctypes.data)
+    lp = light_params if light_params is not None else light()
+    args = [C.cast(lp.position, C.c_void_p), C.cast(lp.ambient, C.c_void_p), C.cast(lp.diffuse, C.c_void_p),
+            C.cast(lp.specular, C.c_void_p)]
+    L.ref_trace_set_pow(C.cast(lib().or_kpow, C.c_void_p) if oracle_pow else None)
+    o4, d4 = _f4(o, 1.0), _f4(d, 0.0)
+    n = o4.shape[0]
+    rgba = np.zeros((n, 4), np.uint8)
+    woop = int(intersection == ISECT_WOOP)
+    if tracer == TRACER_RESTART:
+        L.ref_restart_set_light(*args)
+        prim = np.empty(n, np.int32)
+        th = np.empty((n, 3), np.float32)
+        L.ref_kdrestart(C.byref(sc), woop, int(leaf_skipping), o4.ctypes.data, d4.ctypes.data, n, rgba.ctypes.data,
+                        prim.ctypes.data, th.ctypes.data)
+        return rgba, (prim, th)
+    if tracer == TRACER_SHORTSTACK:
+        L.ref_shortstack_set_light(*args)
+        th = np.empty((n, 3), np.float32)
+        L.ref_shortstack(C.byref(sc), woop, int(leaf_skipping), o4.ctypes.data, d4.ctypes.data, n,
+                         rgba.ctypes.data, th.ctypes.data)
+        return rgba, th
+    L.ref_brute_set_light(*args)
+    L.ref_exhaustive(C.byref(sc), woop, o4.ctypes.data, d4.ctypes.data, n, rgba.ctypes.data)
+    return rgba, None
+
+
+def ref_shadow(tree: Tree, tris, points, light_pos, intersection: int = ISECT_MOELLER):
+    """The reference's own ShadowRay (Raytracer.cu:108-163) per point: 1.0 lit,
+    0.0 in shadow; None where the pin library is not available."""
+    L = refpin_trace_lib()
+    if L is None:
+        return None
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    keep = [_f4(tris[:, 0:3], 1.0), _f4(tris[:, 3:6], 1.0), _f4(tris[:, 6:9], 1.0)]
+    sc = RefTraceScene()
+    sc.n_tris = tris.shape[0]
+    sc.p0, sc.p1, sc.p2 = (k.ctypes.data for k in keep)
+    sc.n_nodes = tree.n_nodes
+    for name in ("info", "split", "children", "prim_index", "bitmap", "aabb_min", "aabb_max", "prim_indices"):
+        arr = np.ascontiguousarray(getattr(tree, name))
+        keep.append(arr)
+        setattr(sc, name, arr.ctypes.data)
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    lp = np.ascontiguousarray(light_pos, np.float32).reshape(3)
+    lit = np.empty(pts.shape[0], np.float32)
+    L.ref_shadow(C.byref(sc), int(intersection == ISECT_WOOP), pts.ctypes.data, pts.shape[0], lp.ctypes.data,
+                 lit.ctypes.data)
+    return lit
 
 
 def pin_functions():

@@ -4,10 +4,9 @@
 // code compiles unmodified with g++ for the oracle's pin test.  TEST
 // INFRASTRUCTURE ONLY: never part of the library.
 //
-// The CUDA-SDK vector helpers are not vendored by the reference; they are
-// defined here in the evaluation order the oracle and the kernels document:
-// dot left to right, standard cross components, every operation rounded
-// separately (compile with -ffp-contract=off).
+// The CUDA-SDK vector helpers are not vendored by the reference; they come
+// from kdgb_pin_vec.h in the evaluation order the oracle and the kernels
+// document.
 #pragma once
 #include <cmath>
 #include <cstddef>
@@ -31,11 +30,7 @@ struct longlong2 { long long x, y; };
 struct longlong4 { long long x, y, z, w; };
 
 inline float3 make_float3(float x, float y, float z) { float3 r = {x, y, z}; return r; }
-inline float3 make_float3(float4 a) { return make_float3(a.x, a.y, a.z); }
-inline float3 make_float3(float s) { return make_float3(s, s, s); }
 inline float4 make_float4(float x, float y, float z, float w) { float4 r = {x, y, z, w}; return r; }
-inline float4 make_float4(float3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
-inline float4 make_float4(float s) { return make_float4(s, s, s, s); }
 inline int2 make_int2(int x, int y) { int2 r = {x, y}; return r; }
 inline int4 make_int4(int x, int y, int z, int w) { int4 r = {x, y, z, w}; return r; }
 
@@ -52,20 +47,8 @@ inline unsigned min(int a, unsigned b) { return min((unsigned)a, b); }
 inline unsigned max(unsigned a, int b) { return max(a, (unsigned)b); }
 inline unsigned max(int a, unsigned b) { return max((unsigned)a, b); }
 
-inline float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
-inline float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
-inline float3 operator*(float3 a, float3 b) { return make_float3(a.x * b.x, a.y * b.y, a.z * b.z); }
-inline float3 operator/(float3 a, float3 b) { return make_float3(a.x / b.x, a.y / b.y, a.z / b.z); }
-inline float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
-inline float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
-inline float3 operator-(float3 a) { return make_float3(-a.x, -a.y, -a.z); }
-inline void operator-=(float3 &a, float3 b) { a = a - b; }
-inline void operator+=(float3 &a, float3 b) { a = a + b; }
-inline float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline float3 cross(float3 a, float3 b)
-{
-    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
+#define KDGB_PIN_HD
+#include <kdgb_pin_vec.h>
 
 // Host copies as plain memory copies (the test keeps everything on the host).
 enum cudaMemcpyKind { cudaMemcpyHostToHost, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice };
@@ -108,5 +91,4 @@ extern uint3 threadIdx, blockIdx;
 extern dim3 blockDim, gridDim;
 inline void __syncthreads() {}
 static const int warpSize = 32;
-inline float length(float3 v) { return sqrtf(dot(v, v)); }
 inline float2 make_float2(float x, float y) { float2 r = {x, y}; return r; }
