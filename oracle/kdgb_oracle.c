@@ -2,11 +2,10 @@
  * kdgb_oracle.c -- CPU restatement of the reference kd-tree build and ray
  * traversal.  TEST INFRASTRUCTURE: the checker for the CUDA library and the
  * timed CPU baseline; never linked into the product.  The intersection
- * primitives, the lower SAH / balanced creators, the three tracers with the
+ * primitives, the upper and lower creators, the three tracers with the
  * shading loop and the shadow rays are pinned bit for bit to the reference's
- * own code (oracle/refpin); the upper build is parity unpinned (it does not
- * compile here and the reference ships no golden vectors).  Every function
- * cites the reference lines it restates.
+ * own code, compiled unmodified and run on the host (oracle/refpin).  Every
+ * function cites the reference lines it restates.
  *
  * Build: gcc -O3 -ffp-contract=off -fopenmp -fPIC -shared (see Makefile).
  * -ffp-contract=off keeps every multiply and add separately rounded, the

@@ -8,20 +8,18 @@
  * extension is missing instead of falling back here.
  *
  * Parity status: the reference's build and tracers cannot be compiled here
- * (they need OpenEngine core, extensions-CUDA, CUDPP and cutil, none of which
- * are present) and it ships no tests, golden vectors or fixtures.  Its
- * header-only intersection primitives do compile unmodified (oracle/refpin,
- * host stand-ins for CUDA): Moeller-Trumbore, Woop (rows and test),
- * AdjustRayDirection, RayBoxIntersection and TriangleAabbIntersectionStep3
- * of this restatement are pinned to them bit for bit (or_pin_*, tested in
- * tests/test_refpin.py).  The lower-phase kernels (LowerTriangleMap.h:
- * CalcSAH, CreateLowerSAHChildren, CalcSplit, CreateChildren and their
- * helpers) compile unmodified too and, replayed on the host one thread at a
- * time from this restatement's upper leaves, reproduce its SAH and balanced
- * lower trees bit for bit.  So do the tracer sources (Raytracer.cu,
- * ShortStack.cu, BruteTracer.cu, compiled with nvcc and run on the host):
- * shaded pixels, first hits and shadow rays match this restatement bit for
- * bit (tests/test_refpin_trace.py).  The upper build is "parity unpinned".
+ * as a whole (they need OpenEngine core, extensions-CUDA, CUDPP and cutil,
+ * none of which are present) and it ships no tests, golden vectors or
+ * fixtures.  Its own code is compiled unmodified in pieces instead
+ * (oracle/refpin, host stand-ins for CUDA) and run on the host, and this
+ * restatement is pinned to it bit for bit:
+ *   - the intersection primitives (or_pin_*, tests/test_refpin.py);
+ *   - the upper creator's kernels (TriangleUpper*.h, EmptySpaceSplitting.h)
+ *     and the lower creators' (LowerTriangleMap.h), replayed one thread at a
+ *     time: whole trees (tests/test_refpin_upper.py, test_refpin.py);
+ *   - the tracer sources (Raytracer.cu, ShortStack.cu, BruteTracer.cu, built
+ *     with nvcc): shaded pixels, first hits and shadow rays
+ *     (tests/test_refpin_trace.py).
  * The restatement follows the reference source line by line
  * (citations on each function) with one documented evaluation order for the
  * un-vendored float3 helpers:

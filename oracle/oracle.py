@@ -3,12 +3,11 @@
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
 cpu_baseline / --impl reference legs of bench.py as the checker and the
 timed CPU baseline.  The product library never imports this module.
-Its intersection primitives, lower SAH / balanced creators, tracers, shading
-loop and shadow rays are pinned bit for bit to the reference's own code
-(refpin_lib, ref_lower, refpin_trace_lib, ref_trace, ref_shadow;
-tests/test_refpin.py, tests/test_refpin_trace.py); the upper build is "parity
-unpinned": it cannot be compiled here and the reference ships no golden
-vectors (see kdgb_oracle.h).
+Its intersection primitives, upper and lower creators, tracers, shading loop
+and shadow rays are pinned bit for bit to the reference's own code, compiled
+unmodified and run on the host (refpin_lib, ref_upper, ref_lower, ref_build,
+refpin_trace_lib, ref_trace, ref_shadow; tests/test_refpin*.py; see
+kdgb_oracle.h).
 """
 from __future__ import annotations
 
@@ -331,6 +330,8 @@ _REFPIN_DIR = os.path.join(_HERE, "refpin")
 _REFPIN_LIB = os.path.join(_HERE, "_ref", "librefpin.so")
 _REFPIN_TRACE_LIB = os.path.join(_HERE, "_ref", "librefpin_trace.so")
 _refpin_trace = None
+_REFPIN_UPPER_LIB = os.path.join(_HERE, "_ref", "librefpin_upper.so")
+_refpin_upper = None
 _refpin = None
 
 
@@ -360,6 +361,100 @@ def refpin_lib():
     L.ref_tri_box_step3.restype = C.c_int
     _refpin = L
     return L
+
+
+def refpin_upper_lib():
+    """Loads oracle/_ref/librefpin_upper.so (the reference's upper-phase
+    kernels run on the host), building it with the committed recipe first.
+    Returns None where the reference tree is not available."""
+    global _refpin_upper
+    if _refpin_upper is not None:
+        return _refpin_upper
+    r = subprocess.run(["make", "-s", "-C", _REFPIN_DIR, "../_ref/librefpin_upper.so"], capture_output=True,
+                       text=True)
+    if r.returncode != 0 or not os.path.exists(_REFPIN_UPPER_LIB):
+        return None
+    L = C.CDLL(_REFPIN_UPPER_LIB)
+    L.ref_upper.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int] + \
+        [C.c_void_p] * 15
+    L.ref_upper.restype = C.c_int
+    _refpin_upper = L
+    return L
+
+
+def ref_upper(tris: np.ndarray, split_method: int = SPLIT_BOX, split_empty_space: bool = True,
+              propagate_aabbs: bool = True, empty_space_threshold: float = 0.35):
+    """The reference's own upper creator (TriangleMapUpperCreator.cu, its
+    kernels run on the host by the pin library).  Returns a dict of the node
+    arrays (`amount` holds the upper leaves' reference counts), the upper-leaf
+    references (prim_min, prim_max, prim_indices), leaf_ids and the level
+    count, or None when the pin library is not available."""
+    L = refpin_upper_lib()
+    if L is None:
+        return None
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    T = tris.shape[0]
+    cap_nodes, cap_refs, cap_leaves = 16 * T + 64, 8 * T + 64, 4 * T + 64
+    out = {
+        "info": np.zeros(cap_nodes, np.int8), "split": np.zeros(cap_nodes, np.float32),
+        "aabb_min": np.zeros((cap_nodes, 4), np.float32), "aabb_max": np.zeros((cap_nodes, 4), np.float32),
+        "prim_index": np.zeros(cap_nodes, np.int32), "amount": np.zeros(cap_nodes, np.int32),
+        "children": np.zeros((cap_nodes, 2), np.int32), "parent": np.zeros(cap_nodes, np.int32),
+        "prim_min": np.zeros((cap_refs, 4), np.float32), "prim_max": np.zeros((cap_refs, 4), np.float32),
+        "prim_indices": np.zeros(cap_refs, np.int32), "leaf_ids": np.zeros(cap_leaves, np.int32),
+    }
+    n_refs, n_leaves, levels = C.c_int(0), C.c_int(0), C.c_int(0)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    n = L.ref_upper(int(split_method), int(split_empty_space), int(propagate_aabbs), float(empty_space_threshold),
+                    P(tris), T, cap_nodes, cap_refs, cap_leaves, P(out["info"]), P(out["split"]), P(out["aabb_min"]),
+                    P(out["aabb_max"]), P(out["prim_index"]), P(out["amount"]), P(out["children"]),
+                    P(out["parent"]), P(out["prim_min"]), P(out["prim_max"]), P(out["prim_indices"]),
+                    C.byref(n_refs), P(out["leaf_ids"]), C.byref(n_leaves), C.byref(levels))
+    if n < 0:
+        raise RuntimeError("ref_upper: capacity too small")
+    res = {k: out[k][:n] for k in ("info", "split", "aabb_min", "aabb_max", "prim_index", "amount", "children",
+                                    "parent")}
+    for k in ("prim_min", "prim_max", "prim_indices"):
+        res[k] = out[k][:n_refs.value]
+    res["leaf_ids"] = out["leaf_ids"][:n_leaves.value]
+    res["levels"] = levels.value
+    return res
+
+
+def ref_build(tris: np.ndarray, lower: int = LOWER_BITMAP, split_method: int = SPLIT_BOX,
+              split_empty_space: bool = True, propagate_aabbs: bool = True, empty_space_threshold: float = 0.35,
+              traversal_cost: float = 24.0):
+    """The reference's whole build from its own kernels: ref_upper, then the
+    BITMAP creator's leaf conversion (TriangleMapBitmapCreator.cu:22-34, two
+    lines restated here: its kernel sits in a .cu whose host code does not
+    compile) or the SAH / BALANCED creator (ref_lower).  Returns a Tree (area
+    zero for BITMAP) and the lower level count, or None when a pin library is
+    not available."""
+    r = ref_upper(tris, split_method, split_empty_space, propagate_aabbs, empty_space_threshold)
+    if r is None:
+        return None
+    info, bitmap, leaves = r["info"].copy(), r["amount"].copy(), r["leaf_ids"]
+    info[leaves] = LEAF
+    bitmap[leaves] = (np.left_shift(1, bitmap[leaves].astype(np.int64)) - 1).astype(np.int32)
+    n = info.shape[0]
+    tree = Tree(info=info, split=r["split"], aabb_min=r["aabb_min"], aabb_max=r["aabb_max"],
+                prim_index=r["prim_index"], bitmap=bitmap, children=r["children"], area=np.zeros(n, np.float32),
+                parent=r["parent"], prim_indices=r["prim_indices"], leaf_ids=leaves, prim_min=r["prim_min"],
+                prim_max=r["prim_max"], upper_levels=r["levels"])
+    if lower == LOWER_BITMAP:
+        return tree, 0
+    res = ref_lower(tris, tree, lower, traversal_cost, propagate_aabbs, max_nodes=64 * n + 64)
+    if res is None:
+        return None
+    nodes, levels = res
+    m = nodes["info"].shape[0]
+    parent = np.zeros(m, np.int32)
+    parent[:n] = tree.parent
+    out = Tree(info=nodes["info"], split=nodes["split"], aabb_min=nodes["aabb_min"], aabb_max=nodes["aabb_max"],
+               prim_index=nodes["prim_index"], bitmap=nodes["bitmap"], children=nodes["children"], area=nodes["area"],
+               parent=parent, prim_indices=tree.prim_indices, leaf_ids=leaves, prim_min=tree.prim_min,
+               prim_max=tree.prim_max, upper_levels=tree.upper_levels, lower_levels=levels)
+    return out, levels
 
 
 class RefTraceScene(C.Structure):

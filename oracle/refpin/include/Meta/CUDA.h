@@ -84,6 +84,7 @@ static KdgbPinDeviceProp activeCudaDevice = {{1024, 1024, 64}, {2147483647, 6553
 // coordinates are globals set by the caller, and shared memory is a static
 // host buffer.
 #define __constant__
+#define __shared__ static
 #define __launch_bounds__(...)
 struct uint3 { unsigned x, y, z; };
 struct dim3 { unsigned x, y, z; };
@@ -92,3 +93,5 @@ extern dim3 blockDim, gridDim;
 inline void __syncthreads() {}
 static const int warpSize = 32;
 inline float2 make_float2(float x, float y) { float2 r = {x, y}; return r; }
+inline float __int_as_float(int i) { float f; memcpy(&f, &i, sizeof f); return f; }
+inline int __float_as_int(float f) { int i; memcpy(&i, &f, sizeof i); return i; }

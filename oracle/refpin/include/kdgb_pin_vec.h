@@ -13,6 +13,7 @@
 KDGB_PIN_HD inline float3 make_float3(float4 a) { return make_float3(a.x, a.y, a.z); }
 KDGB_PIN_HD inline float3 make_float3(float s) { return make_float3(s, s, s); }
 KDGB_PIN_HD inline float4 make_float4(float3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+KDGB_PIN_HD inline float4 make_float4(float3 a) { return make_float4(a.x, a.y, a.z, 0.0f); }
 KDGB_PIN_HD inline float4 make_float4(float s) { return make_float4(s, s, s, s); }
 
 KDGB_PIN_HD inline float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
