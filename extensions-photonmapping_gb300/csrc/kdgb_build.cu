@@ -54,6 +54,17 @@ constexpr int kLanes = 7;                   // per-node scan lanes (see NodeLane
 // Tuned levels: nodes with at least this many references are binned by a
 // whole block, smaller ones by one warp (k_sah_bin).
 constexpr int kSahBlockRefs = 512;
+// A large node is binned in chunks of kSahChunkRefs references, one block
+// each; chunk items are {node index in the level, histogram slot, chunk,
+// chunks}.  The blocks add their histograms into the node's global slot of
+// kSahHist ints (6 x 32 bins and a count of finished chunks); the last one
+// picks the split and zeroes the slot again.
+constexpr int kSahItem = 4;
+constexpr int kSahHist = 6 * 32 + 1;
+constexpr int kSahChunkRefs = 2048;
+// Chunk items a level of `refs` references can list: ceil(cnt / kSahChunkRefs)
+// per node of cnt >= kSahBlockRefs references, at most 2 refs / kSahBlockRefs.
+inline int64_t sah_items(int64_t refs) { return 2 * refs / kSahBlockRefs + 1; }
 constexpr unsigned kFull = 0xffffffffu;
 
 __host__ __device__ inline int64_t chunks_for(int64_t n) { return (n + kChunk - 1) / kChunk; }
@@ -81,6 +92,7 @@ struct Caps {
     int64_t ranges;   // leaf-producing levels
     int64_t low_R;    // SAH lower level arrays
     int64_t tris;     // leaf records of the traversal layout
+    int64_t big;      // binning chunks listed per tuned level (kSahItem ints each)
 };
 
 // Everything a build kernel touches; passed by value to every kernel.
@@ -101,7 +113,7 @@ struct BuildArgs {
     float *area;
     int32_t *prim_indices, *leaf_ids;
     unsigned *keys;
-    int32_t *cnt, *lbase, *chunksum, *tilesum, *tileoff, *big;
+    int32_t *cnt, *lbase, *chunksum, *tilesum, *tileoff, *big, *bighist;
     // Empty-space planes and node counts of a level, in buffer (level & 1)
     // (st->level counts the completed levels): k_children writes the next
     // level's while it reads the current one's.
@@ -392,7 +404,17 @@ __device__ __forceinline__ void node_split_one(const BuildArgs &a, int32_t k, in
     const bool z_higher = mxs < sz;
     a.split[node] = z_higher ? mdz : sp;
     a.info[node] = z_higher ? (int8_t)KDGB_Z : ax;
-    if (sah && a.amt[node] >= kSahBlockRefs) a.big[atomicAdd(&a.st->n_big, 1)] = k;
+    const int32_t cnt = a.amt[node];
+    if (sah && cnt >= kSahBlockRefs) {
+        const int32_t nch = (cnt + kSahChunkRefs - 1) / kSahChunkRefs;
+        const int32_t base = atomicAdd(&a.st->n_big, nch);
+        if ((int64_t)base + nch > a.cap.big) {
+            set_err(a.st, KDGB_ERR_CAPACITY, kErrUpperCapacity);
+            return;
+        }
+        for (int32_t c = 0; c < nch; ++c)
+            reinterpret_cast<int4 *>(a.big)[base + c] = make_int4(k, base, c, nch);
+    }
 }
 
 // The roots' splits (the first level; no empty-space cuts at the root).
@@ -628,16 +650,17 @@ struct SahNode {
     bool valid[3];
 };
 
-// Adds the references of rows row0, row0 + step, ... (32 references each)
-// of one node to the histograms h[(axis * 2 + side) * 32 + bin] (shared
-// memory private to the calling warp), one shared atomic per reference, axis
-// and side (cheaper than merging equal bins first).  kRows rows of loads are
-// in flight before any of them is binned.
+// Adds the references of rows row0, row0 + step, ... below row_end (32
+// references each) of one node to the histograms
+// h[(axis * 2 + side) * 32 + bin] (shared memory private to the calling
+// warp), one shared atomic per reference, axis and side (cheaper than
+// merging equal bins first).  kRows rows of loads are in flight before any
+// of them is binned.
 __device__ __forceinline__ void sah_rows(const float4 *__restrict__ cmin, const float4 *__restrict__ cmax,
-                                         const SahNode &n, int B, int row0, int step, int *h)
+                                         const SahNode &n, int B, int row0, int step, int row_end, int *h)
 {
     const int lane = threadIdx.x & 31;
-    const int rows = (n.cnt + 31) >> 5;
+    const int rows = row_end;
     for (int r0 = row0; r0 < rows; r0 += kRows * step) {
         float4 p[kRows], q[kRows];
         bool in[kRows];
@@ -731,14 +754,18 @@ __device__ __forceinline__ SahNode sah_node(const BuildArgs &a, int32_t node)
 }
 
 // Binned SAH of the active nodes, one launch per tuned level.  First the
-// nodes of kSahBlockRefs references or more (listed with the splits), one
-// block each, taken from a work counter: every warp bins an interleaved
-// share of the rows into its own histograms, which are then summed.  Then
-// the smaller nodes, one warp each.
+// chunks of the nodes with kSahBlockRefs references or more (listed with the
+// splits), one block each, taken from a work counter: every warp bins an
+// interleaved share of the chunk's rows into its own histograms, the block
+// sums them and adds them into the node's global slot, and the block that
+// finishes the node's last chunk picks its split (a node of one chunk is
+// picked from shared memory directly).  Then the smaller nodes, one warp
+// each.  Bin counts are integers, so the order of the additions cannot
+// change them.
 __global__ void __launch_bounds__(kBlock, 4) k_sah_bin(const BuildArgs a)
 {
     __shared__ int s_hist[kWarps][6 * 32];
-    __shared__ int32_t s_big;
+    __shared__ int32_t s_big, s_last;
     BuildState *st = a.st;
     if (!sah_level(a, st)) return;
     const int32_t nb = st->n_big, R = st->R, active = st->active;
@@ -748,27 +775,52 @@ __global__ void __launch_bounds__(kBlock, 4) k_sah_bin(const BuildArgs a)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int *h = s_hist[warp];
     int hv[6];
+    constexpr int kChunkRows = kSahChunkRefs / 32;
     for (;;) {
         if (threadIdx.x == 0) s_big = atomicAdd(&st->big_next, 1);
         __syncthreads();
-        const int32_t k = s_big;
-        if (k >= nb) break;  // block-uniform
-        const SahNode n = sah_node(a, active + a.big[k]);
+        const int32_t it = s_big;
+        if (it >= nb) break;  // block-uniform
+        const int4 item = reinterpret_cast<const int4 *>(a.big)[it];  // {k, slot, chunk, chunks}
+        const SahNode n = sah_node(a, active + item.x);
         for (int j = lane; j < 6 * 32; j += 32) h[j] = 0;
         __syncwarp();
-        sah_rows(cmin, cmax, n, a.B, warp, kWarps, h);
+        const int rows = (n.cnt + 31) >> 5;
+        const int row_end = min(rows, (item.z + 1) * kChunkRows);
+        sah_rows(cmin, cmax, n, a.B, item.z * kChunkRows + warp, kWarps, row_end, h);
         __syncthreads();
-        if (warp == 0) {
+        if (item.w == 1) {
+            if (warp == 0) {
 #pragma unroll
-            for (int j = 0; j < 6; ++j) {
+                for (int j = 0; j < 6; ++j) {
+                    int sum = 0;
+#pragma unroll
+                    for (int w = 0; w < kWarps; ++w) sum += s_hist[w][j * 32 + lane];
+                    hv[j] = sum;
+                }
+                sah_pick(a, n, hv, lane);
+            }
+        } else {
+            int32_t *g = a.bighist + (int64_t)item.y * kSahHist;
+            for (int j = threadIdx.x; j < 6 * 32; j += blockDim.x) {
                 int sum = 0;
 #pragma unroll
-                for (int w = 0; w < kWarps; ++w) sum += s_hist[w][j * 32 + lane];
-                hv[j] = sum;
+                for (int w = 0; w < kWarps; ++w) sum += s_hist[w][j];
+                if (sum) atomicAdd(g + j, sum);
             }
-            sah_pick(a, n, hv, lane);
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) s_last = atomicAdd(g + 6 * 32, 1) == item.w - 1;
+            __syncthreads();
+            if (s_last && warp == 0) {  // every chunk of the node is in g
+                __threadfence();
+#pragma unroll
+                for (int j = 0; j < 6; ++j) hv[j] = atomicExch(g + j * 32 + lane, 0);
+                if (lane == 0) atomicExch(g + 6 * 32, 0);
+                sah_pick(a, n, hv, lane);
+            }
         }
-        __syncthreads();  // s_hist and s_big are reused
+        __syncthreads();  // s_hist, s_big and s_last are reused
     }
     WARP_STRIDE(gw, R) {
         const int32_t node = active + (int32_t)gw;
@@ -776,7 +828,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_sah_bin(const BuildArgs a)
         const SahNode n = sah_node(a, node);
         for (int j = lane; j < 6 * 32; j += 32) h[j] = 0;
         __syncwarp();
-        sah_rows(cmin, cmax, n, a.B, 0, 1, h);
+        sah_rows(cmin, cmax, n, a.B, 0, 1, (n.cnt + 31) >> 5, h);
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < 6; ++j) hv[j] = h[j * 32 + lane];
@@ -1657,6 +1709,11 @@ __global__ void k_pack_nodes(int32_t n_host, const int32_t *n_dev, const int32_t
 // One warp per node; lane j of a leaf writes the record of bitmap bit j at
 // the leaf's offset + the rank of j among the set bits (bitmap order, LSB
 // first), so a leaf's gathers are all in flight at once.
+// Leaf records in leaf order: a warp takes 32 consecutive nodes, whose
+// records are contiguous from off[first node], and writes them 32 at a time,
+// so the stores are coalesced and every lane has a record whatever the leaf
+// sizes.  Record r of the group belongs to the last node j whose exclusive
+// count is <= r, and is the (r - excl_j)-th member (bit order) of its bitmap.
 __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t *err, int64_t cap_tris,
                             const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
                             const int32_t *__restrict__ pidx, const int32_t *__restrict__ prim_indices,
@@ -1666,21 +1723,46 @@ __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t 
 {
     const int32_t n = n_dev ? *n_dev : n_host;
     if (!pack_ok(n, err, off, cap_tris)) return;
-    const unsigned lane = threadIdx.x & 31;
-    WARP_STRIDE(w, n) {
-        const int32_t node = (int32_t)w;
-        if ((info[node] & 3) != KDGB_LEAF) continue;  // warp-uniform
-        const unsigned bmp = (unsigned)bitmap[node];
-        if (!((bmp >> lane) & 1u)) continue;
-        const int64_t rec = off[node] + __popc(bmp & ((1u << lane) - 1u));
-        const int32_t prim = prim_indices[pidx[node] + lane];
-        const float4 pa = p0[prim], pb = p1[prim], pc = p2[prim];
-        const float3 v0 = make_float3(pa.x, pa.y, pa.z);
-        const float3 e1 = sub3(make_float3(pb.x, pb.y, pb.z), v0);
-        const float3 e2 = sub3(make_float3(pc.x, pc.y, pc.z), v0);
-        ttri[3 * rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
-        ttri[3 * rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
-        ttri[3 * rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
+    const int lane = threadIdx.x & 31;
+    WARP_STRIDE(w, (n + 31) >> 5) {
+        const int32_t node = (int32_t)(w << 5) + lane;
+        const bool leaf = node < n && info[node] == KDGB_LEAF;  // as k_leaf_counts counts them
+        const unsigned bmp = leaf ? (unsigned)bitmap[node] : 0u;
+        const int32_t first = leaf ? pidx[node] : 0;
+        const int cnt = __popc(bmp);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int excl = incl - cnt;
+        const int total = __shfl_sync(kFull, incl, 31);
+        const int64_t rec0 = off[(int32_t)(w << 5)];
+        for (int base = 0; base < total; base += 32) {  // warp-uniform trip count
+            const int r = base + lane;
+            int j = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int e = __shfl_sync(kFull, excl, j + step);
+                if (e <= r) j += step;
+            }
+            const int ej = __shfl_sync(kFull, excl, j);
+            unsigned m = __shfl_sync(kFull, bmp, j);
+            const int32_t fj = __shfl_sync(kFull, first, j);
+            if (r < total) {
+                for (int k = r - ej; k > 0; --k) m &= m - 1u;
+                const int32_t prim = prim_indices[fj + __ffs(m) - 1];
+                const float4 pa = p0[prim], pb = p1[prim], pc = p2[prim];
+                const float3 v0 = make_float3(pa.x, pa.y, pa.z);
+                const float3 e1 = sub3(make_float3(pb.x, pb.y, pb.z), v0);
+                const float3 e2 = sub3(make_float3(pc.x, pc.y, pc.z), v0);
+                const int64_t rec = rec0 + r;
+                ttri[3 * rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
+                ttri[3 * rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
+                ttri[3 * rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
+            }
+        }
     }
 }
 
@@ -1820,6 +1902,8 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.tilesum = w.tilesum.p;
     a.tileoff = w.tileoff.p;
     a.big = w.big.p;
+    a.bighist = w.bighist.p;
+    a.cap.big = std::min(w.big.cap / kSahItem, w.bighist.cap / kSahHist);
     a.ranges = w.ranges.p;
     a.roff = w.roff.p;
     a.cap.ranges = std::min(w.ranges.cap, w.roff.cap);
@@ -1865,7 +1949,7 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
     const unsigned gR = L.grid(e.R, kBlock, 2);
     if (tuned_levels) {
         // Enough blocks for one per large node and one warp per node.
-        const int64_t big = std::min<int64_t>(e.R, ceil_div(e.N, kSahBlockRefs));
+        const int64_t big = ceil_div(e.N, kSahBlockRefs);  // at least the large nodes
         k_sah_bin<<<L.grid(std::max<int64_t>(big * kBlock, e.R * 32), kBlock), kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
@@ -1948,7 +2032,7 @@ int emit_pack(const BuildArgs &a, const Launcher &L, const Extents &e, cudaStrea
     k_pack_nodes<<<g, kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info, a.split, a.ch, a.loff,
                                       a.tnode);
     KDGB_LAUNCH_CHECK();
-    k_pack_tris<<<L.grid(e.nodes * 32, kBlock), kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info,
+    k_pack_tris<<<L.grid(e.nodes, kBlock), kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info,
                                                                  a.amt, a.pidx,
                                      a.prim_indices, a.p0, a.p1, a.p2, a.loff, a.ttri);
     KDGB_LAUNCH_CHECK();
@@ -2048,7 +2132,7 @@ uint64_t layout_signature(const Tree &t)
     MIX(w.rmin[0]); MIX(w.rmin[1]); MIX(w.rmax[0]); MIX(w.rmax[1]); MIX(w.fmin); MIX(w.fmax);
     MIX(w.keys); MIX(w.planes[0]); MIX(w.planes[1]); MIX(w.cnt); MIX(w.ess[0]); MIX(w.ess[1]); MIX(w.lbase);
     MIX(w.chunksum);
-    MIX(w.tilesum); MIX(w.tileoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.big); MIX(w.areas); MIX(w.sts);
+    MIX(w.tilesum); MIX(w.tileoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.big); MIX(w.bighist); MIX(w.areas); MIX(w.sts);
     MIX(w.ssplit); MIX(w.saddr); MIX(w.roff); MIX(w.careas); MIX(w.csets); MIX(w.ranges); MIX(w.state);
 #undef MIX
     return h;
@@ -2106,7 +2190,7 @@ int pack_for_traversal(Tree &t, cudaStream_t s)
         k_pack_nodes<<<g, kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p, t.split.p, t.children.p, off,
                                           t.tnode.p);
         KDGB_LAUNCH_CHECK();
-        k_pack_tris<<<L.grid((int64_t)n * 32, kBlock), kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p,
+        k_pack_tris<<<L.grid(n, kBlock), kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p,
                                                                         t.bitmap.p, t.pidx.p, t.prim_indices.p,
                                                                         t.p0.p, t.p1.p, t.p2.p, off, t.ttri.p);
         KDGB_LAUNCH_CHECK();
@@ -2128,7 +2212,8 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
     KDGB_CHECK(grow_nodes(t, M, 0, s));
     KDGB_CHECK(grab(w.planes[0], M, s));
     KDGB_CHECK(grab(w.ess[0], M, s));
-    KDGB_CHECK(grab(w.big, M + 1, s));
+    KDGB_CHECK(grab(w.big, kSahItem * sah_items(T), s));
+    KDGB_CHECK(ensure(w.bighist, kSahHist * sah_items(T), s, 0, true));
     KDGB_CHECK(reserve_keep(w.keys, 6 * (int64_t)M, 0, s));
     KDGB_CHECK(reserve_keep(w.cnt, 2 * (int64_t)M, 0, s));
     KDGB_CHECK(grab(w.ranges, (int64_t)p.max_levels + 1, s));
@@ -2175,8 +2260,8 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
         KDGB_CHECK(grab(w.tileoff, 2 * (ceil_div(N, kTileRefs) + 1), s));
         // This level's large-node list is kept; the next level's is listed
         // by k_children.
-        KDGB_CHECK(reserve_keep(w.big, std::min<int64_t>(2 * R, 2 * N / kSahBlockRefs) + 1,
-                                std::min<int64_t>(R, N / kSahBlockRefs) + 1, s));
+        KDGB_CHECK(reserve_keep(w.big, kSahItem * sah_items(2 * N), kSahItem * sah_items(N), s));
+        KDGB_CHECK(ensure(w.bighist, kSahHist * sah_items(2 * N), s, 0, true));
         const Extents e{N, R, F, n_nodes, 0, 0};
         KDGB_CHECK(emit_upper_level(make_args(t, p, T, M, mesh_off_dev), L, e, tuned_level, w, s));
         KDGB_CHECK(fetch_state(t, st, s));
@@ -2268,7 +2353,8 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.chunksum, 2 * chunks_for(refs), s));
     KDGB_CHECK(ensure(w.tilesum, 2 * ceil_div(refs, kTileRefs), s));
     KDGB_CHECK(ensure(w.tileoff, 2 * (ceil_div(refs, kTileRefs) + 1), s));
-    KDGB_CHECK(ensure(w.big, refs / kSahBlockRefs + 1, s));
+    KDGB_CHECK(ensure(w.big, kSahItem * sah_items(refs), s));
+    KDGB_CHECK(ensure(w.bighist, kSahHist * sah_items(refs), s, 0, true));
     KDGB_CHECK(ensure(w.ranges, (int64_t)p.max_levels + 1, s));
     KDGB_CHECK(ensure(w.roff, (int64_t)p.max_levels + 1, s));
     KDGB_CHECK(ensure(t.leaf_ids, leaves, s));

@@ -88,9 +88,9 @@ struct BuildState {
     int32_t low_levels;   // SAH lower levels completed
     int32_t low_first;    // 1 while the lower level is the upper leaves
     int32_t n_leaf_tris;  // leaf records of the traversal layout
-    int32_t n_big;        // tuned levels: active nodes listed for block-wide SAH binning
+    int32_t n_big;        // tuned levels: chunks of large active nodes listed for block-wide SAH binning
     int32_t done;         // blocks of the current level-closing kernel that have finished
-    int32_t big_next;     // tuned levels: work counter over the listed nodes
+    int32_t big_next;     // tuned levels: work counter over the listed chunks
 };
 
 // Sizes seen by the last host-driven build of a handle; a graph rebuild
@@ -115,6 +115,7 @@ struct Workspace {
     DevArray<int8_t> planes[2];  // empty-space planes of a level, by level parity
     DevArray<int32_t> ess[2];    // empty-space node counts of a level, by level parity
     DevArray<int32_t> cnt, lbase, chunksum, tilesum, tileoff, stats, scan, misc0, misc1, big;
+    DevArray<int32_t> bighist;  // per-node SAH histograms of chunked large nodes, zero between uses
     DevArray<float> areas;
     DevArray<int4> sts;
     DevArray<int32_t> ssplit, saddr, roff;
