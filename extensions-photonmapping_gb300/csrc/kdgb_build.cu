@@ -1368,12 +1368,16 @@ __global__ void k_sah_preprocess(const BuildArgs a)
 // CreateSplittingPlanes (LowerTriangleMap.h:84-155): one warp per node, lane
 // i owns reference slot i.  Sets per axis: {lowLeft, lowRight, highLeft,
 // highRight} of the planes at slot i's box low / high.
+// The members' boxes are staged in shared memory and read back as
+// broadcasts, four members per step, so each member costs two loads instead
+// of six shuffles.
 __global__ void k_sah_planes(const BuildArgs a)
 {
+    __shared__ float4 s_lo[kWarps][32], s_hi[kWarps][32];
     const BuildState *st = a.st;
     if (st->err) return;
     const int64_t F = st->F;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = (threadIdx.x >> 5) & (kWarps - 1);
     WARP_STRIDE(gw, st->n_leaf_ids) {
         const int32_t leaf = a.leaf_ids[gw];
         const int32_t pi = a.pidx[leaf];
@@ -1381,32 +1385,34 @@ __global__ void k_sah_planes(const BuildArgs a)
         const bool mine = (bmp >> lane) & 1u;
         float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
         if (mine) { lo = a.fmin[pi + lane]; hi = a.fmax[pi + lane]; }
+        s_lo[warp][lane] = lo;
+        s_hi[warp][lane] = hi;
+        __syncwarp();
         unsigned sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sz[4] = {0, 0, 0, 0};
-        for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; two members per iteration
-            int jj[2];
-            unsigned mm[2];
+        for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; four members per step
+            int jj[4];
+            unsigned mm[4];
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
+            for (int q = 0; q < 4; ++q) {
                 jj[q] = bits ? __ffs(bits) - 1 : 0;
                 mm[q] = bits ? 1u << jj[q] : 0u;
                 bits &= bits - 1u;
             }
-            float mnx[2], mny[2], mnz[2], mxx[2], mxy[2], mxz[2];
+            float4 mn[4], mx[4];
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                mnx[q] = __shfl_sync(kFull, lo.x, jj[q]); mny[q] = __shfl_sync(kFull, lo.y, jj[q]);
-                mnz[q] = __shfl_sync(kFull, lo.z, jj[q]); mxx[q] = __shfl_sync(kFull, hi.x, jj[q]);
-                mxy[q] = __shfl_sync(kFull, hi.y, jj[q]); mxz[q] = __shfl_sync(kFull, hi.z, jj[q]);
+            for (int q = 0; q < 4; ++q) {
+                mn[q] = s_lo[warp][jj[q]];
+                mx[q] = s_hi[warp][jj[q]];
             }
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
+            for (int q = 0; q < 4; ++q) {
                 const unsigned m = mm[q];
-                sx[0] |= mnx[q] <= lo.x ? m : 0; sx[1] |= lo.x < mxx[q] ? m : 0;
-                sx[2] |= mnx[q] <= hi.x ? m : 0; sx[3] |= hi.x < mxx[q] ? m : 0;
-                sy[0] |= mny[q] <= lo.y ? m : 0; sy[1] |= lo.y < mxy[q] ? m : 0;
-                sy[2] |= mny[q] <= hi.y ? m : 0; sy[3] |= hi.y < mxy[q] ? m : 0;
-                sz[0] |= mnz[q] <= lo.z ? m : 0; sz[1] |= lo.z < mxz[q] ? m : 0;
-                sz[2] |= mnz[q] <= hi.z ? m : 0; sz[3] |= hi.z < mxz[q] ? m : 0;
+                sx[0] |= mn[q].x <= lo.x ? m : 0; sx[1] |= lo.x < mx[q].x ? m : 0;
+                sx[2] |= mn[q].x <= hi.x ? m : 0; sx[3] |= hi.x < mx[q].x ? m : 0;
+                sy[0] |= mn[q].y <= lo.y ? m : 0; sy[1] |= lo.y < mx[q].y ? m : 0;
+                sy[2] |= mn[q].y <= hi.y ? m : 0; sy[3] |= hi.y < mx[q].y ? m : 0;
+                sz[0] |= mn[q].z <= lo.z ? m : 0; sz[1] |= lo.z < mx[q].z ? m : 0;
+                sz[2] |= mn[q].z <= hi.z ? m : 0; sz[3] |= hi.z < mx[q].z ? m : 0;
             }
         }
         if (mine) {
@@ -1414,6 +1420,7 @@ __global__ void k_sah_planes(const BuildArgs a)
             a.sts[F + pi + lane] = make_int4(sy[0], sy[1], sy[2], sy[3]);
             a.sts[2 * F + pi + lane] = make_int4(sz[0], sz[1], sz[2], sz[3]);
         }
+        __syncwarp();  // the staged boxes are rewritten by the warp's next node
     }
 }
 
