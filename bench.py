@@ -378,11 +378,18 @@ def run_frame(args, world, rank, local, pg):
         h_out = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in outs]
         # The rays are not needed until the trace: they are uploaded on a
         # second stream while the tree is rebuilt (after the previous step's
-        # trace has read them).  Every step still copies all its inputs and
-        # reads back all its outputs inside the timed region.
+        # trace has read them).  The outputs are read back on a third stream,
+        # so the read-back of one step overlaps the next step's triangle
+        # upload and rebuild; the next trace waits for it before it rewrites
+        # the output buffers.  Every step still copies all its inputs and
+        # reads back all its outputs inside the timed region, which ends
+        # when the last read-back has landed.
         side = torch.cuda.Stream(device=dev)
+        back = torch.cuda.Stream(device=dev)
         traced = torch.cuda.Event()
         traced.record(stream)
+        read_back = torch.cuda.Event()
+        read_back.record(stream)
 
         def e2e_step():
             side.wait_event(traced)
@@ -394,10 +401,14 @@ def run_frame(args, world, rank, local, pg):
             tris_d.copy_(h_tris, non_blocking=True)
             build()
             stream.wait_event(rays_in)
+            stream.wait_event(read_back)
             tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
             traced.record(stream)
-            for hb, db in zip(h_out, outs):
-                hb.copy_(db, non_blocking=True)
+            back.wait_event(traced)
+            with torch.cuda.stream(back):
+                for hb, db in zip(h_out, outs):
+                    hb.copy_(db, non_blocking=True)
+            read_back.record(back)
 
         for _ in range(2):
             e2e_step()
@@ -408,6 +419,7 @@ def run_frame(args, world, rank, local, pg):
         e0.record(stream)
         for _ in range(args.steps):
             e2e_step()
+        stream.wait_event(read_back)
         e1.record(stream)
         e1.synchronize()
         e2e_ms = e0.elapsed_time(e1) / args.steps
