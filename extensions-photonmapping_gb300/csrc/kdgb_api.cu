@@ -112,7 +112,7 @@ static void release_all(Tree &t, cudaStream_t s)
     release(t.info, s); release(t.split, s); release(t.bmin, s); release(t.bmax, s);
     release(t.pidx, s); release(t.bitmap, s); release(t.parent, s); release(t.children, s);
     release(t.area, s); release(t.prim_indices, s); release(t.leaf_ids, s);
-    release(t.tnode, s); release(t.ttri, s); release(t.mesh_off, s); release(t.woop, s);
+    release(t.tnode, s); release(t.tbmin, s); release(t.tbmax, s); release(t.ttri, s); release(t.mesh_off, s); release(t.woop, s);
     t.woop_valid = false;
     Workspace &w = t.ws;
     for (int b = 0; b < 2; ++b) {

@@ -60,6 +60,8 @@ constexpr int kSahBlockRefs = 512;
 // kSahHist ints (6 x 32 bins and a count of finished chunks); the last one
 // picks the split and zeroes the slot again.
 constexpr int kSahItem = 4;
+// The traversal layout keeps a node index in 30 bits (kdgb_trace.cu).
+constexpr int64_t kMaxPackNodes = int64_t(1) << 29;
 constexpr int kSahHist = 6 * 32 + 1;
 constexpr int kSahChunkRefs = 2048;
 // Chunk items a level of `refs` references can list: ceil(cnt / kSahChunkRefs)
@@ -126,8 +128,10 @@ struct BuildArgs {
     int32_t *ssplit, *saddr;
     float2 *careas;
     int2 *csets;
-    int32_t *lcnt, *loff;
-    int4 *tnode;
+    int32_t *loff;  // PackLanes scan: 2 ints per node and the totals
+    int2 *tnode;
+    float4 *tbmin, *tbmax;
+    int32_t *norder;  // each node's index in the traversal order
     float4 *ttri;
     cudaGraphConditionalHandle upper_cond, lower_cond;
     int use_cond;
@@ -1672,52 +1676,71 @@ __global__ void k_sah_children(const BuildArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// Traversal layout (read by kdgb_trace.cu):
-//   tnode[i]  int4  interior: {split bits, left, right, axis}
-//                   leaf:     {first record, record count, 0, 0}
+// Traversal layout (read by kdgb_trace.cu), in traversal order: roots
+// 0..M-1, then the two children of interior node p (rank r among the
+// interior nodes in node order) at M + 2r (left) and M + 2r + 1 (right).
+//   tnode[j]  int2  interior: {split bits, (left << 2) | axis}
+//                   leaf:     {first record, (record count << 2) | 0}
+//   tbmin/tbmax[j]  the leaf's box (leaf skipping)
 //   ttri[3r..3r+2]  float4 x3 per leaf record, in leaf order (LSB first):
 //                   {v0.xyz, e1.x} {e1.yz, e2.xy} {e2.z, id bits, 0, 0}
-// One 16-byte load per traversal step and three 16-byte loads per triangle
-// test, with no index indirection; e1 = v1 - v0 and e2 = v2 - v0 are the same
-// fp32 values the reference computes per test.  The node count is n_host, or
-// *n_dev when given; err (optional) skips the pass after a failed build.
+// One 8-byte load per traversal step, siblings in one sector, and three
+// 16-byte loads per triangle test, with no index indirection; e1 = v1 - v0
+// and e2 = v2 - v0 are the same fp32 values the reference computes per test.
+// off holds the exclusive scan of PackLanes: off[2i] the first record of
+// node i, off[2i + 1] its interior rank; record n holds the totals.  The
+// node count is n_host, or *n_dev when given; err (optional) skips the pass
+// after a failed build.
 // ---------------------------------------------------------------------------
-__global__ void k_leaf_counts(int32_t n_host, const int32_t *n_dev, const int32_t *err,
-                              const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
-                              int32_t *__restrict__ cnt)
-{
-    if (err && *err) return;
-    const int32_t n = n_dev ? *n_dev : n_host;
-    GRID_STRIDE(i, n) cnt[i] = info[i] == KDGB_LEAF ? __popc((unsigned)bitmap[i]) : 0;
-}
-
 __device__ __forceinline__ bool pack_ok(int32_t n, const int32_t *err, const int32_t *off, int64_t cap_tris)
 {
-    return !(err && *err) && (int64_t)off[n] <= cap_tris;
+    return !(err && *err) && (int64_t)off[2 * (int64_t)n] <= cap_tris;
 }
 
-__global__ void k_pack_nodes(int32_t n_host, const int32_t *n_dev, const int32_t *err, int64_t cap_tris,
-                             const int8_t *__restrict__ info, const float *__restrict__ split,
-                             const int2 *__restrict__ ch, const int32_t *__restrict__ off, int4 *__restrict__ tnode)
+// Each node's traversal index: roots keep theirs, the children of interior
+// node i go to M + 2 rank(i) and the slot after it.  norder starts at -1, so
+// a node that no interior node names stays outside [0, n) and is not packed.
+__global__ void k_pack_order(int32_t n_host, const int32_t *n_dev, const int32_t *err, int64_t cap_tris, int32_t M,
+                             const int8_t *__restrict__ info, const int2 *__restrict__ ch,
+                             const int32_t *__restrict__ off, int32_t *__restrict__ norder)
 {
     const int32_t n = n_dev ? *n_dev : n_host;
     if (!pack_ok(n, err, off, cap_tris)) return;
     GRID_STRIDE(i, n) {
+        if (i < M) norder[i] = (int32_t)i;
+        if ((info[i] & 3) == KDGB_LEAF) continue;
+        const int2 c = ch[i];
+        const int32_t first = M + 2 * off[2 * i + 1];
+        if (c.x >= 0 && c.x < n) norder[c.x] = first;
+        if (c.y >= 0 && c.y < n) norder[c.y] = first + 1;
+    }
+}
+
+__global__ void k_pack_nodes(int32_t n_host, const int32_t *n_dev, const int32_t *err, int64_t cap_tris, int32_t M,
+                             const int8_t *__restrict__ info, const float *__restrict__ split,
+                             const float4 *__restrict__ bmin, const float4 *__restrict__ bmax,
+                             const int32_t *__restrict__ off, const int32_t *__restrict__ norder,
+                             int2 *__restrict__ tnode, float4 *__restrict__ tbmin, float4 *__restrict__ tbmax)
+{
+    const int32_t n = n_dev ? *n_dev : n_host;
+    if (!pack_ok(n, err, off, cap_tris)) return;
+    GRID_STRIDE(i, n) {
+        const int32_t j = norder[i];
+        if (j < 0 || j >= n) continue;  // not reached from a root
         const int ax = info[i] & 3;
         if (ax == KDGB_LEAF) {
-            tnode[i] = make_int4(off[i], off[i + 1] - off[i], 0, 0);
+            const int32_t first = off[2 * i];
+            tnode[j] = make_int2(first, (off[2 * i + 2] - first) << 2);
+            tbmin[j] = bmin[i];
+            tbmax[j] = bmax[i];
         } else {
-            const int2 c = ch[i];
-            tnode[i] = make_int4(__float_as_int(split[i]), c.x, c.y, ax);
+            tnode[j] = make_int2(__float_as_int(split[i]), ((M + 2 * off[2 * i + 1]) << 2) | ax);
         }
     }
 }
 
-// One warp per node; lane j of a leaf writes the record of bitmap bit j at
-// the leaf's offset + the rank of j among the set bits (bitmap order, LSB
-// first), so a leaf's gathers are all in flight at once.
 // Leaf records in leaf order: a warp takes 32 consecutive nodes, whose
-// records are contiguous from off[first node], and writes them 32 at a time,
+// records are contiguous from off[2 * first node], and writes them 32 at a time,
 // so the stores are coalesced and every lane has a record whatever the leaf
 // sizes.  Record r of the group belongs to the last node j whose exclusive
 // count is <= r, and is the (r - excl_j)-th member (bit order) of its bitmap.
@@ -1733,7 +1756,7 @@ __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t 
     const int lane = threadIdx.x & 31;
     WARP_STRIDE(w, (n + 31) >> 5) {
         const int32_t node = (int32_t)(w << 5) + lane;
-        const bool leaf = node < n && info[node] == KDGB_LEAF;  // as k_leaf_counts counts them
+        const bool leaf = node < n && (info[node] & 3) == KDGB_LEAF;  // as PackLanes counts them
         const unsigned bmp = leaf ? (unsigned)bitmap[node] : 0u;
         const int32_t first = leaf ? pidx[node] : 0;
         const int cnt = __popc(bmp);
@@ -1745,7 +1768,7 @@ __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t 
         }
         const int excl = incl - cnt;
         const int total = __shfl_sync(kFull, incl, 31);
-        const int64_t rec0 = off[(int32_t)(w << 5)];
+        const int64_t rec0 = off[2 * (w << 5)];
         for (int base = 0; base < total; base += 32) {  // warp-uniform trip count
             const int r = base + lane;
             int j = 0;
@@ -1777,7 +1800,7 @@ __global__ void k_pack_finish(const BuildArgs a)
 {
     BuildState *st = a.st;
     if (st->err) return;
-    const int32_t total = a.loff[st->n_nodes];
+    const int32_t total = a.loff[2 * (int64_t)st->n_nodes];
     if ((int64_t)total > a.cap.tris) {
         set_err(st, KDGB_ERR_CAPACITY, kErrPackCapacity);
         return;
@@ -1922,9 +1945,11 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.careas = w.careas.p;
     a.csets = w.csets.p;
     a.cap.low_R = INT64_MAX;  // the host sizes each lower level before it runs
-    a.lcnt = w.misc0.p;
+    a.norder = w.misc0.p;
     a.loff = w.misc1.p;
     a.tnode = t.tnode.p;
+    a.tbmin = t.tbmin.p;
+    a.tbmax = t.tbmax.p;
     a.ttri = t.ttri.p;
     a.cap.tris = t.ttri.cap / 3;
     return a;
@@ -2025,9 +2050,8 @@ int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, Wo
 // Leaf record counts, their scan and the recorded total.
 int emit_pack_counts(const BuildArgs &a, const Launcher &L, const Extents &e, Workspace &w, cudaStream_t s)
 {
-    k_leaf_counts<<<L.grid(e.nodes, kBlock), kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.info, a.amt, a.lcnt);
-    KDGB_LAUNCH_CHECK();
-    KDGB_CHECK(scan_exclusive<1>(a.lcnt, a.loff, e.nodes, s, &w.scan, &a.st->n_nodes, &a.st->err));
+    KDGB_CHECK((scan_exclusive_in<2, PackLanes>(PackLanes{a.info, a.amt}, a.loff, e.nodes, s, &w.scan,
+                                                &a.st->n_nodes, &a.st->err)));
     k_pack_finish<<<1, 1, 0, s>>>(a);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
@@ -2036,8 +2060,11 @@ int emit_pack_counts(const BuildArgs &a, const Launcher &L, const Extents &e, Wo
 int emit_pack(const BuildArgs &a, const Launcher &L, const Extents &e, cudaStream_t s)
 {
     const unsigned g = L.grid(e.nodes, kBlock);
-    k_pack_nodes<<<g, kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info, a.split, a.ch, a.loff,
-                                      a.tnode);
+    KDGB_CUDA(cudaMemsetAsync(a.norder, 0xff, sizeof(int32_t) * (size_t)std::max<int64_t>(e.nodes, 1), s));
+    k_pack_order<<<g, kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.M, a.info, a.ch, a.loff, a.norder);
+    KDGB_LAUNCH_CHECK();
+    k_pack_nodes<<<g, kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.M, a.info, a.split, a.bmin, a.bmax,
+                                      a.loff, a.norder, a.tnode, a.tbmin, a.tbmax);
     KDGB_LAUNCH_CHECK();
     k_pack_tris<<<L.grid(e.nodes, kBlock), kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info,
                                                                  a.amt, a.pidx,
@@ -2112,7 +2139,8 @@ void graph_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, const
     a.cap.leaves = t.leaf_ids.cap;
     a.cap.low_R = std::min({w.ssplit.cap, w.saddr.cap - 1, w.careas.cap, w.csets.cap});
     a.cap.fin = std::min({a.cap.fin, t.prim_indices.cap, w.areas.cap, w.sts.cap / 3});
-    a.cap.nodes = std::min({a.cap.nodes, w.misc0.cap, w.misc1.cap - 1, t.tnode.cap});
+    a.cap.nodes = std::min({a.cap.nodes, w.misc0.cap, w.misc1.cap / 2 - 1, t.tnode.cap, t.tbmin.cap, t.tbmax.cap,
+                            kMaxPackNodes - 1});
     a.use_cond = 1;
     e.N = std::min(a.cap.refs[0], a.cap.refs[1]);
     e.R = a.cap.R;
@@ -2135,7 +2163,7 @@ uint64_t layout_signature(const Tree &t)
     const Workspace &w = t.ws;
     MIX(t.p0); MIX(t.p1); MIX(t.p2); MIX(t.info); MIX(t.split); MIX(t.bmin); MIX(t.bmax); MIX(t.pidx);
     MIX(t.bitmap); MIX(t.parent); MIX(t.children); MIX(t.area); MIX(t.prim_indices); MIX(t.leaf_ids);
-    MIX(t.tnode); MIX(t.ttri); MIX(t.mesh_off);
+    MIX(t.tnode); MIX(t.tbmin); MIX(t.tbmax); MIX(t.ttri); MIX(t.mesh_off);
     MIX(w.rmin[0]); MIX(w.rmin[1]); MIX(w.rmax[0]); MIX(w.rmax[1]); MIX(w.fmin); MIX(w.fmax);
     MIX(w.keys); MIX(w.planes[0]); MIX(w.planes[1]); MIX(w.cnt); MIX(w.ess[0]); MIX(w.ess[1]); MIX(w.lbase);
     MIX(w.chunksum);
@@ -2175,27 +2203,31 @@ int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s)
 int pack_for_traversal(Tree &t, cudaStream_t s)
 {
     const int32_t n = t.n_nodes;
+    if ((int64_t)n >= kMaxPackNodes) return fail(KDGB_ERR_CAPACITY, "too many nodes for the traversal layout");
     Workspace &w = t.ws;
     KDGB_CHECK(host_record(w));
-    KDGB_CHECK(grab(w.misc0, n, s));
-    KDGB_CHECK(grab(w.misc1, (int64_t)n + 1, s));
+    KDGB_CHECK(grab(w.misc0, std::max<int64_t>(n, 1), s));
+    KDGB_CHECK(grab(w.misc1, 2 * ((int64_t)n + 1), s));
     const Launcher L{sm_count()};
-    int32_t *cnt = w.misc0.p, *off = w.misc1.p;
-    if (n > 0) {
-        k_leaf_counts<<<L.grid(n, kBlock), kBlock, 0, s>>>(n, nullptr, nullptr, t.info.p, t.bitmap.p, cnt);
-        KDGB_LAUNCH_CHECK();
-    }
-    KDGB_CHECK(scan_exclusive<1>(cnt, off, n, s, &w.scan));
-    KDGB_CUDA(cudaMemcpyAsync(w.host + kHostRec - 1, off + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    int32_t *norder = w.misc0.p, *off = w.misc1.p;
+    KDGB_CHECK((scan_exclusive_in<2, PackLanes>(PackLanes{t.info.p, t.bitmap.p}, off, n, s, &w.scan, nullptr,
+                                                nullptr)));
+    KDGB_CUDA(cudaMemcpyAsync(w.host + kHostRec - 1, off + 2 * (int64_t)n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     KDGB_CUDA(cudaStreamSynchronize(s));
     const int32_t total = w.host[kHostRec - 1];
     KDGB_CHECK(ensure(t.tnode, n, s));
+    KDGB_CHECK(ensure(t.tbmin, n, s));
+    KDGB_CHECK(ensure(t.tbmax, n, s));
     KDGB_CHECK(ensure(t.ttri, 3 * (int64_t)total, s));
     t.n_leaf_tris = total;
     if (n > 0) {
         const unsigned g = L.grid(n, kBlock);
-        k_pack_nodes<<<g, kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p, t.split.p, t.children.p, off,
-                                          t.tnode.p);
+        KDGB_CUDA(cudaMemsetAsync(norder, 0xff, sizeof(int32_t) * (size_t)n, s));
+        k_pack_order<<<g, kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.n_meshes, t.info.p, t.children.p, off,
+                                          norder);
+        KDGB_LAUNCH_CHECK();
+        k_pack_nodes<<<g, kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.n_meshes, t.info.p, t.split.p, t.bmin.p,
+                                          t.bmax.p, off, norder, t.tnode.p, t.tbmin.p, t.tbmax.p);
         KDGB_LAUNCH_CHECK();
         k_pack_tris<<<L.grid(n, kBlock), kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p,
                                                                         t.bitmap.p, t.pidx.p, t.prim_indices.p,
@@ -2303,8 +2335,9 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
 
     // Traversal layout: leaf records sized from the scanned leaf counts.
     const int64_t n = st.n_nodes;
-    KDGB_CHECK(grab(w.misc0, n, s));
-    KDGB_CHECK(grab(w.misc1, n + 1, s));
+    if (n >= kMaxPackNodes) return fail(KDGB_ERR_CAPACITY, "too many nodes for the traversal layout");
+    KDGB_CHECK(grab(w.misc0, std::max<int64_t>(n, 1), s));
+    KDGB_CHECK(grab(w.misc1, 2 * (n + 1), s));
     {
         const Extents e{0, 0, F, n, nl, 0};
         BuildArgs a = make_args(t, p, T, M, mesh_off_dev);
@@ -2312,6 +2345,8 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
         KDGB_CHECK(emit_pack_counts(a, L, e, w, s));
         KDGB_CHECK(fetch_state(t, st, s));
         KDGB_CHECK(ensure(t.tnode, n, s));
+        KDGB_CHECK(ensure(t.tbmin, n, s));
+        KDGB_CHECK(ensure(t.tbmax, n, s));
         KDGB_CHECK(ensure(t.ttri, 3 * (int64_t)st.n_leaf_tris, s));
         KDGB_CHECK(emit_pack(make_args(t, p, T, M, mesh_off_dev), L, e, s));
     }
@@ -2373,8 +2408,10 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.careas, low_R, s));
     KDGB_CHECK(ensure(w.csets, low_R, s));
     KDGB_CHECK(ensure(w.misc0, nodes, s));
-    KDGB_CHECK(ensure(w.misc1, nodes + 1, s));
+    KDGB_CHECK(ensure(w.misc1, 2 * (nodes + 1), s));
     KDGB_CHECK(ensure(t.tnode, nodes, s));
+    KDGB_CHECK(ensure(t.tbmin, nodes, s));
+    KDGB_CHECK(ensure(t.tbmax, nodes, s));
     KDGB_CHECK(ensure(t.ttri, 3 * tris, s));
     // Scan partials for the extents the capture will use.
     BuildArgs a;

@@ -148,9 +148,12 @@ struct Tree {
     DevArray<float> area;
     DevArray<int32_t> prim_indices, leaf_ids;
 
-    // Traversal layout: one 16-byte record per node and leaf-ordered
-    // triangle records (v0, e1, e2, id) of 48 bytes.
-    DevArray<int4> tnode;
+    // Traversal layout: one 8-byte record per node, in an order where the
+    // two children of a node are adjacent, the leaf boxes in that order (for
+    // leaf skipping), and leaf-ordered triangle records (v0, e1, e2, id) of
+    // 48 bytes.
+    DevArray<int2> tnode;
+    DevArray<float4> tbmin, tbmax;
     DevArray<float4> ttri;
 
     // Woop transform rows (m0, m1, m2) per triangle, computed on the first
@@ -228,6 +231,23 @@ struct NodeLanes {
         const int32_t l = cnt[2 * k], r = cnt[2 * k + 1];
         const int ll = l < LS, rl = r < LS;
         v[0] = l; v[1] = r; v[2] = ll ? l : 0; v[3] = rl ? r : 0; v[4] = ll; v[5] = rl; v[6] = ess[*level & 1][k];
+    }
+#endif
+};
+
+// The two per-node lanes of the traversal pack: the node's leaf records
+// (its bitmap's members when it is a leaf, else 0) and whether it is an
+// interior node.  Their exclusive scans give each leaf its first record and
+// each interior node its rank, which places its children.
+struct PackLanes {
+    const int8_t *info;
+    const int32_t *bitmap;
+#ifdef __CUDACC__
+    __device__ __forceinline__ void load(int64_t k, int32_t (&v)[2]) const
+    {
+        const bool leaf = (info[k] & 3) == KDGB_LEAF;
+        v[0] = leaf ? __popc((unsigned)bitmap[k]) : 0;
+        v[1] = leaf ? 0 : 1;
     }
 #endif
 };

@@ -328,6 +328,8 @@ template int scan_exclusive_in<2, ScanArray<2>>(const ScanArray<2> &, int32_t *,
                                              DevArray<int32_t> *, const int32_t *, int32_t *);
 template int scan_exclusive_in<7, ScanArray<7>>(const ScanArray<7> &, int32_t *, int64_t, cudaStream_t,
                                              DevArray<int32_t> *, const int32_t *, int32_t *);
+template int scan_exclusive_in<2, PackLanes>(const PackLanes &, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *,
+                                          const int32_t *, int32_t *);
 template int scan_exclusive_in<7, NodeLanes>(const NodeLanes &, int32_t *, int64_t, cudaStream_t, DevArray<int32_t> *,
                                           const int32_t *, int32_t *);
 

@@ -10,13 +10,14 @@
 // (IRayTracer.h:147-168).  Divisions are IEEE (__frcp_rn), products and sums
 // separately rounded, so hit ids match the CPU restatement bit for bit.
 //
-// Memory layout read by the tracers (built by the pack kernels of kdgb_build.cu):
-//   tnode[i]  int4  interior: {split bits, left, right, axis}
-//                   leaf:     {first record, record count, 0, 0}
+// Memory layout read by the tracers (built by the pack kernels of kdgb_build.cu),
+// in traversal order, where the two children of a node are adjacent:
+//   tnode[j]  int2  interior: {split bits, (left << 2) | axis}, right = left + 1
+//                   leaf:     {first record, (record count << 2) | 0}
 //   ttri[3r..3r+2]  float4 x3 per leaf record, in leaf order:
 //                   {v0.xyz, e1.x} {e1.yz, e2.xy} {e2.z, id bits, 0, 0}
-//   bmin/bmax       float4 node boxes (leaf skipping)
-// One 16-byte load per traversal step and three 16-byte loads per triangle
+//   bmin/bmax       float4 leaf boxes in the same order (leaf skipping)
+// One 8-byte load per traversal step and three 16-byte loads per triangle
 // test, with no index indirection; e1 = v1 - v0 and e2 = v2 - v0 are the
 // same fp32 values the reference computes per test.
 #include <cuda_runtime.h>
@@ -38,13 +39,20 @@ constexpr int kDefaultMaxIterations = 1 << 22;
 inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
 struct Ctx {
-    const int4 *__restrict__ node;
+    const int2 *__restrict__ node;
     const float4 *__restrict__ bmin;
     const float4 *__restrict__ bmax;
     const float4 *__restrict__ tri;
     const float4 *__restrict__ woop;  // per-triangle Woop values, or NULL for Moeller-Trumbore
     int root;  // root node of the ray's tree (forest of a batch: its mesh index)
 };
+
+// Fields of a tnode record.
+__device__ __forceinline__ int node_axis(int2 nd) { return nd.y & 3; }
+__device__ __forceinline__ int node_left(int2 nd) { return nd.y >> 2; }
+__device__ __forceinline__ float node_split(int2 nd) { return __int_as_float(nd.x); }
+__device__ __forceinline__ int32_t leaf_first(int2 nd) { return nd.x; }
+__device__ __forceinline__ int32_t leaf_count(int2 nd) { return nd.y >> 2; }
 
 // True when x = RN(RN(1/det) * n) is certainly negative and nonzero:
 // det and n have opposite signs, n != 0, and |det| <= 2^64, |n| >= 2^-64 so
@@ -144,17 +152,17 @@ __device__ __forceinline__ void woop_test(const float4 *__restrict__ w, int id, 
     if (0.0f <= lambda && lambda <= tb) woop_accept(lambda, __ldg(w), __ldg(w + 1), id, o, d, tie, hit, tb, ub, vb);
 }
 
-__device__ __forceinline__ int leaf_test(const Ctx &c, int4 leaf, float3 o, float3 d, int tie, float &tb, float &ub,
+__device__ __forceinline__ int leaf_test(const Ctx &c, int2 leaf, float3 o, float3 d, int tie, float &tb, float &ub,
                                          float &vb)
 {
     int hit = -1;
     if (c.woop) {
-        for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) {
+        for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) {
             const int id = __float_as_int(__ldg(c.tri + 3 * (int64_t)r + 2).y);
             woop_test(c.woop + 3 * (int64_t)id, id, o, d, tie, hit, tb, ub, vb);
         }
     } else {
-        for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) mt_record(c.tri, r, o, d, tie, hit, tb, ub, vb);
+        for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) mt_record(c.tri, r, o, d, tie, hit, tb, ub, vb);
     }
     return hit;
 }
@@ -162,18 +170,18 @@ __device__ __forceinline__ int leaf_test(const Ctx &c, int4 leaf, float3 o, floa
 // Whether any triangle of the leaf is hit within [0, tb] (the reference's
 // shadow test, REF_LAST acceptance): the first accepted triangle settles it,
 // so the loop stops there with the result testing all of them gives.
-__device__ __forceinline__ bool leaf_any(const Ctx &c, int4 leaf, float3 o, float3 d, float tb)
+__device__ __forceinline__ bool leaf_any(const Ctx &c, int2 leaf, float3 o, float3 d, float tb)
 {
     int hit = -1;
     float ub = 0.0f, vb = 0.0f;
     if (c.woop) {
-        for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) {
+        for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) {
             const int id = __float_as_int(__ldg(c.tri + 3 * (int64_t)r + 2).y);
             woop_test(c.woop + 3 * (int64_t)id, id, o, d, KDGB_TIE_REF_LAST, hit, tb, ub, vb);
             if (hit != -1) return true;
         }
     } else {
-        for (int32_t r = leaf.x; r < leaf.x + leaf.y; ++r) {
+        for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) {
             mt_record(c.tri, r, o, d, KDGB_TIE_REF_LAST, hit, tb, ub, vb);
             if (hit != -1) return true;
         }
@@ -234,18 +242,19 @@ __host__ __device__ __forceinline__ int stack_entries(int tracer, int depth)
 // Descends from `node` (record nd) to a leaf, as the reference's kd-restart
 // loop does (Raytracer.cu:73-86); near decisions are remembered in m when
 // given.
-__device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 inv, float tmin, int &node, int4 &nd,
+__device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 inv, float tmin, int &node, int2 &nd,
                                                 float &tnext, Memo *m)
 {
-    while (nd.w != KDGB_LEAF) {
-        const float ori = axis_of(o, nd.w), dir = axis_of(inv, nd.w);
-        const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
+    while (node_axis(nd) != KDGB_LEAF) {
+        const int ax = node_axis(nd), left = node_left(nd);
+        const float ori = axis_of(o, ax), dir = axis_of(inv, ax);
+        const float ts = __fmul_rn(__fsub_rn(node_split(nd), ori), dir);
         if (tmin < ts) {
             tnext = kmin(ts, tnext);
             if (m) m->push(node, tnext);
-            node = 0 < dir ? nd.y : nd.z;
+            node = 0 < dir ? left : left + 1;
         } else {
-            node = 0 < dir ? nd.z : nd.y;
+            node = 0 < dir ? left + 1 : left;
         }
         nd = __ldg(c.node + node);
     }
@@ -255,7 +264,7 @@ __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 i
 // remembered near decision whose distance is <= tmin (prefix minima fall
 // with depth, so it is the first entry whose minimum is <= tmin), or the
 // root.
-__device__ __forceinline__ void restart_from(const Ctx &c, float3 inv, float tmin, int &node, int4 &nd, float &tnext,
+__device__ __forceinline__ void restart_from(const Ctx &c, float3 inv, float tmin, int &node, int2 &nd, float &tnext,
                                              Memo *m)
 {
     if (m && m->cnt > 0 && tmin < m->base) {
@@ -268,7 +277,7 @@ __device__ __forceinline__ void restart_from(const Ctx &c, float3 inv, float tmi
         tnext = lo > 0 ? __int_as_float(m->at(lo - 1).y) : m->base;
         m->cnt = lo;
         nd = __ldg(c.node + e.x);
-        node = 0 < axis_of(inv, nd.w) ? nd.z : nd.y;
+        node = node_left(nd) + (0 < axis_of(inv, node_axis(nd)) ? 1 : 0);
         nd = __ldg(c.node + node);
         return;
     }
@@ -296,7 +305,7 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
     memo.reset();
     Memo *m = mem ? &memo : nullptr;
     int node = c.root;
-    int4 nd = __ldg(c.node + c.root);
+    int2 nd = __ldg(c.node + c.root);
     float tnext = KDGB_FINF;
     do {
         restart_descend(c, o, inv, tmin, node, nd, tnext, m);
@@ -349,13 +358,14 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
             node = e.x;
             tnext = __int_as_float(e.y);
         }
-        int4 nd = __ldg(c.node + node);
+        int2 nd = __ldg(c.node + node);
         d = fixed ? inv1 : inv3(d);
-        while (nd.w != KDGB_LEAF) {
-            const float ori = axis_of(o, nd.w), dir = axis_of(d, nd.w);
-            const float ts = __fmul_rn(__fsub_rn(__int_as_float(nd.x), ori), dir);
-            const int lower = 0 < dir ? nd.y : nd.z;
-            const int upper = 0 < dir ? nd.z : nd.y;
+        while (node_axis(nd) != KDGB_LEAF) {
+            const int ax = node_axis(nd), left = node_left(nd);
+            const float ori = axis_of(o, ax), dir = axis_of(d, ax);
+            const float ts = __fmul_rn(__fsub_rn(node_split(nd), ori), dir);
+            const int lower = 0 < dir ? left : left + 1;
+            const int upper = 0 < dir ? left + 1 : left;
             if (th < ts) {
                 node = lower;
                 if (ts < tnext) {
@@ -403,7 +413,7 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 
     memo.reset();
     Memo *m = mem ? &memo : nullptr;
     int node = c.root;
-    int4 nd = __ldg(c.node + c.root);
+    int2 nd = __ldg(c.node + c.root);
     float tnext = KDGB_FINF;
     do {
         restart_descend(c, lp, inv, tmin, node, nd, tnext, m);
@@ -924,8 +934,8 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
 {
     TraceArgs a;
     a.c.node = t.tnode.p;
-    a.c.bmin = t.bmin.p;
-    a.c.bmax = t.bmax.p;
+    a.c.bmin = t.tbmin.p;
+    a.c.bmax = t.tbmax.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
     KDGB_CHECK(woop_for(t, p, s, a.c));
@@ -974,8 +984,8 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
 {
     TraceArgs a;
     a.c.node = t.tnode.p;
-    a.c.bmin = t.bmin.p;
-    a.c.bmax = t.bmax.p;
+    a.c.bmin = t.tbmin.p;
+    a.c.bmax = t.tbmax.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
     KDGB_CHECK(woop_for(t, p, s, a.c));
@@ -1013,8 +1023,8 @@ int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_p
 {
     PhotonArgs a;
     a.c.node = t.tnode.p;
-    a.c.bmin = t.bmin.p;
-    a.c.bmax = t.bmax.p;
+    a.c.bmin = t.tbmin.p;
+    a.c.bmax = t.tbmax.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
     KDGB_CHECK(woop_for(t, p, s, a.c));
@@ -1054,8 +1064,8 @@ int shade_launch(const Tree &t, const kdgb_trace_params &p, const float *n0, con
 {
     ShadeArgs a;
     a.c.node = t.tnode.p;
-    a.c.bmin = t.bmin.p;
-    a.c.bmax = t.bmax.p;
+    a.c.bmin = t.tbmin.p;
+    a.c.bmax = t.tbmax.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
     KDGB_CHECK(woop_for(t, p, s, a.c));
