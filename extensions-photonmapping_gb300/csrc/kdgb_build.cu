@@ -1023,21 +1023,30 @@ __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_scatter(const BuildA
                     keys_merge(ar, kr);
                     continue;
                 }
+                // Parents do not decrease along the references, so a row that
+                // leaves the run holds: the run's parent first (its lanes add
+                // to the run before it is flushed), whole parents in between
+                // (reduced and flushed here), and the row's last parent, which
+                // starts the next run.
+                if (run >= 0 && owner == run) {
+                    keys_merge(al, kl);
+                    keys_merge(ar, kr);
+                }
                 if (run >= 0) {
                     keys_reduce(kFull, al);
                     keys_reduce(kFull, ar);
                     if (lane == 0) child_keys_atomic(a, R, run, al, ar);
                 }
-                if (m == kFull && owner >= 0) {
-                    run = owner;
+                const int last = __shfl_sync(kFull, owner, 31);
+                if (owner >= 0 && owner != run && owner != last) {
+                    keys_reduce(m, kl);
+                    keys_reduce(m, kr);
+                    if (lane == (unsigned)(__ffs(m) - 1)) child_keys_atomic(a, R, owner, kl, kr);
+                }
+                run = last >= 0 && last != run ? last : -1;
+                if (run >= 0 && owner == run) {
                     for (int j = 0; j < 6; ++j) { al[j] = kl[j]; ar[j] = kr[j]; }
                 } else {
-                    if (owner >= 0) {
-                        keys_reduce(m, kl);
-                        keys_reduce(m, kr);
-                        if (lane == (unsigned)(__ffs(m) - 1)) child_keys_atomic(a, R, owner, kl, kr);
-                    }
-                    run = -1;
                     keys_neutral(al);
                     keys_neutral(ar);
                 }
