@@ -570,19 +570,30 @@ __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_count(const BuildArg
                 ar += Rf;
                 continue;
             }
+            // As in k_scatter: the run's lanes add to it before it is
+            // flushed, whole parents in between are flushed here, and the
+            // row's last parent starts the next run.
+            if (cw >= 0 && o == cw) {
+                al += L;
+                ar += Rf;
+            }
             if (cw >= 0) {
                 al = __reduce_add_sync(kFull, al);
                 ar = __reduce_add_sync(kFull, ar);
                 if (lane == 0) { atomicAdd(cnt + 2 * cw, al); atomicAdd(cnt + 2 * cw + 1, ar); }
             }
-            if (m == kFull && o >= 0) {
-                cw = o; al = L; ar = Rf;
+            const int last = __shfl_sync(kFull, o, 31);
+            if (o >= 0 && o != cw && o != last) {
+                const int gl = __reduce_add_sync(m, L), gr = __reduce_add_sync(m, Rf);
+                if (lane == (unsigned)(__ffs(m) - 1)) { atomicAdd(cnt + 2 * o, gl); atomicAdd(cnt + 2 * o + 1, gr); }
+            }
+            cw = last >= 0 && last != cw ? last : -1;
+            if (cw >= 0 && o == cw) {
+                al = L;
+                ar = Rf;
             } else {
-                if (o >= 0) {
-                    const int gl = __reduce_add_sync(m, L), gr = __reduce_add_sync(m, Rf);
-                    if (lane == (unsigned)(__ffs(m) - 1)) { atomicAdd(cnt + 2 * o, gl); atomicAdd(cnt + 2 * o + 1, gr); }
-                }
-                cw = -1; al = 0; ar = 0;
+                al = 0;
+                ar = 0;
             }
         }
         if (cw >= 0) {
