@@ -1232,58 +1232,58 @@ __global__ void k_children(const BuildArgs a)
     const int32_t empty = tot[6];
     const int32_t child_start = base + empty;
     const int32_t total_l = tot[0], leaf_l = tot[2], ln_l = tot[4], leaf_nodes = tot[4] + tot[5];
-    GRID_STRIDE(k64, R) {
-        const int32_t k = (int32_t)k64;
+    // Two threads per active node, one per child: the dependent chain of
+    // node-record loads and stores is halved, which is what bounds the deep
+    // levels (few nodes, latency-bound).  The left thread also links the
+    // children and builds the node's empty-space chain.
+    GRID_STRIDE(i64, 2 * (int64_t)R) {
+        const int32_t k = (int32_t)(i64 >> 1);
+        const bool right = i64 & 1;
         const int32_t *lb = a.lbase + kLanes * (int64_t)k;
         const int32_t *nb = a.lbase + kLanes * (int64_t)(k + 1);
-        if (ess) {
-            const int pl = planes[k];
-            if (pl) ess_chain(a, k, active, base + lb[6], pl);
-        }
-        const int32_t l = nb[0] - lb[0], r = nb[1] - lb[1];
         const int32_t par = active + k;
-
-        const bool lleaf = l < LS;
-        const int32_t la = lb[4];
-        const int32_t lnext = k - la;
+        const int32_t la = lb[4], ra = ln_l + lb[5];
+        const int32_t l = nb[0] - lb[0], r = nb[1] - lb[1];
+        const bool lleaf = l < LS, rleaf = r < LS;
+        const int32_t lnext = k - la, rnext = (R + k) - ra;
         const int32_t lid = child_start + (lleaf ? la : lnext + leaf_nodes);
-        const bool rleaf = r < LS;
-        const int32_t ra = ln_l + lb[5];
-        const int32_t rnext = (R + k) - ra;
         const int32_t rid = child_start + (rleaf ? ra : rnext + leaf_nodes);
-
-        ZERO_NODE(lid);
-        ZERO_NODE(rid);
-        a.pidx[lid] = lleaf ? upper + lb[2] : lb[0] - lb[2];
-        a.pidx[rid] = rleaf ? upper + leaf_l + lb[3] : (total_l - leaf_l) + (lb[1] - lb[3]);
-        a.amt[lid] = l;
-        a.amt[rid] = r;
-        a.parent[lid] = par;
-        a.parent[rid] = par;
-        a.ch[par] = make_int2(lid, rid);
-        float4 lmin = make_float4(0.f, 0.f, 0.f, 0.f), lmax = lmin, rmin = lmin, rmax = lmin;
+        if (!right) {
+            if (ess) {
+                const int pl = planes[k];
+                if (pl) ess_chain(a, k, active, base + lb[6], pl);
+            }
+            a.ch[par] = make_int2(lid, rid);
+        }
+        const int32_t id = right ? rid : lid;
+        const bool leaf = right ? rleaf : lleaf;
+        const int32_t next = right ? rnext : lnext;
+        ZERO_NODE(id);
+        a.pidx[id] = right ? (rleaf ? upper + leaf_l + lb[3] : (total_l - leaf_l) + (lb[1] - lb[3]))
+                           : (lleaf ? upper + lb[2] : lb[0] - lb[2]);
+        a.amt[id] = right ? r : l;
+        a.parent[id] = par;
+        float4 cmin = make_float4(0.f, 0.f, 0.f, 0.f), cmax = cmin;
         if (a.ess) {  // PropagateAabbToChildren runs with empty-space splitting
             const int axis = a.info[par] & 3;
             const float sp = a.split[par];
             const float4 mn = a.bmin[par], mx = a.bmax[par];
-            lmin = mn;
-            rmin = make_float4(axis == KDGB_X ? sp : mn.x, axis == KDGB_Y ? sp : mn.y, axis == KDGB_Z ? sp : mn.z, 0.0f);
-            lmax = make_float4(axis == KDGB_X ? sp : mx.x, axis == KDGB_Y ? sp : mx.y, axis == KDGB_Z ? sp : mx.z, 0.0f);
-            rmax = mx;
-            a.bmin[lid] = lmin;
-            a.bmin[rid] = rmin;
-            a.bmax[lid] = lmax;
-            a.bmax[rid] = rmax;
+            if (right) {
+                cmin = make_float4(axis == KDGB_X ? sp : mn.x, axis == KDGB_Y ? sp : mn.y, axis == KDGB_Z ? sp : mn.z,
+                                   0.0f);
+                cmax = mx;
+            } else {
+                cmin = mn;
+                cmax = make_float4(axis == KDGB_X ? sp : mx.x, axis == KDGB_Y ? sp : mx.y, axis == KDGB_Z ? sp : mx.z,
+                                   0.0f);
+            }
+            a.bmin[id] = cmin;
+            a.bmax[id] = cmax;
         }
-        if (!lleaf) {
-            a.cnt[2 * lnext] = 0;
-            a.cnt[2 * lnext + 1] = 0;
-            node_split_one(a, lnext, lid, a.ess, lmin, lmax, sah_next, planes_next, ess_next);
-        }
-        if (!rleaf) {
-            a.cnt[2 * rnext] = 0;
-            a.cnt[2 * rnext + 1] = 0;
-            node_split_one(a, rnext, rid, a.ess, rmin, rmax, sah_next, planes_next, ess_next);
+        if (!leaf) {
+            a.cnt[2 * next] = 0;
+            a.cnt[2 * next + 1] = 0;
+            node_split_one(a, next, id, a.ess, cmin, cmax, sah_next, planes_next, ess_next);
         }
     }
     if (last_block(st)) advance_upper(a, st);
@@ -1998,7 +1998,6 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
                      cudaStream_t s)
 {
     const unsigned gN = L.grid(e.N, kTileRefs);
-    const unsigned gR = L.grid(e.R, kBlock, 2);
     if (tuned_levels) {
         // Enough blocks for one per large node and one warp per node.
         const int64_t big = ceil_div(e.N, kSahBlockRefs);  // at least the large nodes
@@ -2020,7 +2019,7 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
         else k_scatter<false><<<gN, kBlock, 0, s>>>(a);
         KDGB_LAUNCH_CHECK();
     }
-    k_children<<<gR, kBlock, 0, s>>>(a);
+    k_children<<<L.grid(2 * e.R, kBlock, 2), kBlock, 0, s>>>(a);  // a thread per child
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
