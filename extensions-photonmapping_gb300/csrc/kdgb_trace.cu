@@ -470,10 +470,16 @@ struct TraceArgs {
 // A shadow ray waiting in a block's queue: the hit point, the tree root and
 // the ray it belongs to.
 struct ShadowItem {
-    float4 p;  // w = root bits
-    int64_t ray;
-    int64_t pad;
+    float4 p;  // w = bits of the block thread whose primary ray hit there
 };
+
+// The mesh (forest root) of ray i of a batch (the tree's root otherwise).
+__device__ __forceinline__ int ray_mesh_of(const TraceArgs &a, int64_t i)
+{
+    if (!a.mesh_off) return a.c.root;
+    const int m = a.ray_mesh ? a.ray_mesh[i] : (int)(i / a.rays_per_mesh);
+    return m < 0 ? 0 : (m >= a.n_meshes ? a.n_meshes - 1 : m);
+}
 
 // Dynamic shared memory: the per-thread regions of stack_entries() int2
 // (short stack or remembered descents) followed, with shadow rays, by a
@@ -509,10 +515,8 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
         d = ld3(a.d, i);
         int32_t id_off = 0;
         if (a.mesh_off) {
-            int m = a.ray_mesh ? a.ray_mesh[i] : (int)(i / a.rays_per_mesh);
-            m = m < 0 ? 0 : (m >= a.n_meshes ? a.n_meshes - 1 : m);
-            c.root = m;
-            id_off = a.mesh_off[m];
+            c.root = ray_mesh_of(a, i);
+            id_off = a.mesh_off[c.root];
         }
         if (TRACER == KDGB_TRACER_SHORTSTACK)
             h = trace_shortstack<SKIP>(c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u,
@@ -536,17 +540,17 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
             const float3 p = make_float3(__fadd_rn(o.x, __fmul_rn(t, d.x)), __fadd_rn(o.y, __fmul_rn(t, d.y)),
                                          __fadd_rn(o.z, __fmul_rn(t, d.z)));
             const int slot = atomicAdd(&s_count, 1);
-            queue[slot].p = make_float4(p.x, p.y, p.z, __int_as_float(c.root));
-            queue[slot].ray = i;
+            queue[slot].p = make_float4(p.x, p.y, p.z, __int_as_float((int)threadIdx.x));
         } else if (live) {
             a.occ[i] = 0;
         }
         __syncthreads();
         if ((int)threadIdx.x < s_count) {
             const ShadowItem q = queue[threadIdx.x];
+            const int64_t ray = ray_index((int64_t)blockIdx.x * blockDim.x + __float_as_int(q.p.w), a.tile_width);
             Ctx cs = a.c;
-            cs.root = __float_as_int(q.p.w);
-            a.occ[q.ray] = trace_shadow(cs, a.light, make_float3(q.p.x, q.p.y, q.p.z), a.maxit,
+            cs.root = ray_mesh_of(a, ray);
+            a.occ[ray] = trace_shadow(cs, a.light, make_float3(q.p.x, q.p.y, q.p.z), a.maxit,
                                         stack_smem + threadIdx.x, blockDim.x,
                                         memo_cap(stack_entries(TRACER, a.depth)));
         }
