@@ -364,8 +364,8 @@ def run_frame(args, world, rank, local, pg):
             "peak_source": f"{peak_kind} hbm_gbs",
             # The traversal is bound by issue and latency, not by HBM: these
             # are the ncu figures of the committed profile of this kernel.
-            "limiter": "issue/latency (ncu: 71% of issue slots active, 16.4 of 32 lanes per warp instruction, "
-                       "L1 hit 68%, L2 hit 83%)"}
+            "limiter": "issue/latency (ncu: 73% of issue slots active, 16.5 of 32 lanes per warp instruction, "
+                       "L1 hit 67%, L2 hit 83%)"}
     if traffic:
         roof["traffic_source"] = traffic.get("source")
 
