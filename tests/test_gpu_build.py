@@ -101,6 +101,17 @@ def test_tuned_build_options(kdgb_lib, cuda, oracle, opts):
         assert_same_tree(tree.to_host(), ref)
 
 
+def test_tuned_build_large_nodes(kdgb_lib, cuda, oracle):
+    """Binned SAH from level 2 of a 300k-triangle scene: nodes of about 75k
+    references are binned in 2048-reference chunks by many blocks, whose
+    histograms meet in global memory; the tree must still be the oracle's."""
+    kw = dict(TUNED, upper_levels=2)
+    tris = scenes.clustered(300000, seed=23)
+    ref = oracle.build(tris, **kw)
+    with kdgb_lib.KDTree.build(tris, **kw) as tree:
+        assert_same_tree(tree.to_host(), ref)
+
+
 @pytest.mark.parametrize("name", ["c1", "clustered3k", "clustered60k", "soup", "degenerate"])
 @pytest.mark.parametrize("lower", [0, 2])
 def test_divide_build_matches_oracle(kdgb_lib, cuda, oracle, name, lower):

@@ -14,7 +14,9 @@ FIELDS = ("info", "split", "children", "prim_index", "bitmap", "parent", "area",
 SAH_C1 = dict(lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
 TUNED = dict(SAH_C1, mode=1, upper_levels=8, sah_bins=16)
 CONFIGS = {"bitmap": dict(), "sah": SAH_C1, "tuned": TUNED, "no_ess": dict(split_empty_space=0),
-           "balanced_divide": dict(lower=2, split_method=1)}
+           "balanced_divide": dict(lower=2, split_method=1),
+           # binned SAH from level 1: nodes of ~10k references binned in chunks by several blocks
+           "tuned_sah_from_level1": dict(SAH_C1, mode=1, upper_levels=1, sah_bins=32)}
 
 
 def assert_same_tree(a, b):
