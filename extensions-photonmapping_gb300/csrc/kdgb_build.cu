@@ -1389,65 +1389,6 @@ __global__ void k_sah_preprocess(const BuildArgs a)
     }
 }
 
-// CreateSplittingPlanes (LowerTriangleMap.h:84-155): one warp per node, lane
-// i owns reference slot i.  Sets per axis: {lowLeft, lowRight, highLeft,
-// highRight} of the planes at slot i's box low / high.
-// The members' boxes are staged in shared memory and read back as
-// broadcasts, four members per step, so each member costs two loads instead
-// of six shuffles.
-__global__ void k_sah_planes(const BuildArgs a)
-{
-    __shared__ float4 s_lo[kWarps][32], s_hi[kWarps][32];
-    const BuildState *st = a.st;
-    if (st->err) return;
-    const int64_t F = st->F;
-    const int lane = threadIdx.x & 31, warp = (threadIdx.x >> 5) & (kWarps - 1);
-    WARP_STRIDE(gw, st->n_leaf_ids) {
-        const int32_t leaf = a.leaf_ids[gw];
-        const int32_t pi = a.pidx[leaf];
-        const unsigned bmp = (unsigned)a.amt[leaf];
-        const bool mine = (bmp >> lane) & 1u;
-        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
-        if (mine) { lo = a.fmin[pi + lane]; hi = a.fmax[pi + lane]; }
-        s_lo[warp][lane] = lo;
-        s_hi[warp][lane] = hi;
-        __syncwarp();
-        unsigned sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sz[4] = {0, 0, 0, 0};
-        for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; four members per step
-            int jj[4];
-            unsigned mm[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                jj[q] = bits ? __ffs(bits) - 1 : 0;
-                mm[q] = bits ? 1u << jj[q] : 0u;
-                bits &= bits - 1u;
-            }
-            float4 mn[4], mx[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                mn[q] = s_lo[warp][jj[q]];
-                mx[q] = s_hi[warp][jj[q]];
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const unsigned m = mm[q];
-                sx[0] |= mn[q].x <= lo.x ? m : 0; sx[1] |= lo.x < mx[q].x ? m : 0;
-                sx[2] |= mn[q].x <= hi.x ? m : 0; sx[3] |= hi.x < mx[q].x ? m : 0;
-                sy[0] |= mn[q].y <= lo.y ? m : 0; sy[1] |= lo.y < mx[q].y ? m : 0;
-                sy[2] |= mn[q].y <= hi.y ? m : 0; sy[3] |= hi.y < mx[q].y ? m : 0;
-                sz[0] |= mn[q].z <= lo.z ? m : 0; sz[1] |= lo.z < mx[q].z ? m : 0;
-                sz[2] |= mn[q].z <= hi.z ? m : 0; sz[3] |= hi.z < mx[q].z ? m : 0;
-            }
-        }
-        if (mine) {
-            a.sts[pi + lane] = make_int4(sx[0], sx[1], sx[2], sx[3]);
-            a.sts[F + pi + lane] = make_int4(sy[0], sy[1], sy[2], sy[3]);
-            a.sts[2 * F + pi + lane] = make_int4(sz[0], sz[1], sz[2], sz[3]);
-        }
-        __syncwarp();  // the staged boxes are rewritten by the warp's next node
-    }
-}
-
 // The first SAH lower level is the set of upper leaves.
 __global__ void k_lower_begin(const BuildArgs a)
 {
@@ -1489,20 +1430,153 @@ __device__ __forceinline__ void pick_planes(const unsigned (&s)[4], const float 
     }
 }
 
-// CalcSAH (LowerTriangleMap.h:463-555), one warp per node: lane i evaluates
-// the six planes of slot i in the reference's order; the warp keeps the
-// first minimum in (slot, axis, low/high) order.
+// The plane costs of one lower node by its warp (CalcSAH, LowerTriangleMap.h:463-555): lane i holds member
+// slot i's sets (sx, sy, sz: {lowLeft, lowRight, highLeft, highRight} per axis; only members' lanes are read)
+// and evaluates the six planes of its slot in the reference's order; the warp keeps the first minimum in
+// (slot, axis, low/high) order and decides the split.
+__device__ __forceinline__ void sah_eval_node(const BuildArgs &a, int64_t gw, int32_t par, int32_t pi, unsigned bmp,
+                                              int lane, const int4 &sx, const int4 &sy, const int4 &sz)
+{
+    const float ct = a.ct, ci = a.ci;
+    const bool mine = (bmp >> lane) & 1u;
+    const float a_lane = mine ? a.areas[pi + lane] : 0.0f;
+    SahPick mb;
+    mb.cost = KDGB_FINF; mb.la = mb.ra = 0.0f; mb.ls = mb.rs = 0; mb.axis = 0; mb.idx = 0;
+    // One pass over the node's references in bit order accumulates the
+    // area sums of all twelve sets (3 axes x {lowLeft, lowRight, highLeft,
+    // highRight}).
+    unsigned sets[3][4] = {{(unsigned)sx.x & bmp, (unsigned)sx.y & bmp, (unsigned)sx.z & bmp, (unsigned)sx.w & bmp},
+                           {(unsigned)sy.x & bmp, (unsigned)sy.y & bmp, (unsigned)sy.z & bmp, (unsigned)sy.w & bmp},
+                           {(unsigned)sz.x & bmp, (unsigned)sz.y & bmp, (unsigned)sz.z & bmp, (unsigned)sz.w & bmp}};
+    float ar[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    // Only members are added (predicated adds): skipping a +0 term is
+    // exact, so the sums equal the reference's bit-order accumulation.
+    for (unsigned bits = bmp; bits; bits &= bits - 1u) {  // bmp is warp-uniform
+        const int j = __ffs(bits) - 1;
+        const float aj = __shfl_sync(kFull, a_lane, j);
+        const unsigned m = 1u << j;
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (sets[x][c] & m) ar[x][c] = __fadd_rn(ar[x][c], aj);
+    }
+    pick_planes(sets[0], ar[0], KDGB_X, pi + lane, mb);
+    pick_planes(sets[1], ar[1], KDGB_Y, pi + lane, mb);
+    pick_planes(sets[2], ar[2], KDGB_Z, pi + lane, mb);
+    // Warp argmin on (cost, lane); only lanes whose cost beat fInfinity count.
+    float c = mine && mb.cost < KDGB_FINF ? mb.cost : INFINITY;
+    int owner = mine && mb.cost < KDGB_FINF ? lane : 32;
+    for (int o = 16; o > 0; o >>= 1) {
+        const float c2 = __shfl_xor_sync(kFull, c, o);
+        const int w2 = __shfl_xor_sync(kFull, owner, o);
+        if (c2 < c || (c2 == c && w2 < owner)) { c = c2; owner = w2; }
+    }
+    if (lane == (owner < 32 ? owner : 0)) {
+        const int cnt = __popc(bmp);
+        const float opt = owner < 32 ? mb.cost : KDGB_FINF;
+        const float node_area = a.area[par];
+        bool split_it = __fmul_rn(ci, opt) < __fmul_rn(__fsub_rn(__fmul_rn(ci, (float)cnt), ct), node_area);
+        if (cnt <= a.min_leaf) split_it = false;
+        if (split_it) {
+            a.careas[gw] = make_float2(mb.la, mb.ra);
+            a.csets[gw] = make_int2((int)mb.ls, (int)mb.rs);
+            const float4 sp4 = ((unsigned)mb.idx & 0x80000000u) ? a.fmax[(unsigned)mb.idx ^ 0x80000000u]
+                                                                 : a.fmin[mb.idx];
+            a.split[par] = axis_of4(sp4, mb.axis);
+        }
+        a.info[par] = split_it ? (int8_t)mb.axis : (int8_t)KDGB_LEAF;
+        a.ssplit[gw] = split_it;
+    }
+}
+
+// CreateSplittingPlanes (LowerTriangleMap.h:84-155): one warp per node, lane
+// i owns reference slot i.  Sets per axis: {lowLeft, lowRight, highLeft,
+// highRight} of the planes at slot i's box low / high.
+// The members' boxes are staged in shared memory and read back as
+// broadcasts, four members per step, so each member costs two loads instead
+// of six shuffles.  With the SAH creator the warp then evaluates the first
+// lower level's plane costs for its node (k_calc_sah does the later levels).
+__global__ void k_sah_planes(const BuildArgs a)
+{
+    __shared__ float4 s_lo[kWarps][32], s_hi[kWarps][32];
+    const BuildState *st = a.st;
+    if (st->err) return;
+    const int64_t F = st->F;
+    const int lane = threadIdx.x & 31, warp = (threadIdx.x >> 5) & (kWarps - 1);
+    // With the SAH lower creator the warp also evaluates the node's planes
+    // (the first lower level; k_lower_begin checks the same capacity).
+    const bool first_sah = a.lower == KDGB_LOWER_SAH && (int64_t)st->n_leaf_ids <= a.cap.low_R;
+    WARP_STRIDE(gw, st->n_leaf_ids) {
+        const int32_t leaf = a.leaf_ids[gw];
+        const int32_t pi = a.pidx[leaf];
+        const unsigned bmp = (unsigned)a.amt[leaf];
+        const bool mine = (bmp >> lane) & 1u;
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+        if (mine) { lo = a.fmin[pi + lane]; hi = a.fmax[pi + lane]; }
+        s_lo[warp][lane] = lo;
+        s_hi[warp][lane] = hi;
+        __syncwarp();
+        unsigned sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sz[4] = {0, 0, 0, 0};
+        for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; four members per step
+            int jj[4];
+            unsigned mm[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                jj[q] = bits ? __ffs(bits) - 1 : 0;
+                mm[q] = bits ? 1u << jj[q] : 0u;
+                bits &= bits - 1u;
+            }
+            float4 mn[4], mx[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                mn[q] = s_lo[warp][jj[q]];
+                mx[q] = s_hi[warp][jj[q]];
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const unsigned m = mm[q];
+                sx[0] |= mn[q].x <= lo.x ? m : 0; sx[1] |= lo.x < mx[q].x ? m : 0;
+                sx[2] |= mn[q].x <= hi.x ? m : 0; sx[3] |= hi.x < mx[q].x ? m : 0;
+                sy[0] |= mn[q].y <= lo.y ? m : 0; sy[1] |= lo.y < mx[q].y ? m : 0;
+                sy[2] |= mn[q].y <= hi.y ? m : 0; sy[3] |= hi.y < mx[q].y ? m : 0;
+                sz[0] |= mn[q].z <= lo.z ? m : 0; sz[1] |= lo.z < mx[q].z ? m : 0;
+                sz[2] |= mn[q].z <= hi.z ? m : 0; sz[3] |= hi.z < mx[q].z ? m : 0;
+            }
+        }
+        const int4 x4 = make_int4(sx[0], sx[1], sx[2], sx[3]), y4 = make_int4(sy[0], sy[1], sy[2], sy[3]),
+                   z4 = make_int4(sz[0], sz[1], sz[2], sz[3]);
+        if (mine) {
+            a.sts[pi + lane] = x4;
+            a.sts[F + pi + lane] = y4;
+            a.sts[2 * F + pi + lane] = z4;
+        }
+        if (first_sah) {  // the first SAH lower level, from the sets in registers
+            if (__popc(bmp) <= a.min_leaf) {  // never split: skip the plane costs
+                if (lane == 0) {
+                    a.info[leaf] = (int8_t)KDGB_LEAF;
+                    a.ssplit[gw] = 0;
+                }
+            } else {
+                sah_eval_node(a, gw, leaf, pi, bmp, lane, x4, y4, z4);
+            }
+        }
+        __syncwarp();  // the staged boxes are rewritten by the warp's next node
+    }
+}
+
+// CalcSAH (LowerTriangleMap.h:463-555), one warp per node.  The first
+// level (the upper leaves) is evaluated by k_sah_planes, which already holds
+// their plane sets in registers.
 __global__ void k_calc_sah(const BuildArgs a)
 {
     const BuildState *st = a.st;
-    if (st->err) return;
+    if (st->err || st->low_first) return;
     const int32_t R = st->low_R, active = st->low_active;
-    const int32_t *__restrict__ ids = st->low_first ? a.leaf_ids : nullptr;
     const int64_t F = st->F;
-    const float ct = a.ct, ci = a.ci;
     const int lane = threadIdx.x & 31;
     WARP_STRIDE(gw, R) {
-        const int32_t par = ids ? ids[gw] : active + (int32_t)gw;
+        const int32_t par = active + (int32_t)gw;
         const int32_t pi = a.pidx[par];
         const unsigned bmp = (unsigned)a.amt[par];
         if (__popc(bmp) <= a.min_leaf) {  // never split: skip the plane costs
@@ -1513,59 +1587,11 @@ __global__ void k_calc_sah(const BuildArgs a)
             continue;
         }
         const bool mine = (bmp >> lane) & 1u;
-        const float a_lane = mine ? a.areas[pi + lane] : 0.0f;
-        SahPick mb;
-        mb.cost = KDGB_FINF; mb.la = mb.ra = 0.0f; mb.ls = mb.rs = 0; mb.axis = 0; mb.idx = 0;
         const int4 zero4 = make_int4(0, 0, 0, 0);
         const int4 sx = mine ? a.sts[pi + lane] : zero4;
         const int4 sy = mine ? a.sts[F + pi + lane] : zero4;
         const int4 sz = mine ? a.sts[2 * F + pi + lane] : zero4;
-        // One pass over the node's references in bit order accumulates the
-        // area sums of all twelve sets (3 axes x {lowLeft, lowRight, highLeft,
-        // highRight}).
-        unsigned sets[3][4] = {{(unsigned)sx.x & bmp, (unsigned)sx.y & bmp, (unsigned)sx.z & bmp, (unsigned)sx.w & bmp},
-                               {(unsigned)sy.x & bmp, (unsigned)sy.y & bmp, (unsigned)sy.z & bmp, (unsigned)sy.w & bmp},
-                               {(unsigned)sz.x & bmp, (unsigned)sz.y & bmp, (unsigned)sz.z & bmp, (unsigned)sz.w & bmp}};
-        float ar[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-        // Only members are added (predicated adds): skipping a +0 term is
-        // exact, so the sums equal the reference's bit-order accumulation.
-        for (unsigned bits = bmp; bits; bits &= bits - 1u) {  // bmp is warp-uniform
-            const int j = __ffs(bits) - 1;
-            const float aj = __shfl_sync(kFull, a_lane, j);
-            const unsigned m = 1u << j;
-#pragma unroll
-            for (int x = 0; x < 3; ++x)
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    if (sets[x][c] & m) ar[x][c] = __fadd_rn(ar[x][c], aj);
-        }
-        pick_planes(sets[0], ar[0], KDGB_X, pi + lane, mb);
-        pick_planes(sets[1], ar[1], KDGB_Y, pi + lane, mb);
-        pick_planes(sets[2], ar[2], KDGB_Z, pi + lane, mb);
-        // Warp argmin on (cost, lane); only lanes whose cost beat fInfinity count.
-        float c = mine && mb.cost < KDGB_FINF ? mb.cost : INFINITY;
-        int owner = mine && mb.cost < KDGB_FINF ? lane : 32;
-        for (int o = 16; o > 0; o >>= 1) {
-            const float c2 = __shfl_xor_sync(kFull, c, o);
-            const int w2 = __shfl_xor_sync(kFull, owner, o);
-            if (c2 < c || (c2 == c && w2 < owner)) { c = c2; owner = w2; }
-        }
-        if (lane == (owner < 32 ? owner : 0)) {
-            const int cnt = __popc(bmp);
-            const float opt = owner < 32 ? mb.cost : KDGB_FINF;
-            const float node_area = a.area[par];
-            bool split_it = __fmul_rn(ci, opt) < __fmul_rn(__fsub_rn(__fmul_rn(ci, (float)cnt), ct), node_area);
-            if (cnt <= a.min_leaf) split_it = false;
-            if (split_it) {
-                a.careas[gw] = make_float2(mb.la, mb.ra);
-                a.csets[gw] = make_int2((int)mb.ls, (int)mb.rs);
-                const float4 sp4 = ((unsigned)mb.idx & 0x80000000u) ? a.fmax[(unsigned)mb.idx ^ 0x80000000u]
-                                                                     : a.fmin[mb.idx];
-                a.split[par] = axis_of4(sp4, mb.axis);
-            }
-            a.info[par] = split_it ? (int8_t)mb.axis : (int8_t)KDGB_LEAF;
-            a.ssplit[gw] = split_it;
-        }
+        sah_eval_node(a, gw, par, pi, bmp, lane, sx, sy, sz);
     }
 }
 
@@ -2331,7 +2357,16 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
     KDGB_CHECK(ensure(t.leaf_ids, nl, s));
     KDGB_CHECK(ensure(t.prim_indices, F, s));
     if (p.lower == KDGB_LOWER_SAH) KDGB_CHECK(grab(w.areas, F, s));
-    if (lower_loop(p)) KDGB_CHECK(grab(w.sts, 3 * F, s));
+    if (lower_loop(p)) {
+        KDGB_CHECK(grab(w.sts, 3 * F, s));
+        // The first lower level's decision arrays: k_sah_planes already
+        // writes them with the SAH creator (the loop's grab keeps them, as
+        // the first level needs exactly this size).
+        KDGB_CHECK(grab(w.ssplit, nl, s));
+        KDGB_CHECK(grab(w.saddr, nl + 1, s));
+        KDGB_CHECK(grab(w.careas, nl, s));
+        KDGB_CHECK(grab(w.csets, nl, s));
+    }
     {
         const Extents e{0, 0, F, st.n_nodes, nl, 0};
         KDGB_CHECK(emit_after_upper(make_args(t, p, T, M, mesh_off_dev), L, e, p, s));
