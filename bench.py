@@ -9,22 +9,27 @@ Default workload (one "step" = one frame of the 1M-triangle clustered scene):
     fused in the same kernel, one shadow ray per hit toward (0.5, 3, 0.5).
 Metric: rays traced (primary + shadow) per second of the whole step, build
 included, in Mrays/s; the build time and the trace-only throughput are
-reported beside it.
+reported beside it.  The same line carries the batched half of the metric
+(512 meshes, one graph against a per-mesh loop of graph launches and one of
+host-driven rebuilds), a parity record (the GPU tree and a ray sample against
+the oracle, which the CPU baseline builds anyway) and the error of t, u, v
+against an FP64 brute-force oracle on a ray sample.
 
 Timing: CUDA events on the launching stream around each step, L2 flushed
 (a 512 MB write) between steps outside the events; max over ranks.  Under
 torchrun each rank runs an independent replica (weak scaling).
 
---impl reference times the reference's algorithms on the host cores: the CPU
-restatement in oracle/ (the reference itself does not compile here).
+--impl reference times the same frame (same build configuration, tracer and
+rays) with the CPU restatement in oracle/ on all host cores; the reference
+itself does not compile here.
 
 --workload selects the other measured configurations (one JSON line each):
   small    4096-triangle height field, 256x256 rays: kd-restart and brute force
   photons  262,144-triangle clustered scene, 16M photons x 3 diffuse bounces,
            kd-restart vs short-stack, Msegments/s
   batched  512 clustered meshes (log-uniform 1k..200k triangles, ~22M total),
-           64k rays per mesh: one graph (forest build + trace) vs a per-mesh
-           launch loop, parameters from the autotuner
+           64k rays per mesh: one graph (forest build + trace) vs per-mesh
+           loops, parameters from the autotuner
   adjoint  100k-triangle height field (316x158), 512x512 rays: backward pass
 """
 from __future__ import annotations
@@ -43,20 +48,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "extensions-photonmapping_gb300"))
 
-N_TRIS = 1_000_000
-WIDTH, HEIGHT = 1920, 1080
-LIGHT = (0.5, 3.0, 0.5)
-SCENE_SEED = 2
-BUILD = dict(lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
-BUILD_DESC = "reference upper (median + empty space to <32 refs) + SAH lower Ct=1 Ci=1.5 min_leaf=8"
-# The frame's configuration: median/empty-space splits on the top 8 levels, then SAH (binned, 32 bins, down to
-# nodes of < 32 references), then the reference's SAH lower phase (Ct=1, Ci=1.5, leaf threshold 8).
-BUILD_TUNED = dict(BUILD, mode=1, upper_levels=8, sah_bins=32)
-BUILD_TUNED_DESC = ("median + empty space on the top 8 levels, binned SAH (32 bins) below to <32 refs, "
-                    "then SAH lower Ct=1 Ci=1.5 min_leaf=8")
-STACK_DEPTH = 8
+from kdgb import configs  # noqa: E402
+
+METRIC = "kd traversal Mrays/s per frame (1M-tri build + primary + shadow)"
 HEADROOM = 1.1
 FLUSH_BYTES = 512 << 20
+BUILDS = {"tuned": (configs.TUNED, configs.TUNED_DESC), "reference": (configs.SAH, configs.SAH_DESC)}
 
 
 def parse():
@@ -66,9 +63,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="frame", choices=["frame", "small", "photons", "batched", "adjoint"])
-    ap.add_argument("--tris", type=int, default=N_TRIS)
-    ap.add_argument("--width", type=int, default=WIDTH)
-    ap.add_argument("--height", type=int, default=HEIGHT)
+    ap.add_argument("--tris", type=int, default=configs.FRAME_TRIS)
+    ap.add_argument("--width", type=int, default=configs.WIDTH)
+    ap.add_argument("--height", type=int, default=configs.HEIGHT)
     ap.add_argument("--host-build", action="store_true", help="rebuild with the host-driven level loop")
     ap.add_argument("--build", default="tuned", choices=["tuned", "reference"],
                     help="tuned: the frame's configuration; reference: the reference's creators")
@@ -76,7 +73,17 @@ def parse():
                     help="one build and two traces, nothing timed (for ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="leave the batched record out of the frame line")
     return ap.parse_args()
+
+
+def frame_config(args, build_desc, n_hits):
+    """The frame's `config`, identical in both arms."""
+    return {"workload": "clustered-1M-tris 1920x1080 primary + shadow, short-stack depth 8",
+            "tris": args.tris, "rays_primary": args.width * args.height, "rays_shadow": int(n_hits),
+            "light": list(configs.LIGHT), "build": build_desc,
+            "l2": "GPU arm: 512 MB buffer written between timed steps; CPU arm: no GPU",
+            "parallelism": f"replicas x{args.gpus}"}
 
 
 def dist_setup(args):
@@ -94,10 +101,7 @@ def dist_setup(args):
 
 
 def workload(args):
-    from kdgb import scenes
-    tris = scenes.clustered(args.tris, seed=SCENE_SEED)
-    o, d = scenes.camera_rays(args.width, args.height)
-    return tris, o, d
+    return configs.frame_scene(args.tris, args.width, args.height)
 
 
 class ClockSampler:
@@ -180,69 +184,135 @@ def oracle_module():
     return O
 
 
-def cpu_baseline(tris, o, d, build_kw, sample_stride=16, threads=0):
+
+
+def oracle_kwargs(bp):
+    """A library build-parameter struct as keyword arguments of the oracle."""
+    return {name: getattr(bp, name) for name, _ in bp._fields_}
+
+
+def cpu_frame(O, tris, o, d, build_kw, sample_stride=16, threads=0):
     """The oracle (the build and tracers restated in C, OpenMP) on the host
-    cores: full build with the GPU arm's parameters + traced sample of every
-    `sample_stride`-th ray."""
-    O = oracle_module()
+    cores: a full build with the GPU arm's parameters and the primary and
+    shadow rays of every `sample_stride`-th pixel.  Returns the baseline
+    record and, for the parity record, the tree and the sample's results."""
     from kdgb import scenes
     t0 = time.perf_counter()
     tree = O.build(tris, **build_kw)
     t_build = time.perf_counter() - t0
     idx = np.arange(0, o.shape[0], sample_stride)
     t0 = time.perf_counter()
-    h, t, _, _ = O.trace(tree, tris, o[idx], d[idx], tracer=O.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH,
+    h, t, u, v = O.trace(tree, tris, o[idx], d[idx], tracer=O.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH,
                          threads=threads)
-    pts = scenes.hit_points(o[idx], d[idx], t, h)[h >= 0]
-    O.trace_shadow(tree, tris, pts, LIGHT, threads=threads)
+    hitm = h >= 0
+    pts = scenes.hit_points(o[idx], d[idx], t, h)[hitm]
+    occ_hits = O.trace_shadow(tree, tris, pts, configs.LIGHT, threads=threads)
     t_trace = time.perf_counter() - t0
-    n_sample = len(idx) + int((h >= 0).sum())
+    occ = np.zeros(idx.shape[0], np.int32)
+    occ[hitm] = occ_hits
+    n_sample = len(idx) + int(hitm.sum())
     scale = o.shape[0] / len(idx)
     step_s = t_build + t_trace * scale
     rays = n_sample * scale
     cores = threads if threads > 0 else (os.cpu_count() or 1)
-    return {"value": rays / step_s / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
-            "sample": f"full CPU build, same parameters as the GPU arm ({t_build * 1e3:.0f} ms) + every "
-                      f"{sample_stride}th primary ray and its shadow ray ({t_trace * 1e3:.0f} ms), extrapolated "
-                      f"to the frame",
-            "build_ms": t_build * 1e3}
+    rec = {"value": rays / step_s / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+           "sample": f"full CPU build, same parameters as the GPU arm ({t_build * 1e3:.0f} ms) + every "
+                     f"{sample_stride}th primary ray and its shadow ray ({t_trace * 1e3:.0f} ms), extrapolated "
+                     f"to the frame",
+           "build_ms": t_build * 1e3,
+           "compiler": "gcc -O3 -std=c11 -fopenmp -ffp-contract=off -fno-fast-math (oracle/Makefile, no -march)"}
+    return rec, tree, idx, (h, t, u, v, occ)
+
+
+TREE_FIELDS = ("info", "split", "children", "prim_index", "bitmap", "parent", "area", "aabb_min", "aabb_max",
+               "prim_indices", "leaf_ids")
+
+
+def same_bits(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    if a.shape != b.shape:
+        return False
+    if a.dtype.kind == "f":
+        return bool(np.array_equal(a.view(np.uint32), b.view(np.uint32)))
+    return bool(np.array_equal(a, b))
+
+
+def parity_record(gpu_tree, cpu_tree, idx, gpu_out, cpu_out):
+    """The GPU tree and the GPU results on the sampled rays against the
+    oracle's, bit for bit."""
+    h, t, u, v, occ = gpu_out
+    hr, tr, ur, vr, occr = cpu_out
+    hit = hr >= 0
+    tuv = all(same_bits(x[idx][hit], y[hit]) for x, y in ((t, tr), (u, ur), (v, vr)))
+    return {"against": "oracle, same build parameters and tracer (CPU)",
+            "tree_arrays_equal": all(same_bits(getattr(gpu_tree, f), getattr(cpu_tree, f)) for f in TREE_FIELDS),
+            "rays_checked": int(idx.shape[0]), "hit_ids_equal": bool(np.array_equal(h[idx], hr)),
+            "tuv_bits_equal": bool(tuv), "shadow_equal": bool(np.array_equal(occ[idx], occr))}
+
+
+def fp64_error(O, tris, o, d, h, t, u, v, stride):
+    """t, u, v of the fp32 tracer against an FP64 brute-force oracle on every
+    `stride`-th ray (rays on which both find the same triangle)."""
+    idx = np.arange(0, o.shape[0], stride)
+    hf, tf, uf, vf = O.trace_brute_f64(tris, o[idx], d[idx])
+    hs = h[idx]
+    either = (hs >= 0) | (hf >= 0)
+    agree = (hs == hf) & (hf >= 0)
+    rel_t = np.abs(t[idx][agree].astype(np.float64) - tf[agree]) / np.abs(tf[agree])
+    du = np.abs(u[idx][agree].astype(np.float64) - uf[agree])
+    dv = np.abs(v[idx][agree].astype(np.float64) - vf[agree])
+    return {"oracle": "FP64 brute force", "rays": int(idx.shape[0]), "hits_compared": int(agree.sum()),
+            "id_agreement": float(agree.sum() / max(1, either.sum())),
+            "t_max_rel": float(rel_t.max()) if rel_t.size else None,
+            "t_median_rel": float(np.median(rel_t)) if rel_t.size else None,
+            "u_max_abs": float(du.max()) if du.size else None, "v_max_abs": float(dv.max()) if dv.size else None}
 
 
 def run_reference(args, world, rank):
-    """--impl reference: the oracle on all host cores, full frames."""
+    """--impl reference: the same frame (build configuration, tracer, rays)
+    with the oracle on all host cores, full frames."""
     if rank != 0:
         return
     O = oracle_module()
     from kdgb import scenes
     tris, o, d = workload(args)
     cores = os.cpu_count() or 1
+    build_kw, build_desc = BUILDS[args.build]
 
-    def step():
-        tree = O.build(tris, **BUILD)
-        h, t, _, _ = O.trace(tree, tris, o, d, tracer=O.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH)
+    def step(kw):
+        tree = O.build(tris, **kw)
+        h, t, _, _ = O.trace(tree, tris, o, d, tracer=O.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH)
         pts = scenes.hit_points(o, d, t, h)[h >= 0]
-        O.trace_shadow(tree, tris, pts, LIGHT)
+        O.trace_shadow(tree, tris, pts, configs.LIGHT)
         return o.shape[0] + pts.shape[0]
 
     for _ in range(args.warmup):
-        step()
+        rays = step(build_kw)
     t0 = time.perf_counter()
     rays = 0
     for _ in range(args.steps):
-        rays += step()
+        rays += step(build_kw)
     dt = time.perf_counter() - t0
     val = rays / dt / 1e6
-    line = {"impl": "reference", "metric": "kd traversal Mrays/s per frame (1M-tri build + primary + shadow)",
-            "value": val, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "clustered-1M-tris 1920x1080 primary + shadow, short-stack depth 8",
-                       "tris": args.tris, "rays": args.width * args.height,
-                       "build": "reference upper + SAH lower Ct=1 Ci=1.5 min_leaf=8 (host loop)"},
+    n_hits = rays // args.steps - o.shape[0]
+    # The other build configuration, one timed frame, for context.
+    alt = "reference" if args.build == "tuned" else "tuned"
+    alt_kw, alt_desc = BUILDS[alt]
+    t0 = time.perf_counter()
+    alt_rays = step(alt_kw)
+    alt_s = time.perf_counter() - t0
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded clustered scene, pinhole camera)",
+            "config": frame_config(args, build_desc, n_hits),
             "cpu_baseline": {"value": val, "unit": "Mrays/s", "cores": cores, "kind": "port",
-                             "sample": "full frames: CPU restatement of the reference build + short-stack + "
-                                       "shadow rays, OpenMP over all host cores"},
-            "e2e": {"value": val, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": "full frames: the oracle's restatement of the same build + short-stack + "
+                                       "shadow rays, OpenMP over all host cores",
+                             "compiler": "gcc -O3 -std=c11 -fopenmp -ffp-contract=off -fno-fast-math "
+                                         "(oracle/Makefile, no -march)"},
+            "e2e": {"value": val, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "other_build": {"build": alt_desc, "ms_per_step": alt_s * 1e3, "value": alt_rays / alt_s / 1e6}}
     print(json.dumps(line), flush=True)
 
 
@@ -275,9 +345,9 @@ def run_frame(args, world, rank, local, pg):
     tris_d = torch.from_numpy(tris).to(dev)
     o_d = torch.from_numpy(o).to(dev)
     d_d = torch.from_numpy(d).to(dev)
-    build_kw, build_desc = (BUILD_TUNED, BUILD_TUNED_DESC) if args.build == "tuned" else (BUILD, BUILD_DESC)
+    build_kw, build_desc = BUILDS[args.build]
     bp = kdgb.build_params(**build_kw)
-    tp = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH, tile_width=args.width)
+    tp = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH, tile_width=args.width)
     tree = kdgb.KDTree.build(tris_d, bp)
     graph = None if args.host_build else kdgb.Graph(tree, tris_d, params=bp, headroom=HEADROOM)
     outs = (torch.empty(n, dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.float32, device=dev),
@@ -295,14 +365,14 @@ def run_frame(args, world, rank, local, pg):
         build()
         if ev:
             ev[0].record(stream)
-        tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
+        tree.trace_primary_shadow(o_d, d_d, configs.LIGHT, tp, out=outs)
         if ev:
             ev[1].record(stream)
 
     if args.profile:
         build()
-        tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
-        tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
+        tree.trace_primary_shadow(o_d, d_d, configs.LIGHT, tp, out=outs)
+        tree.trace_primary_shadow(o_d, d_d, configs.LIGHT, tp, out=outs)
         torch.cuda.synchronize()
         if graph is not None and graph.status() != 0:
             raise RuntimeError("graph rebuild failed")
@@ -349,6 +419,9 @@ def run_frame(args, world, rank, local, pg):
         total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
     value = rays_per_step * world / (ms_per_step / 1e3) / 1e6
+    # The outputs of the last timed step, for the parity and error records.
+    gpu_out = tuple(x.cpu().numpy() for x in outs)
+    gpu_tree = tree.to_host()
 
     # Roofline of the dominant kernel (fused short-stack primary + shadow).
     T = tris.shape[0]
@@ -362,10 +435,9 @@ def run_frame(args, world, rank, local, pg):
             "traffic": traffic.get("trace_dram_bytes_per_launch") if traffic else None,
             "kernel": "k_trace<SHORTSTACK,leaf-skip,shadow>", "algorithmic_bytes_per_launch": alg_bytes,
             "peak_source": f"{peak_kind} hbm_gbs",
-            # The traversal is bound by issue and latency, not by HBM: these
-            # are the ncu figures of the committed profile of this kernel.
-            "limiter": "issue/latency (ncu: 73% of issue slots active, 16.5 of 32 lanes per warp instruction, "
-                       "L1 hit 67%, L2 hit 83%)"}
+            # The traversal is bound by issue and latency, not by HBM: the
+            # committed profile of this kernel gives the ncu figures.
+            "limiter": "issue/latency (ncu figures in profiles/k_trace_clustered1M_frame.md)"}
     if traffic:
         roof["traffic_source"] = traffic.get("source")
 
@@ -402,7 +474,7 @@ def run_frame(args, world, rank, local, pg):
             build()
             stream.wait_event(rays_in)
             stream.wait_event(read_back)
-            tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
+            tree.trace_primary_shadow(o_d, d_d, configs.LIGHT, tp, out=outs)
             traced.record(stream)
             back.wait_event(traced)
             with torch.cuda.stream(back):
@@ -431,18 +503,21 @@ def run_frame(args, world, rank, local, pg):
         d2h = sum(x.numel() * x.element_size() for x in outs)
         e2e = {"value": rays_per_step * world / (e2e_ms / 1e3) / 1e6, "unit": "Mrays/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+        # The host copy of the last e2e step must equal the device-timed
+        # step's outputs (same inputs, same tree).
+        e2e["outputs_equal_device_steps"] = all(np.array_equal(hb.numpy(), g) for hb, g in zip(h_out, gpu_out))
 
     # The other build configuration on the same inputs, for context.
     variant = None
-    if graph is not None and not args.profile:
-        alt_kw, alt_desc = (BUILD, BUILD_DESC) if args.build == "tuned" else (BUILD_TUNED, BUILD_TUNED_DESC)
+    if graph is not None:
+        alt_kw, alt_desc = BUILDS["reference" if args.build == "tuned" else "tuned"]
         alt_bp = kdgb.build_params(**alt_kw)
         alt_tree = kdgb.KDTree.build(tris_d, alt_bp)
         alt_graph = kdgb.Graph(alt_tree, tris_d, params=alt_bp, headroom=HEADROOM)
 
         def alt_step():
             alt_graph.launch()
-            alt_tree.trace_primary_shadow(o_d, d_d, LIGHT, tp, out=outs)
+            alt_tree.trace_primary_shadow(o_d, d_d, configs.LIGHT, tp, out=outs)
 
         time_steps(alt_step, 3, stream)
         alt_ms = statistics.median(time_steps(alt_step, args.steps, stream, flush))
@@ -454,27 +529,31 @@ def run_frame(args, world, rank, local, pg):
         alt_graph.close()
         alt_tree.close()
 
-    cpu = None
+    cpu = parity = fp64 = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(tris, o, d, build_kw)
+        O = oracle_module()
+        cpu, cpu_tree, idx, cpu_out = cpu_frame(O, tris, o, d, build_kw)
+        parity = parity_record(gpu_tree, cpu_tree, idx, gpu_out, cpu_out)
+        fp64 = fp64_error(O, tris, o, d, *gpu_out[:4], stride=2048)
+
+    batched = None
+    if rank == 0 and world == 1 and not args.no_batched and graph is not None:
+        batched = measure_batched(args, steps=max(3, args.steps // 4), host_loop_steps=1)
 
     if rank == 0:
-        line = {"metric": "kd traversal Mrays/s per frame (1M-tri build + primary + shadow)", "value": value,
-                "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
-                "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32", "data": "synthetic (seeded clustered scene, pinhole camera)",
-                "config": {"workload": "clustered-1M-tris 1920x1080 primary + shadow, short-stack depth 8",
-                           "tris": T, "rays_primary": n, "rays_shadow": n_hits,
-                           "build": build_desc + (", rebuilt by one graph launch" if graph is not None else
-                                                  ", host-driven level loop"),
-                           "l2": "512 MB buffer written between timed steps",
-                           "parallelism": f"replicas x{world}"},
+        line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded clustered scene, pinhole camera)",
+                "config": frame_config(args, build_desc, n_hits),
+                "rebuild": "one graph launch" if graph is not None else "host-driven level loop",
                 "build_ms": statistics.mean(s - t for s, t in zip(step_ms, trace_ms)),
                 "trace_ms": tr_ms, "trace_mrays_s": rays_per_step / (tr_ms / 1e3) / 1e6,
                 "tree": {"nodes": st.n_nodes, "refs": st.n_refs, "upper_levels": st.upper_levels,
                          "lower_levels": st.lower_levels},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clocks, "other_build": variant}
+                "clocks": clocks, "parity": parity, "fp64_err": fp64, "other_build": variant,
+                "batched": batched}
         print(json.dumps(line), flush=True)
     if graph is not None:
         graph.close()
@@ -484,8 +563,6 @@ def run_frame(args, world, rank, local, pg):
 # ---------------------------------------------------------------------------
 # Other configurations (single GPU, rank 0 only).
 # ---------------------------------------------------------------------------
-
-SMALL_BUILD = dict(lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
 
 
 def line_common(args, metric, value, unit, higher, ms, workload_desc, extra):
@@ -507,7 +584,7 @@ def run_small(args):
     n = o.shape[0]
     td, od, dd = (torch.from_numpy(x).cuda() for x in (tris, o, d))
     stream = torch.cuda.current_stream()
-    bp = kdgb.build_params(**SMALL_BUILD)
+    bp = kdgb.build_params(**configs.SAH)
     tree = kdgb.KDTree.build(td, bp)
     graph = kdgb.Graph(tree, td, params=bp, headroom=HEADROOM)
     tp = kdgb.trace_params(tracer=kdgb.TRACER_RESTART)
@@ -522,12 +599,12 @@ def run_small(args):
         res[name] = statistics.median(time_steps(fn, args.steps, stream))
     kdgb.check(graph.status(), "graph rebuild")
     step_ms = res["graph_build"] + res["restart"]
-    cpu = None
+    cpu = fp64 = None
     if not args.no_cpu_baseline:
         O = oracle_module()
         t0 = time.perf_counter()
         for _ in range(5):
-            ot = O.build(tris, **SMALL_BUILD)
+            ot = O.build(tris, **configs.SAH)
         tb = (time.perf_counter() - t0) / 5
         t0 = time.perf_counter()
         for _ in range(5):
@@ -539,36 +616,42 @@ def run_small(args):
         cpu = {"value": n / (tb + tt) / 1e6, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
                "sample": "oracle build + kd-restart over all 65,536 rays (5 runs); brute force over every 16th ray",
                "build_ms": tb * 1e3, "restart_mrays_s": n / tt / 1e6, "brute_mrays_s": n / tbr / 1e6}
+        fp64 = fp64_error(O, tris, o, d, *(x.cpu().numpy() for x in outs), stride=1)
     print(json.dumps(line_common(
         args, "kd-restart Mrays/s per step (4096-tri SAH build + 256x256 primary rays)", n / (step_ms / 1e3) / 1e6,
         "Mrays/s", True, step_ms, "heightfield-64x32 (4096 tris) 256x256 rays, SAH Ct=1 Ci=1.5 leaf 8",
         {"build_ms_graph": res["graph_build"], "build_ms_host": res["host_build"],
          "restart_trace_ms": res["restart"], "restart_mrays_s": n / (res["restart"] / 1e3) / 1e6,
-         "brute_trace_ms": res["brute"], "brute_mrays_s": n / (res["brute"] / 1e3) / 1e6, "cpu_baseline": cpu})),
+         "brute_trace_ms": res["brute"], "brute_mrays_s": n / (res["brute"] / 1e3) / 1e6, "cpu_baseline": cpu,
+         "fp64_err": fp64})),
         flush=True)
     graph.close()
     tree.close()
 
 
 def run_photons(args):
-    """Incoherent load: 16M photons from a point light, 3 cosine-weighted
-    bounces with Russian roulette (p = 0.7), Philox stream; kd-restart vs
-    short-stack on a 262,144-triangle clustered scene."""
+    """Incoherent load: 16M photons from the frame's point light, 3
+    cosine-weighted bounces with Russian roulette (p = 0.7), Philox stream;
+    kd-restart vs short-stack on a 262,144-triangle clustered scene."""
     import torch
     import kdgb
     from kdgb import scenes
-    T, P = 262144, 16 << 20
-    tris = scenes.clustered(T, seed=SCENE_SEED)
+    T, P = configs.PHOTON_TRIS, configs.PHOTONS
+    tris = scenes.clustered(T, seed=configs.FRAME_SEED)
     td = torch.from_numpy(tris).cuda()
     stream = torch.cuda.current_stream()
-    tree = kdgb.KDTree.build(td, **BUILD)
-    ph = kdgb.photon_params(seed=3, bounces=3, survival=0.7)
-    out = (torch.empty((P, 4), dtype=torch.int32, device="cuda"), torch.empty((P, 4), dtype=torch.float32,
-                                                                              device="cuda"))
+    tree = kdgb.KDTree.build(td, **configs.SAH)
+    pkw = dict(light=configs.LIGHT, seed=configs.PHOTON_SEED, bounces=configs.PHOTON_BOUNCES,
+               survival=configs.PHOTON_SURVIVAL)
+    ph = kdgb.photon_params(**pkw)
+    S = configs.PHOTON_BOUNCES + 1
+    out = (torch.empty((P, S), dtype=torch.int32, device="cuda"),
+           torch.empty((P, S), dtype=torch.float32, device="cuda"))
     W = max(args.warmup, 3)
     res = {}
     for name, tp in (("restart", kdgb.trace_params(tracer=kdgb.TRACER_RESTART)),
-                     ("shortstack", kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH))):
+                     ("shortstack", kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK,
+                                                      stack_depth=configs.STACK_DEPTH))):
         fn = lambda tp=tp: tree.trace_photons(P, tp, photons=ph, out=out)
         time_steps(fn, W, stream)
         res[name] = statistics.median(time_steps(fn, args.steps, stream))
@@ -577,18 +660,18 @@ def run_photons(args):
     cpu = None
     if not args.no_cpu_baseline:
         O = oracle_module()
-        ot = O.build(tris, **BUILD)
-        sample = 1 << 18
+        ot = O.build(tris, **configs.SAH)
+        sample = 1 << 20
         t0 = time.perf_counter()
-        h, _ = O.trace_photons(ot, tris, sample, seed=3, bounces=3, survival=0.7, tracer=O.TRACER_SHORTSTACK,
-                               stack_depth=STACK_DEPTH)
+        h, _ = O.trace_photons(ot, tris, sample, tracer=O.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH, **pkw)
         dt = time.perf_counter() - t0
         cpu = {"value": int((h != -2).sum()) / dt / 1e6, "unit": "Msegments/s", "cores": os.cpu_count(),
-               "kind": "port", "sample": f"first {sample} photons, short-stack, OpenMP over all host cores"}
+               "kind": "port", "sample": f"first {sample} photons, short-stack, OpenMP over all host cores",
+               "segments_equal_gpu": bool(np.array_equal(h, out[0][:sample].cpu().numpy()))}
     print(json.dumps(line_common(
         args, "photon segments Msegments/s (262k-tri clustered, 16M photons x 3 bounces)",
         segs / (res[best] / 1e3) / 1e6, "Msegments/s", True, res[best],
-        "clustered-262144-tris, 16M photons from (0.5,0.5,0.5), 3 bounces, RR p=0.7",
+        "clustered-262144-tris, 16M photons from (0.5,3,0.5), 3 bounces, RR p=0.7",
         {"segments": segs, "restart_ms": res["restart"], "shortstack_ms": res["shortstack"],
          "restart_msegments_s": segs / (res["restart"] / 1e3) / 1e6,
          "shortstack_msegments_s": segs / (res["shortstack"] / 1e3) / 1e6, "best": best, "cpu_baseline": cpu})),
@@ -596,35 +679,24 @@ def run_photons(args):
     tree.close()
 
 
-def batched_workload(n_meshes=512, lo=1000, hi=200000, rays_per_mesh=65536, seed=40):
-    from kdgb import scenes
-    u = scenes.uniform(seed, n_meshes, 0)
-    sizes = np.exp(np.log(lo) + (np.log(hi) - np.log(lo)) * u).astype(np.int64)
-    meshes = [scenes.clustered(int(s), seed=seed + 1 + m) for m, s in enumerate(sizes)]
-    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
-    o = np.empty((n_meshes * rays_per_mesh, 3), np.float32)
-    d = np.empty_like(o)
-    for m, t in enumerate(meshes):
-        v = t.reshape(-1, 3)
-        ro, rd = scenes.random_rays(rays_per_mesh, seed + 1000 + m, v.min(0), v.max(0))
-        o[m * rays_per_mesh:(m + 1) * rays_per_mesh] = ro
-        d[m * rays_per_mesh:(m + 1) * rays_per_mesh] = rd
-    return meshes, off, o, d
-
-
-def run_batched(args):
-    """512 meshes: one graph (forest build + batched trace) vs a per-mesh loop
-    of rebuild + trace launches, both with the autotuner's parameters."""
+def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
+    """512 meshes, parameters from the autotuner:
+      * one graph: forest build of all meshes + batched trace (one launch);
+      * per-mesh graph loop: one graph per mesh (its rebuild + its rays),
+        launched one after another on one stream, no host synchronisation;
+      * per-mesh host loop: host-driven rebuild + trace per mesh.
+    Returns the record; the hits of the three must be identical, and a few
+    meshes are checked against the oracle."""
     import torch
     import kdgb
-    R = 65536
-    meshes, off, o, d = batched_workload(rays_per_mesh=R)
+    R = configs.BATCH_RAYS_PER_MESH
+    meshes, off, o, d = configs.batch_scene()
     M = len(meshes)
     tris = np.concatenate(meshes)
     td, od, dd = (torch.from_numpy(x).cuda() for x in (tris, o, d))
     stream = torch.cuda.current_stream()
-    base_b = kdgb.build_params(**BUILD)
-    base_t = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=STACK_DEPTH)
+    base_b = kdgb.build_params(**configs.TUNED)
+    base_t = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH)
     t0 = time.perf_counter()
     tuned = kdgb.autotune(td, od, dd, mesh_offsets=off, rays_per_mesh=R, build=base_b, trace=base_t,
                           builds_per_trace=1.0, reps=2)
@@ -634,40 +706,78 @@ def run_batched(args):
     forest = kdgb.KDTree.build_batch(td, off, bp)
     graph = kdgb.Graph(forest, td, mesh_offsets=off, params=bp, headroom=HEADROOM, o=od, d=dd, rays_per_mesh=R,
                        trace=tp)
-    W = max(args.warmup, 3)
-    time_steps(graph.launch, W, stream)
-    g_ms = time_steps(graph.launch, args.steps, stream)
+    time_steps(graph.launch, 3, stream)
+    g_ms = time_steps(graph.launch, steps, stream)
     kdgb.check(graph.status(), "graph rebuild")
     hits = int((graph.out[0] >= 0).sum().item())
+    ghit = graph.out[0].cpu().numpy()
 
-    # Per-mesh launch loop: one handle per mesh, host-driven rebuild + trace.
     views = [td[off[m]:off[m + 1]] for m in range(M)]
+    oviews = [(od[m * R:(m + 1) * R], dd[m * R:(m + 1) * R]) for m in range(M)]
     trees = [kdgb.KDTree.build(views[m], bp) for m in range(M)]
     louts = [tuple(torch.empty(R, dtype=dt, device="cuda") for dt in (torch.int32, torch.float32, torch.float32,
                                                                       torch.float32)) for _ in range(M)]
-    oviews = [(od[m * R:(m + 1) * R], dd[m * R:(m + 1) * R]) for m in range(M)]
+    mgraphs = [kdgb.Graph(trees[m], views[m], params=bp, headroom=HEADROOM, o=oviews[m][0], d=oviews[m][1],
+                          trace=tp, out=louts[m]) for m in range(M)]
 
-    def loop():
+    def graph_loop():
+        for g in mgraphs:
+            g.launch()
+
+    time_steps(graph_loop, 2, stream)
+    gl_ms = time_steps(graph_loop, steps, stream)
+    for g in mgraphs:
+        kdgb.check(g.status(), "per-mesh graph rebuild")
+    same_graph_loop = all(np.array_equal(louts[m][0].cpu().numpy(), ghit[m * R:(m + 1) * R]) for m in range(M))
+    for g in mgraphs:
+        g.close()
+
+    def host_loop():
         for m in range(M):
             trees[m].rebuild(views[m], bp)
             trees[m].trace(oviews[m][0], oviews[m][1], tp, out=louts[m])
 
-    time_steps(loop, 1, stream)
-    l_ms = time_steps(loop, max(2, args.steps // 3), stream)
-    same = all(torch.equal(louts[m][0], graph.out[0][m * R:(m + 1) * R]) for m in range(M))
-    g, lp = statistics.median(g_ms), statistics.median(l_ms)
-    print(json.dumps(line_common(
-        args, "batched build+trace of 512 meshes, meshes/s (one graph launch)", M / (g / 1e3), "meshes/s", True, g,
-        "512 clustered meshes log-uniform [1k,200k] tris (%d total), 64k random rays each, SAH" % tris.shape[0],
-        {"rays_mrays_s": M * R / (g / 1e3) / 1e6, "per_mesh_loop_ms": lp, "per_mesh_loop_meshes_s": M / (lp / 1e3),
-         "speedup_vs_loop": lp / g, "hits": hits, "loop_hits_identical": bool(same),
-         "autotune": {"leaf_size": bp.leaf_size, "sah_bins": bp.sah_bins, "stack_depth": tp.stack_depth,
-                      "block_size": tp.block_size, "objective_ms": tuned.objective, "baseline_ms": tuned.baseline,
-                      "trials": tuned.trials, "seconds": tune_s}})), flush=True)
+    time_steps(host_loop, 1, stream)
+    hl_ms = time_steps(host_loop, host_loop_steps, stream)
+    same_host_loop = all(np.array_equal(louts[m][0].cpu().numpy(), ghit[m * R:(m + 1) * R]) for m in range(M))
+
+    # A few meshes (small to large) against the oracle's own tree and tracer.
+    O = oracle_module()
+    okw = oracle_kwargs(bp)
+    order = np.argsort([mt.shape[0] for mt in meshes])
+    picks = order[np.linspace(0, M - 1, check_meshes).astype(np.int64)]
+    oracle_ok = True
+    for m in picks:
+        ot = O.build(meshes[m], **okw)
+        hr, _, _, _ = O.trace(ot, meshes[m], o[m * R:(m + 1) * R], d[m * R:(m + 1) * R], tracer=tp.tracer,
+                              stack_depth=tp.stack_depth)
+        oracle_ok &= bool(np.array_equal(hr, ghit[m * R:(m + 1) * R]))
+
+    g, gl, hl = statistics.median(g_ms), statistics.median(gl_ms), statistics.median(hl_ms)
+    rec = {"workload": "512 clustered meshes log-uniform [1k,200k] tris (%d total), 64k random rays each"
+                       % tris.shape[0],
+           "meshes": M, "tris": int(tris.shape[0]), "rays": M * R, "one_graph_ms": g, "meshes_per_s": M / (g / 1e3),
+           "rays_mrays_s": M * R / (g / 1e3) / 1e6, "hits": hits,
+           "per_mesh_graph_loop_ms": gl, "per_mesh_host_loop_ms": hl,
+           "speedup_vs_per_mesh_graph_loop": gl / g, "speedup_vs_per_mesh_host_loop": hl / g,
+           "parity": {"graph_loop_hits_identical": bool(same_graph_loop),
+                      "host_loop_hits_identical": bool(same_host_loop),
+                      "oracle_meshes_checked": int(check_meshes), "oracle_hit_ids_equal": bool(oracle_ok)},
+           "autotune": {"leaf_size": bp.leaf_size, "sah_bins": bp.sah_bins, "stack_depth": tp.stack_depth,
+                        "block_size": tp.block_size, "objective_ms": tuned.objective, "baseline_ms": tuned.baseline,
+                        "trials": tuned.trials, "seconds": tune_s, "scored_on": "graph rebuild + trace"}}
     graph.close()
     forest.close()
     for t in trees:
         t.close()
+    return rec
+
+
+def run_batched(args):
+    rec = measure_batched(args, steps=args.steps, host_loop_steps=max(2, args.steps // 3))
+    print(json.dumps(line_common(
+        args, "batched build+trace of 512 meshes, meshes/s (one graph launch)", rec["meshes_per_s"], "meshes/s",
+        True, rec["one_graph_ms"], rec["workload"], {"batched": rec})), flush=True)
 
 
 def run_adjoint(args):
@@ -684,7 +794,7 @@ def run_adjoint(args):
     vd = torch.from_numpy(np.ascontiguousarray(verts, dtype=np.float32)).cuda()
     idd = torch.from_numpy(np.ascontiguousarray(idx, dtype=np.int32)).cuda()
     od, dd = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
-    tree = kdgb.KDTree.build(td, **SMALL_BUILD)
+    tree = kdgb.KDTree.build(td, **configs.SAH)
     hit, t, u, v = tree.trace(od, dd)
     g = torch.Generator(device="cpu").manual_seed(7)
     w = torch.randn(n, generator=g).cuda()

@@ -436,6 +436,28 @@ int kdgb_tree_destroy(kdgb_tree *tree)
     return KDGB_OK;
 }
 
+int kdgb_tree_release(kdgb_tree *tree, kdgb_stream_t stream)
+{
+    if (!tree) return KDGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    release_all(tree->t, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    delete tree;
+    if (e != cudaSuccess) return cuda_fail(e, "kdgb_tree_release");
+    return KDGB_OK;
+}
+
+int kdgb_check_scan_giveup(int32_t spin_limit, int32_t *recorded_status, int32_t *assumed_prefix,
+                           kdgb_stream_t stream)
+{
+    if (!recorded_status || !assumed_prefix) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    int32_t r[2] = {0, 0};
+    KDGB_CHECK(scan_giveup_check(spin_limit, r, (cudaStream_t)stream));
+    *recorded_status = r[0];
+    *assumed_prefix = r[1];
+    return KDGB_OK;
+}
+
 int kdgb_tree_view_get(const kdgb_tree *tree, kdgb_tree_view *v)
 {
     if (!tree || !v) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -559,8 +581,8 @@ int kdgb_trace_primary_shadow(const kdgb_tree *tree, const kdgb_trace_params *pa
 void kdgb_photon_params_default(kdgb_photon_params *p)
 {
     if (!p) return;
-    p->light[0] = 0.5f;
-    p->light[1] = 0.5f;
+    p->light[0] = 0.5f;  // the frame's point light, above the unit cube
+    p->light[1] = 3.0f;
     p->light[2] = 0.5f;
     p->seed = 3;
     p->bounces = 3;

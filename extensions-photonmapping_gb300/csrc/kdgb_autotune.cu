@@ -5,7 +5,10 @@
 // Search: coordinate descent from the caller's parameters, one parameter at
 // a time in the order leaf_size, sah_bins, stack_depth, block_size; each
 // candidate is scored by builds_per_trace * rebuild_ms + trace_ms, the median
-// of `reps` timed repetitions after one warm-up.  Candidates that fail (a
+// of `reps` timed repetitions after one warm-up.  rebuild_ms is the time of a
+// graph rebuild (kdgb_graph_launch: the whole level loop on the device), the
+// way a per-frame rebuild runs; the host-driven rebuild before it only sizes
+// the graph's buffers.  Candidates that fail (a
 // leaf threshold whose tree does not terminate within a few extra levels, or
 // runs out of memory) are skipped.  Every trial goes through the library's
 // own entry points, so the winner is a parameter set the oracle can replay.
@@ -58,18 +61,32 @@ int trace(kdgb_tree *tree, const Workload &w, const kdgb_trace_params &tp)
     return kdgb_trace(tree, &tp, w.o, w.d, w.n_rays, w.hit, w.t, w.u, w.v, (kdgb_stream_t)w.s);
 }
 
-// Times `reps` rebuilds (when `build`) and traces.
+// Times `reps` graph rebuilds (when `build`) and traces.
 Score measure(kdgb_tree *tree, const Workload &w, const kdgb_build_params &bp, const kdgb_trace_params &tp,
               bool build, int reps, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2)
 {
     Score sc;
+    kdgb_graph *g = nullptr;
+    if (build) {
+        // A host-driven rebuild sizes the graph's buffers for these
+        // parameters; the graph then rebuilds with no host round trip.
+        if (rebuild(tree, w, bp) != KDGB_OK) return sc;
+        if (kdgb_graph_create(tree, w.tri, w.n_tris, w.n_meshes > 1 ? w.offsets : nullptr, w.n_meshes, &bp, 1.1f,
+                              nullptr, nullptr, nullptr, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, &g,
+                              (kdgb_stream_t)w.s) != KDGB_OK)
+            return sc;
+    }
     std::vector<float> bt, tt;
-    for (int r = 0; r <= reps; ++r) {
-        if (cudaEventRecord(e0, w.s) != cudaSuccess) return sc;
-        if (build && rebuild(tree, w, bp) != KDGB_OK) return sc;
-        if (cudaEventRecord(e1, w.s) != cudaSuccess) return sc;
-        if (trace(tree, w, tp) != KDGB_OK) return sc;
-        if (cudaEventRecord(e2, w.s) != cudaSuccess || cudaEventSynchronize(e2) != cudaSuccess) return sc;
+    bool ok = true;
+    for (int r = 0; r <= reps && ok; ++r) {
+        ok = cudaEventRecord(e0, w.s) == cudaSuccess;
+        if (ok && g) ok = kdgb_graph_launch(g, (kdgb_stream_t)w.s) == KDGB_OK;
+        ok = ok && cudaEventRecord(e1, w.s) == cudaSuccess;
+        // The trace reads the tree's host-side counts, which a graph rebuild
+        // refreshes at kdgb_graph_status; they equal the sizing rebuild's.
+        ok = ok && trace(tree, w, tp) == KDGB_OK;
+        ok = ok && cudaEventRecord(e2, w.s) == cudaSuccess && cudaEventSynchronize(e2) == cudaSuccess;
+        if (!ok) break;
         float b = 0.0f, t = 0.0f;
         cudaEventElapsedTime(&b, e0, e1);
         cudaEventElapsedTime(&t, e1, e2);
@@ -78,6 +95,11 @@ Score measure(kdgb_tree *tree, const Workload &w, const kdgb_build_params &bp, c
             tt.push_back(t);
         }
     }
+    if (g) {
+        if (ok && kdgb_graph_status(g, (kdgb_stream_t)w.s) != KDGB_OK) ok = false;
+        kdgb_graph_destroy(g);
+    }
+    if (!ok) return sc;
     sc.ok = true;
     sc.build_ms = median(bt);
     sc.trace_ms = median(tt);

@@ -2373,14 +2373,24 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
     }
     if (lower_loop(p)) {
         KDGB_CHECK(fetch_state(t, st, s));
+        bool first = true;
         while (st.low_R > 0) {
             const int64_t R = st.low_R;
             plan.max_low_R = std::max(plan.max_low_R, R);
             KDGB_CHECK(grow_nodes(t, (int64_t)st.n_nodes + 2 * R, st.n_nodes, s));
-            KDGB_CHECK(grab(w.ssplit, R, s));
-            KDGB_CHECK(grab(w.saddr, R + 1, s));
-            KDGB_CHECK(grab(w.careas, R, s));
-            KDGB_CHECK(grab(w.csets, R, s));
+            if (first) {
+                // The first level's decisions may already sit in these
+                // arrays (k_sah_planes writes them): they were sized for all
+                // upper leaves above and must not be regrown here.
+                if (R > w.ssplit.cap || R + 1 > w.saddr.cap || R > w.careas.cap || R > w.csets.cap)
+                    return fail(KDGB_ERR_CAPACITY, "first SAH lower level exceeds its decision arrays");
+                first = false;
+            } else {
+                KDGB_CHECK(grab(w.ssplit, R, s));
+                KDGB_CHECK(grab(w.saddr, R + 1, s));
+                KDGB_CHECK(grab(w.careas, R, s));
+                KDGB_CHECK(grab(w.csets, R, s));
+            }
             const Extents e{0, 0, F, st.n_nodes, nl, R};
             KDGB_CHECK(emit_lower_level(make_args(t, p, T, M, mesh_off_dev), L, e, w, s));
             KDGB_CHECK(fetch_state(t, st, s));

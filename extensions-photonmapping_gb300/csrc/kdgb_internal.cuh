@@ -273,6 +273,11 @@ inline int scan_exclusive(const int32_t *in, int32_t *out, int64_t n, cudaStream
 // Workspace (int32 elements) a scan of n records of K lanes needs.
 int64_t scan_partials_needed(int K, int64_t n);
 
+// Runs one look-back wait that must give up (see k_scan_giveup): result[0]
+// = the status it recorded, result[1] = the prefix it assumed for the tile
+// that never published.  Synchronises `s`.
+int scan_giveup_check(int32_t spin_limit, int32_t *result, cudaStream_t s);
+
 // Two independent scans (as scan_exclusive_in each) in one launch.
 template <int K1, class In1, int K2, class In2>
 int scan_exclusive_pair(const In1 &in1, int32_t *out1, int64_t n1, const int32_t *n1_dev, const In2 &in2,

@@ -9,8 +9,12 @@
 // (KDGB_NOALLOC_MAX_TRIS * 48 bytes = 3 MiB) until the process exits.
 //
 // Host code cannot use the array's name as a device address; the address is
-// fetched once per device with cudaGetSymbolAddress, on the first call made
-// with that device current, and cached.
+// fetched per device with cudaGetSymbolAddress, on the first call made with
+// that device current, and cached together with the identity of the CUDA
+// context it belongs to.  A context torn down and created again (after
+// cudaDeviceReset) reloads the module, possibly elsewhere: the next call sees
+// a different context id and fetches the address again.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -28,9 +32,42 @@ static __device__ __align__(256) float4 g_noalloc_tris[3 * KDGB_NOALLOC_MAX_TRIS
 
 std::mutex g_noalloc_mu;
 float4 *g_noalloc_addr[kMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kMaxDevices] = {};  // context id the address belongs to
 
-// Device address of g_noalloc_tris on the current device (set up on first use).
-int noalloc_scratch(float4 **out)
+// cuCtxGetCurrent / cuCtxGetId, fetched through the runtime so that the
+// library does not link the driver library itself.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+
+// Id of the context current on this thread; 0 when there is none.
+unsigned long long current_context_id()
+{
+    if (!g_ctx_current || !g_ctx_id) {
+        void *f0 = nullptr, *f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0, q1;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+        g_ctx_id = reinterpret_cast<CtxGetIdFn>(f1);
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx || g_ctx_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of g_noalloc_tris on the current device, looked up on the
+// first call with that device current and again whenever the device's
+// context has changed since.  The lookup may load the library's module, which
+// a stream capture does not allow: a call that needs it while `s` is
+// capturing is refused.
+int noalloc_scratch(float4 **out, cudaStream_t s)
 {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -40,11 +77,19 @@ int noalloc_scratch(float4 **out)
     }
     if (dev < 0 || dev >= kMaxDevices) return fail(KDGB_ERR_UNSUPPORTED, "kdgb_trace_brute_noalloc: device id too large");
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_noalloc_addr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone)
+            return fail(KDGB_ERR_UNSUPPORTED,
+                        "kdgb_trace_brute_noalloc: the first call on a device (or the first after its context was "
+                        "reset) looks up the scratch array and must not be made during stream capture");
+        cudaGetLastError();
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_tris);
         if (e != cudaSuccess) return cuda_fail(e, "kdgb_trace_brute_noalloc: cudaGetSymbolAddress");
         g_noalloc_addr[dev] = static_cast<float4 *>(p);
+        g_noalloc_ctx[dev] = current_context_id();
     }
     *out = g_noalloc_addr[dev];
     return KDGB_OK;
@@ -138,9 +183,9 @@ extern "C" int kdgb_trace_brute_noalloc(const float *tri_v_dev, int32_t n_tris, 
     if (n == 0) return KDGB_OK;
     if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev)
         return fail(KDGB_ERR_INVALID_ARGUMENT, "kdgb_trace_brute_noalloc: NULL ray or output buffer");
-    float4 *rec = nullptr;
-    KDGB_CHECK(noalloc_scratch(&rec));
     cudaStream_t s = (cudaStream_t)stream;
+    float4 *rec = nullptr;
+    KDGB_CHECK(noalloc_scratch(&rec, s));
     if (n_tris > 0) {
         k_noalloc_pack<<<(n_tris + kNoAllocBlock - 1) / kNoAllocBlock, kNoAllocBlock, 0, s>>>(tri_v_dev, n_tris, rec);
         KDGB_LAUNCH_CHECK();

@@ -22,6 +22,7 @@
 #include "kdgb_internal.cuh"
 
 #include <algorithm>
+#include <vector>
 
 namespace kdgb {
 
@@ -117,7 +118,8 @@ __device__ __forceinline__ unsigned load_flag(const int32_t *p)
 // n records of `in`, with its status in `status` (tiles of this scan only).
 template <int K, class In>
 __device__ __forceinline__ void scan_tile(const In &in, int32_t *__restrict__ out, int64_t n, int64_t tile,
-                                          int32_t *status, unsigned epoch, int32_t *err)
+                                          int32_t *status, unsigned epoch, int32_t *err,
+                                          int spin_limit = kSpinLimit)
 {
     __shared__ int32_t s_excl[K];
     const int64_t ntiles = (n + kTile - 1) / kTile;
@@ -152,7 +154,7 @@ __device__ __forceinline__ void scan_tile(const In &in, int32_t *__restrict__ ou
                 int spins = 0;
                 f = load_flag(status + kStatus * t + kFlag);
                 while ((f >> 2) != epoch || (f & 3u) == 0) {
-                    if (++spins > kSpinLimit) {
+                    if (++spins > spin_limit) {
                         if (err) atomicCAS(err, 0, KDGB_ERR_TIMEOUT);
                         f = (epoch << 2) | kPrefix;  // give up: count it as a zero prefix
                         dead = true;
@@ -262,7 +264,50 @@ __global__ void __launch_bounds__(kThreads) scan_pair_kernel(const In1 in1, int3
     scan_finish(ws, epoch);
 }
 
+// Give-up check of the look-back wait: one block scans tile 1 of a
+// two-tile scan whose tile 0 never publishes (its status words are zero, so
+// no flag ever matches).  The wait must stop after `spin_limit` polls, record
+// KDGB_ERR_TIMEOUT in *err, count the missing tile as a zero prefix and
+// finish the tile.  The status and output arrays are the caller's.
+__global__ void __launch_bounds__(kThreads) k_scan_giveup(const int32_t *__restrict__ in, int32_t *out,
+                                                           int32_t *status, int32_t *err, int spin_limit)
+{
+    ScanArray<1> a;
+    a.in = in;
+    scan_tile<1>(a, out, 2 * kTile, 1, status, 1u, err, spin_limit);
+}
+
 }  // namespace
+
+int scan_giveup_check(int32_t spin_limit, int32_t *result, cudaStream_t s)
+{
+    if (spin_limit < 1) return fail(KDGB_ERR_INVALID_ARGUMENT, "scan give-up check: spin_limit must be >= 1");
+    // in: 2 tiles of ones; out: 2 tiles + the totals record; status: 2 tiles;
+    // err: one word.
+    const int64_t n_in = 2 * kTile, n_out = 2 * kTile + 1, n_status = 2 * kStatus;
+    int32_t *buf = nullptr;
+    const int64_t words = n_in + n_out + n_status + 1;
+    KDGB_CUDA(cudaMallocAsync((void **)&buf, sizeof(int32_t) * words, s));
+    int32_t *in = buf, *out = in + n_in, *status = out + n_out, *err = status + n_status;
+    std::vector<int32_t> ones(n_in, 1);
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int32_t) * (n_out + n_status + 1), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(in, ones.data(), sizeof(int32_t) * n_in, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        k_scan_giveup<<<1, kThreads, 0, s>>>(in, out, status, err, spin_limit);
+        note_launch();
+        e = cudaGetLastError();
+    }
+    int32_t host[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&host[0], err, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    // The tile's first output: the exclusive prefix it assumed for tile 0.
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&host[1], out + kTile, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(buf, s);
+    if (e != cudaSuccess) return cuda_fail(e, "scan give-up check");
+    result[0] = host[0];
+    result[1] = host[1];
+    return KDGB_OK;
+}
 
 int64_t scan_partials_needed(int K, int64_t n)
 {

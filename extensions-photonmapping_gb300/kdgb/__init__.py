@@ -81,9 +81,17 @@ class HostTree:
 class KDTree:
     """Owner of one kdgb_tree handle."""
 
-    def __init__(self, handle: C.c_void_p, n_tris: int):
+    def __init__(self, handle: C.c_void_p, n_tris: int, stream: int = 0):
         self._h = handle
         self.n_tris = n_tris
+        # The stream of the last call that queued work on this handle: the
+        # handle's memory is freed ordered on it (kdgb_tree_release).
+        self._last_stream = stream
+
+    def _on(self, stream=None) -> C.c_void_p:
+        """The raw stream of a call, remembered as the handle's last."""
+        self._last_stream = _stream(stream)
+        return C.c_void_p(self._last_stream)
 
     # -- construction -----------------------------------------------------
     @classmethod
@@ -91,15 +99,14 @@ class KDTree:
         tri = _dev(tris, _torch().float32, 9)
         p = params if params is not None else build_params(**kw)
         h = C.c_void_p()
-        check(lib().kdgb_build(_ptr(tri), tri.shape[0], C.byref(p), C.byref(h), C.c_void_p(_stream(stream))),
-              "kdgb_build")
-        return cls(h, tri.shape[0])
+        st = _stream(stream)
+        check(lib().kdgb_build(_ptr(tri), tri.shape[0], C.byref(p), C.byref(h), C.c_void_p(st)), "kdgb_build")
+        return cls(h, tri.shape[0], st)
 
     def rebuild(self, tris, params: BuildParams | None = None, stream=None, **kw) -> None:
         tri = _dev(tris, _torch().float32, 9)
         p = params if params is not None else build_params(**kw)
-        check(lib().kdgb_rebuild(self._h, _ptr(tri), tri.shape[0], C.byref(p), C.c_void_p(_stream(stream))),
-              "kdgb_rebuild")
+        check(lib().kdgb_rebuild(self._h, _ptr(tri), tri.shape[0], C.byref(p), self._on(stream)), "kdgb_rebuild")
         self.n_tris = tri.shape[0]
 
     @classmethod
@@ -131,20 +138,23 @@ class KDTree:
         v.prim_indices = host("prim_indices", np.int32)
         v.leaf_ids = host("leaf_ids", np.int32)
         h = C.c_void_p()
+        st = _stream(stream)
         check(lib().kdgb_tree_upload(C.byref(v), tris.ctypes.data_as(C.c_void_p), tris.shape[0], C.byref(h),
-                                     C.c_void_p(_stream(stream))), "kdgb_tree_upload")
-        return cls(h, tris.shape[0])
+                                     C.c_void_p(st)), "kdgb_tree_upload")
+        return cls(h, tris.shape[0], st)
 
     def close(self) -> None:
+        """Frees the handle after the work queued on the stream it was last
+        used on (kdgb_tree_release)."""
         if self._h:
-            check(lib().kdgb_tree_destroy(self._h), "kdgb_tree_destroy")
-            self._h = None
+            h, self._h = self._h, None
+            check(lib().kdgb_tree_release(h, C.c_void_p(self._last_stream)), "kdgb_tree_release")
 
     def __del__(self):
         try:
             if self._h:
-                lib().kdgb_tree_destroy(self._h)
-                self._h = None
+                h, self._h = self._h, None
+                lib().kdgb_tree_release(h, C.c_void_p(self._last_stream))
         except Exception:
             pass
 
@@ -198,7 +208,7 @@ class KDTree:
                    torch.empty(n, dtype=torch.float32, device=o.device))
         hit, t, u, v = out
         check(lib().kdgb_trace(self._h, C.byref(p), _ptr(o), _ptr(d), n, _ptr(hit), _ptr(t), _ptr(u), _ptr(v),
-                               C.c_void_p(_stream(stream))), "kdgb_trace")
+                               self._on(stream)), "kdgb_trace")
         return hit, t, u, v
 
     def trace_shadow(self, points, light, params: TraceParams | None = None, stream=None, **kw):
@@ -208,7 +218,7 @@ class KDTree:
         lp = (C.c_float * 3)(*[float(x) for x in light])
         occ = torch.empty(pts.shape[0], dtype=torch.int32, device=pts.device)
         check(lib().kdgb_trace_shadow(self._h, C.byref(p), _ptr(pts), pts.shape[0], lp, _ptr(occ),
-                                      C.c_void_p(_stream(stream))), "kdgb_trace_shadow")
+                                      self._on(stream)), "kdgb_trace_shadow")
         return occ
 
     def trace_primary_shadow(self, o, d, light, params: TraceParams | None = None, stream=None, out=None, **kw):
@@ -226,7 +236,7 @@ class KDTree:
                    torch.empty(n, dtype=torch.int32, device=o.device))
         hit, t, u, v, occ = out
         check(lib().kdgb_trace_primary_shadow(self._h, C.byref(p), _ptr(o), _ptr(d), n, lp, _ptr(hit), _ptr(t),
-                                              _ptr(u), _ptr(v), _ptr(occ), C.c_void_p(_stream(stream))),
+                                              _ptr(u), _ptr(v), _ptr(occ), self._on(stream)),
               "kdgb_trace_primary_shadow")
         return hit, t, u, v, occ
 
@@ -244,7 +254,7 @@ def _trace_photons(self, n_photons: int, params: TraceParams | None = None, phot
                torch.empty((n_photons, S), dtype=torch.float32, device="cuda"))
     hit, t = out
     check(lib().kdgb_trace_photons(self._h, C.byref(p), C.byref(ph), n_photons, _ptr(hit), _ptr(t),
-                                   C.c_void_p(_stream(stream))), "kdgb_trace_photons")
+                                   self._on(stream)), "kdgb_trace_photons")
     return hit, t
 
 
@@ -266,7 +276,7 @@ def _trace_shaded(self, o, d, n0, n1, n2, c0, params: TraceParams | None = None,
     if out is None:
         out = torch.empty((n, 4), dtype=torch.uint8, device=o.device)
     check(lib().kdgb_trace_shaded(self._h, C.byref(p), _ptr(n0), _ptr(n1), _ptr(n2), _ptr(c0), C.byref(L),
-                                  max_bounces, _ptr(o), _ptr(d), n, _ptr(out), C.c_void_p(_stream(stream))),
+                                  max_bounces, _ptr(o), _ptr(d), n, _ptr(out), self._on(stream)),
           "kdgb_trace_shaded")
     return out
 
@@ -281,9 +291,10 @@ def _build_batch(cls, tris, mesh_offsets, params: BuildParams | None = None, str
     off = np.ascontiguousarray(mesh_offsets, dtype=np.int32)
     p = params if params is not None else build_params(**kw)
     h = C.c_void_p()
+    st = _stream(stream)
     check(lib().kdgb_build_batch(_ptr(tri), off.ctypes.data_as(C.c_void_p), off.shape[0] - 1, C.byref(p),
-                                 C.byref(h), C.c_void_p(_stream(stream))), "kdgb_build_batch")
-    tree = cls(h, tri.shape[0])
+                                 C.byref(h), C.c_void_p(st)), "kdgb_build_batch")
+    tree = cls(h, tri.shape[0], st)
     tree.mesh_offsets = off
     return tree
 
@@ -302,7 +313,7 @@ def _trace_batch(self, o, d, ray_mesh=None, rays_per_mesh: int = 0, params: Trac
                torch.empty(n, dtype=torch.float32, device=o.device), torch.empty(n, dtype=torch.float32, device=o.device))
     hit, t, u, v = out
     check(lib().kdgb_trace_batch(self._h, C.byref(p), _ptr(o), _ptr(d), _ptr(rm), rays_per_mesh, n, _ptr(hit),
-                                 _ptr(t), _ptr(u), _ptr(v), C.c_void_p(_stream(stream))), "kdgb_trace_batch")
+                                 _ptr(t), _ptr(u), _ptr(v), self._on(stream)), "kdgb_trace_batch")
     return hit, t, u, v
 
 
@@ -312,7 +323,7 @@ def _rebuild_batch(self, tris, mesh_offsets, params: BuildParams | None = None, 
     off = np.ascontiguousarray(mesh_offsets, dtype=np.int32)
     p = params if params is not None else build_params(**kw)
     check(lib().kdgb_rebuild_batch(self._h, _ptr(tri), off.ctypes.data_as(C.c_void_p), off.shape[0] - 1,
-                                   C.byref(p), C.c_void_p(_stream(stream))), "kdgb_rebuild_batch")
+                                   C.byref(p), self._on(stream)), "kdgb_rebuild_batch")
     self.n_tris = tri.shape[0]
     self.mesh_offsets = off
 
@@ -355,15 +366,15 @@ class Graph:
                                       off.ctypes.data_as(C.c_void_p) if off is not None else None, n_meshes,
                                       C.byref(p), headroom, C.byref(tp), _ptr(self.o), _ptr(self.d),
                                       _ptr(self.ray_mesh), rays_per_mesh, n, _ptr(hit), _ptr(t), _ptr(u), _ptr(v),
-                                      C.byref(g), C.c_void_p(_stream(stream))), "kdgb_graph_create")
+                                      C.byref(g), tree._on(stream)), "kdgb_graph_create")
         self._g = g
 
     def launch(self, stream=None) -> None:
-        check(lib().kdgb_graph_launch(self._g, C.c_void_p(_stream(stream))), "kdgb_graph_launch")
+        check(lib().kdgb_graph_launch(self._g, self.tree._on(stream)), "kdgb_graph_launch")
 
     def status(self, stream=None) -> int:
         """Synchronises and returns the last launch's build status (0 = ok)."""
-        return lib().kdgb_graph_status(self._g, C.c_void_p(_stream(stream)))
+        return lib().kdgb_graph_status(self._g, self.tree._on(stream))
 
     def close(self) -> None:
         if getattr(self, "_g", None):

@@ -88,6 +88,8 @@ SIGNATURES = {
     "kdgb_rebuild": (C.c_int, [P, P, C.c_int32, C.POINTER(BuildParams), P]),
     "kdgb_tree_upload": (C.c_int, [C.POINTER(TreeView), P, C.c_int32, C.POINTER(C.c_void_p), P]),
     "kdgb_tree_destroy": (C.c_int, [P]),
+    "kdgb_tree_release": (C.c_int, [P, P]),
+    "kdgb_check_scan_giveup": (C.c_int, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), P]),
     "kdgb_tree_view_get": (C.c_int, [P, C.POINTER(TreeView)]),
     "kdgb_tree_download": (C.c_int, [P, C.POINTER(TreeView)]),
     "kdgb_tree_stats": (C.c_int, [P, C.POINTER(BuildStats)]),

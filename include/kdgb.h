@@ -40,7 +40,7 @@ typedef struct CUstream_st *kdgb_stream_t; /* same type as cudaStream_t */
 #define KDGB_API
 #endif
 
-#define KDGB_ABI_VERSION 3
+#define KDGB_ABI_VERSION 4
 
 /* Utils/CUDA/Utils.h:18: the reference's "infinity" is the integer
  * 0x7f800000 converted to float. */
@@ -189,7 +189,17 @@ KDGB_API int kdgb_rebuild(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tri
 KDGB_API int kdgb_tree_upload(const kdgb_tree_view *host_arrays, const float *tri_v_host, int32_t n_tris,
                      kdgb_tree **out, kdgb_stream_t stream);
 
+/* Frees the handle.  The frees are ordered on the legacy default stream,
+ * which a non-blocking stream does not wait for: work still queued on such
+ * a stream must be finished first, or use kdgb_tree_release. */
 KDGB_API int kdgb_tree_destroy(kdgb_tree *tree);
+
+/* kdgb_tree_destroy ordered on `stream`: the device memory is freed after
+ * the work already queued on `stream` (pass the stream the tree was last
+ * used on), then that stream is synchronised.  The reference's TriangleMap
+ * has no destructor (TriangleMap.cu:27-49); its device blocks live until
+ * exit. */
+KDGB_API int kdgb_tree_release(kdgb_tree *tree, kdgb_stream_t stream);
 
 /* Replaces the KDNode / TriangleNode getters: device SoA pointers, valid
  * until the next kdgb_rebuild or kdgb_tree_destroy of this handle. */
@@ -235,6 +245,8 @@ typedef struct kdgb_photon_params {
     float    survival;   /* Russian-roulette survival probability (0.7) */
 } kdgb_photon_params;
 
+/* Defaults: light (0.5, 3, 0.5) (the frame's point light), seed 3,
+ * 3 bounces, survival 0.7. */
 KDGB_API void kdgb_photon_params_default(kdgb_photon_params *p);
 
 /* Photon tracing (no reference counterpart; the reference's PhotonMapping
@@ -432,6 +444,17 @@ KDGB_API int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t ti
                      int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
                      kdgb_stream_t stream);
 
+/* Check of the bounded device-side waits (no counterpart in the reference,
+ * which ignores CUDPP's return codes, TriangleMapUpperCreator.cu:58-76).
+ * Runs one block of the look-back scan on a tile whose predecessor never
+ * publishes its status, with the wait limited to spin_limit polls (>= 1;
+ * the library's own scans allow 2^22).  The wait gives up, records its
+ * status in *recorded_status (KDGB_ERR_TIMEOUT) and finishes the tile with
+ * the missing prefix counted as *assumed_prefix (0); the device stays
+ * usable.  Allocates a few KB, synchronises `stream`. */
+KDGB_API int kdgb_check_scan_giveup(int32_t spin_limit, int32_t *recorded_status, int32_t *assumed_prefix,
+                                    kdgb_stream_t stream);
+
 /* Largest triangle count kdgb_trace_brute_noalloc accepts. */
 #define KDGB_NOALLOC_MAX_TRIS 65536
 
@@ -445,8 +468,11 @@ KDGB_API int kdgb_trace_brute(const float *tri_v_dev, int32_t n_tris, int32_t ti
  * every GPU that loads the library until the process exits.
  *  - n_tris > KDGB_NOALLOC_MAX_TRIS is rejected with KDGB_ERR_CAPACITY.
  *  - The first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) with that device current and caches it; make
- *    that first call before any stream capture.
+ *    (cudaGetSymbolAddress) with that device current and caches it with the
+ *    id of the device's context; make that first call before any stream
+ *    capture (such a call is refused with KDGB_ERR_UNSUPPORTED).  After
+ *    cudaDeviceReset the context id changes and the next call looks the
+ *    address up again, so it too must come before any capture.
  *  - All calls share the one array and each call overwrites the part it
  *    uses; calls whose work overlaps on the GPU (other streams, other host
  *    threads) race on it and must be serialised by the caller. */

@@ -17,6 +17,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -331,6 +332,14 @@ private:
 
 // Utils/CUDA/IRayTracer.h:28-58.  Trace writes first-hit buffers (device
 // pointers) instead of shading into an OpenGL canvas.
+// What HostTrace found for one pixel: the shaded colour (the reference logs
+// it as "Final color") and the pixel ray's first hit.
+struct HostTraceResult {
+    uchar4 color;
+    int hit;      // triangle id, -1 = miss
+    float t, u, v;
+};
+
 class IRayTracer {
 public:
     enum IntersectionAlgorithm { MOELLER, WOOP };
@@ -344,6 +353,22 @@ public:
     // set) into canvasData, with Light() as the scene light.
     virtual void Trace(const float *origins, const float *directions, int n, uchar4 *canvasData,
                        cudaStream_t s = 0) = 0;
+
+    // HostTrace(int x, int y, TriangleNode*) (IRayTracer.h:48;
+    // Raytracer.cu:392-459, ShortStack.cu:323-351, BruteTracer.cu:174-199):
+    // re-traces the ray of pixel (x, y) -- ray x + y * GetScreenWidth() of
+    // the last Trace call's rays -- and returns its colour and first hit.
+    // The reference runs its tracer function on the host; here the same
+    // device tracer as Trace runs on that one ray and the result is copied
+    // back (synchronises `s`).  `nodes` must be NULL or the traced map's
+    // current GetNodes(): the map's own tree is what is traced.
+    virtual HostTraceResult HostTrace(int x, int y, Scene::TriangleNode *nodes = nullptr, cudaStream_t s = 0) = 0;
+
+    // The image width that maps (x, y) to a ray: Params().tile_width when it
+    // is set, otherwise the width given here (the reference takes it from the
+    // canvas, IRayTracer.cu:45-70).
+    void SetScreenWidth(const int w) { screenWidth_ = w; }
+    int GetScreenWidth() const { return p_.tile_width > 0 ? p_.tile_width : screenWidth_; }
 
     void SetIntersectionAlgorithm(const IntersectionAlgorithm a)
     {
@@ -360,12 +385,81 @@ public:
     kdgb_light &Light() { return light_; }
 
 protected:
+    void Remember(const float *o, const float *d, int n)
+    {
+        lastO_ = o;
+        lastD_ = d;
+        lastN_ = n;
+    }
+    // The device index of ray (x, y) of the last Trace; throws when there is
+    // none.
+    int PixelRay(int x, int y) const
+    {
+        const int w = GetScreenWidth();
+        if (!lastO_ || w <= 0 || x < 0 || x >= w || y < 0)
+            throw Core::Exception("IRayTracer::HostTrace: no traced image or pixel outside it");
+        const int64_t id = (int64_t)x + (int64_t)y * w;
+        if (id >= lastN_) throw Core::Exception("IRayTracer::HostTrace: pixel outside the last traced rays");
+        return (int)id;
+    }
+    // Runs `first_hit` (one ray -> hit/t/u/v on the device) and `shade`
+    // (one ray -> one RGBA pixel) for ray `id` and copies both back.
+    template <class Hit, class Shade>
+    HostTraceResult OnePixel(int id, Hit &&first_hit, Shade &&shade, cudaStream_t s)
+    {
+        detail::DeviceBuffer<float> buf;
+        buf.resize(8);
+        float *t = buf.p, *u = buf.p + 1, *v = buf.p + 2;
+        int *hit = reinterpret_cast<int *>(buf.p + 3);
+        uint8_t *rgba = reinterpret_cast<uint8_t *>(buf.p + 4);
+        const float *o = lastO_ + 3 * (int64_t)id, *d = lastD_ + 3 * (int64_t)id;
+        kdgb_trace_params p = p_;
+        p.tile_width = 0;
+        detail::check(first_hit(p, o, d, hit, t, u, v), "IRayTracer::HostTrace");
+        detail::check(shade(p, o, d, rgba), "IRayTracer::HostTrace");
+        float host[5];
+        detail::cuda(cudaMemcpyAsync(host, buf.p, sizeof(host), cudaMemcpyDeviceToHost, s), "IRayTracer::HostTrace");
+        detail::cuda(cudaStreamSynchronize(s), "IRayTracer::HostTrace");
+        HostTraceResult r;
+        r.t = host[0];
+        r.u = host[1];
+        r.v = host[2];
+        std::memcpy(&r.hit, &host[3], 4);
+        std::memcpy(&r.color, &host[4], 4);
+        return r;
+    }
+    static void CheckNodes(const kdgb_tree *tree, Scene::TriangleNode *nodes)
+    {
+        if (!nodes) return;
+        kdgb_tree_view v;
+        detail::check(kdgb_tree_view_get(tree, &v), "IRayTracer::HostTrace");
+        if (reinterpret_cast<int8_t *>(nodes->GetInfoData()) != v.info)
+            throw Core::Exception("IRayTracer::HostTrace: nodes are not the traced map's current tree");
+    }
     void TraceTree(const kdgb_tree *tree, bool propagate, const float *o, const float *d, int n, int *hit, float *t,
                    float *u, float *v, cudaStream_t s)
     {
+        Remember(o, d, n);
         kdgb_trace_params p = p_;
         if (!propagate) p.leaf_skipping = 0;  // Raytracer.cu:313
         Timed([&] { return kdgb_trace(tree, &p, o, d, n, hit, t, u, v, s); }, "IRayTracer::Trace", s);
+    }
+    HostTraceResult HostTraceTree(const kdgb_tree *tree, bool propagate, const GeometryList *g, int x, int y,
+                                  Scene::TriangleNode *nodes, cudaStream_t s)
+    {
+        CheckNodes(tree, nodes);
+        const int id = PixelRay(x, y);
+        return OnePixel(
+            id,
+            [&](kdgb_trace_params &p, const float *o, const float *d, int *hit, float *t, float *u, float *v) {
+                if (!propagate) p.leaf_skipping = 0;
+                return kdgb_trace(tree, &p, o, d, 1, hit, t, u, v, s);
+            },
+            [&](kdgb_trace_params &p, const float *o, const float *d, uint8_t *rgba) {
+                return kdgb_trace_shaded(tree, &p, g->GetNormal0Data(), g->GetNormal1Data(), g->GetNormal2Data(),
+                                         g->GetColor0Data(), &light_, 0, o, d, 1, rgba, s);
+            },
+            s);
     }
     template <class F>
     void Timed(F &&f, const char *where, cudaStream_t s)
@@ -385,6 +479,7 @@ protected:
     void ShadeTree(const kdgb_tree *tree, bool propagate, const GeometryList *g, const float *o, const float *d, int n,
                    uchar4 *canvas, cudaStream_t s)
     {
+        Remember(o, d, n);
         kdgb_trace_params p = p_;
         if (!propagate) p.leaf_skipping = 0;
         Timed([&] {
@@ -395,6 +490,9 @@ protected:
     kdgb_trace_params p_;
     kdgb_light light_ = DefaultLight();
     float renderTime_ = 0.0f;
+    int screenWidth_ = 0;
+    const float *lastO_ = nullptr, *lastD_ = nullptr;
+    int lastN_ = 0;
 
 private:
     static kdgb_light DefaultLight()
@@ -416,6 +514,10 @@ public:
     {
         ShadeTree(map_->Handle(), map_->GetPropagateBoundingBox(), map_->GetGeometry(), o, d, n, canvas, s);
     }
+    HostTraceResult HostTrace(int x, int y, Scene::TriangleNode *nodes = nullptr, cudaStream_t s = 0) override
+    {
+        return HostTraceTree(map_->Handle(), map_->GetPropagateBoundingBox(), map_->GetGeometry(), x, y, nodes, s);
+    }
 
 private:
     TriangleMap *map_;
@@ -432,6 +534,10 @@ public:
     {
         ShadeTree(map_->Handle(), map_->GetPropagateBoundingBox(), map_->GetGeometry(), o, d, n, canvas, s);
     }
+    HostTraceResult HostTrace(int x, int y, Scene::TriangleNode *nodes = nullptr, cudaStream_t s = 0) override
+    {
+        return HostTraceTree(map_->Handle(), map_->GetPropagateBoundingBox(), map_->GetGeometry(), x, y, nodes, s);
+    }
 
 private:
     TriangleMap *map_;
@@ -443,17 +549,36 @@ public:
     explicit BruteTracer(GeometryList *geom) : IRayTracer(KDGB_TRACER_BRUTE), geom_(geom) {}
     void Trace(const float *o, const float *d, int n, int *hit, float *t, float *u, float *v, cudaStream_t s = 0) override
     {
+        Remember(o, d, n);
         detail::check(kdgb_trace_brute_ex(geom_->GetTriangleData(), geom_->GetSize(), &p_, o, d, n, hit, t, u, v, s),
                       "BruteTracer::Trace");
     }
     void Trace(const float *o, const float *d, int n, uchar4 *canvas, cudaStream_t s = 0) override
     {
+        Remember(o, d, n);
         const GeometryList *g = geom_;
         Timed([&] {
             return kdgb_trace_brute_shaded(g->GetTriangleData(), g->GetSize(), &p_, g->GetNormal0Data(),
                                            g->GetNormal1Data(), g->GetNormal2Data(), g->GetColor0Data(), &light_, 0, o,
                                            d, n, reinterpret_cast<uint8_t *>(canvas), s);
         }, "BruteTracer::Trace", s);
+    }
+    // BruteTracer::HostTrace (BruteTracer.cu:174-199) tests every triangle;
+    // `nodes` is not used, as in the reference.
+    HostTraceResult HostTrace(int x, int y, Scene::TriangleNode * = nullptr, cudaStream_t s = 0) override
+    {
+        const GeometryList *g = geom_;
+        return OnePixel(
+            PixelRay(x, y),
+            [&](kdgb_trace_params &p, const float *o, const float *d, int *hit, float *t, float *u, float *v) {
+                return kdgb_trace_brute_ex(g->GetTriangleData(), g->GetSize(), &p, o, d, 1, hit, t, u, v, s);
+            },
+            [&](kdgb_trace_params &p, const float *o, const float *d, uint8_t *rgba) {
+                return kdgb_trace_brute_shaded(g->GetTriangleData(), g->GetSize(), &p, g->GetNormal0Data(),
+                                               g->GetNormal1Data(), g->GetNormal2Data(), g->GetColor0Data(), &light_,
+                                               0, o, d, 1, rgba, s);
+            },
+            s);
     }
 
 private:

@@ -244,7 +244,7 @@ class PhotonParams(C.Structure):
     _fields_ = [("light", C.c_float * 3), ("seed", C.c_uint64), ("bounces", C.c_int32), ("survival", C.c_float)]
 
 
-def trace_photons(tree: Tree, tris, n: int, light=(0.5, 0.5, 0.5), seed: int = 3, bounces: int = 3,
+def trace_photons(tree: Tree, tris, n: int, light=(0.5, 3.0, 0.5), seed: int = 3, bounces: int = 3,
                   survival: float = 0.7, threads: int = 0, **kw):
     """Photon segments (hit, t) of shape (n, bounces + 1)."""
     L = lib()
@@ -335,15 +335,36 @@ _refpin_upper = None
 _refpin = None
 
 
+# Where the pin recipe reads the reference's sources (its REF).
+REFERENCE_TREE = os.environ.get("KDGB_REFERENCE_TREE", "/root/reference")
+
+
+def reference_tree_available() -> bool:
+    return os.path.isfile(os.path.join(REFERENCE_TREE, "Utils", "CUDA", "IRayTracer.h"))
+
+
+def _make_pin(target: str, lib_path: str, jobs: int = 1) -> bool:
+    """Builds one pin library with oracle/refpin/Makefile.  False where the
+    reference tree is absent (nothing to pin against: callers skip); a
+    recipe that fails with the tree present raises, so a broken pin build
+    cannot turn the pin tests into skips."""
+    if not reference_tree_available():
+        return False
+    r = subprocess.run(["make", "-s", f"-j{jobs}", "-C", _REFPIN_DIR, f"REF={REFERENCE_TREE}", target],
+                       capture_output=True, text=True)
+    if r.returncode != 0 or not os.path.exists(lib_path):
+        raise RuntimeError(f"pin recipe failed for {target} (REF={REFERENCE_TREE}):\n{r.stdout}\n{r.stderr}")
+    return True
+
+
 def refpin_lib():
     """Loads oracle/_ref/librefpin.so, building it with the committed recipe
-    first.  Returns None where the reference tree is not available (the
-    recipe then fails), so callers can skip."""
+    first.  Returns None where the reference tree is not available, so
+    callers can skip; raises when the tree is there and the recipe fails."""
     global _refpin
     if _refpin is not None:
         return _refpin
-    r = subprocess.run(["make", "-s", "-C", _REFPIN_DIR, "../_ref/librefpin.so"], capture_output=True, text=True)
-    if r.returncode != 0 or not os.path.exists(_REFPIN_LIB):
+    if not _make_pin("../_ref/librefpin.so", _REFPIN_LIB):
         return None
     L = C.CDLL(_REFPIN_LIB)
     F = C.POINTER(C.c_float)
@@ -366,13 +387,12 @@ def refpin_lib():
 def refpin_upper_lib():
     """Loads oracle/_ref/librefpin_upper.so (the reference's upper-phase
     kernels run on the host), building it with the committed recipe first.
-    Returns None where the reference tree is not available."""
+    Returns None where the reference tree is not available (raises when
+    it is and the recipe fails)."""
     global _refpin_upper
     if _refpin_upper is not None:
         return _refpin_upper
-    r = subprocess.run(["make", "-s", "-C", _REFPIN_DIR, "../_ref/librefpin_upper.so"], capture_output=True,
-                       text=True)
-    if r.returncode != 0 or not os.path.exists(_REFPIN_UPPER_LIB):
+    if not _make_pin("../_ref/librefpin_upper.so", _REFPIN_UPPER_LIB):
         return None
     L = C.CDLL(_REFPIN_UPPER_LIB)
     L.ref_upper.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int] + \
@@ -470,13 +490,12 @@ def refpin_trace_lib():
     """Loads oracle/_ref/librefpin_trace.so (the reference's Raytracer.cu,
     ShortStack.cu and BruteTracer.cu compiled unmodified, their traversal
     functions called on the host), building it with the committed recipe
-    first.  Returns None where the reference tree or nvcc is not available."""
+    first.  Returns None where the reference tree is not available (raises
+    when it is and the recipe fails)."""
     global _refpin_trace
     if _refpin_trace is not None:
         return _refpin_trace
-    r = subprocess.run(["make", "-s", "-j4", "-C", _REFPIN_DIR, "../_ref/librefpin_trace.so"], capture_output=True,
-                       text=True)
-    if r.returncode != 0 or not os.path.exists(_REFPIN_TRACE_LIB):
+    if not _make_pin("../_ref/librefpin_trace.so", _REFPIN_TRACE_LIB, jobs=4):
         return None
     L = C.CDLL(_REFPIN_TRACE_LIB)
     P, I = C.c_void_p, C.c_int

@@ -6,7 +6,9 @@
 //   int32 T, int32 n, float tris[T*9], float o[n*3], float d[n*3],
 //   then for restart, short-stack, brute: int32 hit[n], float t[n],
 //   then float n0/n1/n2[T*4], uint8 c0[T*4] (the GeometryList attributes),
-//   then for restart, short-stack, brute: uint8 rgba[n*4] (shaded Trace).
+//   then for restart, short-stack, brute: uint8 rgba[n*4] (shaded Trace),
+//   then for restart, short-stack, brute and 4 pixels each: HostTrace's
+//   int32 hit, float t, uint8 rgba[4].
 #include <cstdio>
 #include <vector>
 
@@ -106,6 +108,26 @@ int main(int argc, char **argv)
         tr->Trace(od, dd, n, canvas);
         cudaMemcpy(px.data(), canvas, px.size(), cudaMemcpyDeviceToHost);
         std::fwrite(px.data(), 1, px.size(), f);
+    }
+    // HostTrace of pixels of the last traced image (side x side), after
+    // one more shaded Trace per tracer so that each has rays to look up.
+    const int probes[4][2] = {{0, 0}, {side / 2, side / 3}, {side - 1, 17}, {5, side - 1}};
+    for (IRayTracer *tr : tracers) {
+        tr->SetScreenWidth(side);
+        tr->Trace(od, dd, n, canvas);
+        for (const auto &xy : probes) {
+            const HostTraceResult r = tr->HostTrace(xy[0], xy[1], tr == &brute ? nullptr : map.GetNodes());
+            std::fwrite(&r.hit, 4, 1, f);
+            std::fwrite(&r.t, 4, 1, f);
+            std::fwrite(&r.color, 4, 1, f);
+        }
+        bool outside = false;
+        try {
+            tr->HostTrace(side, 0);
+        } catch (const Core::Exception &) {
+            outside = true;
+        }
+        if (!outside) return 6;
     }
     std::fclose(f);
     std::printf("plugin demo: %d triangles, %d nodes, build %.3f ms\n", T, map.GetNodes()->GetSize(),

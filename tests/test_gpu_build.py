@@ -165,6 +165,26 @@ def test_rebuild_reuses_handle(kdgb_lib, cuda, oracle):
         assert_same_tree(tree.to_host(), oracle.build(a))
 
 
+@pytest.mark.parametrize("lower", [1, 2])
+def test_rebuild_grows_lower_decision_arrays(kdgb_lib, cuda, oracle, lower):
+    """A handle first built over a small scene (small lower-phase arrays)
+    rebuilt host-driven over one with many more upper leaves: the first
+    lower level's decisions, which the plane kernel writes before the lower
+    loop starts, must survive the arrays' growth."""
+    kw = dict(configs_sah(), lower=lower)
+    small, big = scenes.clustered(500, seed=41), scenes.clustered(60000, seed=42)
+    with kdgb_lib.KDTree.build(small, **kw) as tree:
+        tree.rebuild(big, **kw)
+        assert_same_tree(tree.to_host(), oracle.build(big, **kw))
+        tree.rebuild(small, **kw)
+        assert_same_tree(tree.to_host(), oracle.build(small, **kw))
+
+
+def configs_sah():
+    from kdgb import configs
+    return dict(configs.SAH)
+
+
 def test_nonfinite_is_an_error(kdgb_lib, cuda):
     tris = scenes.clustered(1000, seed=2)
     tris[10, 2] = np.inf

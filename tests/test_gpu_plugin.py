@@ -52,6 +52,16 @@ def test_cpp_plugin_frame_matches_oracle(kdgb_lib, cuda, oracle, tmp_path):
     pixels = []
     for _ in range(3):
         pixels.append(raw[off:off + 4 * n].reshape(n, 4)); off += 4 * n
+    side = int(round(np.sqrt(n)))
+    probes = [(0, 0), (side // 2, side // 3), (side - 1, 17), (5, side - 1)]
+    host_traces = []
+    for _ in range(3):
+        rows = []
+        for _ in probes:
+            ht = int(np.frombuffer(raw[off:off + 4].tobytes(), np.int32)[0])
+            tt = np.frombuffer(raw[off + 4:off + 8].tobytes(), np.float32)[0]
+            rows.append((ht, tt, raw[off + 8:off + 12].copy())); off += 12
+        host_traces.append(rows)
     assert off == raw.shape[0]
     assert T == 2 * 48 * 48
     tree = oracle.build(tris, lower=1)  # TriangleMap defaults + SetLowerAlgorithm(SAH)
@@ -65,6 +75,14 @@ def test_cpp_plugin_frame_matches_oracle(kdgb_lib, cuda, oracle, tmp_path):
                                    tracer=tracer)
         assert np.array_equal(px, want), tracer
         assert (px[m, 3] > 0).all()
+        # HostTrace(x, y) re-traces pixel x + y * side on the device: the same
+        # first hit and colour as the full frame.
+        for (x, y), (ht, tt, rgba) in zip(probes, host_traces[tracer]):
+            i = x + y * side
+            assert ht == hr[i], (tracer, x, y)
+            if hr[i] >= 0:
+                assert np.float32(tt).view(np.uint32) == tr[i].view(np.uint32)
+            assert np.array_equal(rgba, want[i]), (tracer, x, y)
 
 
 def test_geometry_gather_matches_numpy(kdgb_lib, cuda):

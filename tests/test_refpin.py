@@ -183,3 +183,13 @@ def test_lower_creators_pinned(oracle, pins, lower, cost, propagate, scene):
             assert np.array_equal(a, b), f
     if lower == 2 or cost < 20:  # both creators split at these costs
         assert ours.n_nodes > upper.n_nodes
+
+
+def test_pin_libraries_build_where_the_reference_is_present(oracle):
+    """Where the reference tree is present every pin library must build: a
+    failing recipe raises instead of turning the pin tests into skips."""
+    if not oracle.reference_tree_available():
+        pytest.skip("no reference tree on this machine (the pins are built where it is)")
+    assert oracle.refpin_lib() is not None
+    assert oracle.refpin_upper_lib() is not None
+    assert oracle.refpin_trace_lib() is not None
