@@ -18,12 +18,20 @@ from kdgb import scenes
 pytestmark = pytest.mark.gpu
 
 REL = 1e-4  # relative tolerance of the contract
-# Per-component floor, as a fraction of A = the sum of the magnitudes of the
-# per-ray terms that make up that gradient component (FP64).  A component
-# whose terms cancel can be far smaller than its terms; fp32 arithmetic and
-# float atomics then leave an error of a few ulps of A, not of the result.
-# Every component must satisfy |g - G| <= REL * |G| + FLOOR * A.
-FLOOR = 1e-5
+EPS32 = 2.0 ** -24
+# Per-component check: |g - G| <= REL * |G| + FLOOR, where the floor is the
+# fp32 rounding that the closed form cannot avoid, summed over the rays that
+# make up the component:
+#   C_TERM * B  first-order rounding bound of each ray's term (B, below),
+#               dominated by the barycentric weights: u = (p . s) / det adds
+#               products of size |p||s| that cancel to u * det when the ray
+#               origin is far from the small triangle (here 1.5 units from
+#               edges of 3e-3), so fp32 u and v carry ~1e-5 relative error;
+#   K * EPS32 * A  fp32 accumulation of the K terms of the component
+#               (A = sum of their magnitudes).
+# Measured against an fp32 restatement of the kernel, each term's error stays
+# below 1.2 B, so C_TERM = 4 leaves a margin of more than 3.
+C_TERM = 4.0
 
 
 def mt64(V, idx, hit, o, d):
@@ -42,9 +50,52 @@ def mt64(V, idx, hit, o, d):
     return np.where(m, t, 0.0), np.where(m, u, 0.0), np.where(m, v, 0.0)
 
 
-def grad64(V, idx, hit, o, d, gt, gu, gv, magnitudes=False):
-    """FP64 brute-force reference gradient: closed form over every ray.
-    With magnitudes=True: the sum of |term| per component instead."""
+def rounding_floor(V, idx, hit, o, d, gt, gu, gv):
+    """Per component (V.shape): the floor of the per-component check,
+    C_TERM * B + K * EPS32 * A (see the module constants), from FP64
+    quantities.  B bounds each term w_k * lambda (w = 1 - u - v, u, v) to
+    first order: |w_k| d(lambda) + d(w_k) |lambda|, with
+      du = eps (sum|p_i s_i| + sum|p_i| (|o_i| + |v0_i|) + |u| sum|p_i e1_i|) / |det|
+      dv likewise with q . d (q = s x e1, s itself rounded),
+      d(lambda_j) = eps (sum_k |g_k| |vec_k,j|) / |D| + eps |lambda_j| sum|d_i n_i| / |D|,
+    where n = e1 x e2, D = d . n and vec = (n, d x e2, d x e1)."""
+    m = hit >= 0
+    h, o, d, gt, gu, gv = hit[m], o[m], d[m], gt[m], gu[m], gv[m]
+    i0, i1, i2 = idx[3 * h], idx[3 * h + 1], idx[3 * h + 2]
+    v0, v1, v2 = V[i0], V[i1], V[i2]
+    e1, e2 = v1 - v0, v2 - v0
+    p = np.cross(d, e2)
+    s = o - v0
+    q = np.cross(s, e1)
+    det = np.einsum("ij,ij->i", p, e1)
+    u = np.einsum("ij,ij->i", p, s) / det
+    v = np.einsum("ij,ij->i", q, d) / det
+    n = np.cross(e1, e2)
+    D = np.einsum("ij,ij->i", d, n)
+    de2, de1 = np.cross(d, e2), np.cross(d, e1)
+    lam = (gt[:, None] * n + gu[:, None] * de2 - gv[:, None] * de1) / D[:, None]
+    ad = np.abs(det)
+    pe = (np.abs(p) * np.abs(e1)).sum(1)
+    du = EPS32 * ((np.abs(p) * np.abs(s)).sum(1) + (np.abs(p) * (np.abs(o) + np.abs(v0))).sum(1) + np.abs(u) * pe) / ad
+    s_mag = np.abs(s) + np.abs(o) + np.abs(v0)
+    dv = EPS32 * ((np.abs(np.cross(s_mag, np.abs(e1))) * np.abs(d)).sum(1) + (np.abs(q) * np.abs(d)).sum(1) +
+                  np.abs(v) * pe) / ad
+    dlam = EPS32 * (np.abs(gt)[:, None] * np.abs(n) + np.abs(gu)[:, None] * np.abs(de2) +
+                    np.abs(gv)[:, None] * np.abs(de1)) / np.abs(D)[:, None] + \
+        EPS32 * np.abs(lam) * ((np.abs(d) * np.abs(n)).sum(1) / np.abs(D))[:, None]
+    w0 = 1 - u - v
+    B = np.zeros_like(V)
+    A = np.zeros_like(V)
+    K = np.zeros(V.shape[0])
+    for ii, wk, dwk in ((i0, w0, du + dv), (i1, u, du), (i2, v, dv)):
+        np.add.at(B, ii, np.abs(wk)[:, None] * dlam + dwk[:, None] * np.abs(lam))
+        np.add.at(A, ii, np.abs(wk[:, None] * lam))
+        np.add.at(K, ii, 1.0)
+    return C_TERM * B + K[:, None] * EPS32 * A
+
+
+def grad64(V, idx, hit, o, d, gt, gu, gv):
+    """FP64 brute-force reference gradient: closed form over every ray."""
     m = hit >= 0
     h, o, d, gt, gu, gv = hit[m], o[m], d[m], gt[m], gu[m], gv[m]
     i0, i1, i2 = idx[3 * h], idx[3 * h + 1], idx[3 * h + 2]
@@ -60,10 +111,9 @@ def grad64(V, idx, hit, o, d, gt, gu, gv, magnitudes=False):
     lam = (gt[:, None] * n + gu[:, None] * np.cross(d, e2) - gv[:, None] * np.cross(d, e1)) / \
         np.einsum("ij,ij->i", d, n)[:, None]
     G = np.zeros_like(V)
-    f = np.abs if magnitudes else (lambda x: x)
-    np.add.at(G, i0, f((1 - u - v)[:, None] * lam))
-    np.add.at(G, i1, f(u[:, None] * lam))
-    np.add.at(G, i2, f(v[:, None] * lam))
+    np.add.at(G, i0, (1 - u - v)[:, None] * lam)
+    np.add.at(G, i1, u[:, None] * lam)
+    np.add.at(G, i2, v[:, None] * lam)
     return G
 
 
@@ -97,15 +147,20 @@ def _fp64_args(c5):
 def test_against_fp64_reference_gradient(c5):
     V = c5["verts"].astype(np.float64)
     G = grad64(V, *_fp64_args(c5))
-    A = grad64(V, *_fp64_args(c5), magnitudes=True)
+    floor = rounding_floor(V, *_fp64_args(c5))
     g = c5["g"].astype(np.float64)
     rel = np.linalg.norm(g - G) / np.linalg.norm(G)
     assert rel < REL, rel
     # Component by component, over all 151,209 components.
     err = np.abs(g - G)
-    bound = REL * np.abs(G) + FLOOR * A
+    bound = REL * np.abs(G) + floor
     bad = err > bound
-    assert not bad.any(), (int(bad.sum()), float((err / np.maximum(bound, 1e-300)).max()))
+    assert not bad.any(), (int(bad.sum()), float((err[bad] / bound[bad]).max()))
+    # The contract's 1e-4 alone holds for most components (an fp32
+    # restatement of the kernel meets it on 92% of the touched ones; the
+    # median relative error is 1e-5).
+    touched = np.abs(G) > 0
+    assert (err <= REL * np.abs(G))[touched].mean() > 0.85
     touched = np.abs(G).sum(1) > 0
     assert (np.abs(g[~touched]) == 0).all()
 
@@ -120,7 +175,7 @@ def test_against_fp64_central_differences(c5):
     sel_v = cand[(scenes.uniform(6, 256, 0) * len(cand)).astype(np.int64)]
     h = 1e-4
     tri_vid = idx.reshape(-1, 3)
-    A = grad64(V, *_fp64_args(c5), magnitudes=True)
+    floor = rounding_floor(V, *_fp64_args(c5))
     num, ana, mag = [], [], []
     for j in sel_v:
         rays = np.nonzero(np.isin(hit, np.nonzero((tri_vid == j).any(1))[0]))[0]
@@ -133,13 +188,13 @@ def test_against_fp64_central_differences(c5):
                 L[k] = np.sum(w[rays] * tt + a[rays] * (uu + vv))
             num.append((8 * (L[1] - L[-1]) - (L[2] - L[-2])) / (12 * h))
             ana.append(g[j, c])
-            mag.append(A[j, c])
+            mag.append(floor[j, c])
     num, ana, mag = np.array(num), np.array(ana), np.array(mag)
     rel = np.linalg.norm(ana - num) / np.linalg.norm(num)
     assert rel < REL, rel
     # Each of the 768 sampled components on its own.
     err = np.abs(ana - num)
-    bound = REL * np.abs(num) + FLOOR * mag
+    bound = REL * np.abs(num) + mag
     assert (err <= bound).all(), (int((err > bound).sum()), float((err / bound).max()))
 
 

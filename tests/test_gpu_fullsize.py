@@ -89,7 +89,9 @@ def test_photons_full_scene_match_oracle(kdgb_lib, cuda, oracle, tracer):
     assert np.array_equal(h, ref_h), f"{(h != ref_h).sum()} segment ids differ"
     m = ref_h >= 0
     assert np.array_equal(t[m].view(np.uint32), ref_t[m].view(np.uint32))
-    assert all((ref_h[:, k] >= 0).sum() > 1000 for k in range(configs.PHOTON_BOUNCES + 1))
+    # Photons leave the light above the scene in all directions: about half
+    # head up and miss; every bounce level still has hits.
+    assert all((ref_h[:, k] >= 0).sum() > 100 for k in range(configs.PHOTON_BOUNCES + 1))
 
 
 def test_batched_64_meshes_match_oracle(kdgb_lib, cuda, oracle):
