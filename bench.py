@@ -711,6 +711,15 @@ def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
     kdgb.check(graph.status(), "graph rebuild")
     hits = int((graph.out[0] >= 0).sum().item())
     ghit = graph.out[0].cpu().numpy()
+    # The forest's trace alone under both schedules (the autotuner picked
+    # one): one thread per ray, or the persistent queue.
+    sched_ms = {}
+    for name, sch in (("grid", kdgb.SCHEDULE_GRID), ("queue", kdgb.SCHEDULE_QUEUE)):
+        tps = kdgb.TraceParams.from_buffer_copy(tp)
+        tps.schedule = sch
+        fn = lambda tps=tps: forest.trace_batch(od, dd, rays_per_mesh=R, params=tps)
+        time_steps(fn, 2, stream)
+        sched_ms[name] = statistics.median(time_steps(fn, steps, stream))
 
     views = [td[off[m]:off[m + 1]] for m in range(M)]
     oviews = [(od[m * R:(m + 1) * R], dd[m * R:(m + 1) * R]) for m in range(M)]
@@ -763,8 +772,11 @@ def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
            "parity": {"graph_loop_hits_identical": bool(same_graph_loop),
                       "host_loop_hits_identical": bool(same_host_loop),
                       "oracle_meshes_checked": int(check_meshes), "oracle_hit_ids_equal": bool(oracle_ok)},
+           "trace_only_ms": sched_ms,
            "autotune": {"leaf_size": bp.leaf_size, "sah_bins": bp.sah_bins, "stack_depth": tp.stack_depth,
-                        "block_size": tp.block_size, "objective_ms": tuned.objective, "baseline_ms": tuned.baseline,
+                        "block_size": tp.block_size,
+                        "schedule": "queue" if tp.schedule == kdgb.SCHEDULE_QUEUE else "grid",
+                        "objective_ms": tuned.objective, "baseline_ms": tuned.baseline,
                         "trials": tuned.trials, "seconds": tune_s, "scored_on": "graph rebuild + trace"}}
     graph.close()
     forest.close()

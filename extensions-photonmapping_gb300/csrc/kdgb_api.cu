@@ -108,11 +108,12 @@ template int ensure<BuildState>(DevArray<BuildState> &, int64_t, cudaStream_t, i
 
 static void release_all(Tree &t, cudaStream_t s)
 {
-    release(t.p0, s); release(t.p1, s); release(t.p2, s);
+    release(t.p0, s); release(t.p1, s); release(t.p2, s); release(t.prec, s);
     release(t.info, s); release(t.split, s); release(t.bmin, s); release(t.bmax, s);
     release(t.pidx, s); release(t.bitmap, s); release(t.parent, s); release(t.children, s);
     release(t.area, s); release(t.prim_indices, s); release(t.leaf_ids, s);
-    release(t.tnode, s); release(t.tbmin, s); release(t.tbmax, s); release(t.ttri, s); release(t.mesh_off, s); release(t.woop, s);
+    release(t.tnode, s); release(t.tbox, s); release(t.ttri, s); release(t.mesh_off, s); release(t.woop, s);
+    release(t.mesh_order, s); release(t.qctr, s);
     t.woop_valid = false;
     Workspace &w = t.ws;
     for (int b = 0; b < 2; ++b) {
@@ -191,8 +192,25 @@ static int validate_trace_params(const kdgb_trace_params &p, int64_t n)
     if (p.tile_width < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "tile_width must be >= 0");
     if (p.intersection != KDGB_ISECT_MOELLER && p.intersection != KDGB_ISECT_WOOP)
         return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown intersection algorithm");
+    if (p.schedule != KDGB_SCHEDULE_GRID && p.schedule != KDGB_SCHEDULE_QUEUE)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "unknown schedule");
     if (p.tile_width > 0 && (p.tile_width % 4 != 0 || n % ((int64_t)p.tile_width * 8) != 0))
         return fail(KDGB_ERR_INVALID_ARGUMENT, "tile_width needs width % 4 == 0 and height % 8 == 0");
+    return KDGB_OK;
+}
+
+// The batch's meshes ordered by triangle count, largest first (ties by
+// mesh index), for queue-scheduled traces.
+static int set_mesh_order(Tree &t, const int32_t *mesh_off_host, int32_t n_meshes, cudaStream_t s)
+{
+    std::vector<int32_t> order(n_meshes);
+    for (int32_t m = 0; m < n_meshes; ++m) order[m] = m;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        return mesh_off_host[x + 1] - mesh_off_host[x] > mesh_off_host[y + 1] - mesh_off_host[y];
+    });
+    KDGB_CHECK(ensure(t.mesh_order, n_meshes, s));
+    KDGB_CUDA(cudaMemcpyAsync(t.mesh_order.p, order.data(), sizeof(int32_t) * n_meshes, cudaMemcpyHostToDevice, s));
+    KDGB_CUDA(cudaStreamSynchronize(s));  // the host vector goes out of scope
     return KDGB_OK;
 }
 
@@ -212,6 +230,7 @@ static int do_build(Tree &t, const float *tri_v_dev, int32_t n_tris, const kdgb_
                                                   cudaMemcpyHostToDevice, s);
             if (e != cudaSuccess) rc = cuda_fail(e, "mesh offsets");
         }
+        if (rc == KDGB_OK) rc = set_mesh_order(t, mesh_off_host, n_meshes, s);
     }
     if (rc == KDGB_OK) rc = build_tree(t, tri_v_dev, n_tris, p, s, n_meshes > 1 ? t.mesh_off.p : nullptr, t.n_meshes);
     cudaEventRecord(e1, s);
@@ -298,6 +317,7 @@ void kdgb_trace_params_default(kdgb_trace_params *p)
     p->max_iterations = 0;
     p->block_size = 0;
     p->tile_width = 0;
+    p->schedule = KDGB_SCHEDULE_GRID;
     p->intersection = KDGB_ISECT_MOELLER;
 }
 
@@ -837,8 +857,12 @@ int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris, c
         KDGB_CHECK(ensure(t.mesh_off, (int64_t)n_meshes + 1, s));
         KDGB_CUDA(cudaMemcpyAsync(t.mesh_off.p, mesh_offsets, sizeof(int32_t) * (n_meshes + 1),
                                   cudaMemcpyHostToDevice, s));
+        KDGB_CHECK(set_mesh_order(t, mesh_offsets, n_meshes, s));
     }
     KDGB_CHECK(reserve_for_graph(t, n_tris, p, n_meshes, headroom, s));
+    // The queue schedule's counters live in the tree, allocated (zeroed)
+    // before capture.
+    if (n_rays > 0 && tp.schedule == KDGB_SCHEDULE_QUEUE && !t.qctr.p) KDGB_CHECK(ensure(t.qctr, 2, s, 0, true));
     if (n_rays > 0 && tp.intersection == KDGB_ISECT_WOOP) {
         // The graph recomputes the Woop rows from the rebuilt geometry.
         KDGB_CHECK(ensure(t.woop, 3 * (int64_t)std::max(n_tris, 1), s));

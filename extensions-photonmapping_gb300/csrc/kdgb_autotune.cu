@@ -3,7 +3,8 @@
 // a workload by timing real rebuilds and traces on the caller's stream.
 //
 // Search: coordinate descent from the caller's parameters, one parameter at
-// a time in the order leaf_size, sah_bins, stack_depth, block_size; each
+// a time in the order leaf_size, sah_bins, stack_depth, block_size,
+// schedule; each
 // candidate is scored by builds_per_trace * rebuild_ms + trace_ms, the median
 // of `reps` timed repetitions after one warm-up.  rebuild_ms is the time of a
 // graph rebuild (kdgb_graph_launch: the whole level loop on the device), the
@@ -220,6 +221,13 @@ int kdgb_autotune(const float *tri_v_dev, int32_t n_tris, const int32_t *mesh_of
             if (bs == (best_t.block_size > 0 ? best_t.block_size : 128)) continue;
             kdgb_trace_params c = best_t;
             c.block_size = bs;
+            try_trace(c);
+        }
+        // The schedule: one thread per ray, or the persistent queue that
+        // hands out the largest meshes' rays first.
+        {
+            kdgb_trace_params c = best_t;
+            c.schedule = best_t.schedule == KDGB_SCHEDULE_QUEUE ? KDGB_SCHEDULE_GRID : KDGB_SCHEDULE_QUEUE;
             try_trace(c);
         }
     }

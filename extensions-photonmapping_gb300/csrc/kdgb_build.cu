@@ -106,6 +106,7 @@ struct BuildArgs {
     float thr, ct, ci;
     const int32_t *mesh_off;
     float4 *p0, *p1, *p2;
+    float4 *prec;  // packed triangle records (Tree::prec)
     float4 *rmin[2], *rmax[2], *fmin, *fmax;
     int8_t *info;
     float *split;
@@ -130,7 +131,7 @@ struct BuildArgs {
     int2 *csets;
     int32_t *loff;  // PackLanes scan: 2 ints per node and the totals
     int2 *tnode;
-    float4 *tbmin, *tbmax;
+    float4 *tbox;
     int32_t *norder;  // each node's index in the traversal order
     float4 *ttri;
     cudaGraphConditionalHandle upper_cond, lower_cond;
@@ -178,9 +179,9 @@ __device__ __forceinline__ int mesh_of(const int32_t *__restrict__ off, int M, i
 }
 
 __global__ void k_load_geometry(const float *__restrict__ tri, int32_t T, float4 *__restrict__ p0,
-                                float4 *__restrict__ p1, float4 *__restrict__ p2,
+                                float4 *__restrict__ p1, float4 *__restrict__ p2, float4 *__restrict__ prec,
                                 float4 *__restrict__ cmin, float4 *__restrict__ cmax,
-                                int *__restrict__ err, const int32_t *__restrict__ mesh_off = nullptr, int M = 1)
+                                int *__restrict__ err, const int32_t *__restrict__ mesh_off, int M)
 {
     GRID_STRIDE(ii, T) {
         const int32_t i = (int32_t)ii;
@@ -195,6 +196,14 @@ __global__ void k_load_geometry(const float *__restrict__ tri, int32_t T, float4
         p0[i] = make_float4(v[0], v[1], v[2], 1.0f);
         p1[i] = make_float4(v[3], v[4], v[5], 1.0f);
         p2[i] = make_float4(v[6], v[7], v[8], 1.0f);
+        {
+            const float3 v0 = make_float3(v[0], v[1], v[2]);
+            const float3 e1 = sub3(make_float3(v[3], v[4], v[5]), v0);
+            const float3 e2 = sub3(make_float3(v[6], v[7], v[8]), v0);
+            prec[3 * (int64_t)i + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
+            prec[3 * (int64_t)i + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
+            prec[3 * (int64_t)i + 2] = make_float4(e2.z, __int_as_float(i), 0.0f, 0.0f);
+        }
         if (cmin) {
             float mnx = kmin(v[0], v[3]), mny = kmin(v[1], v[4]), mnz = kmin(v[2], v[5]);
             float mxx = kmax(v[0], v[3]), mxy = kmax(v[1], v[4]), mxz = kmax(v[2], v[5]);
@@ -1361,9 +1370,10 @@ __global__ void k_areas(const BuildArgs a)
     if (st->err) return;
     GRID_STRIDE(i, st->F) {
         const int32_t prim = a.prim_indices[i];
-        const float4 p = a.p0[prim], q = a.p1[prim], r = a.p2[prim];
-        const float3 v0 = make_float3(p.x, p.y, p.z), v1 = make_float3(q.x, q.y, q.z), v2 = make_float3(r.x, r.y, r.z);
-        const float3 cr = cross3(sub3(v1, v0), sub3(v2, v0));
+        const float4 q = __ldg(a.prec + 3 * (int64_t)prim), r = __ldg(a.prec + 3 * (int64_t)prim + 1),
+                     w = __ldg(a.prec + 3 * (int64_t)prim + 2);
+        // e1 = v1 - v0 and e2 = v2 - v0 as k_load_geometry rounded them.
+        const float3 cr = cross3(make_float3(q.w, r.x, r.y), make_float3(r.z, r.w, w.x));
         a.areas[i] = __fmul_rn(0.5f, __fsqrt_rn(dot3(cr, cr)));
     }
 }
@@ -1727,7 +1737,7 @@ __global__ void k_sah_children(const BuildArgs a)
 // interior nodes in node order) at M + 2r (left) and M + 2r + 1 (right).
 //   tnode[j]  int2  interior: {split bits, (left << 2) | axis}
 //                   leaf:     {first record, (record count << 2) | 0}
-//   tbmin/tbmax[j]  the leaf's box (leaf skipping)
+//   tbox[2j], tbox[2j+1]  min and max of the leaf's box (leaf skipping), one sector
 //   ttri[3r..3r+2]  float4 x3 per leaf record, in leaf order (LSB first):
 //                   {v0.xyz, e1.x} {e1.yz, e2.xy} {e2.z, id bits, 0, 0}
 // One 8-byte load per traversal step, siblings in one sector, and three
@@ -1766,7 +1776,7 @@ __global__ void k_pack_nodes(int32_t n_host, const int32_t *n_dev, const int32_t
                              const int8_t *__restrict__ info, const float *__restrict__ split,
                              const float4 *__restrict__ bmin, const float4 *__restrict__ bmax,
                              const int32_t *__restrict__ off, const int32_t *__restrict__ norder,
-                             int2 *__restrict__ tnode, float4 *__restrict__ tbmin, float4 *__restrict__ tbmax)
+                             int2 *__restrict__ tnode, float4 *__restrict__ tbox)
 {
     const int32_t n = n_dev ? *n_dev : n_host;
     if (!pack_ok(n, err, off, cap_tris)) return;
@@ -1777,8 +1787,8 @@ __global__ void k_pack_nodes(int32_t n_host, const int32_t *n_dev, const int32_t
         if (ax == KDGB_LEAF) {
             const int32_t first = off[2 * i];
             tnode[j] = make_int2(first, (off[2 * i + 2] - first) << 2);
-            tbmin[j] = bmin[i];
-            tbmax[j] = bmax[i];
+            tbox[2 * (int64_t)j] = bmin[i];
+            tbox[2 * (int64_t)j + 1] = bmax[i];
         } else {
             tnode[j] = make_int2(__float_as_int(split[i]), ((M + 2 * off[2 * i + 1]) << 2) | ax);
         }
@@ -1793,8 +1803,7 @@ __global__ void k_pack_nodes(int32_t n_host, const int32_t *n_dev, const int32_t
 __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t *err, int64_t cap_tris,
                             const int8_t *__restrict__ info, const int32_t *__restrict__ bitmap,
                             const int32_t *__restrict__ pidx, const int32_t *__restrict__ prim_indices,
-                            const float4 *__restrict__ p0, const float4 *__restrict__ p1,
-                            const float4 *__restrict__ p2, const int32_t *__restrict__ off,
+                            const float4 *__restrict__ prec, const int32_t *__restrict__ off,
                             float4 *__restrict__ ttri)
 {
     const int32_t n = n_dev ? *n_dev : n_host;
@@ -1829,14 +1838,12 @@ __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t 
             if (r < total) {
                 for (int k = r - ej; k > 0; --k) m &= m - 1u;
                 const int32_t prim = prim_indices[fj + __ffs(m) - 1];
-                const float4 pa = p0[prim], pb = p1[prim], pc = p2[prim];
-                const float3 v0 = make_float3(pa.x, pa.y, pa.z);
-                const float3 e1 = sub3(make_float3(pb.x, pb.y, pb.z), v0);
-                const float3 e2 = sub3(make_float3(pc.x, pc.y, pc.z), v0);
+                const float4 *src = prec + 3 * (int64_t)prim;
+                const float4 qa = __ldg(src), qb = __ldg(src + 1), qc = __ldg(src + 2);
                 const int64_t rec = rec0 + r;
-                ttri[3 * rec + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
-                ttri[3 * rec + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
-                ttri[3 * rec + 2] = make_float4(e2.z, __int_as_float(prim), 0.0f, 0.0f);
+                ttri[3 * rec + 0] = qa;
+                ttri[3 * rec + 1] = qb;
+                ttri[3 * rec + 2] = qc;
             }
         }
     }
@@ -1941,6 +1948,7 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.thr = p.empty_space_threshold;
     a.ct = p.traversal_cost;
     a.ci = p.intersection_cost;
+    a.prec = t.prec.p;
     a.p0 = t.p0.p;
     a.p1 = t.p1.p;
     a.p2 = t.p2.p;
@@ -1994,8 +2002,7 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.norder = w.misc0.p;
     a.loff = w.misc1.p;
     a.tnode = t.tnode.p;
-    a.tbmin = t.tbmin.p;
-    a.tbmax = t.tbmax.p;
+    a.tbox = t.tbox.p;
     a.ttri = t.ttri.p;
     a.cap.tris = t.ttri.cap / 3;
     return a;
@@ -2004,19 +2011,15 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
 // Launch sequences shared by the host-driven and the graph build.
 int emit_begin(const BuildArgs &a, const Launcher &L, const float *tri_v_dev, cudaStream_t s)
 {
-    k_begin<<<L.grid(a.M, kBlock), kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
+    KDGB_KERNEL(k_begin, L.grid(a.M, kBlock), kBlock, 0, s, a);
     if (a.T > 0) {
-        k_load_geometry<<<L.grid(a.T, kBlock), kBlock, 0, s>>>(tri_v_dev, a.T, a.p0, a.p1, a.p2, a.rmin[0],
+        KDGB_KERNEL(k_load_geometry, L.grid(a.T, kBlock), kBlock, 0, s, tri_v_dev, a.T, a.p0, a.p1, a.p2, a.prec, a.rmin[0],
                                                                a.rmax[0], &a.st->nonfinite, a.mesh_off, a.M);
-        KDGB_LAUNCH_CHECK();
         // The roots' tight boxes; later levels get theirs from k_scatter.
-        k_reduce<<<L.grid(a.T, kTileRefs), kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
+        KDGB_KERNEL(k_reduce, L.grid(a.T, kTileRefs), kBlock, 0, s, a);
     }
     // The roots' splits; later levels get theirs from k_children.
-    k_node_split<<<L.grid(a.M, kBlock), kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
+    KDGB_KERNEL(k_node_split, L.grid(a.M, kBlock), kBlock, 0, s, a);
     return KDGB_OK;
 }
 
@@ -2027,13 +2030,11 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
     if (tuned_levels) {
         // Enough blocks for one per large node and one warp per node.
         const int64_t big = ceil_div(e.N, kSahBlockRefs);  // at least the large nodes
-        k_sah_bin<<<L.grid(std::max<int64_t>(big * kBlock, e.R * 32), kBlock), kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
+        KDGB_KERNEL(k_sah_bin, L.grid(std::max<int64_t>(big * kBlock, e.R * 32), kBlock), kBlock, 0, s, a);
     }
     if (e.N > 0) {
-        if (a.divide) k_count<true><<<gN, kBlock, 0, s>>>(a);
-        else k_count<false><<<gN, kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
+        if (a.divide) KDGB_KERNEL(k_count<true>, gN, kBlock, 0, s, a);
+        else KDGB_KERNEL(k_count<false>, gN, kBlock, 0, s, a);
     }
     // Tile offsets and node bases: independent scans, one launch.
     const NodeLanes lanes{a.cnt, {a.ess_cnt[0], a.ess_cnt[1]}, &a.st->level, a.LS};
@@ -2041,54 +2042,42 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
         ScanArray<2>{a.tilesum}, a.tileoff, ceil_div(e.N, kTileRefs), &a.st->ntiles, lanes, a.lbase, e.R, &a.st->R, s,
         &w.scan, &a.st->err)));
     if (e.N > 0) {
-        if (a.divide) k_scatter<true><<<gN, kBlock, 0, s>>>(a);
-        else k_scatter<false><<<gN, kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
+        if (a.divide) KDGB_KERNEL(k_scatter<true>, gN, kBlock, 0, s, a);
+        else KDGB_KERNEL(k_scatter<false>, gN, kBlock, 0, s, a);
     }
-    k_children<<<L.grid(2 * e.R, kBlock, 2), kBlock, 0, s>>>(a);  // a thread per child
-    KDGB_LAUNCH_CHECK();
+    KDGB_KERNEL(k_children, L.grid(2 * e.R, kBlock, 2), kBlock, 0, s, a);  // a thread per child
     return KDGB_OK;
 }
 
 int emit_after_upper(const BuildArgs &a, const Launcher &L, const Extents &e, const kdgb_build_params &p,
                      cudaStream_t s)
 {
-    k_leaf_ids<<<L.grid(e.leaves, kBlock), kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
-    k_extract_indices<<<L.grid(e.F, kBlock), kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
+    KDGB_KERNEL(k_leaf_ids, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
+    KDGB_KERNEL(k_extract_indices, L.grid(e.F, kBlock), kBlock, 0, s, a);
     if (!p.split_empty_space && p.propagate_aabbs) {
-        k_propagate_parent<<<L.grid(e.leaves, kBlock), kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
+        KDGB_KERNEL(k_propagate_parent, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
     }
     if (p.lower == KDGB_LOWER_SAH) {
-        k_areas<<<L.grid(e.F, kBlock), kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
-        k_sah_preprocess<<<L.grid(e.leaves, kBlock), kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
+        KDGB_KERNEL(k_areas, L.grid(e.F, kBlock), kBlock, 0, s, a);
+        KDGB_KERNEL(k_sah_preprocess, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
     } else {
         // Every reference of an upper leaf (PreprocessLeafNodes,
         // LowerTriangleMap.h:40-53 and TriangleMapBitmapCreator.cu:32-49).
-        k_bitmap_leaves<<<L.grid(e.leaves, kBlock), kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
+        KDGB_KERNEL(k_bitmap_leaves, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
     }
     if (lower_loop(p)) {
-        k_sah_planes<<<L.grid(e.leaves * 32, kBlock), kBlock, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
-        k_lower_begin<<<1, 1, 0, s>>>(a);
-        KDGB_LAUNCH_CHECK();
+        KDGB_KERNEL(k_sah_planes, L.grid(e.leaves * 32, kBlock), kBlock, 0, s, a);
+        KDGB_KERNEL(k_lower_begin, 1, 1, 0, s, a);
     }
     return KDGB_OK;
 }
 
 int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, Workspace &w, cudaStream_t s)
 {
-    if (a.lower == KDGB_LOWER_BALANCED) k_calc_balanced<<<L.grid(e.low_R * 32, kBlock), kBlock, 0, s>>>(a);
-    else k_calc_sah<<<L.grid(e.low_R * 32, kBlock), kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
+    if (a.lower == KDGB_LOWER_BALANCED) KDGB_KERNEL(k_calc_balanced, L.grid(e.low_R * 32, kBlock), kBlock, 0, s, a);
+    else KDGB_KERNEL(k_calc_sah, L.grid(e.low_R * 32, kBlock), kBlock, 0, s, a);
     KDGB_CHECK(scan_exclusive<1>(a.ssplit, a.saddr, e.low_R, s, &w.scan, &a.st->low_R, &a.st->err));
-    k_sah_children<<<L.grid(e.low_R, kBlock, 2), kBlock, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
+    KDGB_KERNEL(k_sah_children, L.grid(e.low_R, kBlock, 2), kBlock, 0, s, a);
     return KDGB_OK;
 }
 
@@ -2097,8 +2086,7 @@ int emit_pack_counts(const BuildArgs &a, const Launcher &L, const Extents &e, Wo
 {
     KDGB_CHECK((scan_exclusive_in<2, PackLanes>(PackLanes{a.info, a.amt}, a.loff, e.nodes, s, &w.scan,
                                                 &a.st->n_nodes, &a.st->err)));
-    k_pack_finish<<<1, 1, 0, s>>>(a);
-    KDGB_LAUNCH_CHECK();
+    KDGB_KERNEL(k_pack_finish, 1, 1, 0, s, a);
     return KDGB_OK;
 }
 
@@ -2106,15 +2094,12 @@ int emit_pack(const BuildArgs &a, const Launcher &L, const Extents &e, cudaStrea
 {
     const unsigned g = L.grid(e.nodes, kBlock);
     KDGB_CUDA(cudaMemsetAsync(a.norder, 0xff, sizeof(int32_t) * (size_t)std::max<int64_t>(e.nodes, 1), s));
-    k_pack_order<<<g, kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.M, a.info, a.ch, a.loff, a.norder);
-    KDGB_LAUNCH_CHECK();
-    k_pack_nodes<<<g, kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.M, a.info, a.split, a.bmin, a.bmax,
-                                      a.loff, a.norder, a.tnode, a.tbmin, a.tbmax);
-    KDGB_LAUNCH_CHECK();
-    k_pack_tris<<<L.grid(e.nodes, kBlock), kBlock, 0, s>>>(0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info,
+    KDGB_KERNEL(k_pack_order, g, kBlock, 0, s, 0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.M, a.info, a.ch, a.loff, a.norder);
+    KDGB_KERNEL(k_pack_nodes, g, kBlock, 0, s, 0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.M, a.info, a.split, a.bmin, a.bmax,
+                                      a.loff, a.norder, a.tnode, a.tbox);
+    KDGB_KERNEL(k_pack_tris, L.grid(e.nodes, kBlock), kBlock, 0, s, 0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info,
                                                                  a.amt, a.pidx,
-                                     a.prim_indices, a.p0, a.p1, a.p2, a.loff, a.ttri);
-    KDGB_LAUNCH_CHECK();
+                                     a.prim_indices, a.prec, a.loff, a.ttri);
     return KDGB_OK;
 }
 
@@ -2163,6 +2148,7 @@ int geometry_arrays(Tree &t, int32_t T, cudaStream_t s)
     KDGB_CHECK(ensure(t.p0, T, s));
     KDGB_CHECK(ensure(t.p1, T, s));
     KDGB_CHECK(ensure(t.p2, T, s));
+    KDGB_CHECK(ensure(t.prec, 3 * (int64_t)T, s));
     t.n_tris = T;
     return KDGB_OK;
 }
@@ -2184,7 +2170,7 @@ void graph_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, const
     a.cap.leaves = t.leaf_ids.cap;
     a.cap.low_R = std::min({w.ssplit.cap, w.saddr.cap - 1, w.careas.cap, w.csets.cap});
     a.cap.fin = std::min({a.cap.fin, t.prim_indices.cap, w.areas.cap, w.sts.cap / 3});
-    a.cap.nodes = std::min({a.cap.nodes, w.misc0.cap, w.misc1.cap / 2 - 1, t.tnode.cap, t.tbmin.cap, t.tbmax.cap,
+    a.cap.nodes = std::min({a.cap.nodes, w.misc0.cap, w.misc1.cap / 2 - 1, t.tnode.cap, t.tbox.cap / kBoxStride,
                             kMaxPackNodes - 1});
     a.use_cond = 1;
     e.N = std::min(a.cap.refs[0], a.cap.refs[1]);
@@ -2206,9 +2192,9 @@ uint64_t layout_signature(const Tree &t)
     };
 #define MIX(arr) mix((arr).p, (arr).cap)
     const Workspace &w = t.ws;
-    MIX(t.p0); MIX(t.p1); MIX(t.p2); MIX(t.info); MIX(t.split); MIX(t.bmin); MIX(t.bmax); MIX(t.pidx);
+    MIX(t.p0); MIX(t.p1); MIX(t.p2); MIX(t.prec); MIX(t.info); MIX(t.split); MIX(t.bmin); MIX(t.bmax); MIX(t.pidx);
     MIX(t.bitmap); MIX(t.parent); MIX(t.children); MIX(t.area); MIX(t.prim_indices); MIX(t.leaf_ids);
-    MIX(t.tnode); MIX(t.tbmin); MIX(t.tbmax); MIX(t.ttri); MIX(t.mesh_off);
+    MIX(t.tnode); MIX(t.tbox); MIX(t.ttri); MIX(t.mesh_off); MIX(t.mesh_order); MIX(t.qctr);
     MIX(w.rmin[0]); MIX(w.rmin[1]); MIX(w.rmax[0]); MIX(w.rmax[1]); MIX(w.fmin); MIX(w.fmax);
     MIX(w.keys); MIX(w.planes[0]); MIX(w.planes[1]); MIX(w.cnt); MIX(w.ess[0]); MIX(w.ess[1]); MIX(w.lbase);
     MIX(w.chunksum);
@@ -2236,9 +2222,8 @@ int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s)
     KDGB_CHECK(grab(w.stats, 16, s));
     KDGB_CUDA(cudaMemsetAsync(w.stats.p, 0, sizeof(int), s));
     const Launcher L{sm_count()};
-    k_load_geometry<<<L.grid(T, kBlock), kBlock, 0, s>>>(tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, nullptr, nullptr,
-                                                         w.stats.p);
-    KDGB_LAUNCH_CHECK();
+    KDGB_KERNEL(k_load_geometry, L.grid(T, kBlock), kBlock, 0, s, tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, t.prec.p, nullptr,
+             nullptr, w.stats.p, nullptr, 1);
     KDGB_CUDA(cudaMemcpyAsync(w.host, w.stats.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     KDGB_CUDA(cudaStreamSynchronize(s));
     if (w.host[0]) return fail(KDGB_ERR_NONFINITE, "non-finite vertex coordinate");
@@ -2261,23 +2246,19 @@ int pack_for_traversal(Tree &t, cudaStream_t s)
     KDGB_CUDA(cudaStreamSynchronize(s));
     const int32_t total = w.host[kHostRec - 1];
     KDGB_CHECK(ensure(t.tnode, n, s));
-    KDGB_CHECK(ensure(t.tbmin, n, s));
-    KDGB_CHECK(ensure(t.tbmax, n, s));
+    KDGB_CHECK(ensure(t.tbox, kBoxStride * (int64_t)n, s));
     KDGB_CHECK(ensure(t.ttri, 3 * (int64_t)total, s));
     t.n_leaf_tris = total;
     if (n > 0) {
         const unsigned g = L.grid(n, kBlock);
         KDGB_CUDA(cudaMemsetAsync(norder, 0xff, sizeof(int32_t) * (size_t)n, s));
-        k_pack_order<<<g, kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.n_meshes, t.info.p, t.children.p, off,
+        KDGB_KERNEL(k_pack_order, g, kBlock, 0, s, n, nullptr, nullptr, INT64_MAX, t.n_meshes, t.info.p, t.children.p, off,
                                           norder);
-        KDGB_LAUNCH_CHECK();
-        k_pack_nodes<<<g, kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.n_meshes, t.info.p, t.split.p, t.bmin.p,
-                                          t.bmax.p, off, norder, t.tnode.p, t.tbmin.p, t.tbmax.p);
-        KDGB_LAUNCH_CHECK();
-        k_pack_tris<<<L.grid(n, kBlock), kBlock, 0, s>>>(n, nullptr, nullptr, INT64_MAX, t.info.p,
+        KDGB_KERNEL(k_pack_nodes, g, kBlock, 0, s, n, nullptr, nullptr, INT64_MAX, t.n_meshes, t.info.p, t.split.p, t.bmin.p,
+                                          t.bmax.p, off, norder, t.tnode.p, t.tbox.p);
+        KDGB_KERNEL(k_pack_tris, L.grid(n, kBlock), kBlock, 0, s, n, nullptr, nullptr, INT64_MAX, t.info.p,
                                                                         t.bitmap.p, t.pidx.p, t.prim_indices.p,
-                                                                        t.p0.p, t.p1.p, t.p2.p, off, t.ttri.p);
-        KDGB_LAUNCH_CHECK();
+                                                                        t.prec.p, off, t.ttri.p);
     }
     return KDGB_OK;
 }
@@ -2409,8 +2390,7 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
         KDGB_CHECK(emit_pack_counts(a, L, e, w, s));
         KDGB_CHECK(fetch_state(t, st, s));
         KDGB_CHECK(ensure(t.tnode, n, s));
-        KDGB_CHECK(ensure(t.tbmin, n, s));
-        KDGB_CHECK(ensure(t.tbmax, n, s));
+        KDGB_CHECK(ensure(t.tbox, kBoxStride * (int64_t)n, s));
         KDGB_CHECK(ensure(t.ttri, 3 * (int64_t)st.n_leaf_tris, s));
         KDGB_CHECK(emit_pack(make_args(t, p, T, M, mesh_off_dev), L, e, s));
     }
@@ -2474,8 +2454,7 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.misc0, nodes, s));
     KDGB_CHECK(ensure(w.misc1, 2 * (nodes + 1), s));
     KDGB_CHECK(ensure(t.tnode, nodes, s));
-    KDGB_CHECK(ensure(t.tbmin, nodes, s));
-    KDGB_CHECK(ensure(t.tbmax, nodes, s));
+    KDGB_CHECK(ensure(t.tbox, kBoxStride * (int64_t)nodes, s));
     KDGB_CHECK(ensure(t.ttri, 3 * tris, s));
     // Scan partials for the extents the capture will use.
     BuildArgs a;

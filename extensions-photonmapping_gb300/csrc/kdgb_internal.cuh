@@ -38,6 +38,14 @@ void note_launch(int n = 1);
         KDGB_CUDA(cudaGetLastError());   \
     } while (0)
 
+// kernel<<<grid, block, smem, stream>>>(args...) followed by
+// KDGB_LAUNCH_CHECK(); the kernel may be a template-id in parentheses.
+#define KDGB_KERNEL(kernel, grid, block, smem, stream, ...)     \
+    do {                                                        \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__); \
+        KDGB_LAUNCH_CHECK();                                    \
+    } while (0)
+
 // ---------------------------------------------------------------------------
 // Device arrays owned by a tree handle.  `cap` counts elements.
 // ---------------------------------------------------------------------------
@@ -135,9 +143,16 @@ struct Tree {
     int32_t n_meshes = 1;        // forest roots (kdgb_build_batch)
     kdgb_build_stats stats{};
     DevArray<int32_t> mesh_off;  // n_meshes + 1 triangle offsets (batches only)
+    DevArray<int32_t> mesh_order;  // batch meshes by triangle count, largest first (queue traces)
+    DevArray<unsigned> qctr;       // queue trace state: next chunk, warps done (zero between launches)
 
     // Geometry (GeometryList SoA) and the packed triangle array used by builds.
     DevArray<float4> p0, p1, p2;
+    // The same triangles packed as the traversal layout's 48-byte records,
+    // {v0.xyz, e1.x} {e1.yz, e2.xy} {e2.z, id bits, 0, 0}, 3 float4 per
+    // triangle: the leaf records are copies of these (one contiguous
+    // gather), and the SAH areas read e1 and e2 from them.
+    DevArray<float4> prec;
 
     // TriangleNode SoA (KDNode.h:65-73, TriangleNode.h:20-21).
     DevArray<int8_t> info;
@@ -153,7 +168,7 @@ struct Tree {
     // leaf skipping), and leaf-ordered triangle records (v0, e1, e2, id) of
     // 48 bytes.
     DevArray<int2> tnode;
-    DevArray<float4> tbmin, tbmax;
+    DevArray<float4> tbox;  // leaf boxes: min, max of node j at [2j], [2j + 1]
     DevArray<float4> ttri;
 
     // Woop transform rows (m0, m1, m2) per triangle, computed on the first
@@ -350,6 +365,10 @@ __device__ __forceinline__ float axis_of4(float4 a, int axis)
 }
 
 // IRayTracer.h:60-65 AdjustRayDirection.
+// Leaf boxes of the traversal layout: min then max of node j at [2j] and
+// [2j + 1], so one box is one 32-byte sector.
+constexpr int kBoxStride = 2;
+
 __device__ __forceinline__ float3 adjust_dir(float3 d)
 {
     const float ooeps = 0x1p-80f;

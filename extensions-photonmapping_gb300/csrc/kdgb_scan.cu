@@ -330,8 +330,7 @@ int scan_exclusive_in(const In &in, int32_t *out, int64_t n, cudaStream_t s, Dev
         KDGB_CHECK(ensure(*ws, want, s, ws->p ? kCtl : 0, true));
     }
     const int64_t nb = std::max<int64_t>(1, (n + kTile - 1) / kTile);
-    scan_lookback_kernel<K, In><<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, n_dev, ws->p, err);
-    KDGB_LAUNCH_CHECK();
+    KDGB_KERNEL((scan_lookback_kernel<K, In>), (unsigned)nb, kThreads, 0, s, in, out, n, n_dev, ws->p, err);
     return KDGB_OK;
 }
 
@@ -350,9 +349,8 @@ int scan_exclusive_pair(const In1 &in1, int32_t *out1, int64_t n1, const int32_t
         const int64_t want = std::max<int64_t>(need, ws->cap + ws->cap / 2);
         KDGB_CHECK(ensure(*ws, want, s, ws->p ? kCtl : 0, true));
     }
-    scan_pair_kernel<K1, In1, K2, In2><<<(unsigned)(nb1 + nb2), kThreads, 0, s>>>(in1, out1, n1, n1_dev, nb1, in2,
+    KDGB_KERNEL((scan_pair_kernel<K1, In1, K2, In2>), (unsigned)(nb1 + nb2), kThreads, 0, s, in1, out1, n1, n1_dev, nb1, in2,
                                                                                  out2, n2, n2_dev, ws->p, err);
-    KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
 

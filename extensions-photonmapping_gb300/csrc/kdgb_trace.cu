@@ -16,7 +16,7 @@
 //                   leaf:     {first record, (record count << 2) | 0}
 //   ttri[3r..3r+2]  float4 x3 per leaf record, in leaf order:
 //                   {v0.xyz, e1.x} {e1.yz, e2.xy} {e2.z, id bits, 0, 0}
-//   bmin/bmax       float4 leaf boxes in the same order (leaf skipping)
+//   box[2j], box[2j+1]  float4 min and max of leaf j (leaf skipping), one sector
 // One 8-byte load per traversal step and three 16-byte loads per triangle
 // test, with no index indirection; e1 = v1 - v0 and e2 = v2 - v0 are the
 // same fp32 values the reference computes per test.
@@ -40,12 +40,15 @@ inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b
 
 struct Ctx {
     const int2 *__restrict__ node;
-    const float4 *__restrict__ bmin;
-    const float4 *__restrict__ bmax;
+    const float4 *__restrict__ box;  // leaf boxes, min and max of node j at [2j], [2j + 1]
     const float4 *__restrict__ tri;
     const float4 *__restrict__ woop;  // per-triangle Woop values, or NULL for Moeller-Trumbore
     int root;  // root node of the ray's tree (forest of a batch: its mesh index)
 };
+
+// The box of leaf `node` (leaf skipping).
+__device__ __forceinline__ float4 leaf_min(const Ctx &c, int node) { return __ldg(c.box + 2 * (int64_t)node); }
+__device__ __forceinline__ float4 leaf_max(const Ctx &c, int node) { return __ldg(c.box + 2 * (int64_t)node + 1); }
 
 // Fields of a tnode record.
 __device__ __forceinline__ int node_axis(int2 nd) { return nd.y & 3; }
@@ -310,7 +313,7 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
     do {
         restart_descend(c, o, inv, tmin, node, nd, tnext, m);
         tmin = __fmul_rn(tnext, 1.00001f);
-        if (!SKIP || ray_box(o, inv, __ldg(c.bmin + node), __ldg(c.bmax + node))) {
+        if (!SKIP || ray_box(o, inv, leaf_min(c, node), leaf_max(c, node))) {
             float tb = tmin, ub = 0.0f, vb = 0.0f;
             const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
             if (h != -1) { t = tb; u = ub; v = vb; return h; }
@@ -381,7 +384,7 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
         }
         d = fixed ? d1 : inv3(d);
         th = __fmul_rn(tnext, 1.00001f);
-        if (!SKIP || ray_box(o, fixed ? inv1 : inv3(d), __ldg(c.bmin + node), __ldg(c.bmax + node))) {
+        if (!SKIP || ray_box(o, fixed ? inv1 : inv3(d), leaf_min(c, node), leaf_max(c, node))) {
             float tb = th, ub = 0.0f, vb = 0.0f;
             const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
             if (h != -1) {
@@ -427,19 +430,20 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 
 }
 
 // PacketIndex (IRayTracer.h:67-76): 4x8 pixel packets per warp.
+constexpr int kPW = 4, kPH = 8;  // 4x8 pixels per warp (an 8x4 packet was 5% slower on the frame)
 __device__ __forceinline__ int64_t ray_index(int64_t id, int tile_width)
 {
     if (tile_width <= 0) return id;
     if (id < 0x7fffffff) {  // 32-bit arithmetic for image-sized launches
-        const int32_t i = (int32_t)id, cell = i >> 5, cols = tile_width >> 2;
+        const int32_t i = (int32_t)id, cell = i >> 5, cols = tile_width / kPW;
         const int32_t by = cell / cols, bx = cell - by * cols;
-        return (int64_t)(bx * 4 + (i & 3)) + (int64_t)(by * 8 + ((i & 31) >> 2)) * tile_width;
+        return (int64_t)(bx * kPW + (i & (kPW - 1))) + (int64_t)(by * kPH + ((i & 31) / kPW)) * tile_width;
     }
     const int64_t cell = id / 32;
-    const int64_t cols = tile_width / 4;
+    const int64_t cols = tile_width / kPW;
     const int64_t bx = cell % cols, by = cell / cols;
-    const int64_t x = id % 4, y = (id % 32) / 4;
-    return bx * 4 + x + (by * 8 + y) * tile_width;
+    const int64_t x = id % kPW, y = (id % 32) / kPW;
+    return bx * kPW + x + (by * kPH + y) * tile_width;
 }
 
 __device__ __forceinline__ float3 ld3(const float *__restrict__ p, int64_t i)
@@ -481,6 +485,36 @@ __device__ __forceinline__ int ray_mesh_of(const TraceArgs &a, int64_t i)
     return m < 0 ? 0 : (m >= a.n_meshes ? a.n_meshes - 1 : m);
 }
 
+// First hit of ray i with the tracer of TRACER (its tree: the ray's mesh for
+// a batch), written to the outputs; the thread's stack or memo region is
+// stk[k * stride].  Returns the hit id (relative to the whole tree) and the
+// ray and t for a shadow ray.
+template <int TRACER, bool SKIP>
+__device__ __forceinline__ int trace_ray(const TraceArgs &a, int64_t i, int2 *stk, int stride, float3 &o, float3 &d,
+                                         float &t)
+{
+    o = ld3(a.o, i);
+    d = ld3(a.d, i);
+    Ctx c = a.c;
+    int32_t id_off = 0;
+    if (a.mesh_off) {
+        c.root = ray_mesh_of(a, i);
+        id_off = a.mesh_off[c.root];
+    }
+    float u = 0.0f, v = 0.0f;
+    int h;
+    if (TRACER == KDGB_TRACER_SHORTSTACK)
+        h = trace_shortstack<SKIP>(c, o, d, a.tie, a.depth, a.maxit, stk, stride, t, u, v);
+    else
+        h = trace_restart<SKIP>(c, o, d, a.tie, a.maxit, t, u, v, nullptr, stk, stride);
+    if (h < 0) { t = INFINITY; u = 0.0f; v = 0.0f; }
+    a.hit[i] = h >= 0 ? h - id_off : h;
+    a.t[i] = t;
+    a.u[i] = u;
+    a.v[i] = v;
+    return h;
+}
+
 // Dynamic shared memory: the per-thread regions of stack_entries() int2
 // (short stack or remembered descents) followed, with shadow rays, by a
 // queue of blockDim ShadowItem.  Capped at 40 registers: the traversal is
@@ -507,28 +541,9 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
         return;
     }
     float3 o = make_float3(0.f, 0.f, 0.f), d = o;
-    Ctx c = a.c;
-    float t = 0.0f, u = 0.0f, v = 0.0f;
+    float t = 0.0f;
     int h = -1;
-    if (live) {
-        o = ld3(a.o, i);
-        d = ld3(a.d, i);
-        int32_t id_off = 0;
-        if (a.mesh_off) {
-            c.root = ray_mesh_of(a, i);
-            id_off = a.mesh_off[c.root];
-        }
-        if (TRACER == KDGB_TRACER_SHORTSTACK)
-            h = trace_shortstack<SKIP>(c, o, d, a.tie, a.depth, a.maxit, stack_smem + threadIdx.x, blockDim.x, t, u,
-                                       v);
-        else
-            h = trace_restart<SKIP>(c, o, d, a.tie, a.maxit, t, u, v, nullptr, stack_smem + threadIdx.x, blockDim.x);
-        if (h < 0) { t = INFINITY; u = 0.0f; v = 0.0f; }
-        a.hit[i] = h >= 0 ? h - id_off : h;
-        a.t[i] = t;
-        a.u[i] = u;
-        a.v[i] = v;
-    }
+    if (live) h = trace_ray<TRACER, SKIP>(a, i, stack_smem + threadIdx.x, blockDim.x, o, d, t);
     if (SHADOW) {
         // The block's shadow rays (one per primary hit) are packed onto its
         // first threads, so warps stay full while they are traced.
@@ -553,6 +568,71 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
             a.occ[ray] = trace_shadow(cs, a.light, make_float3(q.p.x, q.p.y, q.p.z), a.maxit,
                                         stack_smem + threadIdx.x, blockDim.x,
                                         memo_cap(stack_entries(TRACER, a.depth)));
+        }
+    }
+}
+
+// Queue schedule (KDGB_SCHEDULE_QUEUE): a persistent grid whose warps take
+// 32-ray chunks from a device-side counter until the rays run out.  With a
+// mesh order (a batch traced with rays_per_mesh), chunk c holds rays
+// [k * 32, k * 32 + 32) of mesh order[c / chunks_per_mesh], k = c %
+// chunks_per_mesh, so the rays of the largest meshes go first and the cheap
+// ones fill the tail; otherwise chunks follow the ray order (4x8 pixel
+// packets with a tile width).  No warp waits for another: the grid only has
+// to start.  The last warp to finish resets the counters for the next
+// launch.
+struct TraceQueue {
+    unsigned *ctr;          // [0] next chunk, [1] warps finished
+    const int32_t *order;   // meshes, largest first, or NULL
+    unsigned n_chunks;
+    int32_t chunks_per_mesh;
+    unsigned n_warps;
+};
+
+template <int TRACER, bool SKIP>
+__global__ void __maxnreg__(40) k_trace_queue(TraceArgs a, TraceQueue q)
+{
+    extern __shared__ __align__(16) unsigned char trace_smem[];
+    int2 *stk = (int2 *)trace_smem + threadIdx.x;
+    const unsigned lane = threadIdx.x & 31;
+    if (a.build_err && *a.build_err) {  // grid-uniform: every ray misses, the queue is not touched
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
+            a.hit[i] = -1;
+            a.t[i] = INFINITY;
+            a.u[i] = 0.0f;
+            a.v[i] = 0.0f;
+        }
+        return;
+    }
+    for (;;) {
+        unsigned chunk = 0;
+        if (lane == 0) chunk = atomicAdd(q.ctr, 1u);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        if (chunk >= q.n_chunks) break;
+        int64_t i;
+        bool live;
+        if (q.order) {
+            const int32_t m = q.order[chunk / (unsigned)q.chunks_per_mesh];
+            const int32_t k = (int32_t)(chunk % (unsigned)q.chunks_per_mesh) * 32 + (int32_t)lane;
+            i = (int64_t)m * a.rays_per_mesh + k;
+            live = k < a.rays_per_mesh && i < a.n;
+        } else {
+            const int64_t id = (int64_t)chunk * 32 + lane;
+            live = id < a.n;
+            i = live ? ray_index(id, a.tile_width) : 0;
+        }
+        if (live) {
+            float3 o, d;
+            float t = 0.0f;
+            trace_ray<TRACER, SKIP>(a, i, stk, blockDim.x, o, d, t);
+        }
+    }
+    if (lane == 0) {
+        __threadfence();
+        if (atomicAdd(q.ctr + 1, 1u) == q.n_warps - 1) {
+            q.ctr[0] = 0;
+            q.ctr[1] = 0;
+            __threadfence();
         }
     }
 }
@@ -932,14 +1012,49 @@ static int woop_for(const Tree &t, const kdgb_trace_params &p, cudaStream_t s, C
 }
 
 
+// The persistent queue-scheduled launch (k_trace_queue) for trace_launch.
+static int trace_queue_launch(const Tree &t, const kdgb_trace_params &p, const TraceArgs &a, int bs, size_t smem,
+                              cudaStream_t s)
+{
+    void (*kernel)(TraceArgs, TraceQueue);
+    const bool skip = p.leaf_skipping != 0;
+    if (p.tracer == KDGB_TRACER_SHORTSTACK)
+        kernel = skip ? k_trace_queue<KDGB_TRACER_SHORTSTACK, true> : k_trace_queue<KDGB_TRACER_SHORTSTACK, false>;
+    else
+        kernel = skip ? k_trace_queue<KDGB_TRACER_RESTART, true> : k_trace_queue<KDGB_TRACER_RESTART, false>;
+    if (smem > 48 * 1024) KDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    Tree &tm = const_cast<Tree &>(t);
+    if (!t.qctr.p) KDGB_CHECK(ensure(tm.qctr, 2, s, 0, true));
+    int per_sm = 0, dev = 0, sms = 0;
+    KDGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, bs, smem));
+    KDGB_CUDA(cudaGetDevice(&dev));
+    KDGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    TraceQueue q;
+    q.ctr = t.qctr.p;
+    q.order = nullptr;
+    q.chunks_per_mesh = 1;
+    int64_t chunks = (a.n + 31) / 32;
+    if (a.mesh_off && !a.ray_mesh && t.mesh_order.p) {
+        q.order = t.mesh_order.p;
+        q.chunks_per_mesh = (a.rays_per_mesh + 31) / 32;
+        chunks = (int64_t)q.chunks_per_mesh * a.n_meshes;
+    }
+    if (chunks >= (int64_t)0xffffffffll) return fail(KDGB_ERR_CAPACITY, "queue trace: too many ray chunks");
+    q.n_chunks = (unsigned)chunks;
+    const int64_t blocks = std::min<int64_t>((int64_t)std::max(per_sm, 1) * sms, std::max<int64_t>(1, (a.n + bs - 1) / bs));
+    q.n_warps = (unsigned)(blocks * (bs / 32));
+    kernel<<<(unsigned)blocks, bs, smem, s>>>(a, q);
+    KDGB_LAUNCH_CHECK();
+    return KDGB_OK;
+}
+
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
                  int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s,
                  const int32_t *ray_mesh, int32_t rays_per_mesh)
 {
     TraceArgs a;
     a.c.node = t.tnode.p;
-    a.c.bmin = t.tbmin.p;
-    a.c.bmax = t.tbmax.p;
+    a.c.box = t.tbox.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
     KDGB_CHECK(woop_for(t, p, s, a.c));
@@ -976,6 +1091,7 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
         kernel = skip ? (shadow ? k_trace<KDGB_TRACER_RESTART, true, true> : k_trace<KDGB_TRACER_RESTART, true, false>)
                       : (shadow ? k_trace<KDGB_TRACER_RESTART, false, true> : k_trace<KDGB_TRACER_RESTART, false, false>);
     }
+    if (p.schedule == KDGB_SCHEDULE_QUEUE && !shadow) return trace_queue_launch(t, p, a, bs, smem, s);
     // Large blocks with deep stacks need more than the default 48 KB.
     if (smem > 48 * 1024) KDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kernel<<<grid, bs, smem, s>>>(a);
@@ -988,8 +1104,7 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
 {
     TraceArgs a;
     a.c.node = t.tnode.p;
-    a.c.bmin = t.tbmin.p;
-    a.c.bmax = t.tbmax.p;
+    a.c.box = t.tbox.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
     KDGB_CHECK(woop_for(t, p, s, a.c));
@@ -1027,8 +1142,7 @@ int photon_launch(const Tree &t, const kdgb_trace_params &p, const kdgb_photon_p
 {
     PhotonArgs a;
     a.c.node = t.tnode.p;
-    a.c.bmin = t.tbmin.p;
-    a.c.bmax = t.tbmax.p;
+    a.c.box = t.tbox.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
     KDGB_CHECK(woop_for(t, p, s, a.c));
@@ -1068,8 +1182,7 @@ int shade_launch(const Tree &t, const kdgb_trace_params &p, const float *n0, con
 {
     ShadeArgs a;
     a.c.node = t.tnode.p;
-    a.c.bmin = t.tbmin.p;
-    a.c.bmax = t.tbmax.p;
+    a.c.box = t.tbox.p;
     a.c.tri = t.ttri.p;
     a.c.root = 0;
     KDGB_CHECK(woop_for(t, p, s, a.c));

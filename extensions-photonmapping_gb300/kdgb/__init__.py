@@ -21,7 +21,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import scenes
-from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ISECT_MOELLER, ISECT_WOOP, ERR_CAPACITY, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, FINF, LEAF, LOWER_BALANCED, LOWER_BITMAP, LOWER_SAH,
+from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ISECT_MOELLER, ISECT_WOOP, SCHEDULE_GRID, SCHEDULE_QUEUE, ERR_CAPACITY, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, FINF, LEAF, LOWER_BALANCED, LOWER_BITMAP, LOWER_SAH,
                    SPLIT_BOX, SPLIT_DIVIDE, SPLIT_SPLIT,
                    TIE_LOWEST_ID, TIE_REF_LAST, TRACER_BRUTE, TRACER_RESTART, TRACER_SHORTSTACK, X, Y, Z,
                    AutotuneResult, BuildParams, BuildStats, KdgbError, Light, light, PhotonParams, TraceParams, TreeView, build_params, check,
@@ -31,7 +31,8 @@ __all__ = ["KDTree", "Graph", "autotune", "AutotuneResult", "Light", "light", "T
            "trace_params", "photon_params", "PhotonParams", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
            "LOWER_BALANCED", "SPLIT_BOX", "SPLIT_DIVIDE", "SPLIT_SPLIT",
            "BUILD_REFERENCE", "BUILD_TUNED", "TRACER_RESTART", "TRACER_SHORTSTACK", "TRACER_BRUTE",
-           "TIE_LOWEST_ID", "TIE_REF_LAST", "ISECT_MOELLER", "ISECT_WOOP", "FINF", "lib", "library_path"]
+           "TIE_LOWEST_ID", "TIE_REF_LAST", "ISECT_MOELLER", "ISECT_WOOP", "SCHEDULE_GRID", "SCHEDULE_QUEUE", "FINF",
+           "lib", "library_path"]
 
 
 def _torch():

@@ -17,6 +17,7 @@ BUILD_REFERENCE, BUILD_TUNED = 0, 1
 TRACER_RESTART, TRACER_SHORTSTACK, TRACER_BRUTE = 0, 1, 2
 TIE_LOWEST_ID, TIE_REF_LAST = 0, 1
 ISECT_MOELLER, ISECT_WOOP = 0, 1
+SCHEDULE_GRID, SCHEDULE_QUEUE = 0, 1
 
 OK = 0
 ERR_INVALID_ARGUMENT = 1
@@ -43,7 +44,7 @@ class BuildParams(C.Structure):
 class TraceParams(C.Structure):
     _fields_ = [("tracer", C.c_int32), ("leaf_skipping", C.c_int32), ("tie", C.c_int32),
                 ("stack_depth", C.c_int32), ("max_iterations", C.c_int32), ("block_size", C.c_int32),
-                ("tile_width", C.c_int32), ("intersection", C.c_int32)]
+                ("tile_width", C.c_int32), ("intersection", C.c_int32), ("schedule", C.c_int32)]
 
 
 class TreeView(C.Structure):

@@ -95,6 +95,16 @@ enum { KDGB_TRACER_RESTART = 0, KDGB_TRACER_SHORTSTACK = 1, KDGB_TRACER_BRUTE = 
  * after each build. */
 enum { KDGB_ISECT_MOELLER = 0, KDGB_ISECT_WOOP = 1 };
 
+/* How a trace is spread over the GPU (no reference counterpart).  GRID:
+ * one thread per ray, blocks in ray order.  QUEUE: a persistent launch
+ * (as many blocks as fit on the device at once) whose warps take 32-ray
+ * chunks from a device-side work queue; for a batch traced with
+ * rays_per_mesh (ray_mesh_dev NULL) the queue hands out the rays of the
+ * meshes with the most triangles first.  Results are identical.  The queue
+ * state lives in the tree handle: QUEUE traces of one handle must not
+ * overlap on the GPU (other streams). */
+enum { KDGB_SCHEDULE_GRID = 0, KDGB_SCHEDULE_QUEUE = 1 };
+
 /* Exact-tie rule between triangles hit at the same t.  LOWEST_ID is the
  * default; REF_LAST keeps the reference's `t <= tBest` (IRayTracer.h:133),
  * where the last triangle tested wins. */
@@ -127,6 +137,8 @@ typedef struct kdgb_trace_params {
     int32_t tile_width;      /* >0: rays are a row-major image of this width; threads walk
                                 4x8 pixel packets (IRayTracer.h:67-76) */
     int32_t intersection;    /* KDGB_ISECT_*, default MOELLER (IRayTracer.cu:33) */
+    int32_t schedule;        /* KDGB_SCHEDULE_*, default GRID; QUEUE is not used by the fused
+                                primary + shadow trace, photons or shading */
 } kdgb_trace_params;
 
 /* SoA device arrays of a tree, mirroring the KDNode / TriangleNode getters
@@ -371,10 +383,12 @@ KDGB_API int kdgb_graph_destroy(kdgb_graph *graph);
 
 /* Autotuner (no reference counterpart).  Picks leaf_size (16/24/32),
  * sah_bins (8/16/32, tuned mode only), stack_depth (2/4/8, short-stack
- * only) and block_size (64/128/256) for a workload by coordinate descent
- * from `build` / `trace`, scoring each candidate by
- * builds_per_trace * rebuild_ms + trace_ms (median of `reps` timed runs on
- * `stream`; 1 = rebuild every frame, 0 = a static scene).  The workload is
+ * only), block_size (64/128/256) and the schedule (grid or queue) for a
+ * workload by coordinate descent from `build` / `trace`, scoring each
+ * candidate by builds_per_trace * rebuild_ms + trace_ms (median of `reps`
+ * timed runs on `stream`; 1 = rebuild every frame, 0 = a static scene).
+ * rebuild_ms is a graph rebuild (kdgb_graph_launch), as a per-frame rebuild
+ * runs; a host-driven rebuild before it only sizes the graph.  The workload is
  * one mesh (n_meshes = 1, mesh_offsets NULL) or a batch (HOST mesh_offsets
  * as in kdgb_build_batch, rays by ray_mesh_dev or rays_per_mesh); n_rays
  * may be 0 to tune the build alone.  Candidates that fail (a tree that does

@@ -73,3 +73,53 @@ def test_single_mesh_batch_equals_build(kdgb_lib, cuda, oracle):
         host = tree.to_host()
     assert np.array_equal(host.split.view(np.uint32), ref.split.view(np.uint32))
     assert np.array_equal(host.children, ref.children) and np.array_equal(host.prim_indices, ref.prim_indices)
+
+
+@pytest.mark.parametrize("tracer", [0, 1])
+def test_queue_schedule_equals_grid(kdgb_lib, cuda, tracer):
+    """The persistent queue-scheduled trace (largest meshes' rays first) gives
+    exactly the grid launch's results: with rays_per_mesh (mesh order), with
+    a per-ray mesh array (ray order), and for one mesh traced as an image
+    (4x8 packets); two launches in a row check that the queue resets."""
+    meshes, off, o, d = make_batch(12, 200, 30000, 1000, seed=90)
+    tris = np.concatenate(meshes)
+    g = dict(tracer=tracer, stack_depth=8)
+    q = dict(g, schedule=kdgb_lib._lib.SCHEDULE_QUEUE)
+    with kdgb_lib.KDTree.build_batch(tris, off, **SAH_C1) as tree:
+        ref = [x.cpu().numpy() for x in tree.trace_batch(o, d, rays_per_mesh=1000, **g)]
+        for _ in range(2):
+            got = [x.cpu().numpy() for x in tree.trace_batch(o, d, rays_per_mesh=1000, **q)]
+            for a, b in zip(got, ref):
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        owner = np.repeat(np.arange(12), 1000).astype(np.int32)
+        got = [x.cpu().numpy() for x in tree.trace_batch(o, d, ray_mesh=owner, **q)]
+        for a, b in zip(got, ref):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    one = scenes.clustered(20000, seed=91)
+    o2, d2 = scenes.camera_rays(64, 48)
+    with kdgb_lib.KDTree.build(one, **SAH_C1) as tree:
+        ref = [x.cpu().numpy() for x in tree.trace(o2, d2, tile_width=64, **g)]
+        got = [x.cpu().numpy() for x in tree.trace(o2, d2, tile_width=64, **q)]
+        for a, b in zip(got, ref):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_queue_schedule_in_graph(kdgb_lib, cuda):
+    """A forest rebuild + queue-scheduled trace recorded as one graph and
+    launched repeatedly equals the grid-scheduled graph."""
+    import torch
+    meshes, off, o, d = make_batch(16, 500, 20000, 512, seed=95)
+    tris = np.concatenate(meshes)
+    td = torch.from_numpy(tris).cuda()
+    outs = []
+    for schedule in (0, 1):
+        tp = kdgb_lib.trace_params(tracer=1, stack_depth=8, schedule=schedule)
+        with kdgb_lib.KDTree.build_batch(td, off, **TUNED) as tree:
+            g = kdgb_lib.Graph(tree, td, mesh_offsets=off, headroom=1.2, o=o, d=d, rays_per_mesh=512, trace=tp, **TUNED)
+            for _ in range(3):
+                g.launch()
+            assert g.status() == 0
+            outs.append([x.cpu().numpy() for x in g.out])
+            g.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
