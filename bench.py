@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="leave the batched record out of the frame line")
+    ap.add_argument("--meshes", type=int, default=configs.BATCH_MESHES,
+                    help="batched workload: number of meshes (the first of the 512-mesh mix)")
     return ap.parse_args()
 
 
@@ -448,20 +450,29 @@ def run_frame(args, world, rank, local, pg):
         h_o = torch.from_numpy(o).pin_memory()
         h_d = torch.from_numpy(d).pin_memory()
         h_out = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in outs]
-        # The rays are not needed until the trace: they are uploaded on a
-        # second stream while the tree is rebuilt (after the previous step's
-        # trace has read them).  The outputs are read back on a third stream,
-        # so the read-back of one step overlaps the next step's triangle
-        # upload and rebuild; the next trace waits for it before it rewrites
-        # the output buffers.  Every step still copies all its inputs and
-        # reads back all its outputs inside the timed region, which ends
-        # when the last read-back has landed.
+        # Three copy streams keep the copies off the critical path:
+        #  * the triangles of the next step are uploaded while this step's
+        #    trace runs: the build reads the input triangles only while it
+        #    loads them into its own arrays, and the trace never reads them;
+        #  * the rays are uploaded while the tree is rebuilt (after the
+        #    previous step's trace has read them);
+        #  * the outputs are read back while the next step uploads and
+        #    rebuilds; the next trace waits for the read-back before it
+        #    rewrites the output buffers.
+        # Each step of the timed loop issues one triangle upload, one ray
+        # upload and one read-back of all outputs; the region ends when the
+        # last read-back has landed.
+        up = torch.cuda.Stream(device=dev)
         side = torch.cuda.Stream(device=dev)
         back = torch.cuda.Stream(device=dev)
         traced = torch.cuda.Event()
         traced.record(stream)
         read_back = torch.cuda.Event()
         read_back.record(stream)
+        tris_in = torch.cuda.Event()
+        with torch.cuda.stream(up):
+            tris_d.copy_(h_tris, non_blocking=True)
+        tris_in.record(up)
 
         def e2e_step():
             side.wait_event(traced)
@@ -470,8 +481,14 @@ def run_frame(args, world, rank, local, pg):
                 d_d.copy_(h_d, non_blocking=True)
             rays_in = torch.cuda.Event()
             rays_in.record(side)
-            tris_d.copy_(h_tris, non_blocking=True)
+            stream.wait_event(tris_in)
             build()
+            built = torch.cuda.Event()
+            built.record(stream)
+            up.wait_event(built)
+            with torch.cuda.stream(up):
+                tris_d.copy_(h_tris, non_blocking=True)  # the next step's triangles
+            tris_in.record(up)
             stream.wait_event(rays_in)
             stream.wait_event(read_back)
             tree.trace_primary_shadow(o_d, d_d, configs.LIGHT, tp, out=outs)
@@ -492,6 +509,7 @@ def run_frame(args, world, rank, local, pg):
         for _ in range(args.steps):
             e2e_step()
         stream.wait_event(read_back)
+        stream.wait_event(tris_in)
         e1.record(stream)
         e1.synchronize()
         e2e_ms = e0.elapsed_time(e1) / args.steps
@@ -672,11 +690,26 @@ def run_photons(args):
         args, "photon segments Msegments/s (262k-tri clustered, 16M photons x 3 bounces)",
         segs / (res[best] / 1e3) / 1e6, "Msegments/s", True, res[best],
         "clustered-262144-tris, 16M photons from (0.5,3,0.5), 3 bounces, RR p=0.7",
-        {"segments": segs, "restart_ms": res["restart"], "shortstack_ms": res["shortstack"],
-         "restart_msegments_s": segs / (res["restart"] / 1e3) / 1e6,
-         "shortstack_msegments_s": segs / (res["shortstack"] / 1e3) / 1e6, "best": best, "cpu_baseline": cpu})),
+        {"segments": segs, "ms": res, "msegments_s": {k: segs / (v / 1e3) / 1e6 for k, v in res.items()},
+         "best": best, "cpu_baseline": cpu})),
         flush=True)
     tree.close()
+
+
+def profile_batched(args):
+    """--workload batched --profile: one host-driven forest build and one
+    batched trace under each schedule, nothing timed (for ncu captures)."""
+    import torch
+    import kdgb
+    R = configs.BATCH_RAYS_PER_MESH
+    meshes, off, o, d = configs.batch_scene(n_meshes=args.meshes)
+    td, od, dd = (torch.from_numpy(x).cuda() for x in (np.concatenate(meshes), o, d))
+    bp = kdgb.build_params(**dict(configs.TUNED, leaf_size=16))
+    with kdgb.KDTree.build_batch(td, off, bp) as forest:
+        for sch in (kdgb.SCHEDULE_GRID, kdgb.SCHEDULE_QUEUE):
+            forest.trace_batch(od, dd, rays_per_mesh=R, tracer=kdgb.TRACER_SHORTSTACK, stack_depth=8,
+                               block_size=64, schedule=sch)
+        torch.cuda.synchronize()
 
 
 def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
@@ -690,7 +723,7 @@ def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
     import torch
     import kdgb
     R = configs.BATCH_RAYS_PER_MESH
-    meshes, off, o, d = configs.batch_scene()
+    meshes, off, o, d = configs.batch_scene(n_meshes=args.meshes)
     M = len(meshes)
     tris = np.concatenate(meshes)
     td, od, dd = (torch.from_numpy(x).cuda() for x in (tris, o, d))
@@ -763,8 +796,8 @@ def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
         oracle_ok &= bool(np.array_equal(hr, ghit[m * R:(m + 1) * R]))
 
     g, gl, hl = statistics.median(g_ms), statistics.median(gl_ms), statistics.median(hl_ms)
-    rec = {"workload": "512 clustered meshes log-uniform [1k,200k] tris (%d total), 64k random rays each"
-                       % tris.shape[0],
+    rec = {"workload": "%d clustered meshes log-uniform [1k,200k] tris (%d total), 64k random rays each"
+                       % (M, tris.shape[0]),
            "meshes": M, "tris": int(tris.shape[0]), "rays": M * R, "one_graph_ms": g, "meshes_per_s": M / (g / 1e3),
            "rays_mrays_s": M * R / (g / 1e3) / 1e6, "hits": hits,
            "per_mesh_graph_loop_ms": gl, "per_mesh_host_loop_ms": hl,
@@ -786,9 +819,13 @@ def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
 
 
 def run_batched(args):
+    if args.profile:
+        profile_batched(args)
+        return
     rec = measure_batched(args, steps=args.steps, host_loop_steps=max(2, args.steps // 3))
     print(json.dumps(line_common(
-        args, "batched build+trace of 512 meshes, meshes/s (one graph launch)", rec["meshes_per_s"], "meshes/s",
+        args, "batched build+trace of %d meshes, meshes/s (one graph launch)" % rec["meshes"], rec["meshes_per_s"],
+        "meshes/s",
         True, rec["one_graph_ms"], rec["workload"], {"batched": rec})), flush=True)
 
 
