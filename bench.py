@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="leave the batched record out of the frame line")
+    ap.add_argument("--no-others", action="store_true",
+                    help="leave the small, photon and adjoint records out of the frame line")
     ap.add_argument("--meshes", type=int, default=configs.BATCH_MESHES,
                     help="batched workload: number of meshes (the first of the 512-mesh mix)")
     return ap.parse_args()
@@ -558,6 +560,16 @@ def run_frame(args, world, rank, local, pg):
     if rank == 0 and world == 1 and not args.no_batched and graph is not None:
         batched = measure_batched(args, steps=max(3, args.steps // 4), host_loop_steps=1)
 
+    # The other configurations, each a compact copy of its own workload's
+    # line (4096-triangle height field, photons, adjoint).
+    others = None
+    if rank == 0 and world == 1 and not args.no_others and graph is not None:
+        keep = {"metric", "value", "unit", "ms_per_step", "higher_is_better", "config"}
+        common = set(line_common(args, "", 0, "", True, 0, "", {}))
+        others = {}
+        for name, fn in (("small", measure_small), ("photons", measure_photons), ("adjoint", measure_adjoint)):
+            others[name] = {k: v for k, v in fn(args).items() if k in keep or k not in common}
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -571,7 +583,7 @@ def run_frame(args, world, rank, local, pg):
                          "lower_levels": st.lower_levels},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clocks, "parity": parity, "fp64_err": fp64, "other_build": variant,
-                "batched": batched}
+                "batched": batched, "other_configs": others}
         print(json.dumps(line), flush=True)
     if graph is not None:
         graph.close()
@@ -591,9 +603,9 @@ def line_common(args, metric, value, unit, higher, ms, workload_desc, extra):
     return d
 
 
-def run_small(args):
+def measure_small(args):
     """4096-triangle height field, 256x256 pinhole rays: SAH build, kd-restart
-    and brute force."""
+    and brute force.  Returns the workload's line."""
     import torch
     import kdgb
     from kdgb import scenes
@@ -635,22 +647,27 @@ def run_small(args):
                "sample": "oracle build + kd-restart over all 65,536 rays (5 runs); brute force over every 16th ray",
                "build_ms": tb * 1e3, "restart_mrays_s": n / tt / 1e6, "brute_mrays_s": n / tbr / 1e6}
         fp64 = fp64_error(O, tris, o, d, *(x.cpu().numpy() for x in outs), stride=1)
-    print(json.dumps(line_common(
+    line = line_common(
         args, "kd-restart Mrays/s per step (4096-tri SAH build + 256x256 primary rays)", n / (step_ms / 1e3) / 1e6,
         "Mrays/s", True, step_ms, "heightfield-64x32 (4096 tris) 256x256 rays, SAH Ct=1 Ci=1.5 leaf 8",
         {"build_ms_graph": res["graph_build"], "build_ms_host": res["host_build"],
          "restart_trace_ms": res["restart"], "restart_mrays_s": n / (res["restart"] / 1e3) / 1e6,
          "brute_trace_ms": res["brute"], "brute_mrays_s": n / (res["brute"] / 1e3) / 1e6, "cpu_baseline": cpu,
-         "fp64_err": fp64})),
-        flush=True)
+         "fp64_err": fp64})
     graph.close()
     tree.close()
+    return line
 
 
-def run_photons(args):
+def run_small(args):
+    print(json.dumps(measure_small(args)), flush=True)
+
+
+def measure_photons(args):
     """Incoherent load: 16M photons from the frame's point light, 3
     cosine-weighted bounces with Russian roulette (p = 0.7), Philox stream;
-    kd-restart vs short-stack on a 262,144-triangle clustered scene."""
+    kd-restart vs short-stack on a 262,144-triangle clustered scene.  Returns
+    the workload's line."""
     import torch
     import kdgb
     from kdgb import scenes
@@ -686,14 +703,18 @@ def run_photons(args):
         cpu = {"value": int((h != -2).sum()) / dt / 1e6, "unit": "Msegments/s", "cores": os.cpu_count(),
                "kind": "port", "sample": f"first {sample} photons, short-stack, OpenMP over all host cores",
                "segments_equal_gpu": bool(np.array_equal(h, out[0][:sample].cpu().numpy()))}
-    print(json.dumps(line_common(
+    line = line_common(
         args, "photon segments Msegments/s (262k-tri clustered, 16M photons x 3 bounces)",
         segs / (res[best] / 1e3) / 1e6, "Msegments/s", True, res[best],
         "clustered-262144-tris, 16M photons from (0.5,3,0.5), 3 bounces, RR p=0.7",
         {"segments": segs, "ms": res, "msegments_s": {k: segs / (v / 1e3) / 1e6 for k, v in res.items()},
-         "best": best, "cpu_baseline": cpu})),
-        flush=True)
+         "best": best, "cpu_baseline": cpu})
     tree.close()
+    return line
+
+
+def run_photons(args):
+    print(json.dumps(measure_photons(args)), flush=True)
 
 
 def profile_batched(args):
@@ -829,9 +850,10 @@ def run_batched(args):
         True, rec["one_graph_ms"], rec["workload"], {"batched": rec})), flush=True)
 
 
-def run_adjoint(args):
+def measure_adjoint(args):
     """Backward pass of t and barycentrics w.r.t. the vertices of a 100k
-    triangle height field for 512x512 rays with fixed forward hits."""
+    triangle height field for 512x512 rays with fixed forward hits.  Returns
+    the workload's line."""
     import torch
     import kdgb
     from kdgb import scenes
@@ -854,12 +876,17 @@ def run_adjoint(args):
     time_steps(fn, W, stream)
     b_ms = statistics.median(time_steps(fn, args.steps, stream))
     f_ms = statistics.median(time_steps(lambda: tree.trace(od, dd), args.steps, stream))
-    print(json.dumps(line_common(
+    line = line_common(
         args, "adjoint backward ms (100k-tri height field, 512x512 rays)", b_ms, "ms", False, b_ms,
         "heightfield-316x158 (%d tris), 512x512 rays, loss sum w*t + v*(u+v)" % tris.shape[0],
         {"forward_trace_ms": f_ms, "hits": int((hit >= 0).sum().item()),
-         "backward_mrays_s": n / (b_ms / 1e3) / 1e6})), flush=True)
+         "backward_mrays_s": n / (b_ms / 1e3) / 1e6})
     tree.close()
+    return line
+
+
+def run_adjoint(args):
+    print(json.dumps(measure_adjoint(args)), flush=True)
 
 
 def main():
