@@ -19,6 +19,13 @@ Timing: CUDA events on the launching stream around each step, L2 flushed
 (a 512 MB write) between steps outside the events; max over ranks.  Under
 torchrun each rank runs an independent replica (weak scaling).
 
+End to end (`e2e`): the same frames through the library's public calls with
+host buffers: every frame uploads its triangles and rays from pinned host
+memory, rebuilds its tree by one graph launch, traces and reads all its
+outputs back.  Two frames are in flight: two tree handles alternate, so frame
+k+1 is uploaded and rebuilt while frame k is traced and frame k-1 is read
+back.  The one-frame-in-flight figure is reported beside it.
+
 --impl reference times the same frame (same build configuration, tracer and
 rays) with the CPU restatement in oracle/ on all host cores; the reference
 itself does not compile here.
@@ -337,6 +344,83 @@ def time_steps(step, steps, stream, flush=None):
     return out
 
 
+def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d, stream):
+    """End to end with two frames in flight: two tree handles (each with its
+    own rebuild graph and its own input and output buffers) alternate, so
+    frame k+1 is uploaded and rebuilt on one stream while frame k is traced on
+    another and frame k-1 is read back on a third.  Every frame still uploads
+    its triangles and rays from pinned host memory, rebuilds its tree, traces
+    all its rays and reads back all its outputs.  Returns the milliseconds per
+    frame and the host copies of the last two frames' outputs."""
+    import torch
+    import kdgb
+    tris2 = tris_d.clone()
+    tree2 = kdgb.KDTree.build(tris2, bp)
+    graph2 = kdgb.Graph(tree2, tris2, params=bp, headroom=HEADROOM)
+    slots = [dict(tree=tree, graph=graph, tris=tris_d, o=o_d, d=d_d, outs=outs),
+             dict(tree=tree2, graph=graph2, tris=tris2, o=o_d.clone(), d=d_d.clone(),
+                  outs=tuple(torch.empty_like(x) for x in outs))]
+    for sl in slots:
+        sl["h_out"] = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in sl["outs"]]
+        for name in ("built", "traced", "read"):
+            sl[name] = torch.cuda.Event()
+            sl[name].record(stream)
+    sb, st = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    up, back = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    last_in = torch.cuda.Event()
+
+    def frame(k):
+        sl = slots[k & 1]
+        up.wait_event(sl["built"])   # the slot's previous rebuild has read its triangles
+        with torch.cuda.stream(up):
+            sl["tris"].copy_(h_tris, non_blocking=True)
+        tin = torch.cuda.Event()
+        tin.record(up)
+        up.wait_event(sl["traced"])  # the slot's previous trace has read its rays
+        with torch.cuda.stream(up):
+            sl["o"].copy_(h_o, non_blocking=True)
+            sl["d"].copy_(h_d, non_blocking=True)
+        rin = torch.cuda.Event()
+        rin.record(up)
+        last_in.record(up)
+        sb.wait_event(tin)
+        sb.wait_event(sl["traced"])  # the slot's previous trace is done with its tree
+        sl["graph"].launch(stream=sb)
+        sl["built"].record(sb)
+        st.wait_event(sl["built"])
+        st.wait_event(rin)
+        st.wait_event(sl["read"])    # the slot's previous outputs have been read back
+        sl["tree"].trace_primary_shadow(sl["o"], sl["d"], configs.LIGHT, tp, stream=st, out=sl["outs"])
+        sl["traced"].record(st)
+        back.wait_event(sl["traced"])
+        with torch.cuda.stream(back):
+            for hb, db in zip(sl["h_out"], sl["outs"]):
+                hb.copy_(db, non_blocking=True)
+        sl["read"].record(back)
+
+    for k in range(4):
+        frame(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s_ in (sb, st, up, back):
+        s_.wait_event(e0)
+    for k in range(args.steps):
+        frame(k)
+    for sl in slots:
+        stream.wait_event(sl["read"])
+    stream.wait_event(last_in)
+    e1.record(stream)
+    e1.synchronize()
+    for sl in slots:
+        kdgb.check(sl["graph"].status(stream=stream), "graph rebuild")
+    ms = e0.elapsed_time(e1) / args.steps
+    h_outs = [sl["h_out"] for sl in slots]
+    graph2.close()
+    tree2.close()
+    return ms, h_outs
+
+
 def run_frame(args, world, rank, local, pg):
     import torch
     import kdgb
@@ -521,11 +605,28 @@ def run_frame(args, world, rank, local, pg):
             e2e_ms = float(t.item())
         h2d = tris.nbytes + o.nbytes + d.nbytes
         d2h = sum(x.numel() * x.element_size() for x in outs)
-        e2e = {"value": rays_per_step * world / (e2e_ms / 1e3) / 1e6, "unit": "Mrays/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
-        # The host copy of the last e2e step must equal the device-timed
-        # step's outputs (same inputs, same tree).
-        e2e["outputs_equal_device_steps"] = all(np.array_equal(hb.numpy(), g) for hb, g in zip(h_out, gpu_out))
+        if graph is not None:
+            inflight = e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d,
+                                            stream)
+        one = {"value": rays_per_step * world / (e2e_ms / 1e3) / 1e6, "ms_per_step": e2e_ms,
+               # The host copy of the last step must equal the device-timed
+               # step's outputs (same inputs, same tree).
+               "outputs_equal_device_steps": all(np.array_equal(hb.numpy(), g) for hb, g in zip(h_out, gpu_out))}
+        e2e = {"value": one["value"], "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms, "frames_in_flight": 1,
+               "outputs_equal_device_steps": one["outputs_equal_device_steps"]}
+        if graph is not None:
+            ms2, h_outs2 = inflight
+            ms2_all = ms2
+            if pg:
+                t = torch.tensor([ms2], device=dev)
+                pg.all_reduce(t, op=pg.ReduceOp.MAX)
+                ms2_all = float(t.item())
+            e2e.update({"value": rays_per_step * world / (ms2_all / 1e3) / 1e6, "ms_per_step": ms2_all,
+                        "frames_in_flight": 2,
+                        "outputs_equal_device_steps": all(np.array_equal(hb.numpy(), g) for ho in h_outs2
+                                                          for hb, g in zip(ho, gpu_out)),
+                        "one_frame_in_flight": one})
 
     # The other build configuration on the same inputs, for context.
     variant = None
