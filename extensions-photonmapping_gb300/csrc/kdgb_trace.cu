@@ -68,16 +68,21 @@ __device__ __forceinline__ bool surely_negative(float det, float n)
 
 // Moeller-Trumbore on one packed record (IRayTracer.h:111-145).  Triangles
 // whose u or v is certainly negative are rejected before the IEEE
-// reciprocal; every accepted value is computed exactly as the reference does.
+// reciprocal, u first: most tests end there (on the 1M-triangle frame 86% of
+// a primary ray's tests and 82% of a shadow ray's), so the v terms are only
+// computed for triangles that pass it (primary trace of the frame 0.803 ->
+// 0.785 ms).  Every accepted value is computed exactly as the reference does.
 __device__ __forceinline__ void mt_test(float3 v0, float3 e1, float3 e2, int id, float3 o, float3 d, int tie,
                                         int &hit, float &tb, float &ub, float &vb)
 {
     const float3 p = cross3(d, e2);
     const float3 t = sub3(o, v0);
-    const float3 q = cross3(t, e1);
     const float det = dot3(p, e1);
-    const float pt = dot3(p, t), qd = dot3(q, d);
-    if (surely_negative(det, pt) || surely_negative(det, qd)) return;
+    const float pt = dot3(p, t);
+    if (surely_negative(det, pt)) return;
+    const float3 q = cross3(t, e1);
+    const float qd = dot3(q, d);
+    if (surely_negative(det, qd)) return;
     const float inv_det = __frcp_rn(det);
     const float ht = __fmul_rn(inv_det, dot3(q, e2));
     if (0.0f <= ht && ht <= tb) {
