@@ -134,6 +134,11 @@ def test_graph_capacity_stop(kdgb_lib, cuda):
         g.launch()
         assert g.status() == kdgb_lib.ERR_CAPACITY
         assert (g.out[0].cpu().numpy() == -1).all()
+        # The queue-scheduled trace of the failed tree reports misses too, and
+        # leaves its queue ready for the next launch.
+        for _ in range(2):
+            h, t, _, _ = tree.trace(o, d, schedule=kdgb_lib.SCHEDULE_QUEUE)
+            assert (h.cpu().numpy() == -1).all() and torch.isinf(t).all()
         g.close()
         tree.rebuild(busy)
         ref, _ = host_tree(kdgb_lib, busy, {})
