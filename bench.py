@@ -22,9 +22,10 @@ torchrun each rank runs an independent replica (weak scaling).
 End to end (`e2e`): the same frames through the library's public calls with
 host buffers: every frame uploads its triangles and rays from pinned host
 memory, rebuilds its tree by one graph launch, traces and reads all its
-outputs back.  Two frames are in flight: two tree handles alternate, so frame
-k+1 is uploaded and rebuilt while frame k is traced and frame k-1 is read
-back.  The one-frame-in-flight figure is reported beside it.
+outputs back.  Three frames are in flight: three tree handles take the frames
+in turn, each rebuilt on its own stream, so the rebuilds of consecutive
+frames overlap each other and the traces of earlier frames.  The
+one-frame-in-flight figure is reported beside it.
 
 --impl reference times the same frame (same build configuration, tracer and
 rays) with the CPU restatement in oracle/ on all host cores; the reference
@@ -344,33 +345,43 @@ def time_steps(step, steps, stream, flush=None):
     return out
 
 
-def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d, stream):
-    """End to end with two frames in flight: two tree handles (each with its
-    own rebuild graph and its own input and output buffers) alternate, so
-    frame k+1 is uploaded and rebuilt on one stream while frame k is traced on
-    another and frame k-1 is read back on a third.  Every frame still uploads
-    its triangles and rays from pinned host memory, rebuilds its tree, traces
-    all its rays and reads back all its outputs.  Returns the milliseconds per
-    frame and the host copies of the last two frames' outputs."""
+FRAMES_IN_FLIGHT = 3
+
+
+def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d, stream,
+                         n_slots=FRAMES_IN_FLIGHT):
+    """End to end with n_slots frames in flight: as many tree handles (each
+    with its own rebuild graph and its own input and output buffers) take the
+    frames in turn.  Frame k is uploaded and rebuilt on slot k's own
+    rebuild stream (high priority, so the rebuild's short kernels are
+    scheduled ahead of the trace's blocks) while earlier frames are traced on
+    the trace stream and read back on the read-back stream; the rebuilds of
+    consecutive frames overlap each other and the traces.  Every frame still
+    uploads its triangles and rays from pinned host memory, rebuilds its tree,
+    traces all its rays and reads back all its outputs.  Returns the
+    milliseconds per frame and the host copies of the last frames' outputs."""
     import torch
     import kdgb
-    tris2 = tris_d.clone()
-    tree2 = kdgb.KDTree.build(tris2, bp)
-    graph2 = kdgb.Graph(tree2, tris2, params=bp, headroom=HEADROOM)
-    slots = [dict(tree=tree, graph=graph, tris=tris_d, o=o_d, d=d_d, outs=outs),
-             dict(tree=tree2, graph=graph2, tris=tris2, o=o_d.clone(), d=d_d.clone(),
-                  outs=tuple(torch.empty_like(x) for x in outs))]
+    slots = [dict(tree=tree, graph=graph, tris=tris_d, o=o_d, d=d_d, outs=outs)]
+    for _ in range(n_slots - 1):
+        t_ = tris_d.clone()
+        tr = kdgb.KDTree.build(t_, bp)
+        slots.append(dict(tree=tr, graph=kdgb.Graph(tr, t_, params=bp, headroom=HEADROOM), tris=t_,
+                          o=o_d.clone(), d=d_d.clone(), outs=tuple(torch.empty_like(x) for x in outs), own=True))
+    high = torch.cuda.Stream.priority_range()[1]
     for sl in slots:
         sl["h_out"] = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in sl["outs"]]
+        sl["build_stream"] = torch.cuda.Stream(device=dev, priority=high)
         for name in ("built", "traced", "read"):
             sl[name] = torch.cuda.Event()
             sl[name].record(stream)
-    sb, st = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
-    up, back = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    st = torch.cuda.Stream(device=dev)
+    up, back = torch.cuda.Stream(device=dev, priority=high), torch.cuda.Stream(device=dev)
     last_in = torch.cuda.Event()
 
     def frame(k):
-        sl = slots[k & 1]
+        sl = slots[k % n_slots]
+        sb = sl["build_stream"]
         up.wait_event(sl["built"])   # the slot's previous rebuild has read its triangles
         with torch.cuda.stream(up):
             sl["tris"].copy_(h_tris, non_blocking=True)
@@ -398,12 +409,12 @@ def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs,
                 hb.copy_(db, non_blocking=True)
         sl["read"].record(back)
 
-    for k in range(4):
+    for k in range(2 * n_slots):
         frame(k)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for s_ in (sb, st, up, back):
+    for s_ in [sl["build_stream"] for sl in slots] + [st, up, back]:
         s_.wait_event(e0)
     for k in range(args.steps):
         frame(k)
@@ -416,8 +427,10 @@ def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs,
         kdgb.check(sl["graph"].status(stream=stream), "graph rebuild")
     ms = e0.elapsed_time(e1) / args.steps
     h_outs = [sl["h_out"] for sl in slots]
-    graph2.close()
-    tree2.close()
+    for sl in slots:
+        if sl.get("own"):
+            sl["graph"].close()
+            sl["tree"].close()
     return ms, h_outs
 
 
@@ -623,7 +636,7 @@ def run_frame(args, world, rank, local, pg):
                 pg.all_reduce(t, op=pg.ReduceOp.MAX)
                 ms2_all = float(t.item())
             e2e.update({"value": rays_per_step * world / (ms2_all / 1e3) / 1e6, "ms_per_step": ms2_all,
-                        "frames_in_flight": 2,
+                        "frames_in_flight": FRAMES_IN_FLIGHT,
                         "outputs_equal_device_steps": all(np.array_equal(hb.numpy(), g) for ho in h_outs2
                                                           for hb, g in zip(ho, gpu_out)),
                         "one_frame_in_flight": one})
