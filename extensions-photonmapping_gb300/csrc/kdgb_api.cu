@@ -126,6 +126,7 @@ static void release_all(Tree &t, cudaStream_t s)
     release(w.tilesum, s); release(w.tileoff, s); release(w.stats, s); release(w.scan, s); release(w.misc0, s); release(w.misc1, s);
     release(w.big, s); release(w.bighist, s); release(w.areas, s); release(w.sts, s); release(w.ssplit, s); release(w.saddr, s);
     release(w.roff, s); release(w.careas, s); release(w.csets, s); release(w.ranges, s); release(w.state, s);
+    release(w.lowlist[0], s); release(w.lowlist[1], s);
     t.plan = BuildPlan();
     if (w.host) {
         cudaStreamSynchronize(s);

@@ -95,6 +95,7 @@ struct Caps {
     int64_t low_R;    // SAH lower level arrays
     int64_t tris;     // leaf records of the traversal layout
     int64_t big;      // binning chunks listed per tuned level (kSahItem ints each)
+    int64_t list[2];  // SAH lower work list entries, by level parity
 };
 
 // Everything a build kernel touches; passed by value to every kernel.
@@ -129,6 +130,7 @@ struct BuildArgs {
     int32_t *ssplit, *saddr;
     float2 *careas;
     int2 *csets;
+    int32_t *lowlist[2];
     int32_t *loff;  // PackLanes scan: 2 ints per node and the totals
     int2 *tnode;
     float4 *tbox;
@@ -1407,6 +1409,7 @@ __global__ void k_lower_begin(const BuildArgs a)
     st->low_active = 0;
     st->low_first = 1;
     st->low_R = 0;
+    st->low_n[0][0] = st->low_n[0][1] = st->low_n[1][0] = st->low_n[1][1] = 0;
     if (st->err) return;
     if ((int64_t)st->n_leaf_ids > a.cap.low_R) {
         set_err(st, KDGB_ERR_CAPACITY, kErrLowerCapacity);
@@ -1440,51 +1443,54 @@ __device__ __forceinline__ void pick_planes(const unsigned (&s)[4], const float 
     }
 }
 
-// The plane costs of one lower node by its warp (CalcSAH, LowerTriangleMap.h:463-555): lane i holds member
-// slot i's sets (sx, sy, sz: {lowLeft, lowRight, highLeft, highRight} per axis; only members' lanes are read)
-// and evaluates the six planes of its slot in the reference's order; the warp keeps the first minimum in
-// (slot, axis, low/high) order and decides the split.
-__device__ __forceinline__ void sah_eval_node(const BuildArgs &a, int64_t gw, int32_t par, int32_t pi, unsigned bmp,
-                                              int lane, const int4 &sx, const int4 &sy, const int4 &sz)
+// Predicated set updates of the SAH plane passes, written as one compare (or
+// bit test) feeding predicated instructions: acc += aj when bit m of s is
+// set; s |= m and acc += aj when x <= y (x < y).  The additions are IEEE
+// round-to-nearest single additions, as __fadd_rn.
+__device__ __forceinline__ void add_if_bit(float &acc, unsigned s, unsigned m, float aj)
 {
-    const float ct = a.ct, ci = a.ci;
-    const bool mine = (bmp >> lane) & 1u;
-    const float a_lane = mine ? a.areas[pi + lane] : 0.0f;
-    SahPick mb;
-    mb.cost = KDGB_FINF; mb.la = mb.ra = 0.0f; mb.ls = mb.rs = 0; mb.axis = 0; mb.idx = 0;
-    // One pass over the node's references in bit order accumulates the
-    // area sums of all twelve sets (3 axes x {lowLeft, lowRight, highLeft,
-    // highRight}).
-    unsigned sets[3][4] = {{(unsigned)sx.x & bmp, (unsigned)sx.y & bmp, (unsigned)sx.z & bmp, (unsigned)sx.w & bmp},
-                           {(unsigned)sy.x & bmp, (unsigned)sy.y & bmp, (unsigned)sy.z & bmp, (unsigned)sy.w & bmp},
-                           {(unsigned)sz.x & bmp, (unsigned)sz.y & bmp, (unsigned)sz.z & bmp, (unsigned)sz.w & bmp}};
-    float ar[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-    // Only members are added (predicated adds): skipping a +0 term is
-    // exact, so the sums equal the reference's bit-order accumulation.
-    for (unsigned bits = bmp; bits; bits &= bits - 1u) {  // bmp is warp-uniform
-        const int j = __ffs(bits) - 1;
-        const float aj = __shfl_sync(kFull, a_lane, j);
-        const unsigned m = 1u << j;
-#pragma unroll
-        for (int x = 0; x < 3; ++x)
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-                if (sets[x][c] & m) ar[x][c] = __fadd_rn(ar[x][c], aj);
-    }
-    pick_planes(sets[0], ar[0], KDGB_X, pi + lane, mb);
-    pick_planes(sets[1], ar[1], KDGB_Y, pi + lane, mb);
-    pick_planes(sets[2], ar[2], KDGB_Z, pi + lane, mb);
-    // Warp argmin on (cost, lane); only lanes whose cost beat fInfinity count.
+    asm("{\n\t.reg .pred p;\n\t.reg .b32 t;\n\tand.b32 t, %1, %2;\n\tsetp.ne.u32 p, t, 0;\n\t"
+        "@p add.rn.f32 %0, %0, %3;\n\t}"
+        : "+f"(acc)
+        : "r"(s), "r"(m), "f"(aj));
+}
+
+__device__ __forceinline__ void set_le(unsigned &s, float &acc, float x, float y, unsigned m, float aj)
+{
+    asm("{\n\t.reg .pred p;\n\tsetp.le.f32 p, %2, %3;\n\t@p or.b32 %0, %0, %4;\n\t@p add.rn.f32 %1, %1, %5;\n\t}"
+        : "+r"(s), "+f"(acc)
+        : "f"(x), "f"(y), "r"(m), "f"(aj));
+}
+
+__device__ __forceinline__ void set_lt(unsigned &s, float &acc, float x, float y, unsigned m, float aj)
+{
+    asm("{\n\t.reg .pred p;\n\tsetp.lt.f32 p, %2, %3;\n\t@p or.b32 %0, %0, %4;\n\t@p add.rn.f32 %1, %1, %5;\n\t}"
+        : "+r"(s), "+f"(acc)
+        : "f"(x), "f"(y), "r"(m), "f"(aj));
+}
+
+// The split decision of one lower node (CalcSAH, LowerTriangleMap.h:463-555) from the candidates of a group
+// of W lanes (the whole warp or one half): lane r of the group holds the best of its own six planes (mb, valid
+// when `mine`), lanes in slot order.  The first minimum in (slot, axis, low/high) order wins; one lane of the
+// group writes the decision.  A group with bmp == 0 holds no node and writes nothing.
+template <int W>
+__device__ __forceinline__ void sah_decide(const BuildArgs &a, int64_t gw, int32_t par, unsigned bmp, int lane,
+                                           bool mine, const SahPick &mb)
+{
+    const int r = lane & (W - 1);
+    // Group argmin on (cost, lane); only lanes whose cost beat fInfinity count.
     float c = mine && mb.cost < KDGB_FINF ? mb.cost : INFINITY;
-    int owner = mine && mb.cost < KDGB_FINF ? lane : 32;
-    for (int o = 16; o > 0; o >>= 1) {
+    int owner = mine && mb.cost < KDGB_FINF ? r : W;
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) {
         const float c2 = __shfl_xor_sync(kFull, c, o);
         const int w2 = __shfl_xor_sync(kFull, owner, o);
         if (c2 < c || (c2 == c && w2 < owner)) { c = c2; owner = w2; }
     }
-    if (lane == (owner < 32 ? owner : 0)) {
+    if (bmp != 0u && r == (owner < W ? owner : 0)) {
         const int cnt = __popc(bmp);
-        const float opt = owner < 32 ? mb.cost : KDGB_FINF;
+        const float ct = a.ct, ci = a.ci;
+        const float opt = owner < W ? mb.cost : KDGB_FINF;
         const float node_area = a.area[par];
         bool split_it = __fmul_rn(ci, opt) < __fmul_rn(__fsub_rn(__fmul_rn(ci, (float)cnt), ct), node_area);
         if (cnt <= a.min_leaf) split_it = false;
@@ -1500,16 +1506,89 @@ __device__ __forceinline__ void sah_eval_node(const BuildArgs &a, int64_t gw, in
     }
 }
 
+__device__ __forceinline__ void sah_pick_init(SahPick &mb)
+{
+    mb.cost = KDGB_FINF; mb.la = mb.ra = 0.0f; mb.ls = mb.rs = 0; mb.axis = 0; mb.idx = 0;
+}
+
+// Bit position of the r-th (from 0) set bit of m, r < popc(m): the largest p
+// with fewer than r + 1 set bits below it.
+__device__ __forceinline__ int nth_bit(unsigned m, int r)
+{
+    int pos = 0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1)
+        if (__popc(m & ((1u << (pos + s)) - 1u)) <= r) pos += s;
+    return pos;
+}
+
+// The plane costs of one lower node by a group of W lanes (a whole warp, or
+// a half warp for a node of at most 16 members, so that one warp evaluates
+// two such nodes at once): lane r of the group takes the node's r-th member
+// in bit order (slot nth_bit(bmp, r)) with its sets {lowLeft, lowRight,
+// highLeft, highRight} per axis, and sums the member areas of all twelve
+// sets in one pass over the members in bit order.  Only members are added
+// (predicated adds: skipping a +0 term is exact), so every sum equals the
+// reference's bit-order accumulation (CalcAreaForSets,
+// LowerTriangleMap.h:412-461).  Both halves of a warp run the same number of
+// steps (the larger member count); a half without a node has bmp == 0.
+template <int W>
+__device__ __forceinline__ void sah_eval_group(const BuildArgs &a, int64_t gw, int32_t par, int32_t pi, unsigned bmp,
+                                               int lane, int64_t F)
+{
+    const int r = lane & (W - 1);
+    const int cnt = __popc(bmp);
+    const bool mine = r < cnt;
+    const int slot = mine ? nth_bit(bmp, r) : 0;
+    int4 sx = make_int4(0, 0, 0, 0), sy = sx, sz = sx;
+    float a_lane = 0.0f;
+    if (mine) {
+        sx = a.sts[pi + slot];
+        sy = a.sts[F + pi + slot];
+        sz = a.sts[2 * F + pi + slot];
+        a_lane = a.areas[pi + slot];
+    }
+    const unsigned sets[3][4] = {
+        {(unsigned)sx.x & bmp, (unsigned)sx.y & bmp, (unsigned)sx.z & bmp, (unsigned)sx.w & bmp},
+        {(unsigned)sy.x & bmp, (unsigned)sy.y & bmp, (unsigned)sy.z & bmp, (unsigned)sy.w & bmp},
+        {(unsigned)sz.x & bmp, (unsigned)sz.y & bmp, (unsigned)sz.z & bmp, (unsigned)sz.w & bmp}};
+    float ar[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    int steps = cnt;
+    if (W < 32) steps = max(steps, __shfl_xor_sync(kFull, steps, 16));
+    const int base = lane & ~(W - 1);
+    unsigned bits = bmp;
+    for (int t = 0; t < steps; ++t) {  // steps is warp-uniform
+        const unsigned m = bits & (0u - bits);  // the t-th member's bit (0 past the last member)
+        bits ^= m;
+        const float aj = __shfl_sync(kFull, a_lane, base | t);
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) add_if_bit(ar[x][c], sets[x][c], m, aj);
+    }
+    SahPick mb;
+    sah_pick_init(mb);
+    pick_planes(sets[0], ar[0], KDGB_X, pi + slot, mb);
+    pick_planes(sets[1], ar[1], KDGB_Y, pi + slot, mb);
+    pick_planes(sets[2], ar[2], KDGB_Z, pi + slot, mb);
+    sah_decide<W>(a, gw, par, bmp, lane, mine, mb);
+}
+
 // CreateSplittingPlanes (LowerTriangleMap.h:84-155): one warp per node, lane
 // i owns reference slot i.  Sets per axis: {lowLeft, lowRight, highLeft,
 // highRight} of the planes at slot i's box low / high.
 // The members' boxes are staged in shared memory and read back as
 // broadcasts, four members per step, so each member costs two loads instead
-// of six shuffles.  With the SAH creator the warp then evaluates the first
-// lower level's plane costs for its node (k_calc_sah does the later levels).
-__global__ void k_sah_planes(const BuildArgs a)
+// of six shuffles.  With the SAH creator the warp also evaluates the first
+// lower level's plane costs for its node (k_calc_sah does the later levels):
+// the area sums of the twelve sets are accumulated in the same pass over the
+// members, in bit order, as each set bit is found.
+__global__ void __launch_bounds__(kBlock, 4) k_sah_planes(const BuildArgs a)
 {
-    __shared__ float4 s_lo[kWarps][32], s_hi[kWarps][32];
+    // Slot 32 is a sentinel member (an empty box that no plane test accepts)
+    // read by the padding of the last step.
+    __shared__ float4 s_lo[kWarps][33], s_hi[kWarps][33];
+    __shared__ float s_ar[kWarps][33];
     const BuildState *st = a.st;
     if (st->err) return;
     const int64_t F = st->F;
@@ -1517,91 +1596,149 @@ __global__ void k_sah_planes(const BuildArgs a)
     // With the SAH lower creator the warp also evaluates the node's planes
     // (the first lower level; k_lower_begin checks the same capacity).
     const bool first_sah = a.lower == KDGB_LOWER_SAH && (int64_t)st->n_leaf_ids <= a.cap.low_R;
+    if (lane == 0) {
+        s_lo[warp][32] = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
+        s_hi[warp][32] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        s_ar[warp][32] = 0.0f;
+    }
     WARP_STRIDE(gw, st->n_leaf_ids) {
         const int32_t leaf = a.leaf_ids[gw];
         const int32_t pi = a.pidx[leaf];
         const unsigned bmp = (unsigned)a.amt[leaf];
         const bool mine = (bmp >> lane) & 1u;
+        const bool eval = first_sah && __popc(bmp) > a.min_leaf;  // warp-uniform
         float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
         if (mine) { lo = a.fmin[pi + lane]; hi = a.fmax[pi + lane]; }
         s_lo[warp][lane] = lo;
         s_hi[warp][lane] = hi;
+        if (eval) s_ar[warp][lane] = mine ? a.areas[pi + lane] : 0.0f;
         __syncwarp();
         unsigned sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sz[4] = {0, 0, 0, 0};
-        for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; four members per step
-            int jj[4];
-            unsigned mm[4];
+        if (eval) {
+            float ar[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+            for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; four members per step
+                int jj[4];
+                unsigned mm[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                jj[q] = bits ? __ffs(bits) - 1 : 0;
-                mm[q] = bits ? 1u << jj[q] : 0u;
-                bits &= bits - 1u;
-            }
-            float4 mn[4], mx[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                mn[q] = s_lo[warp][jj[q]];
-                mx[q] = s_hi[warp][jj[q]];
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const unsigned m = mm[q];
-                sx[0] |= mn[q].x <= lo.x ? m : 0; sx[1] |= lo.x < mx[q].x ? m : 0;
-                sx[2] |= mn[q].x <= hi.x ? m : 0; sx[3] |= hi.x < mx[q].x ? m : 0;
-                sy[0] |= mn[q].y <= lo.y ? m : 0; sy[1] |= lo.y < mx[q].y ? m : 0;
-                sy[2] |= mn[q].y <= hi.y ? m : 0; sy[3] |= hi.y < mx[q].y ? m : 0;
-                sz[0] |= mn[q].z <= lo.z ? m : 0; sz[1] |= lo.z < mx[q].z ? m : 0;
-                sz[2] |= mn[q].z <= hi.z ? m : 0; sz[3] |= hi.z < mx[q].z ? m : 0;
-            }
-        }
-        const int4 x4 = make_int4(sx[0], sx[1], sx[2], sx[3]), y4 = make_int4(sy[0], sy[1], sy[2], sy[3]),
-                   z4 = make_int4(sz[0], sz[1], sz[2], sz[3]);
-        if (mine) {
-            a.sts[pi + lane] = x4;
-            a.sts[F + pi + lane] = y4;
-            a.sts[2 * F + pi + lane] = z4;
-        }
-        if (first_sah) {  // the first SAH lower level, from the sets in registers
-            if (__popc(bmp) <= a.min_leaf) {  // never split: skip the plane costs
-                if (lane == 0) {
-                    a.info[leaf] = (int8_t)KDGB_LEAF;
-                    a.ssplit[gw] = 0;
+                for (int q = 0; q < 4; ++q) {
+                    jj[q] = bits ? __ffs(bits) - 1 : 32;
+                    mm[q] = bits ? 1u << jj[q] : 0u;
+                    bits &= bits - 1u;
                 }
-            } else {
-                sah_eval_node(a, gw, leaf, pi, bmp, lane, x4, y4, z4);
+                float4 mn[4], mx[4];
+                float aq[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    mn[q] = s_lo[warp][jj[q]];
+                    mx[q] = s_hi[warp][jj[q]];
+                    aq[q] = s_ar[warp][jj[q]];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const unsigned m = mm[q];
+                    const float aj = aq[q];
+                    set_le(sx[0], ar[0][0], mn[q].x, lo.x, m, aj);
+                    set_lt(sx[1], ar[0][1], lo.x, mx[q].x, m, aj);
+                    set_le(sx[2], ar[0][2], mn[q].x, hi.x, m, aj);
+                    set_lt(sx[3], ar[0][3], hi.x, mx[q].x, m, aj);
+                    set_le(sy[0], ar[1][0], mn[q].y, lo.y, m, aj);
+                    set_lt(sy[1], ar[1][1], lo.y, mx[q].y, m, aj);
+                    set_le(sy[2], ar[1][2], mn[q].y, hi.y, m, aj);
+                    set_lt(sy[3], ar[1][3], hi.y, mx[q].y, m, aj);
+                    set_le(sz[0], ar[2][0], mn[q].z, lo.z, m, aj);
+                    set_lt(sz[1], ar[2][1], lo.z, mx[q].z, m, aj);
+                    set_le(sz[2], ar[2][2], mn[q].z, hi.z, m, aj);
+                    set_lt(sz[3], ar[2][3], hi.z, mx[q].z, m, aj);
+                }
             }
+            SahPick mb;
+            sah_pick_init(mb);
+            pick_planes(sx, ar[0], KDGB_X, pi + lane, mb);
+            pick_planes(sy, ar[1], KDGB_Y, pi + lane, mb);
+            pick_planes(sz, ar[2], KDGB_Z, pi + lane, mb);
+            sah_decide<32>(a, gw, leaf, bmp, lane, mine, mb);
+        } else {
+            for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; four members per step
+                int jj[4];
+                unsigned mm[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    jj[q] = bits ? __ffs(bits) - 1 : 0;
+                    mm[q] = bits ? 1u << jj[q] : 0u;
+                    bits &= bits - 1u;
+                }
+                float4 mn[4], mx[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    mn[q] = s_lo[warp][jj[q]];
+                    mx[q] = s_hi[warp][jj[q]];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const unsigned m = mm[q];
+                    sx[0] |= mn[q].x <= lo.x ? m : 0; sx[1] |= lo.x < mx[q].x ? m : 0;
+                    sx[2] |= mn[q].x <= hi.x ? m : 0; sx[3] |= hi.x < mx[q].x ? m : 0;
+                    sy[0] |= mn[q].y <= lo.y ? m : 0; sy[1] |= lo.y < mx[q].y ? m : 0;
+                    sy[2] |= mn[q].y <= hi.y ? m : 0; sy[3] |= hi.y < mx[q].y ? m : 0;
+                    sz[0] |= mn[q].z <= lo.z ? m : 0; sz[1] |= lo.z < mx[q].z ? m : 0;
+                    sz[2] |= mn[q].z <= hi.z ? m : 0; sz[3] |= hi.z < mx[q].z ? m : 0;
+                }
+            }
+            if (first_sah && lane == 0) {  // never split: no plane costs
+                a.info[leaf] = (int8_t)KDGB_LEAF;
+                a.ssplit[gw] = 0;
+            }
+        }
+        if (mine) {
+            a.sts[pi + lane] = make_int4(sx[0], sx[1], sx[2], sx[3]);
+            a.sts[F + pi + lane] = make_int4(sy[0], sy[1], sy[2], sy[3]);
+            a.sts[2 * F + pi + lane] = make_int4(sz[0], sz[1], sz[2], sz[3]);
         }
         __syncwarp();  // the staged boxes are rewritten by the warp's next node
     }
 }
 
-// CalcSAH (LowerTriangleMap.h:463-555), one warp per node.  The first
-// level (the upper leaves) is evaluated by k_sah_planes, which already holds
-// their plane sets in registers.
+// CalcSAH (LowerTriangleMap.h:463-555) for the later lower levels (the
+// first, the upper leaves, is evaluated by k_sah_planes).  Nodes with too
+// few members to split are decided one thread each (no plane costs).  The
+// others were listed by the level before (k_sah_children): the warps take
+// them from the lists, two at a time (one per half warp) from the list of
+// nodes of at most 16 members, then one at a time.  The grid is at most one
+// resident wave, so every warp takes about as many list items as any other.
 __global__ void k_calc_sah(const BuildArgs a)
 {
-    const BuildState *st = a.st;
+    BuildState *st = a.st;
     if (st->err || st->low_first) return;
     const int32_t R = st->low_R, active = st->low_active;
     const int64_t F = st->F;
-    const int lane = threadIdx.x & 31;
-    WARP_STRIDE(gw, R) {
-        const int32_t par = active + (int32_t)gw;
-        const int32_t pi = a.pidx[par];
-        const unsigned bmp = (unsigned)a.amt[par];
-        if (__popc(bmp) <= a.min_leaf) {  // never split: skip the plane costs
-            if (lane == 0) {
-                a.info[par] = (int8_t)KDGB_LEAF;
-                a.ssplit[gw] = 0;
-            }
-            continue;
+    const int b = st->low_levels & 1;
+    // k_sah_children of this level lists the next level's nodes in the other
+    // parity's lists.
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->low_n[b ^ 1][0] = st->low_n[b ^ 1][1] = 0;
+    GRID_STRIDE(k64, R) {
+        const int32_t k = (int32_t)k64;
+        if (__popc((unsigned)a.amt[active + k]) <= a.min_leaf) {
+            a.info[active + k] = (int8_t)KDGB_LEAF;
+            a.ssplit[k] = 0;
         }
-        const bool mine = (bmp >> lane) & 1u;
-        const int4 zero4 = make_int4(0, 0, 0, 0);
-        const int4 sx = mine ? a.sts[pi + lane] : zero4;
-        const int4 sy = mine ? a.sts[F + pi + lane] : zero4;
-        const int4 sz = mine ? a.sts[2 * F + pi + lane] : zero4;
-        sah_eval_node(a, gw, par, pi, bmp, lane, sx, sy, sz);
+    }
+    const int32_t ns = st->low_n[b][0], nb = st->low_n[b][1];
+    const int32_t *__restrict__ list = a.lowlist[b];
+    const int64_t cap = a.cap.list[b];
+    const int64_t pairs = ((int64_t)ns + 1) / 2;
+    const int lane = threadIdx.x & 31;
+    WARP_STRIDE(it, pairs + nb) {
+        if (it < pairs) {  // warp-uniform
+            const bool two = 2 * it + 1 < ns;
+            const int32_t k = list[lane < 16 || !two ? 2 * it : 2 * it + 1];
+            unsigned bmp = (unsigned)a.amt[active + k];
+            const int32_t pi = a.pidx[active + k];
+            if (lane >= 16 && !two) bmp = 0u;  // no second node: the upper half idles
+            sah_eval_group<16>(a, k, active + k, pi, bmp, lane, F);
+        } else {
+            const int32_t k = list[cap - 1 - (it - pairs)];
+            sah_eval_group<32>(a, k, active + k, a.pidx[active + k], (unsigned)a.amt[active + k], lane, F);
+        }
     }
 }
 
@@ -1679,7 +1816,8 @@ __device__ void advance_lower(const BuildArgs &a, BuildState *st)
         const int32_t R = st->low_R;
         if (R == 0) break;
         const int32_t splits = a.saddr[R];
-        if (!lower_fits(a, st, splits) || 2 * (int64_t)splits > a.cap.low_R) {
+        if (!lower_fits(a, st, splits) || 2 * (int64_t)splits > a.cap.low_R ||
+            (a.lower == KDGB_LOWER_SAH && 2 * (int64_t)splits > a.cap.list[(st->low_levels + 1) & 1])) {
             set_err(st, KDGB_ERR_CAPACITY, kErrLowerCapacity);
             break;
         }
@@ -1693,8 +1831,51 @@ __device__ void advance_lower(const BuildArgs &a, BuildState *st)
     if (a.use_cond) cudaGraphSetConditional(a.lower_cond, more ? 1u : 0u);
 }
 
+// Appends the next-level positions of this block's children that are to be
+// evaluated (pl / pr, with sl / sr when they have at most 16 members) to the
+// SAH work lists of the next level: small nodes from the front of the list,
+// larger ones from its end.  One global atomic per list and block; every
+// thread of the block calls it.
+__device__ __forceinline__ void lower_list_push(const BuildArgs &a, BuildState *st, int nb, bool pl, bool sl,
+                                                int32_t ql, bool pr, bool sr, int32_t qr)
+{
+    __shared__ int32_t s_n[2], s_base[2];
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned m0 = __ballot_sync(kFull, pl && sl), m1 = __ballot_sync(kFull, pl && !sl);
+    const unsigned m2 = __ballot_sync(kFull, pr && sr), m3 = __ballot_sync(kFull, pr && !sr);
+    if (threadIdx.x == 0) s_n[0] = s_n[1] = 0;
+    __syncthreads();
+    int32_t ws = 0, wb = 0;
+    if (lane == 0) {
+        const int cs = __popc(m0) + __popc(m2), cb = __popc(m1) + __popc(m3);
+        if (cs) ws = atomicAdd(&s_n[0], cs);
+        if (cb) wb = atomicAdd(&s_n[1], cb);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_base[0] = s_n[0] ? atomicAdd(&st->low_n[nb][0], s_n[0]) : 0;
+        s_base[1] = s_n[1] ? atomicAdd(&st->low_n[nb][1], s_n[1]) : 0;
+    }
+    __syncthreads();
+    ws = __shfl_sync(kFull, ws, 0) + s_base[0];
+    wb = __shfl_sync(kFull, wb, 0) + s_base[1];
+    const unsigned below = (1u << lane) - 1u;
+    const int64_t end = a.cap.list[nb] - 1;
+    int32_t *__restrict__ list = a.lowlist[nb];
+    if (pl) {
+        if (sl) list[ws + __popc(m0 & below)] = ql;
+        else list[end - (wb + __popc(m1 & below))] = ql;
+    }
+    if (pr) {
+        if (sr) list[ws + __popc(m0) + __popc(m2 & below)] = qr;
+        else list[end - (wb + __popc(m1) + __popc(m3 & below))] = qr;
+    }
+}
+
 // CreateLowerSAHChildren (LowerTriangleMap.h:557-600) and, when enabled,
-// PropagateAabbToChildren (LowerTriangleMap.h:602-636).
+// PropagateAabbToChildren (LowerTriangleMap.h:602-636).  With the SAH
+// creator the children that have enough members to be split are listed for
+// the next level's k_calc_sah.
 __global__ void k_sah_children(const BuildArgs a)
 {
     BuildState *st = a.st;
@@ -1704,29 +1885,44 @@ __global__ void k_sah_children(const BuildArgs a)
     const int32_t R = (st->err || !lower_fits(a, st, splits)) ? 0 : st->low_R;
     const int32_t *__restrict__ ids = st->low_first ? a.leaf_ids : nullptr;
     const int32_t active = st->low_active, child_base = st->n_nodes;
-    GRID_STRIDE(k64, R) {
-        const int32_t k = (int32_t)k64;
-        if (!a.ssplit[k]) continue;
-        const int32_t par = ids ? ids[k] : active + k;
-        const int32_t l = child_base + a.saddr[k], r = l + splits;
-        ZERO_NODE(l);
-        ZERO_NODE(r);
-        const float2 ca = a.careas[k];
-        const int2 cs = a.csets[k];
-        a.area[l] = ca.x; a.pidx[l] = a.pidx[par]; a.amt[l] = cs.x;
-        a.area[r] = ca.y; a.pidx[r] = a.pidx[par]; a.amt[r] = cs.y;
-        a.ch[par] = make_int2(l, r);
-        if (a.propagate) {
-            const int axis = a.info[par] & 3;
-            const float sp = a.split[par];
-            const float4 mn = a.bmin[par], mx = a.bmax[par];
-            a.bmin[l] = mn;
-            a.bmin[r] = make_float4(axis == KDGB_X ? sp : mn.x, axis == KDGB_Y ? sp : mn.y,
-                                    axis == KDGB_Z ? sp : mn.z, 0.0f);
-            a.bmax[l] = make_float4(axis == KDGB_X ? sp : mx.x, axis == KDGB_Y ? sp : mx.y,
-                                    axis == KDGB_Z ? sp : mx.z, 0.0f);
-            a.bmax[r] = mx;
+    const int nb = (st->low_levels + 1) & 1;
+    const bool list = a.lower == KDGB_LOWER_SAH && 2 * (int64_t)splits <= a.cap.list[nb];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // Block-uniform trip count (the list appends are block-wide).
+    for (int64_t k0 = (int64_t)blockIdx.x * blockDim.x; k0 < R; k0 += stride) {
+        const int32_t k = (int32_t)(k0 + threadIdx.x);
+        bool pl = false, pr = false, sl = false, sr = false;
+        int32_t ql = 0, qr = 0;
+        if (k < R && a.ssplit[k]) {
+            const int32_t par = ids ? ids[k] : active + k;
+            ql = a.saddr[k];
+            qr = ql + splits;
+            const int32_t l = child_base + ql, r = child_base + qr;
+            ZERO_NODE(l);
+            ZERO_NODE(r);
+            const float2 ca = a.careas[k];
+            const int2 cs = a.csets[k];
+            a.area[l] = ca.x; a.pidx[l] = a.pidx[par]; a.amt[l] = cs.x;
+            a.area[r] = ca.y; a.pidx[r] = a.pidx[par]; a.amt[r] = cs.y;
+            a.ch[par] = make_int2(l, r);
+            if (a.propagate) {
+                const int axis = a.info[par] & 3;
+                const float sp = a.split[par];
+                const float4 mn = a.bmin[par], mx = a.bmax[par];
+                a.bmin[l] = mn;
+                a.bmin[r] = make_float4(axis == KDGB_X ? sp : mn.x, axis == KDGB_Y ? sp : mn.y,
+                                        axis == KDGB_Z ? sp : mn.z, 0.0f);
+                a.bmax[l] = make_float4(axis == KDGB_X ? sp : mx.x, axis == KDGB_Y ? sp : mx.y,
+                                        axis == KDGB_Z ? sp : mx.z, 0.0f);
+                a.bmax[r] = mx;
+            }
+            const int cl = __popc((unsigned)cs.x), cr = __popc((unsigned)cs.y);
+            pl = list && cl > a.min_leaf;
+            pr = list && cr > a.min_leaf;
+            sl = cl <= 16;
+            sr = cr <= 16;
         }
+        if (list) lower_list_push(a, st, nb, pl, sl, ql, pr, sr, qr);  // block-uniform
     }
     if (last_block(st)) advance_lower(a, st);
 }
@@ -1999,6 +2195,10 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.careas = w.careas.p;
     a.csets = w.csets.p;
     a.cap.low_R = INT64_MAX;  // the host sizes each lower level before it runs
+    for (int b = 0; b < 2; ++b) {
+        a.lowlist[b] = w.lowlist[b].p;
+        a.cap.list[b] = w.lowlist[b].cap;
+    }
     a.norder = w.misc0.p;
     a.loff = w.misc1.p;
     a.tnode = t.tnode.p;
@@ -2072,12 +2272,28 @@ int emit_after_upper(const BuildArgs &a, const Launcher &L, const Extents &e, co
     return KDGB_OK;
 }
 
+// k_calc_sah runs at most one resident wave (its warps share the level's
+// work lists evenly).
+unsigned calc_sah_grid(const Launcher &L, int64_t R)
+{
+    static int per_sm = 0;
+    if (per_sm <= 0) {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_calc_sah, kBlock, 0) != cudaSuccess || n < 1) {
+            (void)cudaGetLastError();
+            n = 1;
+        }
+        per_sm = n;
+    }
+    return std::min<unsigned>(L.grid(R, kBlock), (unsigned)(L.sms * per_sm));
+}
+
 int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, Workspace &w, cudaStream_t s)
 {
     if (a.lower == KDGB_LOWER_BALANCED) KDGB_KERNEL(k_calc_balanced, L.grid(e.low_R * 32, kBlock), kBlock, 0, s, a);
-    else KDGB_KERNEL(k_calc_sah, L.grid(e.low_R * 32, kBlock), kBlock, 0, s, a);
+    else KDGB_KERNEL(k_calc_sah, calc_sah_grid(L, e.low_R), kBlock, 0, s, a);
     KDGB_CHECK(scan_exclusive<1>(a.ssplit, a.saddr, e.low_R, s, &w.scan, &a.st->low_R, &a.st->err));
-    KDGB_KERNEL(k_sah_children, L.grid(e.low_R, kBlock, 2), kBlock, 0, s, a);
+    KDGB_KERNEL(k_sah_children, L.grid(e.low_R, kBlock), kBlock, 0, s, a);
     return KDGB_OK;
 }
 
@@ -2200,6 +2416,7 @@ uint64_t layout_signature(const Tree &t)
     MIX(w.chunksum);
     MIX(w.tilesum); MIX(w.tileoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.big); MIX(w.bighist); MIX(w.areas); MIX(w.sts);
     MIX(w.ssplit); MIX(w.saddr); MIX(w.roff); MIX(w.careas); MIX(w.csets); MIX(w.ranges); MIX(w.state);
+    MIX(w.lowlist[0]); MIX(w.lowlist[1]);
 #undef MIX
     return h;
 }
@@ -2372,6 +2589,9 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
                 KDGB_CHECK(grab(w.careas, R, s));
                 KDGB_CHECK(grab(w.csets, R, s));
             }
+            // This level lists the next level's nodes (at most 2R) in the
+            // other parity's work list; its own list is not touched.
+            if (p.lower == KDGB_LOWER_SAH) KDGB_CHECK(ensure(w.lowlist[(st.low_levels + 1) & 1], 2 * R, s));
             const Extents e{0, 0, F, st.n_nodes, nl, R};
             KDGB_CHECK(emit_lower_level(make_args(t, p, T, M, mesh_off_dev), L, e, w, s));
             KDGB_CHECK(fetch_state(t, st, s));
@@ -2451,6 +2671,8 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.saddr, low_R + 1, s));
     KDGB_CHECK(ensure(w.careas, low_R, s));
     KDGB_CHECK(ensure(w.csets, low_R, s));
+    KDGB_CHECK(ensure(w.lowlist[0], low_R, s));
+    KDGB_CHECK(ensure(w.lowlist[1], low_R, s));
     KDGB_CHECK(ensure(w.misc0, nodes, s));
     KDGB_CHECK(ensure(w.misc1, 2 * (nodes + 1), s));
     KDGB_CHECK(ensure(t.tnode, nodes, s));

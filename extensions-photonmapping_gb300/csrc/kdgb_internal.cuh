@@ -99,6 +99,9 @@ struct BuildState {
     int32_t n_big;        // tuned levels: chunks of large active nodes listed for block-wide SAH binning
     int32_t done;         // blocks of the current level-closing kernel that have finished
     int32_t big_next;     // tuned levels: work counter over the listed chunks
+    // SAH lower levels: nodes to evaluate, listed by the level before (by
+    // level parity): [0] nodes of at most 16 members, [1] larger ones.
+    int32_t low_n[2][2];
 };
 
 // Sizes seen by the last host-driven build of a handle; a graph rebuild
@@ -127,6 +130,7 @@ struct Workspace {
     DevArray<float> areas;
     DevArray<int4> sts;
     DevArray<int32_t> ssplit, saddr, roff;
+    DevArray<int32_t> lowlist[2];  // SAH lower work lists, by level parity (small nodes first, large from the end)
     DevArray<float2> careas;
     DevArray<int2> csets, ranges;
     DevArray<BuildState> state;
