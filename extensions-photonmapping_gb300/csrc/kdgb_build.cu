@@ -1110,17 +1110,16 @@ __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_scatter(const BuildA
 }
 
 // EmptySpaceSplitting2 (EmptySpaceSplitting.h:74-184): a chain of split
-// nodes, each with an empty leaf, between the parent and the active node.
-__device__ __forceinline__ void ess_chain(const BuildArgs &a, int32_t k, int32_t active, int32_t start, int pl)
+// nodes, each with an empty leaf, between the parent par0 and the active node
+// `leaf` (box [mn, mx]).
+__device__ __forceinline__ void ess_chain(const BuildArgs &a, int32_t leaf, int32_t start, int pl, int32_t par0,
+                                          float4 mn, float4 mx)
 {
-    const int32_t leaf = active + k;
     const int nn = 2 * __popc(pl);
     for (int j = 0; j < nn; ++j) ZERO_NODE(start + j);
-    const int32_t par0 = a.parent[leaf];
     const int2 c = a.ch[par0];
     if (c.x == leaf) a.ch[par0].x = start;
     else a.ch[par0].y = start;
-    const float4 mn = a.bmin[leaf], mx = a.bmax[leaf];
     int32_t par = start;
     const int8_t axes[3] = {KDGB_X, KDGB_Y, KDGB_Z};
     for (int b = 0; b < 3; ++b) {
@@ -1253,32 +1252,42 @@ __global__ void k_children(const BuildArgs a)
         const int32_t *lb = a.lbase + kLanes * (int64_t)k;
         const int32_t *nb = a.lbase + kLanes * (int64_t)(k + 1);
         const int32_t par = active + k;
-        const int32_t la = lb[4], ra = ln_l + lb[5];
-        const int32_t l = nb[0] - lb[0], r = nb[1] - lb[1];
+        // Every load that depends only on the node is issued before the
+        // first store, so that they are in flight together.
+        const int32_t lb0 = lb[0], lb1 = lb[1], lb2 = lb[2], lb3 = lb[3], lb4 = lb[4], lb5 = lb[5], lb6 = lb[6];
+        const int32_t nb0 = nb[0], nb1 = nb[1];
+        const bool chain = !right && ess;
+        const int pl = chain ? planes[k] : 0;
+        const int32_t par0 = chain ? a.parent[par] : 0;
+        int axis = 0;
+        float sp = 0.0f;
+        float4 mn = make_float4(0.f, 0.f, 0.f, 0.f), mx = mn;
+        if (a.ess) {
+            axis = a.info[par] & 3;
+            sp = a.split[par];
+            mn = a.bmin[par];
+            mx = a.bmax[par];
+        }
+        const int32_t la = lb4, ra = ln_l + lb5;
+        const int32_t l = nb0 - lb0, r = nb1 - lb1;
         const bool lleaf = l < LS, rleaf = r < LS;
         const int32_t lnext = k - la, rnext = (R + k) - ra;
         const int32_t lid = child_start + (lleaf ? la : lnext + leaf_nodes);
         const int32_t rid = child_start + (rleaf ? ra : rnext + leaf_nodes);
         if (!right) {
-            if (ess) {
-                const int pl = planes[k];
-                if (pl) ess_chain(a, k, active, base + lb[6], pl);
-            }
+            if (pl) ess_chain(a, par, base + lb6, pl, par0, mn, mx);
             a.ch[par] = make_int2(lid, rid);
         }
         const int32_t id = right ? rid : lid;
         const bool leaf = right ? rleaf : lleaf;
         const int32_t next = right ? rnext : lnext;
         ZERO_NODE(id);
-        a.pidx[id] = right ? (rleaf ? upper + leaf_l + lb[3] : (total_l - leaf_l) + (lb[1] - lb[3]))
-                           : (lleaf ? upper + lb[2] : lb[0] - lb[2]);
+        a.pidx[id] = right ? (rleaf ? upper + leaf_l + lb3 : (total_l - leaf_l) + (lb1 - lb3))
+                           : (lleaf ? upper + lb2 : lb0 - lb2);
         a.amt[id] = right ? r : l;
         a.parent[id] = par;
         float4 cmin = make_float4(0.f, 0.f, 0.f, 0.f), cmax = cmin;
         if (a.ess) {  // PropagateAabbToChildren runs with empty-space splitting
-            const int axis = a.info[par] & 3;
-            const float sp = a.split[par];
-            const float4 mn = a.bmin[par], mx = a.bmax[par];
             if (right) {
                 cmin = make_float4(axis == KDGB_X ? sp : mn.x, axis == KDGB_Y ? sp : mn.y, axis == KDGB_Z ? sp : mn.z,
                                    0.0f);
@@ -1577,66 +1586,60 @@ __device__ __forceinline__ void sah_eval_group(const BuildArgs &a, int64_t gw, i
 // CreateSplittingPlanes (LowerTriangleMap.h:84-155): one warp per node, lane
 // i owns reference slot i.  Sets per axis: {lowLeft, lowRight, highLeft,
 // highRight} of the planes at slot i's box low / high.
-// The members' boxes are staged in shared memory and read back as
-// broadcasts, four members per step, so each member costs two loads instead
-// of six shuffles.  With the SAH creator the warp also evaluates the first
-// lower level's plane costs for its node (k_calc_sah does the later levels):
-// the area sums of the twelve sets are accumulated in the same pass over the
-// members, in bit order, as each set bit is found.
+// The members' boxes are staged in shared memory in bit order (entry r is
+// the r-th member: its box, its bit in the w of the min corner and its area
+// in the w of the max corner) and read back as broadcasts, four members per
+// step, so each member costs two loads.  With the SAH creator the warp also
+// evaluates the first lower level's plane costs for its node (k_calc_sah
+// does the later levels): the area sums of the twelve sets are accumulated
+// in the same pass over the members, in bit order, as each set bit is found.
 __global__ void __launch_bounds__(kBlock, 4) k_sah_planes(const BuildArgs a)
 {
-    // Slot 32 is a sentinel member (an empty box that no plane test accepts)
-    // read by the padding of the last step.
-    __shared__ float4 s_lo[kWarps][33], s_hi[kWarps][33];
-    __shared__ float s_ar[kWarps][33];
+    // Entries past the last member (up to three) are sentinels: an empty box
+    // that no plane test accepts, bit 0.
+    __shared__ float4 s_lo[kWarps][36], s_hi[kWarps][36];
     const BuildState *st = a.st;
     if (st->err) return;
     const int64_t F = st->F;
     const int lane = threadIdx.x & 31, warp = (threadIdx.x >> 5) & (kWarps - 1);
+    const unsigned below = (1u << lane) - 1u;
     // With the SAH lower creator the warp also evaluates the node's planes
     // (the first lower level; k_lower_begin checks the same capacity).
     const bool first_sah = a.lower == KDGB_LOWER_SAH && (int64_t)st->n_leaf_ids <= a.cap.low_R;
-    if (lane == 0) {
-        s_lo[warp][32] = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
-        s_hi[warp][32] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
-        s_ar[warp][32] = 0.0f;
-    }
     WARP_STRIDE(gw, st->n_leaf_ids) {
         const int32_t leaf = a.leaf_ids[gw];
         const int32_t pi = a.pidx[leaf];
         const unsigned bmp = (unsigned)a.amt[leaf];
+        const int cnt = __popc(bmp);
         const bool mine = (bmp >> lane) & 1u;
-        const bool eval = first_sah && __popc(bmp) > a.min_leaf;  // warp-uniform
+        const bool eval = first_sah && cnt > a.min_leaf;  // warp-uniform
         float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
-        if (mine) { lo = a.fmin[pi + lane]; hi = a.fmax[pi + lane]; }
-        s_lo[warp][lane] = lo;
-        s_hi[warp][lane] = hi;
-        if (eval) s_ar[warp][lane] = mine ? a.areas[pi + lane] : 0.0f;
+        if (mine) {
+            lo = a.fmin[pi + lane];
+            hi = a.fmax[pi + lane];
+            const int r = __popc(bmp & below);
+            s_lo[warp][r] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(1u << lane));
+            s_hi[warp][r] = make_float4(hi.x, hi.y, hi.z, eval ? a.areas[pi + lane] : 0.0f);
+        }
+        if (lane < 4) {
+            s_lo[warp][cnt + lane] = make_float4(INFINITY, INFINITY, INFINITY, __uint_as_float(0u));
+            s_hi[warp][cnt + lane] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        }
         __syncwarp();
         unsigned sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sz[4] = {0, 0, 0, 0};
         if (eval) {
             float ar[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-            for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; four members per step
-                int jj[4];
-                unsigned mm[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    jj[q] = bits ? __ffs(bits) - 1 : 32;
-                    mm[q] = bits ? 1u << jj[q] : 0u;
-                    bits &= bits - 1u;
-                }
+            for (int t = 0; t < cnt; t += 4) {  // cnt is warp-uniform; four members per step
                 float4 mn[4], mx[4];
-                float aq[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    mn[q] = s_lo[warp][jj[q]];
-                    mx[q] = s_hi[warp][jj[q]];
-                    aq[q] = s_ar[warp][jj[q]];
+                    mn[q] = s_lo[warp][t + q];
+                    mx[q] = s_hi[warp][t + q];
                 }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const unsigned m = mm[q];
-                    const float aj = aq[q];
+                    const unsigned m = __float_as_uint(mn[q].w);
+                    const float aj = mx[q].w;
                     set_le(sx[0], ar[0][0], mn[q].x, lo.x, m, aj);
                     set_lt(sx[1], ar[0][1], lo.x, mx[q].x, m, aj);
                     set_le(sx[2], ar[0][2], mn[q].x, hi.x, m, aj);
@@ -1658,24 +1661,16 @@ __global__ void __launch_bounds__(kBlock, 4) k_sah_planes(const BuildArgs a)
             pick_planes(sz, ar[2], KDGB_Z, pi + lane, mb);
             sah_decide<32>(a, gw, leaf, bmp, lane, mine, mb);
         } else {
-            for (unsigned bits = bmp; bits;) {  // bmp is warp-uniform; four members per step
-                int jj[4];
-                unsigned mm[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    jj[q] = bits ? __ffs(bits) - 1 : 0;
-                    mm[q] = bits ? 1u << jj[q] : 0u;
-                    bits &= bits - 1u;
-                }
+            for (int t = 0; t < cnt; t += 4) {  // cnt is warp-uniform; four members per step
                 float4 mn[4], mx[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    mn[q] = s_lo[warp][jj[q]];
-                    mx[q] = s_hi[warp][jj[q]];
+                    mn[q] = s_lo[warp][t + q];
+                    mx[q] = s_hi[warp][t + q];
                 }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const unsigned m = mm[q];
+                    const unsigned m = __float_as_uint(mn[q].w);
                     sx[0] |= mn[q].x <= lo.x ? m : 0; sx[1] |= lo.x < mx[q].x ? m : 0;
                     sx[2] |= mn[q].x <= hi.x ? m : 0; sx[3] |= hi.x < mx[q].x ? m : 0;
                     sy[0] |= mn[q].y <= lo.y ? m : 0; sy[1] |= lo.y < mx[q].y ? m : 0;

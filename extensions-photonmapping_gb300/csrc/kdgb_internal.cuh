@@ -247,9 +247,11 @@ struct NodeLanes {
 #ifdef __CUDACC__
     __device__ __forceinline__ void load(int64_t k, int32_t (&v)[7]) const
     {
-        const int32_t l = cnt[2 * k], r = cnt[2 * k + 1];
+        // Both parities' counts are loaded with the level, so no load waits
+        // for another.
+        const int32_t l = cnt[2 * k], r = cnt[2 * k + 1], e0 = ess[0][k], e1 = ess[1][k], lv = *level;
         const int ll = l < LS, rl = r < LS;
-        v[0] = l; v[1] = r; v[2] = ll ? l : 0; v[3] = rl ? r : 0; v[4] = ll; v[5] = rl; v[6] = ess[*level & 1][k];
+        v[0] = l; v[1] = r; v[2] = ll ? l : 0; v[3] = rl ? r : 0; v[4] = ll; v[5] = rl; v[6] = (lv & 1) ? e1 : e0;
     }
 #endif
 };

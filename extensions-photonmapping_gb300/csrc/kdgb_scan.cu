@@ -76,27 +76,6 @@ __device__ __forceinline__ void block_scan(int32_t (&v)[K], int32_t (&total)[K])
     __syncthreads();
 }
 
-// Loads kItems consecutive records starting at `base` (zeros past n) and
-// returns their per-lane sums.
-template <int K, class In>
-__device__ __forceinline__ void load_items(const In &in, int64_t base, int64_t n, int32_t (&vals)[kItems][K],
-                                           int32_t (&s)[K])
-{
-#pragma unroll
-    for (int k = 0; k < K; ++k) s[k] = 0;
-#pragma unroll
-    for (int i = 0; i < kItems; ++i) {
-        if (base + i < n) {
-            in.load(base + i, vals[i]);
-        } else {
-#pragma unroll
-            for (int k = 0; k < K; ++k) vals[i][k] = 0;
-        }
-#pragma unroll
-        for (int k = 0; k < K; ++k) s[k] += vals[i][k];
-    }
-}
-
 // Scan state in the workspace array: kCtl control words, then kStatus ints
 // per tile: the tile totals (K <= 7 lanes, written once), the inclusive
 // prefix (8 + k) and a flag word (epoch << 2 | kind) at kFlag.  Totals and
@@ -121,16 +100,43 @@ __device__ __forceinline__ void scan_tile(const In &in, int32_t *__restrict__ ou
                                           int32_t *status, unsigned epoch, int32_t *err,
                                           int spin_limit = kSpinLimit)
 {
+    // The tile's records, then their exclusive prefixes: loaded and stored
+    // striped (consecutive threads, consecutive records, so every access is
+    // coalesced), scanned blocked (kItems consecutive records per thread).
+    __shared__ int32_t s_rec[kTile * K];
     __shared__ int32_t s_excl[K];
     const int64_t ntiles = (n + kTile - 1) / kTile;
     if (tile >= ntiles) {  // block-uniform
         if (tile == 0 && threadIdx.x < K) out[threadIdx.x] = 0;  // n == 0: the totals record only
         return;
     }
-    const int64_t base = tile * kTile + (int64_t)threadIdx.x * kItems;
+    const int64_t tbase = tile * kTile;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const int j = i * kThreads + threadIdx.x;
+        int32_t v[K];
+        if (tbase + j < n) {
+            in.load(tbase + j, v);
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; ++k) v[k] = 0;
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) s_rec[j * K + k] = v[k];
+    }
+    __syncthreads();
     int32_t vals[kItems][K], s[K], tot[K];
-    load_items<K>(in, base, n, vals, s);
-    block_scan<K, kThreads>(s, tot);
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] = 0;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            vals[i][k] = s_rec[(threadIdx.x * kItems + i) * K + k];
+            s[k] += vals[i][k];
+        }
+    }
+    block_scan<K, kThreads>(s, tot);  // its barriers also end the reads of s_rec above
     int32_t *mine = status + kStatus * tile;
     if (threadIdx.x == 0) {
         // Publish the tile totals (for tile 0 they are the inclusive prefix).
@@ -198,10 +204,13 @@ __device__ __forceinline__ void scan_tile(const In &in, int32_t *__restrict__ ou
     for (int i = 0; i < kItems; ++i) {
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            if (base + i < n) out[(base + i) * K + k] = s[k];
+            s_rec[(threadIdx.x * kItems + i) * K + k] = s[k];
             s[k] += vals[i][k];
         }
     }
+    __syncthreads();
+    const int valid = (int)(n - tbase < kTile ? n - tbase : kTile);
+    for (int f = threadIdx.x; f < valid * K; f += kThreads) out[tbase * K + f] = s_rec[f];
     if (tile == ntiles - 1 && threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < K; ++k) out[n * K + k] = s_excl[k] + tot[k];
