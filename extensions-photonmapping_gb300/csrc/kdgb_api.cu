@@ -124,7 +124,7 @@ static void release_all(Tree &t, cudaStream_t s)
     for (int b = 0; b < 2; ++b) { release(w.planes[b], s); release(w.ess[b], s); }
     release(w.cnt, s); release(w.lbase, s); release(w.chunksum, s);
     release(w.tilesum, s); release(w.tileoff, s); release(w.stats, s); release(w.scan, s); release(w.misc0, s); release(w.misc1, s);
-    release(w.big, s); release(w.bighist, s); release(w.areas, s); release(w.sts, s); release(w.ssplit, s); release(w.saddr, s);
+    release(w.big, s); release(w.bighist, s); release(w.areas, s); release(w.sts, s); release(w.ssplit, s); release(w.lcnt[0], s); release(w.lcnt[1], s);
     release(w.roff, s); release(w.careas, s); release(w.csets, s); release(w.ranges, s); release(w.state, s);
     release(w.lowlist[0], s); release(w.lowlist[1], s);
     t.plan = BuildPlan();

@@ -68,6 +68,10 @@ constexpr int kSahChunkRefs = 2048;
 // per node of cnt >= kSahBlockRefs references, at most 2 refs / kSahBlockRefs.
 inline int64_t sah_items(int64_t refs) { return 2 * refs / kSahBlockRefs + 1; }
 constexpr unsigned kFull = 0xffffffffu;
+// SAH lower levels: the split decisions are counted per tile of kLowTile
+// consecutive nodes of a level; k_sah_children (one block per tile) numbers
+// the children from these counts.
+constexpr int kLowTile = kBlock;
 
 __host__ __device__ inline int64_t chunks_for(int64_t n) { return (n + kChunk - 1) / kChunk; }
 
@@ -96,6 +100,7 @@ struct Caps {
     int64_t tris;     // leaf records of the traversal layout
     int64_t big;      // binning chunks listed per tuned level (kSahItem ints each)
     int64_t list[2];  // SAH lower work list entries, by level parity
+    int64_t lcnt[2];  // SAH lower tile split counts, by level parity
 };
 
 // Everything a build kernel touches; passed by value to every kernel.
@@ -127,7 +132,8 @@ struct BuildArgs {
     int32_t *roff;
     float *areas;
     int4 *sts;
-    int32_t *ssplit, *saddr;
+    int32_t *ssplit;
+    int32_t *lcnt[2];  // split nodes per kLowTile nodes of a lower level, by level parity
     float2 *careas;
     int2 *csets;
     int32_t *lowlist[2];
@@ -1484,7 +1490,7 @@ __device__ __forceinline__ void set_lt(unsigned &s, float &acc, float x, float y
 // group writes the decision.  A group with bmp == 0 holds no node and writes nothing.
 template <int W>
 __device__ __forceinline__ void sah_decide(const BuildArgs &a, int64_t gw, int32_t par, unsigned bmp, int lane,
-                                           bool mine, const SahPick &mb)
+                                           bool mine, const SahPick &mb, int32_t *tcnt)
 {
     const int r = lane & (W - 1);
     // Group argmin on (cost, lane); only lanes whose cost beat fInfinity count.
@@ -1512,6 +1518,7 @@ __device__ __forceinline__ void sah_decide(const BuildArgs &a, int64_t gw, int32
         }
         a.info[par] = split_it ? (int8_t)mb.axis : (int8_t)KDGB_LEAF;
         a.ssplit[gw] = split_it;
+        if (split_it) atomicAdd(tcnt + gw / kLowTile, 1);
     }
 }
 
@@ -1543,7 +1550,7 @@ __device__ __forceinline__ int nth_bit(unsigned m, int r)
 // steps (the larger member count); a half without a node has bmp == 0.
 template <int W>
 __device__ __forceinline__ void sah_eval_group(const BuildArgs &a, int64_t gw, int32_t par, int32_t pi, unsigned bmp,
-                                               int lane, int64_t F)
+                                               int lane, int64_t F, int32_t *tcnt)
 {
     const int r = lane & (W - 1);
     const int cnt = __popc(bmp);
@@ -1580,7 +1587,7 @@ __device__ __forceinline__ void sah_eval_group(const BuildArgs &a, int64_t gw, i
     pick_planes(sets[0], ar[0], KDGB_X, pi + slot, mb);
     pick_planes(sets[1], ar[1], KDGB_Y, pi + slot, mb);
     pick_planes(sets[2], ar[2], KDGB_Z, pi + slot, mb);
-    sah_decide<W>(a, gw, par, bmp, lane, mine, mb);
+    sah_decide<W>(a, gw, par, bmp, lane, mine, mb, tcnt);
 }
 
 // CreateSplittingPlanes (LowerTriangleMap.h:84-155): one warp per node, lane
@@ -1659,7 +1666,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_sah_planes(const BuildArgs a)
             pick_planes(sx, ar[0], KDGB_X, pi + lane, mb);
             pick_planes(sy, ar[1], KDGB_Y, pi + lane, mb);
             pick_planes(sz, ar[2], KDGB_Z, pi + lane, mb);
-            sah_decide<32>(a, gw, leaf, bmp, lane, mine, mb);
+            sah_decide<32>(a, gw, leaf, bmp, lane, mine, mb, a.lcnt[0]);
         } else {
             for (int t = 0; t < cnt; t += 4) {  // cnt is warp-uniform; four members per step
                 float4 mn[4], mx[4];
@@ -1729,10 +1736,10 @@ __global__ void k_calc_sah(const BuildArgs a)
             unsigned bmp = (unsigned)a.amt[active + k];
             const int32_t pi = a.pidx[active + k];
             if (lane >= 16 && !two) bmp = 0u;  // no second node: the upper half idles
-            sah_eval_group<16>(a, k, active + k, pi, bmp, lane, F);
+            sah_eval_group<16>(a, k, active + k, pi, bmp, lane, F, a.lcnt[b]);
         } else {
             const int32_t k = list[cap - 1 - (it - pairs)];
-            sah_eval_group<32>(a, k, active + k, a.pidx[active + k], (unsigned)a.amt[active + k], lane, F);
+            sah_eval_group<32>(a, k, active + k, a.pidx[active + k], (unsigned)a.amt[active + k], lane, F, a.lcnt[b]);
         }
     }
 }
@@ -1793,6 +1800,7 @@ __global__ void k_calc_balanced(const BuildArgs a)
             }
             a.info[par] = split_it ? (int8_t)axis : (int8_t)KDGB_LEAF;
             a.ssplit[gw] = split_it;
+            if (split_it) atomicAdd(a.lcnt[st->low_levels & 1] + gw / kLowTile, 1);
         }
     }
 }
@@ -1803,14 +1811,13 @@ __device__ __forceinline__ bool lower_fits(const BuildArgs &a, const BuildState 
 }
 
 // End of a SAH lower level (one thread of the level's last block).
-__device__ void advance_lower(const BuildArgs &a, BuildState *st)
+__device__ void advance_lower(const BuildArgs &a, BuildState *st, int32_t splits)
 {
     int more = 0;
     do {
         if (st->err) break;
         const int32_t R = st->low_R;
         if (R == 0) break;
-        const int32_t splits = a.saddr[R];
         if (!lower_fits(a, st, splits) || 2 * (int64_t)splits > a.cap.low_R ||
             (a.lower == KDGB_LOWER_SAH && 2 * (int64_t)splits > a.cap.list[(st->low_levels + 1) & 1])) {
             set_err(st, KDGB_ERR_CAPACITY, kErrLowerCapacity);
@@ -1867,30 +1874,67 @@ __device__ __forceinline__ void lower_list_push(const BuildArgs &a, BuildState *
     }
 }
 
+// Sum of v over the block (every thread gets it); s_red holds kWarps ints.
+__device__ __forceinline__ int32_t block_sum(int32_t v, int32_t *s_red)
+{
+    v = __reduce_add_sync(kFull, v);
+    __syncthreads();  // s_red may still be read by the previous call
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int32_t t = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) t += s_red[w];
+    return t;
+}
+
 // CreateLowerSAHChildren (LowerTriangleMap.h:557-600) and, when enabled,
-// PropagateAabbToChildren (LowerTriangleMap.h:602-636).  With the SAH
-// creator the children that have enough members to be split are listed for
-// the next level's k_calc_sah.
+// PropagateAabbToChildren (LowerTriangleMap.h:602-636).  The children of the
+// split nodes are numbered as the reference's scan of the split flags does:
+// left children in node order, then right children.  The level's split
+// decisions were counted per tile of kLowTile nodes; one block takes a tile,
+// its first split's number is the sum of the earlier tiles' counts and each
+// split's rank inside the tile comes from a block scan of the flags.  With
+// the SAH creator the children that have enough members to be split are
+// listed for the next level's k_calc_sah.
 __global__ void k_sah_children(const BuildArgs a)
 {
+    __shared__ int32_t s_red[kWarps], s_wc[kWarps];
     BuildState *st = a.st;
-    const int32_t splits = a.saddr[st->low_R];
+    const int32_t R0 = st->low_R;
+    const int b = st->low_levels & 1, nb = b ^ 1;
+    const int32_t *__restrict__ tc = a.lcnt[b];
+    const int64_t ntile = ((int64_t)R0 + kLowTile - 1) / kLowTile;
+    int32_t part = 0;
+    for (int64_t i = threadIdx.x; i < ntile; i += blockDim.x) part += tc[i];
+    const int32_t splits = block_sum(part, s_red);
     // After a failure, or when the children do not fit (advance_lower
     // records that), no block writes.
-    const int32_t R = (st->err || !lower_fits(a, st, splits)) ? 0 : st->low_R;
+    const int32_t R = (st->err || !lower_fits(a, st, splits)) ? 0 : R0;
     const int32_t *__restrict__ ids = st->low_first ? a.leaf_ids : nullptr;
     const int32_t active = st->low_active, child_base = st->n_nodes;
-    const int nb = (st->low_levels + 1) & 1;
     const bool list = a.lower == KDGB_LOWER_SAH && 2 * (int64_t)splits <= a.cap.list[nb];
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    // Block-uniform trip count (the list appends are block-wide).
-    for (int64_t k0 = (int64_t)blockIdx.x * blockDim.x; k0 < R; k0 += stride) {
-        const int32_t k = (int32_t)(k0 + threadIdx.x);
+    {  // the next level counts its splits from zero
+        const int64_t nt = min((2 * (int64_t)splits + kLowTile - 1) / kLowTile, a.cap.lcnt[nb]);
+        GRID_STRIDE(i, R > 0 ? nt : 0) a.lcnt[nb][i] = 0;
+    }
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t rtiles = ((int64_t)R + kLowTile - 1) / kLowTile;
+    for (int64_t t = blockIdx.x; t < rtiles; t += gridDim.x) {  // block-uniform
+        int32_t ps = 0;
+        for (int64_t i = threadIdx.x; i < t; i += blockDim.x) ps += tc[i];
+        const int32_t pre = block_sum(ps, s_red);
+        const int32_t k = (int32_t)(t * kLowTile) + (int32_t)threadIdx.x;
+        const bool sp = k < R && a.ssplit[k];
+        const unsigned bal = __ballot_sync(kFull, sp);
+        if (lane == 0) s_wc[warp] = __popc(bal);
+        __syncthreads();
+        int32_t wo = 0;
+        for (unsigned w = 0; w < warp; ++w) wo += s_wc[w];
         bool pl = false, pr = false, sl = false, sr = false;
         int32_t ql = 0, qr = 0;
-        if (k < R && a.ssplit[k]) {
+        if (sp) {
             const int32_t par = ids ? ids[k] : active + k;
-            ql = a.saddr[k];
+            ql = pre + wo + __popc(bal & ((1u << lane) - 1u));
             qr = ql + splits;
             const int32_t l = child_base + ql, r = child_base + qr;
             ZERO_NODE(l);
@@ -1902,13 +1946,13 @@ __global__ void k_sah_children(const BuildArgs a)
             a.ch[par] = make_int2(l, r);
             if (a.propagate) {
                 const int axis = a.info[par] & 3;
-                const float sp = a.split[par];
+                const float spl = a.split[par];
                 const float4 mn = a.bmin[par], mx = a.bmax[par];
                 a.bmin[l] = mn;
-                a.bmin[r] = make_float4(axis == KDGB_X ? sp : mn.x, axis == KDGB_Y ? sp : mn.y,
-                                        axis == KDGB_Z ? sp : mn.z, 0.0f);
-                a.bmax[l] = make_float4(axis == KDGB_X ? sp : mx.x, axis == KDGB_Y ? sp : mx.y,
-                                        axis == KDGB_Z ? sp : mx.z, 0.0f);
+                a.bmin[r] = make_float4(axis == KDGB_X ? spl : mn.x, axis == KDGB_Y ? spl : mn.y,
+                                        axis == KDGB_Z ? spl : mn.z, 0.0f);
+                a.bmax[l] = make_float4(axis == KDGB_X ? spl : mx.x, axis == KDGB_Y ? spl : mx.y,
+                                        axis == KDGB_Z ? spl : mx.z, 0.0f);
                 a.bmax[r] = mx;
             }
             const int cl = __popc((unsigned)cs.x), cr = __popc((unsigned)cs.y);
@@ -1919,7 +1963,7 @@ __global__ void k_sah_children(const BuildArgs a)
         }
         if (list) lower_list_push(a, st, nb, pl, sl, ql, pr, sr, qr);  // block-uniform
     }
-    if (last_block(st)) advance_lower(a, st);
+    if (last_block(st)) advance_lower(a, st, splits);
 }
 
 // ---------------------------------------------------------------------------
@@ -2186,7 +2230,10 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
     a.areas = w.areas.p;
     a.sts = w.sts.p;
     a.ssplit = w.ssplit.p;
-    a.saddr = w.saddr.p;
+    for (int b = 0; b < 2; ++b) {
+        a.lcnt[b] = w.lcnt[b].p;
+        a.cap.lcnt[b] = w.lcnt[b].cap;
+    }
     a.careas = w.careas.p;
     a.csets = w.csets.p;
     a.cap.low_R = INT64_MAX;  // the host sizes each lower level before it runs
@@ -2261,11 +2308,18 @@ int emit_after_upper(const BuildArgs &a, const Launcher &L, const Extents &e, co
         KDGB_KERNEL(k_bitmap_leaves, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
     }
     if (lower_loop(p)) {
+        // The split counters of the first two lower levels start at zero
+        // (k_sah_children clears those of every later level).
+        for (int b = 0; b < 2; ++b)
+            KDGB_CUDA(cudaMemsetAsync(a.lcnt[b], 0, sizeof(int32_t) * (size_t)a.cap.lcnt[b], s));
         KDGB_KERNEL(k_sah_planes, L.grid(e.leaves * 32, kBlock), kBlock, 0, s, a);
         KDGB_KERNEL(k_lower_begin, 1, 1, 0, s, a);
     }
     return KDGB_OK;
 }
+
+// Split counters for a lower level of n nodes.
+inline int64_t low_tiles(int64_t n) { return std::max<int64_t>(1, ceil_div(n, kLowTile)); }
 
 // k_calc_sah runs at most one resident wave (its warps share the level's
 // work lists evenly).
@@ -2287,8 +2341,7 @@ int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, Wo
 {
     if (a.lower == KDGB_LOWER_BALANCED) KDGB_KERNEL(k_calc_balanced, L.grid(e.low_R * 32, kBlock), kBlock, 0, s, a);
     else KDGB_KERNEL(k_calc_sah, calc_sah_grid(L, e.low_R), kBlock, 0, s, a);
-    KDGB_CHECK(scan_exclusive<1>(a.ssplit, a.saddr, e.low_R, s, &w.scan, &a.st->low_R, &a.st->err));
-    KDGB_KERNEL(k_sah_children, L.grid(e.low_R, kBlock), kBlock, 0, s, a);
+    KDGB_KERNEL(k_sah_children, L.grid(e.low_R, kLowTile), kLowTile, 0, s, a);  // a block per tile of nodes
     return KDGB_OK;
 }
 
@@ -2379,7 +2432,8 @@ void graph_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, const
     a.cap.refs[1] = std::min(a.cap.refs[1], chunk_refs);
     a.cap.R = std::min(a.cap.R, w.lbase.cap / kLanes - 1);
     a.cap.leaves = t.leaf_ids.cap;
-    a.cap.low_R = std::min({w.ssplit.cap, w.saddr.cap - 1, w.careas.cap, w.csets.cap});
+    a.cap.low_R = std::min({w.ssplit.cap, w.careas.cap, w.csets.cap,
+                            std::min(w.lcnt[0].cap, w.lcnt[1].cap) * (int64_t)kLowTile});
     a.cap.fin = std::min({a.cap.fin, t.prim_indices.cap, w.areas.cap, w.sts.cap / 3});
     a.cap.nodes = std::min({a.cap.nodes, w.misc0.cap, w.misc1.cap / 2 - 1, t.tnode.cap, t.tbox.cap / kBoxStride,
                             kMaxPackNodes - 1});
@@ -2410,7 +2464,7 @@ uint64_t layout_signature(const Tree &t)
     MIX(w.keys); MIX(w.planes[0]); MIX(w.planes[1]); MIX(w.cnt); MIX(w.ess[0]); MIX(w.ess[1]); MIX(w.lbase);
     MIX(w.chunksum);
     MIX(w.tilesum); MIX(w.tileoff); MIX(w.scan); MIX(w.misc0); MIX(w.misc1); MIX(w.big); MIX(w.bighist); MIX(w.areas); MIX(w.sts);
-    MIX(w.ssplit); MIX(w.saddr); MIX(w.roff); MIX(w.careas); MIX(w.csets); MIX(w.ranges); MIX(w.state);
+    MIX(w.ssplit); MIX(w.lcnt[0]); MIX(w.lcnt[1]); MIX(w.roff); MIX(w.careas); MIX(w.csets); MIX(w.ranges); MIX(w.state);
     MIX(w.lowlist[0]); MIX(w.lowlist[1]);
 #undef MIX
     return h;
@@ -2556,7 +2610,9 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
         // writes them with the SAH creator (the loop's grab keeps them, as
         // the first level needs exactly this size).
         KDGB_CHECK(grab(w.ssplit, nl, s));
-        KDGB_CHECK(grab(w.saddr, nl + 1, s));
+        // Split counters of the first two levels (cleared before the first).
+        KDGB_CHECK(ensure(w.lcnt[0], low_tiles(nl), s, 0, true));
+        KDGB_CHECK(ensure(w.lcnt[1], low_tiles(2 * nl), s, 0, true));
         KDGB_CHECK(grab(w.careas, nl, s));
         KDGB_CHECK(grab(w.csets, nl, s));
     }
@@ -2575,12 +2631,14 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
                 // The first level's decisions may already sit in these
                 // arrays (k_sah_planes writes them): they were sized for all
                 // upper leaves above and must not be regrown here.
-                if (R > w.ssplit.cap || R + 1 > w.saddr.cap || R > w.careas.cap || R > w.csets.cap)
+                if (R > w.ssplit.cap || R > w.careas.cap || R > w.csets.cap)
                     return fail(KDGB_ERR_CAPACITY, "first SAH lower level exceeds its decision arrays");
                 first = false;
             } else {
                 KDGB_CHECK(grab(w.ssplit, R, s));
-                KDGB_CHECK(grab(w.saddr, R + 1, s));
+                // This level's counters: cleared by the level before, or
+                // zeroed here when they have to grow.
+                KDGB_CHECK(ensure(w.lcnt[st.low_levels & 1], low_tiles(R), s, 0, true));
                 KDGB_CHECK(grab(w.careas, R, s));
                 KDGB_CHECK(grab(w.csets, R, s));
             }
@@ -2663,7 +2721,8 @@ int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M,
     KDGB_CHECK(ensure(w.areas, fin, s));
     KDGB_CHECK(ensure(w.sts, 3 * fin, s));
     KDGB_CHECK(ensure(w.ssplit, low_R, s));
-    KDGB_CHECK(ensure(w.saddr, low_R + 1, s));
+    KDGB_CHECK(ensure(w.lcnt[0], low_tiles(low_R), s));
+    KDGB_CHECK(ensure(w.lcnt[1], low_tiles(low_R), s));
     KDGB_CHECK(ensure(w.careas, low_R, s));
     KDGB_CHECK(ensure(w.csets, low_R, s));
     KDGB_CHECK(ensure(w.lowlist[0], low_R, s));

@@ -129,7 +129,8 @@ struct Workspace {
     DevArray<int32_t> bighist;  // per-node SAH histograms of chunked large nodes, zero between uses
     DevArray<float> areas;
     DevArray<int4> sts;
-    DevArray<int32_t> ssplit, saddr, roff;
+    DevArray<int32_t> ssplit, roff;
+    DevArray<int32_t> lcnt[2];  // SAH lower levels: split nodes per tile of nodes, by level parity
     DevArray<int32_t> lowlist[2];  // SAH lower work lists, by level parity (small nodes first, large from the end)
     DevArray<float2> careas;
     DevArray<int2> csets, ranges;
