@@ -2068,11 +2068,10 @@ __global__ void k_pack_tris(int32_t n_host, const int32_t *n_dev, const int32_t 
                 if (e <= r) j += step;
             }
             const int ej = __shfl_sync(kFull, excl, j);
-            unsigned m = __shfl_sync(kFull, bmp, j);
+            const unsigned m = __shfl_sync(kFull, bmp, j);
             const int32_t fj = __shfl_sync(kFull, first, j);
             if (r < total) {
-                for (int k = r - ej; k > 0; --k) m &= m - 1u;
-                const int32_t prim = prim_indices[fj + __ffs(m) - 1];
+                const int32_t prim = prim_indices[fj + nth_bit(m, r - ej)];
                 const float4 *src = prec + 3 * (int64_t)prim;
                 const float4 qa = __ldg(src), qb = __ldg(src + 1), qc = __ldg(src + 2);
                 const int64_t rec = rec0 + r;
