@@ -521,8 +521,9 @@ __device__ __forceinline__ int trace_ray(const TraceArgs &a, int64_t i, int2 *st
 }
 
 // Dynamic shared memory: the per-thread regions of stack_entries() int2
-// (short stack or remembered descents) followed, with shadow rays, by a
-// queue of blockDim ShadowItem.  Capped at 40 registers: the traversal is
+// (short stack or remembered descents); with shadow rays, the queue of
+// blockDim ShadowItem the primary rays fill for the shadow pass overlays
+// them (at least two entries per thread).  Capped at 40 registers: the traversal is
 // bound by latency and issue, and the extra resident warps (75% occupancy
 // instead of 56%) gain more than the few spilled values cost (measured on
 // the 1M-triangle frame: 1.61 ms against 1.72 ms uncapped, 1.67 ms at 48
@@ -552,8 +553,10 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
     if (SHADOW) {
         // The block's shadow rays (one per primary hit) are packed onto its
         // first threads, so warps stay full while they are traced.
+        // The queue overlays the stack region, which no primary ray uses any
+        // more once the block has passed this barrier.
         __shared__ int s_count;
-        ShadowItem *queue = (ShadowItem *)(trace_smem + sizeof(int2) * stack_entries(TRACER, a.depth) * blockDim.x);
+        ShadowItem *queue = (ShadowItem *)trace_smem;
         if (threadIdx.x == 0) s_count = 0;
         __syncthreads();
         if (h >= 0) {
@@ -565,8 +568,11 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
             a.occ[i] = 0;
         }
         __syncthreads();
-        if ((int)threadIdx.x < s_count) {
-            const ShadowItem q = queue[threadIdx.x];
+        const bool queued = (int)threadIdx.x < s_count;
+        ShadowItem q;
+        if (queued) q = queue[threadIdx.x];
+        __syncthreads();  // every item is read before the shadow rays' descents reuse the region
+        if (queued) {
             const int64_t ray = ray_index((int64_t)blockIdx.x * blockDim.x + __float_as_int(q.p.w), a.tile_width);
             Ctx cs = a.c;
             cs.root = ray_mesh_of(a, ray);
@@ -1085,8 +1091,9 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
     const unsigned grid = blocks_for(n, bs);
     const bool skip = p.leaf_skipping != 0;
     const bool shadow = occ != nullptr;
-    const size_t smem = sizeof(int2) * (size_t)stack_entries(p.tracer, p.stack_depth) * bs +
-                        (shadow ? sizeof(ShadowItem) * (size_t)bs : 0);
+    // With shadow rays the block's queue (one ShadowItem, two int2, per
+    // thread) overlays the stack region.
+    const size_t smem = sizeof(int2) * (size_t)std::max(stack_entries(p.tracer, p.stack_depth), shadow ? 2 : 0) * bs;
     void (*kernel)(TraceArgs);
     if (p.tracer == KDGB_TRACER_SHORTSTACK) {
         kernel = skip ? (shadow ? k_trace<KDGB_TRACER_SHORTSTACK, true, true> : k_trace<KDGB_TRACER_SHORTSTACK, true, false>)
