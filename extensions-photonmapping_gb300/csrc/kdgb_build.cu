@@ -538,10 +538,7 @@ __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_count(const BuildArg
         GRID_STRIDE(i, 6 * next) a.keys[i] = (i % 6) < 3 ? lo_key : hi_key;
         // This level's list of large nodes has been binned; k_children lists
         // the next level's.
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            a.st->n_big = 0;
-            a.st->big_next = 0;
-        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.st->n_big = 0;
     }
     __shared__ int s_owner[kWarps], s_l[kWarps], s_r[kWarps], s_tl[kWarps], s_tr[kWarps];
     const BuildState *st = a.st;
@@ -787,7 +784,7 @@ __device__ __forceinline__ SahNode sah_node(const BuildArgs &a, int32_t node)
 
 // Binned SAH of the active nodes, one launch per tuned level.  First the
 // chunks of the nodes with kSahBlockRefs references or more (listed with the
-// splits), one block each, taken from a work counter: every warp bins an
+// splits), one block each, dealt to the blocks in turn: every warp bins an
 // interleaved share of the chunk's rows into its own histograms, the block
 // sums them and adds them into the node's global slot, and the block that
 // finishes the node's last chunk picks its split (a node of one chunk is
@@ -797,7 +794,7 @@ __device__ __forceinline__ SahNode sah_node(const BuildArgs &a, int32_t node)
 __global__ void __launch_bounds__(kBlock, 4) k_sah_bin(const BuildArgs a)
 {
     __shared__ int s_hist[kWarps][6 * 32];
-    __shared__ int32_t s_big, s_last;
+    __shared__ int32_t s_last;
     BuildState *st = a.st;
     if (!sah_level(a, st)) return;
     const int32_t nb = st->n_big, R = st->R, active = st->active;
@@ -808,11 +805,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_sah_bin(const BuildArgs a)
     int *h = s_hist[warp];
     int hv[6];
     constexpr int kChunkRows = kSahChunkRefs / 32;
-    for (;;) {
-        if (threadIdx.x == 0) s_big = atomicAdd(&st->big_next, 1);
-        __syncthreads();
-        const int32_t it = s_big;
-        if (it >= nb) break;  // block-uniform
+    // Chunks are dealt to the blocks in turn (they hold at most kSahChunkRefs
+    // references each, so the shares are even); a shared work counter would
+    // make every block of the grid contend for one address twice.
+    for (int32_t it = blockIdx.x; it < nb; it += gridDim.x) {  // block-uniform
         const int4 item = reinterpret_cast<const int4 *>(a.big)[it];  // {k, slot, chunk, chunks}
         const SahNode n = sah_node(a, active + item.x);
         for (int j = lane; j < 6 * 32; j += 32) h[j] = 0;
@@ -852,7 +848,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_sah_bin(const BuildArgs a)
                 sah_pick(a, n, hv, lane);
             }
         }
-        __syncthreads();  // s_hist, s_big and s_last are reused
+        __syncthreads();  // s_hist and s_last are reused
     }
     WARP_STRIDE(gw, R) {
         const int32_t node = active + (int32_t)gw;

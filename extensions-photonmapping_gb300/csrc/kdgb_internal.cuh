@@ -98,7 +98,6 @@ struct BuildState {
     int32_t n_leaf_tris;  // leaf records of the traversal layout
     int32_t n_big;        // tuned levels: chunks of large active nodes listed for block-wide SAH binning
     int32_t done;         // blocks of the current level-closing kernel that have finished
-    int32_t big_next;     // tuned levels: work counter over the listed chunks
     // SAH lower levels: nodes to evaluate, listed by the level before (by
     // level parity): [0] nodes of at most 16 members, [1] larger ones.
     int32_t low_n[2][2];
