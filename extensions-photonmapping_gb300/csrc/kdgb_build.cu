@@ -1313,20 +1313,22 @@ __global__ void k_children(const BuildArgs a)
 
 // MarkLeafNodes (TriangleUpperChildren.h:385-395) over all levels at once:
 // each level appended a contiguous range of leaf node ids.
+__device__ __forceinline__ int32_t upper_leaf_id(const BuildArgs &a, int32_t nr, int32_t i)
+{
+    int lo = 0, hi = nr - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.roff[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    return a.ranges[lo].x + (i - a.roff[lo]);
+}
+
 __global__ void k_leaf_ids(const BuildArgs a)
 {
     const BuildState *st = a.st;
     if (st->err) return;
     const int32_t total = st->n_leaf_ids, nr = st->n_ranges;
-    GRID_STRIDE(ii, total) {
-        const int32_t i = (int32_t)ii;
-        int lo = 0, hi = nr - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (a.roff[mid] <= i) lo = mid; else hi = mid - 1;
-        }
-        a.leaf_ids[i] = a.ranges[lo].x + (i - a.roff[lo]);
-    }
+    GRID_STRIDE(ii, total) a.leaf_ids[ii] = upper_leaf_id(a, nr, (int32_t)ii);
 }
 
 // ExtractIndexFromAabb (TriangleUpper.h:43-52).
@@ -1377,12 +1379,15 @@ __global__ void k_bitmap_leaves(const BuildArgs a)
 // ---------------------------------------------------------------------------
 
 // CalcSurfaceArea (LowerTriangleMap.h:24-38): 0.5 * |e1 x e2|.
+// ExtractIndexFromAabb as k_extract_indices does, and each leaf reference's
+// triangle area (the SAH lower creator's CalcArea).
 __global__ void k_areas(const BuildArgs a)
 {
     const BuildState *st = a.st;
     if (st->err) return;
     GRID_STRIDE(i, st->F) {
-        const int32_t prim = a.prim_indices[i];
+        const int32_t prim = __float_as_int(a.fmin[i].w);
+        a.prim_indices[i] = prim;
         const float4 q = __ldg(a.prec + 3 * (int64_t)prim), r = __ldg(a.prec + 3 * (int64_t)prim + 1),
                      w = __ldg(a.prec + 3 * (int64_t)prim + 2);
         // e1 = v1 - v0 and e2 = v2 - v0 as k_load_geometry rounded them.
@@ -1393,12 +1398,16 @@ __global__ void k_areas(const BuildArgs a)
 
 // PreprocesLowerNodes (LowerTriangleMap.h:56-81): node area and the bitmap of
 // references with non-zero area.
+// MarkLeafNodes as k_leaf_ids does, and each upper leaf's area sum and
+// bitmap of references with a nonzero area (PreprocessLeafNodes).
 __global__ void k_sah_preprocess(const BuildArgs a)
 {
     const BuildState *st = a.st;
     if (st->err) return;
+    const int32_t nr = st->n_ranges;
     GRID_STRIDE(k, st->n_leaf_ids) {
-        const int32_t leaf = a.leaf_ids[k];
+        const int32_t leaf = upper_leaf_id(a, nr, (int32_t)k);
+        a.leaf_ids[k] = leaf;
         const int32_t pi = a.pidx[leaf], n = a.amt[leaf];
         float s = 0.0f;
         unsigned bmp = 0;
@@ -2293,15 +2302,17 @@ int emit_upper_level(const BuildArgs &a, const Launcher &L, const Extents &e, bo
 int emit_after_upper(const BuildArgs &a, const Launcher &L, const Extents &e, const kdgb_build_params &p,
                      cudaStream_t s)
 {
-    KDGB_KERNEL(k_leaf_ids, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
-    KDGB_KERNEL(k_extract_indices, L.grid(e.F, kBlock), kBlock, 0, s, a);
-    if (!p.split_empty_space && p.propagate_aabbs) {
-        KDGB_KERNEL(k_propagate_parent, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
-    }
+    const bool parent_boxes = !p.split_empty_space && p.propagate_aabbs;
     if (p.lower == KDGB_LOWER_SAH) {
+        // k_areas also extracts the triangle indices, k_sah_preprocess also
+        // writes the leaf ids.
         KDGB_KERNEL(k_areas, L.grid(e.F, kBlock), kBlock, 0, s, a);
         KDGB_KERNEL(k_sah_preprocess, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
+        if (parent_boxes) KDGB_KERNEL(k_propagate_parent, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
     } else {
+        KDGB_KERNEL(k_leaf_ids, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
+        KDGB_KERNEL(k_extract_indices, L.grid(e.F, kBlock), kBlock, 0, s, a);
+        if (parent_boxes) KDGB_KERNEL(k_propagate_parent, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
         // Every reference of an upper leaf (PreprocessLeafNodes,
         // LowerTriangleMap.h:40-53 and TriangleMapBitmapCreator.cu:32-49).
         KDGB_KERNEL(k_bitmap_leaves, L.grid(e.leaves, kBlock), kBlock, 0, s, a);
