@@ -77,6 +77,25 @@ def test_build_options_match_oracle(kdgb_lib, cuda, oracle, opts):
         assert_same_tree(tree.to_host(), ref)
 
 
+@pytest.mark.parametrize("min_leaf,ci", [(0, 1.5), (4, 1.5), (15, 1.5), (16, 4.0), (20, 8.0), (31, 1.5)])
+def test_sah_lower_work_lists_match_oracle(kdgb_lib, cuda, oracle, min_leaf, ci):
+    """The SAH lower levels evaluate the nodes with more than min_leaf members
+    from work lists, two nodes of at most 16 members per warp and larger ones
+    one per warp; min_leaf moves the split between the two kinds (0: every
+    node with a member, 16: no pairs at all, 31: nothing after the first
+    level).  Host-driven and graph rebuilds must give the oracle's tree."""
+    kw = dict(lower=1, traversal_cost=1.0, intersection_cost=ci, min_leaf=min_leaf)
+    tris = scenes.clustered(12000, seed=33)
+    ref = oracle.build(tris, **kw)
+    with kdgb_lib.KDTree.build(tris, **kw) as tree:
+        assert_same_tree(tree.to_host(), ref)
+        params = kdgb_lib.build_params(**kw)
+        with kdgb_lib.Graph(tree, tris, params=params, headroom=1.5) as g:
+            g.launch()
+            assert g.status() == 0
+            assert_same_tree(tree.to_host(), ref)
+
+
 TUNED = dict(mode=1, upper_levels=8, sah_bins=32, lower=1, traversal_cost=1.0, intersection_cost=1.5, min_leaf=8)
 
 
