@@ -2347,7 +2347,7 @@ unsigned calc_sah_grid(const Launcher &L, int64_t R)
     return std::min<unsigned>(L.grid(R, kBlock), (unsigned)(L.sms * per_sm));
 }
 
-int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, Workspace &w, cudaStream_t s)
+int emit_lower_level(const BuildArgs &a, const Launcher &L, const Extents &e, cudaStream_t s)
 {
     if (a.lower == KDGB_LOWER_BALANCED) KDGB_KERNEL(k_calc_balanced, L.grid(e.low_R * 32, kBlock), kBlock, 0, s, a);
     else KDGB_KERNEL(k_calc_sah, calc_sah_grid(L, e.low_R), kBlock, 0, s, a);
@@ -2656,7 +2656,7 @@ int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_para
             // other parity's work list; its own list is not touched.
             if (p.lower == KDGB_LOWER_SAH) KDGB_CHECK(ensure(w.lowlist[(st.low_levels + 1) & 1], 2 * R, s));
             const Extents e{0, 0, F, st.n_nodes, nl, R};
-            KDGB_CHECK(emit_lower_level(make_args(t, p, T, M, mesh_off_dev), L, e, w, s));
+            KDGB_CHECK(emit_lower_level(make_args(t, p, T, M, mesh_off_dev), L, e, s));
             KDGB_CHECK(fetch_state(t, st, s));
         }
     }
@@ -2815,7 +2815,7 @@ int capture_build(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_p
         KDGB_CHECK(capture_while(cs, body, [&](cudaGraphConditionalHandle h) {
             BuildArgs b = a;
             b.lower_cond = h;
-            return emit_lower_level(b, L, e, w, body);
+            return emit_lower_level(b, L, e, body);
         }));
     }
     c0 = kdgb_launch_count();
