@@ -964,7 +964,6 @@ __device__ __forceinline__ void child_keys_atomic(const BuildArgs &a, int32_t R,
 template <bool DIVIDE>
 __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_scatter(const BuildArgs a)
 {
-    __shared__ int32_t s_off[kWarps][2];
     __shared__ int s_owner[kWarps];
     __shared__ unsigned s_keys[kWarps][12];
     const BuildState *st = a.st;
@@ -980,22 +979,21 @@ __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_scatter(const BuildA
     const unsigned below = (1u << lane) - 1u;
     const int64_t ntiles = ceil_div(N, kTileRefs);
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        if (threadIdx.x == 0) {
-            int32_t ol = a.tileoff[2 * tile], orr = a.tileoff[2 * tile + 1];
-            for (int w = 0; w < kWarps; ++w) {
-                s_off[w][0] = ol;
-                s_off[w][1] = orr;
-                const int64_t ch = tile * kWarps + w;
-                if (ch * kChunk < N) {
-                    ol += a.chunksum[2 * ch];
-                    orr += a.chunksum[2 * ch + 1];
-                }
-            }
-        }
-        __syncthreads();
         const int64_t chunk = tile * kWarps + warp;
         const int64_t base = chunk * kChunk;
-        int32_t off_l = s_off[warp][0], off_r = s_off[warp][1];
+        // The warp's first ranks: its tile's offsets plus the chunk totals of
+        // the tile's earlier warps (lane w < warp loads warp w's), so no warp
+        // waits for another.
+        int32_t off_l = 0, off_r = 0;
+        {
+            const int64_t ch = tile * kWarps + lane;
+            if (lane < warp && ch * kChunk < N) {
+                off_l = a.chunksum[2 * ch];
+                off_r = a.chunksum[2 * ch + 1];
+            }
+            off_l = __reduce_add_sync(kFull, off_l) + a.tileoff[2 * tile];
+            off_r = __reduce_add_sync(kFull, off_r) + a.tileoff[2 * tile + 1];
+        }
         int run = -1;  // parent whose whole rows this warp is accumulating
         unsigned al[6], ar[6];
         keys_neutral(al);
@@ -1107,7 +1105,7 @@ __global__ void __launch_bounds__(kBlock, DIVIDE ? 2 : 4) k_scatter(const BuildA
             }
             if (o >= 0) child_keys_atomic(a, R, o, kl, kr);
         }
-        __syncthreads();  // s_off, s_owner and s_keys are rewritten by the next tile
+        __syncthreads();  // s_owner and s_keys are rewritten by the next tile
     }
 }
 
