@@ -81,6 +81,9 @@ def parse():
                     help="one build and two traces, nothing timed (for ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--partition", type=int, default=0,
+                    help="e2e with frames in flight: rebuilds on an SM partition of at least this many SMs, traces on "
+                         "the rest (0: the whole device for both)")
     ap.add_argument("--no-batched", action="store_true", help="leave the batched record out of the frame line")
     ap.add_argument("--no-others", action="store_true",
                     help="leave the small, photon and adjoint records out of the frame line")
@@ -349,7 +352,7 @@ FRAMES_IN_FLIGHT = 3
 
 
 def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d, stream,
-                         n_slots=FRAMES_IN_FLIGHT):
+                         n_slots=FRAMES_IN_FLIGHT, partition_sms=0):
     """End to end with n_slots frames in flight: as many tree handles (each
     with its own rebuild graph and its own input and output buffers) take the
     frames in turn.  Frame k is uploaded and rebuilt on slot k's own
@@ -362,20 +365,27 @@ def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs,
     milliseconds per frame and the host copies of the last frames' outputs."""
     import torch
     import kdgb
-    slots = [dict(tree=tree, graph=graph, tris=tris_d, o=o_d, d=d_d, outs=outs)]
-    for _ in range(n_slots - 1):
+    high = torch.cuda.Stream.priority_range()[1]
+    part = kdgb.SmPartition(partition_sms) if partition_sms > 0 else None
+    slots = [] if part else [dict(tree=tree, graph=graph, tris=tris_d, o=o_d, d=d_d, outs=outs)]
+    while len(slots) < n_slots:
         t_ = tris_d.clone()
         tr = kdgb.KDTree.build(t_, bp)
-        slots.append(dict(tree=tr, graph=kdgb.Graph(tr, t_, params=bp, headroom=HEADROOM), tris=t_,
-                          o=o_d.clone(), d=d_d.clone(), outs=tuple(torch.empty_like(x) for x in outs), own=True))
-    high = torch.cuda.Stream.priority_range()[1]
+        # With an SM partition each slot's rebuild graph is captured on a
+        # stream of the rebuild partition, so its kernels keep to those SMs.
+        sb = part.stream(0, priority=high) if part else torch.cuda.Stream(device=dev, priority=high)
+        torch.cuda.synchronize()
+        slots.append(dict(tree=tr, graph=kdgb.Graph(tr, t_, params=bp, headroom=HEADROOM, stream=sb), tris=t_,
+                          o=o_d.clone(), d=d_d.clone(), outs=tuple(torch.empty_like(x) for x in outs), own=True,
+                          build_stream=sb))
     for sl in slots:
         sl["h_out"] = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in sl["outs"]]
-        sl["build_stream"] = torch.cuda.Stream(device=dev, priority=high)
+        if "build_stream" not in sl:
+            sl["build_stream"] = torch.cuda.Stream(device=dev, priority=high)
         for name in ("built", "traced", "read"):
             sl[name] = torch.cuda.Event()
             sl[name].record(stream)
-    st = torch.cuda.Stream(device=dev)
+    st = part.stream(1) if part else torch.cuda.Stream(device=dev)
     up, back = torch.cuda.Stream(device=dev, priority=high), torch.cuda.Stream(device=dev)
     last_in = torch.cuda.Event()
 
@@ -431,6 +441,9 @@ def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs,
         if sl.get("own"):
             sl["graph"].close()
             sl["tree"].close()
+    if part:
+        torch.cuda.synchronize()
+        part.close()
     return ms, h_outs
 
 
@@ -620,7 +633,7 @@ def run_frame(args, world, rank, local, pg):
         d2h = sum(x.numel() * x.element_size() for x in outs)
         if graph is not None:
             inflight = e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d,
-                                            stream)
+                                            stream, partition_sms=args.partition)
         one = {"value": rays_per_step * world / (e2e_ms / 1e3) / 1e6, "ms_per_step": e2e_ms,
                # The host copy of the last step must equal the device-timed
                # step's outputs (same inputs, same tree).

@@ -875,6 +875,9 @@ int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris, c
     if (!g) return fail(KDGB_ERR_OUT_OF_MEMORY, "host allocation");
     g->tree = tree;
     int rc = KDGB_OK;
+    // Captured in the context of the caller's stream: for a stream of an SM
+    // partition the graph's kernels run on that partition's SMs.
+    const StreamContext in_ctx(s);
     cudaError_t e = cudaStreamCreateWithFlags(&g->cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->body, cudaStreamNonBlocking);
     if (e != cudaSuccess) rc = cuda_fail(e, "graph streams");

@@ -2110,6 +2110,9 @@ struct Extents {
 
 int sm_count()
 {
+    // The current context's SMs: a graph captured for an SM partition sizes
+    // its grids for that partition.
+    if (const int c = context_sm_count(); c > 0) return c;
     int dev = 0, n = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {

@@ -17,6 +17,23 @@ void set_error(const std::string &msg);
 int fail(int status, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 
+// SMs of the context current on this thread (a green context's share of the
+// device for a stream of an SM partition), or 0 when the driver cannot say.
+int context_sm_count();
+
+// Makes the context of stream s current for the lifetime of the object when
+// another one is current (a stream of an SM partition), so that the streams
+// created and the work captured meanwhile belong to that context.
+struct StreamContext {
+    explicit StreamContext(cudaStream_t s);
+    ~StreamContext();
+    StreamContext(const StreamContext &) = delete;
+    StreamContext &operator=(const StreamContext &) = delete;
+
+private:
+    bool pushed_ = false;
+};
+
 #define KDGB_CUDA(call)                                        \
     do {                                                       \
         cudaError_t e_ = (call);                               \

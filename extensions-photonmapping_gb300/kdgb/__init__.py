@@ -27,7 +27,7 @@ from ._lib import (BUILD_REFERENCE, BUILD_TUNED, ISECT_MOELLER, ISECT_WOOP, SCHE
                    AutotuneResult, BuildParams, BuildStats, KdgbError, Light, light, PhotonParams, TraceParams, TreeView, build_params, check,
                    lib, library_path, photon_params, trace_params)
 
-__all__ = ["KDTree", "Graph", "autotune", "AutotuneResult", "Light", "light", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
+__all__ = ["KDTree", "Graph", "SmPartition", "autotune", "AutotuneResult", "Light", "light", "TriangleMap", "RayTracer", "ShortStack", "BruteTracer", "trace_brute", "build_params",
            "trace_params", "photon_params", "PhotonParams", "scenes", "KdgbError", "LEAF", "X", "Y", "Z", "LOWER_BITMAP", "LOWER_SAH",
            "LOWER_BALANCED", "SPLIT_BOX", "SPLIT_DIVIDE", "SPLIT_SPLIT",
            "BUILD_REFERENCE", "BUILD_TUNED", "TRACER_RESTART", "TRACER_SHORTSTACK", "TRACER_BRUTE",
@@ -381,6 +381,52 @@ class Graph:
         if getattr(self, "_g", None):
             lib().kdgb_graph_destroy(self._g)
             self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class SmPartition:
+    """The device's SMs in two partitions (kdgb_sm_partition_create): the
+    first with at least `sms` SMs, the second with the rest.  stream(which)
+    gives a torch stream whose kernels run on that partition only; a Graph
+    created with such a stream keeps its rebuild there wherever it is
+    launched.  Close the partition after the graphs captured on its streams."""
+
+    def __init__(self, sms: int):
+        p = C.c_void_p()
+        check(lib().kdgb_sm_partition_create(int(sms), C.byref(p)), "kdgb_sm_partition_create")
+        self._p = p
+        self._streams = []
+
+    def sms(self, which: int) -> int:
+        n = C.c_int32()
+        check(lib().kdgb_sm_partition_sms(self._p, int(which), C.byref(n)), "kdgb_sm_partition_sms")
+        return n.value
+
+    def stream(self, which: int, priority: int = 0):
+        torch = _torch()
+        s = C.c_void_p()
+        check(lib().kdgb_sm_partition_stream(self._p, int(which), int(priority), C.byref(s)),
+              "kdgb_sm_partition_stream")
+        st = torch.cuda.ExternalStream(s.value)
+        self._streams.append(st)
+        return st
+
+    def close(self) -> None:
+        if getattr(self, "_p", None):
+            self._streams = []
+            lib().kdgb_sm_partition_destroy(self._p)
+            self._p = None
 
     def __del__(self):
         try:

@@ -110,6 +110,10 @@ SIGNATURES = {
                                 C.POINTER(TraceParams), C.c_float, C.c_int32, C.POINTER(AutotuneResult), P]),
     "kdgb_graph_status": (C.c_int, [P, P]),
     "kdgb_graph_destroy": (C.c_int, [P]),
+    "kdgb_sm_partition_create": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p)]),
+    "kdgb_sm_partition_sms": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int32)]),
+    "kdgb_sm_partition_stream": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "kdgb_sm_partition_destroy": (C.c_int, [P]),
     "kdgb_geometry_gather": (C.c_int, [P, C.c_int32, P, C.c_int32, P, P, P]),
     "kdgb_geometry_gather_attributes": (C.c_int, [P, P, C.c_int32, P, C.c_int32, P, P, P, P, P, P]),
     "kdgb_light_default": (None, [C.POINTER(Light)]),

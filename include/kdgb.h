@@ -40,7 +40,7 @@ typedef struct CUstream_st *kdgb_stream_t; /* same type as cudaStream_t */
 #define KDGB_API
 #endif
 
-#define KDGB_ABI_VERSION 4
+#define KDGB_ABI_VERSION 5
 
 /* Utils/CUDA/Utils.h:18: the reference's "infinity" is the integer
  * 0x7f800000 converted to float. */
@@ -368,7 +368,10 @@ KDGB_API int kdgb_trace_batch(const kdgb_tree *tree, const kdgb_trace_params *pa
  *    (kdgb_tree_stats, kdgb_tree_view_get are stale until then).
  *  - A host-driven rebuild that reallocates any of the tree's buffers
  *    invalidates the graph: kdgb_graph_launch then returns
- *    KDGB_ERR_INVALID_ARGUMENT.  Destroy graphs before their tree. */
+ *    KDGB_ERR_INVALID_ARGUMENT.  Destroy graphs before their tree.
+ *  - The graph is captured in the context of `stream`: with a stream of an
+ *    SM partition (kdgb_sm_partition_stream) its kernels run on that
+ *    partition's SMs, on whatever stream the graph is launched. */
 typedef struct kdgb_graph kdgb_graph;
 
 KDGB_API int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris,
@@ -380,6 +383,27 @@ KDGB_API int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t 
 KDGB_API int kdgb_graph_launch(kdgb_graph *graph, kdgb_stream_t stream);
 KDGB_API int kdgb_graph_status(kdgb_graph *graph, kdgb_stream_t stream);
 KDGB_API int kdgb_graph_destroy(kdgb_graph *graph);
+
+/* SM partitions (no reference counterpart): the current device's SMs split
+ * into two green contexts, the first with at least `sms` SMs (rounded up to
+ * the device's granularity) and the second with the rest, for pipelined
+ * frames: the rebuilds of the frames in flight on one partition and their
+ * traces on the other, instead of taking the whole device from each other
+ * kernel by kernel.  kdgb_sm_partition_stream makes a non-blocking stream
+ * (priority as cudaStreamCreateWithPriority) whose kernels run on partition
+ * `which` (0 or 1) only; memory, events and copies work with it as with any
+ * stream of the device.  A graph created with such a stream keeps to its
+ * partition (kdgb_graph_create).  The partition owns its streams:
+ * kdgb_sm_partition_destroy synchronises and destroys them, after the
+ * graphs captured on them are destroyed.  KDGB_ERR_UNSUPPORTED when the
+ * driver has no green contexts. */
+typedef struct kdgb_sm_partition kdgb_sm_partition;
+
+KDGB_API int kdgb_sm_partition_create(int32_t sms, kdgb_sm_partition **out);
+KDGB_API int kdgb_sm_partition_sms(const kdgb_sm_partition *part, int32_t which, int32_t *sms);
+KDGB_API int kdgb_sm_partition_stream(kdgb_sm_partition *part, int32_t which, int32_t priority,
+                                      kdgb_stream_t *out);
+KDGB_API int kdgb_sm_partition_destroy(kdgb_sm_partition *part);
 
 /* Autotuner (no reference counterpart).  Picks leaf_size (16/24/32),
  * sah_bins (8/16/32, tuned mode only), stack_depth (2/4/8, short-stack
