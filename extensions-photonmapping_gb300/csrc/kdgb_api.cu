@@ -256,6 +256,7 @@ using namespace kdgb;
 struct kdgb_graph {
     kdgb_tree *tree = nullptr;
     cudaStream_t cs = nullptr, body = nullptr;
+    Fork fork;  // the side branch of the captured build
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     uint64_t signature = 0;
@@ -880,6 +881,8 @@ int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris, c
     const StreamContext in_ctx(s);
     cudaError_t e = cudaStreamCreateWithFlags(&g->cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->body, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->fork.aux, cudaStreamNonBlocking);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&g->fork.ev[i], cudaEventDisableTiming);
     if (e != cudaSuccess) rc = cuda_fail(e, "graph streams");
     if (rc == KDGB_OK) {
         e = cudaStreamBeginCapture(g->cs, cudaStreamCaptureModeRelaxed);
@@ -887,7 +890,7 @@ int kdgb_graph_create(kdgb_tree *tree, const float *tri_v_dev, int32_t n_tris, c
     }
     const int64_t launches0 = kdgb_launch_count();
     if (rc == KDGB_OK) {
-        rc = capture_build(t, tri_v_dev, n_tris, p, g->cs, g->body, n_meshes > 1 ? t.mesh_off.p : nullptr,
+        rc = capture_build(t, tri_v_dev, n_tris, p, g->cs, g->body, g->fork, n_meshes > 1 ? t.mesh_off.p : nullptr,
                            n_meshes, g->kernels);
         const int64_t before_trace = kdgb_launch_count();
         if (rc == KDGB_OK && n_rays > 0)
@@ -943,6 +946,9 @@ int kdgb_graph_destroy(kdgb_graph *graph)
     if (graph->graph) cudaGraphDestroy(graph->graph);
     if (graph->body) cudaStreamDestroy(graph->body);
     if (graph->cs) cudaStreamDestroy(graph->cs);
+    if (graph->fork.aux) cudaStreamDestroy(graph->fork.aux);
+    for (cudaEvent_t ev : graph->fork.ev)
+        if (ev) cudaEventDestroy(ev);
     delete graph;
     return KDGB_OK;
 }

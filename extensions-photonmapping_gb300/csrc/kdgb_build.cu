@@ -187,7 +187,7 @@ __device__ __forceinline__ int mesh_of(const int32_t *__restrict__ off, int M, i
 }
 
 __global__ void k_load_geometry(const float *__restrict__ tri, int32_t T, float4 *__restrict__ p0,
-                                float4 *__restrict__ p1, float4 *__restrict__ p2, float4 *__restrict__ prec,
+                                float4 *__restrict__ p1, float4 *__restrict__ p2,
                                 float4 *__restrict__ cmin, float4 *__restrict__ cmax,
                                 int *__restrict__ err, const int32_t *__restrict__ mesh_off, int M)
 {
@@ -204,14 +204,6 @@ __global__ void k_load_geometry(const float *__restrict__ tri, int32_t T, float4
         p0[i] = make_float4(v[0], v[1], v[2], 1.0f);
         p1[i] = make_float4(v[3], v[4], v[5], 1.0f);
         p2[i] = make_float4(v[6], v[7], v[8], 1.0f);
-        {
-            const float3 v0 = make_float3(v[0], v[1], v[2]);
-            const float3 e1 = sub3(make_float3(v[3], v[4], v[5]), v0);
-            const float3 e2 = sub3(make_float3(v[6], v[7], v[8]), v0);
-            prec[3 * (int64_t)i + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
-            prec[3 * (int64_t)i + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
-            prec[3 * (int64_t)i + 2] = make_float4(e2.z, __int_as_float(i), 0.0f, 0.0f);
-        }
         if (cmin) {
             float mnx = kmin(v[0], v[3]), mny = kmin(v[1], v[4]), mnz = kmin(v[2], v[5]);
             float mxx = kmax(v[0], v[3]), mxy = kmax(v[1], v[4]), mxz = kmax(v[2], v[5]);
@@ -221,6 +213,24 @@ __global__ void k_load_geometry(const float *__restrict__ tri, int32_t T, float4
             const int owner = M > 1 ? mesh_of(mesh_off, M, i) : 0;
             cmax[i] = make_float4(kmax(mxx, v[6]), kmax(mxy, v[7]), kmax(mxz, v[8]), __int_as_float(owner));
         }
+    }
+}
+
+// The packed triangle records {v0.xyz, e1.x} {e1.yz, e2.xy} {e2.z, id, 0, 0}
+// (e1 = v1 - v0, e2 = v2 - v0, rounded as the tracers compute them), read by
+// the SAH areas and copied into the leaf records; nothing on the upper levels
+// reads them, so a captured build makes them beside the level chain.
+__global__ void k_load_prec(const float *__restrict__ tri, int32_t T, float4 *__restrict__ prec)
+{
+    GRID_STRIDE(ii, T) {
+        const int32_t i = (int32_t)ii;
+        const float *tp = tri + 9 * (int64_t)i;
+        const float3 v0 = make_float3(tp[0], tp[1], tp[2]);
+        const float3 e1 = sub3(make_float3(tp[3], tp[4], tp[5]), v0);
+        const float3 e2 = sub3(make_float3(tp[6], tp[7], tp[8]), v0);
+        prec[3 * (int64_t)i + 0] = make_float4(v0.x, v0.y, v0.z, e1.x);
+        prec[3 * (int64_t)i + 1] = make_float4(e1.y, e1.z, e2.x, e2.y);
+        prec[3 * (int64_t)i + 2] = make_float4(e2.z, __int_as_float(i), 0.0f, 0.0f);
     }
 }
 
@@ -2260,11 +2270,36 @@ BuildArgs make_args(Tree &t, const kdgb_build_params &p, int32_t T, int32_t M, c
 }
 
 // Launch sequences shared by the host-driven and the graph build.
-int emit_begin(const BuildArgs &a, const Launcher &L, const float *tri_v_dev, cudaStream_t s)
+// Launches the packed triangle records on fork.aux (joined later with
+// fork_join) when there is a side stream, else on s.
+int emit_prec(const BuildArgs &a, const Launcher &L, const float *tri_v_dev, cudaStream_t s, const Fork *fork)
+{
+    if (a.T <= 0) return KDGB_OK;
+    cudaStream_t ps = s;
+    if (fork && fork->aux) {
+        KDGB_CUDA(cudaEventRecord(fork->ev[0], s));
+        KDGB_CUDA(cudaStreamWaitEvent(fork->aux, fork->ev[0], 0));
+        ps = fork->aux;
+    }
+    KDGB_KERNEL(k_load_prec, L.grid(a.T, kBlock), kBlock, 0, ps, tri_v_dev, a.T, a.prec);
+    if (ps != s) KDGB_CUDA(cudaEventRecord(fork->ev[1], ps));
+    return KDGB_OK;
+}
+
+// s waits for the side branch (nothing to do without one).
+int fork_join(cudaStream_t s, const Fork *fork)
+{
+    if (fork && fork->aux) KDGB_CUDA(cudaStreamWaitEvent(s, fork->ev[1], 0));
+    return KDGB_OK;
+}
+
+int emit_begin(const BuildArgs &a, const Launcher &L, const float *tri_v_dev, cudaStream_t s,
+               const Fork *fork = nullptr)
 {
     KDGB_KERNEL(k_begin, L.grid(a.M, kBlock), kBlock, 0, s, a);
+    KDGB_CHECK(emit_prec(a, L, tri_v_dev, s, fork));
     if (a.T > 0) {
-        KDGB_KERNEL(k_load_geometry, L.grid(a.T, kBlock), kBlock, 0, s, tri_v_dev, a.T, a.p0, a.p1, a.p2, a.prec, a.rmin[0],
+        KDGB_KERNEL(k_load_geometry, L.grid(a.T, kBlock), kBlock, 0, s, tri_v_dev, a.T, a.p0, a.p1, a.p2, a.rmin[0],
                                                                a.rmax[0], &a.st->nonfinite, a.mesh_off, a.M);
         // The roots' tight boxes; later levels get theirs from k_scatter.
         KDGB_KERNEL(k_reduce, L.grid(a.T, kTileRefs), kBlock, 0, s, a);
@@ -2368,17 +2403,26 @@ int emit_pack_counts(const BuildArgs &a, const Launcher &L, const Extents &e, Wo
     return KDGB_OK;
 }
 
-int emit_pack(const BuildArgs &a, const Launcher &L, const Extents &e, cudaStream_t s)
+int emit_pack(const BuildArgs &a, const Launcher &L, const Extents &e, cudaStream_t s, const Fork *fork = nullptr)
 {
     const unsigned g = L.grid(e.nodes, kBlock);
+    // The leaf records need only the scanned leaf counts: on a side stream
+    // they are copied while the nodes are packed.
+    cudaStream_t ts = s;
+    if (fork && fork->aux) {
+        KDGB_CUDA(cudaEventRecord(fork->ev[0], s));
+        KDGB_CUDA(cudaStreamWaitEvent(fork->aux, fork->ev[0], 0));
+        ts = fork->aux;
+    }
+    KDGB_KERNEL(k_pack_tris, L.grid(e.nodes, kBlock), kBlock, 0, ts, 0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info,
+                                                                  a.amt, a.pidx,
+                                     a.prim_indices, a.prec, a.loff, a.ttri);
+    if (ts != s) KDGB_CUDA(cudaEventRecord(fork->ev[1], ts));
     KDGB_CUDA(cudaMemsetAsync(a.norder, 0xff, sizeof(int32_t) * (size_t)std::max<int64_t>(e.nodes, 1), s));
     KDGB_KERNEL(k_pack_order, g, kBlock, 0, s, 0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.M, a.info, a.ch, a.loff, a.norder);
     KDGB_KERNEL(k_pack_nodes, g, kBlock, 0, s, 0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.M, a.info, a.split, a.bmin, a.bmax,
                                       a.loff, a.norder, a.tnode, a.tbox);
-    KDGB_KERNEL(k_pack_tris, L.grid(e.nodes, kBlock), kBlock, 0, s, 0, &a.st->n_nodes, &a.st->err, a.cap.tris, a.info,
-                                                                 a.amt, a.pidx,
-                                     a.prim_indices, a.prec, a.loff, a.ttri);
-    return KDGB_OK;
+    return fork_join(s, fork);
 }
 
 const char *detail_message(int d)
@@ -2502,8 +2546,9 @@ int load_geometry(Tree &t, const float *tri_v_dev, int32_t T, cudaStream_t s)
     KDGB_CHECK(grab(w.stats, 16, s));
     KDGB_CUDA(cudaMemsetAsync(w.stats.p, 0, sizeof(int), s));
     const Launcher L{sm_count()};
-    KDGB_KERNEL(k_load_geometry, L.grid(T, kBlock), kBlock, 0, s, tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, t.prec.p, nullptr,
+    KDGB_KERNEL(k_load_geometry, L.grid(T, kBlock), kBlock, 0, s, tri_v_dev, T, t.p0.p, t.p1.p, t.p2.p, nullptr,
              nullptr, w.stats.p, nullptr, 1);
+    KDGB_KERNEL(k_load_prec, L.grid(T, kBlock), kBlock, 0, s, tri_v_dev, T, t.prec.p);
     KDGB_CUDA(cudaMemcpyAsync(w.host, w.stats.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     KDGB_CUDA(cudaStreamSynchronize(s));
     if (w.host[0]) return fail(KDGB_ERR_NONFINITE, "non-finite vertex coordinate");
@@ -2793,7 +2838,7 @@ int capture_while(cudaStream_t cs, cudaStream_t body, Emit emit)
 }  // namespace
 
 int capture_build(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p, cudaStream_t cs,
-                  cudaStream_t body, const int32_t *mesh_off_dev, int32_t M, GraphKernels &counts)
+                  cudaStream_t body, const Fork &fork, const int32_t *mesh_off_dev, int32_t M, GraphKernels &counts)
 {
     if (M < 1) M = 1;
     Workspace &w = t.ws;
@@ -2802,7 +2847,7 @@ int capture_build(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_p
     Extents e;
     graph_args(t, p, T, M, mesh_off_dev, a, e);
     int64_t c0 = kdgb_launch_count();
-    KDGB_CHECK(emit_begin(a, L, tri_v_dev, cs));
+    KDGB_CHECK(emit_begin(a, L, tri_v_dev, cs, &fork));
     int64_t c1 = kdgb_launch_count();
     counts.fixed = c1 - c0;
     KDGB_CHECK(capture_while(cs, body, [&](cudaGraphConditionalHandle h) {
@@ -2812,6 +2857,7 @@ int capture_build(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_p
     }));
     c0 = kdgb_launch_count();
     counts.upper_body = c0 - c1;
+    KDGB_CHECK(fork_join(cs, &fork));  // the packed triangle records are complete
     KDGB_CHECK(emit_after_upper(a, L, e, p, cs));
     c1 = kdgb_launch_count();
     counts.fixed += c1 - c0;
@@ -2825,7 +2871,7 @@ int capture_build(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_p
     c0 = kdgb_launch_count();
     counts.lower_body = c0 - c1;
     KDGB_CHECK(emit_pack_counts(a, L, e, w, cs));
-    KDGB_CHECK(emit_pack(a, L, e, cs));
+    KDGB_CHECK(emit_pack(a, L, e, cs, &fork));
     counts.fixed += kdgb_launch_count() - c0;
     return KDGB_OK;
 }

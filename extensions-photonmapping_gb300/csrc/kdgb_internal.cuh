@@ -218,11 +218,19 @@ inline bool lower_loop(const kdgb_build_params &p)
 int build_tree(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p, cudaStream_t s,
                const int32_t *mesh_off_dev = nullptr, int32_t M = 1);
 
+// A side branch of a captured build: work that does not lie on the level
+// chain runs on `aux` beside it (fork on ev[0], join on ev[1]).
+struct Fork {
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
 // The same build recorded into the graph being captured on `cs`: fixed
 // buffers sized from t.plan x headroom, level loops as WHILE nodes, no host
-// synchronisation.  `body` is a second stream used to capture loop bodies.
+// synchronisation.  `body` is a second stream used to capture loop bodies;
+// the packed triangle records and the leaf records are made on fork.aux.
 int capture_build(Tree &t, const float *tri_v_dev, int32_t T, const kdgb_build_params &p, cudaStream_t cs,
-                  cudaStream_t body, const int32_t *mesh_off_dev, int32_t M, GraphKernels &counts);
+                  cudaStream_t body, const Fork &fork, const int32_t *mesh_off_dev, int32_t M, GraphKernels &counts);
 
 // Allocates every buffer capture_build uses, before capture starts.
 int reserve_for_graph(Tree &t, int32_t T, const kdgb_build_params &p, int32_t M, double headroom, cudaStream_t s);
