@@ -22,7 +22,7 @@ torchrun each rank runs an independent replica (weak scaling).
 End to end (`e2e`): the same frames through the library's public calls with
 host buffers: every frame uploads its triangles and rays from pinned host
 memory, rebuilds its tree by one graph launch, traces and reads all its
-outputs back.  Three frames are in flight: three tree handles take the frames
+outputs back.  Four frames are in flight: four tree handles take the frames
 in turn, each rebuilt on its own stream, so the rebuilds of consecutive
 frames overlap each other and the traces of earlier frames.  The
 one-frame-in-flight figure is reported beside it.
@@ -348,7 +348,7 @@ def time_steps(step, steps, stream, flush=None):
     return out
 
 
-FRAMES_IN_FLIGHT = 3
+FRAMES_IN_FLIGHT = 4
 
 
 def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d, stream,
