@@ -736,8 +736,11 @@ struct PhotonArgs {
     const int32_t *build_err;  // as TraceArgs::build_err
 };
 
+// Capped at 40 registers like k_trace: 12 blocks of 128 per SM instead of 9
+// (16M photons on the 262k-triangle scene: short-stack 7.54 -> 7.11 ms,
+// kd-restart 11.17 -> 9.17 ms; 48 registers: 7.32 / 9.78 ms).
 template <int TRACER, bool SKIP>
-__global__ void k_photons(PhotonArgs a)
+__global__ void __maxnreg__(40) k_photons(PhotonArgs a)
 {
     extern __shared__ int2 stack_smem[];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
