@@ -39,6 +39,10 @@ itself does not compile here.
            64k rays per mesh: one graph (forest build + trace) vs per-mesh
            loops, parameters from the autotuner
   adjoint  100k-triangle height field (316x158), 512x512 rays: backward pass
+  next     the rows after the hot path: a moving 1M-triangle surface updated,
+           collected (vertices, normals, colours), rebuilt and shaded with
+           reflections at 1920x1080; Woop's test against Moeller-Trumbore and
+           the balanced lower creator and DIVIDE split method on the frame scene
 """
 from __future__ import annotations
 
@@ -70,7 +74,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="frame", choices=["frame", "small", "photons", "batched", "adjoint"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "small", "photons", "batched", "adjoint", "next"])
     ap.add_argument("--tris", type=int, default=configs.FRAME_TRIS)
     ap.add_argument("--width", type=int, default=configs.WIDTH)
     ap.add_argument("--height", type=int, default=configs.HEIGHT)
@@ -688,13 +692,15 @@ def run_frame(args, world, rank, local, pg):
         batched = measure_batched(args, steps=max(3, args.steps // 4), host_loop_steps=1)
 
     # The other configurations, each a compact copy of its own workload's
-    # line (4096-triangle height field, photons, adjoint).
+    # line (4096-triangle height field, photons, adjoint, the rows after the
+    # hot path).
     others = None
     if rank == 0 and world == 1 and not args.no_others and graph is not None:
         keep = {"metric", "value", "unit", "ms_per_step", "higher_is_better", "config"}
         common = set(line_common(args, "", 0, "", True, 0, "", {}))
         others = {}
-        for name, fn in (("small", measure_small), ("photons", measure_photons), ("adjoint", measure_adjoint)):
+        for name, fn in (("small", measure_small), ("photons", measure_photons), ("adjoint", measure_adjoint),
+                         ("next", measure_next)):
             others[name] = {k: v for k, v in fn(args).items() if k in keep or k not in common}
 
     if rank == 0:
@@ -1016,6 +1022,199 @@ def run_adjoint(args):
     print(json.dumps(measure_adjoint(args)), flush=True)
 
 
+# The rows after the hot path, on frame-sized inputs: a moving surface
+# collected and shaded each frame (GeometryList::AddMesh,
+# OscCUDAMeshNode::UpdateSurface, the tracers' shading loop), Woop's test, and
+# the balanced lower creator and DIVIDE split method of the build.
+OSC_DETAIL = 724         # (724+1)^2 vertices, 1,048,352 triangles
+OSC_HEIGHT = 0.0
+OSC_TIME = 0.75
+
+
+def osc_surface(detail=OSC_DETAIL):
+    """The oscillating surface's grid (OscCUDAMeshNode.cu:27-67): vertices
+    i * 0.1, height, j * 0.1, normals, colours and its index buffer."""
+    from kdgb import scenes
+    d = detail + 1
+    i, j = np.meshgrid(np.arange(d), np.arange(d), indexing="xy")
+    verts = np.stack([i.ravel() * 0.1, np.full(d * d, OSC_HEIGHT), j.ravel() * 0.1, np.ones(d * d)],
+                     1).astype(np.float32)
+    idx = scenes.grid_indices(detail, detail).astype(np.int32)
+    normals = np.zeros_like(verts)
+    normals[:, 1] = 1.0
+    g = np.arange(d * d, dtype=np.int64) % 251
+    cols = np.stack([g, 255 - g, (g * 3) % 256, np.where(g % 3 == 0, 128, 255)], 1).astype(np.uint8)
+    return verts, normals, cols, idx
+
+
+def measure_next(args):
+    """The rows after the hot path.  A dynamic frame: the surface is moved
+    (kdgb_osc_update_surface), collected into triangles and per-triangle
+    attributes (kdgb_geometry_gather, kdgb_geometry_gather_attributes; a model
+    matrix fits it into the unit cube), rebuilt by one graph launch (tuned
+    build) and shaded (kdgb_trace_shaded, short-stack, 1920x1080, reflections
+    until alpha 0.97).  On the 1M-triangle frame scene: primary rays with Woop's
+    test against Moeller-Trumbore, and the balanced lower creator and the
+    DIVIDE split method as graph rebuilds.  Parity: pixels, hit ids and trees
+    against the oracle.  Returns the workload's line."""
+    import ctypes as C
+    import torch
+    import kdgb
+    from kdgb import scenes
+    W = max(args.warmup, 3)
+    stream = torch.cuda.current_stream()
+    L = kdgb.lib()
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    sp = lambda: C.c_void_p(stream.cuda_stream)
+    verts, normals, cols, idx = osc_surface()
+    T = idx.shape[0] // 3
+    vd, nd = torch.from_numpy(verts).cuda(), torch.from_numpy(normals).cuda()
+    cd, idd = torch.from_numpy(cols).cuda(), torch.from_numpy(idx).cuda()
+    s = 1.0 / (0.1 * OSC_DETAIL)
+    model = np.array([s, 0, 0, 0, 0, 1, 0, 0.3, 0, 0, s, 0, 0, 0, 0, 1], np.float32)
+    tris = torch.empty((T, 9), dtype=torch.float32, device="cuda")
+    n0, n1, n2 = (torch.empty((T, 4), dtype=torch.float32, device="cuda") for _ in range(3))
+    c0 = torch.empty((T, 4), dtype=torch.uint8, device="cuda")
+    o, d = scenes.camera_rays(configs.WIDTH, configs.HEIGHT)
+    od, dd = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    n = o.shape[0]
+    clock = [0.0]
+
+    def update():
+        clock[0] += 1.0 / 60.0
+        kdgb.check(L.kdgb_osc_update_surface(ptr(vd), ptr(nd), OSC_DETAIL, OSC_HEIGHT, OSC_TIME + clock[0], sp()),
+                   "kdgb_osc_update_surface")
+
+    def gather():
+        kdgb.check(L.kdgb_geometry_gather(ptr(vd), vd.shape[0], ptr(idd), idd.shape[0],
+                                          model.ctypes.data_as(C.c_void_p), ptr(tris), sp()),
+                   "kdgb_geometry_gather")
+        kdgb.check(L.kdgb_geometry_gather_attributes(ptr(nd), ptr(cd), vd.shape[0], ptr(idd), idd.shape[0], None,
+                                                     ptr(n0), ptr(n1), ptr(n2), ptr(c0), sp()),
+                   "kdgb_geometry_gather_attributes")
+
+    update()
+    gather()
+    bp = kdgb.build_params(**configs.TUNED)
+    tree = kdgb.KDTree.build(tris, bp)
+    graph = kdgb.Graph(tree, tris, params=bp, headroom=HEADROOM)
+    tp = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH, tile_width=configs.WIDTH)
+    rgba = torch.empty((n, 4), dtype=torch.uint8, device="cuda")
+    shade = lambda: tree.trace_shaded(od, dd, n0, n1, n2, c0, tp, out=rgba)
+    stages = (("update", update), ("gather", gather), ("rebuild", graph.launch), ("shade", shade))
+
+    def frame():
+        for _, fn in stages:
+            fn()
+
+    time_steps(frame, W, stream)
+    frame_ms = statistics.median(time_steps(frame, args.steps, stream))
+    stage_ms = {}
+    for name, fn in stages:
+        stage_ms[name] = statistics.median(time_steps(fn, args.steps, stream))
+    kdgb.check(graph.status(), "graph rebuild")
+    frame_ms_final = frame_ms
+    # Parity of the last frame: the oracle builds the same triangles and
+    # shades every 97th ray with the same attributes.
+    update()
+    gather()
+    graph.launch()
+    shade()
+    torch.cuda.synchronize()
+    kdgb.check(graph.status(), "graph rebuild")
+    parity = cpu = None
+    if not args.no_cpu_baseline:
+        O = oracle_module()
+        ht, h0, h1, h2, hc = (x.cpu().numpy() for x in (tris, n0, n1, n2, c0))
+        t0 = time.perf_counter()
+        ot = O.build(ht, **configs.TUNED)
+        tb = time.perf_counter() - t0
+        sel = np.arange(0, n, 97)
+        t0 = time.perf_counter()
+        want = O.trace_shaded(ot, ht, o[sel], d[sel], h0, h1, h2, hc, tracer=O.TRACER_SHORTSTACK,
+                              stack_depth=configs.STACK_DEPTH)
+        ts = (time.perf_counter() - t0) * n / sel.size
+        got = rgba.cpu().numpy()[sel]
+        parity = {"against": "oracle, same triangles, attributes and tracer (CPU)", "pixels_checked": int(sel.size),
+                  "pixels_equal": bool(np.array_equal(got, want)),
+                  "lit_pixels": int((want[:, 3] > 0).sum())}
+        cpu = {"value": n / (tb + ts) / 1e6, "unit": "Mrays/s (primary rays shaded)", "cores": os.cpu_count(),
+               "kind": "port", "sample": "oracle build of the frame's triangles + shaded trace of every 97th ray, "
+                                         "extrapolated to the frame", "build_ms": tb * 1e3}
+    graph.close()
+    tree.close()
+
+    # Woop's test against Moeller-Trumbore, and the other build options, on
+    # the frame scene.
+    ftris, fo, fd = configs.frame_scene()
+    ftd, fod, fdd = (torch.from_numpy(x).cuda() for x in (ftris, fo, fd))
+    fn_ = fo.shape[0]
+    extra = {}
+    with kdgb.KDTree.build(ftd, bp) as ft:
+        out = tuple(torch.empty(fn_, dtype=dt, device="cuda") for dt in (torch.int32, torch.float32, torch.float32,
+                                                                          torch.float32))
+        res = {}
+        for name, isect in (("moeller_trumbore", kdgb.ISECT_MOELLER), ("woop", kdgb.ISECT_WOOP)):
+            ptp = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH,
+                                    tile_width=configs.WIDTH, intersection=isect)
+            fn = lambda ptp=ptp: ft.trace(fod, fdd, ptp, out=out)
+            time_steps(fn, W, stream)
+            res[name] = statistics.median(time_steps(fn, args.steps, stream))
+        woop_hits = out[0].cpu().numpy()
+        woop = {"trace_ms": res, "mrays_s": {k: fn_ / (v / 1e3) / 1e6 for k, v in res.items()},
+                "note": "primary rays of the frame; Woop's rows are recomputed from the geometry at the first "
+                        "trace after each rebuild"}
+        if not args.no_cpu_baseline:
+            O = oracle_module()
+            oft = O.build(ftris, **configs.TUNED)
+            sel = np.arange(0, fn_, 61)
+            wh = O.trace(oft, ftris, fo[sel], fd[sel], tracer=O.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH,
+                         intersection=O.ISECT_WOOP)[0]
+            woop["parity"] = {"rays_checked": int(sel.size), "hit_ids_equal": bool(np.array_equal(wh, woop_hits[sel]))}
+        extra["woop"] = woop
+    builds = {}
+    for name, kw in (("balanced", dict(configs.TUNED, lower=kdgb.LOWER_BALANCED, traversal_cost=16.0)),
+                     ("divide", dict(configs.TUNED, split_method=kdgb.SPLIT_DIVIDE))):
+        bp2 = kdgb.build_params(**kw)
+        with kdgb.KDTree.build(ftd, bp2) as bt:
+            g2 = kdgb.Graph(bt, ftd, params=bp2, headroom=HEADROOM)
+            time_steps(g2.launch, W, stream)
+            b_ms = statistics.median(time_steps(g2.launch, args.steps, stream))
+            kdgb.check(g2.status(), "graph rebuild")
+            ptp = kdgb.trace_params(tracer=kdgb.TRACER_SHORTSTACK, stack_depth=configs.STACK_DEPTH,
+                                    tile_width=configs.WIDTH)
+            fn = lambda: bt.trace(fod, fdd, ptp)
+            time_steps(fn, W, stream)
+            t_ms = statistics.median(time_steps(fn, args.steps, stream))
+            st = bt.stats()
+            rec = {"build": kw, "rebuild_ms_graph": b_ms, "primary_trace_ms": t_ms,
+                   "tree": {"nodes": st.n_nodes, "refs": st.n_refs}}
+            if not args.no_cpu_baseline:
+                O = oracle_module()
+                ref = O.build(ftris, **kw)
+                h = bt.to_host()
+                rec["parity"] = {"tree_arrays_equal": all(
+                    np.array_equal(getattr(h, f).view(np.uint32) if getattr(h, f).dtype.kind == "f" else getattr(h, f),
+                                   getattr(ref, f).view(np.uint32) if getattr(ref, f).dtype.kind == "f"
+                                   else getattr(ref, f))
+                    for f in ("info", "split", "children", "bitmap", "prim_indices", "leaf_ids", "aabb_min",
+                              "aabb_max", "area"))}
+            g2.close()
+        builds[name] = rec
+    extra["builds"] = builds
+    line = line_common(
+        args, "dynamic surface frame Mrays/s (surface update + collection + graph rebuild + shaded trace)",
+        n / (frame_ms_final / 1e3) / 1e6, "Mrays/s", True, frame_ms_final,
+        "oscillating surface %d^2 cells (%d tris), 1920x1080 shaded, short-stack depth 8; frame scene for Woop and "
+        "the build options" % (OSC_DETAIL, T),
+        {"stage_ms": stage_ms, "parity": parity, "cpu_baseline": cpu, **extra})
+    return line
+
+
+def run_next(args):
+    print(json.dumps(measure_next(args)), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local, pg = dist_setup(args)
@@ -1027,7 +1226,8 @@ def main():
     elif rank == 0:
         import torch
         torch.cuda.set_device(local)
-        {"small": run_small, "photons": run_photons, "batched": run_batched, "adjoint": run_adjoint}[args.workload](args)
+        {"small": run_small, "photons": run_photons, "batched": run_batched, "adjoint": run_adjoint,
+         "next": run_next}[args.workload](args)
     if pg:
         pg.destroy_process_group()
 

@@ -914,8 +914,10 @@ __device__ __forceinline__ int brute_hit(const ShadeArgs &a, float3 o, float3 d,
     return hit;
 }
 
+// Capped at 48 registers (53 uncapped): 1920x1080 shaded rays on the moving
+// 1M-triangle surface 14.49 -> 13.93 ms (40 registers: 14.03 ms).
 template <int TRACER, bool SKIP>
-__global__ void k_shade(ShadeArgs a)
+__global__ void __maxnreg__(48) k_shade(ShadeArgs a)
 {
     extern __shared__ int2 stack_smem[];
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
