@@ -106,19 +106,23 @@ __device__ __forceinline__ void mt_record(const float4 *__restrict__ tri, int32_
             o, d, tie, hit, tb, ub, vb);
 }
 
-// RayBoxIntersection<true> (IRayTracer.h:147-168).
+// RayBoxIntersection<true> (IRayTracer.h:147-168), with the reference's
+// min / max (fminf / fmaxf, one instruction each).  The values of n and f
+// reach nothing but the comparison n <= f, which does not see the sign of a
+// zero, so the order the tracers' other minima give -0 and +0 is not needed
+// here.
 __device__ __forceinline__ bool ray_box(float3 o, float3 inv, float4 bmin, float4 bmax)
 {
     const float lx = __fmul_rn(__fsub_rn(bmin.x, o.x), inv.x), ly = __fmul_rn(__fsub_rn(bmin.y, o.y), inv.y),
                 lz = __fmul_rn(__fsub_rn(bmin.z, o.z), inv.z);
     const float hx = __fmul_rn(__fsub_rn(bmax.x, o.x), inv.x), hy = __fmul_rn(__fsub_rn(bmax.y, o.y), inv.y),
                 hz = __fmul_rn(__fsub_rn(bmax.z, o.z), inv.z);
-    float n = kmin(lx, hx);
-    n = kmax(n, kmin(ly, hy));
-    n = kmax(n, kmin(lz, hz));
-    float f = kmax(hx, lx);
-    f = kmin(f, kmax(ly, hy));
-    f = kmin(f, kmax(lz, hz));
+    float n = fminf(lx, hx);
+    n = fmaxf(n, fminf(ly, hy));
+    n = fmaxf(n, fminf(lz, hz));
+    float f = fmaxf(hx, lx);
+    f = fminf(f, fmaxf(ly, hy));
+    f = fminf(f, fmaxf(lz, hz));
     return n <= f;
 }
 
@@ -258,7 +262,9 @@ __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 i
         const float ori = axis_of(o, ax), dir = axis_of(inv, ax);
         const float ts = __fmul_rn(__fsub_rn(node_split(nd), ori), dir);
         if (tmin < ts) {
-            tnext = kmin(ts, tnext);
+            // tnext reaches only comparisons and tmin, whose zero sign no
+            // result sees: the reference's fminf is exact here.
+            tnext = fminf(ts, tnext);
             if (m) m->push(node, tnext);
             node = 0 < dir ? left : left + 1;
         } else {
@@ -330,29 +336,22 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
     return -1;
 }
 
-// Short-stack, first hit (ShortStack.cu:58-194).  The stack of this thread
-// lives in shared memory at st[i * stride]; entries are (node, tMax bits).
-// The direction is inverted in place before each descent and inverted back
-// after it (ShortStack.cu:134,148), exactly as the reference does.
-template <bool SKIP>
-__device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int depth, int maxit, int2 *st,
-                                int stride, float &t, float &u, float &v, float3 *dused = nullptr)
+// Short-stack loop (ShortStack.cu:58-194).  The stack of this thread lives
+// in shared memory at st[i * stride]; entries are (node, tMax bits).  The
+// reference inverts the direction in place before each descent and back
+// after it (ShortStack.cu:134,148): with FIXED false, d is that direction
+// and inv is unused.  With FIXED true that sequence is at its fixed point
+// (see trace_shortstack): every descent and slab test uses inv and every
+// triangle test d, neither changing, so the loop holds three registers and
+// no selects fewer.
+template <bool SKIP, bool FIXED>
+__device__ __forceinline__ int shortstack_loop(const Ctx &c, float3 o, float3 d, float3 inv, int tie, int depth,
+                                               int maxit, int2 *st, int stride, float &t, float &u, float &v,
+                                               float3 *dused)
 {
     int nxt = 0, cnt = 0;
-    float3 d = adjust_dir(din);
     float th = 0.0f;
     int iters = 0;
-    // The reference inverts d before each descent and back after it, so d
-    // becomes rcp(rcp(d)) after the first iteration.  When
-    // rcp(rcp(rcp(d))) == rcp(d) the sequence is at its fixed point from
-    // then on: every descent and slab test uses inv1 = rcp(d) and every
-    // triangle test d1 = rcp(inv1).  That holds for all finite nonzero
-    // floats except six values next to FLT_MAX (checked exhaustively); it is
-    // tested per ray, and rays that miss it take the reference's loop.
-    const float3 inv1 = inv3(d), d1 = inv3(inv1), inv2 = inv3(d1);
-    const bool fixed = __float_as_uint(inv2.x) == __float_as_uint(inv1.x) &&
-                       __float_as_uint(inv2.y) == __float_as_uint(inv1.y) &&
-                       __float_as_uint(inv2.z) == __float_as_uint(inv1.z);
     do {
         int node;
         float tnext;
@@ -367,10 +366,11 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
             tnext = __int_as_float(e.y);
         }
         int2 nd = __ldg(c.node + node);
-        d = fixed ? inv1 : inv3(d);
+        if (!FIXED) d = inv3(d);
+        const float3 dn = FIXED ? inv : d;  // the inverse direction of this descent
         while (node_axis(nd) != KDGB_LEAF) {
             const int ax = node_axis(nd), left = node_left(nd);
-            const float ori = axis_of(o, ax), dir = axis_of(d, ax);
+            const float ori = axis_of(o, ax), dir = axis_of(dn, ax);
             const float ts = __fmul_rn(__fsub_rn(node_split(nd), ori), dir);
             const int lower = 0 < dir ? left : left + 1;
             const int upper = 0 < dir ? left + 1 : left;
@@ -381,15 +381,15 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
                     nxt = nxt == depth - 1 ? 0 : nxt + 1;
                     cnt = cnt == depth ? depth : cnt + 1;
                 }
-                tnext = kmin(ts, tnext);
+                tnext = fminf(ts, tnext);  // as in restart_descend
             } else {
                 node = upper;
             }
             nd = __ldg(c.node + node);
         }
-        d = fixed ? d1 : inv3(d);
+        if (!FIXED) d = inv3(d);
         th = __fmul_rn(tnext, 1.00001f);
-        if (!SKIP || ray_box(o, fixed ? inv1 : inv3(d), leaf_min(c, node), leaf_max(c, node))) {
+        if (!SKIP || ray_box(o, FIXED ? inv : inv3(d), leaf_min(c, node), leaf_max(c, node))) {
             float tb = th, ub = 0.0f, vb = 0.0f;
             const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
             if (h != -1) {
@@ -401,6 +401,26 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
         if (++iters >= maxit) break;
     } while (th < KDGB_FINF);
     return -1;
+}
+
+// Short-stack, first hit (ShortStack.cu:58-194).  The reference inverts d
+// before each descent and back after it, so d becomes rcp(rcp(d)) after the
+// first iteration.  When rcp(rcp(rcp(d))) == rcp(d) the sequence is at its
+// fixed point from then on: every descent and slab test uses inv1 = rcp(d)
+// and every triangle test d1 = rcp(inv1).  That holds for all finite nonzero
+// floats except six values next to FLT_MAX (checked exhaustively); it is
+// tested per ray, and rays that miss it take the reference's loop.
+template <bool SKIP>
+__device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int depth, int maxit, int2 *st,
+                                int stride, float &t, float &u, float &v, float3 *dused = nullptr)
+{
+    const float3 d = adjust_dir(din);
+    const float3 inv1 = inv3(d), d1 = inv3(inv1), inv2 = inv3(d1);
+    const bool fixed = __float_as_uint(inv2.x) == __float_as_uint(inv1.x) &&
+                       __float_as_uint(inv2.y) == __float_as_uint(inv1.y) &&
+                       __float_as_uint(inv2.z) == __float_as_uint(inv1.z);
+    if (fixed) return shortstack_loop<SKIP, true>(c, o, d1, inv1, tie, depth, maxit, st, stride, t, u, v, dused);
+    return shortstack_loop<SKIP, false>(c, o, d, d, tie, depth, maxit, st, stride, t, u, v, dused);
 }
 
 // ShadowRay (Raytracer.cu:108-163): from the light toward the point, the
