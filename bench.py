@@ -353,6 +353,8 @@ def time_steps(step, steps, stream, flush=None):
 
 
 FRAMES_IN_FLIGHT = 4
+# Streams of the batched record's concurrent per-mesh comparator.
+CONCURRENT_STREAMS = 16
 
 
 def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d, stream,
@@ -871,8 +873,10 @@ def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
       * one graph: forest build of all meshes + batched trace (one launch);
       * per-mesh graph loop: one graph per mesh (its rebuild + its rays),
         launched one after another on one stream, no host synchronisation;
+      * the same per-mesh graphs over CONCURRENT_STREAMS streams, largest
+        meshes first (independent meshes overlap);
       * per-mesh host loop: host-driven rebuild + trace per mesh.
-    Returns the record; the hits of the three must be identical, and a few
+    Returns the record; the hits of all four must be identical, and a few
     meshes are checked against the oracle."""
     import torch
     import kdgb
@@ -925,6 +929,31 @@ def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
     for g in mgraphs:
         kdgb.check(g.status(), "per-mesh graph rebuild")
     same_graph_loop = all(np.array_equal(louts[m][0].cpu().numpy(), ghit[m * R:(m + 1) * R]) for m in range(M))
+
+    # The same per-mesh graphs spread over concurrent streams (largest meshes
+    # first), so independent meshes overlap as independent work items would.
+    streams = [torch.cuda.Stream() for _ in range(CONCURRENT_STREAMS)]
+    by_size = np.argsort([-mt.shape[0] for mt in meshes], kind="stable")
+
+    def streams_loop():
+        start = torch.cuda.Event()
+        start.record(stream)
+        for s in streams:
+            s.wait_event(start)
+        for j, m in enumerate(by_size):
+            mgraphs[m].launch(stream=streams[j % len(streams)])
+        for s in streams:
+            done = torch.cuda.Event()
+            done.record(s)
+            stream.wait_event(done)
+
+    for g in louts:
+        g[0].fill_(-2)
+    time_steps(streams_loop, 2, stream)
+    gs_ms = time_steps(streams_loop, steps, stream)
+    for g in mgraphs:
+        kdgb.check(g.status(), "per-mesh graph rebuild")
+    same_streams = all(np.array_equal(louts[m][0].cpu().numpy(), ghit[m * R:(m + 1) * R]) for m in range(M))
     for g in mgraphs:
         g.close()
 
@@ -950,13 +979,17 @@ def measure_batched(args, steps, host_loop_steps=2, check_meshes=8):
         oracle_ok &= bool(np.array_equal(hr, ghit[m * R:(m + 1) * R]))
 
     g, gl, hl = statistics.median(g_ms), statistics.median(gl_ms), statistics.median(hl_ms)
+    gs = statistics.median(gs_ms)
     rec = {"workload": "%d clustered meshes log-uniform [1k,200k] tris (%d total), 64k random rays each"
                        % (M, tris.shape[0]),
            "meshes": M, "tris": int(tris.shape[0]), "rays": M * R, "one_graph_ms": g, "meshes_per_s": M / (g / 1e3),
            "rays_mrays_s": M * R / (g / 1e3) / 1e6, "hits": hits,
            "per_mesh_graph_loop_ms": gl, "per_mesh_host_loop_ms": hl,
            "speedup_vs_per_mesh_graph_loop": gl / g, "speedup_vs_per_mesh_host_loop": hl / g,
+           "per_mesh_graphs_concurrent_ms": gs, "concurrent_streams": CONCURRENT_STREAMS,
+           "speedup_vs_per_mesh_graphs_concurrent": gs / g,
            "parity": {"graph_loop_hits_identical": bool(same_graph_loop),
+                      "concurrent_graphs_hits_identical": bool(same_streams),
                       "host_loop_hits_identical": bool(same_host_loop),
                       "oracle_meshes_checked": int(check_meshes), "oracle_hit_ids_equal": bool(oracle_ok)},
            "trace_only_ms": sched_ms,
