@@ -207,14 +207,14 @@ __device__ __forceinline__ bool leaf_any(const Ctx &c, int2 leaf, float3 o, floa
 // near ones whose split distance exceeds tmin' stay near) down to the
 // topmost near decision whose split distance is <= tmin', and turns to the
 // far child there.  Keeping the near decisions of the current descent that
-// lower the prefix minimum of the split distances from the root, as (node,
-// that minimum), lets the descent resume at that node with the previous
-// entry's minimum as tnext: the leaves visited and their tnext values are
-// exactly those of the full restart.  The deepest `cap` (a power of two)
-// such decisions are kept (a
-// ring in shared memory, entry slot s at e[s * stride]); when the turning
-// node lies above them (`base`, the minimum over the dropped ones, is <=
-// tmin') the descent starts again from the root.
+// lower the prefix minimum of the split distances from the root, as (far
+// child, that minimum), lets the descent resume at that child with the
+// previous entry's minimum as tnext: the leaves visited and their tnext
+// values are exactly those of the full restart.  The deepest `cap` (a power
+// of two) such decisions are kept (a ring in shared memory, entry slot s at
+// e[s * stride]); when the turning node lies above them (`base`, the minimum
+// over the dropped ones, is <= tmin') the descent starts again from the root.
+//
 // Capacity where the shared region is sized for it.  With only the lowering
 // decisions kept, 8 entries leave almost no restart from the root, and the
 // halved region leaves more of the SM to L1 (16 -> 8 entries: kd-restart
@@ -233,14 +233,14 @@ struct Memo {
         base = KDGB_FINF;
     }
     __device__ __forceinline__ int2 &at(int i) const { return e[((head + i) & (cap - 1)) * stride]; }
-    __device__ __forceinline__ void push(int node, float pm)
+    __device__ __forceinline__ void push(int far, float pm)
     {
         if (cnt == cap) {  // drop the shallowest; it is the deepest dropped so far
             base = __int_as_float(at(0).y);
             head = (head + 1) & (cap - 1);
             --cnt;
         }
-        at(cnt) = make_int2(node, __float_as_int(pm));
+        at(cnt) = make_int2(far, __float_as_int(pm));
         ++cnt;
     }
 };
@@ -274,8 +274,9 @@ __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 i
             // ts >= tnext lies one with a distance <= ts, so such a decision
             // is never the turning node.  Its entry would only take a ring
             // slot (frame shadow rays: 17 pushes instead of 40, and almost no
-            // restarts from the root).
-            if (m && ts < tnext) m->push(node, ts);
+            // restarts from the root).  The entry names the far child, where a
+            // restart that turns here continues.
+            if (m && ts < tnext) m->push(0 < dir ? left + 1 : left, ts);
             // tnext reaches only comparisons and tmin, whose zero sign no
             // result sees: the reference's fminf is exact here.
             tnext = fminf(ts, tnext);
@@ -291,7 +292,7 @@ __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 i
 // remembered near decision whose distance is <= tmin (prefix minima fall
 // with depth, so it is the first entry whose minimum is <= tmin), or the
 // root.
-__device__ __forceinline__ void restart_from(const Ctx &c, float3 inv, float tmin, int &node, int2 &nd, float &tnext,
+__device__ __forceinline__ void restart_from(const Ctx &c, float tmin, int &node, int2 &nd, float &tnext,
                                              Memo *m)
 {
     if (m && m->cnt > 0 && tmin < m->base) {
@@ -303,8 +304,7 @@ __device__ __forceinline__ void restart_from(const Ctx &c, float3 inv, float tmi
         const int2 e = m->at(lo);
         tnext = lo > 0 ? __int_as_float(m->at(lo - 1).y) : m->base;
         m->cnt = lo;
-        nd = __ldg(c.node + e.x);
-        node = node_left(nd) + (0 < axis_of(inv, node_axis(nd)) ? 1 : 0);
+        node = e.x;  // the far child: one node load instead of two dependent ones
         nd = __ldg(c.node + node);
         return;
     }
@@ -344,7 +344,7 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
         }
         if (++iters >= maxit) break;
         if (!(tmin < KDGB_FINF)) break;
-        restart_from(c, inv, tmin, node, nd, tnext, m);
+        restart_from(c, tmin, node, nd, tnext, m);
     } while (true);
     return -1;
 }
@@ -462,7 +462,7 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 
         if (tmin >= 0.999f) return 0;
         if (leaf_any(c, nd, lp, d, tmin)) return 1;
         if (++iters >= maxit) break;
-        restart_from(c, inv, tmin, node, nd, tnext, m);
+        restart_from(c, tmin, node, nd, tnext, m);
     } while (true);
     return 0;
 }
