@@ -296,13 +296,22 @@ __device__ __forceinline__ void restart_from(const Ctx &c, float tmin, int &node
                                              Memo *m)
 {
     if (m && m->cnt > 0 && tmin < m->base) {
-        int lo = 0, hi = m->cnt - 1;  // the deepest entry's minimum is the last tnext <= tmin
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (__int_as_float(m->at(mid).y) <= tmin) hi = mid; else lo = mid + 1;
+        // Usually the deepest entry: its minimum is the leaf's tnext, and the
+        // one above it lies beyond tmin.  Otherwise the first entry whose
+        // minimum is <= tmin, by binary search over the ones above.
+        int lo = m->cnt - 1;
+        float above = lo > 0 ? __int_as_float(m->at(lo - 1).y) : m->base;
+        if (!(tmin < above)) {
+            int hi = lo - 1;  // the entry at hi already qualifies
+            lo = 0;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (__int_as_float(m->at(mid).y) <= tmin) hi = mid; else lo = mid + 1;
+            }
+            above = lo > 0 ? __int_as_float(m->at(lo - 1).y) : m->base;
         }
         const int2 e = m->at(lo);
-        tnext = lo > 0 ? __int_as_float(m->at(lo - 1).y) : m->base;
+        tnext = above;
         m->cnt = lo;
         node = e.x;  // the far child: one node load instead of two dependent ones
         nd = __ldg(c.node + node);
