@@ -122,6 +122,25 @@ def test_fused_primary_shadow(kdgb_lib, cuda, oracle, clustered, tracer, block_s
         assert np.array_equal(np_(occ), occ_ref)
 
 
+@pytest.mark.parametrize("depth", [1, 2, 3])
+def test_fused_shadow_small_memo(kdgb_lib, cuda, oracle, clustered, depth):
+    """The fused launch's shadow rays remember their descents in the primary
+    ray's stack region: 1 or 2 entries at these depths, so the ring drops
+    entries and restarts from the root on most rays (with 8 entries it hardly
+    ever does on this scene)."""
+    tris, tree, o, d = clustered
+    light = (0.5, 3.0, 0.5)
+    ref = oracle.trace(tree, tris, o, d, tracer=1, stack_depth=depth)
+    pts = scenes.hit_points(o, d, ref[1], ref[0])
+    occ_ref = oracle.trace_shadow(tree, tris, pts, light)
+    occ_ref[ref[0] < 0] = 0
+    with kdgb_lib.KDTree.upload(tree, tris) as gt:
+        h, t, u, v, occ = gt.trace_primary_shadow(o, d, light, tracer=1, stack_depth=depth)
+        assert_hits_equal((h, t, u, v), ref)
+        assert np.array_equal(np_(occ), occ_ref)
+    assert occ_ref.sum() > 100
+
+
 def test_edge_case_rays(kdgb_lib, cuda, oracle):
     tris = scenes.heightfield(16, 16, seed=2)[0]
     tree = oracle.build(tris)
