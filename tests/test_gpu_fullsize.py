@@ -4,7 +4,7 @@
   exactly as bench.py runs it (both the frame's tuned build and the
   reference creators), every tree array against the oracle, and the fused
   short-stack primary + shadow trace over the full 1920x1080 frame (4x8
-  pixel packets, depth 8) bit for bit;
+  pixel packets, depth 8) and kd-restart over the same frame, bit for bit;
 * photons: the 262,144-triangle scene with a 1M-photon sample of the 16M
   photon stream, both kd tracers;
 * batched: 64 meshes drawn from the log-uniform 1k..200k mix, one forest
@@ -59,6 +59,9 @@ def test_frame_build_and_trace_match_oracle(kdgb_lib, cuda, oracle, frame, build
         assert g.status() == 0
         assert_same_tree(tree.to_host(), ref_tree)
         h, t, u, v, occ = (np_(x) for x in tree.trace_primary_shadow(o, d, configs.LIGHT, tp))
+        # kd-restart over the same frame: its descents run deep enough here
+        # to overflow the 8-entry ring of remembered descents.
+        restart = [np_(x) for x in tree.trace(o, d, tracer=kdgb_lib.TRACER_RESTART, tile_width=configs.WIDTH)]
         g.close()
     hr, tr, ur, vr = oracle.trace(ref_tree, tris, o, d, tracer=1, stack_depth=configs.STACK_DEPTH)
     assert np.array_equal(h, hr), f"{(h != hr).sum()} of {h.size} hit ids differ"
@@ -72,6 +75,11 @@ def test_frame_build_and_trace_match_oracle(kdgb_lib, cuda, oracle, frame, build
     assert np.array_equal(occ[m], occ_ref), f"{(occ[m] != occ_ref).sum()} shadow rays differ"
     assert (occ[~m] == 0).all()
     assert 0 < occ_ref.sum() < occ_ref.size
+    hk, tk, uk, vk = oracle.trace(ref_tree, tris, o, d, tracer=0)
+    assert np.array_equal(restart[0], hk), f"{(restart[0] != hk).sum()} kd-restart hit ids differ"
+    mk = hk >= 0
+    for a, b in zip(restart[1:], (tk, uk, vk)):
+        assert np.array_equal(a[mk].view(np.uint32), b[mk].view(np.uint32))
 
 
 @pytest.mark.parametrize("tracer", [0, 1])
