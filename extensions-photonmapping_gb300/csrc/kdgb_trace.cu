@@ -58,12 +58,13 @@ __device__ __forceinline__ int32_t leaf_first(int2 nd) { return nd.x; }
 __device__ __forceinline__ int32_t leaf_count(int2 nd) { return nd.y >> 2; }
 
 // True when x = RN(RN(1/det) * n) is certainly negative and nonzero:
-// det and n have opposite signs, n != 0, and |det| <= 2^64, |n| >= 2^-64 so
-// the product cannot round to -0 (a -0 would pass the `>= 0` tests).
-// det = +-0 gives +-inf, whose product with n is negative as well.
+// det and n have opposite signs, and |det| <= 2^64, |n| >= 2^-64 (so n is
+// not zero, nor NaN) so the product cannot round to -0 (a -0 would pass the
+// `>= 0` tests).  det = +-0 gives +-inf, whose product with n is negative as
+// well.
 __device__ __forceinline__ bool surely_negative(float det, float n)
 {
-    return n != 0.0f && (signbit(det) != signbit(n)) && fabsf(det) <= 0x1p64f && fabsf(n) >= 0x1p-64f;
+    return (signbit(det) != signbit(n)) && fabsf(det) <= 0x1p64f && fabsf(n) >= 0x1p-64f;
 }
 
 // Moeller-Trumbore on one packed record (IRayTracer.h:111-145).  Triangles
