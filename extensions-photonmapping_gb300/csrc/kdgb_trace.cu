@@ -259,10 +259,10 @@ __host__ __device__ __forceinline__ int stack_entries(int tracer, int depth)
 }
 
 // Descends from `node` (record nd) to a leaf, as the reference's kd-restart
-// loop does (Raytracer.cu:73-86); near decisions are remembered in m when
-// given.
+// loop does (Raytracer.cu:73-86); the near decisions that lower tnext are
+// remembered in m.
 __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 inv, float tmin, int &node, int2 &nd,
-                                                float &tnext, Memo *m)
+                                                float &tnext, Memo &m)
 {
     while (node_axis(nd) != KDGB_LEAF) {
         const int ax = node_axis(nd), left = node_left(nd);
@@ -277,7 +277,7 @@ __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 i
             // slot (frame shadow rays: 17 pushes instead of 40, and almost no
             // restarts from the root).  The entry names the far child, where a
             // restart that turns here continues.
-            if (m && ts < tnext) m->push(0 < dir ? left + 1 : left, ts);
+            if (ts < tnext) m.push(0 < dir ? left + 1 : left, ts);
             // tnext reaches only comparisons and tmin, whose zero sign no
             // result sees: the reference's fminf is exact here.
             tnext = fminf(ts, tnext);
@@ -293,42 +293,41 @@ __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 i
 // remembered near decision whose distance is <= tmin (prefix minima fall
 // with depth, so it is the first entry whose minimum is <= tmin), or the
 // root.
-__device__ __forceinline__ void restart_from(const Ctx &c, float tmin, int &node, int2 &nd, float &tnext,
-                                             Memo *m)
+__device__ __forceinline__ void restart_from(const Ctx &c, float tmin, int &node, int2 &nd, float &tnext, Memo &m)
 {
-    if (m && m->cnt > 0 && tmin < m->base) {
+    if (m.cnt > 0 && tmin < m.base) {
         // Usually the deepest entry: its minimum is the leaf's tnext, and the
         // one above it lies beyond tmin.  Otherwise the first entry whose
         // minimum is <= tmin, by binary search over the ones above.
-        int lo = m->cnt - 1;
-        float above = lo > 0 ? __int_as_float(m->at(lo - 1).y) : m->base;
+        int lo = m.cnt - 1;
+        float above = lo > 0 ? __int_as_float(m.at(lo - 1).y) : m.base;
         if (!(tmin < above)) {
             int hi = lo - 1;  // the entry at hi already qualifies
             lo = 0;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (__int_as_float(m->at(mid).y) <= tmin) hi = mid; else lo = mid + 1;
+                if (__int_as_float(m.at(mid).y) <= tmin) hi = mid; else lo = mid + 1;
             }
-            above = lo > 0 ? __int_as_float(m->at(lo - 1).y) : m->base;
+            above = lo > 0 ? __int_as_float(m.at(lo - 1).y) : m.base;
         }
-        const int2 e = m->at(lo);
+        const int2 e = m.at(lo);
         tnext = above;
-        m->cnt = lo;
+        m.cnt = lo;
         node = e.x;  // the far child: one node load instead of two dependent ones
         nd = __ldg(c.node + node);
         return;
     }
-    if (m) m->reset();
+    m.reset();
     node = c.root;
     nd = __ldg(c.node + c.root);
     tnext = KDGB_FINF;
 }
 
-// kd-restart, first hit (Raytracer.cu:57-106, 165-262).
-// With memo storage (mem, stride, cap) the descents are remembered (see Memo).
+// kd-restart, first hit (Raytracer.cu:57-106, 165-262), with the descents
+// remembered in `cap` entries at mem[k * stride] (see Memo).
 template <bool SKIP>
 __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int maxit, float &t, float &u, float &v,
-                             float3 *dused = nullptr, int2 *mem = nullptr, int stride = 0, int cap = kMemo)
+                             float3 *dused, int2 *mem, int stride, int cap = kMemo)
 {
     const float3 d = adjust_dir(din);
     const float3 inv = inv3(d);
@@ -340,12 +339,11 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
     memo.stride = stride;
     memo.cap = cap;
     memo.reset();
-    Memo *m = mem ? &memo : nullptr;
     int node = c.root;
     int2 nd = __ldg(c.node + c.root);
     float tnext = KDGB_FINF;
     do {
-        restart_descend(c, o, inv, tmin, node, nd, tnext, m);
+        restart_descend(c, o, inv, tmin, node, nd, tnext, memo);
         tmin = __fmul_rn(tnext, 1.00001f);
         if (!SKIP || ray_box(o, inv, leaf_min(c, node), leaf_max(c, node))) {
             float tb = tmin, ub = 0.0f, vb = 0.0f;
@@ -354,7 +352,7 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
         }
         if (++iters >= maxit) break;
         if (!(tmin < KDGB_FINF)) break;
-        restart_from(c, tmin, node, nd, tnext, m);
+        restart_from(c, tmin, node, nd, tnext, memo);
     } while (true);
     return -1;
 }
@@ -449,9 +447,8 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
 // ShadowRay (Raytracer.cu:108-163): from the light toward the point, the
 // direction neither normalised nor clamped; leaves whose exit reaches 0.999
 // are not tested; any hit occludes.
-// With memo storage (mem, stride, cap) the descents are remembered (see Memo).
-__device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 *mem = nullptr, int stride = 0,
-                            int cap = kMemo)
+// The descents are remembered in `cap` entries at mem[k * stride] (see Memo).
+__device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 *mem, int stride, int cap = kMemo)
 {
     const float3 d = sub3(pt, lp);
     const float3 inv = inv3(d);
@@ -462,17 +459,16 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 
     memo.stride = stride;
     memo.cap = cap;
     memo.reset();
-    Memo *m = mem ? &memo : nullptr;
     int node = c.root;
     int2 nd = __ldg(c.node + c.root);
     float tnext = KDGB_FINF;
     do {
-        restart_descend(c, lp, inv, tmin, node, nd, tnext, m);
+        restart_descend(c, lp, inv, tmin, node, nd, tnext, memo);
         tmin = __fmul_rn(tnext, 1.00001f);
         if (tmin >= 0.999f) return 0;
         if (leaf_any(c, nd, lp, d, tmin)) return 1;
         if (++iters >= maxit) break;
-        restart_from(c, tmin, node, nd, tnext, m);
+        restart_from(c, tmin, node, nd, tnext, memo);
     } while (true);
     return 0;
 }
