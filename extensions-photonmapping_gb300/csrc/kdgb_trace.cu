@@ -165,11 +165,24 @@ __device__ __forceinline__ void woop_test(const float4 *__restrict__ w, int id, 
     if (0.0f <= lambda && lambda <= tb) woop_accept(lambda, __ldg(w), __ldg(w + 1), id, o, d, tie, hit, tb, ub, vb);
 }
 
+// The intersection test of a kernel: Moeller-Trumbore or Woop's test fixed
+// at compile time (the frame's trace kernels), or chosen per launch by
+// whether c.woop is set (kIsectAny).  A fixed choice takes the other test's
+// branch out of the leaf loops.
+constexpr int kIsectAny = 2;
+
+template <int IS = kIsectAny>
+__device__ __forceinline__ bool use_woop(const Ctx &c)
+{
+    return IS == KDGB_ISECT_WOOP || (IS == kIsectAny && c.woop != nullptr);
+}
+
+template <int IS = kIsectAny>
 __device__ __forceinline__ int leaf_test(const Ctx &c, int2 leaf, float3 o, float3 d, int tie, float &tb, float &ub,
                                          float &vb)
 {
     int hit = -1;
-    if (c.woop) {
+    if (use_woop<IS>(c)) {
         for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) {
             const int id = __float_as_int(__ldg(c.tri + 3 * (int64_t)r + 2).y);
             woop_test(c.woop + 3 * (int64_t)id, id, o, d, tie, hit, tb, ub, vb);
@@ -183,11 +196,12 @@ __device__ __forceinline__ int leaf_test(const Ctx &c, int2 leaf, float3 o, floa
 // Whether any triangle of the leaf is hit within [0, tb] (the reference's
 // shadow test, REF_LAST acceptance): the first accepted triangle settles it,
 // so the loop stops there with the result testing all of them gives.
+template <int IS = kIsectAny>
 __device__ __forceinline__ bool leaf_any(const Ctx &c, int2 leaf, float3 o, float3 d, float tb)
 {
     int hit = -1;
     float ub = 0.0f, vb = 0.0f;
-    if (c.woop) {
+    if (use_woop<IS>(c)) {
         for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) {
             const int id = __float_as_int(__ldg(c.tri + 3 * (int64_t)r + 2).y);
             woop_test(c.woop + 3 * (int64_t)id, id, o, d, KDGB_TIE_REF_LAST, hit, tb, ub, vb);
@@ -325,7 +339,7 @@ __device__ __forceinline__ void restart_from(const Ctx &c, float tmin, int &node
 
 // kd-restart, first hit (Raytracer.cu:57-106, 165-262), with the descents
 // remembered in `cap` entries at mem[k * stride] (see Memo).
-template <bool SKIP>
+template <bool SKIP, int IS = kIsectAny>
 __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int maxit, float &t, float &u, float &v,
                              float3 *dused, int2 *mem, int stride, int cap = kMemo)
 {
@@ -347,7 +361,7 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
         tmin = __fmul_rn(tnext, 1.00001f);
         if (!SKIP || ray_box(o, inv, leaf_min(c, node), leaf_max(c, node))) {
             float tb = tmin, ub = 0.0f, vb = 0.0f;
-            const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
+            const int h = leaf_test<IS>(c, nd, o, d, tie, tb, ub, vb);
             if (h != -1) { t = tb; u = ub; v = vb; return h; }
         }
         if (++iters >= maxit) break;
@@ -365,7 +379,7 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
 // (see trace_shortstack): every descent and slab test uses inv and every
 // triangle test d, neither changing, so the loop holds three registers and
 // no selects fewer.
-template <bool SKIP, bool FIXED>
+template <bool SKIP, bool FIXED, int IS>
 __device__ __forceinline__ int shortstack_loop(const Ctx &c, float3 o, float3 d, float3 inv, int tie, int depth,
                                                int maxit, int2 *st, int stride, float &t, float &u, float &v,
                                                float3 *dused)
@@ -412,7 +426,7 @@ __device__ __forceinline__ int shortstack_loop(const Ctx &c, float3 o, float3 d,
         th = __fmul_rn(tnext, 1.00001f);
         if (!SKIP || ray_box(o, FIXED ? inv : inv3(d), leaf_min(c, node), leaf_max(c, node))) {
             float tb = th, ub = 0.0f, vb = 0.0f;
-            const int h = leaf_test(c, nd, o, d, tie, tb, ub, vb);
+            const int h = leaf_test<IS>(c, nd, o, d, tie, tb, ub, vb);
             if (h != -1) {
                 t = tb; u = ub; v = vb;
                 if (dused) *dused = d;
@@ -431,7 +445,7 @@ __device__ __forceinline__ int shortstack_loop(const Ctx &c, float3 o, float3 d,
 // and every triangle test d1 = rcp(inv1).  That holds for all finite nonzero
 // floats except six values next to FLT_MAX (checked exhaustively); it is
 // tested per ray, and rays that miss it take the reference's loop.
-template <bool SKIP>
+template <bool SKIP, int IS = kIsectAny>
 __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int depth, int maxit, int2 *st,
                                 int stride, float &t, float &u, float &v, float3 *dused = nullptr)
 {
@@ -440,14 +454,15 @@ __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int
     const bool fixed = __float_as_uint(inv2.x) == __float_as_uint(inv1.x) &&
                        __float_as_uint(inv2.y) == __float_as_uint(inv1.y) &&
                        __float_as_uint(inv2.z) == __float_as_uint(inv1.z);
-    if (fixed) return shortstack_loop<SKIP, true>(c, o, d1, inv1, tie, depth, maxit, st, stride, t, u, v, dused);
-    return shortstack_loop<SKIP, false>(c, o, d, d, tie, depth, maxit, st, stride, t, u, v, dused);
+    if (fixed) return shortstack_loop<SKIP, true, IS>(c, o, d1, inv1, tie, depth, maxit, st, stride, t, u, v, dused);
+    return shortstack_loop<SKIP, false, IS>(c, o, d, d, tie, depth, maxit, st, stride, t, u, v, dused);
 }
 
 // ShadowRay (Raytracer.cu:108-163): from the light toward the point, the
 // direction neither normalised nor clamped; leaves whose exit reaches 0.999
 // are not tested; any hit occludes.
 // The descents are remembered in `cap` entries at mem[k * stride] (see Memo).
+template <int IS = kIsectAny>
 __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 *mem, int stride, int cap = kMemo)
 {
     const float3 d = sub3(pt, lp);
@@ -466,7 +481,7 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 
         restart_descend(c, lp, inv, tmin, node, nd, tnext, memo);
         tmin = __fmul_rn(tnext, 1.00001f);
         if (tmin >= 0.999f) return 0;
-        if (leaf_any(c, nd, lp, d, tmin)) return 1;
+        if (leaf_any<IS>(c, nd, lp, d, tmin)) return 1;
         if (++iters >= maxit) break;
         restart_from(c, tmin, node, nd, tnext, memo);
     } while (true);
@@ -533,7 +548,7 @@ __device__ __forceinline__ int ray_mesh_of(const TraceArgs &a, int64_t i)
 // a batch), written to the outputs; the thread's stack or memo region is
 // stk[k * stride].  Returns the hit id (relative to the whole tree) and the
 // ray and t for a shadow ray.
-template <int TRACER, bool SKIP>
+template <int TRACER, bool SKIP, int IS = kIsectAny>
 __device__ __forceinline__ int trace_ray(const TraceArgs &a, int64_t i, int2 *stk, int stride, float3 &o, float3 &d,
                                          float &t)
 {
@@ -548,9 +563,9 @@ __device__ __forceinline__ int trace_ray(const TraceArgs &a, int64_t i, int2 *st
     float u = 0.0f, v = 0.0f;
     int h;
     if (TRACER == KDGB_TRACER_SHORTSTACK)
-        h = trace_shortstack<SKIP>(c, o, d, a.tie, a.depth, a.maxit, stk, stride, t, u, v);
+        h = trace_shortstack<SKIP, IS>(c, o, d, a.tie, a.depth, a.maxit, stk, stride, t, u, v);
     else
-        h = trace_restart<SKIP>(c, o, d, a.tie, a.maxit, t, u, v, nullptr, stk, stride);
+        h = trace_restart<SKIP, IS>(c, o, d, a.tie, a.maxit, t, u, v, nullptr, stk, stride);
     if (h < 0) { t = INFINITY; u = 0.0f; v = 0.0f; }
     a.hit[i] = h >= 0 ? h - id_off : h;
     a.t[i] = t;
@@ -567,7 +582,7 @@ __device__ __forceinline__ int trace_ray(const TraceArgs &a, int64_t i, int2 *st
 // instead of 56%) gain more than the few spilled values cost (measured on
 // the 1M-triangle frame: 1.61 ms against 1.72 ms uncapped, 1.67 ms at 48
 // and 1.83 ms at 32 registers).
-template <int TRACER, bool SKIP, bool SHADOW>
+template <int TRACER, bool SKIP, bool SHADOW, int IS>
 __global__ void __maxnreg__(40) k_trace(TraceArgs a)
 {
     extern __shared__ __align__(16) unsigned char trace_smem[];
@@ -588,7 +603,7 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
     float3 o = make_float3(0.f, 0.f, 0.f), d = o;
     float t = 0.0f;
     int h = -1;
-    if (live) h = trace_ray<TRACER, SKIP>(a, i, stack_smem + threadIdx.x, blockDim.x, o, d, t);
+    if (live) h = trace_ray<TRACER, SKIP, IS>(a, i, stack_smem + threadIdx.x, blockDim.x, o, d, t);
     if (SHADOW) {
         // The block's shadow rays (one per primary hit) are packed onto its
         // first threads, so warps stay full while they are traced.
@@ -615,7 +630,7 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
             const int64_t ray = ray_index((int64_t)blockIdx.x * blockDim.x + __float_as_int(q.p.w), a.tile_width);
             Ctx cs = a.c;
             cs.root = ray_mesh_of(a, ray);
-            a.occ[ray] = trace_shadow(cs, a.light, make_float3(q.p.x, q.p.y, q.p.z), a.maxit,
+            a.occ[ray] = trace_shadow<IS>(cs, a.light, make_float3(q.p.x, q.p.y, q.p.z), a.maxit,
                                         stack_smem + threadIdx.x, blockDim.x,
                                         memo_cap(stack_entries(TRACER, a.depth)));
         }
@@ -687,6 +702,7 @@ __global__ void __maxnreg__(40) k_trace_queue(TraceArgs a, TraceQueue q)
     }
 }
 
+template <int IS>
 __global__ void k_shadow(TraceArgs a)
 {
     extern __shared__ int2 memo_smem[];
@@ -696,7 +712,7 @@ __global__ void k_shadow(TraceArgs a)
         a.occ[i] = 0;
         return;
     }
-    a.occ[i] = trace_shadow(a.c, a.light, ld3(a.o, i), a.maxit, memo_smem + threadIdx.x, blockDim.x);
+    a.occ[i] = trace_shadow<IS>(a.c, a.light, ld3(a.o, i), a.maxit, memo_smem + threadIdx.x, blockDim.x);
 }
 
 // Brute force (BruteTracer.cu:54-96): every ray tests every triangle in id
@@ -1103,6 +1119,27 @@ static int trace_queue_launch(const Tree &t, const kdgb_trace_params &p, const T
     return KDGB_OK;
 }
 
+// The k_trace instance of a launch: tracer, leaf skipping, fused shadow
+// rays and intersection test are template parameters.
+template <int TRACER, bool SKIP, bool SHADOW>
+static void (*trace_kernel_is(bool woop))(TraceArgs)
+{
+    return woop ? k_trace<TRACER, SKIP, SHADOW, KDGB_ISECT_WOOP> : k_trace<TRACER, SKIP, SHADOW, KDGB_ISECT_MOELLER>;
+}
+
+template <int TRACER>
+static void (*trace_kernel_tr(bool skip, bool shadow, bool woop))(TraceArgs)
+{
+    return skip ? (shadow ? trace_kernel_is<TRACER, true, true>(woop) : trace_kernel_is<TRACER, true, false>(woop))
+                : (shadow ? trace_kernel_is<TRACER, false, true>(woop) : trace_kernel_is<TRACER, false, false>(woop));
+}
+
+static void (*trace_kernel(bool shortstack, bool skip, bool shadow, bool woop))(TraceArgs)
+{
+    return shortstack ? trace_kernel_tr<KDGB_TRACER_SHORTSTACK>(skip, shadow, woop)
+                      : trace_kernel_tr<KDGB_TRACER_RESTART>(skip, shadow, woop);
+}
+
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
                  int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s,
                  const int32_t *ray_mesh, int32_t rays_per_mesh)
@@ -1138,15 +1175,7 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
     // With shadow rays the block's queue (one ShadowItem, two int2, per
     // thread) overlays the stack region.
     const size_t smem = sizeof(int2) * (size_t)std::max(stack_entries(p.tracer, p.stack_depth), shadow ? 2 : 0) * bs;
-    void (*kernel)(TraceArgs);
-    if (p.tracer == KDGB_TRACER_SHORTSTACK) {
-        kernel = skip ? (shadow ? k_trace<KDGB_TRACER_SHORTSTACK, true, true> : k_trace<KDGB_TRACER_SHORTSTACK, true, false>)
-                      : (shadow ? k_trace<KDGB_TRACER_SHORTSTACK, false, true>
-                                : k_trace<KDGB_TRACER_SHORTSTACK, false, false>);
-    } else {
-        kernel = skip ? (shadow ? k_trace<KDGB_TRACER_RESTART, true, true> : k_trace<KDGB_TRACER_RESTART, true, false>)
-                      : (shadow ? k_trace<KDGB_TRACER_RESTART, false, true> : k_trace<KDGB_TRACER_RESTART, false, false>);
-    }
+    void (*kernel)(TraceArgs) = trace_kernel(p.tracer == KDGB_TRACER_SHORTSTACK, skip, shadow, a.c.woop != nullptr);
     if (p.schedule == KDGB_SCHEDULE_QUEUE && !shadow) return trace_queue_launch(t, p, a, bs, smem, s);
     // Large blocks with deep stacks need more than the default 48 KB.
     if (smem > 48 * 1024) KDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1177,9 +1206,10 @@ int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, i
     a.tile_width = 0;
     const int bs = p.block_size > 0 ? p.block_size : 128;
     const size_t smem = sizeof(int2) * (size_t)kMemo * bs;
+    void (*kernel)(TraceArgs) = a.c.woop ? k_shadow<KDGB_ISECT_WOOP> : k_shadow<KDGB_ISECT_MOELLER>;
     if (smem > 48 * 1024)
-        KDGB_CUDA(cudaFuncSetAttribute(k_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_shadow<<<blocks_for(n, bs), bs, smem, s>>>(a);
+        KDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<blocks_for(n, bs), bs, smem, s>>>(a);
     KDGB_LAUNCH_CHECK();
     return KDGB_OK;
 }
