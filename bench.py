@@ -355,6 +355,9 @@ def time_steps(step, steps, stream, flush=None):
 FRAMES_IN_FLIGHT = 4
 # Streams of the batched record's concurrent per-mesh comparator.
 CONCURRENT_STREAMS = 16
+# Bytes a traversal step reads: a node record, a leaf's box pair, a
+# triangle record (the traversal layout's sizes).
+TRACE_BYTES = {"node": 8, "box": 32, "tri": 48}
 
 
 def e2e_frames_in_flight(args, dev, tree, graph, bp, tp, tris_d, o_d, d_d, outs, h_tris, h_o, h_d, stream,
@@ -560,6 +563,17 @@ def run_frame(args, world, rank, local, pg):
             "limiter": "issue/latency (ncu figures in profiles/k_trace_clustered1M_frame.md)"}
     if traffic:
         roof["traffic_source"] = traffic.get("source")
+    # Logical bytes of the same trace (what the traversal reads from L1, L2
+    # or HBM), from device step counters in a separate counting run after the
+    # timed region: node records 8 B, leaf boxes 32 B, triangle records 48 B.
+    c_outs = tuple(torch.empty_like(x) for x in outs)
+    _, steps = tree.count_steps(o_d, d_d, configs.LIGHT, tp, out=c_outs)
+    logical = sum(TRACE_BYTES[k] * (steps["primary"][k] + steps["shadow"][k]) for k in TRACE_BYTES)
+    roof["logical"] = {"bytes_per_launch": logical, "gbs": logical / (tr_ms / 1e3) / 1e9,
+                       "bytes_per_step": TRACE_BYTES, "steps": steps,
+                       "outputs_equal_timed": all(torch.equal(a.view(torch.int32), b.view(torch.int32))
+                                                  for a, b in zip(c_outs, outs)),
+                       "source": "device step counters (kdgb_trace_count_steps), separate counting run"}
 
     # End to end through the public API with host buffers.
     e2e = None

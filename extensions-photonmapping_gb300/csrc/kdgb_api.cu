@@ -17,7 +17,7 @@ namespace kdgb {
 
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
                  int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s,
-                 const int32_t *ray_mesh = nullptr, int32_t rays_per_mesh = 0);
+                 const int32_t *ray_mesh = nullptr, int32_t rays_per_mesh = 0, unsigned long long *counts = nullptr);
 int shadow_launch(const Tree &t, const kdgb_trace_params &p, const float *pts, int64_t n, const float *light,
                   int32_t *occ, cudaStream_t s);
 int brute_launch(const float4 *p0, const float4 *p1, const float4 *p2, const float4 *woop, int32_t T, int tie,
@@ -598,6 +598,41 @@ int kdgb_trace_primary_shadow(const kdgb_tree *tree, const kdgb_trace_params *pa
     if (tree->t.n_meshes > 1) return fail(KDGB_ERR_UNSUPPORTED, "shadow rays of a batched tree");
     return trace_launch(tree->t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, occluded_dev, light,
                         (cudaStream_t)stream);
+}
+
+int kdgb_trace_count_steps(const kdgb_tree *tree, const kdgb_trace_params *params, const float *ray_o_dev,
+                           const float *ray_d_dev, int32_t n, const float light[3], int32_t *hit_dev, float *t_dev,
+                           float *u_dev, float *v_dev, int32_t *occluded_dev, uint64_t counts[8], kdgb_stream_t stream)
+{
+    if (!tree || !light || !counts) return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    kdgb_trace_params p;
+    if (params) p = *params; else kdgb_trace_params_default(&p);
+    if (n < 0) return fail(KDGB_ERR_INVALID_ARGUMENT, "negative ray count");
+    KDGB_CHECK(validate_trace_params(p, n));
+    if (p.tracer != KDGB_TRACER_SHORTSTACK) return fail(KDGB_ERR_UNSUPPORTED, "step counts need the short-stack tracer");
+    if (tree->t.n_meshes > 1) return fail(KDGB_ERR_UNSUPPORTED, "step counts of a batched tree");
+    for (int k = 0; k < 8; ++k) counts[k] = 0;
+    if (n == 0) return KDGB_OK;
+    if (!ray_o_dev || !ray_d_dev || !hit_dev || !t_dev || !u_dev || !v_dev || !occluded_dev)
+        return fail(KDGB_ERR_INVALID_ARGUMENT, "NULL ray or output buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long *dev = nullptr;
+    KDGB_CUDA(cudaMallocAsync(&dev, 8 * sizeof(unsigned long long), s));
+    int rc = cudaMemsetAsync(dev, 0, 8 * sizeof(unsigned long long), s) == cudaSuccess
+                 ? trace_launch(tree->t, p, ray_o_dev, ray_d_dev, n, hit_dev, t_dev, u_dev, v_dev, occluded_dev,
+                                light, s, nullptr, 0, dev)
+                 : cuda_fail(cudaGetLastError(), "kdgb_trace_count_steps");
+    unsigned long long host[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (rc == KDGB_OK) {
+        const cudaError_t e = cudaMemcpyAsync(host, dev, sizeof(host), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "kdgb_trace_count_steps");
+    }
+    cudaFreeAsync(dev, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (rc == KDGB_OK && e != cudaSuccess) rc = cuda_fail(e, "kdgb_trace_count_steps");
+    if (rc == KDGB_OK)
+        for (int k = 0; k < 8; ++k) counts[k] = host[k];
+    return rc;
 }
 
 void kdgb_photon_params_default(kdgb_photon_params *p)

@@ -177,11 +177,20 @@ __device__ __forceinline__ bool use_woop(const Ctx &c)
     return IS == KDGB_ISECT_WOOP || (IS == kIsectAny && c.woop != nullptr);
 }
 
-template <int IS = kIsectAny>
+// Traversal steps of one thread, kept only by the counting launch
+// (kdgb_trace_count_steps): node records read, leaves reached, leaf boxes
+// read and triangle records tested.  Every other kernel is instantiated with
+// CNT false, so the counting compiles out of it.
+struct StepCount {
+    unsigned node = 0, leaf = 0, box = 0, tri = 0;
+};
+
+template <int IS = kIsectAny, bool CNT = false>
 __device__ __forceinline__ int leaf_test(const Ctx &c, int2 leaf, float3 o, float3 d, int tie, float &tb, float &ub,
-                                         float &vb)
+                                         float &vb, StepCount *sc = nullptr)
 {
     int hit = -1;
+    if constexpr (CNT) sc->tri += leaf_count(leaf);
     if (use_woop<IS>(c)) {
         for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) {
             const int id = __float_as_int(__ldg(c.tri + 3 * (int64_t)r + 2).y);
@@ -196,19 +205,21 @@ __device__ __forceinline__ int leaf_test(const Ctx &c, int2 leaf, float3 o, floa
 // Whether any triangle of the leaf is hit within [0, tb] (the reference's
 // shadow test, REF_LAST acceptance): the first accepted triangle settles it,
 // so the loop stops there with the result testing all of them gives.
-template <int IS = kIsectAny>
-__device__ __forceinline__ bool leaf_any(const Ctx &c, int2 leaf, float3 o, float3 d, float tb)
+template <int IS = kIsectAny, bool CNT = false>
+__device__ __forceinline__ bool leaf_any(const Ctx &c, int2 leaf, float3 o, float3 d, float tb, StepCount *sc = nullptr)
 {
     int hit = -1;
     float ub = 0.0f, vb = 0.0f;
     if (use_woop<IS>(c)) {
         for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) {
+            if constexpr (CNT) ++sc->tri;
             const int id = __float_as_int(__ldg(c.tri + 3 * (int64_t)r + 2).y);
             woop_test(c.woop + 3 * (int64_t)id, id, o, d, KDGB_TIE_REF_LAST, hit, tb, ub, vb);
             if (hit != -1) return true;
         }
     } else {
         for (int32_t r = leaf_first(leaf), e = r + leaf_count(leaf); r < e; ++r) {
+            if constexpr (CNT) ++sc->tri;
             mt_record(c.tri, r, o, d, KDGB_TIE_REF_LAST, hit, tb, ub, vb);
             if (hit != -1) return true;
         }
@@ -275,8 +286,9 @@ __host__ __device__ __forceinline__ int stack_entries(int tracer, int depth)
 // Descends from `node` (record nd) to a leaf, as the reference's kd-restart
 // loop does (Raytracer.cu:73-86); the near decisions that lower tnext are
 // remembered in m.
+template <bool CNT = false>
 __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 inv, float tmin, int &node, int2 &nd,
-                                                float &tnext, Memo &m)
+                                                float &tnext, Memo &m, StepCount *sc = nullptr)
 {
     while (node_axis(nd) != KDGB_LEAF) {
         const int ax = node_axis(nd), left = node_left(nd);
@@ -300,6 +312,7 @@ __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 i
             node = 0 < dir ? left + 1 : left;
         }
         nd = __ldg(c.node + node);
+        if constexpr (CNT) ++sc->node;
     }
 }
 
@@ -307,8 +320,11 @@ __device__ __forceinline__ void restart_descend(const Ctx &c, float3 o, float3 i
 // remembered near decision whose distance is <= tmin (prefix minima fall
 // with depth, so it is the first entry whose minimum is <= tmin), or the
 // root.
-__device__ __forceinline__ void restart_from(const Ctx &c, float tmin, int &node, int2 &nd, float &tnext, Memo &m)
+template <bool CNT = false>
+__device__ __forceinline__ void restart_from(const Ctx &c, float tmin, int &node, int2 &nd, float &tnext, Memo &m,
+                                             StepCount *sc = nullptr)
 {
+    if constexpr (CNT) ++sc->node;  // one node record on either path
     if (m.cnt > 0 && tmin < m.base) {
         // Usually the deepest entry: its minimum is the leaf's tnext, and the
         // one above it lies beyond tmin.  Otherwise the first entry whose
@@ -379,10 +395,10 @@ __device__ int trace_restart(const Ctx &c, float3 o, float3 din, int tie, int ma
 // (see trace_shortstack): every descent and slab test uses inv and every
 // triangle test d, neither changing, so the loop holds three registers and
 // no selects fewer.
-template <bool SKIP, bool FIXED, int IS>
+template <bool SKIP, bool FIXED, int IS, bool CNT>
 __device__ __forceinline__ int shortstack_loop(const Ctx &c, float3 o, float3 d, float3 inv, int tie, int depth,
                                                int maxit, int2 *st, int stride, float &t, float &u, float &v,
-                                               float3 *dused)
+                                               float3 *dused, StepCount *sc)
 {
     int nxt = 0, cnt = 0;
     float th = 0.0f;
@@ -401,6 +417,7 @@ __device__ __forceinline__ int shortstack_loop(const Ctx &c, float3 o, float3 d,
             tnext = __int_as_float(e.y);
         }
         int2 nd = __ldg(c.node + node);
+        if constexpr (CNT) ++sc->node;
         if (!FIXED) d = inv3(d);
         const float3 dn = FIXED ? inv : d;  // the inverse direction of this descent
         while (node_axis(nd) != KDGB_LEAF) {
@@ -420,12 +437,17 @@ __device__ __forceinline__ int shortstack_loop(const Ctx &c, float3 o, float3 d,
             tnext = go_near ? fminf(ts, tnext) : tnext;  // as in restart_descend
             node = go_near ? lower : upper;
             nd = __ldg(c.node + node);
+            if constexpr (CNT) ++sc->node;
         }
         if (!FIXED) d = inv3(d);
         th = __fmul_rn(tnext, 1.00001f);
+        if constexpr (CNT) {
+            ++sc->leaf;
+            if (SKIP) ++sc->box;
+        }
         if (!SKIP || ray_box(o, FIXED ? inv : inv3(d), leaf_min(c, node), leaf_max(c, node))) {
             float tb = th, ub = 0.0f, vb = 0.0f;
-            const int h = leaf_test<IS>(c, nd, o, d, tie, tb, ub, vb);
+            const int h = leaf_test<IS, CNT>(c, nd, o, d, tie, tb, ub, vb, sc);
             if (h != -1) {
                 t = tb; u = ub; v = vb;
                 if (dused) *dused = d;
@@ -444,25 +466,28 @@ __device__ __forceinline__ int shortstack_loop(const Ctx &c, float3 o, float3 d,
 // and every triangle test d1 = rcp(inv1).  That holds for all finite nonzero
 // floats except six values next to FLT_MAX (checked exhaustively); it is
 // tested per ray, and rays that miss it take the reference's loop.
-template <bool SKIP, int IS = kIsectAny>
+template <bool SKIP, int IS = kIsectAny, bool CNT = false>
 __device__ int trace_shortstack(const Ctx &c, float3 o, float3 din, int tie, int depth, int maxit, int2 *st,
-                                int stride, float &t, float &u, float &v, float3 *dused = nullptr)
+                                int stride, float &t, float &u, float &v, float3 *dused = nullptr,
+                                StepCount *sc = nullptr)
 {
     const float3 d = adjust_dir(din);
     const float3 inv1 = inv3(d), d1 = inv3(inv1), inv2 = inv3(d1);
     const bool fixed = __float_as_uint(inv2.x) == __float_as_uint(inv1.x) &&
                        __float_as_uint(inv2.y) == __float_as_uint(inv1.y) &&
                        __float_as_uint(inv2.z) == __float_as_uint(inv1.z);
-    if (fixed) return shortstack_loop<SKIP, true, IS>(c, o, d1, inv1, tie, depth, maxit, st, stride, t, u, v, dused);
-    return shortstack_loop<SKIP, false, IS>(c, o, d, d, tie, depth, maxit, st, stride, t, u, v, dused);
+    if (fixed)
+        return shortstack_loop<SKIP, true, IS, CNT>(c, o, d1, inv1, tie, depth, maxit, st, stride, t, u, v, dused, sc);
+    return shortstack_loop<SKIP, false, IS, CNT>(c, o, d, d, tie, depth, maxit, st, stride, t, u, v, dused, sc);
 }
 
 // ShadowRay (Raytracer.cu:108-163): from the light toward the point, the
 // direction neither normalised nor clamped; leaves whose exit reaches 0.999
 // are not tested; any hit occludes.
 // The descents are remembered in `cap` entries at mem[k * stride] (see Memo).
-template <int IS = kIsectAny>
-__device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 *mem, int stride, int cap = kMemo)
+template <int IS = kIsectAny, bool CNT = false>
+__device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 *mem, int stride, int cap = kMemo,
+                            StepCount *sc = nullptr)
 {
     const float3 d = sub3(pt, lp);
     const float3 inv = inv3(d);
@@ -475,14 +500,16 @@ __device__ int trace_shadow(const Ctx &c, float3 lp, float3 pt, int maxit, int2 
     memo.reset();
     int node = c.root;
     int2 nd = __ldg(c.node + c.root);
+    if constexpr (CNT) ++sc->node;
     float tnext = KDGB_FINF;
     do {
-        restart_descend(c, lp, inv, tmin, node, nd, tnext, memo);
+        restart_descend<CNT>(c, lp, inv, tmin, node, nd, tnext, memo, sc);
+        if constexpr (CNT) ++sc->leaf;
         tmin = __fmul_rn(tnext, 1.00001f);
         if (tmin >= 0.999f) return 0;
-        if (leaf_any<IS>(c, nd, lp, d, tmin)) return 1;
+        if (leaf_any<IS, CNT>(c, nd, lp, d, tmin, sc)) return 1;
         if (++iters >= maxit) break;
-        restart_from(c, tmin, node, nd, tnext, memo);
+        restart_from<CNT>(c, tmin, node, nd, tnext, memo, sc);
     } while (true);
     return 0;
 }
@@ -527,6 +554,9 @@ struct TraceArgs {
     // outgrew its buffers): every ray then reports a miss without reading
     // the tree.
     const int32_t *build_err;
+    // The counting launch's totals (primary rays' StepCount, then the shadow
+    // rays'); unused by every other launch.
+    unsigned long long *counts = nullptr;
 };
 
 // A shadow ray waiting in a block's queue: the hit point, the tree root and
@@ -547,9 +577,9 @@ __device__ __forceinline__ int ray_mesh_of(const TraceArgs &a, int64_t i)
 // a batch), written to the outputs; the thread's stack or memo region is
 // stk[k * stride].  Returns the hit id (relative to the whole tree) and the
 // ray and t for a shadow ray.
-template <int TRACER, bool SKIP, int IS = kIsectAny>
+template <int TRACER, bool SKIP, int IS = kIsectAny, bool CNT = false>
 __device__ __forceinline__ int trace_ray(const TraceArgs &a, int64_t i, int2 *stk, int stride, float3 &o, float3 &d,
-                                         float &t)
+                                         float &t, StepCount *sc = nullptr)
 {
     o = ld3(a.o, i);
     d = ld3(a.d, i);
@@ -562,7 +592,7 @@ __device__ __forceinline__ int trace_ray(const TraceArgs &a, int64_t i, int2 *st
     float u = 0.0f, v = 0.0f;
     int h;
     if (TRACER == KDGB_TRACER_SHORTSTACK)
-        h = trace_shortstack<SKIP, IS>(c, o, d, a.tie, a.depth, a.maxit, stk, stride, t, u, v);
+        h = trace_shortstack<SKIP, IS, CNT>(c, o, d, a.tie, a.depth, a.maxit, stk, stride, t, u, v, nullptr, sc);
     else
         h = trace_restart<SKIP, IS>(c, o, d, a.tie, a.maxit, t, u, v, nullptr, stk, stride);
     if (h < 0) { t = INFINITY; u = 0.0f; v = 0.0f; }
@@ -581,7 +611,7 @@ __device__ __forceinline__ int trace_ray(const TraceArgs &a, int64_t i, int2 *st
 // instead of 56%) gain more than the few spilled values cost (measured on
 // the 1M-triangle frame: 1.61 ms against 1.72 ms uncapped, 1.67 ms at 48
 // and 1.83 ms at 32 registers).
-template <int TRACER, bool SKIP, bool SHADOW, int IS>
+template <int TRACER, bool SKIP, bool SHADOW, int IS, bool CNT = false>
 __global__ void __maxnreg__(40) k_trace(TraceArgs a)
 {
     extern __shared__ __align__(16) unsigned char trace_smem[];
@@ -602,7 +632,8 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
     float3 o = make_float3(0.f, 0.f, 0.f), d = o;
     float t = 0.0f;
     int h = -1;
-    if (live) h = trace_ray<TRACER, SKIP, IS>(a, i, stack_smem + threadIdx.x, blockDim.x, o, d, t);
+    StepCount cp, cs;  // counting launch only
+    if (live) h = trace_ray<TRACER, SKIP, IS, CNT>(a, i, stack_smem + threadIdx.x, blockDim.x, o, d, t, &cp);
     if (SHADOW) {
         // The block's shadow rays (one per primary hit) are packed onto its
         // first threads, so warps stay full while they are traced.
@@ -627,11 +658,19 @@ __global__ void __maxnreg__(40) k_trace(TraceArgs a)
         __syncthreads();  // every item is read before the shadow rays' descents reuse the region
         if (queued) {
             const int64_t ray = ray_index((int64_t)blockIdx.x * blockDim.x + __float_as_int(q.p.w), a.tile_width);
-            Ctx cs = a.c;
-            cs.root = ray_mesh_of(a, ray);
-            a.occ[ray] = trace_shadow<IS>(cs, a.light, make_float3(q.p.x, q.p.y, q.p.z), a.maxit,
-                                        stack_smem + threadIdx.x, blockDim.x,
-                                        memo_cap(stack_entries(TRACER, a.depth)));
+            Ctx cr = a.c;
+            cr.root = ray_mesh_of(a, ray);
+            a.occ[ray] = trace_shadow<IS, CNT>(cr, a.light, make_float3(q.p.x, q.p.y, q.p.z), a.maxit,
+                                             stack_smem + threadIdx.x, blockDim.x,
+                                             memo_cap(stack_entries(TRACER, a.depth)), &cs);
+        }
+    }
+    if constexpr (CNT) {  // every thread of the block is here: warp sums, one atomic per warp and counter
+        const unsigned v[8] = {cp.node, cp.leaf, cp.box, cp.tri, cs.node, cs.leaf, cs.box, cs.tri};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const unsigned w = __reduce_add_sync(0xffffffffu, v[k]);
+            if ((threadIdx.x & 31) == 0 && w) atomicAdd(a.counts + k, (unsigned long long)w);
         }
     }
 }
@@ -1141,7 +1180,7 @@ static void (*trace_kernel(bool shortstack, bool skip, bool shadow, bool woop))(
 
 int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, const float *d, int64_t n,
                  int32_t *hit, float *tt, float *uu, float *vv, int32_t *occ, const float *light, cudaStream_t s,
-                 const int32_t *ray_mesh, int32_t rays_per_mesh)
+                 const int32_t *ray_mesh, int32_t rays_per_mesh, unsigned long long *counts)
 {
     TraceArgs a;
     a.c.node = t.tnode.p;
@@ -1175,6 +1214,15 @@ int trace_launch(const Tree &t, const kdgb_trace_params &p, const float *o, cons
     // thread) overlays the stack region.
     const size_t smem = sizeof(int2) * (size_t)std::max(stack_entries(p.tracer, p.stack_depth), shadow ? 2 : 0) * bs;
     void (*kernel)(TraceArgs) = trace_kernel(p.tracer == KDGB_TRACER_SHORTSTACK, skip, shadow, a.c.woop != nullptr);
+    if (counts) {  // the counting launch: short-stack primary rays with fused shadow rays only
+        if (p.tracer != KDGB_TRACER_SHORTSTACK || !shadow || t.n_meshes > 1)
+            return fail(KDGB_ERR_UNSUPPORTED, "step counts are kept for short-stack primary + shadow traces only");
+        a.counts = counts;
+        kernel = skip ? (a.c.woop ? k_trace<KDGB_TRACER_SHORTSTACK, true, true, KDGB_ISECT_WOOP, true>
+                                  : k_trace<KDGB_TRACER_SHORTSTACK, true, true, KDGB_ISECT_MOELLER, true>)
+                      : (a.c.woop ? k_trace<KDGB_TRACER_SHORTSTACK, false, true, KDGB_ISECT_WOOP, true>
+                                  : k_trace<KDGB_TRACER_SHORTSTACK, false, true, KDGB_ISECT_MOELLER, true>);
+    }
     if (p.schedule == KDGB_SCHEDULE_QUEUE && !shadow) return trace_queue_launch(t, p, a, bs, smem, s);
     // Large blocks with deep stacks need more than the default 48 KB.
     if (smem > 48 * 1024) KDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -241,6 +241,33 @@ class KDTree:
               "kdgb_trace_primary_shadow")
         return hit, t, u, v, occ
 
+    def count_steps(self, o, d, light, params: TraceParams | None = None, stream=None, out=None, **kw):
+        """trace_primary_shadow (short-stack) with traversal step counters
+        (kdgb_trace_count_steps): returns the outputs and a dict of the
+        primary and shadow rays' node records read, leaves reached, leaf
+        boxes read and triangle records tested."""
+        torch = _torch()
+        o = _dev(o, torch.float32, 3)
+        d = _dev(d, torch.float32, 3)
+        n = o.shape[0]
+        p = params if params is not None else trace_params(**kw)
+        lp = (C.c_float * 3)(*[float(x) for x in light])
+        if out is None:
+            out = (torch.empty(n, dtype=torch.int32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device),
+                   torch.empty(n, dtype=torch.float32, device=o.device),
+                   torch.empty(n, dtype=torch.int32, device=o.device))
+        hit, t, u, v, occ = out
+        counts = (C.c_uint64 * 8)()
+        check(lib().kdgb_trace_count_steps(self._h, C.byref(p), _ptr(o), _ptr(d), n, lp, _ptr(hit), _ptr(t),
+                                           _ptr(u), _ptr(v), _ptr(occ), counts, self._on(stream)),
+              "kdgb_trace_count_steps")
+        names = ("node", "leaf", "box", "tri")
+        steps = {"primary": {k: int(counts[j]) for j, k in enumerate(names)},
+                 "shadow": {k: int(counts[4 + j]) for j, k in enumerate(names)}}
+        return (hit, t, u, v, occ), steps
+
 
 def _trace_photons(self, n_photons: int, params: TraceParams | None = None, photons=None, stream=None, out=None,
                    **kw):

@@ -97,6 +97,8 @@ SIGNATURES = {
     "kdgb_trace": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P]),
     "kdgb_trace_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, C.c_int32, P, P, P]),
     "kdgb_trace_primary_shadow": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P, P, P]),
+    "kdgb_trace_count_steps": (C.c_int, [P, C.POINTER(TraceParams), P, P, C.c_int32, P, P, P, P, P, P,
+                                         C.POINTER(C.c_uint64), P]),
     "kdgb_photon_params_default": (None, [C.POINTER(PhotonParams)]),
     "kdgb_trace_photons": (C.c_int, [P, C.POINTER(TraceParams), C.POINTER(PhotonParams), C.c_int32, P, P, P]),
     "kdgb_build_batch": (C.c_int, [P, P, C.c_int32, C.POINTER(BuildParams), C.POINTER(C.c_void_p), P]),

@@ -40,7 +40,7 @@ typedef struct CUstream_st *kdgb_stream_t; /* same type as cudaStream_t */
 #define KDGB_API
 #endif
 
-#define KDGB_ABI_VERSION 5
+#define KDGB_ABI_VERSION 6
 
 /* Utils/CUDA/Utils.h:18: the reference's "infinity" is the integer
  * 0x7f800000 converted to float. */
@@ -249,6 +249,20 @@ KDGB_API int kdgb_trace_primary_shadow(const kdgb_tree *tree, const kdgb_trace_p
                               const float light[3],
                               int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
                               int32_t *occluded_dev, kdgb_stream_t stream);
+
+/* Measurement aid (no reference counterpart): the same launch as
+ * kdgb_trace_primary_shadow with the short-stack tracer, compiled with
+ * counters, writing the same outputs.  counts (8 host uint64) receive the
+ * primary rays' node records read, leaves reached, leaf boxes read and
+ * triangle records tested, then the same four for the shadow rays (which read
+ * no leaf boxes).  The timed trace kernels are compiled without the
+ * counters.  Synchronises `stream`; allocates 64 bytes of device memory per
+ * call. */
+KDGB_API int kdgb_trace_count_steps(const kdgb_tree *tree, const kdgb_trace_params *params,
+                           const float *ray_o_dev, const float *ray_d_dev, int32_t n,
+                           const float light[3],
+                           int32_t *hit_dev, float *t_dev, float *u_dev, float *v_dev,
+                           int32_t *occluded_dev, uint64_t counts[8], kdgb_stream_t stream);
 
 typedef struct kdgb_photon_params {
     float    light[3];   /* point light position (photon origin) */

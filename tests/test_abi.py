@@ -53,7 +53,7 @@ def test_status_strings(kdgb_lib):
     L = kdgb_lib.lib()
     assert L.kdgb_status_string(0) == b"ok"
     assert L.kdgb_status_string(9) == b"no CUDA device"
-    assert L.kdgb_abi_version() == 5
+    assert L.kdgb_abi_version() == 6
 
 
 def test_no_device_is_an_error_not_a_crash(kdgb_lib):

@@ -141,6 +141,31 @@ def test_fused_shadow_small_memo(kdgb_lib, cuda, oracle, clustered, depth):
     assert occ_ref.sum() > 100
 
 
+def test_step_counts(kdgb_lib, cuda, oracle, clustered):
+    """kdgb_trace_count_steps: the fused launch compiled with counters writes
+    the outputs of the timed launch, counts the same twice, and its counts
+    agree with what the outputs imply."""
+    tris, tree, o, d = clustered
+    light = (0.5, 3.0, 0.5)
+    kw = dict(tracer=1, stack_depth=8)
+    with kdgb_lib.KDTree.upload(tree, tris) as gt:
+        ref = [np_(x) for x in gt.trace_primary_shadow(o, d, light, **kw)]
+        outs, steps = gt.count_steps(o, d, light, **kw)
+        _, again = gt.count_steps(o, d, light, **kw)
+        with pytest.raises(kdgb_lib.KdgbError):
+            gt.count_steps(o, d, light, tracer=0)
+    for a, b in zip((np_(x) for x in outs), ref):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert steps == again
+    p, s = steps["primary"], steps["shadow"]
+    n, hits, occluded = o.shape[0], int((ref[0] >= 0).sum()), int(ref[4].sum())
+    assert p["leaf"] >= n and p["node"] >= p["leaf"]
+    assert p["box"] == p["leaf"]  # leaf skipping: one box per leaf reached
+    assert p["tri"] >= hits
+    assert s["box"] == 0 and s["leaf"] >= hits and s["node"] >= s["leaf"]
+    assert s["tri"] >= occluded > 0
+
+
 def test_edge_case_rays(kdgb_lib, cuda, oracle):
     tris = scenes.heightfield(16, 16, seed=2)[0]
     tree = oracle.build(tris)
