@@ -47,6 +47,7 @@ itself does not compile here.
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import os
 import statistics
@@ -124,42 +125,74 @@ def workload(args):
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks/throttle reasons sampled during the timed region.
+
+    nvidia-smi needs a few hundred ms before its first sample, longer than a
+    short timed region, so start() (called before the warm-up steps) returns
+    only once the first sample has arrived; mark() opens the window at the
+    start of the timed region, and stop() waits for one more sample taken
+    after the region has ended."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 100
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, cmd: str = "nvidia-smi"):
         self.index = index
+        self.cmd = cmd
         self.proc = None
         self.lines = []
+        self.first = 0
+        self.cv = threading.Condition()
 
-    def start(self):
+    def start(self, wait_s: float = 5.0):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+            self.proc = subprocess.Popen([self.cmd, f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            atexit.register(self._end)  # no sampler outlives the run, whatever happens before stop()
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
+            return
+        self._wait_for(1, wait_s)
+        self.mark()
+
+    def mark(self):
+        with self.cv:
+            self.first = len(self.lines)
+
+    def _end(self):
+        if self.proc.poll() is None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            with self.cv:
+                self.lines.append(line.strip())
+                self.cv.notify_all()
 
-    def stop(self):
+    def _wait_for(self, n: int, wait_s: float):
+        with self.cv:
+            self.cv.wait_for(lambda: len(self.lines) >= n, timeout=wait_s)
+
+    def stop(self, wait_s: float = 2.0):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
+        self._wait_for(len(self.lines) + 1, wait_s)
+        self._end()
+        self.t.join(timeout=5)
+        with self.cv:
+            window = self.lines[self.first:]
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in window:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -172,7 +205,7 @@ class ClockSampler:
                 if val.lower() == "active":
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "interval_ms": self.INTERVAL_MS}
 
 
 def measured_peak_gbs():
@@ -502,6 +535,8 @@ def run_frame(args, world, rank, local, pg):
         return
 
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    sampler = ClockSampler(local)
+    sampler.start()
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -511,12 +546,11 @@ def run_frame(args, world, rank, local, pg):
     rays_per_step = n + n_hits
     st = tree.stats()
 
-    sampler = ClockSampler(local)
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
     launches0 = L.kdgb_launch_count()
-    sampler.start()
+    sampler.mark()
     step_ms, trace_ms = [], []
     for _ in range(args.steps):
         flush.zero_()
